@@ -1,0 +1,227 @@
+"""fdfd_gb300 — GB300 solve path for 2-D FDFD problems, host-side mirror of
+the FDFD.jl interface on that path.
+
+The reference (fancompute/FDFD.jl) exposes ``Grid``, ``Device``,
+``setup_ϵᵣ!``, ``setup_src!``, ``solve(d, pol)`` and
+``eigenfrequency(d, pol, nev; which)`` returning ``FieldTM``/``FieldTE``
+(src/grid.jl, src/device.jl, src/solver/driven.jl, src/solver/eigen.jl,
+src/data.jl).  This module keeps those names, argument meanings and return
+shapes and runs every solve through ``libfdfd_cuda`` (the C ABI in
+include/fdfd_cuda.h) — the role ``ENV["FDFD_SOLVER"] = "cuda"`` plays for a
+Julia caller.  There is no CPU fallback: without the CUDA library every solve
+raises.
+
+Arrays are numpy (Nx, Ny) with x the first axis, i.e. the reference's Julia
+column-major layout.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib
+from ._lib import FDFDError, FDFD_PREC_FP64, FDFD_PREC_MIXED  # noqa: F401
+
+__all__ = ["EPS0", "MU0", "C0", "ETA0", "TM", "TE", "Grid", "Device", "Point", "setup_eps", "setup_src",
+           "solve", "eigenfrequency", "FieldTM", "FieldTE", "normalize_parameters", "FDFDError"]
+
+# src/types.jl:6-9
+EPS0 = 8.85418782e-12
+MU0 = 1.25663706e-6
+C0 = math.sqrt(1 / EPS0 / MU0)
+ETA0 = math.sqrt(MU0 / EPS0)
+DEFAULT_L0 = 1e-6          # src/grid.jl:31
+TM, TE = _lib.FDFD_TM, _lib.FDFD_TE   # src/types.jl:20
+
+
+@dataclass
+class Point:
+    """src/types.jl:23-26."""
+    x: float
+    y: float
+
+
+class Grid:
+    """2-D grid (src/grid.jl:33-59): N = round(L/dh) cells per axis, Npml PML
+    cells per side, bounds ((x1, y1), (x2, y2)) in units of L₀."""
+
+    def __init__(self, dh, Npml, xrange, yrange, L0=DEFAULT_L0):
+        L = (float(xrange[1] - xrange[0]), float(yrange[1] - yrange[0]))
+        self.N = (int(round(L[0] / dh)), int(round(L[1] / dh)))
+        self.Npml = (int(Npml[0]), int(Npml[1]))
+        self.bounds = ((float(xrange[0]), float(yrange[0])), (float(xrange[1]), float(yrange[1])))
+        self.L = L
+        self.L0 = float(L0)
+
+    @classmethod
+    def from_cells(cls, Nx, Ny, dx, dy, Npml, x0=0.0, y0=0.0, L0=DEFAULT_L0):
+        g = cls.__new__(cls)
+        g.N = (int(Nx), int(Ny))
+        g.Npml = (int(Npml[0]), int(Npml[1]))
+        g.bounds = ((float(x0), float(y0)), (float(x0 + Nx * dx), float(y0 + Ny * dy)))
+        g.L = (g.bounds[1][0] - g.bounds[0][0], g.bounds[1][1] - g.bounds[0][1])
+        g.L0 = float(L0)
+        return g
+
+    def size(self):
+        return self.N
+
+    def dx(self):  # src/grid.jl:94-96
+        return (self.bounds[1][0] - self.bounds[0][0]) / self.N[0]
+
+    def dy(self):  # src/grid.jl:98-100
+        return (self.bounds[1][1] - self.bounds[0][1]) / self.N[1]
+
+    def xc(self):  # src/grid.jl:102-104
+        return self.bounds[0][0] + self.dx() * (np.arange(self.N[0]) + 0.5)
+
+    def yc(self):  # src/grid.jl:106-108
+        return self.bounds[0][1] + self.dy() * (np.arange(self.N[1]) + 0.5)
+
+    def coord2ind(self, pt: Point):
+        """0-based (ix, iy), src/grid.jl:129-151."""
+        ix = int(round((pt.x - self.bounds[0][0]) / self.L[0] * self.N[0]) + 1)
+        iy = int(round((pt.y - self.bounds[0][1]) / self.L[1] * self.N[1]) + 1)
+        return min(max(ix, 1), self.N[0]) - 1, min(max(iy, 1), self.N[1]) - 1
+
+
+def normalize_parameters(g: Grid):
+    """(ϵ₀L₀, μ₀L₀, c₀/L₀): src/device.jl:40."""
+    return EPS0 * g.L0, MU0 * g.L0, C0 / g.L0
+
+
+@dataclass
+class Device:
+    """src/device.jl:19-35: grid, complex ϵᵣ and src arrays, frequencies ω."""
+    grid: Grid
+    omega: list
+    eps: np.ndarray = None
+    src: np.ndarray = None
+    modes: list = field(default_factory=list)
+
+    def __post_init__(self):
+        if np.isscalar(self.omega):
+            self.omega = [float(self.omega)]
+        if self.eps is None:
+            self.eps = np.ones(self.grid.N, dtype=np.complex128)
+        if self.src is None:
+            self.src = np.zeros(self.grid.N, dtype=np.complex128)
+
+
+def _mask(d: Device, region):
+    X, Y = np.meshgrid(d.grid.xc(), d.grid.yc(), indexing="ij")
+    return np.vectorize(region)(X, Y).astype(bool), X, Y
+
+
+def setup_eps(d: Device, region, value):
+    """setup_ϵᵣ!(d, region, value): src/device.jl:63-89 (region and value may be callables of (x, y))."""
+    m, X, Y = _mask(d, region)
+    d.eps[m] = np.vectorize(value)(X, Y)[m] if callable(value) else value
+
+
+def setup_src(d: Device, where, value=None):
+    """setup_src!(d, pt) puts 1im at the point (src/device.jl:95-98);
+    setup_src!(d, region, value) fills a region (device.jl:92)."""
+    if isinstance(where, Point):
+        ix, iy = d.grid.coord2ind(where)
+        d.src[ix, iy] = 1j
+        return
+    m, X, Y = _mask(d, where)
+    d.src[m] = np.vectorize(value)(X, Y)[m] if callable(value) else value
+
+
+globals()["setup_ϵᵣ"] = setup_eps
+
+
+class _Field:
+    components = ()
+
+    def __init__(self, grid, omega, data):
+        self.grid = grid
+        self.omega = complex(omega)
+        self.data = data            # (Nx, Ny, 3) complex
+
+    def __getitem__(self, comp):
+        if isinstance(comp, str):
+            return self.data[:, :, self.components.index(comp)]
+        return self.data[comp]
+
+    @property
+    def shape(self):
+        return self.data.shape
+
+
+class FieldTM(_Field):
+    """src/data.jl:50-63: Nx x Ny x 3 with components [:Ez, :Hx, :Hy]."""
+    components = ("Ez", "Hx", "Hy")
+
+
+class FieldTE(_Field):
+    """src/data.jl:65-78: Nx x Ny x 3 with components [:Hz, :Ex, :Ey]."""
+    components = ("Hz", "Ex", "Ey")
+
+
+def _prec(precision):
+    if isinstance(precision, str):
+        return {"fp64": FDFD_PREC_FP64, "mixed": FDFD_PREC_MIXED}[precision]
+    return int(precision)
+
+
+def make_handle(d: Device, pol=TM, precision="mixed", pml_m=3.5, pml_lnR=-12.0, tol=1e-10, max_iter=40):
+    g = d.grid
+    h = _lib.Handle(g.N[0], g.N[1], g.Npml[0], g.Npml[1], g.dx(), g.dy(), g.L0, pml_m, pml_lnR, pol,
+                    _prec(precision))
+    h.set_refinement(tol, max_iter)
+    h.set_eps(d.eps)
+    return h
+
+
+def solve(d: Device, pol=TM, precision="mixed", pml_m=3.5, pml_lnR=-12.0, tol=1e-10, max_iter=40,
+          return_stats=False):
+    """solve(d::Device, pol) — src/solver/driven.jl:153-208.
+
+    One factorization per frequency (as the reference re-factors per ω) and a
+    refined solve for d.src.  ``pml_m``/``pml_lnR`` default to the values the
+    reference hard-wires (src/pml.jl:1, S_create does not forward them).
+    Returns a FieldTM/FieldTE, or a list when len(d.omega) > 1 (driven.jl:206-207).
+    """
+    if d.modes:
+        raise FDFDError(_lib.FDFD_EINVAL, "mode sources are not supported by the GPU solve path")
+    h = make_handle(d, pol, precision, pml_m, pml_lnR, tol, max_iter)
+    out, stats = [], []
+    try:
+        for w in d.omega:
+            h.factor(w)
+            f1, f2, f3, st = h.solve(d.src)
+            cls = FieldTM if pol == TM else FieldTE
+            out.append(cls(d.grid, w, np.stack([f1, f2, f3], axis=-1)))
+            stats.append(st.as_dict())
+    finally:
+        h.close()
+    res = out[0] if len(out) == 1 else out
+    return (res, stats) if return_stats else res
+
+
+def eigenfrequency(d: Device, pol, nev, which="LM", precision="mixed", pml_m=3.5, pml_lnR=-12.0, tol=1e-10):
+    """eigenfrequency(d, pol, nev; which) — src/solver/eigen.jl:318-364."""
+    h = make_handle(d, pol, precision, pml_m, pml_lnR, tol)
+    try:
+        N = d.grid.N[0] * d.grid.N[1]
+        om = np.empty(nev, dtype=np.complex128)
+        lam = np.empty(nev, dtype=np.complex128)
+        flds = np.empty((nev, 3, N), dtype=np.complex128)
+        st = _lib.Stats()
+        import ctypes as C
+        rc = h.lib.fdfd_eigfreq(h.h, float(d.omega[0]), int(nev), 0, float(tol), _lib.cptr(om), _lib.cptr(lam),
+                                _lib.cptr(flds), C.byref(st))
+        h._check(rc)
+        cls = FieldTM if pol == TM else FieldTE
+        fields = []
+        for i in range(nev):
+            comps = [_lib.from_natural(flds[i, c], d.grid.N[0], d.grid.N[1])[0] for c in range(3)]
+            fields.append(cls(d.grid, om[i], np.stack(comps, axis=-1)))
+        return om, fields
+    finally:
+        h.close()

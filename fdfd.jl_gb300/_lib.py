@@ -1,0 +1,223 @@
+"""ctypes binding of libfdfd_cuda (include/fdfd_cuda.h).
+
+This is the same binding a Julia ``ccall`` shim makes: plain pointers and
+sizes, complex arrays as interleaved float64 pairs, x fastest.  Loading the
+library never falls back to anything else: a missing or unloadable
+``libfdfd_cuda.so`` raises immediately.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libfdfd_cuda.so")
+
+FDFD_OK, FDFD_EINVAL, FDFD_ENOMEM, FDFD_ESINGULAR, FDFD_ENOCONV, FDFD_ETIMEOUT, FDFD_ECUDA = range(7)
+STATUS_NAMES = {0: "FDFD_OK", 1: "FDFD_EINVAL", 2: "FDFD_ENOMEM", 3: "FDFD_ESINGULAR", 4: "FDFD_ENOCONV",
+                5: "FDFD_ETIMEOUT", 6: "FDFD_ECUDA"}
+FDFD_TM, FDFD_TE = 1, 2
+FDFD_PREC_FP64, FDFD_PREC_MIXED = 0, 1
+FDFD_REFINE_GMRES, FDFD_REFINE_CLASSIC = 0, 1
+
+# every symbol include/fdfd_cuda.h declares
+EXPORTS = ["fdfd_version", "fdfd_create", "fdfd_destroy", "fdfd_last_error", "fdfd_set_refinement",
+           "fdfd_set_eps", "fdfd_factor", "fdfd_solve", "fdfd_solve_device", "fdfd_adjoint", "fdfd_eigfreq",
+           "fdfd_get_stencil", "fdfd_apply", "fdfd_set_profiling", "fdfd_get_profile", "fdfd_debug_gemm"]
+PROF_CLASSES = ["gemm_tc", "gemm_simt", "gj_panel", "sweep", "residual", "other"]
+
+
+class Stats(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("nrhs", C.c_int), ("rel_residual", C.c_double),
+                ("t_assemble_ms", C.c_double), ("t_factor_ms", C.c_double), ("t_solve_ms", C.c_double),
+                ("t_recover_ms", C.c_double), ("t_total_ms", C.c_double), ("factor_flops", C.c_double),
+                ("block", C.c_int), ("nblocks", C.c_int), ("levels", C.c_int), ("tc_gemm", C.c_int),
+                ("device_bytes", C.c_longlong), ("gpu_launches", C.c_longlong)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class Profile(C.Structure):
+    _fields_ = [("ms", C.c_double * 6), ("work", C.c_double * 6), ("launches", C.c_longlong * 6)]
+
+    def as_dict(self):
+        return {k: {"ms": self.ms[i], "work": self.work[i], "launches": self.launches[i]}
+                for i, k in enumerate(PROF_CLASSES)}
+
+
+class FDFDError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{STATUS_NAMES.get(code, code)}: {msg}")
+        self.code = code
+
+
+_lib = None
+
+
+def load(path: str = LIB_PATH) -> C.CDLL:
+    """Load libfdfd_cuda.so and declare its signatures (raises if absent)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise FileNotFoundError(f"{path} is missing: run __graft_entry__.build() (nvcc, sm_103a) first")
+    lib = C.CDLL(path)
+    vp, dp, ip = C.c_void_p, C.POINTER(C.c_double), C.c_int
+    lib.fdfd_version.restype = C.c_char_p
+    lib.fdfd_version.argtypes = []
+    lib.fdfd_create.restype = ip
+    lib.fdfd_create.argtypes = [C.POINTER(vp), ip, ip, ip, ip, C.c_double, C.c_double, C.c_double, C.c_double,
+                                C.c_double, ip, ip]
+    lib.fdfd_destroy.restype = None
+    lib.fdfd_destroy.argtypes = [vp]
+    lib.fdfd_last_error.restype = C.c_char_p
+    lib.fdfd_last_error.argtypes = [vp]
+    lib.fdfd_set_refinement.restype = ip
+    lib.fdfd_set_refinement.argtypes = [vp, C.c_double, ip, ip]
+    lib.fdfd_set_eps.restype = ip
+    lib.fdfd_set_eps.argtypes = [vp, dp]
+    lib.fdfd_factor.restype = ip
+    lib.fdfd_factor.argtypes = [vp, C.c_double]
+    lib.fdfd_solve.restype = ip
+    lib.fdfd_solve.argtypes = [vp, dp, ip, dp, dp, dp, C.POINTER(Stats)]
+    lib.fdfd_solve_device.restype = ip
+    lib.fdfd_solve_device.argtypes = [vp, C.c_void_p, ip, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(Stats)]
+    lib.fdfd_adjoint.restype = ip
+    lib.fdfd_adjoint.argtypes = [vp, dp, dp, dp, dp, dp, C.POINTER(Stats)]
+    lib.fdfd_eigfreq.restype = ip
+    lib.fdfd_eigfreq.argtypes = [vp, C.c_double, ip, ip, C.c_double, dp, dp, dp, C.POINTER(Stats)]
+    lib.fdfd_get_stencil.restype = ip
+    lib.fdfd_get_stencil.argtypes = [vp, dp]
+    lib.fdfd_apply.restype = ip
+    lib.fdfd_apply.argtypes = [vp, dp, ip, dp]
+    lib.fdfd_set_profiling.restype = ip
+    lib.fdfd_set_profiling.argtypes = [vp, ip]
+    lib.fdfd_get_profile.restype = ip
+    lib.fdfd_get_profile.argtypes = [vp, C.POINTER(Profile)]
+    lib.fdfd_debug_gemm.restype = ip
+    lib.fdfd_debug_gemm.argtypes = [ip, ip, ip, dp, dp, dp, ip, ip, dp]
+    _lib = lib
+    return lib
+
+
+def cptr(a: np.ndarray):
+    """Pointer to a C-contiguous complex128/float64 array as double*."""
+    if a is None:
+        return None
+    assert a.flags["C_CONTIGUOUS"] and a.dtype in (np.complex128, np.float64)
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def natural(a: np.ndarray) -> np.ndarray:
+    """(..., Nx, Ny) array -> contiguous buffer in the library's x-fastest order."""
+    a = np.asarray(a, dtype=np.complex128)
+    return np.ascontiguousarray(np.swapaxes(a, -1, -2))
+
+
+def from_natural(buf: np.ndarray, Nx: int, Ny: int) -> np.ndarray:
+    """Inverse of ``natural``: x-fastest buffer holding k*Nx*Ny values -> (k, Nx, Ny)."""
+    k = buf.size // (Nx * Ny)
+    return np.swapaxes(np.reshape(buf, (k, Ny, Nx)), -1, -2)
+
+
+class Handle:
+    """Owning wrapper of one fdfd_handle (create ... destroy)."""
+
+    def __init__(self, Nx, Ny, Npx, Npy, dx, dy, L0=1e-6, pml_m=3.5, pml_lnR=-12.0, pol=FDFD_TM,
+                 precision=FDFD_PREC_MIXED):
+        self.lib = load()
+        self.h = C.c_void_p()
+        rc = self.lib.fdfd_create(C.byref(self.h), int(Nx), int(Ny), int(Npx), int(Npy), float(dx), float(dy),
+                                  float(L0), float(pml_m), float(pml_lnR), int(pol), int(precision))
+        if rc != FDFD_OK:
+            raise FDFDError(rc, "fdfd_create failed")
+        self.Nx, self.Ny, self.pol = int(Nx), int(Ny), int(pol)
+
+    def _check(self, rc):
+        if rc != FDFD_OK:
+            raise FDFDError(rc, self.lib.fdfd_last_error(self.h).decode())
+
+    def close(self):
+        if self.h:
+            self.lib.fdfd_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_refinement(self, tol=1e-10, max_iter=40, mode=FDFD_REFINE_GMRES):
+        self._check(self.lib.fdfd_set_refinement(self.h, float(tol), int(max_iter), int(mode)))
+
+    def set_eps(self, eps):
+        buf = natural(eps)
+        self._check(self.lib.fdfd_set_eps(self.h, cptr(buf)))
+
+    def factor(self, omega):
+        self._check(self.lib.fdfd_factor(self.h, float(omega)))
+
+    def solve(self, src, fields=3):
+        """src (nrhs, Nx, Ny) or (Nx, Ny) -> (f1, f2, f3, stats) arrays shaped like src."""
+        src = np.asarray(src, dtype=np.complex128)
+        single = src.ndim == 2
+        s3 = src[None] if single else src
+        nrhs = s3.shape[0]
+        buf = natural(s3)
+        outs = [np.empty_like(buf) if i < fields else None for i in range(3)]
+        st = Stats()
+        self._check(self.lib.fdfd_solve(self.h, cptr(buf), nrhs, cptr(outs[0]), cptr(outs[1]), cptr(outs[2]),
+                                        C.byref(st)))
+        res = [from_natural(o, self.Nx, self.Ny) if o is not None else None for o in outs]
+        if single:
+            res = [r[0] if r is not None else None for r in res]
+        return res[0], res[1], res[2], st
+
+    def set_profiling(self, on=True):
+        self._check(self.lib.fdfd_set_profiling(self.h, 1 if on else 0))
+
+    def profile(self):
+        p = Profile()
+        self._check(self.lib.fdfd_get_profile(self.h, C.byref(p)))
+        return p.as_dict()
+
+    def solve_device(self, d_src: int, nrhs: int, d_f1: int, d_f2: int, d_f3: int):
+        """fdfd_solve_device on raw device pointers (ints); returns Stats."""
+        st = Stats()
+        self._check(self.lib.fdfd_solve_device(self.h, C.c_void_p(d_src), int(nrhs), C.c_void_p(d_f1),
+                                               C.c_void_p(d_f2), C.c_void_p(d_f3), C.byref(st)))
+        return st
+
+    def stencil(self):
+        out = np.empty((5, self.Ny, self.Nx), dtype=np.complex128)
+        self._check(self.lib.fdfd_get_stencil(self.h, cptr(out)))
+        return np.swapaxes(out, 1, 2)
+
+    def apply(self, x):
+        x = np.asarray(x, dtype=np.complex128)
+        single = x.ndim == 2
+        x3 = x[None] if single else x
+        buf = natural(x3)
+        out = np.empty_like(buf)
+        self._check(self.lib.fdfd_apply(self.h, cptr(buf), x3.shape[0], cptr(out)))
+        y = from_natural(out, self.Nx, self.Ny)
+        return y[0] if single else y
+
+
+def debug_gemm(A, B, precision=FDFD_PREC_MIXED, use_tc=1):
+    """C = A @ B.T through the library's block GEMM kernels (returns C, kernel ms)."""
+    lib = load()
+    A = np.ascontiguousarray(A, dtype=np.complex128)
+    B = np.ascontiguousarray(B, dtype=np.complex128)
+    M, K = A.shape
+    N = B.shape[0]
+    Cm = np.empty((M, N), dtype=np.complex128)
+    ms = C.c_double(0)
+    rc = lib.fdfd_debug_gemm(M, N, K, cptr(A), cptr(B), cptr(Cm), int(precision), int(use_tc), C.byref(ms))
+    if rc != FDFD_OK:
+        raise FDFDError(rc, "fdfd_debug_gemm failed")
+    return Cm, ms.value

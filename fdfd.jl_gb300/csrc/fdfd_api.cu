@@ -1,0 +1,1379 @@
+// libfdfd_cuda: handle, block cyclic reduction plan, factorization driver,
+// sweeps, FP64 refinement and the C ABI declared in include/fdfd_cuda.h.
+//
+// Method.  With the unknowns of a grid line ("node", b = min(Nx, Ny) unknowns)
+// grouped together, the FDFD operator is block-cyclic-tridiagonal over the
+// n = max(Nx, Ny) nodes.  It is factored by block cyclic reduction: each step
+// eliminates every other node of the current ring,
+//     G_k = D_k⁻¹ (blocked Gauss-Jordan with partial pivoting),
+//     X_L = G_k L_k,  X_R = G_k U_k,
+//     D_p -= U_p X_L,  U_p' = -U_p X_R,  D_q -= L_q X_R,  L_q' = -L_q X_L,
+// for k with ring neighbours p (previous) and q (next), until two nodes
+// remain; they are merged and solved directly.  The first step has diagonal
+// couplings and costs O(b²) per node beyond the inversions; every later step
+// is dense complex GEMM work, batched over the eliminated nodes.
+//
+// The solve sweeps the steps forward (z_k = G_k r_k; r_p -= U_p z_k;
+// r_q -= L_q z_k) and backward (x_k = z_k - X_L x_p - X_R x_q).
+// FDFD_PREC_FP64 runs all of it in complex FP64; FDFD_PREC_MIXED stores the
+// factors in complex FP32, forms the products with 3xTF32 tcgen05 MMAs, and
+// recovers FP64 accuracy with flexible GMRES (or classic refinement) whose
+// residuals b - A x and updates are FP64.
+#include "fdfd_cuda.h"
+#include "kernels.cuh"
+#include "gemm_tc.cuh"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <complex>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#define FDFD_VERSION_STR "fdfd_cuda 0.1.0 (sm_103a)"
+
+namespace {
+
+constexpr double kEPS0 = 8.85418782e-12;   // src/types.jl:6
+constexpr double kMU0 = 1.25663706e-6;     // src/types.jl:7
+
+typedef std::complex<double> zd;
+
+struct StepPlan {
+    std::vector<int> elim, eprev, enext;          // eliminated nodes and ring neighbours
+    std::vector<int> surv, sprev, snext;          // survivors (ring order) and neighbours
+    std::vector<char> sprev_elim, snext_elim;
+};
+
+template <typename T> struct DevArr {
+    T* p = nullptr;
+    size_t n = 0;
+};
+
+// all device-side integer job arrays of a plan live in one allocation
+struct JobBlob {
+    std::vector<unsigned char> host;
+    size_t add(const void* src, size_t bytes) {
+        size_t off = (host.size() + 15) & ~size_t(15);
+        host.resize(off + bytes);
+        if (bytes) memcpy(host.data() + off, src, bytes);
+        return off;
+    }
+};
+
+struct StepJobs {     // offsets into the job blob
+    size_t elim = 0, l1 = 0, fwd1 = 0, fwd1y = 0, dswf = 0, dswb = 0, bwd1 = 0, bwd1y = 0;
+    size_t xt_a = 0, xt_b = 0, xt_c = 0;
+    size_t dp_a = 0, dp_b = 0, dp_c = 0, dq_a = 0, dq_b = 0, dq_c = 0;
+    size_t cp_a = 0, cp_b = 0, cp_c = 0, cp_t = 0;
+    size_t cpy = 0;
+    size_t f2 = 0, f2y = 0, bw = 0, bwy = 0;
+    size_t iota = 0;
+    int ne = 0, ns = 0, nl1 = 0, ncp = 0, ncpy = 0, nf2 = 0;
+};
+
+template <typename T> struct FactorStore {
+    Pool<T> D, C, X, GP, RP;
+    T* rv = nullptr; T* xv = nullptr; T* wv = nullptr;
+    int vec_nrhs = 0;
+    int* perm = nullptr;
+    bool tc_ok = false;
+    TcMaps tc;       // TMA descriptors (FP32 only)
+};
+
+}  // namespace
+
+struct fdfd_handle {
+    // problem
+    int Nx, Ny, Npx, Npy, pol, precision;
+    double dx, dy, L0, pml_m, pml_lnR;
+    double tol = 1e-10;
+    int max_iter = 40;
+    int refine_mode = FDFD_REFINE_GMRES;
+    NodeMap map;
+    // state
+    bool eps_set = false, factored = false;
+    int op = OP_TM_DRIVEN;
+    double omega = 0;            // frequency of the factored operator
+    zd sigma = 0;                // eigen shift of the factored operator
+    double scale = 1;            // factorization scaling of A
+    std::string err;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev[8];
+    long long launches = 0;
+    long long dev_bytes = 0;
+    // FP64 device buffers (natural layout)
+    cplx<double>* eps = nullptr;     // Nx*Ny
+    cplx<double>* sf = nullptr;      // 2*(2Nx+2Ny)
+    cplx<double>* st = nullptr;      // 5*Nx*Ny
+    unsigned* derr = nullptr;        // device error word
+    double* part = nullptr;          // reduction partials
+    double* red = nullptr;           // reduced values
+    int part_blocks = 0;
+    size_t part_cap = 0, red_cap = 0;
+    // Krylov workspace (FP64 natural), sized for kr_nrhs right-hand sides
+    cplx<double>* kb = nullptr;      // right-hand sides
+    cplx<double>* kx = nullptr;      // solutions
+    cplx<double>* kr = nullptr;      // residuals
+    cplx<double>* kV = nullptr;      // (m+1) basis vectors
+    cplx<double>* kZ = nullptr;      // m preconditioned vectors
+    cplx<double>* kc = nullptr;      // small coefficient array
+    cplx<double>* io = nullptr;      // staging for the host API (source + 3 fields)
+    size_t io_cap = 0;
+    int kr_nrhs = 0, kr_m = 0;
+    // plan
+    std::vector<StepPlan> steps;
+    int fin_a = -1, fin_c = -1;
+    std::vector<std::vector<int>> Lslot, Uslot;     // [e][node], e = 1..E
+    std::vector<int> XL, XR;                        // [node]
+    int Xf = -1, C01 = -1, C10 = -1;
+    int nCslots = 0, nXslots = 0, max_ne = 0;
+    std::vector<StepJobs> sj;
+    size_t fin_mrg = 0, fin_c_slot = 0, fin_a_slot = 0, fin_xt_a = 0, fin_xt_b = 0, fin_xt_c = 0,
+           fin_da_a = 0, fin_da_b = 0, fin_da_c = 0, fin_g1 = 0, fin_g1y = 0, fin_ra = 0, fin_ray = 0,
+           fin_g0 = 0, fin_g0y = 0, fin_bx = 0, fin_bxy = 0, fin_iota = 0;
+    unsigned char* djobs = nullptr;
+    // factor storage
+    FactorStore<float> f32;
+    FactorStore<double> f64;
+    double last_factor_flops = 0;
+    int tc_used = 0;
+    bool use_tc = true;
+    // profiling (CUDA events around launches on the handle's stream)
+    struct ProfRec { int cls, e0, e1; double work; };
+    bool prof_on = false;
+    std::vector<cudaEvent_t> evpool;
+    std::vector<int> evfree;
+    std::vector<ProfRec> recs;
+    fdfd_profile prof_tot;
+};
+
+namespace {
+
+int set_err(fdfd_handle* h, int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    if (h) h->err = buf;
+    return code;
+}
+
+#define CK(call)                                                                                    \
+    do {                                                                                            \
+        cudaError_t e_ = (call);                                                                    \
+        if (e_ != cudaSuccess)                                                                      \
+            return set_err(h, e_ == cudaErrorMemoryAllocation ? FDFD_ENOMEM : FDFD_ECUDA,           \
+                           "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+    } while (0)
+
+#define RET(x)                  \
+    do {                        \
+        int r_ = (x);           \
+        if (r_ != FDFD_OK) return r_; \
+    } while (0)
+
+#define LAUNCH(kernel, grid, block, smem, ...)                                  \
+    do {                                                                        \
+        kernel<<<(grid), (block), (smem), h->stream>>>(__VA_ARGS__);            \
+        h->launches++;                                                          \
+    } while (0)
+
+int check_launch(fdfd_handle* h, const char* where) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return set_err(h, FDFD_ECUDA, "kernel launch failed in %s: %s", where, cudaGetErrorString(e));
+    return FDFD_OK;
+}
+
+int dev_alloc(fdfd_handle* h, void** p, size_t bytes) {
+    if (bytes == 0) bytes = 16;
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return set_err(h, FDFD_ENOMEM, "cudaMalloc(%zu bytes) failed: %s", bytes, cudaGetErrorString(e));
+    }
+    h->dev_bytes += (long long)bytes;
+    return FDFD_OK;
+}
+
+void dev_free(void* p) {
+    if (p) cudaFree(p);
+}
+
+// ---- profiling -------------------------------------------------------------
+int prof_event(fdfd_handle* h) {
+    if (h->evfree.empty()) {
+        cudaEvent_t e;
+        if (cudaEventCreate(&e) != cudaSuccess) return -1;
+        h->evpool.push_back(e);
+        return (int)h->evpool.size() - 1;
+    }
+    int i = h->evfree.back();
+    h->evfree.pop_back();
+    return i;
+}
+// returns the start event index (or -1 when profiling is off)
+int prof_begin(fdfd_handle* h) {
+    if (!h->prof_on) return -1;
+    int e = prof_event(h);
+    if (e >= 0) cudaEventRecord(h->evpool[e], h->stream);
+    return e;
+}
+void prof_end(fdfd_handle* h, int e0, int cls, double work) {
+    if (e0 < 0) return;
+    int e1 = prof_event(h);
+    if (e1 < 0) return;
+    cudaEventRecord(h->evpool[e1], h->stream);
+    h->recs.push_back({cls, e0, e1, work});
+}
+void prof_collect(fdfd_handle* h) {
+    if (h->recs.empty()) return;
+    cudaStreamSynchronize(h->stream);
+    for (auto& r : h->recs) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, h->evpool[r.e0], h->evpool[r.e1]);
+        h->prof_tot.ms[r.cls] += ms;
+        h->prof_tot.work[r.cls] += r.work;
+        h->prof_tot.launches[r.cls] += 1;
+        h->evfree.push_back(r.e0);
+        h->evfree.push_back(r.e1);
+    }
+    h->recs.clear();
+}
+
+// poll the device error word (synchronises the stream)
+int check_device(fdfd_handle* h, const char* where) {
+    unsigned e = 0;
+    CK(cudaMemcpyAsync(&e, h->derr, sizeof e, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    if (e) {
+        CK(cudaMemsetAsync(h->derr, 0, sizeof(unsigned), h->stream));
+        if (e & FDFD_DEVERR_TIMEOUT)
+            return set_err(h, FDFD_ETIMEOUT, "%s: a bounded device wait timed out", where);
+        if (e & FDFD_DEVERR_SINGULAR)
+            return set_err(h, FDFD_ESINGULAR, "%s: zero or non-finite pivot in a block inversion", where);
+        return set_err(h, FDFD_ECUDA, "%s: device error 0x%x", where, e);
+    }
+    return FDFD_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Plan: ring sequence of the cyclic reduction, slot assignment, job arrays.
+// ---------------------------------------------------------------------------
+void build_plan(fdfd_handle* h) {
+    const int n = h->map.n;
+    h->steps.clear();
+    std::vector<int> ring(n);
+    for (int j = 0; j < n; ++j) ring[j] = j;
+    std::vector<std::vector<int>> rings;
+    rings.push_back(ring);
+    while ((int)ring.size() > 2) {
+        int m = (int)ring.size();
+        StepPlan sp;
+        std::vector<char> is_elim(m, 0);
+        for (int pos = 1; pos < m; pos += 2) is_elim[pos] = 1;
+        for (int pos = 1; pos < m; pos += 2) {
+            sp.elim.push_back(ring[pos]);
+            sp.eprev.push_back(ring[pos - 1]);
+            sp.enext.push_back(ring[(pos + 1) % m]);
+        }
+        std::vector<int> next;
+        for (int pos = 0; pos < m; pos += 2) {
+            sp.surv.push_back(ring[pos]);
+            int pp = (pos - 1 + m) % m, pn = (pos + 1) % m;
+            sp.sprev.push_back(ring[pp]);
+            sp.snext.push_back(ring[pn]);
+            sp.sprev_elim.push_back(is_elim[pp]);
+            sp.snext_elim.push_back(is_elim[pn]);
+            next.push_back(ring[pos]);
+        }
+        h->steps.push_back(sp);
+        ring = next;
+        rings.push_back(ring);
+    }
+    h->fin_a = ring[0];
+    h->fin_c = ring[1];
+    const int E = (int)h->steps.size();   // rings[1..E] carry dense couplings
+    // coupling slots
+    h->Lslot.assign(E + 1, std::vector<int>(n, -1));
+    h->Uslot.assign(E + 1, std::vector<int>(n, -1));
+    int cs = 0;
+    for (int e = 1; e <= E; ++e)
+        for (int s : rings[e]) { h->Lslot[e][s] = cs++; h->Uslot[e][s] = cs++; }
+    h->C01 = cs++;
+    h->C10 = cs++;
+    h->nCslots = cs;
+    h->XL.assign(n, -1);
+    h->XR.assign(n, -1);
+    int xs = 0;
+    h->max_ne = 1;
+    for (int e = 1; e <= E; ++e) {
+        const StepPlan& sp = h->steps[e - 1];
+        h->max_ne = std::max(h->max_ne, (int)sp.elim.size());
+        if (e >= 2)
+            for (int k : sp.elim) { h->XL[k] = xs++; h->XR[k] = xs++; }
+    }
+    h->Xf = xs++;
+    h->nXslots = xs;
+}
+
+// storage form of node s's couplings in ring e: transposed iff s is eliminated next
+bool coupling_trans(const fdfd_handle* h, int e, int s) {
+    const int E = (int)h->steps.size();
+    if (e == E) return s == h->fin_c;
+    const StepPlan& nx = h->steps[e];   // step e+1
+    return std::find(nx.elim.begin(), nx.elim.end(), s) != nx.elim.end();
+}
+
+void build_jobs(fdfd_handle* h, JobBlob& B) {
+    const int E = (int)h->steps.size();
+    h->sj.assign(E + 1, StepJobs());
+    for (int e = 1; e <= E; ++e) {
+        const StepPlan& sp = h->steps[e - 1];
+        StepJobs& J = h->sj[e];
+        const int ne = (int)sp.elim.size(), ns = (int)sp.surv.size();
+        J.ne = ne; J.ns = ns;
+        J.elim = B.add(sp.elim.data(), ne * sizeof(int));
+        std::vector<int> iota(ne);
+        for (int i = 0; i < ne; ++i) iota[i] = i;
+        J.iota = B.add(iota.data(), ne * sizeof(int));
+        // forward F1: z_k = G_k r_k
+        std::vector<int4> f1(ne);
+        std::vector<int2> f1y(ne);
+        for (int i = 0; i < ne; ++i) { f1[i] = make_int4(sp.elim[i], sp.elim[i], -1, -1); f1y[i] = make_int2(sp.elim[i], -1); }
+        J.fwd1 = B.add(f1.data(), ne * sizeof(int4));
+        J.fwd1y = B.add(f1y.data(), ne * sizeof(int2));
+        if (e == 1) {
+            std::vector<L1Job> l1(ns);
+            std::vector<int4> dswf, dswb(ne), b1(ne);
+            std::vector<int2> b1y(ne);
+            for (int i = 0; i < ns; ++i) {
+                int s = sp.surv[i];
+                L1Job j;
+                j.s = s; j.prev = sp.sprev[i]; j.next = sp.snext[i];
+                j.prev_elim = sp.sprev_elim[i]; j.next_elim = sp.snext_elim[i];
+                j.u_slot = h->Uslot[1][s]; j.l_slot = h->Lslot[1][s];
+                j.u_trans = j.l_trans = coupling_trans(h, 1, s) ? 1 : 0;
+                l1[i] = j;
+                int flags = (sp.sprev_elim[i] ? 1 : 0) | (sp.snext_elim[i] ? 2 : 0);
+                if (flags) dswf.push_back(make_int4(s, sp.sprev[i], sp.snext[i], flags));
+            }
+            for (int i = 0; i < ne; ++i) {
+                dswb[i] = make_int4(sp.elim[i], sp.eprev[i], sp.enext[i], 3);
+                b1[i] = make_int4(sp.elim[i], sp.elim[i], -1, -1);     // G_k · w_k
+                b1y[i] = make_int2(sp.elim[i], sp.elim[i]);
+            }
+            J.l1 = B.add(l1.data(), ns * sizeof(L1Job));
+            J.nl1 = ns;
+            J.dswf = B.add(dswf.data(), dswf.size() * sizeof(int4));
+            J.nf2 = (int)dswf.size();
+            J.dswb = B.add(dswb.data(), ne * sizeof(int4));
+            J.bwd1 = B.add(b1.data(), ne * sizeof(int4));
+            J.bwd1y = B.add(b1y.data(), ne * sizeof(int2));
+        } else {
+            std::vector<int> xa(2 * ne), xb(2 * ne), xc(2 * ne);
+            std::vector<int> dpa(ne), dpb(ne), dpc(ne), dqa(ne), dqb(ne), dqc(ne);
+            std::vector<int> cpa(2 * ne), cpb(2 * ne), cpc(2 * ne), cpt(2 * ne);
+            std::vector<int4> bw(ne);
+            std::vector<int2> bwy(ne);
+            for (int i = 0; i < ne; ++i) {
+                int k = sp.elim[i], p = sp.eprev[i], q = sp.enext[i];
+                xa[i] = h->Lslot[e - 1][k]; xb[i] = k; xc[i] = h->XL[k];
+                xa[ne + i] = h->Uslot[e - 1][k]; xb[ne + i] = k; xc[ne + i] = h->XR[k];
+                dpa[i] = h->Uslot[e - 1][p]; dpb[i] = h->XL[k]; dpc[i] = p;
+                dqa[i] = h->Lslot[e - 1][q]; dqb[i] = h->XR[k]; dqc[i] = q;
+                cpa[i] = h->Uslot[e - 1][p]; cpb[i] = h->XR[k]; cpc[i] = h->Uslot[e][p];
+                cpt[i] = coupling_trans(h, e, p) ? 1 : 0;
+                cpa[ne + i] = h->Lslot[e - 1][q]; cpb[ne + i] = h->XL[k]; cpc[ne + i] = h->Lslot[e][q];
+                cpt[ne + i] = coupling_trans(h, e, q) ? 1 : 0;
+                bw[i] = make_int4(h->XL[k], p, h->XR[k], q);
+                bwy[i] = make_int2(k, k);
+            }
+            J.xt_a = B.add(xa.data(), 2 * ne * sizeof(int));
+            J.xt_b = B.add(xb.data(), 2 * ne * sizeof(int));
+            J.xt_c = B.add(xc.data(), 2 * ne * sizeof(int));
+            J.dp_a = B.add(dpa.data(), ne * sizeof(int)); J.dp_b = B.add(dpb.data(), ne * sizeof(int));
+            J.dp_c = B.add(dpc.data(), ne * sizeof(int));
+            J.dq_a = B.add(dqa.data(), ne * sizeof(int)); J.dq_b = B.add(dqb.data(), ne * sizeof(int));
+            J.dq_c = B.add(dqc.data(), ne * sizeof(int));
+            J.cp_a = B.add(cpa.data(), 2 * ne * sizeof(int)); J.cp_b = B.add(cpb.data(), 2 * ne * sizeof(int));
+            J.cp_c = B.add(cpc.data(), 2 * ne * sizeof(int)); J.cp_t = B.add(cpt.data(), 2 * ne * sizeof(int));
+            J.ncp = 2 * ne;
+            // couplings that cross no eliminated node: copied (transposed if the form changes)
+            std::vector<int3> cpy;
+            std::vector<int4> f2;
+            std::vector<int2> f2y;
+            for (int i = 0; i < ns; ++i) {
+                int s = sp.surv[i];
+                int tr = coupling_trans(h, e, s) ? 1 : 0;
+                if (!sp.snext_elim[i]) cpy.push_back(make_int3(h->Uslot[e][s], h->Uslot[e - 1][s], tr));
+                if (!sp.sprev_elim[i]) cpy.push_back(make_int3(h->Lslot[e][s], h->Lslot[e - 1][s], tr));
+                if (sp.snext_elim[i] || sp.sprev_elim[i]) {
+                    f2.push_back(make_int4(sp.snext_elim[i] ? h->Uslot[e - 1][s] : -1, sp.snext[i],
+                                           sp.sprev_elim[i] ? h->Lslot[e - 1][s] : -1, sp.sprev[i]));
+                    f2y.push_back(make_int2(s, s));
+                }
+            }
+            J.cpy = B.add(cpy.data(), cpy.size() * sizeof(int3));
+            J.ncpy = (int)cpy.size();
+            J.f2 = B.add(f2.data(), f2.size() * sizeof(int4));
+            J.f2y = B.add(f2y.data(), f2y.size() * sizeof(int2));
+            J.nf2 = (int)f2.size();
+            J.bw = B.add(bw.data(), ne * sizeof(int4));
+            J.bwy = B.add(bwy.data(), ne * sizeof(int2));
+        }
+    }
+    // final two nodes
+    const int a = h->fin_a, c = h->fin_c;
+    int3 mrg[2] = {make_int3(h->C01, h->Uslot[E][a], h->Lslot[E][a]),
+                   make_int3(h->C10, h->Uslot[E][c], h->Lslot[E][c])};
+    h->fin_mrg = B.add(mrg, sizeof mrg);
+    h->fin_c_slot = B.add(&c, sizeof(int));
+    h->fin_a_slot = B.add(&a, sizeof(int));
+    int zero = 0;
+    h->fin_iota = B.add(&zero, sizeof(int));
+    h->fin_xt_a = B.add(&h->C10, sizeof(int));
+    h->fin_xt_b = B.add(&c, sizeof(int));
+    h->fin_xt_c = B.add(&h->Xf, sizeof(int));
+    h->fin_da_a = B.add(&h->C01, sizeof(int));
+    h->fin_da_b = B.add(&h->Xf, sizeof(int));
+    h->fin_da_c = B.add(&a, sizeof(int));
+    int4 g1 = make_int4(c, c, -1, -1); int2 g1y = make_int2(c, -1);
+    int4 ra = make_int4(h->C01, c, -1, -1); int2 ray = make_int2(a, a);
+    int4 g0 = make_int4(a, a, -1, -1); int2 g0y = make_int2(a, -1);
+    int4 bx = make_int4(h->Xf, a, -1, -1); int2 bxy = make_int2(c, c);
+    h->fin_g1 = B.add(&g1, sizeof g1); h->fin_g1y = B.add(&g1y, sizeof g1y);
+    h->fin_ra = B.add(&ra, sizeof ra); h->fin_ray = B.add(&ray, sizeof ray);
+    h->fin_g0 = B.add(&g0, sizeof g0); h->fin_g0y = B.add(&g0y, sizeof g0y);
+    h->fin_bx = B.add(&bx, sizeof bx); h->fin_bxy = B.add(&bxy, sizeof bxy);
+}
+
+template <typename U> U* J(fdfd_handle* h, size_t off) { return reinterpret_cast<U*>(h->djobs + off); }
+
+// ---------------------------------------------------------------------------
+// Factor storage
+// ---------------------------------------------------------------------------
+template <typename T> FactorStore<T>& store(fdfd_handle* h);
+template <> FactorStore<float>& store<float>(fdfd_handle* h) { return h->f32; }
+template <> FactorStore<double>& store<double>(fdfd_handle* h) { return h->f64; }
+
+template <typename T> int panel_nb(int b) {
+    if (sizeof(T) == 4) return b <= 800 ? 32 : 16;
+    return b <= 768 ? 16 : 8;
+}
+
+template <typename T> int alloc_pool(fdfd_handle* h, Pool<T>& P, int rows, int cols, int ld, int planes,
+                                     long long count) {
+    P.rows = rows; P.cols = cols; P.ld = ld; P.planes = planes; P.count = count;
+    size_t bytes = (size_t)P.slot_elems() * count * sizeof(T);
+    void* p = nullptr;
+    RET(dev_alloc(h, &p, bytes));
+    P.base = (T*)p;
+    return FDFD_OK;
+}
+
+template <typename T> int alloc_factor(fdfd_handle* h) {
+    FactorStore<T>& F = store<T>(h);
+    if (F.D.base) return FDFD_OK;
+    const int b = h->map.b, n = h->map.n, ld = h->map.ld;
+    const int planes = sizeof(T) == 4 ? 4 : 2;
+    const int pc = sizeof(T) == 4 ? 32 : panel_nb<T>(b);
+    RET(alloc_pool<T>(h, F.D, b, b, ld, planes, n));
+    RET(alloc_pool<T>(h, F.C, b, b, ld, planes, h->nCslots));
+    RET(alloc_pool<T>(h, F.X, b, b, ld, planes, h->nXslots));
+    RET(alloc_pool<T>(h, F.GP, b, pc, pc, planes, h->max_ne));
+    RET(alloc_pool<T>(h, F.RP, b, pc, pc, planes, h->max_ne));
+    RET(dev_alloc(h, (void**)&F.perm, (size_t)h->max_ne * b * sizeof(int)));
+    if (sizeof(T) == 4 && h->use_tc) {
+        F.tc_ok = tc_make_maps(reinterpret_cast<Pool<float>*>(&F.D), reinterpret_cast<Pool<float>*>(&F.C),
+                               reinterpret_cast<Pool<float>*>(&F.X), reinterpret_cast<Pool<float>*>(&F.GP),
+                               reinterpret_cast<Pool<float>*>(&F.RP), &F.tc);
+    }
+    return FDFD_OK;
+}
+
+template <typename T> int alloc_vectors(fdfd_handle* h, int nrhs) {
+    FactorStore<T>& F = store<T>(h);
+    if (F.vec_nrhs >= nrhs) return FDFD_OK;
+    dev_free(F.rv); dev_free(F.xv); dev_free(F.wv);
+    F.rv = F.xv = F.wv = nullptr;
+    size_t bytes = (size_t)h->map.n * nrhs * 2 * h->map.ld * sizeof(T);
+    RET(dev_alloc(h, (void**)&F.rv, bytes));
+    RET(dev_alloc(h, (void**)&F.xv, bytes));
+    RET(dev_alloc(h, (void**)&F.wv, bytes));
+    CK(cudaMemsetAsync(F.rv, 0, bytes, h->stream));
+    CK(cudaMemsetAsync(F.xv, 0, bytes, h->stream));
+    CK(cudaMemsetAsync(F.wv, 0, bytes, h->stream));
+    F.vec_nrhs = nrhs;
+    return FDFD_OK;
+}
+
+// ---------------------------------------------------------------------------
+// GEMM dispatch
+// ---------------------------------------------------------------------------
+enum PoolId { P_D = 0, P_C = 1, P_X = 2, P_GP = 3, P_RP = 4 };
+
+template <typename T> Pool<T>& pool_of(FactorStore<T>& F, int id) {
+    switch (id) {
+        case P_D: return F.D;
+        case P_C: return F.C;
+        case P_X: return F.X;
+        case P_GP: return F.GP;
+        default: return F.RP;
+    }
+}
+
+template <typename T>
+int gemm(fdfd_handle* h, int pa, int pb, int pc, const int* a_slot, const int* b_slot, const int* c_slot,
+         const int* c_trans_arr, int c_trans, int njobs, int M, int N, int K, T alpha, int beta, int mask_c0,
+         int mask_w) {
+    if (njobs == 0) return FDFD_OK;
+    FactorStore<T>& F = store<T>(h);
+    GemmArgs<T> g;
+    g.A = pool_of(F, pa); g.B = pool_of(F, pb); g.C = pool_of(F, pc);
+    g.a_slot = a_slot; g.b_slot = b_slot; g.c_slot = c_slot;
+    g.M = M; g.N = N; g.K = K; g.alpha = alpha; g.beta = beta;
+    g.mask_c0 = mask_c0; g.mask_w = mask_w; g.c_trans = c_trans;
+    g.c_trans_arr = nullptr;
+    g.err = h->derr;
+    const double flops = 8.0 * M * N * K * njobs;
+    int ev = prof_begin(h);
+    if (sizeof(T) == 4 && F.tc_ok) {
+        int rc = tc_gemm_launch(reinterpret_cast<GemmArgs<float>*>(&g), c_trans_arr, pa, pb, njobs, &F.tc,
+                                h->stream);
+        if (rc != 0) return set_err(h, FDFD_ECUDA, "tcgen05 GEMM launch failed (%d)", rc);
+        prof_end(h, ev, FDFD_PROF_GEMM_TC, flops);
+        h->launches++;
+        h->tc_used = 1;
+        return check_launch(h, "gemm_tc");
+    }
+    g.c_trans_arr = c_trans_arr;
+    launch_gemm_simt<T>(h->stream, njobs, g);
+    prof_end(h, ev, FDFD_PROF_GEMM_SIMT, flops);
+    h->launches++;
+    return check_launch(h, "gemm_simt");
+}
+
+// ---------------------------------------------------------------------------
+// Gauss-Jordan inversion of D-pool slots (batched)
+// ---------------------------------------------------------------------------
+template <typename T> int gj_invert(fdfd_handle* h, const int* d_slots, const int* d_iota, int njobs) {
+    if (njobs == 0) return FDFD_OK;
+    FactorStore<T>& F = store<T>(h);
+    const int b = h->map.b;
+    const int nb = panel_nb<T>(b);
+    launch_perm_init(h->stream, njobs, F.perm, b);
+    h->launches++;
+    for (int c0 = 0; c0 < b; c0 += nb) {
+        int w = std::min(nb, b - c0);
+        int ev = prof_begin(h);
+        int e = launch_gj_panel<T>(h->stream, nb, njobs, F.D, d_slots, F.GP, F.RP, F.perm, c0, h->derr);
+        prof_end(h, ev, FDFD_PROF_GJ_PANEL, 0.0);
+        h->launches++;
+        if (e) return set_err(h, FDFD_ECUDA, "gj_panel launch failed: %s", cudaGetErrorString((cudaError_t)e));
+        RET(gemm<T>(h, P_GP, P_RP, P_D, d_iota, d_iota, d_slots, nullptr, 0, njobs, b, b, F.GP.cols, (T)1, 1,
+                    c0, w));
+    }
+    launch_gj_unpermute<T>(h->stream, njobs, F.D, d_slots, F.perm);
+    h->launches++;
+    return check_launch(h, "gj_unpermute");
+}
+
+// ---------------------------------------------------------------------------
+// Factorization
+// ---------------------------------------------------------------------------
+template <typename T> int factor_impl(fdfd_handle* h) {
+    RET(alloc_factor<T>(h));
+    FactorStore<T>& F = store<T>(h);
+    const int b = h->map.b;
+    const int E = (int)h->steps.size();
+    double flops = 0;
+    const double b3 = (double)b * b * b;
+    for (int e = 1; e <= E; ++e) {
+        const StepJobs& S = h->sj[e];
+        const int ne = S.ne;
+        if (e == 1) {
+            launch_build_tridiag<T>(h->stream, ne, h->map, h->st, h->scale, F.D, J<int>(h, S.elim));
+            h->launches++;
+            RET(check_launch(h, "build_tridiag"));
+            RET(gj_invert<T>(h, J<int>(h, S.elim), J<int>(h, S.iota), ne));
+            flops += 8.0 * b3 * ne;
+            launch_level1_combine<T>(h->stream, S.nl1, h->map, h->st, h->scale, F.D, F.C, J<L1Job>(h, S.l1));
+            h->launches++;
+            RET(check_launch(h, "level1_combine"));
+        } else {
+            RET(gj_invert<T>(h, J<int>(h, S.elim), J<int>(h, S.iota), ne));
+            // Xᵀ = [Lᵀ; Uᵀ] Gᵀ
+            RET(gemm<T>(h, P_C, P_D, P_X, J<int>(h, S.xt_a), J<int>(h, S.xt_b), J<int>(h, S.xt_c), nullptr, 0,
+                        2 * ne, b, b, b, (T)1, 0, 0, 0));
+            // D_p -= U_p X_L ; D_q -= L_q X_R
+            RET(gemm<T>(h, P_C, P_X, P_D, J<int>(h, S.dp_a), J<int>(h, S.dp_b), J<int>(h, S.dp_c), nullptr, 0,
+                        ne, b, b, b, (T)-1, 1, 0, 0));
+            RET(gemm<T>(h, P_C, P_X, P_D, J<int>(h, S.dq_a), J<int>(h, S.dq_b), J<int>(h, S.dq_c), nullptr, 0,
+                        ne, b, b, b, (T)-1, 1, 0, 0));
+            // new couplings U_p' = -U_p X_R, L_q' = -L_q X_L (storage form per node)
+            RET(gemm<T>(h, P_C, P_X, P_C, J<int>(h, S.cp_a), J<int>(h, S.cp_b), J<int>(h, S.cp_c),
+                        J<int>(h, S.cp_t), 0, S.ncp, b, b, b, (T)-1, 0, 0, 0));
+            if (S.ncpy) {
+                launch_mcopy<T>(h->stream, S.ncpy, F.C, F.C, J<int3>(h, S.cpy));
+                h->launches++;
+                RET(check_launch(h, "mcopy"));
+            }
+            flops += 8.0 * b3 * ne * 7;   // inversion + 2 (Xᵀ) + 4 (updates)
+        }
+    }
+    // final pair (a, c)
+    launch_madd<T>(h->stream, 2, F.C, J<int3>(h, h->fin_mrg));
+    h->launches++;
+    RET(check_launch(h, "madd"));
+    RET(gj_invert<T>(h, J<int>(h, h->fin_c_slot), J<int>(h, h->fin_iota), 1));
+    RET(gemm<T>(h, P_C, P_D, P_X, J<int>(h, h->fin_xt_a), J<int>(h, h->fin_xt_b), J<int>(h, h->fin_xt_c), nullptr,
+                0, 1, b, b, b, (T)1, 0, 0, 0));
+    RET(gemm<T>(h, P_C, P_X, P_D, J<int>(h, h->fin_da_a), J<int>(h, h->fin_da_b), J<int>(h, h->fin_da_c), nullptr,
+                0, 1, b, b, b, (T)-1, 1, 0, 0));
+    RET(gj_invert<T>(h, J<int>(h, h->fin_a_slot), J<int>(h, h->fin_iota), 1));
+    flops += 8.0 * b3 * 4;
+    h->last_factor_flops = flops;
+    return FDFD_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Solve sweeps: F.rv holds the (scaled) right-hand sides in node layout on
+// entry; F.xv holds the solution on exit.
+// ---------------------------------------------------------------------------
+template <typename T> int gemv(fdfd_handle* h, int tr, int p1, int p2, const T* V1, const T* V2, const T* Y0, T* Y,
+                               const int4* jobs, const int2* yjobs, int njobs, int nrhs, T alpha) {
+    if (njobs == 0) return FDFD_OK;
+    FactorStore<T>& F = store<T>(h);
+    const int b = h->map.b;
+    int rmax = (int)std::min<size_t>(8, (size_t)(150 * 1024) / ((size_t)4 * b * sizeof(T)));
+    if (rmax < 1) rmax = 1;
+    for (int r0 = 0; r0 < nrhs; r0 += rmax) {
+        GemvArgs<T> g;
+        g.P1 = pool_of(F, p1); g.P2 = pool_of(F, p2);
+        g.V1 = V1; g.V2 = V2; g.Y0 = Y0; g.Y = Y;
+        g.jobs = jobs; g.yjobs = yjobs;
+        g.b = b; g.ld = h->map.ld; g.nrhs = std::min(rmax, nrhs - r0); g.rtot = nrhs; g.r0 = r0;
+        g.alpha = alpha;
+        int ev = prof_begin(h);
+        int e = launch_gemv<T>(h->stream, tr, njobs, g);
+        // algorithmic bytes: every referenced block (re + im planes) read once, vectors in and out
+        prof_end(h, ev, FDFD_PROF_SWEEP,
+                 (double)njobs * (2.0 * b * b * 2 * sizeof(T) + 3.0 * g.nrhs * 2 * b * sizeof(T)));
+        h->launches++;
+        if (e) return set_err(h, FDFD_ECUDA, "gemv launch failed: %s", cudaGetErrorString((cudaError_t)e));
+    }
+    return FDFD_OK;
+}
+
+template <typename T> int sweep_impl(fdfd_handle* h, int nrhs) {
+    FactorStore<T>& F = store<T>(h);
+    const int E = (int)h->steps.size();
+    // forward
+    for (int e = 1; e <= E; ++e) {
+        const StepJobs& S = h->sj[e];
+        RET(gemv<T>(h, 0, P_D, P_D, F.rv, F.rv, nullptr, F.xv, J<int4>(h, S.fwd1), J<int2>(h, S.fwd1y), S.ne, nrhs,
+                    (T)1));
+        if (e == 1) {
+            if (S.nf2) {
+                launch_diag_sweep<T>(h->stream, S.nf2, h->map, h->st, h->scale, nrhs, J<int4>(h, S.dswf), 0,
+                                     (const T*)F.xv, F.rv);
+                h->launches++;
+            }
+        } else {
+            RET(gemv<T>(h, 0, P_C, P_C, F.xv, F.xv, F.rv, F.rv, J<int4>(h, S.f2), J<int2>(h, S.f2y), S.nf2, nrhs,
+                        (T)-1));
+        }
+    }
+    // final pair
+    RET(gemv<T>(h, 0, P_D, P_D, F.rv, F.rv, nullptr, F.xv, J<int4>(h, h->fin_g1), J<int2>(h, h->fin_g1y), 1, nrhs,
+                (T)1));
+    RET(gemv<T>(h, 0, P_C, P_C, F.xv, F.xv, F.rv, F.rv, J<int4>(h, h->fin_ra), J<int2>(h, h->fin_ray), 1, nrhs,
+                (T)-1));
+    RET(gemv<T>(h, 0, P_D, P_D, F.rv, F.rv, nullptr, F.xv, J<int4>(h, h->fin_g0), J<int2>(h, h->fin_g0y), 1, nrhs,
+                (T)1));
+    RET(gemv<T>(h, 1, P_X, P_X, F.xv, F.xv, F.xv, F.xv, J<int4>(h, h->fin_bx), J<int2>(h, h->fin_bxy), 1, nrhs,
+                (T)-1));
+    // backward
+    for (int e = E; e >= 1; --e) {
+        const StepJobs& S = h->sj[e];
+        if (e == 1) {
+            launch_diag_sweep<T>(h->stream, S.ne, h->map, h->st, h->scale, nrhs, J<int4>(h, S.dswb), 1,
+                                 (const T*)F.xv, F.wv);
+            h->launches++;
+            RET(gemv<T>(h, 0, P_D, P_D, F.wv, F.wv, F.xv, F.xv, J<int4>(h, S.bwd1), J<int2>(h, S.bwd1y), S.ne, nrhs,
+                        (T)-1));
+        } else {
+            RET(gemv<T>(h, 1, P_X, P_X, F.xv, F.xv, F.xv, F.xv, J<int4>(h, S.bw), J<int2>(h, S.bwy), S.ne, nrhs,
+                        (T)-1));
+        }
+    }
+    return check_launch(h, "sweep");
+}
+
+// preconditioner: out = (scale·A)⁻¹ (scale·in) = A⁻¹ in  (FP64 natural layout, nrhs vectors)
+template <typename T> int precond_impl(fdfd_handle* h, const cplx<double>* in, cplx<double>* out, int nrhs) {
+    RET(alloc_vectors<T>(h, nrhs));
+    FactorStore<T>& F = store<T>(h);
+    long long N = (long long)h->Nx * h->Ny;
+    dim3 grid(ceil_div(N, 256), nrhs);
+    launch_to_nodes<T>(grid, h->stream, h->map, nrhs, in, h->scale, F.rv);
+    h->launches++;
+    RET(sweep_impl<T>(h, nrhs));
+    launch_from_nodes<T>(grid, h->stream, h->map, nrhs, (const T*)F.xv, 1.0, 0, out);
+    h->launches++;
+    return check_launch(h, "precond");
+}
+
+int precond(fdfd_handle* h, const cplx<double>* in, cplx<double>* out, int nrhs) {
+    return h->precision == FDFD_PREC_FP64 ? precond_impl<double>(h, in, out, nrhs)
+                                          : precond_impl<float>(h, in, out, nrhs);
+}
+
+// ---------------------------------------------------------------------------
+// Reductions and Krylov refinement (FP64, natural layout)
+// ---------------------------------------------------------------------------
+int ensure_part(fdfd_handle* h, size_t doubles) {
+    if (h->part_cap >= doubles) return FDFD_OK;
+    dev_free(h->part);
+    h->part = nullptr;
+    RET(dev_alloc(h, (void**)&h->part, doubles * sizeof(double)));
+    h->part_cap = doubles;
+    return FDFD_OK;
+}
+int ensure_red(fdfd_handle* h, size_t doubles) {
+    if (h->red_cap >= doubles) return FDFD_OK;
+    dev_free(h->red);
+    h->red = nullptr;
+    RET(dev_alloc(h, (void**)&h->red, doubles * sizeof(double)));
+    h->red_cap = doubles;
+    return FDFD_OK;
+}
+
+// r = b - A x (b may be null: r = A x); optionally ||r||², ||b||² per rhs to host
+int residual(fdfd_handle* h, const cplx<double>* x, const cplx<double>* b, cplx<double>* r, int nrhs,
+             std::vector<double>* norms) {
+    long long N = (long long)h->Nx * h->Ny;
+    int nb = ceil_div(N, 256);
+    RET(ensure_part(h, (size_t)nrhs * nb * 2));
+    RET(ensure_red(h, (size_t)nrhs * 2));
+    int ev = prof_begin(h);
+    LAUNCH(residual_kernel, dim3(nb, nrhs), 256, 0, h->Nx, h->Ny, nrhs, h->st, x, b, r, norms ? h->part : nullptr);
+    // algorithmic bytes per unknown: 5 stencil coefficients (80 B), x, r and b (16 B each)
+    prof_end(h, ev, FDFD_PROF_RESIDUAL, (double)N * nrhs * (80.0 + 16.0 * (b ? 3 : 2)));
+    if (norms) {
+        LAUNCH(reduce_partials_kernel, nrhs, 256, 0, h->part, nb, 2, h->red);
+        norms->resize(2 * nrhs);
+        CK(cudaMemcpyAsync(norms->data(), h->red, 2 * nrhs * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+    }
+    return check_launch(h, "residual");
+}
+
+// out[rhs*nvec + j] = V_jᴴ w  (complex)
+int dots(fdfd_handle* h, const cplx<double>* V, long long vstride, int nvec, const cplx<double>* w, int nrhs,
+         std::vector<zd>& out) {
+    long long N = (long long)h->Nx * h->Ny;
+    const int nb = 152;
+    RET(ensure_part(h, (size_t)nrhs * nb * 2 * nvec));
+    RET(ensure_red(h, (size_t)nrhs * 2 * nvec));
+    LAUNCH(vdots_kernel, dim3(nb, nrhs), 256, 0, N, nvec, V, vstride, w, h->part);
+    LAUNCH(reduce_partials_kernel, nrhs, 256, 0, h->part, nb, 2 * nvec, h->red);
+    std::vector<double> tmp(2 * nvec * nrhs);
+    CK(cudaMemcpyAsync(tmp.data(), h->red, tmp.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    out.resize(nvec * nrhs);
+    for (int i = 0; i < nvec * nrhs; ++i) out[i] = zd(tmp[2 * i], tmp[2 * i + 1]);
+    return check_launch(h, "dots");
+}
+
+// y[rhs] += sign Σ_j c[rhs][j] V_j[rhs]
+int combine(fdfd_handle* h, const cplx<double>* V, long long vstride, int nvec, const std::vector<zd>& c, int nrhs,
+            double sign, cplx<double>* y) {
+    long long N = (long long)h->Nx * h->Ny;
+    CK(cudaMemcpyAsync(h->kc, c.data(), c.size() * sizeof(zd), cudaMemcpyHostToDevice, h->stream));
+    LAUNCH(vcombine_kernel, dim3(ceil_div(N, 256), nrhs), 256, 0, N, nvec, V, vstride, h->kc, nvec, sign, y);
+    return check_launch(h, "combine");
+}
+
+int scale_vec(fdfd_handle* h, const cplx<double>* x, const std::vector<zd>& s, int nrhs, cplx<double>* y) {
+    long long N = (long long)h->Nx * h->Ny;
+    CK(cudaMemcpyAsync(h->kc, s.data(), nrhs * sizeof(zd), cudaMemcpyHostToDevice, h->stream));
+    LAUNCH(vscale_kernel, dim3(ceil_div(N, 256), nrhs), 256, 0, N, x, h->kc, y);
+    return check_launch(h, "scale");
+}
+
+int ensure_krylov(fdfd_handle* h, int nrhs, int m) {
+    if (h->kr_nrhs >= nrhs && h->kr_m >= m) return FDFD_OK;
+    dev_free(h->kb); dev_free(h->kx); dev_free(h->kr); dev_free(h->kV); dev_free(h->kZ); dev_free(h->kc);
+    long long N = (long long)h->Nx * h->Ny;
+    size_t v = (size_t)N * nrhs * sizeof(cplx<double>);
+    RET(dev_alloc(h, (void**)&h->kb, v));
+    RET(dev_alloc(h, (void**)&h->kx, v));
+    RET(dev_alloc(h, (void**)&h->kr, v));
+    RET(dev_alloc(h, (void**)&h->kV, v * (m + 1)));
+    RET(dev_alloc(h, (void**)&h->kZ, v * m));
+    RET(dev_alloc(h, (void**)&h->kc, (size_t)nrhs * (m + 2) * sizeof(cplx<double>) * 2));
+    h->kr_nrhs = nrhs;
+    h->kr_m = m;
+    return FDFD_OK;
+}
+
+// Solve A x = b (h->kb, nrhs vectors) into h->kx to ||b - A x||/||b|| <= tol.
+// GMRES mode: restarted flexible GMRES (Saad 1993) with classical Gram-Schmidt
+// and one re-orthogonalisation, right-preconditioned by the factorization.
+int refine(fdfd_handle* h, int nrhs, int* iters, double* relres) {
+    long long N = (long long)h->Nx * h->Ny;
+    const int m = 20;
+    RET(ensure_krylov(h, nrhs, m));
+    const size_t vs = (size_t)N * nrhs;   // stride between basis vectors
+    CK(cudaMemsetAsync(h->kx, 0, vs * sizeof(cplx<double>), h->stream));
+    std::vector<double> nrm;
+    RET(residual(h, h->kx, h->kb, h->kr, nrhs, &nrm));
+    std::vector<double> bnorm(nrhs), rel(nrhs);
+    for (int r = 0; r < nrhs; ++r) {
+        bnorm[r] = std::sqrt(nrm[2 * r + 1]);
+        if (bnorm[r] == 0) bnorm[r] = 1;
+        rel[r] = std::sqrt(nrm[2 * r]) / bnorm[r];
+    }
+    int it = 0;
+    auto maxrel = [&]() { return *std::max_element(rel.begin(), rel.end()); };
+    if (h->refine_mode == FDFD_REFINE_CLASSIC) {
+        while (maxrel() > h->tol && it < h->max_iter) {
+            RET(precond(h, h->kr, h->kZ, nrhs));
+            ++it;
+            std::vector<zd> one(nrhs, zd(1, 0));
+            RET(combine(h, h->kZ, 0, 1, one, nrhs, 1.0, h->kx));
+            RET(residual(h, h->kx, h->kb, h->kr, nrhs, &nrm));
+            for (int r = 0; r < nrhs; ++r) rel[r] = std::sqrt(nrm[2 * r]) / bnorm[r];
+        }
+    } else {
+        while (maxrel() > h->tol && it < h->max_iter) {
+            // start a cycle from the current residual
+            std::vector<double> beta(nrhs);
+            std::vector<zd> inv(nrhs);
+            for (int r = 0; r < nrhs; ++r) {
+                beta[r] = rel[r] * bnorm[r];
+                inv[r] = beta[r] > 0 ? zd(1.0 / beta[r], 0) : zd(0, 0);
+            }
+            RET(scale_vec(h, h->kr, inv, nrhs, h->kV));
+            std::vector<std::vector<zd>> H(nrhs, std::vector<zd>((m + 1) * m, 0));
+            std::vector<std::vector<zd>> cs(nrhs, std::vector<zd>(m)), sn(nrhs, std::vector<zd>(m));
+            std::vector<std::vector<zd>> gvec(nrhs, std::vector<zd>(m + 1, 0));
+            for (int r = 0; r < nrhs; ++r) gvec[r][0] = beta[r];
+            std::vector<char> done(nrhs, 0);
+            int j = 0;
+            for (; j < m && it < h->max_iter; ++j) {
+                cplx<double>* Vj = h->kV + j * vs;
+                cplx<double>* Vn = h->kV + (j + 1) * vs;
+                cplx<double>* Zj = h->kZ + j * vs;
+                RET(precond(h, Vj, Zj, nrhs));
+                ++it;
+                RET(residual(h, Zj, nullptr, Vn, nrhs, nullptr));   // Vn = A Zj
+                std::vector<zd> hc, hc2;
+                RET(dots(h, h->kV, vs, j + 1, Vn, nrhs, hc));
+                RET(combine(h, h->kV, vs, j + 1, hc, nrhs, -1.0, Vn));
+                RET(dots(h, h->kV, vs, j + 1, Vn, nrhs, hc2));
+                RET(combine(h, h->kV, vs, j + 1, hc2, nrhs, -1.0, Vn));
+                std::vector<zd> nn;
+                RET(dots(h, Vn, 0, 1, Vn, nrhs, nn));
+                std::vector<zd> sc(nrhs);
+                bool all = true;
+                for (int r = 0; r < nrhs; ++r) {
+                    std::vector<zd>& Hr = H[r];
+                    for (int i = 0; i <= j; ++i) Hr[i * m + j] = hc[r * (j + 1) + i] + hc2[r * (j + 1) + i];
+                    double hn = std::sqrt(std::max(0.0, nn[r].real()));
+                    Hr[(j + 1) * m + j] = hn;
+                    sc[r] = hn > 1e-300 ? zd(1.0 / hn, 0) : zd(0, 0);
+                    // apply previous Givens rotations
+                    for (int i = 0; i < j; ++i) {
+                        zd a = Hr[i * m + j], bb = Hr[(i + 1) * m + j];
+                        Hr[i * m + j] = std::conj(cs[r][i]) * a + std::conj(sn[r][i]) * bb;
+                        Hr[(i + 1) * m + j] = -sn[r][i] * a + cs[r][i] * bb;
+                    }
+                    zd a = Hr[j * m + j], bb = Hr[(j + 1) * m + j];
+                    double den = std::sqrt(std::norm(a) + std::norm(bb));
+                    if (den == 0) { cs[r][j] = 1; sn[r][j] = 0; }
+                    else { cs[r][j] = a / den; sn[r][j] = bb / den; }
+                    Hr[j * m + j] = std::conj(cs[r][j]) * a + std::conj(sn[r][j]) * bb;
+                    Hr[(j + 1) * m + j] = 0;
+                    zd g0 = gvec[r][j];
+                    gvec[r][j] = std::conj(cs[r][j]) * g0;
+                    gvec[r][j + 1] = -sn[r][j] * g0;
+                    double est = std::abs(gvec[r][j + 1]) / bnorm[r];
+                    if (est <= 0.5 * h->tol || hn <= 1e-300 * bnorm[r]) done[r] = 1;
+                    if (!done[r]) all = false;
+                }
+                RET(scale_vec(h, Vn, sc, nrhs, Vn));
+                if (all) { ++j; break; }
+            }
+            // x += Z y  with H y = g (upper triangular, j columns)
+            int k = j;
+            std::vector<zd> coef((size_t)nrhs * k);
+            for (int r = 0; r < nrhs; ++r) {
+                std::vector<zd> y(k);
+                for (int i = k - 1; i >= 0; --i) {
+                    zd s = gvec[r][i];
+                    for (int l = i + 1; l < k; ++l) s -= H[r][i * m + l] * y[l];
+                    zd d = H[r][i * m + i];
+                    y[i] = std::abs(d) > 0 ? s / d : zd(0, 0);
+                }
+                for (int i = 0; i < k; ++i) coef[(size_t)r * k + i] = y[i];
+            }
+            if (k > 0) RET(combine(h, h->kZ, vs, k, coef, nrhs, 1.0, h->kx));
+            RET(residual(h, h->kx, h->kb, h->kr, nrhs, &nrm));
+            for (int r = 0; r < nrhs; ++r) rel[r] = std::sqrt(nrm[2 * r]) / bnorm[r];
+        }
+    }
+    *iters = it;
+    *relres = maxrel();
+    return FDFD_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Assembly + factorization of the operator `op`
+// ---------------------------------------------------------------------------
+int assemble(fdfd_handle* h, int op, double omega_pml, zd sigma, double omega_drv) {
+    SFactorArgs sa;
+    sa.Nx = h->Nx; sa.Ny = h->Ny; sa.Npx = h->Npx; sa.Npy = h->Npy;
+    sa.dx = h->dx; sa.dy = h->dy; sa.omega = omega_pml; sa.eps0n = kEPS0 * h->L0;
+    sa.eta0 = std::sqrt(kMU0 / kEPS0); sa.m = h->pml_m; sa.lnR = h->pml_lnR;
+    int tot = 2 * h->Nx + 2 * h->Ny;
+    LAUNCH(sfactor_kernel, ceil_div(tot, 128), 128, 0, sa, h->sf);
+    StencilArgs a;
+    a.Nx = h->Nx; a.Ny = h->Ny; a.op = op;
+    a.idx = 1.0 / h->dx; a.idy = 1.0 / h->dy;
+    a.imu0 = 1.0 / (kMU0 * h->L0);
+    a.eps0n = kEPS0 * h->L0;
+    a.omega2 = omega_drv * omega_drv;
+    a.omega2mu0 = omega_drv * omega_drv * (kMU0 * h->L0);
+    a.sigma_re = sigma.real(); a.sigma_im = sigma.imag();
+    long long N = (long long)h->Nx * h->Ny;
+    LAUNCH(stencil_kernel, ceil_div(N, 256), 256, 0, a, h->eps, h->sf, h->st);
+    RET(check_launch(h, "assemble"));
+    // factorization scale: power of two nearest 1/Σ|off-diagonal| at the grid centre
+    long long kc = h->Nx / 2 + (long long)h->Nx * (h->Ny / 2);
+    cplx<double> c[5];
+    for (int p = 0; p < 5; ++p)
+        CK(cudaMemcpyAsync(&c[p], h->st + p * N + kc, sizeof(cplx<double>), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    double s = 0;
+    for (int p = 1; p < 5; ++p) s += std::hypot(c[p].re, c[p].im);
+    if (!(s > 0) || !std::isfinite(s)) return set_err(h, FDFD_EINVAL, "degenerate operator (zero couplings)");
+    h->scale = std::ldexp(1.0, -(int)std::lround(std::log2(s)));
+    h->op = op;
+    return FDFD_OK;
+}
+
+int factor_op(fdfd_handle* h) {
+    int rc = h->precision == FDFD_PREC_FP64 ? factor_impl<double>(h) : factor_impl<float>(h);
+    if (rc != FDFD_OK) return rc;
+    RET(check_device(h, "factor"));
+    h->factored = true;
+    return FDFD_OK;
+}
+
+double elapsed_ms(cudaEvent_t a, cudaEvent_t b) {
+    float ms = 0;
+    cudaEventElapsedTime(&ms, a, b);
+    return ms;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+const char* fdfd_version(void) { return FDFD_VERSION_STR; }
+
+const char* fdfd_last_error(const fdfd_handle* h) { return h ? h->err.c_str() : "null handle"; }
+
+int fdfd_create(fdfd_handle** out, int Nx, int Ny, int Npx, int Npy, double dx, double dy, double L0, double pml_m,
+                double pml_lnR, int pol, int precision) {
+    if (!out) return FDFD_EINVAL;
+    *out = nullptr;
+    if (Nx < 3 || Ny < 3 || Npx < 0 || Npy < 0 || 2 * Npx > Nx || 2 * Npy > Ny) return FDFD_EINVAL;
+    if (!(dx > 0) || !(dy > 0) || !(L0 > 0) || !std::isfinite(pml_m) || !std::isfinite(pml_lnR)) return FDFD_EINVAL;
+    if (pol != FDFD_TM && pol != FDFD_TE) return FDFD_EINVAL;
+    if (precision != FDFD_PREC_FP64 && precision != FDFD_PREC_MIXED) return FDFD_EINVAL;
+    if (std::min(Nx, Ny) > 2048) return FDFD_EINVAL;
+    fdfd_handle* h = new fdfd_handle();
+    h->Nx = Nx; h->Ny = Ny; h->Npx = Npx; h->Npy = Npy;
+    h->dx = dx; h->dy = dy; h->L0 = L0; h->pml_m = pml_m; h->pml_lnR = pml_lnR;
+    h->pol = pol; h->precision = precision;
+    const char* env = getenv("FDFD_DISABLE_TC");
+    if (env && env[0] == '1') h->use_tc = false;
+    NodeMap& m = h->map;
+    m.Nx = Nx; m.Ny = Ny;
+    m.transposed = Nx > Ny ? 1 : 0;
+    m.b = m.transposed ? Ny : Nx;
+    m.n = m.transposed ? Nx : Ny;
+    m.ld = (m.b + 31) / 32 * 32;
+    auto fail = [&](int rc) {
+        fdfd_destroy(h);
+        return rc;
+    };
+    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaGetLastError();
+        delete h;
+        return FDFD_ECUDA;
+    }
+    for (auto& e : h->ev) cudaEventCreate(&e);
+    long long N = (long long)Nx * Ny;
+    int rc;
+    if ((rc = dev_alloc(h, (void**)&h->eps, N * sizeof(cplx<double>)))) return fail(rc);
+    if ((rc = dev_alloc(h, (void**)&h->sf, 2 * (2 * Nx + 2 * Ny) * sizeof(cplx<double>)))) return fail(rc);
+    if ((rc = dev_alloc(h, (void**)&h->st, 5 * N * sizeof(cplx<double>)))) return fail(rc);
+    if ((rc = dev_alloc(h, (void**)&h->derr, sizeof(unsigned)))) return fail(rc);
+    cudaMemsetAsync(h->derr, 0, sizeof(unsigned), h->stream);
+    build_plan(h);
+    JobBlob B;
+    build_jobs(h, B);
+    if ((rc = dev_alloc(h, (void**)&h->djobs, B.host.size()))) return fail(rc);
+    if (cudaMemcpy(h->djobs, B.host.data(), B.host.size(), cudaMemcpyHostToDevice) != cudaSuccess) return fail(FDFD_ECUDA);
+    *out = h;
+    return FDFD_OK;
+}
+
+void fdfd_destroy(fdfd_handle* h) {
+    if (!h) return;
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    void* bufs[] = {h->eps, h->sf, h->st, h->derr, h->part, h->red, h->kb, h->kx, h->kr, h->kV, h->kZ, h->kc, h->io,
+                    h->djobs, h->f32.D.base, h->f32.C.base, h->f32.X.base, h->f32.GP.base, h->f32.RP.base,
+                    h->f32.rv, h->f32.xv, h->f32.wv, h->f32.perm, h->f64.D.base, h->f64.C.base, h->f64.X.base,
+                    h->f64.GP.base, h->f64.RP.base, h->f64.rv, h->f64.xv, h->f64.wv, h->f64.perm};
+    for (void* p : bufs) dev_free(p);
+    for (auto& e : h->ev) if (e) cudaEventDestroy(e);
+    for (auto& e : h->evpool) cudaEventDestroy(e);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+}
+
+int fdfd_set_refinement(fdfd_handle* h, double tol, int max_iter, int mode) {
+    if (!h) return FDFD_EINVAL;
+    if (!(tol > 0) || max_iter < 1 || (mode != FDFD_REFINE_GMRES && mode != FDFD_REFINE_CLASSIC))
+        return set_err(h, FDFD_EINVAL, "invalid refinement settings");
+    h->tol = tol; h->max_iter = max_iter; h->refine_mode = mode;
+    return FDFD_OK;
+}
+
+int fdfd_set_eps(fdfd_handle* h, const double* eps_r) {
+    if (!h || !eps_r) return h ? set_err(h, FDFD_EINVAL, "eps_r is NULL") : FDFD_EINVAL;
+    long long N = (long long)h->Nx * h->Ny;
+    for (long long k = 0; k < 2 * N; ++k)
+        if (!std::isfinite(eps_r[k])) return set_err(h, FDFD_EINVAL, "eps_r has a non-finite entry at %lld", k / 2);
+    for (long long k = 0; k < N; ++k)
+        if (eps_r[2 * k] == 0 && eps_r[2 * k + 1] == 0) return set_err(h, FDFD_EINVAL, "eps_r is zero at %lld", k);
+    CK(cudaMemcpyAsync(h->eps, eps_r, N * sizeof(cplx<double>), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    h->eps_set = true;
+    h->factored = false;
+    return FDFD_OK;
+}
+
+int fdfd_factor(fdfd_handle* h, double omega) {
+    if (!h) return FDFD_EINVAL;
+    if (!h->eps_set) return set_err(h, FDFD_EINVAL, "fdfd_set_eps must be called before fdfd_factor");
+    if (!(omega > 0) || !std::isfinite(omega)) return set_err(h, FDFD_EINVAL, "omega must be positive and finite");
+    h->launches = 0;
+    h->factored = false;
+    cudaEventRecord(h->ev[0], h->stream);
+    RET(assemble(h, h->pol == FDFD_TM ? OP_TM_DRIVEN : OP_TE_DRIVEN, omega, zd(0, 0), omega));
+    cudaEventRecord(h->ev[1], h->stream);
+    RET(factor_op(h));
+    cudaEventRecord(h->ev[2], h->stream);
+    h->omega = omega;
+    return FDFD_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// driven solve on device buffers: src (nrhs natural vectors) -> fields
+int solve_core(fdfd_handle* h, const cplx<double>* d_src, int nrhs, cplx<double>* f1, cplx<double>* f2,
+               cplx<double>* f3, fdfd_stats* st) {
+    if (!h->factored || (h->op != OP_TM_DRIVEN && h->op != OP_TE_DRIVEN))
+        return set_err(h, FDFD_EINVAL, "fdfd_factor must be called before the solve");
+    long long N = (long long)h->Nx * h->Ny;
+    RET(ensure_krylov(h, nrhs, 20));
+    cudaEventRecord(h->ev[3], h->stream);
+    // b = iω·src   (driven.jl:185,195)
+    std::vector<zd> iw(nrhs, zd(0, h->omega));
+    RET(scale_vec(h, d_src, iw, nrhs, h->kb));
+    int iters = 0;
+    double rel = 0;
+    RET(refine(h, nrhs, &iters, &rel));
+    cudaEventRecord(h->ev[4], h->stream);
+    RET(check_device(h, "solve"));
+    if (f1) CK(cudaMemcpyAsync(f1, h->kx, N * nrhs * sizeof(cplx<double>), cudaMemcpyDeviceToDevice, h->stream));
+    if (f2 || f3) {
+        // coefficients per rhs (driven.jl:189-190, 199-200)
+        std::vector<zd> coef(2 * nrhs);
+        const double w = h->omega, mu0 = kMU0 * h->L0;
+        for (int r = 0; r < nrhs; ++r) {
+            if (h->pol == FDFD_TM) {
+                coef[2 * r] = zd(-0.0, (1.0 / w) / mu0);      // -1/1im/ω/μ₀
+                coef[2 * r + 1] = zd(0.0, (-1.0 / w) / mu0);  //  1/1im/ω/μ₀
+            } else {
+                coef[2 * r] = zd(0.0, -1.0 / w);              //  1/1im/ω
+                coef[2 * r + 1] = coef[2 * r];
+            }
+        }
+        CK(cudaMemcpyAsync(h->kc, coef.data(), coef.size() * sizeof(zd), cudaMemcpyHostToDevice, h->stream));
+        RecoverArgs ra;
+        ra.Nx = h->Nx; ra.Ny = h->Ny; ra.mode = h->pol == FDFD_TM ? REC_TM_DRIVEN : REC_TE_DRIVEN;
+        ra.idx = 1.0 / h->dx; ra.idy = 1.0 / h->dy; ra.eps0n = kEPS0 * h->L0;
+        cplx<double>* g1 = f2 ? f2 : h->kr;
+        cplx<double>* g2 = f3 ? f3 : h->kr;
+        LAUNCH(recover_kernel, dim3(ceil_div(N, 256), nrhs), 256, 0, ra, h->sf, h->eps, h->kx, h->kc, g1, g2);
+        RET(check_launch(h, "recover"));
+    }
+    cudaEventRecord(h->ev[5], h->stream);
+    CK(cudaStreamSynchronize(h->stream));
+    if (st) {
+        st->iterations = iters;
+        st->nrhs = nrhs;
+        st->rel_residual = rel;
+        st->t_assemble_ms = elapsed_ms(h->ev[0], h->ev[1]);
+        st->t_factor_ms = elapsed_ms(h->ev[1], h->ev[2]);
+        st->t_solve_ms = elapsed_ms(h->ev[3], h->ev[4]);
+        st->t_recover_ms = elapsed_ms(h->ev[4], h->ev[5]);
+        st->factor_flops = h->last_factor_flops;
+        st->block = h->map.b;
+        st->nblocks = h->map.n;
+        st->levels = (int)h->steps.size() + 1;
+        st->tc_gemm = h->tc_used;
+        st->device_bytes = h->dev_bytes;
+        st->gpu_launches = h->launches;
+    }
+    if (!(rel <= h->tol))
+        return set_err(h, FDFD_ENOCONV, "refinement stopped at relative residual %.3e > tol %.1e after %d iterations",
+                       rel, h->tol, iters);
+    return FDFD_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fdfd_solve_device(fdfd_handle* h, const double* d_src, int nrhs, double* d_f1, double* d_f2, double* d_f3,
+                      fdfd_stats* stats) {
+    if (!h) return FDFD_EINVAL;
+    if (!d_src || nrhs < 1) return set_err(h, FDFD_EINVAL, "invalid source arguments");
+    auto t0 = std::chrono::steady_clock::now();
+    int rc = solve_core(h, (const cplx<double>*)d_src, nrhs, (cplx<double>*)d_f1, (cplx<double>*)d_f2,
+                        (cplx<double>*)d_f3, stats);
+    if (stats) stats->t_total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return rc;
+}
+
+int fdfd_solve(fdfd_handle* h, const double* src, int nrhs, double* f1, double* f2, double* f3, fdfd_stats* stats) {
+    if (!h) return FDFD_EINVAL;
+    if (!src || nrhs < 1) return set_err(h, FDFD_EINVAL, "invalid source arguments");
+    auto t0 = std::chrono::steady_clock::now();
+    long long N = (long long)h->Nx * h->Ny;
+    for (long long k = 0; k < 2 * N * nrhs; ++k)
+        if (!std::isfinite(src[k])) return set_err(h, FDFD_EINVAL, "src has a non-finite entry");
+    size_t bytes = (size_t)N * nrhs * sizeof(cplx<double>);
+    // staging: [src | f1 | f2 | f3], kept by the handle between calls
+    if (h->io_cap < 4 * bytes) {
+        dev_free(h->io);
+        h->io = nullptr;
+        h->dev_bytes -= (long long)h->io_cap;
+        h->io_cap = 0;
+        RET(dev_alloc(h, (void**)&h->io, 4 * bytes));
+        h->io_cap = 4 * bytes;
+    }
+    cplx<double>* io = h->io;
+    cplx<double>* dsrc = io;
+    cplx<double>* d1 = f1 ? io + N * nrhs : nullptr;
+    cplx<double>* d2 = f2 ? io + 2 * N * nrhs : nullptr;
+    cplx<double>* d3 = f3 ? io + 3 * N * nrhs : nullptr;
+    int rc = FDFD_OK;
+    if (cudaMemcpyAsync(dsrc, src, bytes, cudaMemcpyHostToDevice, h->stream) != cudaSuccess)
+        rc = set_err(h, FDFD_ECUDA, "copy of src failed");
+    if (rc == FDFD_OK) rc = solve_core(h, dsrc, nrhs, d1, d2, d3, stats);
+    if (rc == FDFD_OK || rc == FDFD_ENOCONV) {
+        if (f1) cudaMemcpyAsync(f1, d1, bytes, cudaMemcpyDeviceToHost, h->stream);
+        if (f2) cudaMemcpyAsync(f2, d2, bytes, cudaMemcpyDeviceToHost, h->stream);
+        if (f3) cudaMemcpyAsync(f3, d3, bytes, cudaMemcpyDeviceToHost, h->stream);
+        if (cudaStreamSynchronize(h->stream) != cudaSuccess) rc = set_err(h, FDFD_ECUDA, "copy of fields failed");
+    }
+    if (stats) stats->t_total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return rc;
+}
+
+int fdfd_set_profiling(fdfd_handle* h, int on) {
+    if (!h) return FDFD_EINVAL;
+    prof_collect(h);
+    h->prof_on = on != 0;
+    memset(&h->prof_tot, 0, sizeof h->prof_tot);
+    return FDFD_OK;
+}
+
+int fdfd_get_profile(fdfd_handle* h, fdfd_profile* out) {
+    if (!h || !out) return FDFD_EINVAL;
+    prof_collect(h);
+    *out = h->prof_tot;
+    return FDFD_OK;
+}
+
+int fdfd_get_stencil(fdfd_handle* h, double* out) {
+    if (!h || !out) return FDFD_EINVAL;
+    if (!h->factored) return set_err(h, FDFD_EINVAL, "no assembled operator");
+    long long N = (long long)h->Nx * h->Ny;
+    CK(cudaMemcpyAsync(out, h->st, 5 * N * sizeof(cplx<double>), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return FDFD_OK;
+}
+
+int fdfd_apply(fdfd_handle* h, const double* x, int nrhs, double* y) {
+    if (!h || !x || !y || nrhs < 1) return FDFD_EINVAL;
+    if (!h->factored) return set_err(h, FDFD_EINVAL, "no assembled operator");
+    long long N = (long long)h->Nx * h->Ny;
+    size_t bytes = (size_t)N * nrhs * sizeof(cplx<double>);
+    cplx<double>* buf = nullptr;
+    RET(dev_alloc(h, (void**)&buf, 2 * bytes));
+    int rc = FDFD_OK;
+    if (cudaMemcpyAsync(buf, x, bytes, cudaMemcpyHostToDevice, h->stream) != cudaSuccess) rc = FDFD_ECUDA;
+    if (rc == FDFD_OK) rc = residual(h, buf, nullptr, buf + N * nrhs, nrhs, nullptr);
+    if (rc == FDFD_OK && cudaMemcpyAsync(y, buf + N * nrhs, bytes, cudaMemcpyDeviceToHost, h->stream) != cudaSuccess)
+        rc = FDFD_ECUDA;
+    cudaStreamSynchronize(h->stream);
+    cudaFree(buf);
+    h->dev_bytes -= 2 * (long long)bytes;
+    return rc == FDFD_ECUDA ? set_err(h, rc, "fdfd_apply copy failed") : rc;
+}
+
+int fdfd_adjoint(fdfd_handle* h, const double* src, const double* mvec, double* J, double* grad, double* ez,
+                 fdfd_stats* stats) {
+    (void)src; (void)mvec; (void)J; (void)grad; (void)ez; (void)stats;
+    return h ? set_err(h, FDFD_EINVAL, "fdfd_adjoint: not available in this build") : FDFD_EINVAL;
+}
+
+int fdfd_eigfreq(fdfd_handle* h, double omega0, int nev, int which, double tol, double* omega, double* lambda,
+                 double* fields, fdfd_stats* stats) {
+    (void)omega0; (void)nev; (void)which; (void)tol; (void)omega; (void)lambda; (void)fields; (void)stats;
+    return h ? set_err(h, FDFD_EINVAL, "fdfd_eigfreq: not available in this build") : FDFD_EINVAL;
+}
+
+}  // extern "C"
+
+namespace {
+
+template <typename T>
+int debug_gemm_impl(int M, int N, int K, const double* A, const double* B, double* C, int use_tc, double* ms) {
+    const int planes = sizeof(T) == 4 ? 4 : 2;
+    Pool<T> PA, PB, PC;
+    auto setp = [&](Pool<T>& P, int rows, int cols) {
+        P.rows = rows; P.cols = cols; P.ld = (cols + 31) / 32 * 32; P.planes = planes; P.count = 1;
+    };
+    setp(PA, M, K); setp(PB, N, K); setp(PC, M, N);
+    auto upload = [&](Pool<T>& P, const double* src) -> int {
+        std::vector<T> host((size_t)P.slot_elems(), (T)0);
+        long long pe = P.plane_elems();
+        for (int r = 0; r < P.rows; ++r)
+            for (int c = 0; c < P.cols; ++c) {
+                double re = src[2 * ((size_t)r * P.cols + c)], im = src[2 * ((size_t)r * P.cols + c) + 1];
+                size_t o = (size_t)r * P.ld + c;
+                host[o] = (T)re;
+                host[pe + o] = (T)im;
+                if (planes == 4) {
+                    float fr = (float)re, fi = (float)im;
+                    uint32_t ur, ui;
+                    memcpy(&ur, &fr, 4); memcpy(&ui, &fi, 4);
+                    ur &= 0xffffe000u; ui &= 0xffffe000u;
+                    float hr, hi;
+                    memcpy(&hr, &ur, 4); memcpy(&hi, &ui, 4);
+                    host[2 * pe + o] = (T)(fr - hr);
+                    host[3 * pe + o] = (T)(fi - hi);
+                }
+            }
+        if (cudaMalloc(&P.base, host.size() * sizeof(T)) != cudaSuccess) return FDFD_ENOMEM;
+        if (cudaMemcpy(P.base, host.data(), host.size() * sizeof(T), cudaMemcpyHostToDevice) != cudaSuccess)
+            return FDFD_ECUDA;
+        return FDFD_OK;
+    };
+    int rc = upload(PA, A);
+    if (rc == FDFD_OK) rc = upload(PB, B);
+    std::vector<double> zeros((size_t)2 * M * N, 0.0);
+    if (rc == FDFD_OK) rc = upload(PC, zeros.data());
+    int* slots = nullptr;
+    unsigned* derr = nullptr;
+    if (rc == FDFD_OK && cudaMalloc(&slots, sizeof(int)) != cudaSuccess) rc = FDFD_ENOMEM;
+    if (rc == FDFD_OK && cudaMalloc(&derr, sizeof(unsigned)) != cudaSuccess) rc = FDFD_ENOMEM;
+    if (rc == FDFD_OK) {
+        cudaMemset(slots, 0, sizeof(int));
+        cudaMemset(derr, 0, sizeof(unsigned));
+    }
+    if (rc == FDFD_OK) {
+        GemmArgs<T> g;
+        g.A = PA; g.B = PB; g.C = PC;
+        g.a_slot = g.b_slot = g.c_slot = slots;
+        g.M = M; g.N = N; g.K = K; g.alpha = (T)1; g.beta = 0; g.mask_c0 = 0; g.mask_w = 0;
+        g.c_trans = 0; g.c_trans_arr = nullptr; g.err = derr;
+        cudaEvent_t e0, e1;
+        cudaEventCreate(&e0); cudaEventCreate(&e1);
+        if (sizeof(T) == 4 && use_tc) {
+            CUtensorMap ma[2], mb[2];
+            const Pool<float>* fa = reinterpret_cast<const Pool<float>*>(&PA);
+            const Pool<float>* fb = reinterpret_cast<const Pool<float>*>(&PB);
+            if (!tc_make_map(*fa, &ma[0], &ma[1]) || !tc_make_map(*fb, &mb[0], &mb[1])) rc = FDFD_ECUDA;
+            if (rc == FDFD_OK) {
+                cudaEventRecord(e0);
+                if (tc_gemm_launch_maps(reinterpret_cast<GemmArgs<float>*>(&g), nullptr, &ma[0], &mb[1], 1, 0) != 0)
+                    rc = FDFD_ECUDA;
+                cudaEventRecord(e1);
+            }
+        } else {
+            cudaEventRecord(e0);
+            launch_gemm_simt<T>(0, 1, g);
+            cudaEventRecord(e1);
+        }
+        if (cudaDeviceSynchronize() != cudaSuccess) rc = FDFD_ECUDA;
+        float t = 0;
+        cudaEventElapsedTime(&t, e0, e1);
+        if (ms) *ms = t;
+        cudaEventDestroy(e0); cudaEventDestroy(e1);
+        unsigned e = 0;
+        cudaMemcpy(&e, derr, sizeof e, cudaMemcpyDeviceToHost);
+        if (rc == FDFD_OK && e) rc = (e & FDFD_DEVERR_TIMEOUT) ? FDFD_ETIMEOUT : FDFD_ECUDA;
+    }
+    if (rc == FDFD_OK) {
+        std::vector<T> host((size_t)PC.slot_elems());
+        cudaMemcpy(host.data(), PC.base, host.size() * sizeof(T), cudaMemcpyDeviceToHost);
+        long long pe = PC.plane_elems();
+        for (int r = 0; r < M; ++r)
+            for (int c = 0; c < N; ++c) {
+                C[2 * ((size_t)r * N + c)] = host[(size_t)r * PC.ld + c];
+                C[2 * ((size_t)r * N + c) + 1] = host[pe + (size_t)r * PC.ld + c];
+            }
+    }
+    cudaFree(PA.base); cudaFree(PB.base); cudaFree(PC.base); cudaFree(slots); cudaFree(derr);
+    return rc;
+}
+
+}  // namespace
+
+extern "C" {
+
+// Test entry point: C = A·Bᵀ (complex, A: M x K, B: N x K, C: M x N, row-major
+// interleaved host arrays) through the library's GEMM kernels: precision
+// FDFD_PREC_FP64 (SIMT FP64) or FDFD_PREC_MIXED (FP32 storage; use_tc selects
+// the tcgen05 3xTF32 kernel or the SIMT FP32 kernel).  *ms receives the kernel
+// time.  No counterpart in the reference.
+int fdfd_debug_gemm(int M, int N, int K, const double* A, const double* B, double* C, int precision, int use_tc,
+                    double* ms) {
+    if (M < 1 || N < 1 || K < 1 || !A || !B || !C) return FDFD_EINVAL;
+    if (precision == FDFD_PREC_FP64) return debug_gemm_impl<double>(M, N, K, A, B, C, 0, ms);
+    return debug_gemm_impl<float>(M, N, K, A, B, C, use_tc, ms);
+}
+
+}  // extern "C"

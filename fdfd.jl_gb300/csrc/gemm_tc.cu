@@ -1,0 +1,375 @@
+// Batched complex TN GEMM on the sm_103a tensor cores: tcgen05.mma kind::tf32
+// with 3xTF32 split precision, TMA-staged operands, accumulators in TMEM.
+//
+//   C[m][n] = beta(m,n)·C[m][n] + alpha·Σ_k A[m][k]·B[n][k]      (complex)
+//
+// Operands are FP32 planar pools whose slots hold four planes: re, im and
+// their TF32 residuals lo = x - (x with the low 13 mantissa bits cleared).
+// The tensor core reads only the top 19 bits of an FP32 operand, so the raw
+// plane serves as the "hi" term and
+//   a·b ≈ hi(a)·hi(b) + hi(a)·lo(b) + lo(a)·hi(b)
+// recovers close to FP32 accuracy (the split of Markidis et al., 2018, as used
+// for 3xTF32 GEMMs).  Each complex product is four real products (the im·im
+// term through the instruction's negate-A bit), so one K-step issues 12 MMAs
+// into two TMEM accumulators (real and imaginary, 256 columns each).
+//
+// CTA tile 128 x 256 (complex outputs), K-step 8 (one 32-byte swizzle row per
+// operand row), 4-stage TMA pipeline, 192 threads:
+//   warp 0      TMA producer (one elected lane)
+//   warp 1      TMEM allocator and MMA issuer (one elected lane)
+//   warps 2..5  epilogue: tcgen05.ld -> registers -> global (N- or T-form)
+// Every mbarrier wait is bounded (2 s of %globaltimer); on timeout the CTA sets
+// FDFD_DEVERR_TIMEOUT, drains its own TMA copies (bounded), frees TMEM and exits.
+#include "gemm_tc.cuh"
+
+namespace {
+
+constexpr int BM = 128, BN = 256, BK = 8, STAGES = 4;
+constexpr int A_PLANE_BYTES = BM * BK * 4;                  // 4 KB
+constexpr int B_PLANE_BYTES = BN * BK * 4;                  // 8 KB
+constexpr int STAGE_BYTES = 4 * A_PLANE_BYTES + 4 * B_PLANE_BYTES;   // 48 KB
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024;     // + alignment slack
+constexpr uint32_t TMEM_COLS = 512;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// bounded wait: false after FDFD_WAIT_LIMIT_NS
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+    if (mbar_try(bar, parity)) return true;
+    uint64_t t0 = globaltimer_ns();
+    while (true) {
+        if (mbar_try(bar, parity)) return true;
+        if (globaltimer_ns() - t0 > FDFD_WAIT_LIMIT_NS) return false;
+        __nanosleep(64);
+    }
+}
+
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map, int c0, int c1, int c2,
+                                            uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(bar)
+        : "memory");
+}
+
+// tcgen05 shared-memory matrix descriptor, K-major, 32-byte swizzle:
+// start address >> 4 (bits 0-13), leading byte offset >> 4 (16-29, unused for
+// swizzled K-major), stride byte offset >> 4 (32-45: 8 rows x 32 B = 256 B
+// between 8-row groups), descriptor version 1 (bits 46-47), swizzle mode
+// 6 = 32-byte (bits 61-63).
+__device__ __forceinline__ uint64_t sdesc_sw32(uint32_t saddr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFF);
+    d |= (uint64_t)1 << 16;
+    d |= (uint64_t)(256 >> 4) << 32;
+    d |= (uint64_t)1 << 46;
+    d |= (uint64_t)6 << 61;
+    return d;
+}
+
+// instruction descriptor, kind::tf32: D=F32 (bits 4-5 = 1), A=B=TF32 (bits 7-9,
+// 10-12 = 2), negate A (bit 13), both K-major (bits 15,16 = 0), N>>3 (17-22),
+// M>>4 (24-28).
+__host__ __device__ constexpr uint32_t idesc_tf32(int M, int N, int negA) {
+    return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)negA << 13) | ((uint32_t)(N >> 3) << 17) |
+           ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_tf32(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accum) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(dtmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accum));
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+                 : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&v)[32]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+        "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+        "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+          "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]),
+          "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]),
+          "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+        : "r"(taddr));
+}
+
+struct TcParams {
+    GemmArgs<float> g;
+};
+
+__global__ void __launch_bounds__(192, 1)
+    gemm_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
+                   const TcParams P) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    __shared__ __align__(8) uint64_t bar_full[STAGES], bar_empty[STAGES], bar_acc;
+    __shared__ uint32_t tmem_base_slot;
+    __shared__ int s_abort;
+
+    const GemmArgs<float>& g = P.g;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int job = blockIdx.z;
+    const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+    const int nk = (g.K + BK - 1) / BK;
+    unsigned char* smem = reinterpret_cast<unsigned char*>(
+        (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+    const uint32_t sbase = smem_u32(smem);
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < STAGES; ++s) {
+            mbar_init(smem_u32(&bar_full[s]), 1);
+            mbar_init(smem_u32(&bar_empty[s]), 1);
+        }
+        mbar_init(smem_u32(&bar_acc), 1);
+        s_abort = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         smem_u32(&tmem_base_slot)),
+                     "r"(TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = tmem_base_slot;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            const int aslot = g.a_slot[job], bslot = g.b_slot[job];
+            int issued = 0;
+            bool ok = true;
+            for (int kt = 0; kt < nk; ++kt) {
+                const int s = kt % STAGES;
+                if (kt >= STAGES) {
+                    if (!mbar_wait(smem_u32(&bar_empty[s]), ((kt / STAGES) - 1) & 1)) { ok = false; break; }
+                }
+                const uint32_t bar = smem_u32(&bar_full[s]);
+                mbar_expect_tx(bar, STAGE_BYTES);
+                const uint32_t st = sbase + s * STAGE_BYTES;
+                const int k0 = kt * BK;
+                for (int p = 0; p < 4; ++p)
+                    tma_load_3d(st + p * A_PLANE_BYTES, &mapA, k0, m0, aslot * 4 + p, bar);
+                for (int p = 0; p < 4; ++p)
+                    tma_load_3d(st + 4 * A_PLANE_BYTES + p * B_PLANE_BYTES, &mapB, k0, n0, bslot * 4 + p, bar);
+                issued = kt + 1;
+            }
+            if (!ok) {
+                dev_error(g.err, FDFD_DEVERR_TIMEOUT);
+                atomicExch(&s_abort, 1);
+            }
+            // drain this CTA's copies in flight (bounded)
+            for (int kt = (issued > STAGES ? issued - STAGES : 0); kt < issued; ++kt)
+                if (!mbar_wait(smem_u32(&bar_full[kt % STAGES]), (kt / STAGES) & 1)) {
+                    dev_error(g.err, FDFD_DEVERR_TIMEOUT);
+                    break;
+                }
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            bool ok = true;
+            const uint32_t acc_re = tmem, acc_im = tmem + 256;
+            const uint32_t id_pos = idesc_tf32(BM, BN, 0), id_neg = idesc_tf32(BM, BN, 1);
+            for (int kt = 0; kt < nk; ++kt) {
+                const int s = kt % STAGES;
+                if (!mbar_wait(smem_u32(&bar_full[s]), (kt / STAGES) & 1)) { ok = false; break; }
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t st = sbase + s * STAGE_BYTES;
+                uint64_t a[4], b[4];
+                for (int p = 0; p < 4; ++p) {
+                    a[p] = sdesc_sw32(st + p * A_PLANE_BYTES);
+                    b[p] = sdesc_sw32(st + 4 * A_PLANE_BYTES + p * B_PLANE_BYTES);
+                }
+                const uint32_t first = (kt > 0) ? 1u : 0u;
+                // planes: 0 re, 1 im, 2 re_lo, 3 im_lo
+                mma_tf32(acc_re, a[0], b[0], id_pos, first);   // re·re
+                mma_tf32(acc_re, a[0], b[2], id_pos, 1);
+                mma_tf32(acc_re, a[2], b[0], id_pos, 1);
+                mma_tf32(acc_re, a[1], b[1], id_neg, 1);       // -im·im
+                mma_tf32(acc_re, a[1], b[3], id_neg, 1);
+                mma_tf32(acc_re, a[3], b[1], id_neg, 1);
+                mma_tf32(acc_im, a[0], b[1], id_pos, first);   // re·im
+                mma_tf32(acc_im, a[0], b[3], id_pos, 1);
+                mma_tf32(acc_im, a[2], b[1], id_pos, 1);
+                mma_tf32(acc_im, a[1], b[0], id_pos, 1);       // im·re
+                mma_tf32(acc_im, a[1], b[2], id_pos, 1);
+                mma_tf32(acc_im, a[3], b[0], id_pos, 1);
+                mma_commit(smem_u32(&bar_empty[s]));
+            }
+            if (!ok) {
+                dev_error(g.err, FDFD_DEVERR_TIMEOUT);
+                atomicExch(&s_abort, 1);
+            }
+            mma_commit(smem_u32(&bar_acc));
+        }
+    } else {
+        // epilogue warps 2..5; TMEM lane quarter = warp % 4
+        const int q = warp & 3;
+        const bool ok_l = mbar_wait(smem_u32(&bar_acc), 0);
+        const bool ok = __all_sync(0xffffffffu, ok_l);
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const int abort = __shfl_sync(0xffffffffu, *(volatile int*)&s_abort, 0);
+        if (!ok) {
+            if (lane == 0) dev_error(g.err, FDFD_DEVERR_TIMEOUT);
+        } else if (!abort) {
+            const int row0 = m0 + q * 32;
+            const int row = row0 + lane;
+            const int ctr = g.c_trans_arr ? g.c_trans_arr[job] : g.c_trans;
+            float* C = g.C.slot(g.c_slot[job]);
+            const long long pe = g.C.plane_elems();
+            const long long ld = g.C.ld;
+            const uint32_t lane_off = (uint32_t)(q * 32) << 16;
+            // per-warp staging tile (the pipeline buffers are idle once the accumulator is final)
+            float* stg = reinterpret_cast<float*>(smem) + q * (2 * 32 * 33);
+            for (int ch = 0; ch < BN / 32; ++ch) {
+                const int nb = n0 + ch * 32;
+                if (nb >= g.N) break;
+                uint32_t vr[32], vi[32];
+                tmem_ld32(tmem + lane_off + ch * 32, vr);
+                tmem_ld32(tmem + lane_off + 256 + ch * 32, vi);
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                if (ctr) {
+                    // transposed store: lanes (rows) are contiguous in Cᵀ -> coalesced per column
+                    if (row < g.M) {
+#pragma unroll
+                        for (int j = 0; j < 32; ++j) {
+                            const int n = nb + j;
+                            if (n >= g.N) break;
+                            const float xr = g.alpha * __uint_as_float(vr[j]);
+                            const float xi = g.alpha * __uint_as_float(vi[j]);
+                            const long long off = (long long)n * ld + row;
+                            C[off] = xr;
+                            C[pe + off] = xi;
+                            C[2 * pe + off] = tf32_lo(xr);
+                            C[3 * pe + off] = tf32_lo(xi);
+                        }
+                    }
+                } else {
+                    // row-major store through shared memory: one 128-byte row segment per instruction
+#pragma unroll
+                    for (int j = 0; j < 32; ++j) {
+                        stg[lane * 33 + j] = __uint_as_float(vr[j]);
+                        stg[32 * 33 + lane * 33 + j] = __uint_as_float(vi[j]);
+                    }
+                    __syncwarp();
+                    const int n = nb + lane;
+                    const bool mcol = (n >= g.mask_c0 && n < g.mask_c0 + g.mask_w);
+                    for (int rr = 0; rr < 32; ++rr) {
+                        const int r = row0 + rr;
+                        if (r >= g.M) break;
+                        if (n < g.N) {
+                            float xr = g.alpha * stg[rr * 33 + lane];
+                            float xi = g.alpha * stg[32 * 33 + rr * 33 + lane];
+                            const bool masked = mcol || (r >= g.mask_c0 && r < g.mask_c0 + g.mask_w);
+                            const long long off = (long long)r * ld + n;
+                            if (g.beta && !masked) { xr += C[off]; xi += C[pe + off]; }
+                            C[off] = xr;
+                            C[pe + off] = xi;
+                            C[2 * pe + off] = tf32_lo(xr);
+                            C[3 * pe + off] = tf32_lo(xi);
+                        }
+                    }
+                    __syncwarp();
+                }
+            }
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    }
+    __syncthreads();
+    if (warp == 1) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS)
+                     : "memory");
+    }
+}
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn get_encode() {
+    static EncodeTiledFn fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (EncodeTiledFn)p;
+        else
+            cudaGetLastError();
+    }
+    return fn;
+}
+
+bool encode_pool(const Pool<float>& P, int box_rows, CUtensorMap* out) {
+    EncodeTiledFn enc = get_encode();
+    if (!enc || !P.base) return false;
+    cuuint64_t dims[3] = {(cuuint64_t)P.cols, (cuuint64_t)P.rows, (cuuint64_t)(P.count * P.planes)};
+    cuuint64_t strides[2] = {(cuuint64_t)P.ld * 4, (cuuint64_t)P.rows * P.ld * 4};
+    cuuint32_t box[3] = {(cuuint32_t)BK, (cuuint32_t)box_rows, 1};
+    cuuint32_t estr[3] = {1, 1, 1};
+    CUresult r = enc(out, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, (void*)P.base, dims, strides, box, estr,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_32B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS;
+}
+
+}  // namespace
+
+bool tc_make_map(const Pool<float>& P, CUtensorMap* box128, CUtensorMap* box256) {
+    if (P.planes != 4 || (P.ld % 4) != 0) return false;
+    return encode_pool(P, BM, box128) && encode_pool(P, BN, box256);
+}
+
+bool tc_make_maps(const Pool<float>* D, const Pool<float>* C, const Pool<float>* X, const Pool<float>* GP,
+                  const Pool<float>* RP, TcMaps* out) {
+    const Pool<float>* pools[5] = {D, C, X, GP, RP};
+    for (int i = 0; i < 5; ++i)
+        if (!tc_make_map(*pools[i], &out->map[i][0], &out->map[i][1])) return false;
+    return true;
+}
+
+int tc_gemm_launch_maps(const GemmArgs<float>* g, const int* c_trans_arr, const CUtensorMap* mapA,
+                        const CUtensorMap* mapB, int njobs, cudaStream_t stream) {
+    static bool attr = false;
+    if (!attr) {
+        cudaError_t e = cudaFuncSetAttribute(gemm_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+        if (e != cudaSuccess) return (int)e;
+        attr = true;
+    }
+    TcParams P;
+    P.g = *g;
+    if (c_trans_arr) P.g.c_trans_arr = c_trans_arr;
+    dim3 grid((g->N + BN - 1) / BN, (g->M + BM - 1) / BM, njobs);
+    gemm_tc_kernel<<<grid, 192, SMEM_BYTES, stream>>>(*mapA, *mapB, P);
+    return (int)cudaGetLastError();
+}

@@ -1,0 +1,120 @@
+// Kernel argument structs and declarations shared by the library's .cu files.
+#pragma once
+#include "common.cuh"
+
+enum { OP_TM_DRIVEN = 0, OP_TE_DRIVEN = 1, OP_TM_EIGEN = 2, OP_TE_EIGEN = 3 };
+enum { REC_TM_DRIVEN = 0, REC_TE_DRIVEN = 1, REC_TM_EIGEN = 2, REC_TE_EIGEN = 3 };
+
+struct SFactorArgs { int Nx, Ny, Npx, Npy; double dx, dy, omega, eps0n, eta0, m, lnR; };
+struct StencilArgs { int Nx, Ny, op; double idx, idy, imu0, eps0n, omega2, omega2mu0, sigma_re, sigma_im; };
+struct RecoverArgs { int Nx, Ny, mode; double idx, idy, eps0n; };
+
+// Mapping between natural unknowns and (node, in-block index).
+struct NodeMap {
+    int Nx, Ny;
+    int b, n, ld;        // block size, block count, vector/matrix leading dimension
+    int transposed;      // 0: node = iy, i = ix (b = Nx); 1: node = ix, i = iy (b = Ny)
+    __host__ __device__ long long nat(int node, int i) const {
+        return transposed ? (long long)node + (long long)Nx * i : (long long)i + (long long)Nx * node;
+    }
+    // stencil planes [self, x-1, x+1, y-1, y+1]: in-line prev/next and coupling prev/next
+    __host__ __device__ int p_inprev() const { return transposed ? 3 : 1; }
+    __host__ __device__ int p_innext() const { return transposed ? 4 : 2; }
+    __host__ __device__ int p_cprev() const { return transposed ? 1 : 3; }
+    __host__ __device__ int p_cnext() const { return transposed ? 2 : 4; }
+};
+
+// ---- assemble.cu -----------------------------------------------------------
+__global__ void sfactor_kernel(SFactorArgs a, cplx<double>* out);
+__global__ void stencil_kernel(StencilArgs a, const cplx<double>* eps, const cplx<double>* sf, cplx<double>* st);
+__global__ void residual_kernel(int Nx, int Ny, int nrhs, const cplx<double>* st, const cplx<double>* x,
+                                const cplx<double>* b, cplx<double>* r, double* part);
+__global__ void reduce_partials_kernel(const double* part, int nblocks, int nvals, double* out);
+__global__ void recover_kernel(RecoverArgs a, const cplx<double>* sf, const cplx<double>* eps,
+                               const cplx<double>* f, const cplx<double>* coef, cplx<double>* g1,
+                               cplx<double>* g2);
+template <typename T>
+void launch_to_nodes(dim3 grid, cudaStream_t s, NodeMap m, int nrhs, const cplx<double>* in, double scale, T* out);
+template <typename T>
+void launch_from_nodes(dim3 grid, cudaStream_t s, NodeMap m, int nrhs, const T* in, double scale, int accumulate,
+                       cplx<double>* out);
+__global__ void vscale_kernel(long long N, const cplx<double>* x, const cplx<double>* s, cplx<double>* y);
+__global__ void vcombine_kernel(long long N, int nvec, const cplx<double>* V, long long vstride,
+                                const cplx<double>* c, int ldc, double sign, cplx<double>* y);
+__global__ void vdots_kernel(long long N, int nvec, const cplx<double>* V, long long vstride,
+                             const cplx<double>* w, double* part);
+__global__ void pscale_kernel(int Nx, int Ny, const cplx<double>* sf, int mode, const cplx<double>* in,
+                              cplx<double>* out);
+__global__ void adjoint_grad_kernel(long long N, cplx<double> coef, const cplx<double>* lam,
+                                    const cplx<double>* E, double* grad);
+__global__ void vdotu_kernel(long long N, const cplx<double>* m, const cplx<double>* E, double* part);
+
+// ---- blocks.cu ----------------------------------------------------------------
+struct L1Job {                 // survivor of the first reduction step
+    int s, prev, next;         // node and its ring neighbours
+    int prev_elim, next_elim;  // neighbour eliminated in this step
+    int u_slot, l_slot;        // coupling-pool slots of the new U, L
+    int u_trans, l_trans;      // store transposed (node eliminated next step)
+};
+
+// Host launchers (each kernel template is instantiated in its own translation unit).
+template <typename T>
+void launch_build_tridiag(cudaStream_t s, int njobs, NodeMap m, const cplx<double>* st, double scale, Pool<T> D,
+                          const int* nodes);
+template <typename T>
+void launch_level1_combine(cudaStream_t s, int njobs, NodeMap m, const cplx<double>* st, double scale, Pool<T> D,
+                           Pool<T> C, const L1Job* jobs);
+void launch_perm_init(cudaStream_t s, int njobs, int* perm, int b);
+// Gauss-Jordan panel step with panel width nb (returns a cudaError_t value)
+template <typename T>
+int launch_gj_panel(cudaStream_t s, int nb, int njobs, Pool<T> M, const int* slots, Pool<T> GP, Pool<T> RP,
+                    int* perm, int c0, unsigned* err);
+template <typename T>
+void launch_gj_unpermute(cudaStream_t s, int njobs, Pool<T> M, const int* slots, const int* perm);
+// C[dst] = A[s1] + A[s2] (same storage form); also writes lo planes
+template <typename T>
+void launch_madd(cudaStream_t s, int njobs, Pool<T> P, const int3* jobs);
+// dst = src (optionally transposed) between pools; writes lo planes
+template <typename T>
+void launch_mcopy(cudaStream_t s, int njobs, Pool<T> S, Pool<T> Dp, const int3* jobs);
+
+// ---- gemm_simt.cu / gemm_tc.cu --------------------------------------------
+// Batched complex "TN" GEMM on planar pools:
+//   C[m][n] = beta(m,n)·C[m][n] + alpha·Σ_k A[m][k]·B[n][k]
+// with A, B, C row-major slots; beta(m,n) = beta unless m or n lies in
+// [mask_c0, mask_c0 + mask_w), where it is 0; c_trans stores Cᵀ instead.
+template <typename T> struct GemmArgs {
+    Pool<T> A, B, C;
+    const int* a_slot; const int* b_slot; const int* c_slot;
+    int M, N, K;
+    T alpha; int beta;
+    int mask_c0, mask_w;
+    int c_trans;
+    const int* c_trans_arr;   // per-job override of c_trans (device, may be null)
+    unsigned* err;
+};
+template <typename T>
+void launch_gemm_simt(cudaStream_t s, int njobs, const GemmArgs<T>& g);
+
+// ---- sweep.cu -------------------------------------------------------------------
+// y[job] = y0[job] + alpha·(op(M1)·v1 + op(M2)·v2) on node-planar vectors,
+// op = identity (N-form storage) or the stored transpose (T-form storage).
+template <typename T> struct GemvArgs {
+    Pool<T> P1, P2;
+    const T* V1; const T* V2;
+    const T* Y0; T* Y;
+    const int4* jobs;   // (m1_slot, v1_node, m2_slot, v2_node), -1 = absent
+    const int2* yjobs;  // (y_node, y0_node), y0_node -1 = zero
+    int b, ld, nrhs;    // nrhs: right-hand sides handled by this launch (<= 8)
+    int rtot, r0;       // right-hand sides stored per node, first one handled
+    T alpha;
+};
+// TR = 1: matrices stored transposed.  Returns a cudaError_t value.
+template <typename T>
+int launch_gemv(cudaStream_t s, int tr, int njobs, const GemvArgs<T>& g);
+// r[s] -= u_s ⊙ z[next] + l_s ⊙ z[prev]  (first reduction step, diagonal couplings)
+// mode 0: survivors update r from eliminated neighbours (jobs: L1Job-like int4 (s, prev, next, flags))
+// mode 1: eliminated k: w[k] = l_k ⊙ x[prev] + u_k ⊙ x[next]
+template <typename T>
+void launch_diag_sweep(cudaStream_t s, int njobs, NodeMap m, const cplx<double>* st, double scale, int nrhs,
+                       const int4* jobs, int mode, const T* src, T* dst);

@@ -1,0 +1,177 @@
+/*
+ * libfdfd_cuda — GB300 (sm_103a) solve path for 2-D FDFD problems.
+ *
+ * C ABI for the drop-in replacement of the FDFD.jl solve path.  The reference
+ * has no FFI; its backend seam is `dolinearsolve(A, b, sym)`
+ * (src/solver/solver.jl:4-41), which sees only a CSC matrix.  This library
+ * sits one level up and replaces, per frequency, the assembly, the linear
+ * solve and the field recovery of
+ *   solve(d::Device, pol)                       src/solver/driven.jl:153-208
+ *   eigenfrequency(d, pol, nev; which)          src/solver/eigen.jl:318-364
+ * so that Julia's `solve`/`eigenfrequency` can `ccall` it when
+ * ENV["FDFD_SOLVER"] == "cuda".
+ *
+ * Array conventions (all entry points): complex arrays are interleaved
+ * {re, im} doubles (Julia ComplexF64 / C `double _Complex`), Nx*Ny values per
+ * field, x fastest (Julia column-major `A[:]`, driven.jl:170).  Host arrays
+ * belong to the caller and are only read/written during the call.  Every call
+ * blocks until its results are in the caller's arrays.  A handle is used by one
+ * thread at a time; distinct handles are independent.
+ *
+ * Status codes: every entry point returns FDFD_OK or one of the errors below
+ * and leaves a message retrievable with fdfd_last_error().
+ */
+#ifndef FDFD_CUDA_H
+#define FDFD_CUDA_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FDFD_OK         0
+#define FDFD_EINVAL     1  /* bad argument (sizes, NaN/Inf input, call order) */
+#define FDFD_ENOMEM     2  /* device or pinned-host allocation failed        */
+#define FDFD_ESINGULAR  3  /* zero or non-finite pivot in a block inversion   */
+#define FDFD_ENOCONV    4  /* refinement hit its iteration cap above tol      */
+#define FDFD_ETIMEOUT   5  /* a bounded device-side wait gave up              */
+#define FDFD_ECUDA      6  /* CUDA runtime/driver error                       */
+
+#define FDFD_TM 1          /* src/types.jl:20 (@enum Polarization TM=1 TE=2) */
+#define FDFD_TE 2
+
+#define FDFD_PREC_FP64  0  /* complex FP64 factorization and sweeps          */
+#define FDFD_PREC_MIXED 1  /* complex FP32 storage, 3xTF32 tcgen05 products,
+                              FP64 residual and refinement                   */
+
+#define FDFD_REFINE_GMRES   0  /* flexible GMRES in FP64, factor as preconditioner */
+#define FDFD_REFINE_CLASSIC 1  /* x += M^-1 (b - A x)                              */
+
+#define FDFD_WHICH_LM 0    /* eigenvalues of A nearest sigma (ARPACK :LM in shift-invert) */
+
+typedef struct fdfd_handle fdfd_handle;
+
+/* Per-call statistics, filled by the solve/adjoint/eigen entry points. */
+typedef struct {
+    int    iterations;       /* preconditioner applications (factor solves)         */
+    int    nrhs;             /* right-hand sides in the call                         */
+    double rel_residual;     /* max over RHS of ||b - A x|| / ||b|| (FP64)           */
+    double t_assemble_ms;    /* stencil + block assembly                             */
+    double t_factor_ms;      /* block cyclic reduction factorization                 */
+    double t_solve_ms;       /* refinement loop incl. factor solves and residuals    */
+    double t_recover_ms;     /* H (TM) / E (TE) recovery and copies out              */
+    double t_total_ms;       /* wall time of the call                                */
+    double factor_flops;     /* algorithmic real flops of the last factorization     */
+    int    block;            /* dense block size b = min(Nx, Ny)                     */
+    int    nblocks;          /* number of blocks n = max(Nx, Ny)                     */
+    int    levels;           /* cyclic-reduction elimination steps                   */
+    int    tc_gemm;          /* 1 when the tcgen05 3xTF32 GEMM ran                   */
+    long long device_bytes;  /* device memory held by the handle                     */
+    long long gpu_launches;  /* kernels this library launched during the call        */
+} fdfd_stats;
+
+/* Version string of the library. */
+const char* fdfd_version(void);
+
+/* Create a handle for an Nx x Ny grid (Grid, src/grid.jl:33-59) with Npx/Npy
+ * PML cells per side, cell sizes dx, dy in units of L0 metres (grid.jl:94-100),
+ * PML grading m and ln(R) (create_sfactor, src/pml.jl:1-31; the reference
+ * hard-wires m=3.5, lnR=-12 because S_create does not forward them,
+ * pml.jl:35-38), polarization FDFD_TM/FDFD_TE and precision FDFD_PREC_*.
+ * Requires Nx, Ny >= 3. */
+int  fdfd_create(fdfd_handle** h, int Nx, int Ny, int Npx, int Npy, double dx,
+                 double dy, double L0, double pml_m, double pml_lnR, int pol,
+                 int precision);
+void fdfd_destroy(fdfd_handle* h);
+const char* fdfd_last_error(const fdfd_handle* h);
+
+/* Refinement stopping rule: ||b - A x||/||b|| <= tol within max_iter factor
+ * solves (FDFD_REFINE_GMRES restarts every max_iter/… internally). */
+int  fdfd_set_refinement(fdfd_handle* h, double tol, int max_iter, int mode);
+
+/* Relative permittivity ϵᵣ (Device.ϵᵣ, src/device.jl:19-25), Nx*Ny complex.
+ * Rejects NaN/Inf.  Invalidates any existing factorization. */
+int  fdfd_set_eps(fdfd_handle* h, const double* eps_r);
+
+/* Assemble the driven operator of solve() at angular frequency omega (SI
+ * rad/s) and factor it:  TM A = δxf μ₀⁻¹ δxb + δyf μ₀⁻¹ δyb + ω² Tϵ,
+ * TE A = δxf Tϵxi δxb + δyf Tϵyi δyb + ω² μ₀ I  (driven.jl:170-194). */
+int  fdfd_factor(fdfd_handle* h, double omega);
+
+/* Driven solve with the current factorization for nrhs current sources
+ * (Device.src, b = iω·src, driven.jl:185,195), each Nx*Ny complex, stacked.
+ * Outputs (each nrhs*Nx*Ny complex, any may be NULL):
+ *   TM: f1 = Ez, f2 = Hx, f3 = Hy  (driven.jl:187-191)
+ *   TE: f1 = Hz, f2 = Ex, f3 = Ey  (driven.jl:197-202)
+ * Replaces dolinearsolve (solver.jl:4-41) plus the recovery SpMVs. */
+int  fdfd_solve(fdfd_handle* h, const double* src, int nrhs, double* f1,
+                double* f2, double* f3, fdfd_stats* stats);
+
+/* As fdfd_solve, but every array is a DEVICE pointer (cudaMalloc'd by the
+ * caller, same layout).  Used to time the solve with inputs resident in HBM. */
+int  fdfd_solve_device(fdfd_handle* h, const double* d_src, int nrhs,
+                       double* d_f1, double* d_f2, double* d_f3,
+                       fdfd_stats* stats);
+
+/* Adjoint gradient of J = |Σ_k m_k Ez_k|² with respect to real ϵᵣ for the
+ * current TM factorization and one source (no counterpart in the reference,
+ * which has no gradient code).  Solves A E = iω·src and Aᵀ λ = m by reusing
+ * the forward factors (P·A is complex symmetric for the diagonal PML scaling
+ * P, so Aᵀ = P A P⁻¹), then dJ/dϵᵣ_k = -2 Re(conj(mᵀE)·ω²ϵ₀·λ_k·E_k).
+ * Outputs: J (scalar), grad (Nx*Ny doubles), ez (Nx*Ny complex, may be NULL). */
+int  fdfd_adjoint(fdfd_handle* h, const double* src, const double* mvec,
+                  double* J, double* grad, double* ez, fdfd_stats* stats);
+
+/* Shift-invert eigenfrequencies (eigenfrequency, src/solver/eigen.jl:318-364):
+ * with the PML frozen at omega0, TM finds eigenpairs of
+ * A = Tϵᵣ⁻¹(δxf δxb + δyf δyb) nearest σ = -ω₀²μ₀ϵ₀, TE of
+ * A = δxf Tϵx⁻¹ δxb + δyf Tϵy⁻¹ δyb nearest σ = -ω₀²μ₀, by Krylov-Schur
+ * Arnoldi on (A - σI)⁻¹ with this library's factorization.  Outputs:
+ * omega (nev complex: sqrt(-λ/(μ₀ϵ₀)) TM, sqrt(-λ/μ₀) TE), lambda (nev
+ * complex eigenvalues of A, may be NULL), fields (nev*3*Nx*Ny complex:
+ * per mode f1,f2,f3 as in fdfd_solve but with the eigen.jl recovery, may be
+ * NULL). */
+int  fdfd_eigfreq(fdfd_handle* h, double omega0, int nev, int which,
+                  double tol, double* omega, double* lambda, double* fields,
+                  fdfd_stats* stats);
+
+/* Debug/parity: copy the assembled FP64 5-point stencil of the last factored
+ * operator to the host: 5*Nx*Ny complex, planes [self, x-1, x+1, y-1, y+1]
+ * (periodic neighbours, unscaled, reference units). */
+int  fdfd_get_stencil(fdfd_handle* h, double* out);
+
+/* Matrix-free product y = A x with the assembled FP64 operator (host arrays,
+ * nrhs stacked vectors). */
+int  fdfd_apply(fdfd_handle* h, const double* x, int nrhs, double* y);
+
+/* Per-kernel-class timing (no counterpart in the reference; it only logs wall
+ * time, src/solver/solver.jl:5,38).  While profiling is on, the library
+ * brackets each launch of the classes below with CUDA events on its stream
+ * and accumulates device time and algorithmic work (flops for GEMMs, bytes
+ * for the HBM-bound kernels).  fdfd_set_profiling(h, 1) resets the totals. */
+typedef struct {
+    double ms[6];            /* device time per class                           */
+    double work[6];          /* flops (classes 0, 1) or bytes (classes 3, 4, 5)  */
+    long long launches[6];   /* launches per class                              */
+} fdfd_profile;
+#define FDFD_PROF_GEMM_TC   0  /* tcgen05 3xTF32 block GEMM (flops, complex 8MNK) */
+#define FDFD_PROF_GEMM_SIMT 1  /* CUDA-core block GEMM (flops)                    */
+#define FDFD_PROF_GJ_PANEL  2  /* Gauss-Jordan panel steps                        */
+#define FDFD_PROF_SWEEP     3  /* solve sweeps: block GEMV (factor bytes read)    */
+#define FDFD_PROF_RESIDUAL  4  /* FP64 stencil residual / product (bytes)         */
+#define FDFD_PROF_OTHER     5  /* assembly, layout, Krylov vector kernels         */
+int  fdfd_set_profiling(fdfd_handle* h, int on);
+int  fdfd_get_profile(fdfd_handle* h, fdfd_profile* out);
+
+/* Kernel test entry (no counterpart in the reference): C = A·Bᵀ for complex
+ * row-major interleaved host matrices A (M x K), B (N x K), C (M x N), through
+ * the library's block GEMM: precision FDFD_PREC_FP64 (CUDA-core FP64) or
+ * FDFD_PREC_MIXED (FP32 storage; use_tc = 1 selects the tcgen05 3xTF32
+ * kernel, 0 the CUDA-core FP32 kernel).  *ms (may be NULL) receives the
+ * kernel time in milliseconds. */
+int  fdfd_debug_gemm(int M, int N, int K, const double* A, const double* B,
+                     double* C, int precision, int use_tc, double* ms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FDFD_CUDA_H */

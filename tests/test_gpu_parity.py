@@ -1,0 +1,179 @@
+"""GPU parity of the CUDA solve path (through the C ABI) against the FP64 oracle."""
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+DRIVEN = ["tm_point_guide_60x40", "tm_design_48x72", "te_design_64x40"]
+
+# tolerances (relative 2-norm errors)
+TOL_RES = 1e-10        # ||b - A x|| / ||b||
+TOL_FIELD_MIXED = 1e-8  # field error vs FP64 oracle, mixed precision
+TOL_FIELD_FP64 = 1e-10  # field error vs FP64 oracle, FP64 factorization
+
+
+def rel(a, b):
+    return float(np.linalg.norm(np.ravel(a - b)) / np.linalg.norm(np.ravel(b)))
+
+
+def handle_for(fdfd, Nx, Ny, npml, dx, dy, m, lnR, pol, prec):
+    h = fdfd._lib.Handle(Nx, Ny, npml[0], npml[1], dx, dy, 1e-6, m, lnR, pol, prec)
+    h.set_refinement(TOL_RES, 40)
+    return h
+
+
+def oracle_solve(oracle, p, pol):
+    g = oracle.Grid((p.Nx, p.Ny), tuple(p.npml), ((0.0, 0.0), (p.Nx * p.dx, p.Ny * p.dy)))
+    return oracle.solve(g, p.eps, p.src, p.omega, pol, p.pml_m, p.pml_lnR)
+
+
+# ---------------------------------------------------------------------------
+# block GEMM kernels
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("M,N,K", [(100, 70, 40), (128, 256, 32), (480, 480, 480), (300, 520, 96)])
+@pytest.mark.parametrize("kind", ["tc", "simt32", "simt64"])
+def test_block_gemm(lib, fdfd, M, N, K, kind):
+    rng = np.random.default_rng(M * 7 + N * 3 + K)
+    A = rng.standard_normal((M, K)) + 1j * rng.standard_normal((M, K))
+    B = rng.standard_normal((N, K)) + 1j * rng.standard_normal((N, K))
+    ref = A @ B.T
+    prec = fdfd.FDFD_PREC_FP64 if kind == "simt64" else fdfd.FDFD_PREC_MIXED
+    C, ms = fdfd._lib.debug_gemm(A, B, prec, 1 if kind == "tc" else 0)
+    err = rel(C, ref)
+    # FP32 inputs carry 6e-8 relative rounding; 3xTF32 products keep ~2^-21
+    tol = {"tc": 3e-6, "simt32": 1e-6, "simt64": 1e-13}[kind]
+    assert err <= tol, (kind, err)
+
+
+# ---------------------------------------------------------------------------
+# assembly
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("name", DRIVEN)
+def test_stencil_matches_oracle(lib, fdfd, name):
+    g = np.load(os.path.join(GOLD, name + ".npz"))
+    Nx, Ny = int(g["Nx"]), int(g["Ny"])
+    h = handle_for(fdfd, Nx, Ny, g["npml"], float(g["dx"]), float(g["dy"]), float(g["pml_m"]),
+                   float(g["pml_lnR"]), int(g["pol"]), fdfd.FDFD_PREC_FP64)
+    h.set_eps(g["eps"])
+    h.factor(float(g["omega"]))
+    st = h.stencil()
+    h.close()
+    ref = np.swapaxes(g["stencil"].reshape(5, Ny, Nx), 1, 2)
+    scale = np.abs(ref).max()
+    assert np.abs(st - ref).max() <= 1e-14 * scale
+
+
+# ---------------------------------------------------------------------------
+# driven solves
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+@pytest.mark.parametrize("name", DRIVEN)
+def test_solve_golden(lib, fdfd, name, prec):
+    g = np.load(os.path.join(GOLD, name + ".npz"))
+    Nx, Ny = int(g["Nx"]), int(g["Ny"])
+    P = fdfd.FDFD_PREC_FP64 if prec == "fp64" else fdfd.FDFD_PREC_MIXED
+    h = handle_for(fdfd, Nx, Ny, g["npml"], float(g["dx"]), float(g["dy"]), float(g["pml_m"]),
+                   float(g["pml_lnR"]), int(g["pol"]), P)
+    h.set_eps(g["eps"])
+    h.factor(float(g["omega"]))
+    f1, f2, f3, st = h.solve(g["src"])
+    h.close()
+    tol = TOL_FIELD_FP64 if prec == "fp64" else TOL_FIELD_MIXED
+    assert st.rel_residual <= TOL_RES
+    for f, k in ((f1, "f1"), (f2, "f2"), (f3, "f3")):
+        assert rel(f, g[k]) <= tol, (k, rel(f, g[k]))
+
+
+@pytest.mark.parametrize("shape", [(3, 3), (5, 7), (7, 5), (16, 3), (3, 16), (33, 17), (17, 33), (40, 41),
+                                   (64, 64), (61, 37)])
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_solve_ring_shapes(lib, fdfd, oracle, shape, prec):
+    """Odd/even ring sizes, both block orientations, tiny grids, complex ϵᵣ."""
+    Nx, Ny = shape
+    rng = np.random.default_rng(Nx * 100 + Ny)
+    npml = (min(4, Nx // 4), min(4, Ny // 4))
+    eps = rng.uniform(1, 4, (Nx, Ny)) + 1j * rng.uniform(0, 0.1, (Nx, Ny))
+    src = rng.standard_normal((Nx, Ny)) + 1j * rng.standard_normal((Nx, Ny))
+    dx = dy = 0.05
+    omega = 2 * np.pi * oracle.C0 / 1.55e-6
+    P = fdfd.FDFD_PREC_FP64 if prec == "fp64" else fdfd.FDFD_PREC_MIXED
+    h = handle_for(fdfd, Nx, Ny, npml, dx, dy, 4.0, np.log(1e-8), fdfd.TM, P)
+    h.set_eps(eps)
+    h.factor(omega)
+    f1, f2, f3, st = h.solve(src)
+    h.close()
+    g = oracle.Grid((Nx, Ny), npml, ((0.0, 0.0), (Nx * dx, Ny * dy)))
+    r1, r2, r3 = oracle.solve(g, eps, src, omega, oracle.TM, 4.0, np.log(1e-8))
+    tol = TOL_FIELD_FP64 if prec == "fp64" else TOL_FIELD_MIXED
+    assert st.rel_residual <= TOL_RES
+    assert rel(f1, r1) <= tol and rel(f2, r2) <= tol and rel(f3, r3) <= tol
+
+
+def test_point_guide_200x120(lib, fdfd, oracle):
+    """Plain FP64 TM solve: 200x120 straight guide, Jz=1 point source."""
+    from fdfd_gb300 import workloads as W
+    p = W.point_source_guide()
+    ref = oracle_solve(oracle, p, oracle.TM)
+    for prec, tol in ((fdfd.FDFD_PREC_FP64, TOL_FIELD_FP64), (fdfd.FDFD_PREC_MIXED, TOL_FIELD_MIXED)):
+        h = handle_for(fdfd, p.Nx, p.Ny, p.npml, p.dx, p.dy, p.pml_m, p.pml_lnR, fdfd.TM, prec)
+        h.set_eps(p.eps)
+        h.factor(p.omega)
+        f1, f2, f3, st = h.solve(p.src)
+        h.close()
+        assert st.rel_residual <= TOL_RES
+        assert max(rel(f1, ref[0]), rel(f2, ref[1]), rel(f3, ref[2])) <= tol
+
+
+def test_multi_rhs_matches_single(lib, fdfd, oracle):
+    from fdfd_gb300 import workloads as W
+    p = W.design_guide(96, 64, design=(24, 24), seed=3, npml=10)
+    rng = np.random.default_rng(1)
+    srcs = rng.standard_normal((3, p.Nx, p.Ny)) + 1j * rng.standard_normal((3, p.Nx, p.Ny))
+    h = handle_for(fdfd, p.Nx, p.Ny, p.npml, p.dx, p.dy, p.pml_m, p.pml_lnR, fdfd.TM, fdfd.FDFD_PREC_MIXED)
+    h.set_eps(p.eps)
+    h.factor(p.omega)
+    F1, _, _, st = h.solve(srcs)
+    assert st.rel_residual <= TOL_RES
+    for k in range(3):
+        f1, _, _, _ = h.solve(srcs[k])
+        assert rel(F1[k], f1) <= 1e-9
+    h.close()
+
+
+def test_reference_dipole_problem(lib, fdfd, oracle):
+    """The reference's own test problem (test/runtests.jl:7-21): 6x6 µm, dh = 0.01,
+    15 PML cells, ω = 2π·200 THz, point source 1im at (0, 0), default PML
+    grading; the GPU solve must agree with the FP64 direct solve as the
+    reference's two solvers must (√eps relative), here to the mixed tolerance."""
+    d = fdfd.Device(fdfd.Grid(0.01, [15, 15], [-3, 3], [-3, 3]), 2 * np.pi * 200e12)
+    fdfd.setup_src(d, fdfd.Point(0, 0))
+    field = fdfd.solve(d, fdfd.TM, precision="mixed")
+    g = oracle.Grid.from_ranges(0.01, [15, 15], [-3, 3], [-3, 3])
+    src = np.zeros(g.N, dtype=complex)
+    src[g.x2ind(0), g.y2ind(0)] = 1j
+    r = oracle.solve(g, np.ones(g.N, dtype=complex), src, 2 * np.pi * 200e12, oracle.TM)
+    assert rel(field["Ez"], r[0]) <= TOL_FIELD_MIXED
+    assert rel(field["Hx"], r[1]) <= TOL_FIELD_MIXED
+    assert rel(field["Hy"], r[2]) <= TOL_FIELD_MIXED
+
+
+# ---------------------------------------------------------------------------
+# error behaviour
+# ---------------------------------------------------------------------------
+def test_errors(lib, fdfd):
+    h = handle_for(fdfd, 20, 16, (2, 2), 0.05, 0.05, 4.0, np.log(1e-8), fdfd.TM, fdfd.FDFD_PREC_MIXED)
+    with pytest.raises(fdfd.FDFDError) as e:
+        h.solve(np.ones((20, 16)))
+    assert e.value.code == fdfd._lib.FDFD_EINVAL
+    eps = np.ones((20, 16), dtype=complex)
+    eps[3, 4] = np.nan
+    with pytest.raises(fdfd.FDFDError) as e:
+        h.set_eps(eps)
+    assert e.value.code == fdfd._lib.FDFD_EINVAL
+    h.set_eps(np.ones((20, 16)))
+    with pytest.raises(fdfd.FDFDError):
+        h.factor(-1.0)
+    h.close()

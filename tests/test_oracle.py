@@ -1,0 +1,157 @@
+"""CPU checks that pin the FP64 oracle (no GPU needed).
+
+The reference holds no golden vectors (its test/runtests.jl only checks that
+two FP64 direct solvers agree), so the oracle is pinned by hand-derived
+operator entries, solver agreement, an analytic Green's-function answer and
+the committed golden fixtures (regression).
+"""
+import os
+
+import numpy as np
+import pytest
+import scipy.sparse as sp
+from scipy.special import hankel2
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def small_grid(oracle, N=(4, 3), npml=(1, 1), d=(0.1, 0.2)):
+    return oracle.Grid(N, npml, ((0.0, 0.0), (N[0] * d[0], N[1] * d[1])))
+
+
+def test_constants(oracle):
+    # src/types.jl:6-9
+    assert oracle.EPS0 == 8.85418782e-12 and oracle.MU0 == 1.25663706e-6
+    assert oracle.C0 == pytest.approx(299792458.0, rel=1e-8)
+    assert oracle.normalize_parameters(1e-6) == (oracle.EPS0 * 1e-6, oracle.MU0 * 1e-6, oracle.C0 / 1e-6)
+
+
+def test_grid_round_half_even(oracle):
+    # src/grid.jl:54: N = round(L/dh), Julia rounds half to even
+    g = oracle.Grid.from_ranges(1.0, [0, 0], [0.0, 2.5], [0.0, 3.5])
+    assert g.N == (2, 4)
+    assert np.allclose(g.xc(), [0.625, 1.875])
+
+
+def test_delta_hand_entries(oracle):
+    g = small_grid(oracle)
+    dx, dy = g.dx(), g.dy()
+    f1 = np.array([[-1, 1, 0, 0], [0, -1, 1, 0], [0, 0, -1, 1], [1, 0, 0, -1]]) / dx
+    b1 = np.array([[1, 0, 0, -1], [-1, 1, 0, 0], [0, -1, 1, 0], [0, 0, -1, 1]]) / dx
+    assert np.array_equal(oracle.delta(oracle.X, oracle.FORWARD, g).toarray(), np.kron(np.eye(3), f1))
+    assert np.array_equal(oracle.delta(oracle.X, oracle.BACKWARD, g).toarray(), np.kron(np.eye(3), b1))
+    fy = np.array([[-1, 1, 0], [0, -1, 1], [1, 0, -1]]) / dy
+    by = np.array([[1, 0, -1], [-1, 1, 0], [0, -1, 1]]) / dy
+    assert np.array_equal(oracle.delta(oracle.Y, oracle.FORWARD, g).toarray(), np.kron(fy, np.eye(4)))
+    assert np.array_equal(oracle.delta(oracle.Y, oracle.BACKWARD, g).toarray(), np.kron(by, np.eye(4)))
+    # backward difference is minus the transpose of forward (periodic)
+    D = oracle.delta(oracle.X, oracle.FORWARD, g)
+    assert np.array_equal(oracle.delta(oracle.X, oracle.BACKWARD, g).toarray(), -D.T.toarray())
+
+
+def test_grid_average_periodic(oracle):
+    a = np.arange(12.0).reshape(4, 3)
+    gx = oracle.grid_average(a, oracle.X)
+    assert gx[0, 0] == (a[0, 0] + a[3, 0]) / 2 and gx[2, 1] == (a[2, 1] + a[1, 1]) / 2
+    gy = oracle.grid_average(a, oracle.Y)
+    assert gy[1, 0] == (a[1, 0] + a[1, 2]) / 2
+
+
+def test_sfactor_hand_values(oracle):
+    # src/pml.jl:1-31 with N=10 cells, 3 PML cells, dw = 0.1, m = 3.5, lnR = -12
+    g = oracle.Grid((10, 10), (3, 3), ((0.0, 0.0), (1.0, 1.0)))
+    w = 2e15
+    eps0 = oracle.EPS0 * 1e-6
+    T = 3 * 0.1   # Npml * dw, as pml.jl:192 computes it
+    smax = -(3.5 + 1) * (-12) / (2 * oracle.ETA0 * T)
+    S = lambda l: 1 - 1j * smax * (l / T) ** 3.5 / (w * eps0)
+    f = oracle.create_sfactor(oracle.X, oracle.FORWARD, g, w)
+    b = oracle.create_sfactor(oracle.X, oracle.BACKWARD, g, w)
+    ap = lambda v: pytest.approx(v, rel=1e-14)
+    assert f[0] == ap(S(0.1 * 2.5)) and f[2] == ap(S(0.1 * 0.5)) and f[3] == 1 and f[9] == ap(S(0.1 * 2.5))
+    assert b[0] == ap(S(0.3)) and b[2] == ap(S(0.1)) and b[7] == 1 and b[8] == ap(S(0.1)) and b[9] == ap(S(0.2))
+
+
+def test_tm_operator_is_P_symmetric(oracle):
+    """P·A is complex symmetric for P = diag(s_xf s_yf): the identity the adjoint uses."""
+    g = oracle.Grid((12, 9), (3, 2), ((0.0, 0.0), (1.2, 0.9)))
+    rng = np.random.default_rng(0)
+    eps = rng.uniform(1, 5, g.N) + 0.1j
+    w = 1.2e15
+    A = oracle.assemble(g, eps, w, oracle.TM)
+    sxf = oracle.create_sfactor(oracle.X, oracle.FORWARD, g, w)
+    syf = oracle.create_sfactor(oracle.Y, oracle.FORWARD, g, w)
+    P = sp.diags(oracle.vec(sxf[:, None] * syf[None, :]))
+    PA = (P @ A).toarray()
+    assert np.abs(PA - PA.T).max() <= 1e-15 * np.abs(PA).max()
+
+
+@pytest.mark.parametrize("pol", [1, 2])
+def test_solver_agreement(oracle, pol):
+    """The reference's test pattern (test/runtests.jl:7-21): two independent FP64
+    direct solvers agree; here SuperLU vs dense LAPACK on a small problem."""
+    g = oracle.Grid((30, 24), (5, 5), ((0.0, 0.0), (1.5, 1.2)))
+    rng = np.random.default_rng(pol)
+    eps = rng.uniform(1, 12, g.N) + 0j
+    src = np.zeros(g.N, dtype=complex)
+    src[10, 12] = 1j
+    w = 2 * np.pi * oracle.C0 / 1.55e-6
+    A = oracle.assemble(g, eps, w, pol, 4.0, np.log(1e-8))
+    b = 1j * w * oracle.vec(src)
+    x1 = oracle.dolinearsolve(A, b)
+    x2 = np.linalg.solve(A.toarray(), b)
+    assert np.linalg.norm(x1 - x2) <= 1e-12 * np.linalg.norm(x2)
+
+
+def test_dipole_matches_greens_function(oracle):
+    """Known answer: a point current 1im in free space radiates
+    Ez = -(i/4)·ω·μ₀·dx·dy·H0⁽²⁾(k r) (outgoing under the e^{+iωt} convention
+    implied by the PML stretch s = 1 - iσ/(ωϵ₀), pml.jl:198)."""
+    dx = 0.025
+    N = 240
+    g = oracle.Grid((N, N), (20, 20), ((-N * dx / 2, -N * dx / 2), (N * dx / 2, N * dx / 2)))
+    w = 2 * np.pi * oracle.C0 / 1.55e-6
+    src = np.zeros(g.N, dtype=complex)
+    src[N // 2, N // 2] = 1j
+    ez, _, _ = oracle.solve(g, np.ones(g.N, dtype=complex), src, w, oracle.TM, 4.0, np.log(1e-8))
+    eps0, mu0, _ = oracle.normalize_parameters(1e-6)
+    k = w * np.sqrt(mu0 * eps0)
+    xs = g.xc()
+    c = N // 2
+    worst = 0.0
+    for off in (40, 60, 80):
+        r = abs(xs[c + off] - xs[c])
+        ana = -0.25j * w * mu0 * dx * dx * hankel2(0, k * r)
+        worst = max(worst, abs(ez[c + off, c] - ana) / abs(ana))
+    assert worst <= 0.03, worst
+
+
+@pytest.mark.parametrize("name", ["tm_point_guide_60x40", "tm_design_48x72", "te_design_64x40"])
+def test_golden_regression(oracle, name):
+    g = np.load(os.path.join(GOLD, name + ".npz"))
+    Nx, Ny = int(g["Nx"]), int(g["Ny"])
+    grid = oracle.Grid((Nx, Ny), tuple(g["npml"]), ((0.0, 0.0), (Nx * float(g["dx"]), Ny * float(g["dy"]))))
+    f = oracle.solve(grid, g["eps"], g["src"], float(g["omega"]), int(g["pol"]), float(g["pml_m"]),
+                     float(g["pml_lnR"]))
+    for i, k in enumerate(("f1", "f2", "f3")):
+        assert np.linalg.norm(f[i] - g[k]) <= 1e-12 * np.linalg.norm(g[k])
+
+
+def test_adjoint_gradient_matches_fd(oracle):
+    """FP64 adjoint of J = |mᵀE|² against central differences (step 1e-4 in ϵᵣ)."""
+    g = oracle.Grid((28, 22), (4, 4), ((0.0, 0.0), (28 * 0.0775, 22 * 0.0775)))
+    rng = np.random.default_rng(5)
+    eps = rng.uniform(1, 12.25, g.N) + 0j
+    src = np.zeros(g.N, dtype=complex)
+    src[7, :] = np.exp(-((np.arange(22) - 11) / 4.0) ** 2)
+    m = np.zeros(g.N, dtype=complex)
+    m[20, :] = np.exp(-((np.arange(22) - 11) / 4.0) ** 2)
+    w = 2 * np.pi * oracle.C0 / 1.55e-6
+    J, grad, _ = oracle.adjoint_gradient(g, eps, src, w, m, 4.0, np.log(1e-8))
+    for (i, j) in [(12, 9), (14, 11), (16, 13)]:
+        ep, em = eps.copy(), eps.copy()
+        ep[i, j] += 1e-4
+        em[i, j] -= 1e-4
+        fd = (oracle.objective(g, ep, src, w, m, 4.0, np.log(1e-8)) -
+              oracle.objective(g, em, src, w, m, 4.0, np.log(1e-8))) / 2e-4
+        assert abs(fd - grad[i, j]) <= 1e-5 * abs(grad[i, j]) + 1e-12 * J
