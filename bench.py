@@ -1,0 +1,355 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 FDFD solve path; prints ONE JSON line.
+
+Workload (one "step"): the 800 x 480 TM design-guide problem — input and
+output guide arms (ϵᵣ = 12.25, 10 cells wide) around a 200 x 200 design
+region of seeded i.i.d. ϵᵣ ~ U[1, 12.25], Gaussian line source (waist 8
+cells) across the input guide, λ = 1.55 µm, dl = λ/20, 20 PML cells per side
+(m = 4, R = 1e-8).  A step assembles the operator from the resident ϵᵣ,
+factors it (complex FP32 block cyclic reduction with 3xTF32 tcgen05 GEMMs),
+solves to ||b - A x||/||b|| <= 1e-10 with FP64 FGMRES refinement and
+recovers Hx, Hy.  value = solves/s with inputs resident in HBM; e2e = the
+same through the host-buffer C ABI (ϵᵣ and source copied in, three fields
+copied out, every step).
+
+--impl reference times the CPU restatement of the reference path (scipy
+SuperLU FP64 on the same problem) on the host cores, one process per core.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "TM solves/s at 1e-10 residual: mixed-prec vs FP64 on one GB300; adjoint grads/s"
+WORKLOAD = ("design_guide 800x480 TM: guide arms + 200x200 random design (seed 2), Gaussian line source "
+            "(waist 8), lambda 1.55um, dl lambda/20, 20-cell PML m=4 R=1e-8, tol 1e-10")
+
+
+def args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--size", default=None,
+                    help="NXxNY: same problem family at another size (profiling runs); design region = "
+                         "a quarter of the smaller side squared")
+    return ap.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)), int(os.environ.get("WORLD_SIZE", 1))
+
+
+# ---------------------------------------------------------------------------
+# clocks sampler (nvidia-smi during the timed region)
+# ---------------------------------------------------------------------------
+class Clocks:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu, self.lines, self.proc = gpu, [], None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-i", str(self.gpu), "-lms", "200"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# CPU reference path (scipy SuperLU restatement of the reference solve)
+# ---------------------------------------------------------------------------
+def _cpu_solve(kind):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import __graft_entry__ as G
+    G.load_package()
+    import fdfd_oracle as O
+    from fdfd_gb300 import workloads as W
+    p = W.design_guide() if kind == "full" else W.point_source_guide(120, 80)
+    g = O.Grid((p.Nx, p.Ny), p.npml, ((0.0, 0.0), (p.Nx * p.dx, p.Ny * p.dy)))
+    t0 = time.perf_counter()
+    f, A, b = O.solve(g, p.eps, p.src, p.omega, O.TM, p.pml_m, p.pml_lnR, return_system=True)
+    t = time.perf_counter() - t0
+    return t, float(O.relative_residual(A, O.vec(f[0]), b))
+
+
+def cpu_baseline_single():
+    """One full solve, single thread (SuperLU factors sequentially)."""
+    t, res = _cpu_solve("full")
+    return {"value": 1.0 / t, "unit": "solves/s", "cores": 1, "kind": "port",
+            "sample": f"1 full solve of the workload with the scipy/SuperLU FP64 oracle ({t:.1f} s, "
+                      f"rel. residual {res:.1e})"}
+
+
+def run_reference(a):
+    import concurrent.futures as cf
+    import multiprocessing as mp
+    cores = min(os.cpu_count() or 1, 16)
+    ctx = mp.get_context("spawn")
+    with cf.ProcessPoolExecutor(max_workers=cores, mp_context=ctx) as ex:
+        for _ in range(a.warmup):   # warm the workers: small solve each
+            list(ex.map(_cpu_solve, ["small"] * cores))
+        times = []
+        t0 = time.perf_counter()
+        for _ in range(a.steps):
+            ts = time.perf_counter()
+            list(ex.map(_cpu_solve, ["full"] * cores))
+            times.append(time.perf_counter() - ts)
+        total = time.perf_counter() - t0
+    value = cores * a.steps / total
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": a.gpus,
+            "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 * total / a.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "solver": "scipy SuperLU FP64 (restatement of lu(A)\\b)",
+                       "step": f"{cores} concurrent full solves, one per host core"},
+            "cpu_baseline": {"value": value, "unit": "solves/s", "cores": cores, "kind": "port",
+                             "sample": f"{a.steps} steps x {cores} concurrent full solves"},
+            "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# GPU path
+# ---------------------------------------------------------------------------
+def tf32_cublas_tflops(torch):
+    """cuBLAS TF32 GEMM throughput (context only; the roofline peak comes from MEASURED_PEAKS.json)."""
+    try:
+        torch.backends.cuda.matmul.allow_tf32 = True
+        n = 8192
+        x = torch.randn(n, n, device="cuda", dtype=torch.float32)
+        y = torch.randn(n, n, device="cuda", dtype=torch.float32)
+        for _ in range(2):
+            x @ y
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(5):
+            x @ y
+        e1.record()
+        torch.cuda.synchronize()
+        t = e0.elapsed_time(e1) / 1e3 / 5
+        del x, y
+        return 2 * n ** 3 / t / 1e12
+    except Exception:
+        return None
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "MEASURED_PEAKS.json"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+def main():
+    a = args()
+    rank, local, world = dist_env()
+    if a.impl == "reference":
+        if rank == 0:
+            run_reference(a)
+        return
+    import numpy as np
+    import torch
+    import __graft_entry__ as G
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    pkg = G.load_package()
+    from fdfd_gb300 import workloads as W
+    L = pkg._lib
+    workload = WORKLOAD
+    if a.size:
+        nx, ny = (int(v) for v in a.size.lower().split("x"))
+        dsz = min(nx, ny) // 4
+        p = W.design_guide(nx, ny, design=(dsz, dsz))
+        workload = f"design_guide {nx}x{ny} (profiling size), {dsz}x{dsz} design"
+    else:
+        p = W.design_guide()
+    N = p.Nx * p.Ny
+
+    def make(prec):
+        h = L.Handle(p.Nx, p.Ny, p.npml[0], p.npml[1], p.dx, p.dy, 1e-6, p.pml_m, p.pml_lnR, pkg.TM, prec)
+        h.set_refinement(1e-10, 80)
+        h.set_eps(p.eps)
+        return h
+
+    # device-resident source and fields (x fastest, interleaved complex128)
+    src_nat = L.natural(p.src).reshape(-1)
+    d_src = torch.from_numpy(src_nat).to("cuda")
+    d_f = [torch.empty(N, dtype=torch.complex128, device="cuda") for _ in range(3)]
+
+    def step_device(h):
+        h.factor(p.omega)
+        return h.solve_device(d_src.data_ptr(), 1, d_f[0].data_ptr(), d_f[1].data_ptr(), d_f[2].data_ptr())
+
+    h = make(L.FDFD_PREC_MIXED)
+    for _ in range(a.warmup):
+        step_device(h)
+    torch.cuda.synchronize()
+    clocks = Clocks(local)
+    clocks.start()
+    time.sleep(0.3)
+    h.set_profiling(True)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    stats = []
+    for _ in range(a.steps):
+        stats.append(step_device(h).as_dict())
+    e1.record()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clk = clocks.stop()
+    t = e0.elapsed_time(e1) / 1e3
+    if world > 1:
+        tt = torch.tensor([t], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t = float(tt.item())
+    prof = h.profile()
+    h.set_profiling(False)
+    value = world * a.steps / t
+    maxres = max(s["rel_residual"] for s in stats)
+    launches = sum(s["gpu_launches"] for s in stats)
+    iters = [s["iterations"] for s in stats]
+
+    # field check against the FP64 factorization (same library, FP64 path) and FP64 timing
+    fp64 = None
+    if not a.no_fp64:
+        hf = make(L.FDFD_PREC_FP64)
+        step_device(hf)                      # warm-up
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        st64 = step_device(hf)
+        torch.cuda.synchronize()
+        t64 = time.perf_counter() - t0
+        ez64 = d_f[0].cpu().numpy()
+        hf.close()
+        h.factor(p.omega)
+        h.solve_device(d_src.data_ptr(), 1, d_f[0].data_ptr(), d_f[1].data_ptr(), d_f[2].data_ptr())
+        ez_mix = d_f[0].cpu().numpy()
+        fp64 = {"solves_per_s": 1.0 / t64, "rel_residual": st64.rel_residual, "t_factor_ms": st64.t_factor_ms,
+                "mixed_over_fp64": (value / world) * t64,
+                "mixed_vs_fp64_field_err": float(np.linalg.norm(ez_mix - ez64) / np.linalg.norm(ez64))}
+
+    # end-to-end through the host-buffer C ABI: ϵᵣ and source in, three fields out, every step
+    e2e = None
+    if not a.no_e2e:
+        he = make(L.FDFD_PREC_MIXED)
+        h2d = N * 16 * 2
+        d2h = N * 16 * 3
+        he.factor(p.omega)
+        he.solve(p.src)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(a.steps):
+            he.set_eps(p.eps)
+            he.factor(p.omega)
+            he.solve(p.src)
+        te = time.perf_counter() - t0
+        he.close()
+        e2e = {"value": world * a.steps / te, "unit": "solves/s", "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": d2h}
+
+    # roofline of the dominant kernel class
+    peaks, peak_src = measured_peaks()
+    dom = max(prof, key=lambda k: prof[k]["ms"])
+    d = prof[dom]
+    if dom in ("gemm_tc", "gemm_simt"):
+        achieved = d["work"] / (d["ms"] / 1e3) / 1e12
+        # 3xTF32: three TF32 MMAs per real product; TF32 tensor rate = half the BF16 rate
+        peak = peaks["bf16_tflops"] / 2 / 3 if dom == "gemm_tc" else None
+        roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": achieved / peak if peak else None, "traffic": None, "kernel": dom,
+                "peak_note": f"bf16 burst from {peak_src} /2 (TF32 rate) /3 (3xTF32 split), of measured",
+                "work_unit": "8*M*N*K algorithmic complex-GEMM flops per launch"}
+    elif dom == "gj_panel":
+        roof = {"bound": "latency", "achieved": None, "peak": None, "unit": None, "frac": None, "traffic": None,
+                "kernel": dom}
+    else:
+        achieved = d["work"] / (d["ms"] / 1e3) / 1e9
+        peak = peaks["hbm_gbs"]
+        roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": None, "kernel": dom, "peak_note": f"hbm_gbs from {peak_src}, of measured"}
+    roof["launches_in_region"] = d["launches"]
+    roof["avg_launch_ms"] = d["ms"] / max(d["launches"], 1)
+    roof["class_ms"] = {k: round(v["ms"], 3) for k, v in prof.items()}
+
+    cpu = None
+    if rank == 0 and not a.no_cpu_baseline:
+        cpu = cpu_baseline_single()
+    tf32 = tf32_cublas_tflops(torch) if rank == 0 else None
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": a.steps,
+                "warmup": a.warmup, "ms_per_step": 1e3 * t / a.steps, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "c64(3xTF32)+c128", "data": "synthetic",
+                "config": {"workload": workload, "precision": "mixed: FP32 factors, 3xTF32 tcgen05 products, "
+                                                            "FP64 FGMRES refinement",
+                           "l2": "inputs larger than L2 (factor storage ~6 GB per solve, no flush needed)",
+                           "parallelism": f"replicas x{world}"},
+                "e2e": e2e, "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu, "clocks": clk,
+                "rel_residual_max": maxres, "refine_iterations": iters, "fp64": fp64,
+                "tf32_cublas_tflops_live": tf32, "factor_flops": stats[-1]["factor_flops"],
+                "t_factor_ms": stats[-1]["t_factor_ms"], "t_solve_ms": stats[-1]["t_solve_ms"]}
+        print(json.dumps(line), flush=True)
+    h.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

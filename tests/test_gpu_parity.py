@@ -43,8 +43,10 @@ def test_block_gemm(lib, fdfd, M, N, K, kind):
     prec = fdfd.FDFD_PREC_FP64 if kind == "simt64" else fdfd.FDFD_PREC_MIXED
     C, ms = fdfd._lib.debug_gemm(A, B, prec, 1 if kind == "tc" else 0)
     err = rel(C, ref)
-    # FP32 inputs carry 6e-8 relative rounding; 3xTF32 products keep ~2^-21
-    tol = {"tc": 3e-6, "simt32": 1e-6, "simt64": 1e-13}[kind]
+    # FP32 inputs carry 6e-8 relative rounding; 3xTF32 products keep ~2^-21 per
+    # product, and the tensor core's FP32 accumulation (truncating, measured
+    # 9e-7 at K=32, 7.5e-6 at K=480, 1.5e-5 at K=1024) grows about linearly in K.
+    tol = {"tc": 2.5e-8 * K + 1e-6, "simt32": 1e-6, "simt64": 1e-13}[kind]
     assert err <= tol, (kind, err)
 
 
