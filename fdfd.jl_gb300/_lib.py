@@ -25,7 +25,8 @@ FDFD_REFINE_GMRES, FDFD_REFINE_CLASSIC = 0, 1
 # every symbol include/fdfd_cuda.h declares
 EXPORTS = ["fdfd_version", "fdfd_create", "fdfd_destroy", "fdfd_last_error", "fdfd_set_refinement",
            "fdfd_set_eps", "fdfd_factor", "fdfd_solve", "fdfd_solve_device", "fdfd_adjoint", "fdfd_eigfreq",
-           "fdfd_get_stencil", "fdfd_apply", "fdfd_set_profiling", "fdfd_get_profile", "fdfd_debug_gemm"]
+           "fdfd_get_stencil", "fdfd_apply", "fdfd_set_profiling", "fdfd_get_profile", "fdfd_residual_noalloc",
+           "fdfd_debug_gemm"]
 PROF_CLASSES = ["gemm_tc", "gemm_simt", "gj_panel", "sweep", "residual", "other"]
 
 
@@ -97,6 +98,9 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.fdfd_set_profiling.argtypes = [vp, ip]
     lib.fdfd_get_profile.restype = ip
     lib.fdfd_get_profile.argtypes = [vp, C.POINTER(Profile)]
+    lib.fdfd_residual_noalloc.restype = ip
+    lib.fdfd_residual_noalloc.argtypes = [ip, ip, ip, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                          C.c_void_p]
     lib.fdfd_debug_gemm.restype = ip
     lib.fdfd_debug_gemm.argtypes = [ip, ip, ip, dp, dp, dp, ip, ip, dp]
     _lib = lib

@@ -162,6 +162,27 @@ typedef struct {
 int  fdfd_set_profiling(fdfd_handle* h, int on);
 int  fdfd_get_profile(fdfd_handle* h, fdfd_profile* out);
 
+/* Allocation-free residual: r = b - A x (or r = A x when b is NULL) and, per
+ * right-hand side, norms[2k] = ||r_k||², norms[2k+1] = ||b_k||², for nrhs
+ * stacked FP64 vectors.  No counterpart in the reference.  It exists for
+ * callers that may not let a library call cudaMalloc/cudaFree: runtimes that
+ * own all device memory through their own pool (CUDA.jl, PyTorch's caching
+ * allocator, fixed-budget servers) and code that cannot take the device-wide
+ * synchronisation those calls may imply.  Every pointer is a caller-owned
+ * DEVICE pointer: stencil is the 5*Nx*Ny complex operator in the layout of
+ * fdfd_get_stencil, x/b/r hold nrhs*Nx*Ny complex values, norms 2*nrhs
+ * doubles.  stream is a cudaStream_t (NULL = default stream); the call
+ * returns after the stream has finished its work.  Scratch: a fixed 1 MiB
+ * device array of the library (block partial sums), allocated when the
+ * library is loaded and held by every GPU that loads it until exit; sizes with
+ * ceil(Nx*Ny/256)*nrhs > 65536 are rejected with FDFD_EINVAL.  The first call
+ * on a device resolves that array's device address (cudaGetSymbolAddress) and
+ * should come before any stream capture.  All calls share the array, so calls
+ * that overlap on the GPU (other streams or threads) race; serialise them. */
+int  fdfd_residual_noalloc(int Nx, int Ny, int nrhs, const double* stencil,
+                           const double* x, const double* b, double* r,
+                           double* norms, void* stream);
+
 /* Kernel test entry (no counterpart in the reference): C = A·Bᵀ for complex
  * row-major interleaved host matrices A (M x K), B (N x K), C (M x N), through
  * the library's block GEMM: precision FDFD_PREC_FP64 (CUDA-core FP64) or
