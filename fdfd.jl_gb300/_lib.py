@@ -181,6 +181,17 @@ class Handle:
             res = [r[0] if r is not None else None for r in res]
         return res[0], res[1], res[2], st
 
+    def adjoint(self, src, mvec):
+        """Gradient of J = |Σ m·Ez|² w.r.t. real ϵᵣ -> (J, grad (Nx, Ny), Ez (Nx, Ny), stats)."""
+        s = natural(src)
+        m = natural(mvec)
+        grad = np.empty((self.Ny, self.Nx), dtype=np.float64)
+        ez = np.empty_like(s)
+        J = C.c_double(0)
+        st = Stats()
+        self._check(self.lib.fdfd_adjoint(self.h, cptr(s), cptr(m), C.byref(J), cptr(grad), cptr(ez), C.byref(st)))
+        return J.value, grad.T.copy(), from_natural(ez, self.Nx, self.Ny)[0], st
+
     def set_profiling(self, on=True):
         self._check(self.lib.fdfd_set_profiling(self.h, 1 if on else 0))
 

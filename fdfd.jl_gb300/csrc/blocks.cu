@@ -68,52 +68,55 @@ __global__ void level1_combine_kernel(NodeMap m, const cplx<double>* st, double 
     long long pe = D.plane_elems();
     T* Ds = D.slot(J.s);
     int c = c0 + tx;
-    cplx<double> lc_next = cmk(0.0, 0.0), uc_next = cmk(0.0, 0.0), uc_prev = cmk(0.0, 0.0),
-                 lc_prev = cmk(0.0, 0.0);
+    // stencil values are FP64; the arithmetic runs in the factor precision T
+    auto tv = [&](cplx<double> v) { return cmk((T)(v.re * scale), (T)(v.im * scale)); };
+    const cplx<T> z = cmk((T)0, (T)0);
+    cplx<T> lc_next = z, uc_next = z, uc_prev = z, lc_prev = z;
     if (c < b) {
         if (J.next_elim) {
-            lc_next = cscale(st_at<T>(st, m, m.p_cprev(), J.next, c), scale);
-            uc_next = cscale(st_at<T>(st, m, m.p_cnext(), J.next, c), scale);
+            lc_next = tv(st_at<T>(st, m, m.p_cprev(), J.next, c));
+            uc_next = tv(st_at<T>(st, m, m.p_cnext(), J.next, c));
         }
         if (J.prev_elim) {
-            uc_prev = cscale(st_at<T>(st, m, m.p_cnext(), J.prev, c), scale);
-            lc_prev = cscale(st_at<T>(st, m, m.p_cprev(), J.prev, c), scale);
+            uc_prev = tv(st_at<T>(st, m, m.p_cnext(), J.prev, c));
+            lc_prev = tv(st_at<T>(st, m, m.p_cprev(), J.prev, c));
         }
     }
     for (int q = 0; q < 4; ++q) {
         int rl = ty + 8 * q;
         int r = r0 + rl;
-        cplx<double> dv = cmk(0.0, 0.0), uv = cmk(0.0, 0.0), lv = cmk(0.0, 0.0);
+        cplx<T> dv = z, uv = z, lv = z;
         bool ok = (r < b && c < b);
         if (ok) {
-            cplx<double> ls = cscale(st_at<T>(st, m, m.p_cprev(), J.s, r), scale);
-            cplx<double> us = cscale(st_at<T>(st, m, m.p_cnext(), J.s, r), scale);
-            if (c == r) dv = st_at<T>(st, m, 0, J.s, r);
-            if (c == (r + b - 1) % b) dv = cadd(dv, st_at<T>(st, m, m.p_inprev(), J.s, r));
-            if (c == (r + 1) % b) dv = cadd(dv, st_at<T>(st, m, m.p_innext(), J.s, r));
-            dv = cscale(dv, scale);
+            const cplx<T> ls = tv(st_at<T>(st, m, m.p_cprev(), J.s, r));
+            const cplx<T> us = tv(st_at<T>(st, m, m.p_cnext(), J.s, r));
+            cplx<double> tri = cmk(0.0, 0.0);
+            if (c == r) tri = st_at<T>(st, m, 0, J.s, r);
+            if (c == (r + b - 1) % b) tri = cadd(tri, st_at<T>(st, m, m.p_inprev(), J.s, r));
+            if (c == (r + 1) % b) tri = cadd(tri, st_at<T>(st, m, m.p_innext(), J.s, r));
+            dv = tv(tri);
             if (J.prev_elim) {
-                long long o = (long long)r * D.ld + c;
-                cplx<double> g = cmk((double)Gp[o], (double)Gp[pe + o]);
-                dv = csub(dv, cmul(cmul(ls, g), uc_prev));
-                lv = cneg(cmul(cmul(ls, g), lc_prev));
+                const long long o = (long long)r * D.ld + c;
+                const cplx<T> lg = cmul(ls, cmk(Gp[o], Gp[pe + o]));
+                dv = csub(dv, cmul(lg, uc_prev));
+                lv = cneg(cmul(lg, lc_prev));
             } else if (c == r) {
                 lv = ls;
             }
             if (J.next_elim) {
-                long long o = (long long)r * D.ld + c;
-                cplx<double> g = cmk((double)Gn[o], (double)Gn[pe + o]);
-                dv = csub(dv, cmul(cmul(us, g), lc_next));
-                uv = cneg(cmul(cmul(us, g), uc_next));
+                const long long o = (long long)r * D.ld + c;
+                const cplx<T> ug = cmul(us, cmk(Gn[o], Gn[pe + o]));
+                dv = csub(dv, cmul(ug, lc_next));
+                uv = cneg(cmul(ug, uc_next));
             } else if (c == r) {
                 uv = us;
             }
-            store_elem<T>(D, Ds, r, c, cmk((T)dv.re, (T)dv.im), 0);
+            store_elem<T>(D, Ds, r, c, dv, 0);
         }
-        if (!J.u_trans) { if (ok) store_elem<T>(C, C.slot(J.u_slot), r, c, cmk((T)uv.re, (T)uv.im), 0); }
-        else { tU[0][rl][tx] = (T)uv.re; tU[1][rl][tx] = (T)uv.im; }
-        if (!J.l_trans) { if (ok) store_elem<T>(C, C.slot(J.l_slot), r, c, cmk((T)lv.re, (T)lv.im), 0); }
-        else { tL[0][rl][tx] = (T)lv.re; tL[1][rl][tx] = (T)lv.im; }
+        if (!J.u_trans) { if (ok) store_elem<T>(C, C.slot(J.u_slot), r, c, uv, 0); }
+        else { tU[0][rl][tx] = uv.re; tU[1][rl][tx] = uv.im; }
+        if (!J.l_trans) { if (ok) store_elem<T>(C, C.slot(J.l_slot), r, c, lv, 0); }
+        else { tL[0][rl][tx] = lv.re; tL[1][rl][tx] = lv.im; }
     }
     if (J.u_trans || J.l_trans) {
         __syncthreads();
@@ -142,12 +145,14 @@ __global__ void perm_init_kernel(int* perm, int b) {
 // Blocked in-place Gauss-Jordan inversion with partial pivoting, panel step.
 //
 // For the panel of columns [c0, c0+w) of each matrix M (b x b) the kernel
-//  1. loads the panel M[:, c0:c0+w) into shared memory and runs w column
-//     steps of in-place Gauss-Jordan on it: pivot = largest |re|+|im| among
-//     the rows not yet used as pivots, row swap, pivot row scaled by 1/p with
-//     the pivot entry replaced by 1/p, every other row i updated by
-//     -M[i,j]·(scaled pivot row) with its pivot-column entry set to -M[i,j]/p.
-//     The result G (b x w) holds the panel's block transformation;
+//  1. loads the panel M[:, c0:c0+w) into registers (thread t owns rows t and
+//     t + 512) and runs w column steps of in-place Gauss-Jordan on it: pivot
+//     = largest |re|+|im| among the rows not yet used as pivots (ties: lowest
+//     row), row exchange, pivot row scaled by 1/p with the pivot entry
+//     replaced by 1/p, every other row i updated by -M[i,j]·(scaled pivot row)
+//     with its pivot-column entry set to -M[i,j]/p.  One step costs a block
+//     argmax, a row exchange through shared memory and a broadcast of the
+//     pivot row.  The result G (b x w) holds the panel's block transformation;
 //  2. applies the same row swaps to the full rows of M and records them in perm;
 //  3. writes Rᵀ: the (swapped) panel rows M[c0:c0+w, :] transposed, with the
 //     panel columns replaced by the identity.
@@ -155,119 +160,182 @@ __global__ void perm_init_kernel(int* perm, int b) {
 // mask [c0, c0+w)).  After the last panel M holds (P M₀)⁻¹, and
 // gj_unpermute_kernel restores M₀⁻¹.  The in-place Gauss-Jordan scheme is the
 // textbook one (e.g. G. W. Stewart, Matrix Algorithms I, §3.1).
-// grid: njobs, block 512, dynamic smem (2*b*NB + 2*b)*sizeof(T)
+// grid: njobs, block 512; requires b <= 512*RPT.
 // ---------------------------------------------------------------------------
-template <typename T, int NB>
-__global__ void __launch_bounds__(512) gj_panel_kernel(Pool<T> M, const int* slots, Pool<T> GP, Pool<T> RP,
-                                                       int* perm, int c0, unsigned* err) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    T* pre = reinterpret_cast<T*>(smem_raw);
-    const int b = M.rows;
-    T* pim = pre + (size_t)b * NB;
-    T* fre = pim + (size_t)b * NB;
-    T* fim = fre + b;
-    __shared__ T rowre[NB], rowim[NB];
-    __shared__ int pivs[NB];
-    __shared__ T redv[32];
-    __shared__ int redi[32];
+template <typename T, int NB, int RPT>
+__global__ void __launch_bounds__(512, 1) gj_panel_kernel(Pool<T> M, const int* slots, Pool<T> GP, Pool<T> RP,
+                                                          int* perm, int c0, unsigned* err) {
+    constexpr int NT = 512;
+    __shared__ T xre[2][NB], xim[2][NB];       // row exchange
+    __shared__ T pre_[NB], pim_[NB];           // scaled pivot row
+    __shared__ T redv[NT / 32];
+    __shared__ int redi[NT / 32];
     __shared__ int s_piv;
+    __shared__ int pivs[NB];
 
-    const int tid = threadIdx.x, nt = blockDim.x;
+    const int b = M.rows;
+    const int tid = threadIdx.x;
     const int job = blockIdx.x;
-    const int slot = slots[job];
-    T* Mre = M.slot(slot);
+    T* Mre = M.slot(slots[job]);
     T* Mim = Mre + M.plane_elems();
     const int ld = M.ld;
     const int w = min(NB, b - c0);
 
-    for (int idx = tid; idx < b * NB; idx += nt) {
-        int i = idx / NB, jj = idx % NB;
-        T vr = 0, vi = 0;
-        if (jj < w) { vr = Mre[(size_t)i * ld + c0 + jj]; vi = Mim[(size_t)i * ld + c0 + jj]; }
-        pre[idx] = vr; pim[idx] = vi;
+    T vr[RPT][NB], vi[RPT][NB];
+#pragma unroll
+    for (int t = 0; t < RPT; ++t) {
+        const int i = tid + t * NT;
+#pragma unroll
+        for (int jj = 0; jj < NB; ++jj) {
+            T a = 0, c = 0;
+            if (i < b && jj < w) { a = Mre[(size_t)i * ld + c0 + jj]; c = Mim[(size_t)i * ld + c0 + jj]; }
+            vr[t][jj] = a;
+            vi[t][jj] = c;
+        }
     }
-    __syncthreads();
 
-    for (int jj = 0; jj < w; ++jj) {
-        const int r0 = c0 + jj;
-        T best = (T)-1; int bi = b;
-        for (int i = r0 + tid; i < b; i += nt) {
-            T v = fabs(pre[i * NB + jj]) + fabs(pim[i * NB + jj]);
-            if (v > best) { best = v; bi = i; }
-        }
-        for (int o = 16; o > 0; o >>= 1) {
-            T ov = __shfl_down_sync(0xffffffffu, best, o);
-            int oi = __shfl_down_sync(0xffffffffu, bi, o);
-            if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
-        }
-        if ((tid & 31) == 0) { redv[tid >> 5] = best; redi[tid >> 5] = bi; }
-        __syncthreads();
-        if (tid < 32) {
-            int nw = nt >> 5;
-            best = tid < nw ? redv[tid] : (T)-1;
-            bi = tid < nw ? redi[tid] : b;
+#pragma unroll
+    for (int jj = 0; jj < NB; ++jj) {
+        if (jj < w) {
+            const int r0 = c0 + jj;
+            // ---- block argmax over rows >= r0 of column jj
+            T best = (T)-1;
+            int bi = b;
+#pragma unroll
+            for (int t = 0; t < RPT; ++t) {
+                const int i = tid + t * NT;
+                if (i >= r0 && i < b) {
+                    const T v = fabs(vr[t][jj]) + fabs(vi[t][jj]);
+                    if (v > best) { best = v; bi = i; }
+                }
+            }
+#pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
-                T ov = __shfl_down_sync(0xffffffffu, best, o);
-                int oi = __shfl_down_sync(0xffffffffu, bi, o);
+                const T ov = __shfl_down_sync(0xffffffffu, best, o);
+                const int oi = __shfl_down_sync(0xffffffffu, bi, o);
                 if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
             }
-            if (tid == 0) {
-                if (!(best > (T)0) || bi >= b || !isfinite((double)best)) {
-                    dev_error(err, FDFD_DEVERR_SINGULAR);
-                    bi = r0;
+            if ((tid & 31) == 0) { redv[tid >> 5] = best; redi[tid >> 5] = bi; }
+            __syncthreads();
+            if (tid < 32) {
+                best = tid < NT / 32 ? redv[tid] : (T)-1;
+                bi = tid < NT / 32 ? redi[tid] : b;
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    const T ov = __shfl_down_sync(0xffffffffu, best, o);
+                    const int oi = __shfl_down_sync(0xffffffffu, bi, o);
+                    if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
                 }
-                s_piv = bi;
-                pivs[jj] = bi;
+                if (tid == 0) {
+                    if (!(best > (T)0) || bi >= b || !isfinite((double)best)) {
+                        dev_error(err, FDFD_DEVERR_SINGULAR);
+                        bi = r0;
+                    }
+                    s_piv = bi;
+                    pivs[jj] = bi;
+                }
+            }
+            __syncthreads();
+            const int piv = s_piv;
+            const int o0 = r0 % NT, t0 = r0 / NT;      // owner of position r0
+            const int op = piv % NT, tp = piv / NT;    // owner of the pivot row
+            // ---- exchange rows r0 and piv through shared memory
+            if (piv != r0) {
+#pragma unroll
+                for (int t = 0; t < RPT; ++t) {
+                    if (tid == o0 && t == t0)
+#pragma unroll
+                        for (int k = 0; k < NB; ++k) { xre[0][k] = vr[t][k]; xim[0][k] = vi[t][k]; }
+                    if (tid == op && t == tp)
+#pragma unroll
+                        for (int k = 0; k < NB; ++k) { xre[1][k] = vr[t][k]; xim[1][k] = vi[t][k]; }
+                }
+                __syncthreads();
+#pragma unroll
+                for (int t = 0; t < RPT; ++t) {
+                    if (tid == o0 && t == t0)
+#pragma unroll
+                        for (int k = 0; k < NB; ++k) { vr[t][k] = xre[1][k]; vi[t][k] = xim[1][k]; }
+                    if (tid == op && t == tp)
+#pragma unroll
+                        for (int k = 0; k < NB; ++k) { vr[t][k] = xre[0][k]; vi[t][k] = xim[0][k]; }
+                }
+            }
+            // ---- the owner of r0 scales the pivot row and publishes it
+#pragma unroll
+            for (int t = 0; t < RPT; ++t) {
+                if (tid == o0 && t == t0) {
+                    const cplx<T> p = cmk(vr[t][jj], vi[t][jj]);
+                    const cplx<T> inv = (p.re == (T)0 && p.im == (T)0) ? cmk((T)0, (T)0) : cinv(p);
+#pragma unroll
+                    for (int k = 0; k < NB; ++k) {
+                        cplx<T> v = (k == jj) ? inv : cmul(cmk(vr[t][k], vi[t][k]), inv);
+                        if (k >= w) v = cmk((T)0, (T)0);
+                        pre_[k] = v.re;
+                        pim_[k] = v.im;
+                        vr[t][k] = v.re;
+                        vi[t][k] = v.im;
+                    }
+                }
+            }
+            __syncthreads();
+            // ---- eliminate column jj from every other row
+            const cplx<T> inv = cmk(pre_[jj], pim_[jj]);
+#pragma unroll
+            for (int t = 0; t < RPT; ++t) {
+                const int i = tid + t * NT;
+                if (i < b && i != r0) {
+                    const cplx<T> f = cmk(vr[t][jj], vi[t][jj]);
+#pragma unroll
+                    for (int k = 0; k < NB; ++k) {
+                        if (k == jj) {
+                            const cplx<T> v = cneg(cmul(f, inv));
+                            vr[t][k] = v.re;
+                            vi[t][k] = v.im;
+                        } else {
+                            const cplx<T> prk = cmk(pre_[k], pim_[k]);
+                            vr[t][k] -= f.re * prk.re - f.im * prk.im;
+                            vi[t][k] -= f.re * prk.im + f.im * prk.re;
+                        }
+                    }
+                }
             }
         }
-        __syncthreads();
-        const int piv = s_piv;
-        if (piv != r0 && tid < NB) {
-            T a = pre[r0 * NB + tid]; pre[r0 * NB + tid] = pre[piv * NB + tid]; pre[piv * NB + tid] = a;
-            T c = pim[r0 * NB + tid]; pim[r0 * NB + tid] = pim[piv * NB + tid]; pim[piv * NB + tid] = c;
-        }
-        __syncthreads();
-        cplx<T> p = cmk(pre[r0 * NB + jj], pim[r0 * NB + jj]);
-        cplx<T> inv = (p.re == (T)0 && p.im == (T)0) ? cmk((T)0, (T)0) : cinv(p);
-        for (int i = tid; i < b; i += nt) { fre[i] = pre[i * NB + jj]; fim[i] = pim[i * NB + jj]; }
-        if (tid < NB) {
-            cplx<T> v = cmk((T)0, (T)0);
-            if (tid < w) v = (tid == jj) ? inv : cmul(cmk(pre[r0 * NB + tid], pim[r0 * NB + tid]), inv);
-            rowre[tid] = v.re; rowim[tid] = v.im;
-        }
-        __syncthreads();
-        for (int idx = tid; idx < b * NB; idx += nt) {
-            int i = idx / NB, j2 = idx % NB;
-            if (j2 >= w) continue;
-            if (i == r0) {
-                pre[idx] = rowre[j2]; pim[idx] = rowim[j2];
-            } else {
-                cplx<T> f = cmk(fre[i], fim[i]);
-                cplx<T> nv;
-                if (j2 == jj) nv = cneg(cmul(f, inv));
-                else nv = csub(cmk(pre[idx], pim[idx]), cmul(f, cmk(rowre[j2], rowim[j2])));
-                pre[idx] = nv.re; pim[idx] = nv.im;
-            }
-        }
-        __syncthreads();
     }
 
     // 1. G panel (b x GP.cols, zero padded)
     {
         T* g = GP.slot(job);
-        const int gc = GP.cols;
-        for (int idx = tid; idx < b * gc; idx += nt) {
-            int i = idx / gc, k = idx % gc;
-            cplx<T> v = cmk((T)0, (T)0);
-            if (k < w) v = cmk(pre[i * NB + k], pim[i * NB + k]);
-            store_elem<T>(GP, g, i, k, v, 0);
+        const long long pe = GP.plane_elems();
+#pragma unroll
+        for (int t = 0; t < RPT; ++t) {
+            const int i = tid + t * NT;
+            if (i < b) {
+#pragma unroll
+                for (int k = 0; k < NB; ++k) {     // GP.cols >= NB; columns >= w are zero already
+                    const long long o = (long long)i * GP.ld + k;
+                    g[o] = vr[t][k];
+                    g[pe + o] = vi[t][k];
+                    if (GP.planes == 4) {
+                        g[2 * pe + o] = (T)tf32_lo((float)vr[t][k]);
+                        g[3 * pe + o] = (T)tf32_lo((float)vi[t][k]);
+                    }
+                }
+                for (int k = NB; k < GP.cols; ++k) {
+                    const long long o = (long long)i * GP.ld + k;
+                    g[o] = 0;
+                    g[pe + o] = 0;
+                    if (GP.planes == 4) { g[2 * pe + o] = 0; g[3 * pe + o] = 0; }
+                }
+            }
         }
     }
+    __syncthreads();
     // 2. row swaps on the full matrix, in order
     for (int jj = 0; jj < w; ++jj) {
-        int r0 = c0 + jj, piv = pivs[jj];
+        const int r0 = c0 + jj, piv = pivs[jj];
         if (piv != r0) {
-            for (int c = tid; c < b; c += nt) {
+            for (int c = tid; c < b; c += NT) {
                 T a = Mre[(size_t)r0 * ld + c]; Mre[(size_t)r0 * ld + c] = Mre[(size_t)piv * ld + c];
                 Mre[(size_t)piv * ld + c] = a;
                 T d = Mim[(size_t)r0 * ld + c]; Mim[(size_t)r0 * ld + c] = Mim[(size_t)piv * ld + c];
@@ -284,8 +352,8 @@ __global__ void __launch_bounds__(512) gj_panel_kernel(Pool<T> M, const int* slo
     {
         T* rt = RP.slot(job);
         const int rc = RP.cols;
-        for (int idx = tid; idx < b * rc; idx += nt) {
-            int k = idx / b, c = idx % b;    // c fastest: coalesced reads of M rows
+        for (int idx = tid; idx < b * rc; idx += NT) {
+            const int k = idx / b, c = idx % b;    // c fastest: coalesced reads of M rows
             cplx<T> v = cmk((T)0, (T)0);
             if (k < w) {
                 if (c >= c0 && c < c0 + w) v = cmk((T)((c - c0) == k ? 1 : 0), (T)0);
@@ -366,8 +434,187 @@ __global__ void mcopy_kernel(Pool<T> S, Pool<T> Dp, const int3* jobs) {
 }
 
 // ---------------------------------------------------------------------------
+// Inverse of the cyclic tridiagonal blocks of the first reduction step, O(b²).
+//
+// D_k = T0 + a0·e_0·e_{b-1}ᵀ + cN·e_{b-1}·e_0ᵀ with T0 tridiagonal (the in-line
+// neighbours without the periodic wrap) and the two corner terms of the wrap.
+// T0 is factored with partial pivoting by the recurrences of LAPACK's
+// xGTTRF (row interchanges between neighbours, a second superdiagonal du2),
+// Z = T0⁻¹ is formed column by column with the xGTTRS recurrences (thread j
+// solves T0 z = e_j), and the corners are added back by the Sherman-Morrison-
+// Woodbury identity with the 2x2 capacitance matrix S = I + Vᵀ Z U:
+//     D_k⁻¹ = Z − [Z[:,0], Z[:,b−1]] · S⁻¹ · [a0·Z[b−1,:] ; cN·Z[0,:]].
+// Result (with TF32 residual planes) in the D-pool slot of the node.
+// grid: njobs, block 512, dynamic smem 6*b*sizeof(cplx<T>) + b*sizeof(int)
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(512) tri_inverse_kernel(NodeMap m, const cplx<double>* st, double scale, Pool<T> D,
+                                                          const int* nodes, unsigned* err) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int b = m.b;
+    cplx<T>* dl = reinterpret_cast<cplx<T>*>(smem_raw);
+    cplx<T>* dd = dl + b;      // diagonal, then its reciprocal
+    cplx<T>* du = dd + b;
+    cplx<T>* du2 = du + b;
+    cplx<T>* z0 = du2 + b;     // Z[:, 0]
+    cplx<T>* zN = z0 + b;      // Z[:, b-1]
+    int* ipiv = reinterpret_cast<int*>(zN + b);
+    __shared__ cplx<T> s_inv[4];
+    __shared__ cplx<T> s_a0, s_cN;
+    __shared__ int s_bad;
+
+    const int node = nodes[blockIdx.x];
+    const int tid = threadIdx.x, nt = blockDim.x;
+    T* Gre = D.slot(node);
+    const long long pe = D.plane_elems();
+    T* Gim = Gre + pe;
+    const int ld = D.ld;
+    auto coef = [&](int plane, int i) {
+        cplx<double> v = cscale(st_at<T>(st, m, plane, node, i), scale);
+        return cmk((T)v.re, (T)v.im);
+    };
+    for (int i = tid; i < b; i += nt) {
+        dd[i] = coef(0, i);
+        dl[i] = (i + 1 < b) ? coef(m.p_inprev(), i + 1) : cmk((T)0, (T)0);   // T0[i+1][i]
+        du[i] = (i + 1 < b) ? coef(m.p_innext(), i) : cmk((T)0, (T)0);      // T0[i][i+1]
+        du2[i] = cmk((T)0, (T)0);
+        ipiv[i] = i;
+    }
+    if (tid == 0) {
+        s_a0 = coef(m.p_inprev(), 0);        // D[0][b-1]
+        s_cN = coef(m.p_innext(), b - 1);    // D[b-1][0]
+        s_bad = 0;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        // xGTTRF recurrences (partial pivoting between neighbouring rows)
+        for (int i = 0; i + 1 < b; ++i) {
+            if (cabs1(dd[i]) >= cabs1(dl[i])) {
+                if (cabs1(dd[i]) > (T)0) {
+                    cplx<T> fact = cmul(dl[i], cinv(dd[i]));
+                    dl[i] = fact;
+                    dd[i + 1] = csub(dd[i + 1], cmul(fact, du[i]));
+                }
+            } else {
+                cplx<T> fact = cmul(dd[i], cinv(dl[i]));
+                dd[i] = dl[i];
+                dl[i] = fact;
+                cplx<T> temp = du[i];
+                du[i] = dd[i + 1];
+                dd[i + 1] = csub(temp, cmul(fact, dd[i + 1]));
+                if (i + 2 < b) {
+                    du2[i] = du[i + 1];
+                    du[i + 1] = cneg(cmul(fact, du[i + 1]));
+                }
+                ipiv[i] = i + 1;
+            }
+        }
+        for (int i = 0; i < b; ++i) {
+            if (!(cabs1(dd[i]) > (T)0) || !isfinite((double)cabs1(dd[i]))) { s_bad = 1; dd[i] = cmk((T)1, (T)0); }
+            dd[i] = cinv(dd[i]);
+        }
+    }
+    __syncthreads();
+    // Z = T0⁻¹, column j per thread (xGTTRS recurrences with right-hand side e_j)
+    for (int j = tid; j < b; j += nt) {
+        cplx<T> cur = cmk((T)(j == 0 ? 1 : 0), (T)0);
+        for (int i = 0; i + 1 < b; ++i) {
+            cplx<T> nxt = cmk((T)(i + 1 == j ? 1 : 0), (T)0);
+            cplx<T> yi;
+            if (ipiv[i] == i) {
+                yi = cur;
+                nxt = csub(nxt, cmul(dl[i], cur));
+            } else {
+                yi = nxt;
+                nxt = csub(cur, cmul(dl[i], nxt));
+            }
+            Gre[(size_t)i * ld + j] = yi.re;
+            Gim[(size_t)i * ld + j] = yi.im;
+            cur = nxt;
+        }
+        // back substitution with U (diagonal, du, du2); y read back in blocks of 8 rows
+        cplx<T> x1 = cmul(cur, dd[b - 1]);          // x[b-1]
+        Gre[(size_t)(b - 1) * ld + j] = x1.re;
+        Gim[(size_t)(b - 1) * ld + j] = x1.im;
+        cplx<T> x2 = cmk((T)0, (T)0);               // x[i+2]
+        int i = b - 2;
+        while (i >= 0) {
+            const int n8 = min(8, i + 1);
+            cplx<T> yv[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u)
+                if (u < n8) yv[u] = cmk(Gre[(size_t)(i - u) * ld + j], Gim[(size_t)(i - u) * ld + j]);
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                if (u < n8) {
+                    const int r = i - u;
+                    cplx<T> s = csub(yv[u], cmul(du[r], x1));
+                    if (r + 2 < b) s = csub(s, cmul(du2[r], x2));
+                    const cplx<T> xr = cmul(s, dd[r]);
+                    Gre[(size_t)r * ld + j] = xr.re;
+                    Gim[(size_t)r * ld + j] = xr.im;
+                    x2 = x1;
+                    x1 = xr;
+                }
+            }
+            i -= n8;
+        }
+    }
+    __syncthreads();
+    for (int i = tid; i < b; i += nt) {
+        z0[i] = cmk(Gre[(size_t)i * ld], Gim[(size_t)i * ld]);
+        zN[i] = cmk(Gre[(size_t)i * ld + b - 1], Gim[(size_t)i * ld + b - 1]);
+    }
+    __syncthreads();
+    if (tid == 0) {
+        // S = I + [[a0 Z[b-1][0], a0 Z[b-1][b-1]], [cN Z[0][0], cN Z[0][b-1]]]
+        const cplx<T> s00 = cadd(cmk((T)1, (T)0), cmul(s_a0, z0[b - 1]));
+        const cplx<T> s01 = cmul(s_a0, zN[b - 1]);
+        const cplx<T> s10 = cmul(s_cN, z0[0]);
+        const cplx<T> s11 = cadd(cmk((T)1, (T)0), cmul(s_cN, zN[0]));
+        const cplx<T> det = csub(cmul(s00, s11), cmul(s01, s10));
+        if (!(cabs1(det) > (T)0)) s_bad = 1;
+        const cplx<T> id = cabs1(det) > (T)0 ? cinv(det) : cmk((T)0, (T)0);
+        s_inv[0] = cmul(s11, id);
+        s_inv[1] = cneg(cmul(s01, id));
+        s_inv[2] = cneg(cmul(s10, id));
+        s_inv[3] = cmul(s00, id);
+        if (s_bad) dev_error(err, FDFD_DEVERR_SINGULAR);
+    }
+    __syncthreads();
+    // Woodbury correction, column j per thread; writes the TF32 residual planes too
+    for (int j = tid; j < b; j += nt) {
+        const cplx<T> v0 = cmul(s_a0, cmk(Gre[(size_t)(b - 1) * ld + j], Gim[(size_t)(b - 1) * ld + j]));
+        const cplx<T> v1 = cmul(s_cN, cmk(Gre[j], Gim[j]));
+        const cplx<T> w0 = cadd(cmul(s_inv[0], v0), cmul(s_inv[1], v1));
+        const cplx<T> w1 = cadd(cmul(s_inv[2], v0), cmul(s_inv[3], v1));
+        // column j is read and rewritten by this thread only (columns 0 and b-1 are in z0, zN)
+        for (int i0 = 0; i0 < b; i0 += 8) {
+            cplx<T> zv[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u)
+                if (i0 + u < b) zv[u] = cmk(Gre[(size_t)(i0 + u) * ld + j], Gim[(size_t)(i0 + u) * ld + j]);
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const int i = i0 + u;
+                if (i < b) {
+                    const cplx<T> g = csub(csub(zv[u], cmul(z0[i], w0)), cmul(zN[i], w1));
+                    store_elem<T>(D, Gre, i, j, g, 0);
+                }
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Host launchers
 // ---------------------------------------------------------------------------
+template <typename T>
+void launch_tri_inverse(cudaStream_t s, int njobs, NodeMap m, const cplx<double>* st, double scale, Pool<T> D,
+                        const int* nodes, unsigned* err) {
+    size_t smem = 6 * (size_t)m.b * sizeof(cplx<T>) + (size_t)m.b * sizeof(int);
+    tri_inverse_kernel<T><<<njobs, 512, smem, s>>>(m, st, scale, D, nodes, err);
+}
 template <typename T>
 void launch_build_tridiag(cudaStream_t s, int njobs, NodeMap m, const cplx<double>* st, double scale, Pool<T> D,
                           const int* nodes) {
@@ -382,29 +629,21 @@ void launch_level1_combine(cudaStream_t s, int njobs, NodeMap m, const cplx<doub
 void launch_perm_init(cudaStream_t s, int njobs, int* perm, int b) {
     perm_init_kernel<int><<<dim3(ceil_div(b, 256), njobs), 256, 0, s>>>(perm, b);
 }
-template <typename T, int NB>
-static int gj_panel_nb(cudaStream_t s, int njobs, Pool<T> M, const int* slots, Pool<T> GP, Pool<T> RP, int* perm,
-                       int c0, unsigned* err) {
-    static bool attr = false;
-    if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(gj_panel_kernel<T, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             220 * 1024);
-        if (e != cudaSuccess) return (int)e;
-        attr = true;
-    }
-    size_t smem = ((size_t)2 * M.rows * NB + 2 * M.rows) * sizeof(T);
-    gj_panel_kernel<T, NB><<<njobs, 512, smem, s>>>(M, slots, GP, RP, perm, c0, err);
-    return (int)cudaGetLastError();
-}
 template <typename T>
 int launch_gj_panel(cudaStream_t s, int nb, int njobs, Pool<T> M, const int* slots, Pool<T> GP, Pool<T> RP,
                     int* perm, int c0, unsigned* err) {
-    switch (nb) {
-        case 32: return gj_panel_nb<T, 32>(s, njobs, M, slots, GP, RP, perm, c0, err);
-        case 16: return gj_panel_nb<T, 16>(s, njobs, M, slots, GP, RP, perm, c0, err);
-        case 8: return gj_panel_nb<T, 8>(s, njobs, M, slots, GP, RP, perm, c0, err);
-        default: return (int)cudaErrorInvalidValue;
+    const bool two = M.rows > 512;
+    if (M.rows > 1024) return (int)cudaErrorInvalidValue;
+    if constexpr (sizeof(T) == 4) {
+        if (nb == 32 && !two) gj_panel_kernel<T, 32, 1><<<njobs, 512, 0, s>>>(M, slots, GP, RP, perm, c0, err);
+        else if (nb == 16 && two) gj_panel_kernel<T, 16, 2><<<njobs, 512, 0, s>>>(M, slots, GP, RP, perm, c0, err);
+        else return (int)cudaErrorInvalidValue;
+    } else {
+        if (nb == 16 && !two) gj_panel_kernel<T, 16, 1><<<njobs, 512, 0, s>>>(M, slots, GP, RP, perm, c0, err);
+        else if (nb == 8 && two) gj_panel_kernel<T, 8, 2><<<njobs, 512, 0, s>>>(M, slots, GP, RP, perm, c0, err);
+        else return (int)cudaErrorInvalidValue;
     }
+    return (int)cudaGetLastError();
 }
 template <typename T>
 void launch_gj_unpermute(cudaStream_t s, int njobs, Pool<T> M, const int* slots, const int* perm) {
@@ -428,6 +667,8 @@ void launch_mcopy(cudaStream_t s, int njobs, Pool<T> S, Pool<T> Dp, const int3* 
                                     unsigned*);                                                              \
     template void launch_gj_unpermute<T>(cudaStream_t, int, Pool<T>, const int*, const int*);                \
     template void launch_madd<T>(cudaStream_t, int, Pool<T>, const int3*);                                    \
-    template void launch_mcopy<T>(cudaStream_t, int, Pool<T>, Pool<T>, const int3*);
+    template void launch_mcopy<T>(cudaStream_t, int, Pool<T>, Pool<T>, const int3*);                         \
+    template void launch_tri_inverse<T>(cudaStream_t, int, NodeMap, const cplx<double>*, double, Pool<T>,    \
+                                        const int*, unsigned*);
 INST(float)
 INST(double)

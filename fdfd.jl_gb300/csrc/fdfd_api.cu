@@ -142,6 +142,7 @@ struct fdfd_handle {
     double last_factor_flops = 0;
     int tc_used = 0;
     bool use_tc = true;
+    bool level1_gj = false;     // invert first-step blocks by Gauss-Jordan instead of the O(b²) kernel
     // profiling (CUDA events around launches on the handle's stream)
     struct ProfRec { int cls, e0, e1; double work; };
     bool prof_on = false;
@@ -461,9 +462,11 @@ template <typename T> FactorStore<T>& store(fdfd_handle* h);
 template <> FactorStore<float>& store<float>(fdfd_handle* h) { return h->f32; }
 template <> FactorStore<double>& store<double>(fdfd_handle* h) { return h->f64; }
 
+// Gauss-Jordan panel width: the panel lives in registers, one (b <= 512) or two
+// (b <= 1024) rows per thread of a 512-thread block.
 template <typename T> int panel_nb(int b) {
-    if (sizeof(T) == 4) return b <= 800 ? 32 : 16;
-    return b <= 768 ? 16 : 8;
+    if (sizeof(T) == 4) return b <= 512 ? 32 : 16;
+    return b <= 512 ? 16 : 8;
 }
 
 template <typename T> int alloc_pool(fdfd_handle* h, Pool<T>& P, int rows, int cols, int ld, int planes,
@@ -530,7 +533,7 @@ template <typename T> Pool<T>& pool_of(FactorStore<T>& F, int id) {
 template <typename T>
 int gemm(fdfd_handle* h, int pa, int pb, int pc, const int* a_slot, const int* b_slot, const int* c_slot,
          const int* c_trans_arr, int c_trans, int njobs, int M, int N, int K, T alpha, int beta, int mask_c0,
-         int mask_w) {
+         int mask_w, int write_lo = 1) {
     if (njobs == 0) return FDFD_OK;
     FactorStore<T>& F = store<T>(h);
     GemmArgs<T> g;
@@ -539,6 +542,7 @@ int gemm(fdfd_handle* h, int pa, int pb, int pc, const int* a_slot, const int* b
     g.M = M; g.N = N; g.K = K; g.alpha = alpha; g.beta = beta;
     g.mask_c0 = mask_c0; g.mask_w = mask_w; g.c_trans = c_trans;
     g.c_trans_arr = nullptr;
+    g.write_lo = write_lo;
     g.err = h->derr;
     const double flops = 8.0 * M * N * K * njobs;
     int ev = prof_begin(h);
@@ -575,8 +579,9 @@ template <typename T> int gj_invert(fdfd_handle* h, const int* d_slots, const in
         prof_end(h, ev, FDFD_PROF_GJ_PANEL, 0.0);
         h->launches++;
         if (e) return set_err(h, FDFD_ECUDA, "gj_panel launch failed: %s", cudaGetErrorString((cudaError_t)e));
+        // no residual planes here: gj_unpermute_kernel rewrites every element of the inverse
         RET(gemm<T>(h, P_GP, P_RP, P_D, d_iota, d_iota, d_slots, nullptr, 0, njobs, b, b, F.GP.cols, (T)1, 1,
-                    c0, w));
+                    c0, w, 0));
     }
     launch_gj_unpermute<T>(h->stream, njobs, F.D, d_slots, F.perm);
     h->launches++;
@@ -597,11 +602,19 @@ template <typename T> int factor_impl(fdfd_handle* h) {
         const StepJobs& S = h->sj[e];
         const int ne = S.ne;
         if (e == 1) {
-            launch_build_tridiag<T>(h->stream, ne, h->map, h->st, h->scale, F.D, J<int>(h, S.elim));
-            h->launches++;
-            RET(check_launch(h, "build_tridiag"));
-            RET(gj_invert<T>(h, J<int>(h, S.elim), J<int>(h, S.iota), ne));
-            flops += 8.0 * b3 * ne;
+            if (h->level1_gj) {
+                launch_build_tridiag<T>(h->stream, ne, h->map, h->st, h->scale, F.D, J<int>(h, S.elim));
+                h->launches++;
+                RET(check_launch(h, "build_tridiag"));
+                RET(gj_invert<T>(h, J<int>(h, S.elim), J<int>(h, S.iota), ne));
+                flops += 8.0 * b3 * ne;
+            } else {
+                int ev = prof_begin(h);
+                launch_tri_inverse<T>(h->stream, ne, h->map, h->st, h->scale, F.D, J<int>(h, S.elim), h->derr);
+                prof_end(h, ev, FDFD_PROF_OTHER, 0.0);
+                h->launches++;
+                RET(check_launch(h, "tri_inverse"));
+            }
             launch_level1_combine<T>(h->stream, S.nl1, h->map, h->st, h->scale, F.D, F.C, J<L1Job>(h, S.l1));
             h->launches++;
             RET(check_launch(h, "level1_combine"));
@@ -650,8 +663,7 @@ template <typename T> int gemv(fdfd_handle* h, int tr, int p1, int p2, const T* 
     if (njobs == 0) return FDFD_OK;
     FactorStore<T>& F = store<T>(h);
     const int b = h->map.b;
-    int rmax = (int)std::min<size_t>(8, (size_t)(150 * 1024) / ((size_t)4 * b * sizeof(T)));
-    if (rmax < 1) rmax = 1;
+    const int rmax = gemv_max_rhs<T>(b);
     for (int r0 = 0; r0 < nrhs; r0 += rmax) {
         GemvArgs<T> g;
         g.P1 = pool_of(F, p1); g.P2 = pool_of(F, p2);
@@ -1002,13 +1014,15 @@ int fdfd_create(fdfd_handle** out, int Nx, int Ny, int Npx, int Npy, double dx, 
     if (!(dx > 0) || !(dy > 0) || !(L0 > 0) || !std::isfinite(pml_m) || !std::isfinite(pml_lnR)) return FDFD_EINVAL;
     if (pol != FDFD_TM && pol != FDFD_TE) return FDFD_EINVAL;
     if (precision != FDFD_PREC_FP64 && precision != FDFD_PREC_MIXED) return FDFD_EINVAL;
-    if (std::min(Nx, Ny) > 2048) return FDFD_EINVAL;
+    if (std::min(Nx, Ny) > 1024) return FDFD_EINVAL;   // dense block size limit of the panel kernel
     fdfd_handle* h = new fdfd_handle();
     h->Nx = Nx; h->Ny = Ny; h->Npx = Npx; h->Npy = Npy;
     h->dx = dx; h->dy = dy; h->L0 = L0; h->pml_m = pml_m; h->pml_lnR = pml_lnR;
     h->pol = pol; h->precision = precision;
     const char* env = getenv("FDFD_DISABLE_TC");
     if (env && env[0] == '1') h->use_tc = false;
+    const char* env1 = getenv("FDFD_LEVEL1_GJ");
+    if (env1 && env1[0] == '1') h->level1_gj = true;
     NodeMap& m = h->map;
     m.Nx = Nx; m.Ny = Ny;
     m.transposed = Nx > Ny ? 1 : 0;
@@ -1254,8 +1268,84 @@ int fdfd_apply(fdfd_handle* h, const double* x, int nrhs, double* y) {
 
 int fdfd_adjoint(fdfd_handle* h, const double* src, const double* mvec, double* J, double* grad, double* ez,
                  fdfd_stats* stats) {
-    (void)src; (void)mvec; (void)J; (void)grad; (void)ez; (void)stats;
-    return h ? set_err(h, FDFD_EINVAL, "fdfd_adjoint: not available in this build") : FDFD_EINVAL;
+    if (!h) return FDFD_EINVAL;
+    if (!src || !mvec || !J || !grad) return set_err(h, FDFD_EINVAL, "fdfd_adjoint: NULL argument");
+    if (!h->factored || h->op != OP_TM_DRIVEN)
+        return set_err(h, FDFD_EINVAL, "fdfd_adjoint needs a factored TM driven operator (fdfd_factor, FDFD_TM)");
+    auto t0 = std::chrono::steady_clock::now();
+    const long long N = (long long)h->Nx * h->Ny;
+    for (long long k = 0; k < 2 * N; ++k)
+        if (!std::isfinite(src[k]) || !std::isfinite(mvec[k]))
+            return set_err(h, FDFD_EINVAL, "fdfd_adjoint: non-finite input");
+    const size_t bytes = (size_t)N * sizeof(cplx<double>);
+    RET(ensure_krylov(h, 2, 20));
+    if (h->io_cap < 4 * bytes) {
+        dev_free(h->io);
+        h->io = nullptr;
+        h->dev_bytes -= (long long)h->io_cap;
+        h->io_cap = 0;
+        RET(dev_alloc(h, (void**)&h->io, 4 * bytes));
+        h->io_cap = 4 * bytes;
+    }
+    cplx<double>* d_src = h->io;
+    cplx<double>* d_m = h->io + N;
+    cplx<double>* d_lam = h->io + 2 * N;
+    double* d_grad = reinterpret_cast<double*>(h->io + 3 * N);
+    CK(cudaMemcpyAsync(d_src, src, bytes, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(d_m, mvec, bytes, cudaMemcpyHostToDevice, h->stream));
+    cudaEventRecord(h->ev[3], h->stream);
+    // right-hand sides: E solves A E = iω·src; μ solves A μ = P⁻¹ m, so that
+    // λ = P μ solves Aᵀ λ = m (P·A is complex symmetric for P = diag(s_xf s_yf)).
+    std::vector<zd> iw(1, zd(0, h->omega));
+    RET(scale_vec(h, d_src, iw, 1, h->kb));
+    const int nb = ceil_div(N, 256);
+    LAUNCH(pscale_kernel, nb, 256, 0, h->Nx, h->Ny, h->sf, 0, d_m, h->kb + N);
+    int iters = 0;
+    double rel = 0;
+    RET(refine(h, 2, &iters, &rel));
+    LAUNCH(pscale_kernel, nb, 256, 0, h->Nx, h->Ny, h->sf, 1, h->kx + N, d_lam);
+    // s = mᵀE (no conjugation), reduced on the host from per-block partials
+    RET(ensure_part(h, 2 * 152));
+    LAUNCH(vdotu_kernel, 152, 256, 0, N, d_m, h->kx, h->part);
+    std::vector<double> part(2 * 152);
+    CK(cudaMemcpyAsync(part.data(), h->part, part.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    zd s(0, 0);
+    for (int i = 0; i < 152; ++i) s += zd(part[2 * i], part[2 * i + 1]);
+    // dJ/dϵᵣ_k = -2 Re(conj(s)·ω²ϵ₀·λ_k·E_k)
+    const zd coef = std::conj(s) * (h->omega * h->omega * kEPS0 * h->L0);
+    cplx<double> c;
+    c.re = coef.real();
+    c.im = coef.imag();
+    LAUNCH(adjoint_grad_kernel, nb, 256, 0, N, c, d_lam, h->kx, d_grad);
+    RET(check_launch(h, "adjoint"));
+    CK(cudaMemcpyAsync(grad, d_grad, N * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    if (ez) CK(cudaMemcpyAsync(ez, h->kx, bytes, cudaMemcpyDeviceToHost, h->stream));
+    cudaEventRecord(h->ev[4], h->stream);
+    CK(cudaStreamSynchronize(h->stream));
+    RET(check_device(h, "adjoint"));
+    *J = std::norm(s);
+    if (stats) {
+        stats->iterations = iters;
+        stats->nrhs = 2;
+        stats->rel_residual = rel;
+        stats->t_assemble_ms = elapsed_ms(h->ev[0], h->ev[1]);
+        stats->t_factor_ms = elapsed_ms(h->ev[1], h->ev[2]);
+        stats->t_solve_ms = elapsed_ms(h->ev[3], h->ev[4]);
+        stats->t_recover_ms = 0;
+        stats->factor_flops = h->last_factor_flops;
+        stats->block = h->map.b;
+        stats->nblocks = h->map.n;
+        stats->levels = (int)h->steps.size() + 1;
+        stats->tc_gemm = h->tc_used;
+        stats->device_bytes = h->dev_bytes;
+        stats->gpu_launches = h->launches;
+        stats->t_total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    }
+    if (!(rel <= h->tol))
+        return set_err(h, FDFD_ENOCONV, "adjoint refinement stopped at relative residual %.3e > tol %.1e", rel,
+                       h->tol);
+    return FDFD_OK;
 }
 
 int fdfd_eigfreq(fdfd_handle* h, double omega0, int nev, int which, double tol, double* omega, double* lambda,
@@ -1318,7 +1408,7 @@ int debug_gemm_impl(int M, int N, int K, const double* A, const double* B, doubl
         g.A = PA; g.B = PB; g.C = PC;
         g.a_slot = g.b_slot = g.c_slot = slots;
         g.M = M; g.N = N; g.K = K; g.alpha = (T)1; g.beta = 0; g.mask_c0 = 0; g.mask_w = 0;
-        g.c_trans = 0; g.c_trans_arr = nullptr; g.err = derr;
+        g.c_trans = 0; g.c_trans_arr = nullptr; g.write_lo = 1; g.err = derr;
         cudaEvent_t e0, e1;
         cudaEventCreate(&e0); cudaEventCreate(&e1);
         if (sizeof(T) == 4 && use_tc) {

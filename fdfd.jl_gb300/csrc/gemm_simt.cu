@@ -81,7 +81,7 @@ __global__ void __launch_bounds__(256) gemm_simt_kernel(GemmArgs<T> g) {
             if (g.beta && !masked) { vr += C[off]; vi += C[cpe + off]; }
             C[off] = vr;
             C[cpe + off] = vi;
-            if (g.C.planes == 4) {
+            if (g.C.planes == 4 && g.write_lo) {
                 C[2 * cpe + off] = (T)tf32_lo((float)vr);
                 C[3 * cpe + off] = (T)tf32_lo((float)vi);
             }

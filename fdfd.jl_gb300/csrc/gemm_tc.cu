@@ -246,7 +246,7 @@ __global__ void __launch_bounds__(192, 1)
             const long long ld = g.C.ld;
             const uint32_t lane_off = (uint32_t)(q * 32) << 16;
             // per-warp staging tile (the pipeline buffers are idle once the accumulator is final)
-            float* stg = reinterpret_cast<float*>(smem) + q * (2 * 32 * 33);
+            float* stg = reinterpret_cast<float*>(smem) + q * (2 * 32 * 36);
             for (int ch = 0; ch < BN / 32; ++ch) {
                 const int nb = n0 + ch * 32;
                 if (nb >= g.N) break;
@@ -266,33 +266,90 @@ __global__ void __launch_bounds__(192, 1)
                             const long long off = (long long)n * ld + row;
                             C[off] = xr;
                             C[pe + off] = xi;
-                            C[2 * pe + off] = tf32_lo(xr);
-                            C[3 * pe + off] = tf32_lo(xi);
+                            if (g.write_lo) {
+                                C[2 * pe + off] = tf32_lo(xr);
+                                C[3 * pe + off] = tf32_lo(xi);
+                            }
                         }
                     }
                 } else {
-                    // row-major store through shared memory: one 128-byte row segment per instruction
+                    // Row-major store through shared memory.  The 32x32 sub-tile is staged
+                    // (row stride 36 floats keeps float4 rows 16-byte aligned and the staging
+                    // writes conflict-free), then read back as float4: 8 lanes cover one
+                    // 128-byte row segment, 4 rows per instruction, and every C load of the
+                    // sub-tile is issued before the first store.
 #pragma unroll
-                    for (int j = 0; j < 32; ++j) {
-                        stg[lane * 33 + j] = __uint_as_float(vr[j]);
-                        stg[32 * 33 + lane * 33 + j] = __uint_as_float(vi[j]);
+                    for (int q4 = 0; q4 < 8; ++q4) {
+                        *reinterpret_cast<float4*>(&stg[lane * 36 + 4 * q4]) =
+                            make_float4(__uint_as_float(vr[4 * q4]), __uint_as_float(vr[4 * q4 + 1]),
+                                        __uint_as_float(vr[4 * q4 + 2]), __uint_as_float(vr[4 * q4 + 3]));
+                        *reinterpret_cast<float4*>(&stg[32 * 36 + lane * 36 + 4 * q4]) =
+                            make_float4(__uint_as_float(vi[4 * q4]), __uint_as_float(vi[4 * q4 + 1]),
+                                        __uint_as_float(vi[4 * q4 + 2]), __uint_as_float(vi[4 * q4 + 3]));
                     }
                     __syncwarp();
-                    const int n = nb + lane;
-                    const bool mcol = (n >= g.mask_c0 && n < g.mask_c0 + g.mask_w);
-                    for (int rr = 0; rr < 32; ++rr) {
-                        const int r = row0 + rr;
-                        if (r >= g.M) break;
-                        if (n < g.N) {
-                            float xr = g.alpha * stg[rr * 33 + lane];
-                            float xi = g.alpha * stg[32 * 33 + rr * 33 + lane];
-                            const bool masked = mcol || (r >= g.mask_c0 && r < g.mask_c0 + g.mask_w);
+                    const int sub = lane >> 3, cq = lane & 7;
+                    const int n = nb + 4 * cq;
+                    const bool full4 = (n + 3 < g.N);
+                    float4 cre[8], cim[8];
+#pragma unroll
+                    for (int it = 0; it < 8; ++it) {
+                        const int r = row0 + 4 * it + sub;
+                        cre[it] = make_float4(0.f, 0.f, 0.f, 0.f);
+                        cim[it] = cre[it];
+                        if (g.beta && r < g.M) {
                             const long long off = (long long)r * ld + n;
-                            if (g.beta && !masked) { xr += C[off]; xi += C[pe + off]; }
-                            C[off] = xr;
-                            C[pe + off] = xi;
-                            C[2 * pe + off] = tf32_lo(xr);
-                            C[3 * pe + off] = tf32_lo(xi);
+                            if (full4) {
+                                cre[it] = __ldcg(reinterpret_cast<const float4*>(C + off));
+                                cim[it] = __ldcg(reinterpret_cast<const float4*>(C + pe + off));
+                            } else {
+                                float* a = reinterpret_cast<float*>(&cre[it]);
+                                float* c = reinterpret_cast<float*>(&cim[it]);
+                                for (int e = 0; e < 4; ++e)
+                                    if (n + e < g.N) { a[e] = __ldcg(C + off + e); c[e] = __ldcg(C + pe + off + e); }
+                            }
+                        }
+                    }
+#pragma unroll
+                    for (int it = 0; it < 8; ++it) {
+                        const int rl = 4 * it + sub;
+                        const int r = row0 + rl;
+                        if (r >= g.M) continue;
+                        const bool mrow = (r >= g.mask_c0 && r < g.mask_c0 + g.mask_w);
+                        const float4 sr = *reinterpret_cast<const float4*>(&stg[rl * 36 + 4 * cq]);
+                        const float4 si = *reinterpret_cast<const float4*>(&stg[32 * 36 + rl * 36 + 4 * cq]);
+                        const float* srp = reinterpret_cast<const float*>(&sr);
+                        const float* sip = reinterpret_cast<const float*>(&si);
+                        const float* crp = reinterpret_cast<const float*>(&cre[it]);
+                        const float* cip = reinterpret_cast<const float*>(&cim[it]);
+                        float xr[4], xi[4], lr[4], li[4];
+#pragma unroll
+                        for (int e = 0; e < 4; ++e) {
+                            const int col = n + e;
+                            const bool keep = g.beta && !(mrow || (col >= g.mask_c0 && col < g.mask_c0 + g.mask_w));
+                            xr[e] = g.alpha * srp[e] + (keep ? crp[e] : 0.f);
+                            xi[e] = g.alpha * sip[e] + (keep ? cip[e] : 0.f);
+                            lr[e] = tf32_lo(xr[e]);
+                            li[e] = tf32_lo(xi[e]);
+                        }
+                        const long long off = (long long)r * ld + n;
+                        if (full4) {
+                            *reinterpret_cast<float4*>(C + off) = make_float4(xr[0], xr[1], xr[2], xr[3]);
+                            *reinterpret_cast<float4*>(C + pe + off) = make_float4(xi[0], xi[1], xi[2], xi[3]);
+                            if (g.write_lo) {
+                                *reinterpret_cast<float4*>(C + 2 * pe + off) = make_float4(lr[0], lr[1], lr[2], lr[3]);
+                                *reinterpret_cast<float4*>(C + 3 * pe + off) = make_float4(li[0], li[1], li[2], li[3]);
+                            }
+                        } else {
+                            for (int e = 0; e < 4; ++e)
+                                if (n + e < g.N) {
+                                    C[off + e] = xr[e];
+                                    C[pe + off + e] = xi[e];
+                                    if (g.write_lo) {
+                                        C[2 * pe + off + e] = lr[e];
+                                        C[3 * pe + off + e] = li[e];
+                                    }
+                                }
                         }
                     }
                     __syncwarp();

@@ -65,6 +65,10 @@ template <typename T>
 void launch_level1_combine(cudaStream_t s, int njobs, NodeMap m, const cplx<double>* st, double scale, Pool<T> D,
                            Pool<T> C, const L1Job* jobs);
 void launch_perm_init(cudaStream_t s, int njobs, int* perm, int b);
+// D[node] = (cyclic tridiagonal block of node)⁻¹ in O(b²) (first reduction step)
+template <typename T>
+void launch_tri_inverse(cudaStream_t s, int njobs, NodeMap m, const cplx<double>* st, double scale, Pool<T> D,
+                        const int* nodes, unsigned* err);
 // Gauss-Jordan panel step with panel width nb (returns a cudaError_t value)
 template <typename T>
 int launch_gj_panel(cudaStream_t s, int nb, int njobs, Pool<T> M, const int* slots, Pool<T> GP, Pool<T> RP,
@@ -91,6 +95,7 @@ template <typename T> struct GemmArgs {
     int mask_c0, mask_w;
     int c_trans;
     const int* c_trans_arr;   // per-job override of c_trans (device, may be null)
+    int write_lo;             // also write the TF32 residual planes of C (FP32 pools)
     unsigned* err;
 };
 template <typename T>
@@ -112,6 +117,9 @@ template <typename T> struct GemvArgs {
 // TR = 1: matrices stored transposed.  Returns a cudaError_t value.
 template <typename T>
 int launch_gemv(cudaStream_t s, int tr, int njobs, const GemvArgs<T>& g);
+// right-hand sides one launch_gemv call may take for block size b
+template <typename T>
+int gemv_max_rhs(int b);
 // r[s] -= u_s ⊙ z[next] + l_s ⊙ z[prev]  (first reduction step, diagonal couplings)
 // mode 0: survivors update r from eliminated neighbours (jobs: L1Job-like int4 (s, prev, next, flags))
 // mode 1: eliminated k: w[k] = l_k ⊙ x[prev] + u_k ⊙ x[next]

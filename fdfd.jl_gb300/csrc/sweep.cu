@@ -1,119 +1,216 @@
 // Forward/backward sweeps of the cyclic-reduction solve: batched complex
 // matrix-vector products (1..8 right-hand sides) on node-planar vectors.
-// These are HBM-bound: every factor matrix is streamed once per sweep.
+// They stream every factor block once per sweep, so they are HBM-bound; both
+// kernels issue all of a thread's 16-byte loads for a row (or a group of rows)
+// before the first FMA so that enough bytes are in flight per SM.
 #include "common.cuh"
 #include "kernels.cuh"
 
-#define GEMV_MAXR 8
+namespace {
 
-// TR = 0: matrices stored N-form (row-major), warp per row, lanes over columns.
-// TR = 1: matrices stored as their transpose (row-major Mᵀ): thread per output
-//         row i reads column i of the stored array, coalesced across threads.
-// grid: (ceil(b/32), njobs), block 256 (8 warps); dynamic smem 2 terms x b x nrhs complex.
-template <typename T, int TR>
-__global__ void __launch_bounds__(256) gemv_kernel(GemvArgs<T> g) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    T* sv = reinterpret_cast<T*>(smem_raw);        // [term][rhs][plane][b]
-    const int b = g.b, ld = g.ld, R = g.nrhs;
-    const int4 J = g.jobs[blockIdx.y];
-    const int2 Y = g.yjobs[blockIdx.y];
-    const int tid = threadIdx.x;
-    const int mslot[2] = {J.x, J.z}, vnode[2] = {J.y, J.w};
+template <typename T> struct V16;
+template <> struct V16<float> { typedef float4 type; };
+template <> struct V16<double> { typedef double2 type; };
+
+template <typename T> __device__ __forceinline__ typename V16<T>::type ld16(const T* p) {
+    return __ldcs(reinterpret_cast<const typename V16<T>::type*>(p));
+}
+template <typename T> __device__ __forceinline__ typename V16<T>::type zero16() {
+    typename V16<T>::type v;
+    T* e = reinterpret_cast<T*>(&v);
+#pragma unroll
+    for (int i = 0; i < (int)(16 / sizeof(T)); ++i) e[i] = 0;
+    return v;
+}
+
+// stage the (up to two) input vectors of a job into shared memory, zero padded:
+// sv[((t*R + r)*2 + plane)*bpad + i]
+template <typename T>
+__device__ void stage_vectors(const GemvArgs<T>& g, const int mslot[2], const int vnode[2], T* sv, int R, int bpad) {
     const T* V[2] = {g.V1, g.V2};
-    // stage the input vectors
     for (int t = 0; t < 2; ++t) {
         if (mslot[t] < 0) continue;
-        const T* v = V[t] + ((size_t)vnode[t] * g.rtot + g.r0) * 2 * ld;
-        for (int idx = tid; idx < R * 2 * b; idx += blockDim.x) {
-            int r = idx / (2 * b), rem = idx % (2 * b), p = rem / b, i = rem % b;
-            sv[((size_t)t * R + r) * 2 * b + p * b + i] = v[((size_t)r * 2 + p) * ld + i];
+        const T* v = V[t] + ((size_t)vnode[t] * g.rtot + g.r0) * 2 * g.ld;
+        for (int idx = threadIdx.x; idx < R * 2 * bpad; idx += blockDim.x) {
+            const int r = idx / (2 * bpad), rem = idx % (2 * bpad), p = rem / bpad, i = rem % bpad;
+            sv[((size_t)t * R + r) * 2 * bpad + p * bpad + i] =
+                (i < g.b && r < g.nrhs) ? v[((size_t)r * 2 + p) * g.ld + i] : (T)0;
         }
     }
+}
+
+}  // namespace
+
+// N-form (row-major blocks): warp per row, lanes over 16-byte column groups.
+// grid: (ceil(b/32), njobs), block 256 (8 warps x 4 rows)
+template <typename T, int R>
+__global__ void __launch_bounds__(256) gemv_n_kernel(GemvArgs<T> g) {
+    constexpr int VW = 16 / sizeof(T);
+    constexpr int CW = 32 * VW;       // columns per warp-wide load
+    constexpr int GRP = 4;            // column chunks whose loads are issued together
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* sv = reinterpret_cast<T*>(smem_raw);
+    const int b = g.b;
+    const int nch = (b + CW - 1) / CW;
+    const int bpad = nch * CW;
+    const int4 J = g.jobs[blockIdx.y];
+    const int2 Y = g.yjobs[blockIdx.y];
+    const int mslot[2] = {J.x, J.z}, vnode[2] = {J.y, J.w};
+    stage_vectors<T>(g, mslot, vnode, sv, R, bpad);
     __syncthreads();
-    T* y = g.Y + ((size_t)Y.x * g.rtot + g.r0) * 2 * ld;
-    const T* y0 = Y.y >= 0 ? g.Y0 + ((size_t)Y.y * g.rtot + g.r0) * 2 * ld : nullptr;
-    if (TR == 0) {
-        const int warp = tid >> 5, lane = tid & 31;
-        for (int q = 0; q < 4; ++q) {
-            int row = blockIdx.x * 32 + warp * 4 + q;
-            if (row >= b) break;
-            T ar[GEMV_MAXR], ai[GEMV_MAXR];
+    T* y = g.Y + ((size_t)Y.x * g.rtot + g.r0) * 2 * g.ld;
+    const T* y0 = Y.y >= 0 ? g.Y0 + ((size_t)Y.y * g.rtot + g.r0) * 2 * g.ld : nullptr;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int q = 0; q < 4; ++q) {
+        const int row = blockIdx.x * 32 + warp * 4 + q;
+        if (row >= b) break;
+        T ar[R], ai[R];
 #pragma unroll
-            for (int r = 0; r < GEMV_MAXR; ++r) { ar[r] = 0; ai[r] = 0; }
-            for (int t = 0; t < 2; ++t) {
-                if (mslot[t] < 0) continue;
-                const Pool<T>& P = t ? g.P2 : g.P1;
-                const T* Mr = P.slot(mslot[t]) + (size_t)row * P.ld;
-                const T* Mi = Mr + P.plane_elems();
-                const T* vt = sv + (size_t)t * R * 2 * b;
-                for (int j = lane; j < b; j += 32) {
-                    T mr = Mr[j], mi = Mi[j];
+        for (int r = 0; r < R; ++r) { ar[r] = 0; ai[r] = 0; }
+        for (int t = 0; t < 2; ++t) {
+            if (mslot[t] < 0) continue;
+            const Pool<T>& P = t ? g.P2 : g.P1;
+            const T* Mr = P.slot(mslot[t]) + (size_t)row * P.ld;
+            const T* Mi = Mr + P.plane_elems();
+            const T* vt = sv + (size_t)t * R * 2 * bpad;
+            for (int c0 = 0; c0 < nch; c0 += GRP) {
+                typename V16<T>::type mr[GRP], mi[GRP];
 #pragma unroll
-                    for (int r = 0; r < GEMV_MAXR; ++r) {
-                        if (r >= R) break;
-                        T vr = vt[(r * 2) * b + j], vi = vt[(r * 2 + 1) * b + j];
-                        ar[r] = fma(mr, vr, ar[r]); ar[r] = fma(-mi, vi, ar[r]);
-                        ai[r] = fma(mr, vi, ai[r]); ai[r] = fma(mi, vr, ai[r]);
-                    }
+                for (int u = 0; u < GRP; ++u) {
+                    const int c = (c0 + u) * CW + lane * VW;
+                    if (c0 + u < nch && c < b) { mr[u] = ld16<T>(Mr + c); mi[u] = ld16<T>(Mi + c); }
+                    else { mr[u] = zero16<T>(); mi[u] = zero16<T>(); }
                 }
-            }
 #pragma unroll
-            for (int r = 0; r < GEMV_MAXR; ++r) {
-                if (r >= R) break;
-                for (int o = 16; o > 0; o >>= 1) {
-                    ar[r] += __shfl_down_sync(0xffffffffu, ar[r], o);
-                    ai[r] += __shfl_down_sync(0xffffffffu, ai[r], o);
-                }
-            }
-            if (lane == 0) {
-                for (int r = 0; r < R; ++r) {
-                    T br = 0, bi = 0;
-                    if (y0) { br = y0[(r * 2) * ld + row]; bi = y0[(r * 2 + 1) * ld + row]; }
-                    y[(r * 2) * ld + row] = br + g.alpha * ar[r];
-                    y[(r * 2 + 1) * ld + row] = bi + g.alpha * ai[r];
-                }
-            }
-        }
-    } else {
-        // 256 threads: 32 output rows x 8 j-groups, reduced through shared memory
-        __shared__ T red[2][8][32][GEMV_MAXR];
-        const int il = tid & 31, jg = tid >> 5;
-        const int row = blockIdx.x * 32 + il;
-        T ar[GEMV_MAXR], ai[GEMV_MAXR];
+                for (int u = 0; u < GRP; ++u) {
+                    const int c = (c0 + u) * CW + lane * VW;
+                    const T* er = reinterpret_cast<const T*>(&mr[u]);
+                    const T* ei = reinterpret_cast<const T*>(&mi[u]);
 #pragma unroll
-        for (int r = 0; r < GEMV_MAXR; ++r) { ar[r] = 0; ai[r] = 0; }
-        if (row < b) {
-            for (int t = 0; t < 2; ++t) {
-                if (mslot[t] < 0) continue;
-                const Pool<T>& P = t ? g.P2 : g.P1;
-                const T* Mr = P.slot(mslot[t]);
-                const T* Mi = Mr + P.plane_elems();
-                const T* vt = sv + (size_t)t * R * 2 * b;
-                for (int j = jg; j < b; j += 8) {
-                    T mr = Mr[(size_t)j * P.ld + row], mi = Mi[(size_t)j * P.ld + row];
+                    for (int e = 0; e < VW; ++e) {
+                        if (c + e < b) {      // masks the row padding beyond b
 #pragma unroll
-                    for (int r = 0; r < GEMV_MAXR; ++r) {
-                        if (r >= R) break;
-                        T vr = vt[(r * 2) * b + j], vi = vt[(r * 2 + 1) * b + j];
-                        ar[r] = fma(mr, vr, ar[r]); ar[r] = fma(-mi, vi, ar[r]);
-                        ai[r] = fma(mr, vi, ai[r]); ai[r] = fma(mi, vr, ai[r]);
+                            for (int r = 0; r < R; ++r) {
+                                const T vr = vt[(r * 2) * bpad + c + e], vi = vt[(r * 2 + 1) * bpad + c + e];
+                                ar[r] = fma(er[e], vr, ar[r]); ar[r] = fma(-ei[e], vi, ar[r]);
+                                ai[r] = fma(er[e], vi, ai[r]); ai[r] = fma(ei[e], vr, ai[r]);
+                            }
+                        }
                     }
                 }
             }
         }
 #pragma unroll
-        for (int r = 0; r < GEMV_MAXR; ++r) { red[0][jg][il][r] = ar[r]; red[1][jg][il][r] = ai[r]; }
-        __syncthreads();
-        if (jg == 0 && row < b) {
+        for (int r = 0; r < R; ++r)
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                ar[r] += __shfl_down_sync(0xffffffffu, ar[r], o);
+                ai[r] += __shfl_down_sync(0xffffffffu, ai[r], o);
+            }
+        if (lane == 0) {
+#pragma unroll
             for (int r = 0; r < R; ++r) {
-                T sr = 0, si = 0;
-                for (int q = 0; q < 8; ++q) { sr += red[0][q][il][r]; si += red[1][q][il][r]; }
+                if (r >= g.nrhs) break;
                 T br = 0, bi = 0;
-                if (y0) { br = y0[(r * 2) * ld + row]; bi = y0[(r * 2 + 1) * ld + row]; }
-                y[(r * 2) * ld + row] = br + g.alpha * sr;
-                y[(r * 2 + 1) * ld + row] = bi + g.alpha * si;
+                if (y0) { br = y0[(r * 2) * g.ld + row]; bi = y0[(r * 2 + 1) * g.ld + row]; }
+                y[(r * 2) * g.ld + row] = br + g.alpha * ar[r];
+                y[(r * 2 + 1) * g.ld + row] = bi + g.alpha * ai[r];
             }
         }
+    }
+}
+
+// Stored-transpose form (row-major Mᵀ): y[i] = Σ_j Mᵀ[j][i] v[j].  A lane owns
+// VW consecutive outputs (one 16-byte load per row j), the 8 warps split the j
+// range, partial sums are reduced through shared memory.
+// grid: (ceil(b/(32*VW)), njobs), block 256
+template <typename T, int R>
+__global__ void __launch_bounds__(256) gemv_t_kernel(GemvArgs<T> g) {
+    constexpr int VW = 16 / sizeof(T);
+    constexpr int U = 4;              // rows j whose loads are issued together
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int b = g.b;
+    const int bpad = (b + 31) / 32 * 32;
+    T* sv = reinterpret_cast<T*>(smem_raw);
+    T* red = sv + (size_t)2 * R * 2 * bpad;          // [warp][out][r][re|im]
+    const int4 J = g.jobs[blockIdx.y];
+    const int2 Y = g.yjobs[blockIdx.y];
+    const int mslot[2] = {J.x, J.z}, vnode[2] = {J.y, J.w};
+    stage_vectors<T>(g, mslot, vnode, sv, R, bpad);
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int i0 = blockIdx.x * 32 * VW + lane * VW;
+    T ar[VW][R], ai[VW][R];
+#pragma unroll
+    for (int e = 0; e < VW; ++e)
+#pragma unroll
+        for (int r = 0; r < R; ++r) { ar[e][r] = 0; ai[e][r] = 0; }
+    if (i0 < b) {
+        for (int t = 0; t < 2; ++t) {
+            if (mslot[t] < 0) continue;
+            const Pool<T>& P = t ? g.P2 : g.P1;
+            const T* Mr = P.slot(mslot[t]) + i0;
+            const T* Mi = Mr + P.plane_elems();
+            const T* vt = sv + (size_t)t * R * 2 * bpad;
+            for (int j0 = warp; j0 < b; j0 += 8 * U) {
+                typename V16<T>::type mr[U], mi[U];
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    const int j = j0 + 8 * u;
+                    if (j < b) {
+                        mr[u] = ld16<T>(Mr + (size_t)j * P.ld);
+                        mi[u] = ld16<T>(Mi + (size_t)j * P.ld);
+                    } else {
+                        mr[u] = zero16<T>(); mi[u] = zero16<T>();
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    const int j = j0 + 8 * u;
+                    if (j < b) {
+                        const T* er = reinterpret_cast<const T*>(&mr[u]);
+                        const T* ei = reinterpret_cast<const T*>(&mi[u]);
+#pragma unroll
+                        for (int r = 0; r < R; ++r) {
+                            const T vr = vt[(r * 2) * bpad + j], vi = vt[(r * 2 + 1) * bpad + j];
+#pragma unroll
+                            for (int e = 0; e < VW; ++e) {
+                                ar[e][r] = fma(er[e], vr, ar[e][r]); ar[e][r] = fma(-ei[e], vi, ar[e][r]);
+                                ai[e][r] = fma(er[e], vi, ai[e][r]); ai[e][r] = fma(ei[e], vr, ai[e][r]);
+                            }
+                        }
+                    }
+                }
+            }
+        }
+    }
+    // cross-warp reduction
+    const int nout = 32 * VW;
+#pragma unroll
+    for (int e = 0; e < VW; ++e)
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const size_t o = (((size_t)warp * nout + lane * VW + e) * R + r) * 2;
+            red[o] = ar[e][r];
+            red[o + 1] = ai[e][r];
+        }
+    __syncthreads();
+    T* y = g.Y + ((size_t)Y.x * g.rtot + g.r0) * 2 * g.ld;
+    const T* y0 = Y.y >= 0 ? g.Y0 + ((size_t)Y.y * g.rtot + g.r0) * 2 * g.ld : nullptr;
+    for (int idx = threadIdx.x; idx < nout * g.nrhs; idx += blockDim.x) {
+        const int out = idx % nout, r = idx / nout;
+        const int i = blockIdx.x * nout + out;
+        if (i >= b) continue;
+        T sr = 0, si = 0;
+        for (int w = 0; w < 8; ++w) {
+            const size_t o = (((size_t)w * nout + out) * R + r) * 2;
+            sr += red[o];
+            si += red[o + 1];
+        }
+        T br = 0, bi = 0;
+        if (y0) { br = y0[(r * 2) * g.ld + i]; bi = y0[(r * 2 + 1) * g.ld + i]; }
+        y[(r * 2) * g.ld + i] = br + g.alpha * sr;
+        y[(r * 2 + 1) * g.ld + i] = bi + g.alpha * si;
     }
 }
 
@@ -130,47 +227,80 @@ __global__ void diag_sweep_kernel(NodeMap m, const cplx<double>* st, double scal
     if (i >= m.b) return;
     long long N = (long long)m.Nx * m.Ny;
     long long k = m.nat(J.x, i);
-    cplx<double> l = cscale(st[m.p_cprev() * N + k], scale);
-    cplx<double> u = cscale(st[m.p_cnext() * N + k], scale);
+    const cplx<double> ld_ = cscale(st[m.p_cprev() * N + k], scale);
+    const cplx<double> ud_ = cscale(st[m.p_cnext() * N + k], scale);
+    const cplx<T> l = cmk((T)ld_.re, (T)ld_.im), u = cmk((T)ud_.re, (T)ud_.im);
     const int ld = m.ld;
     for (int r = 0; r < nrhs; ++r) {
-        cplx<double> acc = cmk(0.0, 0.0);
+        cplx<T> acc = cmk((T)0, (T)0);
         if (J.w & 1) {
             const T* s = src + ((size_t)J.y * nrhs + r) * 2 * ld;
-            acc = cadd(acc, cmul(l, cmk((double)s[i], (double)s[ld + i])));
+            acc = cadd(acc, cmul(l, cmk(s[i], s[ld + i])));
         }
         if (J.w & 2) {
             const T* s = src + ((size_t)J.z * nrhs + r) * 2 * ld;
-            acc = cadd(acc, cmul(u, cmk((double)s[i], (double)s[ld + i])));
+            acc = cadd(acc, cmul(u, cmk(s[i], s[ld + i])));
         }
         T* d = dst + ((size_t)J.x * nrhs + r) * 2 * ld;
         if (mode == 0) {
-            d[i] = (T)((double)d[i] - acc.re);
-            d[ld + i] = (T)((double)d[ld + i] - acc.im);
+            d[i] -= acc.re;
+            d[ld + i] -= acc.im;
         } else {
-            d[i] = (T)acc.re;
-            d[ld + i] = (T)acc.im;
+            d[i] = acc.re;
+            d[ld + i] = acc.im;
         }
     }
 }
 
-template <typename T>
-int launch_gemv(cudaStream_t s, int tr, int njobs, const GemvArgs<T>& g) {
+namespace {
+template <typename T, int R>
+size_t gemv_smem(int tr, int b) {
+    constexpr int VW = 16 / sizeof(T);
+    if (tr) {
+        const int bpad = (b + 31) / 32 * 32;
+        return ((size_t)2 * R * 2 * bpad + (size_t)8 * 32 * VW * R * 2) * sizeof(T);
+    }
+    const int bpad = ceil_div(b, 32 * VW) * 32 * VW;
+    return (size_t)2 * R * 2 * bpad * sizeof(T);
+}
+
+template <typename T, int R>
+int gemv_launch_r(cudaStream_t s, int tr, int njobs, const GemvArgs<T>& g) {
+    constexpr int VW = 16 / sizeof(T);
     static bool attr = false;
     if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(gemv_kernel<T, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             160 * 1024);
+        cudaError_t e = cudaFuncSetAttribute(gemv_n_kernel<T, R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             200 * 1024);
         if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(gemv_kernel<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+            e = cudaFuncSetAttribute(gemv_t_kernel<T, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
         if (e != cudaSuccess) return (int)e;
         attr = true;
     }
-    size_t smem = (size_t)2 * g.nrhs * 2 * g.b * sizeof(T);
-    dim3 grid(ceil_div(g.b, 32), njobs);
-    if (tr) gemv_kernel<T, 1><<<grid, 256, smem, s>>>(g);
-    else gemv_kernel<T, 0><<<grid, 256, smem, s>>>(g);
+    const size_t smem = gemv_smem<T, R>(tr, g.b);
+    if (tr) gemv_t_kernel<T, R><<<dim3(ceil_div(g.b, 32 * VW), njobs), 256, smem, s>>>(g);
+    else gemv_n_kernel<T, R><<<dim3(ceil_div(g.b, 32), njobs), 256, smem, s>>>(g);
     return (int)cudaGetLastError();
 }
+}  // namespace
+
+// g.nrhs must not exceed gemv_max_rhs<T>(b).
+template <typename T>
+int launch_gemv(cudaStream_t s, int tr, int njobs, const GemvArgs<T>& g) {
+    if (g.nrhs <= 1) return gemv_launch_r<T, 1>(s, tr, njobs, g);
+    if (g.nrhs <= 2) return gemv_launch_r<T, 2>(s, tr, njobs, g);
+    if (g.nrhs <= 4) return gemv_launch_r<T, 4>(s, tr, njobs, g);
+    return gemv_launch_r<T, 8>(s, tr, njobs, g);
+}
+
+// largest right-hand-side count (8, 4, 2 or 1) whose shared memory fits both forms
+template <typename T>
+int gemv_max_rhs(int b) {
+    if (gemv_smem<T, 8>(1, b) <= 200 * 1024) return 8;
+    if (gemv_smem<T, 4>(1, b) <= 200 * 1024) return 4;
+    if (gemv_smem<T, 2>(1, b) <= 200 * 1024) return 2;
+    return 1;
+}
+
 template <typename T>
 void launch_diag_sweep(cudaStream_t s, int njobs, NodeMap m, const cplx<double>* st, double scale, int nrhs,
                        const int4* jobs, int mode, const T* src, T* dst) {
@@ -178,6 +308,8 @@ void launch_diag_sweep(cudaStream_t s, int njobs, NodeMap m, const cplx<double>*
 }
 template int launch_gemv<float>(cudaStream_t, int, int, const GemvArgs<float>&);
 template int launch_gemv<double>(cudaStream_t, int, int, const GemvArgs<double>&);
+template int gemv_max_rhs<float>(int);
+template int gemv_max_rhs<double>(int);
 template void launch_diag_sweep<float>(cudaStream_t, int, NodeMap, const cplx<double>*, double, int, const int4*,
                                        int, const float*, float*);
 template void launch_diag_sweep<double>(cudaStream_t, int, NodeMap, const cplx<double>*, double, int, const int4*,
