@@ -163,6 +163,99 @@ def test_reference_dipole_problem(lib, fdfd, oracle):
 
 
 # ---------------------------------------------------------------------------
+# adjoint gradient
+# ---------------------------------------------------------------------------
+def adjoint_problem_small():
+    from fdfd_gb300 import workloads as W
+    p = W.adjoint_problem(Nx=64, Ny=48, design=(16, 16), seed=9, waist=4.0, npml=8)
+    return p
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_adjoint_matches_oracle(lib, fdfd, oracle, prec):
+    p = adjoint_problem_small()
+    P = fdfd.FDFD_PREC_FP64 if prec == "fp64" else fdfd.FDFD_PREC_MIXED
+    h = handle_for(fdfd, p.Nx, p.Ny, p.npml, p.dx, p.dy, p.pml_m, p.pml_lnR, fdfd.TM, P)
+    h.set_eps(p.eps)
+    h.factor(p.omega)
+    J, grad, ez, st = h.adjoint(p.src, p.extra["mvec"])
+    h.close()
+    g = oracle.Grid((p.Nx, p.Ny), p.npml, ((0.0, 0.0), (p.Nx * p.dx, p.Ny * p.dy)))
+    J0, grad0, E0 = oracle.adjoint_gradient(g, p.eps, p.src, p.omega, p.extra["mvec"], p.pml_m, p.pml_lnR)
+    tol = TOL_FIELD_FP64 if prec == "fp64" else TOL_FIELD_MIXED
+    assert st.rel_residual <= TOL_RES
+    assert abs(J - J0) <= tol * J0
+    assert rel(ez, E0) <= tol
+    assert rel(grad, grad0) <= 10 * tol
+
+
+def test_adjoint_matches_finite_differences(lib, fdfd):
+    """Central differences (step 1e-4 in ϵᵣ, FP64 solves) on seeded design pixels, ≤ 1e-5 relative."""
+    p = adjoint_problem_small()
+    h = handle_for(fdfd, p.Nx, p.Ny, p.npml, p.dx, p.dy, p.pml_m, p.pml_lnR, fdfd.TM, fdfd.FDFD_PREC_FP64)
+    h.set_eps(p.eps)
+    h.factor(p.omega)
+    J, grad, _, _ = h.adjoint(p.src, p.extra["mvec"])
+    x0, y0, dwx, dwy = p.extra["design_box"]
+    rng = np.random.default_rng(17)
+    pix = [(x0 + rng.integers(dwx), y0 + rng.integers(dwy)) for _ in range(4)]
+    for (i, j) in pix:
+        Js = []
+        for d in (1e-4, -1e-4):
+            e = p.eps.copy()
+            e[i, j] += d
+            h.set_eps(e)
+            h.factor(p.omega)
+            Js.append(h.adjoint(p.src, p.extra["mvec"])[0])
+        fd = (Js[0] - Js[1]) / 2e-4
+        assert abs(fd - grad[i, j]) <= 1e-5 * abs(grad[i, j]) + 1e-9 * J, (i, j, fd, grad[i, j])
+    h.close()
+
+
+# ---------------------------------------------------------------------------
+# eigenfrequency
+# ---------------------------------------------------------------------------
+def match_eigs(om, ref):
+    """max relative distance from each reference eigenfrequency to the nearest computed one"""
+    return max(np.min(np.abs(om - r)) / abs(r) for r in ref)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_eigfreq_golden(lib, fdfd, prec):
+    g = np.load(os.path.join(GOLD, "tm_phc_eigen_56.npz"))
+    Nx, Ny = int(g["Nx"]), int(g["Ny"])
+    P = fdfd.FDFD_PREC_FP64 if prec == "fp64" else fdfd.FDFD_PREC_MIXED
+    h = handle_for(fdfd, Nx, Ny, g["npml"], float(g["dx"]), float(g["dy"]), float(g["pml_m"]),
+                   float(g["pml_lnR"]), int(g["pol"]), P)
+    h.set_eps(g["eps"])
+    nev = len(g["omega"])
+    om, lam, f, st = h.eigfreq(float(g["omega0"]), nev)
+    assert match_eigs(om, g["omega"]) <= 1e-8
+    # eigenvectors: (A - σI) y = (λ - σ) y with the assembled shifted operator
+    sigma = -float(g["omega0"]) ** 2 * (fdfd.MU0 * 1e-6) * (fdfd.EPS0 * 1e-6)   # eigen.jl:335
+    ay = h.apply(f[:, 0])
+    for q in range(nev):
+        r = ay[q] - (lam[q] - sigma) * f[q, 0]
+        assert np.linalg.norm(r) <= 1e-7 * abs(lam[q] - sigma) * np.linalg.norm(f[q, 0])
+    h.close()
+
+
+def test_eigfreq_phc_cavity_280(lib, fdfd, oracle):
+    """12x12 rod lattice cavity (ϵ = 8.9, r = 0.2a, 20 cells per a, 20-cell PML), 6 eigenfrequencies
+    nearest ωa/2πc = 0.38, mixed precision with refinement inside each Arnoldi step."""
+    from fdfd_gb300 import workloads as W
+    p, w0 = W.phc_cavity()
+    h = handle_for(fdfd, p.Nx, p.Ny, p.npml, p.dx, p.dy, p.pml_m, p.pml_lnR, fdfd.TM, fdfd.FDFD_PREC_MIXED)
+    h.set_eps(p.eps)
+    om, lam, f, st = h.eigfreq(w0, 6)
+    h.close()
+    g = oracle.Grid((p.Nx, p.Ny), p.npml, ((0.0, 0.0), (p.Nx * p.dx, p.Ny * p.dy)))
+    ref, _, _ = oracle.eigenfrequency(g, p.eps, w0, oracle.TM, 6, "LM", p.pml_m, p.pml_lnR,
+                                      v0=np.ones(p.Nx * p.Ny, dtype=complex))
+    assert match_eigs(om, ref) <= 1e-8
+
+
+# ---------------------------------------------------------------------------
 # error behaviour
 # ---------------------------------------------------------------------------
 def test_errors(lib, fdfd):
