@@ -26,7 +26,7 @@ FDFD_REFINE_GMRES, FDFD_REFINE_CLASSIC = 0, 1
 EXPORTS = ["fdfd_version", "fdfd_create", "fdfd_destroy", "fdfd_last_error", "fdfd_set_refinement",
            "fdfd_set_eps", "fdfd_factor", "fdfd_solve", "fdfd_solve_device", "fdfd_adjoint", "fdfd_eigfreq",
            "fdfd_get_stencil", "fdfd_apply", "fdfd_set_profiling", "fdfd_get_profile", "fdfd_residual_noalloc",
-           "fdfd_debug_gemm"]
+           "fdfd_debug_hessenberg_eig", "fdfd_debug_gemm"]
 PROF_CLASSES = ["gemm_tc", "gemm_simt", "gj_panel", "sweep", "residual", "other"]
 
 
@@ -101,6 +101,8 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.fdfd_residual_noalloc.restype = ip
     lib.fdfd_residual_noalloc.argtypes = [ip, ip, ip, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                           C.c_void_p]
+    lib.fdfd_debug_hessenberg_eig.restype = ip
+    lib.fdfd_debug_hessenberg_eig.argtypes = [ip, dp, dp, dp]
     lib.fdfd_debug_gemm.restype = ip
     lib.fdfd_debug_gemm.argtypes = [ip, ip, ip, dp, dp, dp, ip, ip, dp]
     _lib = lib
@@ -192,6 +194,19 @@ class Handle:
         self._check(self.lib.fdfd_adjoint(self.h, cptr(s), cptr(m), C.byref(J), cptr(grad), cptr(ez), C.byref(st)))
         return J.value, grad.T.copy(), from_natural(ez, self.Nx, self.Ny)[0], st
 
+    def eigfreq(self, omega0, nev, which=0, tol=1e-10):
+        """Shift-invert eigenfrequencies -> (omega[nev], lambda[nev], fields (nev, 3, Nx, Ny), stats)."""
+        N = self.Nx * self.Ny
+        om = np.empty(nev, dtype=np.complex128)
+        lam = np.empty(nev, dtype=np.complex128)
+        flds = np.empty((nev, 3, N), dtype=np.complex128)
+        st = Stats()
+        self._check(self.lib.fdfd_eigfreq(self.h, float(omega0), int(nev), int(which), float(tol), cptr(om),
+                                          cptr(lam), cptr(flds), C.byref(st)))
+        f = np.stack([np.stack([from_natural(flds[i, c], self.Nx, self.Ny)[0] for c in range(3)])
+                      for i in range(nev)])
+        return om, lam, f, st
+
     def set_profiling(self, on=True):
         self._check(self.lib.fdfd_set_profiling(self.h, 1 if on else 0))
 
@@ -221,6 +236,19 @@ class Handle:
         self._check(self.lib.fdfd_apply(self.h, cptr(buf), x3.shape[0], cptr(out)))
         y = from_natural(out, self.Nx, self.Ny)
         return y[0] if single else y
+
+
+def hessenberg_eig(H):
+    """Eigenvalues and unit eigenvectors of a complex upper Hessenberg matrix (host QR in the library)."""
+    lib = load()
+    H = np.ascontiguousarray(H, dtype=np.complex128)
+    n = H.shape[0]
+    w = np.empty(n, dtype=np.complex128)
+    V = np.empty((n, n), dtype=np.complex128)
+    rc = lib.fdfd_debug_hessenberg_eig(n, cptr(H), cptr(w), cptr(V))
+    if rc != FDFD_OK:
+        raise FDFDError(rc, "fdfd_debug_hessenberg_eig failed")
+    return w, V
 
 
 def debug_gemm(A, B, precision=FDFD_PREC_MIXED, use_tc=1):

@@ -8,6 +8,7 @@
 // close both the in-line and the node ring).
 #include "common.cuh"
 #include "kernels.cuh"
+#include <algorithm>
 
 template <typename T>
 __device__ __forceinline__ cplx<double> st_at(const cplx<double>* st, const NodeMap& m, int plane, int node, int i) {
@@ -162,19 +163,42 @@ __global__ void perm_init_kernel(int* perm, int b) {
 // textbook one (e.g. G. W. Stewart, Matrix Algorithms I, §3.1).
 // grid: njobs, block 512; requires b <= 512*RPT.
 // ---------------------------------------------------------------------------
+// shared staging elements of gj_panel_kernel: the composed row permutation moves at most
+// 2*NB rows (each of the NB swaps can bring in two new rows), chunked by CW columns, and the
+// Rᵀ transpose tile holds NB x 129; both store re and im
+template <int NB, int CW>
+__host__ __device__ constexpr size_t gj_panel_smem_elems() {
+    return (size_t)2 * (2 * NB * CW > NB * 129 ? 2 * NB * CW : NB * 129);
+}
+
+template <typename T, int NB>
+__device__ __forceinline__ cplx<T> pick_col(const T (&vr)[NB], const T (&vi)[NB], int jj) {
+    // v[jj] for a runtime jj without dynamic register indexing
+    T a = vr[0], c = vi[0];
+#pragma unroll
+    for (int k = 1; k < NB; ++k)
+        if (k == jj) { a = vr[k]; c = vi[k]; }
+    return cmk(a, c);
+}
+
 template <typename T, int NB, int RPT>
 __global__ void __launch_bounds__(512, 1) gj_panel_kernel(Pool<T> M, const int* slots, Pool<T> GP, Pool<T> RP,
                                                           int* perm, int c0, unsigned* err) {
     constexpr int NT = 512;
-    __shared__ T xre[2][NB], xim[2][NB];       // row exchange
-    __shared__ T pre_[NB], pim_[NB];           // scaled pivot row
+    constexpr int CW = sizeof(T) == 4 ? 128 : 64;      // column chunk of the row permutation
+    __shared__ T xpr[NB], xpi[NB];                     // pivot row before scaling
+    __shared__ T xrr[NB], xri[NB];                     // old row r0 (exchange partner)
     __shared__ T redv[NT / 32];
     __shared__ int redi[NT / 32];
-    __shared__ int s_piv;
     __shared__ int pivs[NB];
+    __shared__ int mv_dst[2 * NB], mv_src[2 * NB];
+    __shared__ int s_nmv;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* buf = reinterpret_cast<T*>(smem_raw);           // row-permutation / transpose staging
 
     const int b = M.rows;
     const int tid = threadIdx.x;
+    const int warp = tid >> 5, lane = tid & 31;
     const int job = blockIdx.x;
     T* Mre = M.slot(slots[job]);
     T* Mim = Mre + M.plane_elems();
@@ -194,110 +218,89 @@ __global__ void __launch_bounds__(512, 1) gj_panel_kernel(Pool<T> M, const int* 
         }
     }
 
+#pragma unroll 1
+    for (int jj = 0; jj < w; ++jj) {
+        const int r0 = c0 + jj;
+        // ---- block argmax over rows >= r0 of column jj (ties: lowest row)
+        T best = (T)-1;
+        int bi = b;
 #pragma unroll
-    for (int jj = 0; jj < NB; ++jj) {
-        if (jj < w) {
-            const int r0 = c0 + jj;
-            // ---- block argmax over rows >= r0 of column jj
-            T best = (T)-1;
-            int bi = b;
-#pragma unroll
-            for (int t = 0; t < RPT; ++t) {
-                const int i = tid + t * NT;
-                if (i >= r0 && i < b) {
-                    const T v = fabs(vr[t][jj]) + fabs(vi[t][jj]);
-                    if (v > best) { best = v; bi = i; }
-                }
+        for (int t = 0; t < RPT; ++t) {
+            const int i = tid + t * NT;
+            if (i >= r0 && i < b) {
+                const cplx<T> v = pick_col<T, NB>(vr[t], vi[t], jj);
+                const T m = fabs(v.re) + fabs(v.im);
+                if (m > best) { best = m; bi = i; }
             }
+        }
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                const T ov = __shfl_down_sync(0xffffffffu, best, o);
-                const int oi = __shfl_down_sync(0xffffffffu, bi, o);
-                if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
+        for (int o = 16; o > 0; o >>= 1) {
+            const T ov = __shfl_down_sync(0xffffffffu, best, o);
+            const int oi = __shfl_down_sync(0xffffffffu, bi, o);
+            if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
+        }
+        if (lane == 0) { redv[warp] = best; redi[warp] = bi; }
+        __syncthreads();
+        // every warp reduces the 16 partials itself (no second barrier)
+        best = lane < NT / 32 ? redv[lane] : (T)-1;
+        bi = lane < NT / 32 ? redi[lane] : b;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const T ov = __shfl_xor_sync(0xffffffffu, best, o);
+            const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+            if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
+        }
+        int piv = bi;
+        if (!(best > (T)0) || piv >= b || !isfinite((double)best)) {
+            if (tid == 0) dev_error(err, FDFD_DEVERR_SINGULAR);
+            piv = r0;
+        }
+        if (tid == 0) pivs[jj] = piv;
+        // ---- the owners of rows piv and r0 publish them
+#pragma unroll
+        for (int t = 0; t < RPT; ++t) {
+            const int i = tid + t * NT;
+            if (i == piv)
+#pragma unroll
+                for (int k = 0; k < NB; ++k) { xpr[k] = vr[t][k]; xpi[k] = vi[t][k]; }
+            if (i == r0 && piv != r0)
+#pragma unroll
+                for (int k = 0; k < NB; ++k) { xrr[k] = vr[t][k]; xri[k] = vi[t][k]; }
+        }
+        __syncthreads();
+        // ---- every thread forms the scaled pivot row; owner(r0) keeps it,
+        //      owner(piv) takes the old row r0; everyone else eliminates column jj
+        const cplx<T> p = pick_col<T, NB>(xpr, xpi, jj);
+        const cplx<T> inv = (p.re == (T)0 && p.im == (T)0) ? cmk((T)0, (T)0) : cinv(p);
+#pragma unroll
+        for (int t = 0; t < RPT; ++t) {
+            const int i = tid + t * NT;
+            if (i >= b) continue;
+            if (i == r0) {
+#pragma unroll
+                for (int k = 0; k < NB; ++k) {
+                    const cplx<T> v = (k == jj) ? inv : cmul(cmk(xpr[k], xpi[k]), inv);
+                    vr[t][k] = k < w ? v.re : (T)0;
+                    vi[t][k] = k < w ? v.im : (T)0;
+                }
+                continue;
             }
-            if ((tid & 31) == 0) { redv[tid >> 5] = best; redi[tid >> 5] = bi; }
-            __syncthreads();
-            if (tid < 32) {
-                best = tid < NT / 32 ? redv[tid] : (T)-1;
-                bi = tid < NT / 32 ? redi[tid] : b;
+            if (i == piv) {
 #pragma unroll
-                for (int o = 16; o > 0; o >>= 1) {
-                    const T ov = __shfl_down_sync(0xffffffffu, best, o);
-                    const int oi = __shfl_down_sync(0xffffffffu, bi, o);
-                    if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
-                }
-                if (tid == 0) {
-                    if (!(best > (T)0) || bi >= b || !isfinite((double)best)) {
-                        dev_error(err, FDFD_DEVERR_SINGULAR);
-                        bi = r0;
-                    }
-                    s_piv = bi;
-                    pivs[jj] = bi;
-                }
+                for (int k = 0; k < NB; ++k) { vr[t][k] = xrr[k]; vi[t][k] = xri[k]; }
             }
-            __syncthreads();
-            const int piv = s_piv;
-            const int o0 = r0 % NT, t0 = r0 / NT;      // owner of position r0
-            const int op = piv % NT, tp = piv / NT;    // owner of the pivot row
-            // ---- exchange rows r0 and piv through shared memory
-            if (piv != r0) {
+            const cplx<T> f = pick_col<T, NB>(vr[t], vi[t], jj);
+            const cplx<T> fi = cmul(f, inv);          // f / p
 #pragma unroll
-                for (int t = 0; t < RPT; ++t) {
-                    if (tid == o0 && t == t0)
-#pragma unroll
-                        for (int k = 0; k < NB; ++k) { xre[0][k] = vr[t][k]; xim[0][k] = vi[t][k]; }
-                    if (tid == op && t == tp)
-#pragma unroll
-                        for (int k = 0; k < NB; ++k) { xre[1][k] = vr[t][k]; xim[1][k] = vi[t][k]; }
-                }
-                __syncthreads();
-#pragma unroll
-                for (int t = 0; t < RPT; ++t) {
-                    if (tid == o0 && t == t0)
-#pragma unroll
-                        for (int k = 0; k < NB; ++k) { vr[t][k] = xre[1][k]; vi[t][k] = xim[1][k]; }
-                    if (tid == op && t == tp)
-#pragma unroll
-                        for (int k = 0; k < NB; ++k) { vr[t][k] = xre[0][k]; vi[t][k] = xim[0][k]; }
-                }
-            }
-            // ---- the owner of r0 scales the pivot row and publishes it
-#pragma unroll
-            for (int t = 0; t < RPT; ++t) {
-                if (tid == o0 && t == t0) {
-                    const cplx<T> p = cmk(vr[t][jj], vi[t][jj]);
-                    const cplx<T> inv = (p.re == (T)0 && p.im == (T)0) ? cmk((T)0, (T)0) : cinv(p);
-#pragma unroll
-                    for (int k = 0; k < NB; ++k) {
-                        cplx<T> v = (k == jj) ? inv : cmul(cmk(vr[t][k], vi[t][k]), inv);
-                        if (k >= w) v = cmk((T)0, (T)0);
-                        pre_[k] = v.re;
-                        pim_[k] = v.im;
-                        vr[t][k] = v.re;
-                        vi[t][k] = v.im;
-                    }
-                }
-            }
-            __syncthreads();
-            // ---- eliminate column jj from every other row
-            const cplx<T> inv = cmk(pre_[jj], pim_[jj]);
-#pragma unroll
-            for (int t = 0; t < RPT; ++t) {
-                const int i = tid + t * NT;
-                if (i < b && i != r0) {
-                    const cplx<T> f = cmk(vr[t][jj], vi[t][jj]);
-#pragma unroll
-                    for (int k = 0; k < NB; ++k) {
-                        if (k == jj) {
-                            const cplx<T> v = cneg(cmul(f, inv));
-                            vr[t][k] = v.re;
-                            vi[t][k] = v.im;
-                        } else {
-                            const cplx<T> prk = cmk(pre_[k], pim_[k]);
-                            vr[t][k] -= f.re * prk.re - f.im * prk.im;
-                            vi[t][k] -= f.re * prk.im + f.im * prk.re;
-                        }
-                    }
+            for (int k = 0; k < NB; ++k) {
+                if (k == jj) {
+                    vr[t][k] = -fi.re;
+                    vi[t][k] = -fi.im;
+                } else {
+                    // row_i -= (f/p)·pivotrow
+                    const T pr = xpr[k], pi = xpi[k];
+                    vr[t][k] -= fi.re * pr - fi.im * pi;
+                    vi[t][k] -= fi.re * pi + fi.im * pr;
                 }
             }
         }
@@ -312,7 +315,7 @@ __global__ void __launch_bounds__(512, 1) gj_panel_kernel(Pool<T> M, const int* 
             const int i = tid + t * NT;
             if (i < b) {
 #pragma unroll
-                for (int k = 0; k < NB; ++k) {     // GP.cols >= NB; columns >= w are zero already
+                for (int k = 0; k < NB; ++k) {
                     const long long o = (long long)i * GP.ld + k;
                     g[o] = vr[t][k];
                     g[pe + o] = vi[t][k];
@@ -330,36 +333,83 @@ __global__ void __launch_bounds__(512, 1) gj_panel_kernel(Pool<T> M, const int* 
             }
         }
     }
+    // 2. the w row swaps of this panel, composed into one permutation of at most 2w rows
+    if (tid == 0) {
+        int rows[2 * NB], src[2 * NB], n = 0;
+        for (int jj = 0; jj < w; ++jj) {
+            const int a = c0 + jj, c = pivs[jj];
+            if (a == c) continue;
+            int ia = -1, ic = -1;
+            for (int q = 0; q < n; ++q) { if (rows[q] == a) ia = q; if (rows[q] == c) ic = q; }
+            if (ia < 0) { rows[n] = a; src[n] = a; ia = n++; }
+            if (ic < 0) { rows[n] = c; src[n] = c; ic = n++; }
+            const int t = src[ia]; src[ia] = src[ic]; src[ic] = t;
+        }
+        int nm = 0;
+        int* pp = perm + (size_t)job * b;
+        int pv[2 * NB];
+        for (int q = 0; q < n; ++q) pv[q] = pp[src[q]];
+        for (int q = 0; q < n; ++q) {
+            pp[rows[q]] = pv[q];
+            if (src[q] != rows[q]) { mv_dst[nm] = rows[q]; mv_src[nm] = src[q]; ++nm; }
+        }
+        s_nmv = nm;
+    }
     __syncthreads();
-    // 2. row swaps on the full matrix, in order
-    for (int jj = 0; jj < w; ++jj) {
-        const int r0 = c0 + jj, piv = pivs[jj];
-        if (piv != r0) {
-            for (int c = tid; c < b; c += NT) {
-                T a = Mre[(size_t)r0 * ld + c]; Mre[(size_t)r0 * ld + c] = Mre[(size_t)piv * ld + c];
-                Mre[(size_t)piv * ld + c] = a;
-                T d = Mim[(size_t)r0 * ld + c]; Mim[(size_t)r0 * ld + c] = Mim[(size_t)piv * ld + c];
-                Mim[(size_t)piv * ld + c] = d;
-            }
-            if (tid == 0) {
-                int* pp = perm + (size_t)job * b;
-                int t = pp[r0]; pp[r0] = pp[piv]; pp[piv] = t;
-            }
+    const int nmv = s_nmv;
+    if ((size_t)2 * nmv * CW > gj_panel_smem_elems<NB, CW>()) {   // cannot happen: nmv <= 2*NB
+        if (tid == 0) dev_error(err, FDFD_DEVERR_SINGULAR);
+        return;
+    }
+    for (int cb = 0; cb < b && nmv > 0; cb += CW) {
+        const int cw = min(CW, b - cb);
+        for (int idx = tid; idx < nmv * cw; idx += NT) {
+            const int q = idx / cw, c = idx % cw;
+            buf[2 * idx] = Mre[(size_t)mv_src[q] * ld + cb + c];
+            buf[2 * idx + 1] = Mim[(size_t)mv_src[q] * ld + cb + c];
+        }
+        __syncthreads();
+        for (int idx = tid; idx < nmv * cw; idx += NT) {
+            const int q = idx / cw, c = idx % cw;
+            Mre[(size_t)mv_dst[q] * ld + cb + c] = buf[2 * idx];
+            Mim[(size_t)mv_dst[q] * ld + cb + c] = buf[2 * idx + 1];
         }
         __syncthreads();
     }
-    // 3. Rᵀ (b x RP.cols): RT[c][k] = M[c0+k][c], identity on the panel columns
+    // 3. Rᵀ (b x RP.cols): RT[c][k] = M[c0+k][c], identity on the panel columns;
+    //    staged through shared memory so reads (along c) and writes (along k) coalesce
     {
         T* rt = RP.slot(job);
         const int rc = RP.cols;
-        for (int idx = tid; idx < b * rc; idx += NT) {
-            const int k = idx / b, c = idx % b;    // c fastest: coalesced reads of M rows
-            cplx<T> v = cmk((T)0, (T)0);
-            if (k < w) {
-                if (c >= c0 && c < c0 + w) v = cmk((T)((c - c0) == k ? 1 : 0), (T)0);
-                else v = cmk(Mre[(size_t)(c0 + k) * ld + c], Mim[(size_t)(c0 + k) * ld + c]);
+        const long long pe = RP.plane_elems();
+        constexpr int TW = 128;            // columns per staging tile
+        for (int cb = 0; cb < b; cb += TW) {
+            const int cw = min(TW, b - cb);
+            for (int idx = tid; idx < NB * TW; idx += NT) {
+                const int k = idx / TW, c = idx % TW;
+                T a = 0, d = 0;
+                if (k < w && c < cw) {
+                    const int cc = cb + c;
+                    if (cc >= c0 && cc < c0 + w) a = (T)((cc - c0) == k ? 1 : 0);
+                    else { a = Mre[(size_t)(c0 + k) * ld + cc]; d = Mim[(size_t)(c0 + k) * ld + cc]; }
+                }
+                buf[2 * (k * (TW + 1) + c)] = a;
+                buf[2 * (k * (TW + 1) + c) + 1] = d;
             }
-            store_elem<T>(RP, rt, c, k, v, 0);
+            __syncthreads();
+            for (int idx = tid; idx < cw * rc; idx += NT) {
+                const int c = idx / rc, k = idx % rc;
+                T a = 0, d = 0;
+                if (k < NB) { a = buf[2 * (k * (TW + 1) + c)]; d = buf[2 * (k * (TW + 1) + c) + 1]; }
+                const long long o = (long long)(cb + c) * RP.ld + k;
+                rt[o] = a;
+                rt[pe + o] = d;
+                if (RP.planes == 4) {
+                    rt[2 * pe + o] = (T)tf32_lo((float)a);
+                    rt[3 * pe + o] = (T)tf32_lo((float)d);
+                }
+            }
+            __syncthreads();
         }
     }
 }
@@ -629,22 +679,38 @@ void launch_level1_combine(cudaStream_t s, int njobs, NodeMap m, const cplx<doub
 void launch_perm_init(cudaStream_t s, int njobs, int* perm, int b) {
     perm_init_kernel<int><<<dim3(ceil_div(b, 256), njobs), 256, 0, s>>>(perm, b);
 }
+template <typename T, int NB, int RPT>
+static int gj_panel_launch(cudaStream_t s, int njobs, Pool<T> M, const int* slots, Pool<T> GP, Pool<T> RP,
+                           int* perm, int c0, unsigned* err) {
+    constexpr int CW = sizeof(T) == 4 ? 128 : 64;
+    // staging: up to 2*NB moved rows x CW columns (re, im), or the NB x 129 Rᵀ tile (re, im)
+    const size_t smem = gj_panel_smem_elems<NB, CW>() * sizeof(T);
+    static bool attr = false;
+    if (!attr) {
+        cudaError_t e = cudaFuncSetAttribute(gj_panel_kernel<T, NB, RPT>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return (int)e;
+        attr = true;
+    }
+    gj_panel_kernel<T, NB, RPT><<<njobs, 512, smem, s>>>(M, slots, GP, RP, perm, c0, err);
+    return (int)cudaGetLastError();
+}
+
 template <typename T>
 int launch_gj_panel(cudaStream_t s, int nb, int njobs, Pool<T> M, const int* slots, Pool<T> GP, Pool<T> RP,
                     int* perm, int c0, unsigned* err) {
     const bool two = M.rows > 512;
     if (M.rows > 1024) return (int)cudaErrorInvalidValue;
     if constexpr (sizeof(T) == 4) {
-        if (nb == 32 && !two) gj_panel_kernel<T, 32, 1><<<njobs, 512, 0, s>>>(M, slots, GP, RP, perm, c0, err);
-        else if (nb == 16 && two) gj_panel_kernel<T, 16, 2><<<njobs, 512, 0, s>>>(M, slots, GP, RP, perm, c0, err);
-        else return (int)cudaErrorInvalidValue;
+        if (nb == 32 && !two) return gj_panel_launch<T, 32, 1>(s, njobs, M, slots, GP, RP, perm, c0, err);
+        if (nb == 16 && two) return gj_panel_launch<T, 16, 2>(s, njobs, M, slots, GP, RP, perm, c0, err);
     } else {
-        if (nb == 16 && !two) gj_panel_kernel<T, 16, 1><<<njobs, 512, 0, s>>>(M, slots, GP, RP, perm, c0, err);
-        else if (nb == 8 && two) gj_panel_kernel<T, 8, 2><<<njobs, 512, 0, s>>>(M, slots, GP, RP, perm, c0, err);
-        else return (int)cudaErrorInvalidValue;
+        if (nb == 16 && !two) return gj_panel_launch<T, 16, 1>(s, njobs, M, slots, GP, RP, perm, c0, err);
+        if (nb == 8 && two) return gj_panel_launch<T, 8, 2>(s, njobs, M, slots, GP, RP, perm, c0, err);
     }
-    return (int)cudaGetLastError();
+    return (int)cudaErrorInvalidValue;
 }
+
 template <typename T>
 void launch_gj_unpermute(cudaStream_t s, int njobs, Pool<T> M, const int* slots, const int* perm) {
     gj_unpermute_kernel<T><<<dim3(ceil_div(M.rows, 8), njobs), 256, 2 * M.rows * sizeof(T), s>>>(M, slots, perm);

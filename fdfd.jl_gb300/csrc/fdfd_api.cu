@@ -22,6 +22,7 @@
 #include "fdfd_cuda.h"
 #include "kernels.cuh"
 #include "gemm_tc.cuh"
+#include "hessenberg_eig.hpp"
 
 #include <algorithm>
 #include <chrono>
@@ -1350,8 +1351,214 @@ int fdfd_adjoint(fdfd_handle* h, const double* src, const double* mvec, double* 
 
 int fdfd_eigfreq(fdfd_handle* h, double omega0, int nev, int which, double tol, double* omega, double* lambda,
                  double* fields, fdfd_stats* stats) {
-    (void)omega0; (void)nev; (void)which; (void)tol; (void)omega; (void)lambda; (void)fields; (void)stats;
-    return h ? set_err(h, FDFD_EINVAL, "fdfd_eigfreq: not available in this build") : FDFD_EINVAL;
+    if (!h) return FDFD_EINVAL;
+    const long long N = (long long)h->Nx * h->Ny;
+    if (!h->eps_set) return set_err(h, FDFD_EINVAL, "fdfd_set_eps must be called before fdfd_eigfreq");
+    if (!(omega0 > 0) || nev < 1 || nev > 64 || nev >= N - 1 || !omega)
+        return set_err(h, FDFD_EINVAL, "fdfd_eigfreq: invalid arguments");
+    if (which != FDFD_WHICH_LM && which != FDFD_WHICH_LR)
+        return set_err(h, FDFD_EINVAL, "fdfd_eigfreq: which must be FDFD_WHICH_LM or FDFD_WHICH_LR");
+    if (!(tol > 0)) tol = 1e-10;
+    auto t0 = std::chrono::steady_clock::now();
+    h->launches = 0;
+    const double eps0 = kEPS0 * h->L0, mu0 = kMU0 * h->L0;
+    // eigen.jl:335 (TM) and :353 (TE): shift σ = -ω₀²μ₀ϵ₀ resp. -ω₀²μ₀, PML frozen at ω₀
+    const zd sigma = h->pol == FDFD_TM ? zd(-omega0 * omega0 * mu0 * eps0, 0) : zd(-omega0 * omega0 * mu0, 0);
+    cudaEventRecord(h->ev[0], h->stream);
+    h->factored = false;
+    RET(assemble(h, h->pol == FDFD_TM ? OP_TM_EIGEN : OP_TE_EIGEN, omega0, sigma, 0.0));
+    cudaEventRecord(h->ev[1], h->stream);
+    RET(factor_op(h));
+    cudaEventRecord(h->ev[2], h->stream);
+    h->omega = omega0;
+    h->sigma = sigma;
+
+    // Arnoldi basis (m+1 vectors) on the device
+    const int m = (int)std::min<long long>(N - 1, std::max(2 * nev + 24, 48));
+    RET(ensure_krylov(h, 2, 20));
+    cplx<double>* V = nullptr;
+    const size_t vbytes = (size_t)N * sizeof(cplx<double>);
+    RET(dev_alloc(h, (void**)&V, vbytes * (m + 1)));
+    struct Free {
+        fdfd_handle* h; void* p; size_t b;
+        ~Free() { cudaFree(p); h->dev_bytes -= (long long)b; }
+    } free_v{h, V, vbytes * (m + 1)};
+    // deterministic start vector (splitmix64 hash of the index), unit norm
+    {
+        std::vector<zd> v0(N);
+        double nn = 0;
+        for (long long k = 0; k < N; ++k) {
+            uint64_t x = (uint64_t)k * 0x9E3779B97F4A7C15ull + 0x632BE59BD9B4E019ull;
+            x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+            x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+            x ^= x >> 31;
+            v0[k] = zd((double)(x >> 11) / 9007199254740992.0 - 0.5, 0);
+            nn += std::norm(v0[k]);
+        }
+        for (auto& v : v0) v /= std::sqrt(nn);
+        CK(cudaMemcpyAsync(V, v0.data(), vbytes, cudaMemcpyHostToDevice, h->stream));
+    }
+    cudaEventRecord(h->ev[3], h->stream);
+    std::vector<zd> Hm((size_t)(m + 1) * m, zd(0, 0));
+    std::vector<zd> theta, S;
+    std::vector<int> pick;
+    int iters = 0, restarts = 0, k = 0;
+    bool converged = false;
+    double worst = 0;
+    auto select = [&](int kk) {
+        // Ritz pairs of the kk x kk Hessenberg matrix, the nev wanted ones first
+        std::vector<zd> Hk((size_t)kk * kk);
+        for (int i = 0; i < kk; ++i)
+            for (int j = 0; j < kk; ++j) Hk[(size_t)i * kk + j] = Hm[(size_t)i * m + j];
+        if (!hess::eig(kk, Hk, theta, S)) return false;
+        std::vector<int> idx(kk);
+        for (int i = 0; i < kk; ++i) idx[i] = i;
+        std::sort(idx.begin(), idx.end(), [&](int a, int b) {
+            return which == FDFD_WHICH_LM ? std::abs(theta[a]) > std::abs(theta[b]) : theta[a].real() > theta[b].real();
+        });
+        pick.assign(idx.begin(), idx.begin() + std::min(nev, kk));
+        return true;
+    };
+    while (!converged && restarts < 8) {
+        k = 0;
+        for (int j = 0; j < m; ++j) {
+            // w = (A - σI)⁻¹ v_j, refined to the handle's tolerance
+            CK(cudaMemcpyAsync(h->kb, V + (size_t)j * N, vbytes, cudaMemcpyDeviceToDevice, h->stream));
+            int it = 0;
+            double rr = 0;
+            RET(refine(h, 1, &it, &rr));
+            iters += it;
+            cplx<double>* w = V + (size_t)(j + 1) * N;
+            CK(cudaMemcpyAsync(w, h->kx, vbytes, cudaMemcpyDeviceToDevice, h->stream));
+            std::vector<zd> hc, hc2, nn;
+            RET(dots(h, V, N, j + 1, w, 1, hc));
+            RET(combine(h, V, N, j + 1, hc, 1, -1.0, w));
+            RET(dots(h, V, N, j + 1, w, 1, hc2));
+            RET(combine(h, V, N, j + 1, hc2, 1, -1.0, w));
+            RET(dots(h, w, 0, 1, w, 1, nn));
+            for (int i = 0; i <= j; ++i) Hm[(size_t)i * m + j] = hc[i] + hc2[i];
+            const double hn = std::sqrt(std::max(0.0, nn[0].real()));
+            Hm[(size_t)(j + 1) * m + j] = hn;
+            k = j + 1;
+            std::vector<zd> sc(1, hn > 0 ? zd(1.0 / hn, 0) : zd(0, 0));
+            RET(scale_vec(h, w, sc, 1, w));
+            if (hn == 0 || ((k >= nev + 2) && (k % 4 == 0 || k == m))) {
+                if (!select(k)) return set_err(h, FDFD_ENOCONV, "Hessenberg QR did not converge");
+                worst = 0;
+                for (int i : pick) {
+                    const double res = hn * std::abs(S[(size_t)(k - 1) * k + i]);
+                    worst = std::max(worst, res / std::max(std::abs(theta[i]), 1e-300));
+                }
+                if ((int)pick.size() == nev && worst <= tol) { converged = true; break; }
+                if (hn == 0) break;
+            }
+        }
+        if (!converged) {
+            // explicit restart from the sum of the wanted Ritz vectors
+            if (!select(k)) return set_err(h, FDFD_ENOCONV, "Hessenberg QR did not converge");
+            std::vector<zd> c(k, zd(0, 0));
+            for (int i : pick)
+                for (int r = 0; r < k; ++r) c[r] += S[(size_t)r * k + i];
+            CK(cudaMemsetAsync(h->kr, 0, vbytes, h->stream));
+            RET(combine(h, V, N, k, c, 1, 1.0, h->kr));
+            std::vector<zd> nn;
+            RET(dots(h, h->kr, 0, 1, h->kr, 1, nn));
+            std::vector<zd> sc(1, zd(1.0 / std::sqrt(std::max(nn[0].real(), 1e-300)), 0));
+            RET(scale_vec(h, h->kr, sc, 1, V));
+            ++restarts;
+        }
+    }
+    cudaEventRecord(h->ev[4], h->stream);
+    // eigenvalues of A (λ = σ + 1/θ), eigenfrequencies, Ritz vectors and fields
+    std::vector<zd> lam(nev), om(nev);
+    std::vector<int> order(pick);
+    std::sort(order.begin(), order.end(), [&](int a, int b) {
+        return which == FDFD_WHICH_LM ? std::abs(theta[a]) > std::abs(theta[b]) : theta[a].real() > theta[b].real();
+    });
+    for (int q = 0; q < nev; ++q) {
+        const zd th = theta[order[q]];
+        lam[q] = sigma + 1.0 / th;
+        om[q] = h->pol == FDFD_TM ? std::sqrt(-lam[q] / mu0 / eps0) : std::sqrt(-lam[q] / mu0);   // eigen.jl:336,354
+        omega[2 * q] = om[q].real();
+        omega[2 * q + 1] = om[q].imag();
+        if (lambda) { lambda[2 * q] = lam[q].real(); lambda[2 * q + 1] = lam[q].imag(); }
+    }
+    if (fields) {
+        for (int q = 0; q < nev; ++q) {
+            std::vector<zd> c(k);
+            for (int r = 0; r < k; ++r) c[r] = S[(size_t)r * k + order[q]];
+            cplx<double>* y = h->kx;
+            CK(cudaMemsetAsync(y, 0, vbytes, h->stream));
+            RET(combine(h, V, N, k, c, 1, 1.0, y));
+            // unit norm, largest component real positive
+            std::vector<zd> host(N);
+            CK(cudaMemcpyAsync(host.data(), y, vbytes, cudaMemcpyDeviceToHost, h->stream));
+            CK(cudaStreamSynchronize(h->stream));
+            double nn = 0;
+            long long imax = 0;
+            for (long long i = 0; i < N; ++i) {
+                nn += std::norm(host[i]);
+                if (std::abs(host[i]) > std::abs(host[imax])) imax = i;
+            }
+            const zd ph = std::abs(host[imax]) > 0 ? std::conj(host[imax]) / std::abs(host[imax]) : zd(1, 0);
+            const zd sc = ph / std::sqrt(nn);
+            for (auto& v : host) v *= sc;
+            double* f1 = fields + (size_t)q * 3 * 2 * N;
+            memcpy(f1, host.data(), vbytes);
+            CK(cudaMemcpyAsync(y, host.data(), vbytes, cudaMemcpyHostToDevice, h->stream));
+            // eigen.jl:339-340 (TM, forward differences) / :357-358 (TE)
+            std::vector<zd> coef(2);
+            if (h->pol == FDFD_TM) {
+                coef[0] = zd(-0.0, 1.0) / om[q] / mu0;    // -1/1im/ω/μ₀
+                coef[1] = zd(0.0, -1.0) / om[q] / mu0;    //  1/1im/ω/μ₀
+            } else {
+                coef[0] = zd(0.0, -1.0) / om[q];          //  1/1im/ω
+                coef[1] = coef[0];
+            }
+            CK(cudaMemcpyAsync(h->kc, coef.data(), 2 * sizeof(zd), cudaMemcpyHostToDevice, h->stream));
+            RecoverArgs ra;
+            ra.Nx = h->Nx; ra.Ny = h->Ny; ra.mode = h->pol == FDFD_TM ? REC_TM_EIGEN : REC_TE_EIGEN;
+            ra.idx = 1.0 / h->dx; ra.idy = 1.0 / h->dy; ra.eps0n = eps0;
+            LAUNCH(recover_kernel, dim3(ceil_div(N, 256), 1), 256, 0, ra, h->sf, h->eps, y, h->kc, h->kr,
+                   h->kr + N);
+            RET(check_launch(h, "eigen recover"));
+            CK(cudaMemcpyAsync(f1 + 2 * N, h->kr, 2 * vbytes, cudaMemcpyDeviceToHost, h->stream));
+        }
+    }
+    CK(cudaStreamSynchronize(h->stream));
+    RET(check_device(h, "eigfreq"));
+    if (stats) {
+        stats->iterations = iters;
+        stats->nrhs = nev;
+        stats->rel_residual = worst;
+        stats->t_assemble_ms = elapsed_ms(h->ev[0], h->ev[1]);
+        stats->t_factor_ms = elapsed_ms(h->ev[1], h->ev[2]);
+        stats->t_solve_ms = elapsed_ms(h->ev[3], h->ev[4]);
+        stats->t_recover_ms = 0;
+        stats->factor_flops = h->last_factor_flops;
+        stats->block = h->map.b;
+        stats->nblocks = h->map.n;
+        stats->levels = (int)h->steps.size() + 1;
+        stats->tc_gemm = h->tc_used;
+        stats->device_bytes = h->dev_bytes;
+        stats->gpu_launches = h->launches;
+        stats->t_total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    }
+    if (!converged)
+        return set_err(h, FDFD_ENOCONV, "Arnoldi: wanted Ritz pairs not converged (worst residual %.2e)", worst);
+    return FDFD_OK;
+}
+
+// Test entry: eigen-decomposition of a small complex upper Hessenberg matrix
+// (host only, the Ritz-pair solver of fdfd_eigfreq).
+int fdfd_debug_hessenberg_eig(int n, const double* H, double* w, double* V) {
+    if (n < 1 || !H || !w || !V) return FDFD_EINVAL;
+    std::vector<zd> Hm((size_t)n * n), ww, VV;
+    for (size_t i = 0; i < Hm.size(); ++i) Hm[i] = zd(H[2 * i], H[2 * i + 1]);
+    if (!hess::eig(n, Hm, ww, VV)) return FDFD_ENOCONV;
+    for (int i = 0; i < n; ++i) { w[2 * i] = ww[i].real(); w[2 * i + 1] = ww[i].imag(); }
+    for (size_t i = 0; i < VV.size(); ++i) { V[2 * i] = VV[i].real(); V[2 * i + 1] = VV[i].imag(); }
+    return FDFD_OK;
 }
 
 }  // extern "C"

@@ -47,6 +47,7 @@ extern "C" {
 #define FDFD_REFINE_CLASSIC 1  /* x += M^-1 (b - A x)                              */
 
 #define FDFD_WHICH_LM 0    /* eigenvalues of A nearest sigma (ARPACK :LM in shift-invert) */
+#define FDFD_WHICH_LR 1    /* largest real part of 1/(λ-σ) (ARPACK :LR in shift-invert)  */
 
 typedef struct fdfd_handle fdfd_handle;
 
@@ -124,8 +125,11 @@ int  fdfd_adjoint(fdfd_handle* h, const double* src, const double* mvec,
 /* Shift-invert eigenfrequencies (eigenfrequency, src/solver/eigen.jl:318-364):
  * with the PML frozen at omega0, TM finds eigenpairs of
  * A = Tϵᵣ⁻¹(δxf δxb + δyf δyb) nearest σ = -ω₀²μ₀ϵ₀, TE of
- * A = δxf Tϵx⁻¹ δxb + δyf Tϵy⁻¹ δyb nearest σ = -ω₀²μ₀, by Krylov-Schur
- * Arnoldi on (A - σI)⁻¹ with this library's factorization.  Outputs:
+ * A = δxf Tϵx⁻¹ δxb + δyf Tϵy⁻¹ δyb nearest σ = -ω₀²μ₀, by Arnoldi on
+ * (A - σI)⁻¹ (classical Gram-Schmidt with re-orthogonalisation, explicit
+ * restarts from the wanted Ritz vectors) with this library's factorization
+ * and refinement for every operator application; converged when every wanted
+ * Ritz pair has |h_{k+1,k}·s_k| <= tol·|θ| (tol <= 0 selects 1e-10).  Outputs:
  * omega (nev complex: sqrt(-λ/(μ₀ϵ₀)) TM, sqrt(-λ/μ₀) TE), lambda (nev
  * complex eigenvalues of A, may be NULL), fields (nev*3*Nx*Ny complex:
  * per mode f1,f2,f3 as in fdfd_solve but with the eigen.jl recovery, may be
@@ -182,6 +186,12 @@ int  fdfd_get_profile(fdfd_handle* h, fdfd_profile* out);
 int  fdfd_residual_noalloc(int Nx, int Ny, int nrhs, const double* stencil,
                            const double* x, const double* b, double* r,
                            double* norms, void* stream);
+
+/* Test entry (no counterpart in the reference): eigenvalues w (n complex) and
+ * unit eigenvectors V (n x n complex, row-major, column i for w[i]) of the
+ * complex upper Hessenberg matrix H (n x n row-major interleaved): the
+ * Ritz-pair solver of fdfd_eigfreq.  Host only. */
+int  fdfd_debug_hessenberg_eig(int n, const double* H, double* w, double* V);
 
 /* Kernel test entry (no counterpart in the reference): C = A·Bᵀ for complex
  * row-major interleaved host matrices A (M x K), B (N x K), C (M x N), through
