@@ -251,6 +251,17 @@ def run_extras(L, pkg, W, a):
     return out
 
 
+def gemm_traffic_bytes():
+    """DRAM bytes per launch of the tensor-core GEMM from the committed ncu summary
+    (profiles/gemm_tc_traffic.json: read + write of one captured launch and the units it processed),
+    or None when no capture exists."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "gemm_tc_traffic.json")) as f:
+            return json.load(f)
+    except Exception:
+        return None
+
+
 def measured_peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -373,29 +384,35 @@ def main():
         e2e = {"value": world * a.steps / te, "unit": "solves/s", "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": d2h}
 
-    # roofline of the dominant kernel class
+    # rooflines: the factorization's tensor-core GEMM (tensor-bound) and the solve sweeps (HBM-bound);
+    # class_ms shows every kernel class, dominant_class the largest by device time
     peaks, peak_src = measured_peaks()
-    dom = max(prof, key=lambda k: prof[k]["ms"])
-    d = prof[dom]
-    if dom in ("gemm_tc", "gemm_simt"):
-        achieved = d["work"] / (d["ms"] / 1e3) / 1e12
-        # 3xTF32: three TF32 MMAs per real product; TF32 tensor rate = half the BF16 rate
-        peak = peaks["bf16_tflops"] / 2 / 3 if dom == "gemm_tc" else None
-        roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                "frac": achieved / peak if peak else None, "traffic": None, "kernel": dom,
-                "peak_note": f"bf16 burst from {peak_src} /2 (TF32 rate) /3 (3xTF32 split), of measured",
-                "work_unit": "8*M*N*K algorithmic complex-GEMM flops per launch"}
-    elif dom == "gj_panel":
-        roof = {"bound": "latency", "achieved": None, "peak": None, "unit": None, "frac": None, "traffic": None,
-                "kernel": dom}
-    else:
-        achieved = d["work"] / (d["ms"] / 1e3) / 1e9
-        peak = peaks["hbm_gbs"]
-        roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": None, "kernel": dom, "peak_note": f"hbm_gbs from {peak_src}, of measured"}
-    roof["launches_in_region"] = d["launches"]
-    roof["avg_launch_ms"] = d["ms"] / max(d["launches"], 1)
-    roof["class_ms"] = {k: round(v["ms"], 3) for k, v in prof.items()}
+    gk = "gemm_tc" if prof["gemm_tc"]["launches"] else "gemm_simt"
+    d = prof[gk]
+    achieved = d["work"] / (d["ms"] / 1e3) / 1e12 if d["ms"] else None
+    # 3xTF32: three TF32 MMAs per real product; TF32 tensor rate = half the BF16 rate
+    peak = peaks["bf16_tflops"] / 2 / 3
+    roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+            "frac": achieved / peak if achieved else None, "kernel": gk,
+            "traffic": (gemm_traffic_bytes() or {}).get("bytes"),
+            "traffic_note": (gemm_traffic_bytes() or {}).get("note"),
+            "peak_note": f"bf16 burst from {peak_src} /2 (TF32 rate) /3 (3xTF32 split), of measured",
+            "work_unit": "8*M*N*K algorithmic complex-GEMM flops per launch",
+            "launches_in_region": d["launches"], "avg_launch_ms": d["ms"] / max(d["launches"], 1),
+            "class_ms": {k: round(v["ms"], 3) for k, v in prof.items()},
+            "dominant_class": max(prof, key=lambda k: prof[k]["ms"])}
+    # HBM-bound classes: achieved = algorithmic bytes / device time
+    hbm_units = {"sweep": "factor blocks (re, im planes) read once per sweep + node vectors",
+                 "gj_update": "each matrix read and written once per Gauss-Jordan panel (re, im planes)",
+                 "level1": "first-step inverses written; two inverses read, three blocks written per survivor"}
+    roof_hbm = {}
+    for k, unit in hbm_units.items():
+        c = prof[k]
+        ach = c["work"] / (c["ms"] / 1e3) / 1e9 if c["ms"] else None
+        roof_hbm[k] = {"bound": "hbm", "unit": "GB/s", "peak": peaks["hbm_gbs"], "achieved": ach,
+                       "frac": ach / peaks["hbm_gbs"] if ach else None, "ms": round(c["ms"], 3),
+                       "launches": c["launches"], "work_unit": unit}
+    roof_hbm["peak_note"] = f"hbm_gbs from {peak_src}, of measured"
 
     extras = {} if (a.no_extras or rank != 0) else run_extras(L, pkg, W, a)
 
@@ -411,7 +428,8 @@ def main():
                                                             "FP64 FGMRES refinement",
                            "l2": "inputs larger than L2 (factor storage ~6 GB per solve, no flush needed)",
                            "parallelism": f"replicas x{world}"},
-                "e2e": e2e, "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu, "clocks": clk,
+                "e2e": e2e, "gpu_launches": launches, "roofline": roof, "roofline_hbm": roof_hbm,
+                "cpu_baseline": cpu, "clocks": clk,
                 "rel_residual_max": maxres, "refine_iterations": iters, "fp64": fp64,
                 "tf32_cublas_tflops_live": tf32, "factor_flops": stats[-1]["factor_flops"],
                 "t_factor_ms": stats[-1]["t_factor_ms"], "t_solve_ms": stats[-1]["t_solve_ms"], **extras}

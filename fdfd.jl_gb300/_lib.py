@@ -27,7 +27,7 @@ EXPORTS = ["fdfd_version", "fdfd_create", "fdfd_destroy", "fdfd_last_error", "fd
            "fdfd_set_eps", "fdfd_factor", "fdfd_solve", "fdfd_solve_device", "fdfd_adjoint", "fdfd_eigfreq",
            "fdfd_get_stencil", "fdfd_apply", "fdfd_set_profiling", "fdfd_get_profile", "fdfd_residual_noalloc",
            "fdfd_debug_hessenberg_eig", "fdfd_debug_gemm"]
-PROF_CLASSES = ["gemm_tc", "gemm_simt", "gj_panel", "sweep", "residual", "other"]
+PROF_CLASSES = ["gemm_tc", "gemm_simt", "gj_panel", "sweep", "residual", "other", "gj_update", "level1"]
 
 
 class Stats(C.Structure):
@@ -42,7 +42,7 @@ class Stats(C.Structure):
 
 
 class Profile(C.Structure):
-    _fields_ = [("ms", C.c_double * 6), ("work", C.c_double * 6), ("launches", C.c_longlong * 6)]
+    _fields_ = [("ms", C.c_double * 8), ("work", C.c_double * 8), ("launches", C.c_longlong * 8)]
 
     def as_dict(self):
         return {k: {"ms": self.ms[i], "work": self.work[i], "launches": self.launches[i]}

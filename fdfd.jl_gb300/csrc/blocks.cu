@@ -143,7 +143,7 @@ __global__ void perm_init_kernel(int* perm, int b) {
 }
 
 // ---------------------------------------------------------------------------
-// Blocked in-place Gauss-Jordan inversion with partial pivoting, panel step.
+// Blocked Gauss-Jordan inversion with partial pivoting, panel step.
 //
 // For the panel of columns [c0, c0+w) of each matrix M (b x b) the kernel
 //  1. loads the panel M[:, c0:c0+w) into registers (thread t owns rows t and
@@ -151,85 +151,91 @@ __global__ void perm_init_kernel(int* perm, int b) {
 //     = largest |re|+|im| among the rows not yet used as pivots (ties: lowest
 //     row), row exchange, pivot row scaled by 1/p with the pivot entry
 //     replaced by 1/p, every other row i updated by -M[i,j]·(scaled pivot row)
-//     with its pivot-column entry set to -M[i,j]/p.  One step costs a block
-//     argmax, a row exchange through shared memory and a broadcast of the
-//     pivot row.  The result G (b x w) holds the panel's block transformation;
-//  2. applies the same row swaps to the full rows of M and records them in perm;
-//  3. writes Rᵀ: the (swapped) panel rows M[c0:c0+w, :] transposed, with the
-//     panel columns replaced by the identity.
-// The rank-w update M = mask(M) + G·R is then one TN GEMM (gemm_*_kernel with
-// mask [c0, c0+w)).  After the last panel M holds (P M₀)⁻¹, and
-// gj_unpermute_kernel restores M₀⁻¹.  The in-place Gauss-Jordan scheme is the
-// textbook one (e.g. G. W. Stewart, Matrix Algorithms I, §3.1).
+//     with its pivot-column entry set to -M[i,j]/p.  The register row rotates
+//     by one position per step so that the pivot column always sits in
+//     register 0 (no indexed register access).  One step costs a block argmax
+//     and a broadcast of the pivot row and its exchange partner through shared
+//     memory.  The result G (b x w) holds the panel's block transformation;
+//  2. composes the panel's row exchanges into rowsrc (row r of the exchanged
+//     matrix is row rowsrc[r] of M) and into perm; no row of M moves;
+//  3. writes Rᵀ: the exchanged panel rows M[rowsrc[c0:c0+w], :] transposed,
+//     with the panel columns replaced by the identity.
+// The rank-w update M' = mask(M[rowsrc]) + G·R is then one TN GEMM
+// (gemm_*_kernel with mask [c0, c0+w) reading its β term through rowsrc into
+// a second buffer).  After the last panel M holds (P M₀)⁻¹, and
+// gj_unpermute_kernel restores M₀⁻¹.  The Gauss-Jordan scheme is the textbook
+// one (e.g. G. W. Stewart, Matrix Algorithms I, §3.1).
 // grid: njobs, block 512; requires b <= 512*RPT.
 // ---------------------------------------------------------------------------
-// shared staging elements of gj_panel_kernel: the composed row permutation moves at most
-// 2*NB rows (each of the NB swaps can bring in two new rows), chunked by CW columns, and the
-// Rᵀ transpose tile holds NB x 129; both store re and im
-template <int NB, int CW>
+// shared staging elements of gj_panel_kernel: the NB x 129 Rᵀ transpose tile (re, im)
+template <int NB>
 __host__ __device__ constexpr size_t gj_panel_smem_elems() {
-    return (size_t)2 * (2 * NB * CW > NB * 129 ? 2 * NB * CW : NB * 129);
+    return (size_t)2 * NB * 129;
 }
 
-template <typename T, int NB>
-__device__ __forceinline__ cplx<T> pick_col(const T (&vr)[NB], const T (&vi)[NB], int jj) {
-    // v[jj] for a runtime jj without dynamic register indexing
-    T a = vr[0], c = vi[0];
-#pragma unroll
-    for (int k = 1; k < NB; ++k)
-        if (k == jj) { a = vr[k]; c = vi[k]; }
-    return cmk(a, c);
-}
+template <typename T> struct Vec16;
+template <> struct Vec16<float> { typedef float4 type; };
+template <> struct Vec16<double> { typedef double2 type; };
 
 template <typename T, int NB, int RPT>
 __global__ void __launch_bounds__(512, 1) gj_panel_kernel(Pool<T> M, const int* slots, Pool<T> GP, Pool<T> RP,
-                                                          int* perm, int c0, unsigned* err) {
+                                                          int* perm, int* rowsrc, int c0, unsigned* err) {
     constexpr int NT = 512;
-    constexpr int CW = sizeof(T) == 4 ? 128 : 64;      // column chunk of the row permutation
-    __shared__ T xpr[NB], xpi[NB];                     // pivot row before scaling
-    __shared__ T xrr[NB], xri[NB];                     // old row r0 (exchange partner)
+    constexpr int VW = 16 / sizeof(T);                 // elements per 16-byte vector
+    typedef typename Vec16<T>::type VT;
+    __shared__ __align__(16) T xpr[NB], xpi[NB];       // pivot row (rotated positions) before scaling
+    __shared__ __align__(16) T xrr[NB], xri[NB];       // row r0 (exchange partner)
     __shared__ T redv[NT / 32];
     __shared__ int redi[NT / 32];
     __shared__ int pivs[NB];
-    __shared__ int mv_dst[2 * NB], mv_src[2 * NB];
-    __shared__ int s_nmv;
+    __shared__ int rsm[NT * RPT];                      // composed row exchanges
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    T* buf = reinterpret_cast<T*>(smem_raw);           // row-permutation / transpose staging
+    T* buf = reinterpret_cast<T*>(smem_raw);           // Rᵀ transpose tile
 
     const int b = M.rows;
     const int tid = threadIdx.x;
     const int warp = tid >> 5, lane = tid & 31;
     const int job = blockIdx.x;
-    T* Mre = M.slot(slots[job]);
-    T* Mim = Mre + M.plane_elems();
+    const T* Mre = M.slot(slots[job]);
+    const T* Mim = Mre + M.plane_elems();
     const int ld = M.ld;
     const int w = min(NB, b - c0);
 
+    // Thread t owns rows t and t + 512.  Register position k holds panel column
+    // (jj + k) mod NB at step jj: the pivot column is always position 0.
     T vr[RPT][NB], vi[RPT][NB];
 #pragma unroll
     for (int t = 0; t < RPT; ++t) {
         const int i = tid + t * NT;
 #pragma unroll
-        for (int jj = 0; jj < NB; ++jj) {
-            T a = 0, c = 0;
-            if (i < b && jj < w) { a = Mre[(size_t)i * ld + c0 + jj]; c = Mim[(size_t)i * ld + c0 + jj]; }
-            vr[t][jj] = a;
-            vi[t][jj] = c;
+        for (int q = 0; q < NB / VW; ++q) {
+            VT a = {}, c = {};
+            // c0 + NB <= ld (ld is a multiple of 32 and of NB): the vector stays in the row
+            if (i < b && q * VW < w) {
+                a = *reinterpret_cast<const VT*>(Mre + (size_t)i * ld + c0 + q * VW);
+                c = *reinterpret_cast<const VT*>(Mim + (size_t)i * ld + c0 + q * VW);
+            }
+#pragma unroll
+            for (int e = 0; e < VW; ++e) {
+                const int k = q * VW + e;
+                const bool ok = i < b && k < w;
+                vr[t][k] = ok ? reinterpret_cast<const T*>(&a)[e] : (T)0;
+                vi[t][k] = ok ? reinterpret_cast<const T*>(&c)[e] : (T)0;
+            }
         }
     }
 
 #pragma unroll 1
     for (int jj = 0; jj < w; ++jj) {
         const int r0 = c0 + jj;
-        // ---- block argmax over rows >= r0 of column jj (ties: lowest row)
+        // ---- block argmax over rows >= r0 of the pivot column (ties: lowest row)
         T best = (T)-1;
         int bi = b;
 #pragma unroll
         for (int t = 0; t < RPT; ++t) {
             const int i = tid + t * NT;
             if (i >= r0 && i < b) {
-                const cplx<T> v = pick_col<T, NB>(vr[t], vi[t], jj);
-                const T m = fabs(v.re) + fabs(v.im);
+                const T m = fabs(vr[t][0]) + fabs(vi[t][0]);
                 if (m > best) { best = m; bi = i; }
             }
         }
@@ -241,7 +247,6 @@ __global__ void __launch_bounds__(512, 1) gj_panel_kernel(Pool<T> M, const int* 
         }
         if (lane == 0) { redv[warp] = best; redi[warp] = bi; }
         __syncthreads();
-        // every warp reduces the 16 partials itself (no second barrier)
         best = lane < NT / 32 ? redv[lane] : (T)-1;
         bi = lane < NT / 32 ? redi[lane] : b;
 #pragma unroll
@@ -256,128 +261,156 @@ __global__ void __launch_bounds__(512, 1) gj_panel_kernel(Pool<T> M, const int* 
             piv = r0;
         }
         if (tid == 0) pivs[jj] = piv;
-        // ---- the owners of rows piv and r0 publish them
+        // ---- the owners of rows piv and r0 publish them (16-byte stores)
 #pragma unroll
         for (int t = 0; t < RPT; ++t) {
             const int i = tid + t * NT;
-            if (i == piv)
+            if (i == piv) {
 #pragma unroll
-                for (int k = 0; k < NB; ++k) { xpr[k] = vr[t][k]; xpi[k] = vi[t][k]; }
-            if (i == r0 && piv != r0)
+                for (int q = 0; q < NB / VW; ++q) {
+                    VT a, c;
 #pragma unroll
-                for (int k = 0; k < NB; ++k) { xrr[k] = vr[t][k]; xri[k] = vi[t][k]; }
+                    for (int e = 0; e < VW; ++e) {
+                        reinterpret_cast<T*>(&a)[e] = vr[t][q * VW + e];
+                        reinterpret_cast<T*>(&c)[e] = vi[t][q * VW + e];
+                    }
+                    reinterpret_cast<VT*>(xpr)[q] = a;
+                    reinterpret_cast<VT*>(xpi)[q] = c;
+                }
+            }
+            if (i == r0 && piv != r0) {
+#pragma unroll
+                for (int q = 0; q < NB / VW; ++q) {
+                    VT a, c;
+#pragma unroll
+                    for (int e = 0; e < VW; ++e) {
+                        reinterpret_cast<T*>(&a)[e] = vr[t][q * VW + e];
+                        reinterpret_cast<T*>(&c)[e] = vi[t][q * VW + e];
+                    }
+                    reinterpret_cast<VT*>(xrr)[q] = a;
+                    reinterpret_cast<VT*>(xri)[q] = c;
+                }
+            }
         }
         __syncthreads();
-        // ---- every thread forms the scaled pivot row; owner(r0) keeps it,
-        //      owner(piv) takes the old row r0; everyone else eliminates column jj
-        const cplx<T> p = pick_col<T, NB>(xpr, xpi, jj);
+        // ---- scaled pivot row (formed by every thread from shared memory);
+        //      owner(r0) keeps it, owner(piv) takes the old row r0, everyone eliminates
+        const cplx<T> p = cmk(xpr[0], xpi[0]);
         const cplx<T> inv = (p.re == (T)0 && p.im == (T)0) ? cmk((T)0, (T)0) : cinv(p);
 #pragma unroll
         for (int t = 0; t < RPT; ++t) {
             const int i = tid + t * NT;
             if (i >= b) continue;
             if (i == r0) {
+                vr[t][0] = inv.re;
+                vi[t][0] = inv.im;
 #pragma unroll
-                for (int k = 0; k < NB; ++k) {
-                    const cplx<T> v = (k == jj) ? inv : cmul(cmk(xpr[k], xpi[k]), inv);
-                    vr[t][k] = k < w ? v.re : (T)0;
-                    vi[t][k] = k < w ? v.im : (T)0;
+                for (int k = 1; k < NB; ++k) {
+                    const cplx<T> v = cmul(cmk(xpr[k], xpi[k]), inv);
+                    vr[t][k] = v.re;
+                    vi[t][k] = v.im;
                 }
-                continue;
-            }
-            if (i == piv) {
+            } else {
+                if (i == piv) {
 #pragma unroll
-                for (int k = 0; k < NB; ++k) { vr[t][k] = xrr[k]; vi[t][k] = xri[k]; }
-            }
-            const cplx<T> f = pick_col<T, NB>(vr[t], vi[t], jj);
-            const cplx<T> fi = cmul(f, inv);          // f / p
+                    for (int k = 0; k < NB; ++k) { vr[t][k] = xrr[k]; vi[t][k] = xri[k]; }
+                }
+                const cplx<T> fi = cmul(cmk(vr[t][0], vi[t][0]), inv);   // f / p
+                vr[t][0] = -fi.re;
+                vi[t][0] = -fi.im;
 #pragma unroll
-            for (int k = 0; k < NB; ++k) {
-                if (k == jj) {
-                    vr[t][k] = -fi.re;
-                    vi[t][k] = -fi.im;
-                } else {
-                    // row_i -= (f/p)·pivotrow
+                for (int k = 1; k < NB; ++k) {
                     const T pr = xpr[k], pi = xpi[k];
                     vr[t][k] -= fi.re * pr - fi.im * pi;
                     vi[t][k] -= fi.re * pi + fi.im * pr;
                 }
             }
+            // rotate left by one: the next pivot column moves to position 0
+            const T r0v = vr[t][0], i0v = vi[t][0];
+#pragma unroll
+            for (int k = 0; k + 1 < NB; ++k) { vr[t][k] = vr[t][k + 1]; vi[t][k] = vi[t][k + 1]; }
+            vr[t][NB - 1] = r0v;
+            vi[t][NB - 1] = i0v;
+        }
+    }
+    // complete the rotation cycle of a short last panel (w < NB) so position k is column k
+#pragma unroll 1
+    for (int extra = w; extra < NB; ++extra) {
+#pragma unroll
+        for (int t = 0; t < RPT; ++t) {
+            const T r0v = vr[t][0], i0v = vi[t][0];
+#pragma unroll
+            for (int k = 0; k + 1 < NB; ++k) { vr[t][k] = vr[t][k + 1]; vi[t][k] = vi[t][k + 1]; }
+            vr[t][NB - 1] = r0v;
+            vi[t][NB - 1] = i0v;
         }
     }
 
-    // 1. G panel (b x GP.cols, zero padded)
+    // 1. G panel (b x GP.cols, zero padded), 16-byte stores of each thread's row
     {
         T* g = GP.slot(job);
         const long long pe = GP.plane_elems();
 #pragma unroll
         for (int t = 0; t < RPT; ++t) {
             const int i = tid + t * NT;
-            if (i < b) {
+            if (i >= b) continue;
 #pragma unroll
-                for (int k = 0; k < NB; ++k) {
-                    const long long o = (long long)i * GP.ld + k;
-                    g[o] = vr[t][k];
-                    g[pe + o] = vi[t][k];
-                    if (GP.planes == 4) {
-                        g[2 * pe + o] = (T)tf32_lo((float)vr[t][k]);
-                        g[3 * pe + o] = (T)tf32_lo((float)vi[t][k]);
-                    }
+            for (int q = 0; q < NB / VW; ++q) {
+                VT a, c, al, cl;
+#pragma unroll
+                for (int e = 0; e < VW; ++e) {
+                    const T x = vr[t][q * VW + e], y = vi[t][q * VW + e];
+                    reinterpret_cast<T*>(&a)[e] = x;
+                    reinterpret_cast<T*>(&c)[e] = y;
+                    reinterpret_cast<T*>(&al)[e] = (T)tf32_lo((float)x);
+                    reinterpret_cast<T*>(&cl)[e] = (T)tf32_lo((float)y);
                 }
-                for (int k = NB; k < GP.cols; ++k) {
-                    const long long o = (long long)i * GP.ld + k;
-                    g[o] = 0;
-                    g[pe + o] = 0;
-                    if (GP.planes == 4) { g[2 * pe + o] = 0; g[3 * pe + o] = 0; }
+                const long long o = (long long)i * GP.ld + q * VW;
+                *reinterpret_cast<VT*>(g + o) = a;
+                *reinterpret_cast<VT*>(g + pe + o) = c;
+                if (GP.planes == 4) {
+                    *reinterpret_cast<VT*>(g + 2 * pe + o) = al;
+                    *reinterpret_cast<VT*>(g + 3 * pe + o) = cl;
                 }
+            }
+            for (int k = NB; k < GP.cols; ++k) {
+                const long long o = (long long)i * GP.ld + k;
+                g[o] = 0;
+                g[pe + o] = 0;
+                if (GP.planes == 4) { g[2 * pe + o] = 0; g[3 * pe + o] = 0; }
             }
         }
     }
-    // 2. the w row swaps of this panel, composed into one permutation of at most 2w rows
+    __syncthreads();
+    // 2. the panel's row exchanges, composed: row r of the exchanged matrix is
+    //    row rsm[r] of M (the GEMM reads through this map, no rows move here)
+    for (int i = tid; i < b; i += NT) rsm[i] = i;
+    __syncthreads();
     if (tid == 0) {
-        int rows[2 * NB], src[2 * NB], n = 0;
         for (int jj = 0; jj < w; ++jj) {
             const int a = c0 + jj, c = pivs[jj];
-            if (a == c) continue;
-            int ia = -1, ic = -1;
-            for (int q = 0; q < n; ++q) { if (rows[q] == a) ia = q; if (rows[q] == c) ic = q; }
-            if (ia < 0) { rows[n] = a; src[n] = a; ia = n++; }
-            if (ic < 0) { rows[n] = c; src[n] = c; ic = n++; }
-            const int t = src[ia]; src[ia] = src[ic]; src[ic] = t;
+            const int t = rsm[a]; rsm[a] = rsm[c]; rsm[c] = t;
         }
-        int nm = 0;
-        int* pp = perm + (size_t)job * b;
-        int pv[2 * NB];
-        for (int q = 0; q < n; ++q) pv[q] = pp[src[q]];
-        for (int q = 0; q < n; ++q) {
-            pp[rows[q]] = pv[q];
-            if (src[q] != rows[q]) { mv_dst[nm] = rows[q]; mv_src[nm] = src[q]; ++nm; }
-        }
-        s_nmv = nm;
     }
     __syncthreads();
-    const int nmv = s_nmv;
-    if ((size_t)2 * nmv * CW > gj_panel_smem_elems<NB, CW>()) {   // cannot happen: nmv <= 2*NB
-        if (tid == 0) dev_error(err, FDFD_DEVERR_SINGULAR);
-        return;
-    }
-    for (int cb = 0; cb < b && nmv > 0; cb += CW) {
-        const int cw = min(CW, b - cb);
-        for (int idx = tid; idx < nmv * cw; idx += NT) {
-            const int q = idx / cw, c = idx % cw;
-            buf[2 * idx] = Mre[(size_t)mv_src[q] * ld + cb + c];
-            buf[2 * idx + 1] = Mim[(size_t)mv_src[q] * ld + cb + c];
+    {
+        int* rs = rowsrc + (size_t)job * b;
+        int* pp = perm + (size_t)job * b;
+        int pv[RPT];
+#pragma unroll
+        for (int t = 0; t < RPT; ++t) {
+            const int i = tid + t * NT;
+            if (i < b) pv[t] = pp[rsm[i]];
         }
-        __syncthreads();
-        for (int idx = tid; idx < nmv * cw; idx += NT) {
-            const int q = idx / cw, c = idx % cw;
-            Mre[(size_t)mv_dst[q] * ld + cb + c] = buf[2 * idx];
-            Mim[(size_t)mv_dst[q] * ld + cb + c] = buf[2 * idx + 1];
+        __syncthreads();   // every old perm entry is read before any is overwritten
+#pragma unroll
+        for (int t = 0; t < RPT; ++t) {
+            const int i = tid + t * NT;
+            if (i < b) { pp[i] = pv[t]; rs[i] = rsm[i]; }
         }
-        __syncthreads();
     }
-    // 3. Rᵀ (b x RP.cols): RT[c][k] = M[c0+k][c], identity on the panel columns;
-    //    staged through shared memory so reads (along c) and writes (along k) coalesce
+    // 3. Rᵀ (b x RP.cols): RT[c][k] = (row c0+k after the interchanges)[c], identity on the
+    //    panel columns; staged through shared memory so reads and writes coalesce
     {
         T* rt = RP.slot(job);
         const int rc = RP.cols;
@@ -391,7 +424,11 @@ __global__ void __launch_bounds__(512, 1) gj_panel_kernel(Pool<T> M, const int* 
                 if (k < w && c < cw) {
                     const int cc = cb + c;
                     if (cc >= c0 && cc < c0 + w) a = (T)((cc - c0) == k ? 1 : 0);
-                    else { a = Mre[(size_t)(c0 + k) * ld + cc]; d = Mim[(size_t)(c0 + k) * ld + cc]; }
+                    else {
+                        const int sr = rsm[c0 + k];
+                        a = Mre[(size_t)sr * ld + cc];
+                        d = Mim[(size_t)sr * ld + cc];
+                    }
                 }
                 buf[2 * (k * (TW + 1) + c)] = a;
                 buf[2 * (k * (TW + 1) + c) + 1] = d;
@@ -414,31 +451,30 @@ __global__ void __launch_bounds__(512, 1) gj_panel_kernel(Pool<T> M, const int* 
     }
 }
 
-// M[:, perm[j]] = M[:, j] per row (in place via shared memory); rewrites lo planes.
-// grid: (ceil(b/rows_per_block), njobs), block 256
+// Dst[r][perm[j]] = Src[r][j] per row (through shared memory, so Src may be Dst);
+// writes the TF32 residual planes.  grid: (ceil(b/8), njobs), block 256
 template <typename T>
-__global__ void gj_unpermute_kernel(Pool<T> M, const int* slots, const int* perm) {
+__global__ void gj_unpermute_kernel(Pool<T> Src, const int* sslots, Pool<T> Dst, const int* dslots,
+                                    const int* perm) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int b = M.rows;
+    const int b = Src.rows;
     T* rre = reinterpret_cast<T*>(smem_raw);
     T* rim = rre + b;
-    int job = blockIdx.y;
-    T* base = M.slot(slots[job]);
-    long long pe = M.plane_elems();
+    const int job = blockIdx.y;
+    const T* sb = Src.slot(sslots[job]);
+    T* db = Dst.slot(dslots[job]);
+    const long long spe = Src.plane_elems();
     const int* pp = perm + (size_t)job * b;
     const int rows_per = 8;
     for (int rr = 0; rr < rows_per; ++rr) {
-        int r = blockIdx.x * rows_per + rr;
+        const int r = blockIdx.x * rows_per + rr;
         if (r >= b) break;
         for (int j = threadIdx.x; j < b; j += blockDim.x) {
-            rre[j] = base[(size_t)r * M.ld + j];
-            rim[j] = base[pe + (size_t)r * M.ld + j];
+            rre[j] = sb[(size_t)r * Src.ld + j];
+            rim[j] = sb[spe + (size_t)r * Src.ld + j];
         }
         __syncthreads();
-        for (int j = threadIdx.x; j < b; j += blockDim.x) {
-            int dst = pp[j];
-            store_elem<T>(M, base, r, dst, cmk(rre[j], rim[j]), 0);
-        }
+        for (int j = threadIdx.x; j < b; j += blockDim.x) store_elem<T>(Dst, db, r, pp[j], cmk(rre[j], rim[j]), 0);
         __syncthreads();
     }
 }
@@ -681,10 +717,8 @@ void launch_perm_init(cudaStream_t s, int njobs, int* perm, int b) {
 }
 template <typename T, int NB, int RPT>
 static int gj_panel_launch(cudaStream_t s, int njobs, Pool<T> M, const int* slots, Pool<T> GP, Pool<T> RP,
-                           int* perm, int c0, unsigned* err) {
-    constexpr int CW = sizeof(T) == 4 ? 128 : 64;
-    // staging: up to 2*NB moved rows x CW columns (re, im), or the NB x 129 Rᵀ tile (re, im)
-    const size_t smem = gj_panel_smem_elems<NB, CW>() * sizeof(T);
+                           int* perm, int* rowsrc, int c0, unsigned* err) {
+    const size_t smem = gj_panel_smem_elems<NB>() * sizeof(T);
     static bool attr = false;
     if (!attr) {
         cudaError_t e = cudaFuncSetAttribute(gj_panel_kernel<T, NB, RPT>,
@@ -692,28 +726,29 @@ static int gj_panel_launch(cudaStream_t s, int njobs, Pool<T> M, const int* slot
         if (e != cudaSuccess) return (int)e;
         attr = true;
     }
-    gj_panel_kernel<T, NB, RPT><<<njobs, 512, smem, s>>>(M, slots, GP, RP, perm, c0, err);
+    gj_panel_kernel<T, NB, RPT><<<njobs, 512, smem, s>>>(M, slots, GP, RP, perm, rowsrc, c0, err);
     return (int)cudaGetLastError();
 }
 
 template <typename T>
 int launch_gj_panel(cudaStream_t s, int nb, int njobs, Pool<T> M, const int* slots, Pool<T> GP, Pool<T> RP,
-                    int* perm, int c0, unsigned* err) {
+                    int* perm, int* rowsrc, int c0, unsigned* err) {
     const bool two = M.rows > 512;
     if (M.rows > 1024) return (int)cudaErrorInvalidValue;
     if constexpr (sizeof(T) == 4) {
-        if (nb == 32 && !two) return gj_panel_launch<T, 32, 1>(s, njobs, M, slots, GP, RP, perm, c0, err);
-        if (nb == 16 && two) return gj_panel_launch<T, 16, 2>(s, njobs, M, slots, GP, RP, perm, c0, err);
+        if (nb == 32 && !two) return gj_panel_launch<T, 32, 1>(s, njobs, M, slots, GP, RP, perm, rowsrc, c0, err);
+        if (nb == 16 && two) return gj_panel_launch<T, 16, 2>(s, njobs, M, slots, GP, RP, perm, rowsrc, c0, err);
     } else {
-        if (nb == 16 && !two) return gj_panel_launch<T, 16, 1>(s, njobs, M, slots, GP, RP, perm, c0, err);
-        if (nb == 8 && two) return gj_panel_launch<T, 8, 2>(s, njobs, M, slots, GP, RP, perm, c0, err);
+        if (nb == 16 && !two) return gj_panel_launch<T, 16, 1>(s, njobs, M, slots, GP, RP, perm, rowsrc, c0, err);
+        if (nb == 8 && two) return gj_panel_launch<T, 8, 2>(s, njobs, M, slots, GP, RP, perm, rowsrc, c0, err);
     }
     return (int)cudaErrorInvalidValue;
 }
-
 template <typename T>
-void launch_gj_unpermute(cudaStream_t s, int njobs, Pool<T> M, const int* slots, const int* perm) {
-    gj_unpermute_kernel<T><<<dim3(ceil_div(M.rows, 8), njobs), 256, 2 * M.rows * sizeof(T), s>>>(M, slots, perm);
+void launch_gj_unpermute(cudaStream_t s, int njobs, Pool<T> Src, const int* sslots, Pool<T> Dst,
+                         const int* dslots, const int* perm) {
+    gj_unpermute_kernel<T><<<dim3(ceil_div(Src.rows, 8), njobs), 256, 2 * Src.rows * sizeof(T), s>>>(
+        Src, sslots, Dst, dslots, perm);
 }
 template <typename T>
 void launch_madd(cudaStream_t s, int njobs, Pool<T> P, const int3* jobs) {
@@ -729,9 +764,10 @@ void launch_mcopy(cudaStream_t s, int njobs, Pool<T> S, Pool<T> Dp, const int3* 
                                           const int*);                                                       \
     template void launch_level1_combine<T>(cudaStream_t, int, NodeMap, const cplx<double>*, double, Pool<T>,  \
                                            Pool<T>, const L1Job*);                                           \
-    template int launch_gj_panel<T>(cudaStream_t, int, int, Pool<T>, const int*, Pool<T>, Pool<T>, int*, int, \
-                                    unsigned*);                                                              \
-    template void launch_gj_unpermute<T>(cudaStream_t, int, Pool<T>, const int*, const int*);                \
+    template int launch_gj_panel<T>(cudaStream_t, int, int, Pool<T>, const int*, Pool<T>, Pool<T>, int*, int*,\
+                                    int, unsigned*);                                                         \
+    template void launch_gj_unpermute<T>(cudaStream_t, int, Pool<T>, const int*, Pool<T>, const int*,        \
+                                         const int*);                                                       \
     template void launch_madd<T>(cudaStream_t, int, Pool<T>, const int3*);                                    \
     template void launch_mcopy<T>(cudaStream_t, int, Pool<T>, Pool<T>, const int3*);                         \
     template void launch_tri_inverse<T>(cudaStream_t, int, NodeMap, const cplx<double>*, double, Pool<T>,    \

@@ -78,9 +78,11 @@ struct StepJobs {     // offsets into the job blob
 
 template <typename T> struct FactorStore {
     Pool<T> D, C, X, GP, RP;
+    Pool<T> Tg;                 // Gauss-Jordan ping-pong buffer (re, im planes)
     T* rv = nullptr; T* xv = nullptr; T* wv = nullptr;
     int vec_nrhs = 0;
     int* perm = nullptr;
+    int* rowsrc = nullptr;      // per-panel composed row exchanges
     bool tc_ok = false;
     TcMaps tc;       // TMA descriptors (FP32 only)
 };
@@ -492,6 +494,13 @@ template <typename T> int alloc_factor(fdfd_handle* h) {
     RET(alloc_pool<T>(h, F.GP, b, pc, pc, planes, h->max_ne));
     RET(alloc_pool<T>(h, F.RP, b, pc, pc, planes, h->max_ne));
     RET(dev_alloc(h, (void**)&F.perm, (size_t)h->max_ne * b * sizeof(int)));
+    RET(dev_alloc(h, (void**)&F.rowsrc, (size_t)h->max_ne * b * sizeof(int)));
+    // largest Gauss-Jordan batch: the eliminated nodes of steps >= 2 (and of step 1
+    // when it inverts by Gauss-Jordan), or the final pair's single matrices
+    int gj_max = 1;
+    for (int e = 1; e < (int)h->sj.size(); ++e)
+        if (e >= 2 || h->level1_gj) gj_max = std::max(gj_max, h->sj[e].ne);
+    RET(alloc_pool<T>(h, F.Tg, b, b, ld, 2, gj_max));
     if (sizeof(T) == 4 && h->use_tc) {
         F.tc_ok = tc_make_maps(reinterpret_cast<Pool<float>*>(&F.D), reinterpret_cast<Pool<float>*>(&F.C),
                                reinterpret_cast<Pool<float>*>(&F.X), reinterpret_cast<Pool<float>*>(&F.GP),
@@ -519,7 +528,7 @@ template <typename T> int alloc_vectors(fdfd_handle* h, int nrhs) {
 // ---------------------------------------------------------------------------
 // GEMM dispatch
 // ---------------------------------------------------------------------------
-enum PoolId { P_D = 0, P_C = 1, P_X = 2, P_GP = 3, P_RP = 4 };
+enum PoolId { P_D = 0, P_C = 1, P_X = 2, P_GP = 3, P_RP = 4, P_TG = 5 };
 
 template <typename T> Pool<T>& pool_of(FactorStore<T>& F, int id) {
     switch (id) {
@@ -527,6 +536,7 @@ template <typename T> Pool<T>& pool_of(FactorStore<T>& F, int id) {
         case P_C: return F.C;
         case P_X: return F.X;
         case P_GP: return F.GP;
+        case P_TG: return F.Tg;
         default: return F.RP;
     }
 }
@@ -534,12 +544,15 @@ template <typename T> Pool<T>& pool_of(FactorStore<T>& F, int id) {
 template <typename T>
 int gemm(fdfd_handle* h, int pa, int pb, int pc, const int* a_slot, const int* b_slot, const int* c_slot,
          const int* c_trans_arr, int c_trans, int njobs, int M, int N, int K, T alpha, int beta, int mask_c0,
-         int mask_w, int write_lo = 1) {
+         int mask_w, int write_lo = 1, int pcin = -1, const int* cin_slot = nullptr,
+         const int* row_src = nullptr, int prof_cls = -1, double prof_work = 0.0) {
     if (njobs == 0) return FDFD_OK;
     FactorStore<T>& F = store<T>(h);
     GemmArgs<T> g;
     g.A = pool_of(F, pa); g.B = pool_of(F, pb); g.C = pool_of(F, pc);
     g.a_slot = a_slot; g.b_slot = b_slot; g.c_slot = c_slot;
+    g.Cin = pcin >= 0 ? pool_of(F, pcin) : Pool<T>();
+    g.cin_slot = cin_slot; g.row_src = row_src;
     g.M = M; g.N = N; g.K = K; g.alpha = alpha; g.beta = beta;
     g.mask_c0 = mask_c0; g.mask_w = mask_w; g.c_trans = c_trans;
     g.c_trans_arr = nullptr;
@@ -551,14 +564,14 @@ int gemm(fdfd_handle* h, int pa, int pb, int pc, const int* a_slot, const int* b
         int rc = tc_gemm_launch(reinterpret_cast<GemmArgs<float>*>(&g), c_trans_arr, pa, pb, njobs, &F.tc,
                                 h->stream);
         if (rc != 0) return set_err(h, FDFD_ECUDA, "tcgen05 GEMM launch failed (%d)", rc);
-        prof_end(h, ev, FDFD_PROF_GEMM_TC, flops);
+        prof_end(h, ev, prof_cls >= 0 ? prof_cls : FDFD_PROF_GEMM_TC, prof_cls >= 0 ? prof_work : flops);
         h->launches++;
         h->tc_used = 1;
         return check_launch(h, "gemm_tc");
     }
     g.c_trans_arr = c_trans_arr;
     launch_gemm_simt<T>(h->stream, njobs, g);
-    prof_end(h, ev, FDFD_PROF_GEMM_SIMT, flops);
+    prof_end(h, ev, prof_cls >= 0 ? prof_cls : FDFD_PROF_GEMM_SIMT, prof_cls >= 0 ? prof_work : flops);
     h->launches++;
     return check_launch(h, "gemm_simt");
 }
@@ -571,20 +584,31 @@ template <typename T> int gj_invert(fdfd_handle* h, const int* d_slots, const in
     FactorStore<T>& F = store<T>(h);
     const int b = h->map.b;
     const int nb = panel_nb<T>(b);
+    if (njobs > F.Tg.count) return set_err(h, FDFD_EINVAL, "Gauss-Jordan batch %d exceeds %lld", njobs, F.Tg.count);
     launch_perm_init(h->stream, njobs, F.perm, b);
     h->launches++;
+    // the matrices alternate between the D slots and the ping-pong buffer: each
+    // panel's update reads the current buffer through the panel's row exchanges
+    // and writes the other one
+    int cur = P_D, alt = P_TG;
+    const int* cur_slots = d_slots;
+    const int* alt_slots = d_iota;
     for (int c0 = 0; c0 < b; c0 += nb) {
         int w = std::min(nb, b - c0);
         int ev = prof_begin(h);
-        int e = launch_gj_panel<T>(h->stream, nb, njobs, F.D, d_slots, F.GP, F.RP, F.perm, c0, h->derr);
+        int e = launch_gj_panel<T>(h->stream, nb, njobs, pool_of(F, cur), cur_slots, F.GP, F.RP, F.perm, F.rowsrc,
+                                   c0, h->derr);
         prof_end(h, ev, FDFD_PROF_GJ_PANEL, 0.0);
         h->launches++;
         if (e) return set_err(h, FDFD_ECUDA, "gj_panel launch failed: %s", cudaGetErrorString((cudaError_t)e));
         // no residual planes here: gj_unpermute_kernel rewrites every element of the inverse
-        RET(gemm<T>(h, P_GP, P_RP, P_D, d_iota, d_iota, d_slots, nullptr, 0, njobs, b, b, F.GP.cols, (T)1, 1,
-                    c0, w, 0));
+        RET(gemm<T>(h, P_GP, P_RP, alt, d_iota, d_iota, alt_slots, nullptr, 0, njobs, b, b, F.GP.cols, (T)1, 1,
+                    c0, w, 0, cur, cur_slots, F.rowsrc, FDFD_PROF_GJ_UPDATE,
+                    4.0 * sizeof(T) * (double)b * b * njobs));
+        std::swap(cur, alt);
+        std::swap(cur_slots, alt_slots);
     }
-    launch_gj_unpermute<T>(h->stream, njobs, F.D, d_slots, F.perm);
+    launch_gj_unpermute<T>(h->stream, njobs, pool_of(F, cur), cur_slots, F.D, d_slots, F.perm);
     h->launches++;
     return check_launch(h, "gj_unpermute");
 }
@@ -612,11 +636,14 @@ template <typename T> int factor_impl(fdfd_handle* h) {
             } else {
                 int ev = prof_begin(h);
                 launch_tri_inverse<T>(h->stream, ne, h->map, h->st, h->scale, F.D, J<int>(h, S.elim), h->derr);
-                prof_end(h, ev, FDFD_PROF_OTHER, 0.0);
+                prof_end(h, ev, FDFD_PROF_LEVEL1, (double)F.D.planes * sizeof(T) * b * b * ne);
                 h->launches++;
                 RET(check_launch(h, "tri_inverse"));
             }
+            // bytes: two inverses read (re, im), D and both couplings written (all planes)
+            int ev1 = prof_begin(h);
             launch_level1_combine<T>(h->stream, S.nl1, h->map, h->st, h->scale, F.D, F.C, J<L1Job>(h, S.l1));
+            prof_end(h, ev1, FDFD_PROF_LEVEL1, (4.0 + 3.0 * F.D.planes) * sizeof(T) * b * b * S.nl1);
             h->launches++;
             RET(check_launch(h, "level1_combine"));
         } else {
@@ -1614,6 +1641,7 @@ int debug_gemm_impl(int M, int N, int K, const double* A, const double* B, doubl
         GemmArgs<T> g;
         g.A = PA; g.B = PB; g.C = PC;
         g.a_slot = g.b_slot = g.c_slot = slots;
+        g.Cin = Pool<T>(); g.cin_slot = nullptr; g.row_src = nullptr;
         g.M = M; g.N = N; g.K = K; g.alpha = (T)1; g.beta = 0; g.mask_c0 = 0; g.mask_w = 0;
         g.c_trans = 0; g.c_trans_arr = nullptr; g.write_lo = 1; g.err = derr;
         cudaEvent_t e0, e1;

@@ -66,6 +66,12 @@ __global__ void __launch_bounds__(256) gemm_simt_kernel(GemmArgs<T> g) {
     }
     // epilogue
     const int ctr = g.c_trans_arr ? g.c_trans_arr[job] : g.c_trans;
+    // β term source: C itself, or row row_src[m] of Cin (N-form only)
+    const bool sep = g.Cin.base != nullptr;
+    const T* Ci = sep ? g.Cin.slot(g.cin_slot[job]) : C;
+    const long long cipe = sep ? g.Cin.plane_elems() : cpe;
+    const long long cild = sep ? (long long)g.Cin.ld : (long long)g.C.ld;
+    const int* rsrc = (sep && g.row_src) ? g.row_src + (long long)job * g.M : nullptr;
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
         int m = m0 + ty * 4 + i;
@@ -78,7 +84,11 @@ __global__ void __launch_bounds__(256) gemm_simt_kernel(GemmArgs<T> g) {
             T vr = g.alpha * accr[i][j], vi = g.alpha * acci[i][j];
             bool masked = mrow || (n >= g.mask_c0 && n < g.mask_c0 + g.mask_w);
             long long off = ctr ? (long long)n * g.C.ld + m : (long long)m * g.C.ld + n;
-            if (g.beta && !masked) { vr += C[off]; vi += C[cpe + off]; }
+            if (g.beta && !masked) {
+                const long long io = ctr ? off : (long long)(rsrc ? rsrc[m] : m) * cild + n;
+                vr += Ci[io];
+                vi += Ci[cipe + io];
+            }
             C[off] = vr;
             C[cpe + off] = vi;
             if (g.C.planes == 4 && g.write_lo) {

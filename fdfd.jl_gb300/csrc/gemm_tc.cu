@@ -1,7 +1,7 @@
 // Batched complex TN GEMM on the sm_103a tensor cores: tcgen05.mma kind::tf32
 // with 3xTF32 split precision, TMA-staged operands, accumulators in TMEM.
 //
-//   C[m][n] = beta(m,n)·C[m][n] + alpha·Σ_k A[m][k]·B[n][k]      (complex)
+//   C[m][n] = beta(m,n)·Cin[src(m)][n] + alpha·Σ_k A[m][k]·B[n][k]      (complex)
 //
 // Operands are FP32 planar pools whose slots hold four planes: re, im and
 // their TF32 residuals lo = x - (x with the low 13 mantissa bits cleared).
@@ -244,9 +244,22 @@ __global__ void __launch_bounds__(192, 1)
             float* C = g.C.slot(g.c_slot[job]);
             const long long pe = g.C.plane_elems();
             const long long ld = g.C.ld;
+            // β term source: C itself, or row row_src[m] of Cin
+            const bool sep = g.Cin.base != nullptr;
+            const float* Ci = sep ? g.Cin.slot(g.cin_slot[job]) : C;
+            const long long cipe = sep ? g.Cin.plane_elems() : pe;
+            const long long cild = sep ? (long long)g.Cin.ld : ld;
+            const int* rsrc = (sep && g.row_src) ? g.row_src + (long long)job * g.M : nullptr;
             const uint32_t lane_off = (uint32_t)(q * 32) << 16;
             // per-warp staging tile (the pipeline buffers are idle once the accumulator is final)
             float* stg = reinterpret_cast<float*>(smem) + q * (2 * 32 * 36);
+            // β-source row offsets of the 8 rows this lane reads in the row-major epilogue
+            long long srow[8];
+#pragma unroll
+            for (int it = 0; it < 8; ++it) {
+                const int r = row0 + 4 * it + (lane >> 3);
+                srow[it] = (long long)(rsrc && r < g.M ? rsrc[r] : r) * cild;
+            }
             for (int ch = 0; ch < BN / 32; ++ch) {
                 const int nb = n0 + ch * 32;
                 if (nb >= g.N) break;
@@ -297,16 +310,17 @@ __global__ void __launch_bounds__(192, 1)
                         const int r = row0 + 4 * it + sub;
                         cre[it] = make_float4(0.f, 0.f, 0.f, 0.f);
                         cim[it] = cre[it];
-                        if (g.beta && r < g.M) {
-                            const long long off = (long long)r * ld + n;
+                        const bool mrow = (r >= g.mask_c0 && r < g.mask_c0 + g.mask_w);
+                        if (g.beta && r < g.M && !mrow) {
+                            const long long off = srow[it] + n;
                             if (full4) {
-                                cre[it] = __ldcg(reinterpret_cast<const float4*>(C + off));
-                                cim[it] = __ldcg(reinterpret_cast<const float4*>(C + pe + off));
+                                cre[it] = __ldcg(reinterpret_cast<const float4*>(Ci + off));
+                                cim[it] = __ldcg(reinterpret_cast<const float4*>(Ci + cipe + off));
                             } else {
                                 float* a = reinterpret_cast<float*>(&cre[it]);
                                 float* c = reinterpret_cast<float*>(&cim[it]);
                                 for (int e = 0; e < 4; ++e)
-                                    if (n + e < g.N) { a[e] = __ldcg(C + off + e); c[e] = __ldcg(C + pe + off + e); }
+                                    if (n + e < g.N) { a[e] = __ldcg(Ci + off + e); c[e] = __ldcg(Ci + cipe + off + e); }
                             }
                         }
                     }

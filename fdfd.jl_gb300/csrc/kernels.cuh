@@ -69,12 +69,17 @@ void launch_perm_init(cudaStream_t s, int njobs, int* perm, int b);
 template <typename T>
 void launch_tri_inverse(cudaStream_t s, int njobs, NodeMap m, const cplx<double>* st, double scale, Pool<T> D,
                         const int* nodes, unsigned* err);
-// Gauss-Jordan panel step with panel width nb (returns a cudaError_t value)
+// Gauss-Jordan panel step with panel width nb on the matrices M[slots[job]]
+// (returns a cudaError_t value).  Writes the panel transformation to GP, the
+// transposed pivot rows to RP, updates perm and writes rowsrc[job][r], the
+// row of M that lands at row r after this panel's interchanges.
 template <typename T>
 int launch_gj_panel(cudaStream_t s, int nb, int njobs, Pool<T> M, const int* slots, Pool<T> GP, Pool<T> RP,
-                    int* perm, int c0, unsigned* err);
+                    int* perm, int* rowsrc, int c0, unsigned* err);
+// Dst[dslots[job]][r][perm[j]] = Src[sslots[job]][r][j] (Src may equal Dst); writes the TF32 residual planes
 template <typename T>
-void launch_gj_unpermute(cudaStream_t s, int njobs, Pool<T> M, const int* slots, const int* perm);
+void launch_gj_unpermute(cudaStream_t s, int njobs, Pool<T> Src, const int* sslots, Pool<T> Dst,
+                         const int* dslots, const int* perm);
 // C[dst] = A[s1] + A[s2] (same storage form); also writes lo planes
 template <typename T>
 void launch_madd(cudaStream_t s, int njobs, Pool<T> P, const int3* jobs);
@@ -84,11 +89,16 @@ void launch_mcopy(cudaStream_t s, int njobs, Pool<T> S, Pool<T> Dp, const int3* 
 
 // ---- gemm_simt.cu / gemm_tc.cu --------------------------------------------
 // Batched complex "TN" GEMM on planar pools:
-//   C[m][n] = beta(m,n)·C[m][n] + alpha·Σ_k A[m][k]·B[n][k]
+//   C[m][n] = beta(m,n)·Cin[src(m)][n] + alpha·Σ_k A[m][k]·B[n][k]
 // with A, B, C row-major slots; beta(m,n) = beta unless m or n lies in
 // [mask_c0, mask_c0 + mask_w), where it is 0; c_trans stores Cᵀ instead.
+// Cin is C itself (src(m) = m) unless Cin.base is set; then src(m) =
+// row_src[job*M + m] when row_src is set.
 template <typename T> struct GemmArgs {
     Pool<T> A, B, C;
+    Pool<T> Cin;
+    const int* cin_slot;
+    const int* row_src;
     const int* a_slot; const int* b_slot; const int* c_slot;
     int M, N, K;
     T alpha; int beta;

@@ -153,16 +153,20 @@ int  fdfd_apply(fdfd_handle* h, const double* x, int nrhs, double* y);
  * and accumulates device time and algorithmic work (flops for GEMMs, bytes
  * for the HBM-bound kernels).  fdfd_set_profiling(h, 1) resets the totals. */
 typedef struct {
-    double ms[6];            /* device time per class                           */
-    double work[6];          /* flops (classes 0, 1) or bytes (classes 3, 4, 5)  */
-    long long launches[6];   /* launches per class                              */
+    double ms[8];            /* device time per class                           */
+    double work[8];          /* flops (classes 0, 1) or bytes (the others)       */
+    long long launches[8];   /* launches per class                              */
 } fdfd_profile;
-#define FDFD_PROF_GEMM_TC   0  /* tcgen05 3xTF32 block GEMM (flops, complex 8MNK) */
-#define FDFD_PROF_GEMM_SIMT 1  /* CUDA-core block GEMM (flops)                    */
+#define FDFD_PROF_GEMM_TC   0  /* tcgen05 3xTF32 Schur-update GEMMs (flops, 8MNK) */
+#define FDFD_PROF_GEMM_SIMT 1  /* CUDA-core Schur-update GEMMs (flops)            */
 #define FDFD_PROF_GJ_PANEL  2  /* Gauss-Jordan panel steps                        */
 #define FDFD_PROF_SWEEP     3  /* solve sweeps: block GEMV (factor bytes read)    */
 #define FDFD_PROF_RESIDUAL  4  /* FP64 stencil residual / product (bytes)         */
 #define FDFD_PROF_OTHER     5  /* assembly, layout, Krylov vector kernels         */
+#define FDFD_PROF_GJ_UPDATE 6  /* Gauss-Jordan rank-panel updates, either GEMM    */
+                               /* (bytes: each matrix read and written once)      */
+#define FDFD_PROF_LEVEL1    7  /* first reduction step: O(b^2) inverses and Schur */
+                               /* updates (bytes of the blocks written)           */
 int  fdfd_set_profiling(fdfd_handle* h, int on);
 int  fdfd_get_profile(fdfd_handle* h, fdfd_profile* out);
 
