@@ -17,12 +17,13 @@ __device__ __forceinline__ cplx<double> st_at(const cplx<double>* st, const Node
 }
 
 template <typename T>
-__device__ __forceinline__ void store_elem(const Pool<T>& P, T* base, int r, int c, cplx<T> v, int trans) {
+__device__ __forceinline__ void store_elem(const Pool<T>& P, T* base, int r, int c, cplx<T> v, int trans,
+                                           bool lo = true) {
     long long off = trans ? (long long)c * P.ld + r : (long long)r * P.ld + c;
     long long pe = P.plane_elems();
     base[off] = v.re;
     base[pe + off] = v.im;
-    if (P.planes == 4) {
+    if (lo && P.planes == 4) {
         base[2 * pe + off] = (T)tf32_lo((float)v.re);
         base[3 * pe + off] = (T)tf32_lo((float)v.im);
     }
@@ -112,7 +113,8 @@ __global__ void level1_combine_kernel(NodeMap m, const cplx<double>* st, double 
             } else if (c == r) {
                 uv = us;
             }
-            store_elem<T>(D, Ds, r, c, dv, 0);
+            // re/im only: D_s is read as re/im until its inversion writes all planes
+            store_elem<T>(D, Ds, r, c, dv, 0, false);
         }
         if (!J.u_trans) { if (ok) store_elem<T>(C, C.slot(J.u_slot), r, c, uv, 0); }
         else { tU[0][rl][tx] = uv.re; tU[1][rl][tx] = uv.im; }
@@ -183,10 +185,13 @@ __global__ void __launch_bounds__(512, 1) gj_panel_kernel(Pool<T> M, const int* 
     constexpr int NT = 512;
     constexpr int VW = 16 / sizeof(T);                 // elements per 16-byte vector
     typedef typename Vec16<T>::type VT;
-    __shared__ __align__(16) T xpr[NB], xpi[NB];       // pivot row (rotated positions) before scaling
-    __shared__ __align__(16) T xrr[NB], xri[NB];       // row r0 (exchange partner)
-    __shared__ T redv[NT / 32];
-    __shared__ int redi[NT / 32];
+    constexpr int NW = NT / 32;
+    // per step (double-buffered by step parity): each warp's candidate pivot row,
+    // its key and row index, and row r0 (the exchange partner)
+    __shared__ __align__(16) T cand_r[2][NW][NB], cand_i[2][NW][NB];
+    __shared__ __align__(16) T xrr[2][NB], xri[2][NB];
+    __shared__ unsigned cand_key[2][NW];
+    __shared__ int cand_row[2][NW];
     __shared__ int pivs[NB];
     __shared__ int rsm[NT * RPT];                      // composed row exchanges
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -225,78 +230,73 @@ __global__ void __launch_bounds__(512, 1) gj_panel_kernel(Pool<T> M, const int* 
         }
     }
 
+    // One barrier per column step.  Pivot key: the bit pattern of the FP32 value
+    // |re|+|im| (non-negative floats order like their bit patterns; NaN sorts
+    // above +inf, so a NaN column entry is picked and reported as singular).
+    // Ties go to the lowest row.
 #pragma unroll 1
     for (int jj = 0; jj < w; ++jj) {
         const int r0 = c0 + jj;
-        // ---- block argmax over rows >= r0 of the pivot column (ties: lowest row)
-        T best = (T)-1;
-        int bi = b;
+        const int q = jj & 1;
+        unsigned key = 0;
+        int row = INT_MAX, tsel = -1;
 #pragma unroll
         for (int t = 0; t < RPT; ++t) {
             const int i = tid + t * NT;
             if (i >= r0 && i < b) {
-                const T m = fabs(vr[t][0]) + fabs(vi[t][0]);
-                if (m > best) { best = m; bi = i; }
+                const unsigned k = __float_as_uint((float)(fabs(vr[t][0]) + fabs(vi[t][0])));
+                if (tsel < 0 || k > key) { key = k; row = i; tsel = t; }
             }
         }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            const T ov = __shfl_down_sync(0xffffffffu, best, o);
-            const int oi = __shfl_down_sync(0xffffffffu, bi, o);
-            if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
-        }
-        if (lane == 0) { redv[warp] = best; redi[warp] = bi; }
-        __syncthreads();
-        best = lane < NT / 32 ? redv[lane] : (T)-1;
-        bi = lane < NT / 32 ? redi[lane] : b;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            const T ov = __shfl_xor_sync(0xffffffffu, best, o);
-            const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-            if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
-        }
-        int piv = bi;
-        if (!(best > (T)0) || piv >= b || !isfinite((double)best)) {
-            if (tid == 0) dev_error(err, FDFD_DEVERR_SINGULAR);
-            piv = r0;
-        }
-        if (tid == 0) pivs[jj] = piv;
-        // ---- the owners of rows piv and r0 publish them (16-byte stores)
+        const unsigned wkey = __reduce_max_sync(0xffffffffu, key);
+        const int wrow = __reduce_min_sync(0xffffffffu, key == wkey ? row : INT_MAX);
+        // the warp's winner publishes its row; lane 0 publishes key and row index
 #pragma unroll
         for (int t = 0; t < RPT; ++t) {
-            const int i = tid + t * NT;
-            if (i == piv) {
+            if (tsel == t && row == wrow) {
 #pragma unroll
-                for (int q = 0; q < NB / VW; ++q) {
+                for (int v = 0; v < NB / VW; ++v) {
                     VT a, c;
 #pragma unroll
                     for (int e = 0; e < VW; ++e) {
-                        reinterpret_cast<T*>(&a)[e] = vr[t][q * VW + e];
-                        reinterpret_cast<T*>(&c)[e] = vi[t][q * VW + e];
+                        reinterpret_cast<T*>(&a)[e] = vr[t][v * VW + e];
+                        reinterpret_cast<T*>(&c)[e] = vi[t][v * VW + e];
                     }
-                    reinterpret_cast<VT*>(xpr)[q] = a;
-                    reinterpret_cast<VT*>(xpi)[q] = c;
+                    reinterpret_cast<VT*>(cand_r[q][warp])[v] = a;
+                    reinterpret_cast<VT*>(cand_i[q][warp])[v] = c;
                 }
             }
-            if (i == r0 && piv != r0) {
+            if (tid + t * NT == r0) {
 #pragma unroll
-                for (int q = 0; q < NB / VW; ++q) {
+                for (int v = 0; v < NB / VW; ++v) {
                     VT a, c;
 #pragma unroll
                     for (int e = 0; e < VW; ++e) {
-                        reinterpret_cast<T*>(&a)[e] = vr[t][q * VW + e];
-                        reinterpret_cast<T*>(&c)[e] = vi[t][q * VW + e];
+                        reinterpret_cast<T*>(&a)[e] = vr[t][v * VW + e];
+                        reinterpret_cast<T*>(&c)[e] = vi[t][v * VW + e];
                     }
-                    reinterpret_cast<VT*>(xrr)[q] = a;
-                    reinterpret_cast<VT*>(xri)[q] = c;
+                    reinterpret_cast<VT*>(xrr[q])[v] = a;
+                    reinterpret_cast<VT*>(xri[q])[v] = c;
                 }
             }
         }
+        if (lane == 0) { cand_key[q][warp] = wkey; cand_row[q][warp] = wrow; }
         __syncthreads();
-        // ---- scaled pivot row (formed by every thread from shared memory);
-        //      owner(r0) keeps it, owner(piv) takes the old row r0, everyone eliminates
+        // block winner (every warp computes it); row r0 is always a candidate, so piv is in [r0, b)
+        const unsigned ck = lane < NW ? cand_key[q][lane] : 0u;
+        const int cr = lane < NW ? cand_row[q][lane] : INT_MAX;
+        const unsigned gkey = __reduce_max_sync(0xffffffffu, ck);
+        const int piv = __reduce_min_sync(0xffffffffu, (lane < NW && ck == gkey) ? cr : INT_MAX);
+        const T* xpr = cand_r[q][(piv & (NT - 1)) >> 5];
+        const T* xpi = cand_i[q][(piv & (NT - 1)) >> 5];
+        if (tid == 0) pivs[jj] = piv;
+        // scaled pivot row (formed by every thread from shared memory); the owner
+        // of r0 keeps it, the owner of piv takes the old row r0, every other row
+        // is eliminated
         const cplx<T> p = cmk(xpr[0], xpi[0]);
-        const cplx<T> inv = (p.re == (T)0 && p.im == (T)0) ? cmk((T)0, (T)0) : cinv(p);
+        const bool bad = !(fabs(p.re) + fabs(p.im) > (T)0) || !isfinite(p.re) || !isfinite(p.im);
+        if (bad && tid == 0) dev_error(err, FDFD_DEVERR_SINGULAR);
+        const cplx<T> inv = bad ? cmk((T)0, (T)0) : cinv(p);
 #pragma unroll
         for (int t = 0; t < RPT; ++t) {
             const int i = tid + t * NT;
@@ -313,7 +313,7 @@ __global__ void __launch_bounds__(512, 1) gj_panel_kernel(Pool<T> M, const int* 
             } else {
                 if (i == piv) {
 #pragma unroll
-                    for (int k = 0; k < NB; ++k) { vr[t][k] = xrr[k]; vi[t][k] = xri[k]; }
+                    for (int k = 0; k < NB; ++k) { vr[t][k] = xrr[q][k]; vi[t][k] = xri[q][k]; }
                 }
                 const cplx<T> fi = cmul(cmk(vr[t][0], vi[t][0]), inv);   // f / p
                 vr[t][0] = -fi.re;
@@ -699,6 +699,12 @@ template <typename T>
 void launch_tri_inverse(cudaStream_t s, int njobs, NodeMap m, const cplx<double>* st, double scale, Pool<T> D,
                         const int* nodes, unsigned* err) {
     size_t smem = 6 * (size_t)m.b * sizeof(cplx<T>) + (size_t)m.b * sizeof(int);
+    // above 48 KB (FP64 blocks of more than ~500 unknowns) the kernel must opt in
+    static size_t opted = 48 * 1024;
+    if (smem > opted &&
+        cudaFuncSetAttribute(tri_inverse_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) ==
+            cudaSuccess)
+        opted = smem;
     tri_inverse_kernel<T><<<njobs, 512, smem, s>>>(m, st, scale, D, nodes, err);
 }
 template <typename T>

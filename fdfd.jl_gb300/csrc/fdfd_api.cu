@@ -640,10 +640,10 @@ template <typename T> int factor_impl(fdfd_handle* h) {
                 h->launches++;
                 RET(check_launch(h, "tri_inverse"));
             }
-            // bytes: two inverses read (re, im), D and both couplings written (all planes)
+            // bytes: two inverses read (re, im), D written (re, im), both couplings written (all planes)
             int ev1 = prof_begin(h);
             launch_level1_combine<T>(h->stream, S.nl1, h->map, h->st, h->scale, F.D, F.C, J<L1Job>(h, S.l1));
-            prof_end(h, ev1, FDFD_PROF_LEVEL1, (4.0 + 3.0 * F.D.planes) * sizeof(T) * b * b * S.nl1);
+            prof_end(h, ev1, FDFD_PROF_LEVEL1, (6.0 + 2.0 * F.C.planes) * sizeof(T) * b * b * S.nl1);
             h->launches++;
             RET(check_launch(h, "level1_combine"));
         } else {
@@ -651,11 +651,12 @@ template <typename T> int factor_impl(fdfd_handle* h) {
             // Xᵀ = [Lᵀ; Uᵀ] Gᵀ
             RET(gemm<T>(h, P_C, P_D, P_X, J<int>(h, S.xt_a), J<int>(h, S.xt_b), J<int>(h, S.xt_c), nullptr, 0,
                         2 * ne, b, b, b, (T)1, 0, 0, 0));
-            // D_p -= U_p X_L ; D_q -= L_q X_R
+            // D_p -= U_p X_L ; D_q -= L_q X_R.  No residual planes: a D block is only
+            // read as re/im until its inversion writes G with all planes.
             RET(gemm<T>(h, P_C, P_X, P_D, J<int>(h, S.dp_a), J<int>(h, S.dp_b), J<int>(h, S.dp_c), nullptr, 0,
-                        ne, b, b, b, (T)-1, 1, 0, 0));
+                        ne, b, b, b, (T)-1, 1, 0, 0, 0));
             RET(gemm<T>(h, P_C, P_X, P_D, J<int>(h, S.dq_a), J<int>(h, S.dq_b), J<int>(h, S.dq_c), nullptr, 0,
-                        ne, b, b, b, (T)-1, 1, 0, 0));
+                        ne, b, b, b, (T)-1, 1, 0, 0, 0));
             // new couplings U_p' = -U_p X_R, L_q' = -L_q X_L (storage form per node)
             RET(gemm<T>(h, P_C, P_X, P_C, J<int>(h, S.cp_a), J<int>(h, S.cp_b), J<int>(h, S.cp_c),
                         J<int>(h, S.cp_t), 0, S.ncp, b, b, b, (T)-1, 0, 0, 0));
@@ -675,7 +676,7 @@ template <typename T> int factor_impl(fdfd_handle* h) {
     RET(gemm<T>(h, P_C, P_D, P_X, J<int>(h, h->fin_xt_a), J<int>(h, h->fin_xt_b), J<int>(h, h->fin_xt_c), nullptr,
                 0, 1, b, b, b, (T)1, 0, 0, 0));
     RET(gemm<T>(h, P_C, P_X, P_D, J<int>(h, h->fin_da_a), J<int>(h, h->fin_da_b), J<int>(h, h->fin_da_c), nullptr,
-                0, 1, b, b, b, (T)-1, 1, 0, 0));
+                0, 1, b, b, b, (T)-1, 1, 0, 0, 0));
     RET(gj_invert<T>(h, J<int>(h, h->fin_a_slot), J<int>(h, h->fin_iota), 1));
     flops += 8.0 * b3 * 4;
     h->last_factor_flops = flops;

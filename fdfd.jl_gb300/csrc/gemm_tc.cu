@@ -70,6 +70,12 @@ __device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map
         : "memory");
 }
 
+// bulk prefetch of a global range into L2 (16-byte aligned address, size a multiple of 16)
+__device__ __forceinline__ void l2_prefetch(const void* src, uint32_t bytes) {
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(reinterpret_cast<uint64_t>(src)), "r"(bytes)
+                 : "memory");
+}
+
 // tcgen05 shared-memory matrix descriptor, K-major, 32-byte swizzle:
 // start address >> 4 (bits 0-13), leading byte offset >> 4 (16-29, unused for
 // swizzled K-major), stride byte offset >> 4 (32-45: 8 rows x 32 B = 256 B
@@ -231,6 +237,24 @@ __global__ void __launch_bounds__(192, 1)
     } else {
         // epilogue warps 2..5; TMEM lane quarter = warp % 4
         const int q = warp & 3;
+        // A short-K product (the Gauss-Jordan rank-panel update) is bound by its β read:
+        // each lane pulls its β row (re, im) into L2 while the MMAs run.  Rows are
+        // ld-padded, so the range [n0, min(n0 + BN, ld)) is 16-byte aligned and sized.
+        if (g.beta && nk <= STAGES && !(g.c_trans_arr ? g.c_trans_arr[job] : g.c_trans)) {
+            const bool sep = g.Cin.base != nullptr;
+            const float* Ci = sep ? g.Cin.slot(g.cin_slot[job]) : g.C.slot(g.c_slot[job]);
+            const long long cipe = sep ? g.Cin.plane_elems() : g.C.plane_elems();
+            const int cild = sep ? g.Cin.ld : g.C.ld;
+            const int* rsrc = (sep && g.row_src) ? g.row_src + (long long)job * g.M : nullptr;
+            const int r = m0 + q * 32 + lane;
+            const int ncols = min(BN, cild - n0);
+            const bool mrow = (r >= g.mask_c0 && r < g.mask_c0 + g.mask_w);
+            if (r < g.M && !mrow && ncols > 0) {
+                const float* src = Ci + (long long)(rsrc ? rsrc[r] : r) * cild + n0;
+                l2_prefetch(src, (uint32_t)ncols * 4u);
+                l2_prefetch(src + cipe, (uint32_t)ncols * 4u);
+            }
+        }
         const bool ok_l = mbar_wait(smem_u32(&bar_acc), 0);
         const bool ok = __all_sync(0xffffffffu, ok_l);
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");

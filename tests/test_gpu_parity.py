@@ -129,6 +129,46 @@ def test_point_guide_200x120(lib, fdfd, oracle):
         assert max(rel(f1, ref[0]), rel(f2, ref[1]), rel(f3, ref[2])) <= tol
 
 
+def test_block_size_above_512(lib, fdfd):
+    """Blocks of more than 512 unknowns take the two-rows-per-thread panel
+    kernels (FP32 panel width 16, FP64 width 8).  Both factorizations must
+    reach the residual bound, and the two fields must agree."""
+    Nx, Ny = 530, 516
+    rng = np.random.default_rng(5)
+    eps = rng.uniform(1, 3, (Nx, Ny)) + 1j * rng.uniform(0, 0.05, (Nx, Ny))
+    src = np.zeros((Nx, Ny), complex)
+    src[Nx // 3, Ny // 2] = 1j
+    src[2 * Nx // 3, Ny // 3] = 0.5
+    omega = 2 * np.pi * 299792458.0 / 1.55e-6
+    out = {}
+    for prec in (fdfd.FDFD_PREC_FP64, fdfd.FDFD_PREC_MIXED):
+        h = handle_for(fdfd, Nx, Ny, (12, 12), 0.05, 0.05, 4.0, np.log(1e-8), fdfd.TM, prec)
+        h.set_eps(eps)
+        h.factor(omega)
+        f1, _, _, st = h.solve(src)
+        h.close()
+        assert st.block == 516 and st.rel_residual <= TOL_RES
+        out[prec] = f1
+    assert rel(out[fdfd.FDFD_PREC_MIXED], out[fdfd.FDFD_PREC_FP64]) <= TOL_FIELD_MIXED
+
+
+def test_profile_classes(lib, fdfd):
+    """Per-class device timing: every class of a mixed solve is populated."""
+    from fdfd_gb300 import workloads as W
+    p = W.point_source_guide()
+    h = handle_for(fdfd, p.Nx, p.Ny, p.npml, p.dx, p.dy, p.pml_m, p.pml_lnR, fdfd.TM, fdfd.FDFD_PREC_MIXED)
+    h.set_eps(p.eps)
+    h.set_profiling(True)
+    h.factor(p.omega)
+    _, _, _, st = h.solve(p.src)
+    prof = h.profile()
+    h.close()
+    gk = "gemm_tc" if st.tc_gemm else "gemm_simt"
+    for k in (gk, "gj_panel", "gj_update", "sweep", "residual", "level1"):
+        assert prof[k]["launches"] > 0 and prof[k]["ms"] > 0, k
+    assert prof[gk]["work"] > 0 and prof["gj_update"]["work"] > 0 and prof["level1"]["work"] > 0
+
+
 def test_multi_rhs_matches_single(lib, fdfd, oracle):
     from fdfd_gb300 import workloads as W
     p = W.design_guide(96, 64, design=(24, 24), seed=3, npml=10)
