@@ -169,33 +169,48 @@ __global__ void perm_init_kernel(int* perm, int b) {
 // one (e.g. G. W. Stewart, Matrix Algorithms I, §3.1).
 // grid: njobs, block 512; requires b <= 512*RPT.
 // ---------------------------------------------------------------------------
-// shared staging elements of gj_panel_kernel: the NB x 129 Rᵀ transpose tile (re, im)
+// dynamic shared memory of gj_panel_kernel (elements of T): the larger of the
+// Rᵀ transpose tile (NB x 129, re and im) and the G staging tile (128 rows x NB+4)
 template <int NB>
 __host__ __device__ constexpr size_t gj_panel_smem_elems() {
-    return (size_t)2 * NB * 129;
+    return (size_t)2 * (NB * 129 > 128 * (NB + 4) ? NB * 129 : 128 * (NB + 4));
 }
 
 template <typename T> struct Vec16;
 template <> struct Vec16<float> { typedef float4 type; };
 template <> struct Vec16<double> { typedef double2 type; };
 
+// rotate a register row left by S positions (static indices only)
+template <typename T, int NB, int S>
+__device__ __forceinline__ void rotate_left(T (&v)[NB]) {
+    T tmp[S];
+#pragma unroll
+    for (int k = 0; k < S; ++k) tmp[k] = v[k];
+#pragma unroll
+    for (int k = 0; k + S < NB; ++k) v[k] = v[k + S];
+#pragma unroll
+    for (int k = 0; k < S; ++k) v[NB - S + k] = tmp[k];
+}
+
 template <typename T, int NB, int RPT>
 __global__ void __launch_bounds__(512, 1) gj_panel_kernel(Pool<T> M, const int* slots, Pool<T> GP, Pool<T> RP,
                                                           int* perm, int* rowsrc, int c0, unsigned* err) {
     constexpr int NT = 512;
     constexpr int VW = 16 / sizeof(T);                 // elements per 16-byte vector
+    constexpr int NV = NB / VW;                        // vectors per panel row
     typedef typename Vec16<T>::type VT;
     constexpr int NW = NT / 32;
+    constexpr int GS = 4;                              // column steps per rotation group
+    static_assert(NB % GS == 0 && NB % VW == 0, "panel width");
     // per step (double-buffered by step parity): each warp's candidate pivot row,
-    // its key and row index, and row r0 (the exchange partner)
+    // its key and logical row
     __shared__ __align__(16) T cand_r[2][NW][NB], cand_i[2][NW][NB];
-    __shared__ __align__(16) T xrr[2][NB], xri[2][NB];
     __shared__ unsigned cand_key[2][NW];
     __shared__ int cand_row[2][NW];
-    __shared__ int pivs[NB];
     __shared__ int rsm[NT * RPT];                      // composed row exchanges
+    __shared__ cplx<T> alpha_s[NT * RPT];              // deferred pivot-row scale factors
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    T* buf = reinterpret_cast<T*>(smem_raw);           // Rᵀ transpose tile
+    T* buf = reinterpret_cast<T*>(smem_raw);           // G staging / Rᵀ transpose tile
 
     const int b = M.rows;
     const int tid = threadIdx.x;
@@ -206,23 +221,33 @@ __global__ void __launch_bounds__(512, 1) gj_panel_kernel(Pool<T> M, const int* 
     const int ld = M.ld;
     const int w = min(NB, b - c0);
 
-    // Thread t owns rows t and t + 512.  Register position k holds panel column
-    // (jj + k) mod NB at step jj: the pivot column is always position 0.
+    // Thread t holds physical rows t and t + 512.  No data moves between threads:
+    // a row exchange only swaps the logical row numbers (lrow) of the two
+    // holders, and a pivot row is not scaled in place: its holder keeps the
+    // unscaled row with 1 in the pivot column and the factor 1/p in alpha_s (the
+    // later eliminations are linear in the row, so the true row is alpha times
+    // the stored one throughout).  Every thread then runs the same instruction
+    // stream in every step.  Steps run in groups of GS: within group g register
+    // position s holds panel column GS*g + s (static indices), and the row
+    // rotates left by GS positions between groups.
     T vr[RPT][NB], vi[RPT][NB];
+    int lrow[RPT];
 #pragma unroll
     for (int t = 0; t < RPT; ++t) {
         const int i = tid + t * NT;
+        lrow[t] = i < b ? i : INT_MAX;
+        alpha_s[i] = cmk((T)1, (T)0);
 #pragma unroll
-        for (int q = 0; q < NB / VW; ++q) {
+        for (int v = 0; v < NV; ++v) {
             VT a = {}, c = {};
             // c0 + NB <= ld (ld is a multiple of 32 and of NB): the vector stays in the row
-            if (i < b && q * VW < w) {
-                a = *reinterpret_cast<const VT*>(Mre + (size_t)i * ld + c0 + q * VW);
-                c = *reinterpret_cast<const VT*>(Mim + (size_t)i * ld + c0 + q * VW);
+            if (i < b && v * VW < w) {
+                a = *reinterpret_cast<const VT*>(Mre + (size_t)i * ld + c0 + v * VW);
+                c = *reinterpret_cast<const VT*>(Mim + (size_t)i * ld + c0 + v * VW);
             }
 #pragma unroll
             for (int e = 0; e < VW; ++e) {
-                const int k = q * VW + e;
+                const int k = v * VW + e;
                 const bool ok = i < b && k < w;
                 vr[t][k] = ok ? reinterpret_cast<const T*>(&a)[e] : (T)0;
                 vi[t][k] = ok ? reinterpret_cast<const T*>(&c)[e] : (T)0;
@@ -233,139 +258,166 @@ __global__ void __launch_bounds__(512, 1) gj_panel_kernel(Pool<T> M, const int* 
     // One barrier per column step.  Pivot key: the bit pattern of the FP32 value
     // |re|+|im| (non-negative floats order like their bit patterns; NaN sorts
     // above +inf, so a NaN column entry is picked and reported as singular).
-    // Ties go to the lowest row.
+    // Candidates are the logical rows >= r0; ties go to the lowest logical row.
+    int groups = 0;
 #pragma unroll 1
-    for (int jj = 0; jj < w; ++jj) {
-        const int r0 = c0 + jj;
-        const int q = jj & 1;
-        unsigned key = 0;
-        int row = INT_MAX, tsel = -1;
+    for (int j4 = 0; j4 < w; j4 += GS, ++groups) {
 #pragma unroll
-        for (int t = 0; t < RPT; ++t) {
-            const int i = tid + t * NT;
-            if (i >= r0 && i < b) {
-                const unsigned k = __float_as_uint((float)(fabs(vr[t][0]) + fabs(vi[t][0])));
-                if (tsel < 0 || k > key) { key = k; row = i; tsel = t; }
+        for (int s = 0; s < GS; ++s) {
+            const int jj = j4 + s;
+            if (jj >= w) break;   // uniform
+            const int r0 = c0 + jj;
+            const int q = jj & 1;
+            unsigned key = 0;
+            int row = INT_MAX, tsel = -1;
+#pragma unroll
+            for (int t = 0; t < RPT; ++t) {
+                if (lrow[t] >= r0 && lrow[t] < b) {
+                    const unsigned k = __float_as_uint((float)(fabs(vr[t][s]) + fabs(vi[t][s])));
+                    if (tsel < 0 || k > key || (k == key && lrow[t] < row)) { key = k; row = lrow[t]; tsel = t; }
+                }
+            }
+            const unsigned wkey = __reduce_max_sync(0xffffffffu, key);
+            const int wrow = __reduce_min_sync(0xffffffffu, key == wkey ? row : INT_MAX);
+            // the warp's winner publishes its row; lane 0 publishes key and logical row
+#pragma unroll
+            for (int t = 0; t < RPT; ++t) {
+                if (tsel == t && row == wrow) {
+#pragma unroll
+                    for (int v = 0; v < NV; ++v) {
+                        VT a, c;
+#pragma unroll
+                        for (int e = 0; e < VW; ++e) {
+                            reinterpret_cast<T*>(&a)[e] = vr[t][v * VW + e];
+                            reinterpret_cast<T*>(&c)[e] = vi[t][v * VW + e];
+                        }
+                        reinterpret_cast<VT*>(cand_r[q][warp])[v] = a;
+                        reinterpret_cast<VT*>(cand_i[q][warp])[v] = c;
+                    }
+                }
+            }
+            if (lane == 0) { cand_key[q][warp] = wkey; cand_row[q][warp] = wrow; }
+            __syncthreads();
+            // block winner (every warp computes it).  The holder of logical row r0
+            // is always a candidate, so the winner is a real row in [r0, b).
+            const unsigned ck = lane < NW ? cand_key[q][lane] : 0u;
+            const int cr = lane < NW ? cand_row[q][lane] : INT_MAX;
+            const unsigned gkey = __reduce_max_sync(0xffffffffu, ck);
+            const int gid = __reduce_min_sync(0xffffffffu,
+                                              (lane < NW && ck == gkey && cr < b) ? cr * 32 + lane : INT_MAX);
+            const int pl = gid >> 5;                   // logical row of the pivot
+            const VT* xpr = reinterpret_cast<const VT*>(cand_r[q][gid & 31]);
+            const VT* xpi = reinterpret_cast<const VT*>(cand_i[q][gid & 31]);
+            const cplx<T> p = cmk(reinterpret_cast<const T*>(xpr)[s], reinterpret_cast<const T*>(xpi)[s]);
+            const bool bad = !(fabs(p.re) + fabs(p.im) > (T)0) || !isfinite(p.re) || !isfinite(p.im);
+            if (bad && tid == 0) dev_error(err, FDFD_DEVERR_SINGULAR);
+            const cplx<T> inv = bad ? cmk((T)0, (T)0) : cinv(p);
+            // every row: v -= (v[s]/p)·(pivot row), pivot column <- -v[s]/p; the
+            // pivot row itself: f = 0 (unchanged), pivot column <- 1, alpha <- 1/p
+            cplx<T> f[RPT];
+            bool isp[RPT];
+#pragma unroll
+            for (int t = 0; t < RPT; ++t) {
+                isp[t] = (lrow[t] == pl);
+                const cplx<T> fi = cmul(cmk(vr[t][s], vi[t][s]), inv);
+                f[t] = isp[t] ? cmk((T)0, (T)0) : fi;
+            }
+#pragma unroll
+            for (int v = 0; v < NV; ++v) {
+                const VT a = xpr[v], c = xpi[v];
+#pragma unroll
+                for (int e = 0; e < VW; ++e) {
+                    const int k = v * VW + e;
+                    if (k == s) continue;
+                    const T pr = reinterpret_cast<const T*>(&a)[e], pi = reinterpret_cast<const T*>(&c)[e];
+#pragma unroll
+                    for (int t = 0; t < RPT; ++t) {
+                        vr[t][k] -= f[t].re * pr - f[t].im * pi;
+                        vi[t][k] -= f[t].re * pi + f[t].im * pr;
+                    }
+                }
+            }
+#pragma unroll
+            for (int t = 0; t < RPT; ++t) {
+                vr[t][s] = isp[t] ? (T)1 : -f[t].re;
+                vi[t][s] = isp[t] ? (T)0 : -f[t].im;
+                if (isp[t]) alpha_s[tid + t * NT] = inv;
+                // exchange of logical rows r0 and pl between their holders
+                lrow[t] = (lrow[t] == r0) ? pl : (isp[t] ? r0 : lrow[t]);
             }
         }
-        const unsigned wkey = __reduce_max_sync(0xffffffffu, key);
-        const int wrow = __reduce_min_sync(0xffffffffu, key == wkey ? row : INT_MAX);
-        // the warp's winner publishes its row; lane 0 publishes key and row index
 #pragma unroll
         for (int t = 0; t < RPT; ++t) {
-            if (tsel == t && row == wrow) {
-#pragma unroll
-                for (int v = 0; v < NB / VW; ++v) {
-                    VT a, c;
-#pragma unroll
-                    for (int e = 0; e < VW; ++e) {
-                        reinterpret_cast<T*>(&a)[e] = vr[t][v * VW + e];
-                        reinterpret_cast<T*>(&c)[e] = vi[t][v * VW + e];
-                    }
-                    reinterpret_cast<VT*>(cand_r[q][warp])[v] = a;
-                    reinterpret_cast<VT*>(cand_i[q][warp])[v] = c;
-                }
-            }
-            if (tid + t * NT == r0) {
-#pragma unroll
-                for (int v = 0; v < NB / VW; ++v) {
-                    VT a, c;
-#pragma unroll
-                    for (int e = 0; e < VW; ++e) {
-                        reinterpret_cast<T*>(&a)[e] = vr[t][v * VW + e];
-                        reinterpret_cast<T*>(&c)[e] = vi[t][v * VW + e];
-                    }
-                    reinterpret_cast<VT*>(xrr[q])[v] = a;
-                    reinterpret_cast<VT*>(xri[q])[v] = c;
-                }
-            }
-        }
-        if (lane == 0) { cand_key[q][warp] = wkey; cand_row[q][warp] = wrow; }
-        __syncthreads();
-        // block winner (every warp computes it); row r0 is always a candidate, so piv is in [r0, b)
-        const unsigned ck = lane < NW ? cand_key[q][lane] : 0u;
-        const int cr = lane < NW ? cand_row[q][lane] : INT_MAX;
-        const unsigned gkey = __reduce_max_sync(0xffffffffu, ck);
-        const int piv = __reduce_min_sync(0xffffffffu, (lane < NW && ck == gkey) ? cr : INT_MAX);
-        const T* xpr = cand_r[q][(piv & (NT - 1)) >> 5];
-        const T* xpi = cand_i[q][(piv & (NT - 1)) >> 5];
-        if (tid == 0) pivs[jj] = piv;
-        // scaled pivot row (formed by every thread from shared memory); the owner
-        // of r0 keeps it, the owner of piv takes the old row r0, every other row
-        // is eliminated
-        const cplx<T> p = cmk(xpr[0], xpi[0]);
-        const bool bad = !(fabs(p.re) + fabs(p.im) > (T)0) || !isfinite(p.re) || !isfinite(p.im);
-        if (bad && tid == 0) dev_error(err, FDFD_DEVERR_SINGULAR);
-        const cplx<T> inv = bad ? cmk((T)0, (T)0) : cinv(p);
-#pragma unroll
-        for (int t = 0; t < RPT; ++t) {
-            const int i = tid + t * NT;
-            if (i >= b) continue;
-            if (i == r0) {
-                vr[t][0] = inv.re;
-                vi[t][0] = inv.im;
-#pragma unroll
-                for (int k = 1; k < NB; ++k) {
-                    const cplx<T> v = cmul(cmk(xpr[k], xpi[k]), inv);
-                    vr[t][k] = v.re;
-                    vi[t][k] = v.im;
-                }
-            } else {
-                if (i == piv) {
-#pragma unroll
-                    for (int k = 0; k < NB; ++k) { vr[t][k] = xrr[q][k]; vi[t][k] = xri[q][k]; }
-                }
-                const cplx<T> fi = cmul(cmk(vr[t][0], vi[t][0]), inv);   // f / p
-                vr[t][0] = -fi.re;
-                vi[t][0] = -fi.im;
-#pragma unroll
-                for (int k = 1; k < NB; ++k) {
-                    const T pr = xpr[k], pi = xpi[k];
-                    vr[t][k] -= fi.re * pr - fi.im * pi;
-                    vi[t][k] -= fi.re * pi + fi.im * pr;
-                }
-            }
-            // rotate left by one: the next pivot column moves to position 0
-            const T r0v = vr[t][0], i0v = vi[t][0];
-#pragma unroll
-            for (int k = 0; k + 1 < NB; ++k) { vr[t][k] = vr[t][k + 1]; vi[t][k] = vi[t][k + 1]; }
-            vr[t][NB - 1] = r0v;
-            vi[t][NB - 1] = i0v;
+            rotate_left<T, NB, GS>(vr[t]);
+            rotate_left<T, NB, GS>(vi[t]);
         }
     }
-    // complete the rotation cycle of a short last panel (w < NB) so position k is column k
+    // complete the rotation cycle (GS * groups <= NB) so register position k is column k
 #pragma unroll 1
-    for (int extra = w; extra < NB; ++extra) {
+    for (int g = groups; g < NB / GS; ++g) {
 #pragma unroll
         for (int t = 0; t < RPT; ++t) {
-            const T r0v = vr[t][0], i0v = vi[t][0];
+            rotate_left<T, NB, GS>(vr[t]);
+            rotate_left<T, NB, GS>(vi[t]);
+        }
+    }
+    // apply the deferred pivot-row scale factors
 #pragma unroll
-            for (int k = 0; k + 1 < NB; ++k) { vr[t][k] = vr[t][k + 1]; vi[t][k] = vi[t][k + 1]; }
-            vr[t][NB - 1] = r0v;
-            vi[t][NB - 1] = i0v;
+    for (int t = 0; t < RPT; ++t) {
+        const cplx<T> al = alpha_s[tid + t * NT];
+#pragma unroll
+        for (int k = 0; k < NB; ++k) {
+            const cplx<T> x = cmul(al, cmk(vr[t][k], vi[t][k]));
+            vr[t][k] = x.re;
+            vi[t][k] = x.im;
         }
     }
 
-    // 1. G panel (b x GP.cols, zero padded), 16-byte stores of each thread's row
+    // 1. G panel (b x GP.cols, zero padded) with its TF32 residual planes.  Rows
+    //    are staged 128 at a time in shared memory (row stride NB+4 keeps the
+    //    16-byte staging stores conflict-free) and written as whole 16-byte
+    //    vectors of consecutive columns, so each warp store covers full rows.
     {
         T* g = GP.slot(job);
         const long long pe = GP.plane_elems();
+        constexpr int SR = NB + 4;
+        const int gv = GP.cols / VW;                   // vectors per G row (GP.cols % VW == 0)
+        for (int r0 = 0; r0 < b; r0 += 128) {
+            __syncthreads();
 #pragma unroll
-        for (int t = 0; t < RPT; ++t) {
-            const int i = tid + t * NT;
-            if (i >= b) continue;
+            for (int t = 0; t < RPT; ++t) {
+                const int L = lrow[t];                 // G row L is the row of logical row L
+                if (L >= r0 && L < r0 + 128 && L < b) {
+                    T* sr = buf + (size_t)(L - r0) * SR;
+                    T* si = buf + (size_t)128 * SR + (size_t)(L - r0) * SR;
 #pragma unroll
-            for (int q = 0; q < NB / VW; ++q) {
-                VT a, c, al, cl;
+                    for (int v = 0; v < NV; ++v) {
+                        VT a, c;
+#pragma unroll
+                        for (int e = 0; e < VW; ++e) {
+                            reinterpret_cast<T*>(&a)[e] = vr[t][v * VW + e];
+                            reinterpret_cast<T*>(&c)[e] = vi[t][v * VW + e];
+                        }
+                        reinterpret_cast<VT*>(sr)[v] = a;
+                        reinterpret_cast<VT*>(si)[v] = c;
+                    }
+                }
+            }
+            __syncthreads();
+            const int nr = min(128, b - r0);
+            for (int idx = tid; idx < nr * gv; idx += NT) {
+                const int rl = idx / gv, v = idx % gv;
+                VT a = {}, c = {}, al, cl;
+                if (v < NV) {
+                    a = reinterpret_cast<const VT*>(buf + (size_t)rl * SR)[v];
+                    c = reinterpret_cast<const VT*>(buf + (size_t)128 * SR + (size_t)rl * SR)[v];
+                }
 #pragma unroll
                 for (int e = 0; e < VW; ++e) {
-                    const T x = vr[t][q * VW + e], y = vi[t][q * VW + e];
-                    reinterpret_cast<T*>(&a)[e] = x;
-                    reinterpret_cast<T*>(&c)[e] = y;
-                    reinterpret_cast<T*>(&al)[e] = (T)tf32_lo((float)x);
-                    reinterpret_cast<T*>(&cl)[e] = (T)tf32_lo((float)y);
+                    reinterpret_cast<T*>(&al)[e] = (T)tf32_lo((float)reinterpret_cast<const T*>(&a)[e]);
+                    reinterpret_cast<T*>(&cl)[e] = (T)tf32_lo((float)reinterpret_cast<const T*>(&c)[e]);
                 }
-                const long long o = (long long)i * GP.ld + q * VW;
+                const long long o = (long long)(r0 + rl) * GP.ld + v * VW;
                 *reinterpret_cast<VT*>(g + o) = a;
                 *reinterpret_cast<VT*>(g + pe + o) = c;
                 if (GP.planes == 4) {
@@ -373,25 +425,14 @@ __global__ void __launch_bounds__(512, 1) gj_panel_kernel(Pool<T> M, const int* 
                     *reinterpret_cast<VT*>(g + 3 * pe + o) = cl;
                 }
             }
-            for (int k = NB; k < GP.cols; ++k) {
-                const long long o = (long long)i * GP.ld + k;
-                g[o] = 0;
-                g[pe + o] = 0;
-                if (GP.planes == 4) { g[2 * pe + o] = 0; g[3 * pe + o] = 0; }
-            }
         }
     }
-    __syncthreads();
     // 2. the panel's row exchanges, composed: row r of the exchanged matrix is
-    //    row rsm[r] of M (the GEMM reads through this map, no rows move here)
-    for (int i = tid; i < b; i += NT) rsm[i] = i;
-    __syncthreads();
-    if (tid == 0) {
-        for (int jj = 0; jj < w; ++jj) {
-            const int a = c0 + jj, c = pivs[jj];
-            const int t = rsm[a]; rsm[a] = rsm[c]; rsm[c] = t;
-        }
-    }
+    //    row rsm[r] of M, the physical row that holds logical row r (the GEMM
+    //    reads through this map, no rows move here)
+#pragma unroll
+    for (int t = 0; t < RPT; ++t)
+        if (lrow[t] < b) rsm[lrow[t]] = tid + t * NT;
     __syncthreads();
     {
         int* rs = rowsrc + (size_t)job * b;
@@ -409,29 +450,40 @@ __global__ void __launch_bounds__(512, 1) gj_panel_kernel(Pool<T> M, const int* 
             if (i < b) { pp[i] = pv[t]; rs[i] = rsm[i]; }
         }
     }
-    // 3. Rᵀ (b x RP.cols): RT[c][k] = (row c0+k after the interchanges)[c], identity on the
-    //    panel columns; staged through shared memory so reads and writes coalesce
+    // 3. Rᵀ (b x RP.cols): RT[c][k] = (row c0+k after the exchanges)[c], identity on the
+    //    panel columns; staged through shared memory so reads and writes coalesce.
+    //    Each thread issues all of its loads of a tile before its shared-memory stores.
     {
         T* rt = RP.slot(job);
         const int rc = RP.cols;
         const long long pe = RP.plane_elems();
-        constexpr int TW = 128;            // columns per staging tile
+        constexpr int TW = 128;                        // columns per staging tile
+        constexpr int IT = NB * TW / NT;               // loads per thread per tile
+        static_assert((NB * TW) % NT == 0, "tile split");
         for (int cb = 0; cb < b; cb += TW) {
             const int cw = min(TW, b - cb);
-            for (int idx = tid; idx < NB * TW; idx += NT) {
+            T la[IT], lb[IT];
+#pragma unroll
+            for (int u = 0; u < IT; ++u) {
+                const int idx = tid + u * NT;
                 const int k = idx / TW, c = idx % TW;
-                T a = 0, d = 0;
+                const int cc = cb + c;
+                la[u] = 0; lb[u] = 0;
                 if (k < w && c < cw) {
-                    const int cc = cb + c;
-                    if (cc >= c0 && cc < c0 + w) a = (T)((cc - c0) == k ? 1 : 0);
+                    if (cc >= c0 && cc < c0 + w) la[u] = (T)((cc - c0) == k ? 1 : 0);
                     else {
                         const int sr = rsm[c0 + k];
-                        a = Mre[(size_t)sr * ld + cc];
-                        d = Mim[(size_t)sr * ld + cc];
+                        la[u] = Mre[(size_t)sr * ld + cc];
+                        lb[u] = Mim[(size_t)sr * ld + cc];
                     }
                 }
-                buf[2 * (k * (TW + 1) + c)] = a;
-                buf[2 * (k * (TW + 1) + c) + 1] = d;
+            }
+#pragma unroll
+            for (int u = 0; u < IT; ++u) {
+                const int idx = tid + u * NT;
+                const int k = idx / TW, c = idx % TW;
+                buf[2 * (k * (TW + 1) + c)] = la[u];
+                buf[2 * (k * (TW + 1) + c) + 1] = lb[u];
             }
             __syncthreads();
             for (int idx = tid; idx < cw * rc; idx += NT) {
