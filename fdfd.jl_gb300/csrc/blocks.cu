@@ -148,16 +148,12 @@ __global__ void perm_init_kernel(int* perm, int b) {
 // Blocked Gauss-Jordan inversion with partial pivoting, panel step.
 //
 // For the panel of columns [c0, c0+w) of each matrix M (b x b) the kernel
-//  1. loads the panel M[:, c0:c0+w) into registers (thread t owns rows t and
-//     t + 512) and runs w column steps of in-place Gauss-Jordan on it: pivot
-//     = largest |re|+|im| among the rows not yet used as pivots (ties: lowest
-//     row), row exchange, pivot row scaled by 1/p with the pivot entry
-//     replaced by 1/p, every other row i updated by -M[i,j]·(scaled pivot row)
-//     with its pivot-column entry set to -M[i,j]/p.  The register row rotates
-//     by one position per step so that the pivot column always sits in
-//     register 0 (no indexed register access).  One step costs a block argmax
-//     and a broadcast of the pivot row and its exchange partner through shared
-//     memory.  The result G (b x w) holds the panel's block transformation;
+//  1. loads the panel M[:, c0:c0+w) into registers and runs w column steps of
+//     in-place Gauss-Jordan on it: pivot = largest |re|+|im| among the rows not
+//     yet used as pivots (ties: lowest row), row exchange, pivot row scaled by
+//     1/p with the pivot entry replaced by 1/p, every other row i updated by
+//     -M[i,j]·(scaled pivot row) with its pivot-column entry set to -M[i,j]/p.
+//     The result G (b x w) holds the panel's block transformation;
 //  2. composes the panel's row exchanges into rowsrc (row r of the exchanged
 //     matrix is row rowsrc[r] of M) and into perm; no row of M moves;
 //  3. writes Rᵀ: the exchanged panel rows M[rowsrc[c0:c0+w], :] transposed,
@@ -167,236 +163,272 @@ __global__ void perm_init_kernel(int* perm, int b) {
 // a second buffer).  After the last panel M holds (P M₀)⁻¹, and
 // gj_unpermute_kernel restores M₀⁻¹.  The Gauss-Jordan scheme is the textbook
 // one (e.g. G. W. Stewart, Matrix Algorithms I, §3.1).
-// grid: njobs, block 512; requires b <= 512*RPT.
+//
+// Register tiling: the b x NB panel is cut into NB/C column blocks of 128
+// threads each (4 warps, so a warp never straddles two blocks); thread rg of
+// column block cb holds rows rg*R .. rg*R+R-1, columns cb*C .. cb*C+C-1.  A
+// column step needs the pivot row only in the thread's C columns and the
+// pivot column only in its R rows, which keeps the shared-memory traffic per
+// step near b·(C+R) elements instead of b·NB.
+// grid: njobs, block 512; requires b <= 128*R.
 // ---------------------------------------------------------------------------
-// dynamic shared memory of gj_panel_kernel (elements of T): the larger of the
-// Rᵀ transpose tile (NB x 129, re and im) and the G staging tile (128 rows x NB+4)
-template <int NB>
+// Pivot search key of a candidate row: the FP32 bit pattern of |re|+|im| with
+// its low 11 bits replaced by 2047 - (physical row).  Non-negative floats
+// order like their bit patterns, so one unsigned max selects the largest
+// magnitude; magnitudes that agree to 2^-12 relative go to the lowest physical
+// row.  NaN sorts above +inf, so a NaN entry is picked and reported as
+// singular.  Every candidate key is >= 1024, above the 0 of a non-candidate.
+__device__ __forceinline__ unsigned pivot_key(float mag, int phys) {
+    return (__float_as_uint(mag) & 0xFFFFF800u) | (unsigned)(2047 - phys);
+}
+__device__ __forceinline__ int pivot_key_row(unsigned key) { return 2047 - (int)(key & 0x7FFu); }
+
+// 1/z = conj(z)/|z|² with z first scaled by a power of two (exact), so that
+// |z|² neither overflows nor underflows; one reciprocal instead of the three
+// divisions of Smith's algorithm.  z must be finite and non-zero.
+template <typename T> __device__ __forceinline__ cplx<T> cinv_pow2(cplx<T> z) {
+    int e;
+    frexp(fmax(fabs(z.re), fabs(z.im)), &e);
+    const T a = ldexp(z.re, -e), b = ldexp(z.im, -e);
+    const T r = (T)1 / (a * a + b * b);
+    return cmk(ldexp(a * r, -e), ldexp(-b * r, -e));
+}
+
+// dynamic shared memory of gj_panel_kernel (elements of T): the largest of the
+// G staging tile (128 rows x NB+4, re and im), the Rᵀ transpose tile (NB x 129,
+// re and im) and the double-buffered pivot column (2 x 2 planes x 128*R)
+template <int NB, int R>
 __host__ __device__ constexpr size_t gj_panel_smem_elems() {
-    return (size_t)2 * (NB * 129 > 128 * (NB + 4) ? NB * 129 : 128 * (NB + 4));
+    return (size_t)2 * (128 * (NB + 4) > NB * 129 ? (128 * (NB + 4) > 2 * 128 * R ? 128 * (NB + 4) : 2 * 128 * R)
+                                                  : (NB * 129 > 2 * 128 * R ? NB * 129 : 2 * 128 * R));
 }
 
 template <typename T> struct Vec16;
 template <> struct Vec16<float> { typedef float4 type; };
 template <> struct Vec16<double> { typedef double2 type; };
 
-// rotate a register row left by S positions (static indices only)
-template <typename T, int NB, int S>
-__device__ __forceinline__ void rotate_left(T (&v)[NB]) {
-    T tmp[S];
-#pragma unroll
-    for (int k = 0; k < S; ++k) tmp[k] = v[k];
-#pragma unroll
-    for (int k = 0; k + S < NB; ++k) v[k] = v[k + S];
-#pragma unroll
-    for (int k = 0; k < S; ++k) v[NB - S + k] = tmp[k];
-}
-
-template <typename T, int NB, int RPT>
+template <typename T, int NB, int R, int C>
 __global__ void __launch_bounds__(512, 1) gj_panel_kernel(Pool<T> M, const int* slots, Pool<T> GP, Pool<T> RP,
                                                           int* perm, int* rowsrc, int c0, unsigned* err) {
     constexpr int NT = 512;
+    constexpr int NCB = NB / C;                        // column blocks
+    constexpr int TPB = NT / NCB;                      // threads per column block
+    constexpr int WPB = TPB / 32;                      // warps per column block
+    constexpr int ROWS = TPB * R;                      // rows the block covers
     constexpr int VW = 16 / sizeof(T);                 // elements per 16-byte vector
-    constexpr int NV = NB / VW;                        // vectors per panel row
     typedef typename Vec16<T>::type VT;
-    constexpr int NW = NT / 32;
-    constexpr int GS = 4;                              // column steps per rotation group
-    static_assert(NB % GS == 0 && NB % VW == 0, "panel width");
-    // per step (double-buffered by step parity): each warp's candidate pivot row,
-    // its key and logical row
-    __shared__ __align__(16) T cand_r[2][NW][NB], cand_i[2][NW][NB];
-    __shared__ unsigned cand_key[2][NW];
-    __shared__ int cand_row[2][NW];
-    __shared__ int rsm[NT * RPT];                      // composed row exchanges
-    __shared__ cplx<T> alpha_s[NT * RPT];              // deferred pivot-row scale factors
+    static_assert(NCB * TPB == NT && TPB % 32 == 0 && C % VW == 0 && R % VW == 0, "panel tiling");
+    __shared__ __align__(16) T prow_r[R][NB], prow_i[R][NB];  // the pivot row's row group
+    __shared__ unsigned cand_key[WPB];
+    __shared__ cplx<T> cand_p[WPB], cand_inv[WPB];      // each warp's candidate pivot and its inverse
+    __shared__ int lrow_st[R];                         // logical rows of the pivot row's group
+    __shared__ int rsm[ROWS];                          // composed row exchanges
+    __shared__ cplx<T> alpha_s[ROWS];                  // deferred pivot-row scale factors
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    T* buf = reinterpret_cast<T*>(smem_raw);           // G staging / Rᵀ transpose tile
+    T* buf = reinterpret_cast<T*>(smem_raw);           // pivot column / G staging / Rᵀ transpose tile
 
     const int b = M.rows;
     const int tid = threadIdx.x;
-    const int warp = tid >> 5, lane = tid & 31;
+    const int cb = tid / TPB, rg = tid % TPB;          // column block (warp-uniform), row group
+    const int lane = tid & 31, wic = rg >> 5;          // warp index within the column block
     const int job = blockIdx.x;
     const T* Mre = M.slot(slots[job]);
     const T* Mim = Mre + M.plane_elems();
     const int ld = M.ld;
     const int w = min(NB, b - c0);
 
-    // Thread t holds physical rows t and t + 512.  No data moves between threads:
-    // a row exchange only swaps the logical row numbers (lrow) of the two
-    // holders, and a pivot row is not scaled in place: its holder keeps the
-    // unscaled row with 1 in the pivot column and the factor 1/p in alpha_s (the
-    // later eliminations are linear in the row, so the true row is alpha times
-    // the stored one throughout).  Every thread then runs the same instruction
-    // stream in every step.  Steps run in groups of GS: within group g register
-    // position s holds panel column GS*g + s (static indices), and the row
-    // rotates left by GS positions between groups.
-    T vr[RPT][NB], vi[RPT][NB];
-    int lrow[RPT];
+    // No data moves between threads: a row exchange only swaps the logical row
+    // numbers (lrow) of the two physical rows, and a pivot row is not scaled in
+    // place: its holders keep the unscaled row with 1 in the pivot column and
+    // the factor 1/p goes to alpha_s (the later eliminations are linear in the
+    // row, so the true row is alpha times the stored one throughout).
+    T vr[R][C], vi[R][C];
+    int lrow[R];
 #pragma unroll
-    for (int t = 0; t < RPT; ++t) {
-        const int i = tid + t * NT;
-        lrow[t] = i < b ? i : INT_MAX;
-        alpha_s[i] = cmk((T)1, (T)0);
+    for (int j = 0; j < R; ++j) {
+        const int i = rg * R + j;
+        lrow[j] = i < b ? i : INT_MAX;
+        if (cb == 0) alpha_s[i] = cmk((T)1, (T)0);
 #pragma unroll
-        for (int v = 0; v < NV; ++v) {
+        for (int v = 0; v < C / VW; ++v) {
+            const int col = cb * C + v * VW;
             VT a = {}, c = {};
             // c0 + NB <= ld (ld is a multiple of 32 and of NB): the vector stays in the row
-            if (i < b && v * VW < w) {
-                a = *reinterpret_cast<const VT*>(Mre + (size_t)i * ld + c0 + v * VW);
-                c = *reinterpret_cast<const VT*>(Mim + (size_t)i * ld + c0 + v * VW);
+            if (i < b && col < w) {
+                a = *reinterpret_cast<const VT*>(Mre + (size_t)i * ld + c0 + col);
+                c = *reinterpret_cast<const VT*>(Mim + (size_t)i * ld + c0 + col);
             }
 #pragma unroll
             for (int e = 0; e < VW; ++e) {
-                const int k = v * VW + e;
-                const bool ok = i < b && k < w;
-                vr[t][k] = ok ? reinterpret_cast<const T*>(&a)[e] : (T)0;
-                vi[t][k] = ok ? reinterpret_cast<const T*>(&c)[e] : (T)0;
+                const bool ok = i < b && col + e < w;
+                vr[j][v * VW + e] = ok ? reinterpret_cast<const T*>(&a)[e] : (T)0;
+                vi[j][v * VW + e] = ok ? reinterpret_cast<const T*>(&c)[e] : (T)0;
             }
         }
     }
 
-    // One barrier per column step.  Pivot key: the bit pattern of the FP32 value
-    // |re|+|im| (non-negative floats order like their bit patterns; NaN sorts
-    // above +inf, so a NaN column entry is picked and reported as singular).
-    // Candidates are the logical rows >= r0; ties go to the lowest logical row.
-    int groups = 0;
+    // Column step jj = g*C + sp (sp static): column block g holds the pivot
+    // column.  Candidates are the logical rows >= r0, compared by pivot_key:
+    // one 32-bit max-reduction per warp and one per block select the pivot.
 #pragma unroll 1
-    for (int j4 = 0; j4 < w; j4 += GS, ++groups) {
+    for (int g = 0; g * C < w; ++g) {
 #pragma unroll
-        for (int s = 0; s < GS; ++s) {
-            const int jj = j4 + s;
-            if (jj >= w) break;   // uniform
+        for (int sp = 0; sp < C; ++sp) {
+            const int jj = g * C + sp;
+            if (jj < w) {   // uniform
             const int r0 = c0 + jj;
-            const int q = jj & 1;
-            unsigned key = 0;
-            int row = INT_MAX, tsel = -1;
+            T* cs_r = buf + (size_t)((jj & 1) * 2) * ROWS;   // pivot column, double-buffered
+            T* cs_i = cs_r + ROWS;
+            // A: column block g publishes the pivot column and its warps' candidates
+            if (cb == g) {
+                // each thread also inverts its own best candidate, so the winner's
+                // 1/p is ready when the block has chosen (off the step's critical path)
+                unsigned key = 0;
+                T cvr = (T)1, cvi = (T)0;
 #pragma unroll
-            for (int t = 0; t < RPT; ++t) {
-                if (lrow[t] >= r0 && lrow[t] < b) {
-                    const unsigned k = __float_as_uint((float)(fabs(vr[t][s]) + fabs(vi[t][s])));
-                    if (tsel < 0 || k > key || (k == key && lrow[t] < row)) { key = k; row = lrow[t]; tsel = t; }
+                for (int j = 0; j < R; ++j)
+                    if (lrow[j] >= r0 && lrow[j] < b) {
+                        const unsigned k = pivot_key((float)(fabs(vr[j][sp]) + fabs(vi[j][sp])), rg * R + j);
+                        if (k > key) { key = k; cvr = vr[j][sp]; cvi = vi[j][sp]; }
+                    }
+                const cplx<T> cinv_c = cinv_pow2(cmk(cvr, cvi));
+#pragma unroll
+                for (int v = 0; v < R / VW; ++v) {
+                    VT a, c;
+#pragma unroll
+                    for (int e = 0; e < VW; ++e) {
+                        reinterpret_cast<T*>(&a)[e] = vr[v * VW + e][sp];
+                        reinterpret_cast<T*>(&c)[e] = vi[v * VW + e][sp];
+                    }
+                    reinterpret_cast<VT*>(cs_r + rg * R)[v] = a;
+                    reinterpret_cast<VT*>(cs_i + rg * R)[v] = c;
+                }
+                const unsigned wkey = __reduce_max_sync(0xffffffffu, key);
+                if (lane == 0) cand_key[wic] = wkey;
+                if (key != 0u && key == wkey) {        // keys are unique: one lane per warp
+                    cand_p[wic] = cmk(cvr, cvi);
+                    cand_inv[wic] = cinv_c;
                 }
             }
-            const unsigned wkey = __reduce_max_sync(0xffffffffu, key);
-            const int wrow = __reduce_min_sync(0xffffffffu, key == wkey ? row : INT_MAX);
-            // the warp's winner publishes its row; lane 0 publishes key and logical row
+            __syncthreads();
+            // B: block winner (every warp computes it; the holder of logical row r0
+            // is always a candidate, so the winner is a real row); the threads of
+            // the pivot row's group publish its rows and their logical numbers
+            // (all R rows are staged: selecting one in registers would index the
+            // register array at run time)
+            const unsigned gkey = __reduce_max_sync(0xffffffffu, lane < WPB ? cand_key[lane] : 0u);
+            const int pphys = pivot_key_row(gkey);     // physical row of the pivot
+            const cplx<T> p = cand_p[(pphys / R) >> 5];
+            const cplx<T> pinv = cand_inv[(pphys / R) >> 5];
+            if (pphys / R == rg) {
 #pragma unroll
-            for (int t = 0; t < RPT; ++t) {
-                if (tsel == t && row == wrow) {
+                for (int j = 0; j < R; ++j) {
 #pragma unroll
-                    for (int v = 0; v < NV; ++v) {
+                    for (int v = 0; v < C / VW; ++v) {
                         VT a, c;
 #pragma unroll
                         for (int e = 0; e < VW; ++e) {
-                            reinterpret_cast<T*>(&a)[e] = vr[t][v * VW + e];
-                            reinterpret_cast<T*>(&c)[e] = vi[t][v * VW + e];
+                            reinterpret_cast<T*>(&a)[e] = vr[j][v * VW + e];
+                            reinterpret_cast<T*>(&c)[e] = vi[j][v * VW + e];
                         }
-                        reinterpret_cast<VT*>(cand_r[q][warp])[v] = a;
-                        reinterpret_cast<VT*>(cand_i[q][warp])[v] = c;
+                        reinterpret_cast<VT*>(&prow_r[j][cb * C])[v] = a;
+                        reinterpret_cast<VT*>(&prow_i[j][cb * C])[v] = c;
                     }
+                    if (cb == 0) lrow_st[j] = lrow[j];
                 }
             }
-            if (lane == 0) { cand_key[q][warp] = wkey; cand_row[q][warp] = wrow; }
             __syncthreads();
-            // block winner (every warp computes it).  The holder of logical row r0
-            // is always a candidate, so the winner is a real row in [r0, b).
-            const unsigned ck = lane < NW ? cand_key[q][lane] : 0u;
-            const int cr = lane < NW ? cand_row[q][lane] : INT_MAX;
-            const unsigned gkey = __reduce_max_sync(0xffffffffu, ck);
-            const int gid = __reduce_min_sync(0xffffffffu,
-                                              (lane < NW && ck == gkey && cr < b) ? cr * 32 + lane : INT_MAX);
-            const int pl = gid >> 5;                   // logical row of the pivot
-            const VT* xpr = reinterpret_cast<const VT*>(cand_r[q][gid & 31]);
-            const VT* xpi = reinterpret_cast<const VT*>(cand_i[q][gid & 31]);
-            const cplx<T> p = cmk(reinterpret_cast<const T*>(xpr)[s], reinterpret_cast<const T*>(xpi)[s]);
+            const T* pr_r = prow_r[pphys % R];
+            const T* pr_i = prow_i[pphys % R];
+            const int pl = lrow_st[pphys % R];         // logical row of the pivot
+            // C: every element: v -= (v[jj]/p)·(pivot row), pivot column <- -v[jj]/p;
+            // the pivot row itself: f = 0 (unchanged), pivot column <- 1, alpha <- 1/p
             const bool bad = !(fabs(p.re) + fabs(p.im) > (T)0) || !isfinite(p.re) || !isfinite(p.im);
             if (bad && tid == 0) dev_error(err, FDFD_DEVERR_SINGULAR);
-            const cplx<T> inv = bad ? cmk((T)0, (T)0) : cinv(p);
-            // every row: v -= (v[s]/p)·(pivot row), pivot column <- -v[s]/p; the
-            // pivot row itself: f = 0 (unchanged), pivot column <- 1, alpha <- 1/p
-            cplx<T> f[RPT];
-            bool isp[RPT];
+            const cplx<T> inv = bad ? cmk((T)0, (T)0) : pinv;
+            T xr[C], xi[C];
 #pragma unroll
-            for (int t = 0; t < RPT; ++t) {
-                isp[t] = (lrow[t] == pl);
-                const cplx<T> fi = cmul(cmk(vr[t][s], vi[t][s]), inv);
-                f[t] = isp[t] ? cmk((T)0, (T)0) : fi;
-            }
-#pragma unroll
-            for (int v = 0; v < NV; ++v) {
-                const VT a = xpr[v], c = xpi[v];
+            for (int v = 0; v < C / VW; ++v) {
+                const VT a = reinterpret_cast<const VT*>(pr_r + cb * C)[v];
+                const VT c = reinterpret_cast<const VT*>(pr_i + cb * C)[v];
 #pragma unroll
                 for (int e = 0; e < VW; ++e) {
-                    const int k = v * VW + e;
-                    if (k == s) continue;
-                    const T pr = reinterpret_cast<const T*>(&a)[e], pi = reinterpret_cast<const T*>(&c)[e];
+                    xr[v * VW + e] = reinterpret_cast<const T*>(&a)[e];
+                    xi[v * VW + e] = reinterpret_cast<const T*>(&c)[e];
+                }
+            }
+            cplx<T> f[R];
+            bool isp[R];
 #pragma unroll
-                    for (int t = 0; t < RPT; ++t) {
-                        vr[t][k] -= f[t].re * pr - f[t].im * pi;
-                        vi[t][k] -= f[t].re * pi + f[t].im * pr;
-                    }
+            for (int v = 0; v < R / VW; ++v) {
+                const VT a = reinterpret_cast<const VT*>(cs_r + rg * R)[v];
+                const VT c = reinterpret_cast<const VT*>(cs_i + rg * R)[v];
+#pragma unroll
+                for (int e = 0; e < VW; ++e) {
+                    const int j = v * VW + e;
+                    isp[j] = (lrow[j] == pl);
+                    const cplx<T> fi = cmul(cmk(reinterpret_cast<const T*>(&a)[e], reinterpret_cast<const T*>(&c)[e]),
+                                            inv);
+                    f[j] = isp[j] ? cmk((T)0, (T)0) : fi;
                 }
             }
 #pragma unroll
-            for (int t = 0; t < RPT; ++t) {
-                vr[t][s] = isp[t] ? (T)1 : -f[t].re;
-                vi[t][s] = isp[t] ? (T)0 : -f[t].im;
-                if (isp[t]) alpha_s[tid + t * NT] = inv;
+            for (int j = 0; j < R; ++j)
+#pragma unroll
+                for (int k = 0; k < C; ++k) {
+                    vr[j][k] = fma(-f[j].re, xr[k], fma(f[j].im, xi[k], vr[j][k]));
+                    vi[j][k] = fma(-f[j].re, xi[k], fma(-f[j].im, xr[k], vi[j][k]));
+                }
+#pragma unroll
+            for (int j = 0; j < R; ++j) {
+                if (cb == g) {
+                    vr[j][sp] = isp[j] ? (T)1 : -f[j].re;
+                    vi[j][sp] = isp[j] ? (T)0 : -f[j].im;
+                }
+                if (cb == 0 && isp[j]) alpha_s[rg * R + j] = inv;
                 // exchange of logical rows r0 and pl between their holders
-                lrow[t] = (lrow[t] == r0) ? pl : (isp[t] ? r0 : lrow[t]);
+                lrow[j] = (lrow[j] == r0) ? pl : (isp[j] ? r0 : lrow[j]);
+            }
             }
         }
-#pragma unroll
-        for (int t = 0; t < RPT; ++t) {
-            rotate_left<T, NB, GS>(vr[t]);
-            rotate_left<T, NB, GS>(vi[t]);
-        }
     }
-    // complete the rotation cycle (GS * groups <= NB) so register position k is column k
-#pragma unroll 1
-    for (int g = groups; g < NB / GS; ++g) {
-#pragma unroll
-        for (int t = 0; t < RPT; ++t) {
-            rotate_left<T, NB, GS>(vr[t]);
-            rotate_left<T, NB, GS>(vi[t]);
-        }
-    }
+    __syncthreads();
     // apply the deferred pivot-row scale factors
 #pragma unroll
-    for (int t = 0; t < RPT; ++t) {
-        const cplx<T> al = alpha_s[tid + t * NT];
+    for (int j = 0; j < R; ++j) {
+        const cplx<T> al = alpha_s[rg * R + j];
 #pragma unroll
-        for (int k = 0; k < NB; ++k) {
-            const cplx<T> x = cmul(al, cmk(vr[t][k], vi[t][k]));
-            vr[t][k] = x.re;
-            vi[t][k] = x.im;
+        for (int k = 0; k < C; ++k) {
+            const cplx<T> x = cmul(al, cmk(vr[j][k], vi[j][k]));
+            vr[j][k] = x.re;
+            vi[j][k] = x.im;
         }
     }
 
     // 1. G panel (b x GP.cols, zero padded) with its TF32 residual planes.  Rows
-    //    are staged 128 at a time in shared memory (row stride NB+4 keeps the
-    //    16-byte staging stores conflict-free) and written as whole 16-byte
+    //    are staged by logical row, 128 at a time, in shared memory (row stride
+    //    NB+4 keeps 16-byte accesses conflict-free) and written as whole 16-byte
     //    vectors of consecutive columns, so each warp store covers full rows.
     {
-        T* g = GP.slot(job);
+        T* gp = GP.slot(job);
         const long long pe = GP.plane_elems();
         constexpr int SR = NB + 4;
         const int gv = GP.cols / VW;                   // vectors per G row (GP.cols % VW == 0)
-        for (int r0 = 0; r0 < b; r0 += 128) {
+        for (int ch = 0; ch < b; ch += 128) {
             __syncthreads();
 #pragma unroll
-            for (int t = 0; t < RPT; ++t) {
-                const int L = lrow[t];                 // G row L is the row of logical row L
-                if (L >= r0 && L < r0 + 128 && L < b) {
-                    T* sr = buf + (size_t)(L - r0) * SR;
-                    T* si = buf + (size_t)128 * SR + (size_t)(L - r0) * SR;
+            for (int j = 0; j < R; ++j) {
+                const int L = lrow[j];                 // G row L is the row of logical row L
+                if (L >= ch && L < ch + 128 && L < b) {
+                    T* sr = buf + (size_t)(L - ch) * SR + cb * C;
+                    T* si = buf + (size_t)128 * SR + (size_t)(L - ch) * SR + cb * C;
 #pragma unroll
-                    for (int v = 0; v < NV; ++v) {
+                    for (int v = 0; v < C / VW; ++v) {
                         VT a, c;
 #pragma unroll
                         for (int e = 0; e < VW; ++e) {
-                            reinterpret_cast<T*>(&a)[e] = vr[t][v * VW + e];
-                            reinterpret_cast<T*>(&c)[e] = vi[t][v * VW + e];
+                            reinterpret_cast<T*>(&a)[e] = vr[j][v * VW + e];
+                            reinterpret_cast<T*>(&c)[e] = vi[j][v * VW + e];
                         }
                         reinterpret_cast<VT*>(sr)[v] = a;
                         reinterpret_cast<VT*>(si)[v] = c;
@@ -404,11 +436,11 @@ __global__ void __launch_bounds__(512, 1) gj_panel_kernel(Pool<T> M, const int* 
                 }
             }
             __syncthreads();
-            const int nr = min(128, b - r0);
+            const int nr = min(128, b - ch);
             for (int idx = tid; idx < nr * gv; idx += NT) {
                 const int rl = idx / gv, v = idx % gv;
                 VT a = {}, c = {}, al, cl;
-                if (v < NV) {
+                if (v < NB / VW) {
                     a = reinterpret_cast<const VT*>(buf + (size_t)rl * SR)[v];
                     c = reinterpret_cast<const VT*>(buf + (size_t)128 * SR + (size_t)rl * SR)[v];
                 }
@@ -417,12 +449,12 @@ __global__ void __launch_bounds__(512, 1) gj_panel_kernel(Pool<T> M, const int* 
                     reinterpret_cast<T*>(&al)[e] = (T)tf32_lo((float)reinterpret_cast<const T*>(&a)[e]);
                     reinterpret_cast<T*>(&cl)[e] = (T)tf32_lo((float)reinterpret_cast<const T*>(&c)[e]);
                 }
-                const long long o = (long long)(r0 + rl) * GP.ld + v * VW;
-                *reinterpret_cast<VT*>(g + o) = a;
-                *reinterpret_cast<VT*>(g + pe + o) = c;
+                const long long o = (long long)(ch + rl) * GP.ld + v * VW;
+                *reinterpret_cast<VT*>(gp + o) = a;
+                *reinterpret_cast<VT*>(gp + pe + o) = c;
                 if (GP.planes == 4) {
-                    *reinterpret_cast<VT*>(g + 2 * pe + o) = al;
-                    *reinterpret_cast<VT*>(g + 3 * pe + o) = cl;
+                    *reinterpret_cast<VT*>(gp + 2 * pe + o) = al;
+                    *reinterpret_cast<VT*>(gp + 3 * pe + o) = cl;
                 }
             }
         }
@@ -430,22 +462,25 @@ __global__ void __launch_bounds__(512, 1) gj_panel_kernel(Pool<T> M, const int* 
     // 2. the panel's row exchanges, composed: row r of the exchanged matrix is
     //    row rsm[r] of M, the physical row that holds logical row r (the GEMM
     //    reads through this map, no rows move here)
+    if (cb == 0) {
 #pragma unroll
-    for (int t = 0; t < RPT; ++t)
-        if (lrow[t] < b) rsm[lrow[t]] = tid + t * NT;
+        for (int j = 0; j < R; ++j)
+            if (lrow[j] < b) rsm[lrow[j]] = rg * R + j;
+    }
     __syncthreads();
     {
         int* rs = rowsrc + (size_t)job * b;
         int* pp = perm + (size_t)job * b;
-        int pv[RPT];
+        constexpr int PPT = ROWS / NT;                 // rows per thread here (ROWS is a multiple of NT)
+        int pv[PPT];
 #pragma unroll
-        for (int t = 0; t < RPT; ++t) {
+        for (int t = 0; t < PPT; ++t) {
             const int i = tid + t * NT;
             if (i < b) pv[t] = pp[rsm[i]];
         }
         __syncthreads();   // every old perm entry is read before any is overwritten
 #pragma unroll
-        for (int t = 0; t < RPT; ++t) {
+        for (int t = 0; t < PPT; ++t) {
             const int i = tid + t * NT;
             if (i < b) { pp[i] = pv[t]; rs[i] = rsm[i]; }
         }
@@ -773,18 +808,18 @@ void launch_level1_combine(cudaStream_t s, int njobs, NodeMap m, const cplx<doub
 void launch_perm_init(cudaStream_t s, int njobs, int* perm, int b) {
     perm_init_kernel<int><<<dim3(ceil_div(b, 256), njobs), 256, 0, s>>>(perm, b);
 }
-template <typename T, int NB, int RPT>
+template <typename T, int NB, int R, int C>
 static int gj_panel_launch(cudaStream_t s, int njobs, Pool<T> M, const int* slots, Pool<T> GP, Pool<T> RP,
                            int* perm, int* rowsrc, int c0, unsigned* err) {
-    const size_t smem = gj_panel_smem_elems<NB>() * sizeof(T);
+    const size_t smem = gj_panel_smem_elems<NB, R>() * sizeof(T);
     static bool attr = false;
     if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(gj_panel_kernel<T, NB, RPT>,
+        cudaError_t e = cudaFuncSetAttribute(gj_panel_kernel<T, NB, R, C>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return (int)e;
         attr = true;
     }
-    gj_panel_kernel<T, NB, RPT><<<njobs, 512, smem, s>>>(M, slots, GP, RP, perm, rowsrc, c0, err);
+    gj_panel_kernel<T, NB, R, C><<<njobs, 512, smem, s>>>(M, slots, GP, RP, perm, rowsrc, c0, err);
     return (int)cudaGetLastError();
 }
 
@@ -794,11 +829,11 @@ int launch_gj_panel(cudaStream_t s, int nb, int njobs, Pool<T> M, const int* slo
     const bool two = M.rows > 512;
     if (M.rows > 1024) return (int)cudaErrorInvalidValue;
     if constexpr (sizeof(T) == 4) {
-        if (nb == 32 && !two) return gj_panel_launch<T, 32, 1>(s, njobs, M, slots, GP, RP, perm, rowsrc, c0, err);
-        if (nb == 16 && two) return gj_panel_launch<T, 16, 2>(s, njobs, M, slots, GP, RP, perm, rowsrc, c0, err);
+        if (nb == 32 && !two) return gj_panel_launch<T, 32, 4, 8>(s, njobs, M, slots, GP, RP, perm, rowsrc, c0, err);
+        if (nb == 16 && two) return gj_panel_launch<T, 16, 8, 4>(s, njobs, M, slots, GP, RP, perm, rowsrc, c0, err);
     } else {
-        if (nb == 16 && !two) return gj_panel_launch<T, 16, 1>(s, njobs, M, slots, GP, RP, perm, rowsrc, c0, err);
-        if (nb == 8 && two) return gj_panel_launch<T, 8, 2>(s, njobs, M, slots, GP, RP, perm, rowsrc, c0, err);
+        if (nb == 16 && !two) return gj_panel_launch<T, 16, 4, 4>(s, njobs, M, slots, GP, RP, perm, rowsrc, c0, err);
+        if (nb == 8 && two) return gj_panel_launch<T, 8, 8, 2>(s, njobs, M, slots, GP, RP, perm, rowsrc, c0, err);
     }
     return (int)cudaErrorInvalidValue;
 }

@@ -92,6 +92,7 @@ template <typename T> struct FactorStore {
 struct fdfd_handle {
     // problem
     int Nx, Ny, Npx, Npy, pol, precision;
+    int num_sms = 1;             // streaming multiprocessors of the device (launch shapes)
     double dx, dy, L0, pml_m, pml_lnR;
     double tol = 1e-10;
     int max_iter = 40;
@@ -562,7 +563,7 @@ int gemm(fdfd_handle* h, int pa, int pb, int pc, const int* a_slot, const int* b
     int ev = prof_begin(h);
     if (sizeof(T) == 4 && F.tc_ok) {
         int rc = tc_gemm_launch(reinterpret_cast<GemmArgs<float>*>(&g), c_trans_arr, pa, pb, njobs, &F.tc,
-                                h->stream);
+                                h->num_sms, h->stream);
         if (rc != 0) return set_err(h, FDFD_ECUDA, "tcgen05 GEMM launch failed (%d)", rc);
         prof_end(h, ev, prof_cls >= 0 ? prof_cls : FDFD_PROF_GEMM_TC, prof_cls >= 0 ? prof_work : flops);
         h->launches++;
@@ -1068,6 +1069,12 @@ int fdfd_create(fdfd_handle** out, int Nx, int Ny, int Npx, int Npy, double dx, 
         return FDFD_ECUDA;
     }
     for (auto& e : h->ev) cudaEventCreate(&e);
+    {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || h->num_sms < 1)
+            h->num_sms = 1;
+    }
     long long N = (long long)Nx * Ny;
     int rc;
     if ((rc = dev_alloc(h, (void**)&h->eps, N * sizeof(cplx<double>)))) return fail(rc);
@@ -1648,13 +1655,20 @@ int debug_gemm_impl(int M, int N, int K, const double* A, const double* B, doubl
         cudaEvent_t e0, e1;
         cudaEventCreate(&e0); cudaEventCreate(&e1);
         if (sizeof(T) == 4 && use_tc) {
-            CUtensorMap ma[2], mb[2];
+            CUtensorMap ma[3], mb[3];
             const Pool<float>* fa = reinterpret_cast<const Pool<float>*>(&PA);
             const Pool<float>* fb = reinterpret_cast<const Pool<float>*>(&PB);
-            if (!tc_make_map(*fa, &ma[0], &ma[1]) || !tc_make_map(*fb, &mb[0], &mb[1])) rc = FDFD_ECUDA;
+            if (!tc_make_map(*fa, &ma[0], &ma[1], &ma[2]) || !tc_make_map(*fb, &mb[0], &mb[1], &mb[2]))
+                rc = FDFD_ECUDA;
+            int dev = 0, sms = 0;
+            cudaGetDevice(&dev);
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+            const int bn = (use_tc == 64 || use_tc == 128 || use_tc == 256) ? use_tc : tc_pick_bn(M, N, 1, sms);
+            const int bi = bn == 256 ? 1 : (bn == 128 ? 0 : 2);
             if (rc == FDFD_OK) {
                 cudaEventRecord(e0);
-                if (tc_gemm_launch_maps(reinterpret_cast<GemmArgs<float>*>(&g), nullptr, &ma[0], &mb[1], 1, 0) != 0)
+                if (tc_gemm_launch_maps(reinterpret_cast<GemmArgs<float>*>(&g), nullptr, &ma[0], &mb[bi], bn, 1, 0) !=
+                    0)
                     rc = FDFD_ECUDA;
                 cudaEventRecord(e1);
             }

@@ -11,10 +11,12 @@
 // recovers close to FP32 accuracy (the split of Markidis et al., 2018, as used
 // for 3xTF32 GEMMs).  Each complex product is four real products (the im·im
 // term through the instruction's negate-A bit), so one K-step issues 12 MMAs
-// into two TMEM accumulators (real and imaginary, 256 columns each).
+// into two TMEM accumulators (real and imaginary, BN columns each).
 //
-// CTA tile 128 x 256 (complex outputs), K-step 8 (one 32-byte swizzle row per
-// operand row), 4-stage TMA pipeline, 192 threads:
+// CTA tile 128 x BN (complex outputs, BN = 256, 128 or 64: the launcher takes
+// the widest tile that still fills the GPU, so small batches get more CTAs),
+// K-step 8 (one 32-byte swizzle row per operand row), 4-stage TMA pipeline,
+// 192 threads:
 //   warp 0      TMA producer (one elected lane)
 //   warp 1      TMEM allocator and MMA issuer (one elected lane)
 //   warps 2..5  epilogue: tcgen05.ld -> registers -> global (N- or T-form)
@@ -24,12 +26,16 @@
 
 namespace {
 
-constexpr int BM = 128, BN = 256, BK = 8, STAGES = 4;
+constexpr int BM = 128, BK = 8, STAGES = 4;
 constexpr int A_PLANE_BYTES = BM * BK * 4;                  // 4 KB
-constexpr int B_PLANE_BYTES = BN * BK * 4;                  // 8 KB
-constexpr int STAGE_BYTES = 4 * A_PLANE_BYTES + 4 * B_PLANE_BYTES;   // 48 KB
-constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024;     // + alignment slack
-constexpr uint32_t TMEM_COLS = 512;
+template <int BN> struct TcTile {
+    static constexpr int B_PLANE_BYTES = BN * BK * 4;
+    static constexpr int STAGE_BYTES = 4 * A_PLANE_BYTES + 4 * B_PLANE_BYTES;
+    static constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024;   // + alignment slack
+    static constexpr uint32_t TMEM_COLS = 2 * BN;                     // re and im accumulators
+    // the epilogue stages 4 warps x 2 x 32 x 36 floats in the idle pipeline buffers
+    static_assert(STAGES * STAGE_BYTES >= 4 * 2 * 32 * 36 * 4, "epilogue staging");
+};
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
     return (uint32_t)__cvta_generic_to_shared(p);
@@ -128,9 +134,13 @@ struct TcParams {
     GemmArgs<float> g;
 };
 
-__global__ void __launch_bounds__(192, 1)
+template <int BN>
+__global__ void __launch_bounds__(192, BN <= 64 ? 2 : 1)
     gemm_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
                    const TcParams P) {
+    constexpr int B_PLANE_BYTES = TcTile<BN>::B_PLANE_BYTES;
+    constexpr int STAGE_BYTES = TcTile<BN>::STAGE_BYTES;
+    constexpr uint32_t TMEM_COLS = TcTile<BN>::TMEM_COLS;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     __shared__ __align__(8) uint64_t bar_full[STAGES], bar_empty[STAGES], bar_acc;
     __shared__ uint32_t tmem_base_slot;
@@ -200,7 +210,7 @@ __global__ void __launch_bounds__(192, 1)
     } else if (warp == 1) {
         if (lane == 0) {
             bool ok = true;
-            const uint32_t acc_re = tmem, acc_im = tmem + 256;
+            const uint32_t acc_re = tmem, acc_im = tmem + BN;
             const uint32_t id_pos = idesc_tf32(BM, BN, 0), id_neg = idesc_tf32(BM, BN, 1);
             for (int kt = 0; kt < nk; ++kt) {
                 const int s = kt % STAGES;
@@ -289,7 +299,7 @@ __global__ void __launch_bounds__(192, 1)
                 if (nb >= g.N) break;
                 uint32_t vr[32], vi[32];
                 tmem_ld32(tmem + lane_off + ch * 32, vr);
-                tmem_ld32(tmem + lane_off + 256 + ch * 32, vi);
+                tmem_ld32(tmem + lane_off + BN + ch * 32, vi);
                 asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
                 if (ctr) {
                     // transposed store: lanes (rows) are contiguous in Cᵀ -> coalesced per column
@@ -440,24 +450,27 @@ bool encode_pool(const Pool<float>& P, int box_rows, CUtensorMap* out) {
 
 }  // namespace
 
-bool tc_make_map(const Pool<float>& P, CUtensorMap* box128, CUtensorMap* box256) {
+bool tc_make_map(const Pool<float>& P, CUtensorMap* box128, CUtensorMap* box256, CUtensorMap* box64) {
     if (P.planes != 4 || (P.ld % 4) != 0) return false;
-    return encode_pool(P, BM, box128) && encode_pool(P, BN, box256);
+    return encode_pool(P, 128, box128) && encode_pool(P, 256, box256) && encode_pool(P, 64, box64);
 }
 
 bool tc_make_maps(const Pool<float>* D, const Pool<float>* C, const Pool<float>* X, const Pool<float>* GP,
                   const Pool<float>* RP, TcMaps* out) {
     const Pool<float>* pools[5] = {D, C, X, GP, RP};
     for (int i = 0; i < 5; ++i)
-        if (!tc_make_map(*pools[i], &out->map[i][0], &out->map[i][1])) return false;
+        if (!tc_make_map(*pools[i], &out->map[i][0], &out->map[i][1], &out->map[i][2])) return false;
     return true;
 }
 
-int tc_gemm_launch_maps(const GemmArgs<float>* g, const int* c_trans_arr, const CUtensorMap* mapA,
-                        const CUtensorMap* mapB, int njobs, cudaStream_t stream) {
+namespace {
+template <int BN>
+int tc_launch_bn(const GemmArgs<float>* g, const int* c_trans_arr, const CUtensorMap* mapA, const CUtensorMap* mapB,
+                 int njobs, cudaStream_t stream) {
     static bool attr = false;
     if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(gemm_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+        cudaError_t e = cudaFuncSetAttribute(gemm_tc_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             TcTile<BN>::SMEM_BYTES);
         if (e != cudaSuccess) return (int)e;
         attr = true;
     }
@@ -465,6 +478,25 @@ int tc_gemm_launch_maps(const GemmArgs<float>* g, const int* c_trans_arr, const 
     P.g = *g;
     if (c_trans_arr) P.g.c_trans_arr = c_trans_arr;
     dim3 grid((g->N + BN - 1) / BN, (g->M + BM - 1) / BM, njobs);
-    gemm_tc_kernel<<<grid, 192, SMEM_BYTES, stream>>>(*mapA, *mapB, P);
+    gemm_tc_kernel<BN><<<grid, 192, TcTile<BN>::SMEM_BYTES, stream>>>(*mapA, *mapB, P);
     return (int)cudaGetLastError();
+}
+}  // namespace
+
+int tc_gemm_launch_maps(const GemmArgs<float>* g, const int* c_trans_arr, const CUtensorMap* mapA,
+                        const CUtensorMap* mapB, int bn, int njobs, cudaStream_t stream) {
+    switch (bn) {
+        case 256: return tc_launch_bn<256>(g, c_trans_arr, mapA, mapB, njobs, stream);
+        case 128: return tc_launch_bn<128>(g, c_trans_arr, mapA, mapB, njobs, stream);
+        case 64: return tc_launch_bn<64>(g, c_trans_arr, mapA, mapB, njobs, stream);
+        default: return (int)cudaErrorInvalidValue;
+    }
+}
+
+int tc_pick_bn(int M, int N, int njobs, int num_sms) {
+    const long long mt = (M + BM - 1) / BM;
+    auto tiles = [&](int bn) { return mt * ((N + bn - 1) / bn) * njobs; };
+    if (tiles(256) >= num_sms) return 256;
+    if (tiles(128) >= num_sms) return 128;
+    return 64;
 }

@@ -4,27 +4,33 @@
 #include "kernels.cuh"
 
 // TMA descriptors of the five FP32 pools (D, C, X, GP, RP), each with a
-// 128-row box (A operand tiles) and a 256-row box (B operand tiles).
+// 128-row box (A operand tiles and BN = 128 B tiles), a 256-row and a 64-row
+// box (B operand tiles of the other widths).
 struct TcMaps {
-    CUtensorMap map[5][2];
+    CUtensorMap map[5][3];
 };
 
-// Encodes the two descriptors of one pool; false if the driver refuses.
-bool tc_make_map(const Pool<float>& P, CUtensorMap* box128, CUtensorMap* box256);
+// Encodes the three descriptors of one pool; false if the driver refuses.
+bool tc_make_map(const Pool<float>& P, CUtensorMap* box128, CUtensorMap* box256, CUtensorMap* box64);
 
 // Encodes the descriptors of the five pools; false if any is refused (the
 // SIMT GEMM is used then).
 bool tc_make_maps(const Pool<float>* D, const Pool<float>* C, const Pool<float>* X, const Pool<float>* GP,
                   const Pool<float>* RP, TcMaps* out);
 
-// Launches the batched TN GEMM of `g` on the tensor cores with A tiles read
-// through `mapA` (128-row box) and B tiles through `mapB` (256-row box).
-// c_trans_arr (device, per job, may be null) overrides g->c_trans.
-// Returns 0 or a cudaError_t value.
+// Launches the batched TN GEMM of `g` on the tensor cores with 128 x bn tiles
+// (bn = 256, 128 or 64), A tiles read through `mapA` (128-row box) and B tiles
+// through `mapB` (bn-row box).  c_trans_arr (device, per job, may be null)
+// overrides g->c_trans.  Returns 0 or a cudaError_t value.
 int tc_gemm_launch_maps(const GemmArgs<float>* g, const int* c_trans_arr, const CUtensorMap* mapA,
-                        const CUtensorMap* mapB, int njobs, cudaStream_t stream);
+                        const CUtensorMap* mapB, int bn, int njobs, cudaStream_t stream);
+
+// Widest tile (256, 128 or 64 columns) whose tile count still covers num_sms.
+int tc_pick_bn(int M, int N, int njobs, int num_sms);
 
 inline int tc_gemm_launch(const GemmArgs<float>* g, const int* c_trans_arr, int pa, int pb, int njobs,
-                          const TcMaps* maps, cudaStream_t stream) {
-    return tc_gemm_launch_maps(g, c_trans_arr, &maps->map[pa][0], &maps->map[pb][1], njobs, stream);
+                          const TcMaps* maps, int num_sms, cudaStream_t stream) {
+    const int bn = tc_pick_bn(g->M, g->N, njobs, num_sms);
+    const int bi = bn == 256 ? 1 : (bn == 128 ? 0 : 2);
+    return tc_gemm_launch_maps(g, c_trans_arr, &maps->map[pa][0], &maps->map[pb][bi], bn, njobs, stream);
 }

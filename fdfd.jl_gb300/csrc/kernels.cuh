@@ -123,6 +123,8 @@ template <typename T> struct GemvArgs {
     int b, ld, nrhs;    // nrhs: right-hand sides handled by this launch (<= 8)
     int rtot, r0;       // right-hand sides stored per node, first one handled
     T alpha;
+    int rpw, og;        // launch shape, set by launch_gemv: rows per warp (N form),
+                        // lanes per output group (T form)
 };
 // TR = 1: matrices stored transposed.  Returns a cudaError_t value.
 template <typename T>

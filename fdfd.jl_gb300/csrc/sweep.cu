@@ -42,7 +42,7 @@ __device__ void stage_vectors(const GemvArgs<T>& g, const int mslot[2], const in
 }  // namespace
 
 // N-form (row-major blocks): warp per row, lanes over 16-byte column groups.
-// grid: (ceil(b/32), njobs), block 256 (8 warps x 4 rows)
+// grid: (ceil(b/(8*rpw)), njobs), block 256 (8 warps x rpw rows)
 template <typename T, int R>
 __global__ void __launch_bounds__(256) gemv_n_kernel(GemvArgs<T> g) {
     constexpr int VW = 16 / sizeof(T);
@@ -61,8 +61,9 @@ __global__ void __launch_bounds__(256) gemv_n_kernel(GemvArgs<T> g) {
     T* y = g.Y + ((size_t)Y.x * g.rtot + g.r0) * 2 * g.ld;
     const T* y0 = Y.y >= 0 ? g.Y0 + ((size_t)Y.y * g.rtot + g.r0) * 2 * g.ld : nullptr;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int q = 0; q < 4; ++q) {
-        const int row = blockIdx.x * 32 + warp * 4 + q;
+    const int rpw = g.rpw;
+    for (int q = 0; q < rpw; ++q) {
+        const int row = (blockIdx.x * 8 + warp) * rpw + q;
         if (row >= b) break;
         T ar[R], ai[R];
 #pragma unroll
@@ -121,9 +122,10 @@ __global__ void __launch_bounds__(256) gemv_n_kernel(GemvArgs<T> g) {
 }
 
 // Stored-transpose form (row-major Mᵀ): y[i] = Σ_j Mᵀ[j][i] v[j].  A lane owns
-// VW consecutive outputs (one 16-byte load per row j), the 8 warps split the j
-// range, partial sums are reduced through shared memory.
-// grid: (ceil(b/(32*VW)), njobs), block 256
+// VW consecutive outputs (one 16-byte load per row j); a group of og lanes
+// covers og*VW outputs, the 8*(32/og) lane groups of the block split the j
+// range, and the partial sums are reduced through shared memory.
+// grid: (ceil(b/(og*VW)), njobs), block 256
 template <typename T, int R>
 __global__ void __launch_bounds__(256) gemv_t_kernel(GemvArgs<T> g) {
     constexpr int VW = 16 / sizeof(T);
@@ -132,14 +134,19 @@ __global__ void __launch_bounds__(256) gemv_t_kernel(GemvArgs<T> g) {
     const int b = g.b;
     const int bpad = (b + 31) / 32 * 32;
     T* sv = reinterpret_cast<T*>(smem_raw);
-    T* red = sv + (size_t)2 * R * 2 * bpad;          // [warp][out][r][re|im]
+    T* red = sv + (size_t)2 * R * 2 * bpad;          // [group][out][r][re|im]
     const int4 J = g.jobs[blockIdx.y];
     const int2 Y = g.yjobs[blockIdx.y];
     const int mslot[2] = {J.x, J.z}, vnode[2] = {J.y, J.w};
     stage_vectors<T>(g, mslot, vnode, sv, R, bpad);
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int i0 = blockIdx.x * 32 * VW + lane * VW;
+    const int og = g.og, ngrp = 32 / og;          // lanes per output group, groups per warp
+    const int grp = lane / og, sub = lane % og;
+    const int nout = og * VW;                     // outputs of this block
+    const int pid = warp * ngrp + grp;            // partial-sum index, 0 .. 8*ngrp-1
+    const int rstride = 8 * ngrp;                 // j stride between a group's rows
+    const int i0 = blockIdx.x * nout + sub * VW;
     T ar[VW][R], ai[VW][R];
 #pragma unroll
     for (int e = 0; e < VW; ++e)
@@ -152,11 +159,11 @@ __global__ void __launch_bounds__(256) gemv_t_kernel(GemvArgs<T> g) {
             const T* Mr = P.slot(mslot[t]) + i0;
             const T* Mi = Mr + P.plane_elems();
             const T* vt = sv + (size_t)t * R * 2 * bpad;
-            for (int j0 = warp; j0 < b; j0 += 8 * U) {
+            for (int j0 = pid; j0 < b; j0 += rstride * U) {
                 typename V16<T>::type mr[U], mi[U];
 #pragma unroll
                 for (int u = 0; u < U; ++u) {
-                    const int j = j0 + 8 * u;
+                    const int j = j0 + rstride * u;
                     if (j < b) {
                         mr[u] = ld16<T>(Mr + (size_t)j * P.ld);
                         mi[u] = ld16<T>(Mi + (size_t)j * P.ld);
@@ -166,7 +173,7 @@ __global__ void __launch_bounds__(256) gemv_t_kernel(GemvArgs<T> g) {
                 }
 #pragma unroll
                 for (int u = 0; u < U; ++u) {
-                    const int j = j0 + 8 * u;
+                    const int j = j0 + rstride * u;
                     if (j < b) {
                         const T* er = reinterpret_cast<const T*>(&mr[u]);
                         const T* ei = reinterpret_cast<const T*>(&mi[u]);
@@ -184,13 +191,12 @@ __global__ void __launch_bounds__(256) gemv_t_kernel(GemvArgs<T> g) {
             }
         }
     }
-    // cross-warp reduction
-    const int nout = 32 * VW;
+    // cross-group reduction
 #pragma unroll
     for (int e = 0; e < VW; ++e)
 #pragma unroll
         for (int r = 0; r < R; ++r) {
-            const size_t o = (((size_t)warp * nout + lane * VW + e) * R + r) * 2;
+            const size_t o = (((size_t)pid * nout + sub * VW + e) * R + r) * 2;
             red[o] = ar[e][r];
             red[o + 1] = ai[e][r];
         }
@@ -202,7 +208,7 @@ __global__ void __launch_bounds__(256) gemv_t_kernel(GemvArgs<T> g) {
         const int i = blockIdx.x * nout + out;
         if (i >= b) continue;
         T sr = 0, si = 0;
-        for (int w = 0; w < 8; ++w) {
+        for (int w = 0; w < rstride; ++w) {
             const size_t o = (((size_t)w * nout + out) * R + r) * 2;
             sr += red[o];
             si += red[o + 1];
@@ -277,8 +283,20 @@ int gemv_launch_r(cudaStream_t s, int tr, int njobs, const GemvArgs<T>& g) {
         attr = true;
     }
     const size_t smem = gemv_smem<T, R>(tr, g.b);
-    if (tr) gemv_t_kernel<T, R><<<dim3(ceil_div(g.b, 32 * VW), njobs), 256, smem, s>>>(g);
-    else gemv_n_kernel<T, R><<<dim3(ceil_div(g.b, 32), njobs), 256, smem, s>>>(g);
+    // Launch shape: the widest per-block tile that still gives about four blocks
+    // per SM.  Small batches (the deep reduction levels) get narrow tiles, so
+    // their few blocks are still spread over the whole GPU.
+    const long long want = 4LL * 152;
+    GemvArgs<T> a = g;
+    if (tr) {
+        a.og = 32;
+        while (a.og > 8 && (long long)ceil_div(g.b, a.og * VW) * njobs < want) a.og >>= 1;
+        gemv_t_kernel<T, R><<<dim3(ceil_div(g.b, a.og * VW), njobs), 256, smem, s>>>(a);
+    } else {
+        a.rpw = 4;
+        while (a.rpw > 1 && (long long)ceil_div(g.b, 8 * a.rpw) * njobs < want) a.rpw >>= 1;
+        gemv_n_kernel<T, R><<<dim3(ceil_div(g.b, 8 * a.rpw), njobs), 256, smem, s>>>(a);
+    }
     return (int)cudaGetLastError();
 }
 }  // namespace
