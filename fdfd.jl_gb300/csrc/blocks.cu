@@ -54,85 +54,182 @@ __global__ void build_tridiag_kernel(NodeMap m, const cplx<double>* st, double s
 //   D_s  = tri_s - [prev elim] diag(l_s) G_prev diag(u_prev) - [next elim] diag(u_s) G_next diag(l_next)
 //   U_s' = next elim ? -diag(u_s) G_next diag(u_next) : diag(u_s)
 //   L_s' = prev elim ? -diag(l_s) G_prev diag(l_prev) : diag(l_s)
-// 32x32 tiles, block (32, 8); transposed stores go through shared memory.
-// grid: (ceil(b/32), ceil(b/32), njobs)
+// Tiles of 32 rows x 128 columns, block 256: warp w takes rows w, w+8, ..,
+// each lane 4 consecutive columns, so block loads and row-major stores are
+// 16-byte vectors and the per-row stencil factors are loaded once per lane.
+// Transposed stores are staged in shared memory and written 32 elements
+// (one transposed row segment) per warp instruction.
+// grid: (ceil(b/128), ceil(b/32), njobs), dynamic smem level1_combine_smem<T>()
 // ---------------------------------------------------------------------------
+template <typename T> struct Vec16;
+template <> struct Vec16<float> { typedef float4 type; };
+template <> struct Vec16<double> { typedef double2 type; };
+
 template <typename T>
-__global__ void level1_combine_kernel(NodeMap m, const cplx<double>* st, double scale, Pool<T> D,
-                                      Pool<T> C, const L1Job* jobs) {
-    __shared__ T tU[2][32][33], tL[2][32][33];
+constexpr size_t level1_combine_smem() { return (size_t)2 * 2 * 128 * 33 * sizeof(T); }
+
+template <typename T>
+__global__ void __launch_bounds__(256) level1_combine_kernel(NodeMap m, const cplx<double>* st, double scale,
+                                                             Pool<T> D, Pool<T> C, const L1Job* jobs) {
+    constexpr int CPL = 4;                    // columns per lane
+    constexpr int VW = 16 / sizeof(T);
+    constexpr int NVL = CPL / VW;             // 16-byte vectors per lane and plane
+    typedef typename Vec16<T>::type VT;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* tU = reinterpret_cast<T*>(smem_raw);  // [plane][tile column][tile row], row stride 33
+    T* tL = tU + 2 * 128 * 33;
     const L1Job J = jobs[blockIdx.z];
-    int b = m.b;
-    int c0 = blockIdx.x * 32, r0 = blockIdx.y * 32;
-    int tx = threadIdx.x, ty = threadIdx.y;
+    const int b = m.b;
+    const int c0 = blockIdx.x * 128, r0 = blockIdx.y * 32;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int cl0 = lane * CPL;              // first tile column of this lane
+    const int cb0 = c0 + cl0;                // its matrix column
     const T* Gp = D.slot(J.prev);
     const T* Gn = D.slot(J.next);
-    long long pe = D.plane_elems();
+    const long long pe = D.plane_elems();
     T* Ds = D.slot(J.s);
-    int c = c0 + tx;
+    T* Us = C.slot(J.u_slot);
+    T* Ls = C.slot(J.l_slot);
+    const long long cpe = C.plane_elems();
     // stencil values are FP64; the arithmetic runs in the factor precision T
     auto tv = [&](cplx<double> v) { return cmk((T)(v.re * scale), (T)(v.im * scale)); };
     const cplx<T> z = cmk((T)0, (T)0);
-    cplx<T> lc_next = z, uc_next = z, uc_prev = z, lc_prev = z;
-    if (c < b) {
-        if (J.next_elim) {
-            lc_next = tv(st_at<T>(st, m, m.p_cprev(), J.next, c));
-            uc_next = tv(st_at<T>(st, m, m.p_cnext(), J.next, c));
-        }
-        if (J.prev_elim) {
-            uc_prev = tv(st_at<T>(st, m, m.p_cnext(), J.prev, c));
-            lc_prev = tv(st_at<T>(st, m, m.p_cprev(), J.prev, c));
+    cplx<T> lcn[CPL], ucn[CPL], ucp[CPL], lcp[CPL];
+#pragma unroll
+    for (int e = 0; e < CPL; ++e) {
+        const int c = cb0 + e;
+        lcn[e] = ucn[e] = ucp[e] = lcp[e] = z;
+        if (c < b) {
+            if (J.next_elim) {
+                lcn[e] = tv(st_at<T>(st, m, m.p_cprev(), J.next, c));
+                ucn[e] = tv(st_at<T>(st, m, m.p_cnext(), J.next, c));
+            }
+            if (J.prev_elim) {
+                ucp[e] = tv(st_at<T>(st, m, m.p_cnext(), J.prev, c));
+                lcp[e] = tv(st_at<T>(st, m, m.p_cprev(), J.prev, c));
+            }
         }
     }
+    const bool full = cb0 + CPL <= b;        // all four columns inside the matrix
     for (int q = 0; q < 4; ++q) {
-        int rl = ty + 8 * q;
-        int r = r0 + rl;
-        cplx<T> dv = z, uv = z, lv = z;
-        bool ok = (r < b && c < b);
-        if (ok) {
-            const cplx<T> ls = tv(st_at<T>(st, m, m.p_cprev(), J.s, r));
-            const cplx<T> us = tv(st_at<T>(st, m, m.p_cnext(), J.s, r));
+        const int rl = warp + 8 * q;
+        const int r = r0 + rl;
+        if (r >= b || cb0 >= b) {
+            // nothing to compute; the transposed staging of this element stays unused
+            continue;
+        }
+        const cplx<T> ls = tv(st_at<T>(st, m, m.p_cprev(), J.s, r));
+        const cplx<T> us = tv(st_at<T>(st, m, m.p_cnext(), J.s, r));
+        T gpr[CPL], gpi[CPL], gnr[CPL], gni[CPL];
+        const long long o = (long long)r * D.ld + cb0;   // cb0 < b <= ld, cb0 % 4 == 0: vectors stay in the row
+#pragma unroll
+        for (int v = 0; v < NVL; ++v) {
+            VT a = {}, c = {}, d = {}, f = {};
+            if (J.prev_elim) {
+                a = reinterpret_cast<const VT*>(Gp + o)[v];
+                c = reinterpret_cast<const VT*>(Gp + pe + o)[v];
+            }
+            if (J.next_elim) {
+                d = reinterpret_cast<const VT*>(Gn + o)[v];
+                f = reinterpret_cast<const VT*>(Gn + pe + o)[v];
+            }
+#pragma unroll
+            for (int e = 0; e < VW; ++e) {
+                gpr[v * VW + e] = reinterpret_cast<const T*>(&a)[e];
+                gpi[v * VW + e] = reinterpret_cast<const T*>(&c)[e];
+                gnr[v * VW + e] = reinterpret_cast<const T*>(&d)[e];
+                gni[v * VW + e] = reinterpret_cast<const T*>(&f)[e];
+            }
+        }
+        T dr[CPL], di[CPL], ur[CPL], ui[CPL], lr[CPL], li[CPL];
+#pragma unroll
+        for (int e = 0; e < CPL; ++e) {
+            const int c = cb0 + e;
             cplx<double> tri = cmk(0.0, 0.0);
             if (c == r) tri = st_at<T>(st, m, 0, J.s, r);
             if (c == (r + b - 1) % b) tri = cadd(tri, st_at<T>(st, m, m.p_inprev(), J.s, r));
             if (c == (r + 1) % b) tri = cadd(tri, st_at<T>(st, m, m.p_innext(), J.s, r));
-            dv = tv(tri);
+            cplx<T> dv = tv(tri), uv = z, lv = z;
             if (J.prev_elim) {
-                const long long o = (long long)r * D.ld + c;
-                const cplx<T> lg = cmul(ls, cmk(Gp[o], Gp[pe + o]));
-                dv = csub(dv, cmul(lg, uc_prev));
-                lv = cneg(cmul(lg, lc_prev));
+                const cplx<T> lg = cmul(ls, cmk(gpr[e], gpi[e]));
+                dv = csub(dv, cmul(lg, ucp[e]));
+                lv = cneg(cmul(lg, lcp[e]));
             } else if (c == r) {
                 lv = ls;
             }
             if (J.next_elim) {
-                const long long o = (long long)r * D.ld + c;
-                const cplx<T> ug = cmul(us, cmk(Gn[o], Gn[pe + o]));
-                dv = csub(dv, cmul(ug, lc_next));
-                uv = cneg(cmul(ug, uc_next));
+                const cplx<T> ug = cmul(us, cmk(gnr[e], gni[e]));
+                dv = csub(dv, cmul(ug, lcn[e]));
+                uv = cneg(cmul(ug, ucn[e]));
             } else if (c == r) {
                 uv = us;
             }
-            // re/im only: D_s is read as re/im until its inversion writes all planes
-            store_elem<T>(D, Ds, r, c, dv, 0, false);
+            dr[e] = dv.re; di[e] = dv.im; ur[e] = uv.re; ui[e] = uv.im; lr[e] = lv.re; li[e] = lv.im;
         }
-        if (!J.u_trans) { if (ok) store_elem<T>(C, C.slot(J.u_slot), r, c, uv, 0); }
-        else { tU[0][rl][tx] = uv.re; tU[1][rl][tx] = uv.im; }
-        if (!J.l_trans) { if (ok) store_elem<T>(C, C.slot(J.l_slot), r, c, lv, 0); }
-        else { tL[0][rl][tx] = lv.re; tL[1][rl][tx] = lv.im; }
+        // D_s: re/im only (read as re/im until its inversion writes all planes)
+        auto put_row = [&](T* base, long long ppe, const T* xr, const T* xi, bool lo) {
+            const long long ob = (long long)r * C.ld + cb0;
+            if (full) {
+#pragma unroll
+                for (int v = 0; v < NVL; ++v) {
+                    VT a, c, al, cl;
+#pragma unroll
+                    for (int e = 0; e < VW; ++e) {
+                        reinterpret_cast<T*>(&a)[e] = xr[v * VW + e];
+                        reinterpret_cast<T*>(&c)[e] = xi[v * VW + e];
+                        reinterpret_cast<T*>(&al)[e] = (T)tf32_lo((float)xr[v * VW + e]);
+                        reinterpret_cast<T*>(&cl)[e] = (T)tf32_lo((float)xi[v * VW + e]);
+                    }
+                    reinterpret_cast<VT*>(base + ob)[v] = a;
+                    reinterpret_cast<VT*>(base + ppe + ob)[v] = c;
+                    if (lo) {
+                        reinterpret_cast<VT*>(base + 2 * ppe + ob)[v] = al;
+                        reinterpret_cast<VT*>(base + 3 * ppe + ob)[v] = cl;
+                    }
+                }
+            } else {
+#pragma unroll
+                for (int e = 0; e < CPL; ++e) {
+                    if (cb0 + e < b) {
+                        base[ob + e] = xr[e];
+                        base[ppe + ob + e] = xi[e];
+                        if (lo) {
+                            base[2 * ppe + ob + e] = (T)tf32_lo((float)xr[e]);
+                            base[3 * ppe + ob + e] = (T)tf32_lo((float)xi[e]);
+                        }
+                    }
+                }
+            }
+        };
+        put_row(Ds, pe, dr, di, false);
+        const bool clo = C.planes == 4;
+        if (!J.u_trans) put_row(Us, cpe, ur, ui, clo);
+        else {
+#pragma unroll
+            for (int e = 0; e < CPL; ++e) {
+                tU[(cl0 + e) * 33 + rl] = ur[e];
+                tU[128 * 33 + (cl0 + e) * 33 + rl] = ui[e];
+            }
+        }
+        if (!J.l_trans) put_row(Ls, cpe, lr, li, clo);
+        else {
+#pragma unroll
+            for (int e = 0; e < CPL; ++e) {
+                tL[(cl0 + e) * 33 + rl] = lr[e];
+                tL[128 * 33 + (cl0 + e) * 33 + rl] = li[e];
+            }
+        }
     }
     if (J.u_trans || J.l_trans) {
         __syncthreads();
-        // transposed store: element (r, c) -> position (c, r); thread writes row c0+ty*4+q, col r0+tx
-        for (int q = 0; q < 4; ++q) {
-            int cl = ty + 8 * q;
-            int cc = c0 + cl, rr = r0 + tx;
-            if (cc < b && rr < b) {
-                if (J.u_trans)
-                    store_elem<T>(C, C.slot(J.u_slot), cc, rr, cmk(tU[0][tx][cl], tU[1][tx][cl]), 0);
-                if (J.l_trans)
-                    store_elem<T>(C, C.slot(J.l_slot), cc, rr, cmk(tL[0][tx][cl], tL[1][tx][cl]), 0);
-            }
+        // transposed store: element (r, c) -> position (c, r); warp w writes the
+        // transposed rows c0+w, c0+w+8, ..., lane = tile row
+        const int rr = r0 + lane;
+        for (int cl = warp; cl < 128; cl += 8) {
+            const int cc = c0 + cl;
+            if (cc >= b || rr >= b) continue;
+            if (J.u_trans) store_elem<T>(C, Us, cc, rr, cmk(tU[cl * 33 + lane], tU[128 * 33 + cl * 33 + lane]), 0);
+            if (J.l_trans) store_elem<T>(C, Ls, cc, rr, cmk(tL[cl * 33 + lane], tL[128 * 33 + cl * 33 + lane]), 0);
         }
     }
 }
@@ -203,9 +300,6 @@ __host__ __device__ constexpr size_t gj_panel_smem_elems() {
                                                   : (NB * 129 > 2 * 128 * R ? NB * 129 : 2 * 128 * R));
 }
 
-template <typename T> struct Vec16;
-template <> struct Vec16<float> { typedef float4 type; };
-template <> struct Vec16<double> { typedef double2 type; };
 
 template <typename T, int NB, int R, int C>
 __global__ void __launch_bounds__(512, 1) gj_panel_kernel(Pool<T> M, const int* slots, Pool<T> GP, Pool<T> RP,
@@ -611,171 +705,254 @@ __global__ void mcopy_kernel(Pool<T> S, Pool<T> Dp, const int3* jobs) {
 //
 // D_k = T0 + a0·e_0·e_{b-1}ᵀ + cN·e_{b-1}·e_0ᵀ with T0 tridiagonal (the in-line
 // neighbours without the periodic wrap) and the two corner terms of the wrap.
-// T0 is factored with partial pivoting by the recurrences of LAPACK's
-// xGTTRF (row interchanges between neighbours, a second superdiagonal du2),
-// Z = T0⁻¹ is formed column by column with the xGTTRS recurrences (thread j
-// solves T0 z = e_j), and the corners are added back by the Sherman-Morrison-
-// Woodbury identity with the 2x2 capacitance matrix S = I + Vᵀ Z U:
-//     D_k⁻¹ = Z − [Z[:,0], Z[:,b−1]] · S⁻¹ · [a0·Z[b−1,:] ; cN·Z[0,:]].
-// Result (with TF32 residual planes) in the D-pool slot of the node.
-// grid: njobs, block 512, dynamic smem 6*b*sizeof(cplx<T>) + b*sizeof(int)
+// With Z = T0⁻¹ the Sherman-Morrison-Woodbury identity gives
+//     D_k⁻¹ = Z − [z0, zN] · W,   W = S⁻¹ [a0·Z[b−1,:] ; cN·Z[0,:]],
+//     S = I + [[a0 z0[b−1], a0 zN[b−1]], [cN z0[0], cN zN[0]]],
+// z0 = Z[:,0], zN = Z[:,b−1].  Two kernels:
+//  * tri_factor_kernel, a warp per node, all in shared memory: lane 0 factors T0 with partial
+//    pivoting by the recurrences of LAPACK's xGTTRF (row interchanges between
+//    neighbours, a second superdiagonal du2); lanes 0-3 then solve for the two
+//    columns z0, zN (xGTTRS recurrences) and the two rows Z[0,:], Z[b−1,:]
+//    (the transposed recurrences, solving T0ᵀ x = e); all lanes form W.
+//  * tri_columns_kernel, a thread per column j: Z[:,j] by the forward and
+//    backward recurrences (the forward one starts at row j−1: rows above are
+//    zero), the Woodbury correction applied as each row is finished, and the
+//    column of G = D_k⁻¹ written once (re and im: these inverses are never GEMM operands).
+// Factor workspace per node (cplx<T>): [dl | du | du2 | dinv | z0 | zN | w0 | w1],
+// b entries each; ipiv: b ints per node.
 // ---------------------------------------------------------------------------
 template <typename T>
-__global__ void __launch_bounds__(512) tri_inverse_kernel(NodeMap m, const cplx<double>* st, double scale, Pool<T> D,
-                                                          const int* nodes, unsigned* err) {
+__global__ void __launch_bounds__(32) tri_factor_kernel(NodeMap m, const cplx<double>* st, double scale,
+                                                        const int* nodes, cplx<T>* fac, int* piv, unsigned* err) {
+    // everything runs out of shared memory: the serial recurrences then wait on
+    // shared-memory latency, not on global loads.  Layout (cplx<T>, b each):
+    // dl, du, du2, dinv, z0, zN, w0, w1, then ipiv (b ints)
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int b = m.b;
     cplx<T>* dl = reinterpret_cast<cplx<T>*>(smem_raw);
-    cplx<T>* dd = dl + b;      // diagonal, then its reciprocal
-    cplx<T>* du = dd + b;
+    cplx<T>* du = dl + b;
     cplx<T>* du2 = du + b;
-    cplx<T>* z0 = du2 + b;     // Z[:, 0]
-    cplx<T>* zN = z0 + b;      // Z[:, b-1]
-    int* ipiv = reinterpret_cast<int*>(zN + b);
-    __shared__ cplx<T> s_inv[4];
-    __shared__ cplx<T> s_a0, s_cN;
-    __shared__ int s_bad;
-
-    const int node = nodes[blockIdx.x];
-    const int tid = threadIdx.x, nt = blockDim.x;
-    T* Gre = D.slot(node);
-    const long long pe = D.plane_elems();
-    T* Gim = Gre + pe;
-    const int ld = D.ld;
+    cplx<T>* dinv = du2 + b;
+    cplx<T>* z0 = dinv + b;
+    cplx<T>* zN = z0 + b;
+    cplx<T>* w0 = zN + b;
+    cplx<T>* w1 = w0 + b;
+    int* ipiv = reinterpret_cast<int*>(w1 + b);
+    const int job = blockIdx.x;
+    const int lane = threadIdx.x;
+    const int node = nodes[job];
     auto coef = [&](int plane, int i) {
-        cplx<double> v = cscale(st_at<T>(st, m, plane, node, i), scale);
+        const cplx<double> v = cscale(st_at<T>(st, m, plane, node, i), scale);
         return cmk((T)v.re, (T)v.im);
     };
-    for (int i = tid; i < b; i += nt) {
-        dd[i] = coef(0, i);
-        dl[i] = (i + 1 < b) ? coef(m.p_inprev(), i + 1) : cmk((T)0, (T)0);   // T0[i+1][i]
-        du[i] = (i + 1 < b) ? coef(m.p_innext(), i) : cmk((T)0, (T)0);      // T0[i][i+1]
-        du2[i] = cmk((T)0, (T)0);
-        ipiv[i] = i;
+    const cplx<T> z = cmk((T)0, (T)0);
+    // T0 into shared memory: diagonal (in dinv), sub-diagonal T0[i+1][i] (in dl),
+    // super-diagonal T0[i][i+1] (in du)
+    for (int i = lane; i < b; i += 32) {
+        dinv[i] = coef(0, i);
+        dl[i] = i + 1 < b ? coef(m.p_inprev(), i + 1) : z;
+        du[i] = i + 1 < b ? coef(m.p_innext(), i) : z;
+        du2[i] = z;
     }
-    if (tid == 0) {
-        s_a0 = coef(m.p_inprev(), 0);        // D[0][b-1]
-        s_cN = coef(m.p_innext(), b - 1);    // D[b-1][0]
-        s_bad = 0;
-    }
-    __syncthreads();
-    if (tid == 0) {
-        // xGTTRF recurrences (partial pivoting between neighbouring rows)
+    __syncwarp();
+    if (lane == 0) {
+        // xGTTRF recurrences; the diagonal is replaced by the reciprocals of its final entries
+        int bad = 0;
+        cplx<T> d = dinv[0];
         for (int i = 0; i + 1 < b; ++i) {
-            if (cabs1(dd[i]) >= cabs1(dl[i])) {
-                if (cabs1(dd[i]) > (T)0) {
-                    cplx<T> fact = cmul(dl[i], cinv(dd[i]));
-                    dl[i] = fact;
-                    dd[i + 1] = csub(dd[i + 1], cmul(fact, du[i]));
+            cplx<T> lo = dl[i];
+            cplx<T> dn = dinv[i + 1];
+            const cplx<T> upper = du[i];
+            int ip = i;
+            if (cabs1(d) >= cabs1(lo)) {
+                cplx<T> fact = z;
+                if (cabs1(d) > (T)0) {
+                    fact = cmul(lo, cinv_pow2(d));
+                    dn = csub(dn, cmul(fact, upper));
                 }
+                lo = fact;
             } else {
-                cplx<T> fact = cmul(dd[i], cinv(dl[i]));
-                dd[i] = dl[i];
-                dl[i] = fact;
-                cplx<T> temp = du[i];
-                du[i] = dd[i + 1];
-                dd[i + 1] = csub(temp, cmul(fact, dd[i + 1]));
+                const cplx<T> fact = cmul(d, cinv_pow2(lo));
+                d = lo;
+                du[i] = dn;
+                dn = csub(upper, cmul(fact, dn));
                 if (i + 2 < b) {
                     du2[i] = du[i + 1];
                     du[i + 1] = cneg(cmul(fact, du[i + 1]));
                 }
-                ipiv[i] = i + 1;
+                lo = fact;
+                ip = i + 1;
             }
+            if (!(cabs1(d) > (T)0) || !isfinite((double)cabs1(d))) { bad = 1; d = cmk((T)1, (T)0); }
+            dl[i] = lo;
+            dinv[i] = cinv_pow2(d);
+            ipiv[i] = ip;
+            d = dn;
         }
-        for (int i = 0; i < b; ++i) {
-            if (!(cabs1(dd[i]) > (T)0) || !isfinite((double)cabs1(dd[i]))) { s_bad = 1; dd[i] = cmk((T)1, (T)0); }
-            dd[i] = cinv(dd[i]);
-        }
+        if (!(cabs1(d) > (T)0) || !isfinite((double)cabs1(d))) { bad = 1; d = cmk((T)1, (T)0); }
+        dl[b - 1] = z;
+        du[b - 1] = z;
+        dinv[b - 1] = cinv_pow2(d);
+        ipiv[b - 1] = b - 1;
+        if (bad) dev_error(err, FDFD_DEVERR_SINGULAR);
     }
-    __syncthreads();
-    // Z = T0⁻¹, column j per thread (xGTTRS recurrences with right-hand side e_j)
-    for (int j = tid; j < b; j += nt) {
-        cplx<T> cur = cmk((T)(j == 0 ? 1 : 0), (T)0);
-        for (int i = 0; i + 1 < b; ++i) {
-            cplx<T> nxt = cmk((T)(i + 1 == j ? 1 : 0), (T)0);
-            cplx<T> yi;
-            if (ipiv[i] == i) {
-                yi = cur;
-                nxt = csub(nxt, cmul(dl[i], cur));
-            } else {
-                yi = nxt;
-                nxt = csub(cur, cmul(dl[i], nxt));
-            }
-            Gre[(size_t)i * ld + j] = yi.re;
-            Gim[(size_t)i * ld + j] = yi.im;
-            cur = nxt;
-        }
-        // back substitution with U (diagonal, du, du2); y read back in blocks of 8 rows
-        cplx<T> x1 = cmul(cur, dd[b - 1]);          // x[b-1]
-        Gre[(size_t)(b - 1) * ld + j] = x1.re;
-        Gim[(size_t)(b - 1) * ld + j] = x1.im;
-        cplx<T> x2 = cmk((T)0, (T)0);               // x[i+2]
-        int i = b - 2;
-        while (i >= 0) {
-            const int n8 = min(8, i + 1);
-            cplx<T> yv[8];
-#pragma unroll
-            for (int u = 0; u < 8; ++u)
-                if (u < n8) yv[u] = cmk(Gre[(size_t)(i - u) * ld + j], Gim[(size_t)(i - u) * ld + j]);
-#pragma unroll
-            for (int u = 0; u < 8; ++u) {
-                if (u < n8) {
-                    const int r = i - u;
-                    cplx<T> s = csub(yv[u], cmul(du[r], x1));
-                    if (r + 2 < b) s = csub(s, cmul(du2[r], x2));
-                    const cplx<T> xr = cmul(s, dd[r]);
-                    Gre[(size_t)r * ld + j] = xr.re;
-                    Gim[(size_t)r * ld + j] = xr.im;
-                    x2 = x1;
-                    x1 = xr;
+    __syncwarp();
+    // two columns (lanes 0, 1: T0 x = e_0, e_{b-1}) and two rows (lanes 2, 3:
+    // T0ᵀ x = e_0, e_{b-1}); results in z0, zN, w1 (row 0), w0 (row b-1)
+    for (int i = lane; i < b; i += 32) {
+        z0[i] = cmk((T)(i == 0 ? 1 : 0), (T)0);
+        zN[i] = cmk((T)(i == b - 1 ? 1 : 0), (T)0);
+        w1[i] = z0[i];
+        w0[i] = zN[i];
+    }
+    __syncwarp();
+    if (lane < 4) {
+        cplx<T>* x = lane == 0 ? z0 : (lane == 1 ? zN : (lane == 2 ? w1 : w0));
+        if (lane < 2) {
+            // L y = e (interchanges between neighbours), then U x = y
+            for (int i = 0; i + 1 < b; ++i) {
+                if (ipiv[i] == i) {
+                    x[i + 1] = csub(x[i + 1], cmul(dl[i], x[i]));
+                } else {
+                    const cplx<T> t = x[i];
+                    x[i] = x[i + 1];
+                    x[i + 1] = csub(t, cmul(dl[i], x[i]));
                 }
             }
-            i -= n8;
-        }
-    }
-    __syncthreads();
-    for (int i = tid; i < b; i += nt) {
-        z0[i] = cmk(Gre[(size_t)i * ld], Gim[(size_t)i * ld]);
-        zN[i] = cmk(Gre[(size_t)i * ld + b - 1], Gim[(size_t)i * ld + b - 1]);
-    }
-    __syncthreads();
-    if (tid == 0) {
-        // S = I + [[a0 Z[b-1][0], a0 Z[b-1][b-1]], [cN Z[0][0], cN Z[0][b-1]]]
-        const cplx<T> s00 = cadd(cmk((T)1, (T)0), cmul(s_a0, z0[b - 1]));
-        const cplx<T> s01 = cmul(s_a0, zN[b - 1]);
-        const cplx<T> s10 = cmul(s_cN, z0[0]);
-        const cplx<T> s11 = cadd(cmk((T)1, (T)0), cmul(s_cN, zN[0]));
-        const cplx<T> det = csub(cmul(s00, s11), cmul(s01, s10));
-        if (!(cabs1(det) > (T)0)) s_bad = 1;
-        const cplx<T> id = cabs1(det) > (T)0 ? cinv(det) : cmk((T)0, (T)0);
-        s_inv[0] = cmul(s11, id);
-        s_inv[1] = cneg(cmul(s01, id));
-        s_inv[2] = cneg(cmul(s10, id));
-        s_inv[3] = cmul(s00, id);
-        if (s_bad) dev_error(err, FDFD_DEVERR_SINGULAR);
-    }
-    __syncthreads();
-    // Woodbury correction, column j per thread; writes the TF32 residual planes too
-    for (int j = tid; j < b; j += nt) {
-        const cplx<T> v0 = cmul(s_a0, cmk(Gre[(size_t)(b - 1) * ld + j], Gim[(size_t)(b - 1) * ld + j]));
-        const cplx<T> v1 = cmul(s_cN, cmk(Gre[j], Gim[j]));
-        const cplx<T> w0 = cadd(cmul(s_inv[0], v0), cmul(s_inv[1], v1));
-        const cplx<T> w1 = cadd(cmul(s_inv[2], v0), cmul(s_inv[3], v1));
-        // column j is read and rewritten by this thread only (columns 0 and b-1 are in z0, zN)
-        for (int i0 = 0; i0 < b; i0 += 8) {
-            cplx<T> zv[8];
-#pragma unroll
-            for (int u = 0; u < 8; ++u)
-                if (i0 + u < b) zv[u] = cmk(Gre[(size_t)(i0 + u) * ld + j], Gim[(size_t)(i0 + u) * ld + j]);
-#pragma unroll
-            for (int u = 0; u < 8; ++u) {
-                const int i = i0 + u;
-                if (i < b) {
-                    const cplx<T> g = csub(csub(zv[u], cmul(z0[i], w0)), cmul(zN[i], w1));
-                    store_elem<T>(D, Gre, i, j, g, 0);
+            cplx<T> x1 = cmul(x[b - 1], dinv[b - 1]), x2 = z;
+            x[b - 1] = x1;
+            for (int i = b - 2; i >= 0; --i) {
+                const cplx<T> xi = cmul(csub(csub(x[i], cmul(du[i], x1)), cmul(du2[i], x2)), dinv[i]);
+                x[i] = xi;
+                x2 = x1;
+                x1 = xi;
+            }
+        } else {
+            // Uᵀ y = e, then Lᵀ x = y (interchanges applied in reverse)
+            cplx<T> y1 = cmul(x[0], dinv[0]), y2 = z;   // y[i-1], y[i-2]
+            x[0] = y1;
+            for (int i = 1; i < b; ++i) {
+                cplx<T> yi = csub(x[i], cmul(du[i - 1], y1));
+                if (i >= 2) yi = csub(yi, cmul(du2[i - 2], y2));
+                yi = cmul(yi, dinv[i]);
+                x[i] = yi;
+                y2 = y1;
+                y1 = yi;
+            }
+            for (int i = b - 2; i >= 0; --i) {
+                if (ipiv[i] == i) {
+                    x[i] = csub(x[i], cmul(dl[i], x[i + 1]));
+                } else {
+                    const cplx<T> t = x[i + 1];
+                    x[i + 1] = csub(x[i], cmul(dl[i], t));
+                    x[i] = t;
                 }
             }
         }
+    }
+    __syncwarp();
+    // W = S⁻¹ [a0·Z[b−1,:]; cN·Z[0,:]] (w0 holds Z[b−1,:], w1 holds Z[0,:])
+    const cplx<T> a0 = coef(m.p_inprev(), 0);        // D[0][b-1]
+    const cplx<T> cN = coef(m.p_innext(), b - 1);    // D[b-1][0]
+    const cplx<T> one = cmk((T)1, (T)0);
+    const cplx<T> s00 = cadd(one, cmul(a0, z0[b - 1]));
+    const cplx<T> s01 = cmul(a0, zN[b - 1]);
+    const cplx<T> s10 = cmul(cN, z0[0]);
+    const cplx<T> s11 = cadd(one, cmul(cN, zN[0]));
+    const cplx<T> det = csub(cmul(s00, s11), cmul(s01, s10));
+    const bool dbad = !(cabs1(det) > (T)0) || !isfinite((double)cabs1(det));
+    if (dbad && lane == 0) dev_error(err, FDFD_DEVERR_SINGULAR);
+    const cplx<T> id = dbad ? z : cinv_pow2(det);
+    const cplx<T> i00 = cmul(s11, id), i01 = cneg(cmul(s01, id));
+    const cplx<T> i10 = cneg(cmul(s10, id)), i11 = cmul(s00, id);
+    __syncwarp();
+    for (int j = lane; j < b; j += 32) {
+        const cplx<T> v0 = cmul(a0, w0[j]), v1 = cmul(cN, w1[j]);
+        w0[j] = cadd(cmul(i00, v0), cmul(i01, v1));
+        w1[j] = cadd(cmul(i10, v0), cmul(i11, v1));
+    }
+    __syncwarp();
+    // the node's factors to global memory (coalesced)
+    cplx<T>* f = fac + (size_t)job * 8 * b;
+    for (int i = lane; i < 8 * b; i += 32) f[i] = dl[i];
+    for (int i = lane; i < b; i += 32) piv[(size_t)job * b + i] = ipiv[i];
+}
+
+// G[:, j] = Z[:, j] − z0·w0[j] − zN·w1[j] with Z[:, j] = T0⁻¹ e_j; the factor
+// arrays of the node are staged in shared memory (read by every thread in the
+// same order).  grid: (ceil(b/128), njobs), block 128,
+// dynamic smem 6*b*sizeof(cplx<T>) + b*sizeof(int)
+template <typename T>
+__global__ void __launch_bounds__(128) tri_columns_kernel(int b, Pool<T> D, const int* nodes, const cplx<T>* fac,
+                                                          const int* piv) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    cplx<T>* s_dl = reinterpret_cast<cplx<T>*>(smem_raw);
+    cplx<T>* s_du = s_dl + b;
+    cplx<T>* s_du2 = s_du + b;
+    cplx<T>* s_dinv = s_du2 + b;
+    cplx<T>* s_z0 = s_dinv + b;
+    cplx<T>* s_zN = s_z0 + b;
+    int* s_piv = reinterpret_cast<int*>(s_zN + b);
+    const int job = blockIdx.y;
+    const cplx<T>* f = fac + (size_t)job * 8 * b;
+    for (int i = threadIdx.x; i < 6 * b; i += blockDim.x) s_dl[i] = f[i];
+    for (int i = threadIdx.x; i < b; i += blockDim.x) s_piv[i] = piv[(size_t)job * b + i];
+    __syncthreads();
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= b) return;
+    const cplx<T> w0 = f[6 * b + j], w1 = f[7 * b + j];
+    T* Gre = D.slot(nodes[job]);
+    const long long pe = D.plane_elems();
+    T* Gim = Gre + pe;
+    const int ld = D.ld;
+    const int i0 = j > 0 ? j - 1 : 0;          // rows above j-1 of T0⁻¹ e_j are zero after L⁻¹
+    // forward: y = L⁻¹ e_j, rows i0 .. b-2 stored in G (as scratch)
+    cplx<T> cur = cmk((T)(j == i0 ? 1 : 0), (T)0);
+    for (int i = i0; i + 1 < b; ++i) {
+        cplx<T> nxt = cmk((T)(i + 1 == j ? 1 : 0), (T)0);
+        cplx<T> yi;
+        if (s_piv[i] == i) {
+            yi = cur;
+            nxt = csub(nxt, cmul(s_dl[i], cur));
+        } else {
+            yi = nxt;
+            nxt = csub(cur, cmul(s_dl[i], nxt));
+        }
+        Gre[(size_t)i * ld + j] = yi.re;
+        Gim[(size_t)i * ld + j] = yi.im;
+        cur = nxt;
+    }
+    // backward: x = U⁻¹ y, each finished row corrected and written with all planes
+    auto put = [&](int r, cplx<T> x) {
+        const cplx<T> g = csub(csub(x, cmul(s_z0[r], w0)), cmul(s_zN[r], w1));
+        // re/im only: first-step inverses are read by the combine and the sweeps, never as GEMM operands
+        store_elem<T>(D, Gre, r, j, g, 0, false);
+    };
+    cplx<T> x1 = cmul(cur, s_dinv[b - 1]);     // x[b-1]
+    put(b - 1, x1);
+    cplx<T> x2 = cmk((T)0, (T)0);             // x[i+2]
+    int i = b - 2;
+    while (i >= 0) {
+        const int n8 = min(8, i + 1);
+        cplx<T> yv[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const int r = i - u;
+            yv[u] = cmk((T)0, (T)0);
+            if (u < n8 && r >= i0) yv[u] = cmk(Gre[(size_t)r * ld + j], Gim[(size_t)r * ld + j]);
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            if (u < n8) {
+                const int r = i - u;
+                const cplx<T> sr = csub(csub(yv[u], cmul(s_du[r], x1)), cmul(s_du2[r], x2));
+                const cplx<T> xr = cmul(sr, s_dinv[r]);
+                put(r, xr);
+                x2 = x1;
+                x1 = xr;
+            }
+        }
+        i -= n8;
     }
 }
 
@@ -784,15 +961,22 @@ __global__ void __launch_bounds__(512) tri_inverse_kernel(NodeMap m, const cplx<
 // ---------------------------------------------------------------------------
 template <typename T>
 void launch_tri_inverse(cudaStream_t s, int njobs, NodeMap m, const cplx<double>* st, double scale, Pool<T> D,
-                        const int* nodes, unsigned* err) {
-    size_t smem = 6 * (size_t)m.b * sizeof(cplx<T>) + (size_t)m.b * sizeof(int);
+                        const int* nodes, cplx<T>* fac, int* piv, unsigned* err) {
+    const size_t fsmem = 8 * (size_t)m.b * sizeof(cplx<T>) + (size_t)m.b * sizeof(int);
+    static size_t fopted = 48 * 1024;
+    if (fsmem > fopted &&
+        cudaFuncSetAttribute(tri_factor_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsmem) ==
+            cudaSuccess)
+        fopted = fsmem;
+    tri_factor_kernel<T><<<njobs, 32, fsmem, s>>>(m, st, scale, nodes, fac, piv, err);
+    const size_t smem = 6 * (size_t)m.b * sizeof(cplx<T>) + (size_t)m.b * sizeof(int);
     // above 48 KB (FP64 blocks of more than ~500 unknowns) the kernel must opt in
     static size_t opted = 48 * 1024;
     if (smem > opted &&
-        cudaFuncSetAttribute(tri_inverse_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) ==
+        cudaFuncSetAttribute(tri_columns_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) ==
             cudaSuccess)
         opted = smem;
-    tri_inverse_kernel<T><<<njobs, 512, smem, s>>>(m, st, scale, D, nodes, err);
+    tri_columns_kernel<T><<<dim3(ceil_div(m.b, 128), njobs), 128, smem, s>>>(m.b, D, nodes, fac, piv);
 }
 template <typename T>
 void launch_build_tridiag(cudaStream_t s, int njobs, NodeMap m, const cplx<double>* st, double scale, Pool<T> D,
@@ -802,8 +986,13 @@ void launch_build_tridiag(cudaStream_t s, int njobs, NodeMap m, const cplx<doubl
 template <typename T>
 void launch_level1_combine(cudaStream_t s, int njobs, NodeMap m, const cplx<double>* st, double scale, Pool<T> D,
                            Pool<T> C, const L1Job* jobs) {
-    level1_combine_kernel<T><<<dim3(ceil_div(m.b, 32), ceil_div(m.b, 32), njobs), dim3(32, 8), 0, s>>>(
-        m, st, scale, D, C, jobs);
+    const size_t smem = level1_combine_smem<T>();
+    static bool attr = false;
+    if (!attr && cudaFuncSetAttribute(level1_combine_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem) == cudaSuccess)
+        attr = true;
+    level1_combine_kernel<T><<<dim3(ceil_div(m.b, 128), ceil_div(m.b, 32), njobs), 256, smem, s>>>(m, st, scale, D,
+                                                                                                  C, jobs);
 }
 void launch_perm_init(cudaStream_t s, int njobs, int* perm, int b) {
     perm_init_kernel<int><<<dim3(ceil_div(b, 256), njobs), 256, 0, s>>>(perm, b);
@@ -864,6 +1053,6 @@ void launch_mcopy(cudaStream_t s, int njobs, Pool<T> S, Pool<T> Dp, const int3* 
     template void launch_madd<T>(cudaStream_t, int, Pool<T>, const int3*);                                    \
     template void launch_mcopy<T>(cudaStream_t, int, Pool<T>, Pool<T>, const int3*);                         \
     template void launch_tri_inverse<T>(cudaStream_t, int, NodeMap, const cplx<double>*, double, Pool<T>,    \
-                                        const int*, unsigned*);
+                                        const int*, cplx<T>*, int*, unsigned*);
 INST(float)
 INST(double)

@@ -83,6 +83,8 @@ template <typename T> struct FactorStore {
     int vec_nrhs = 0;
     int* perm = nullptr;
     int* rowsrc = nullptr;      // per-panel composed row exchanges
+    cplx<T>* trifac = nullptr;  // first-step tridiagonal factors (8*b per node)
+    int* tripiv = nullptr;      // and their interchanges (b per node)
     bool tc_ok = false;
     TcMaps tc;       // TMA descriptors (FP32 only)
 };
@@ -502,6 +504,11 @@ template <typename T> int alloc_factor(fdfd_handle* h) {
     for (int e = 1; e < (int)h->sj.size(); ++e)
         if (e >= 2 || h->level1_gj) gj_max = std::max(gj_max, h->sj[e].ne);
     RET(alloc_pool<T>(h, F.Tg, b, b, ld, 2, gj_max));
+    if (h->sj.size() > 1 && !h->level1_gj) {
+        const size_t n1 = (size_t)std::max(1, h->sj[1].ne);
+        RET(dev_alloc(h, (void**)&F.trifac, n1 * 8 * b * sizeof(cplx<T>)));
+        RET(dev_alloc(h, (void**)&F.tripiv, n1 * b * sizeof(int)));
+    }
     if (sizeof(T) == 4 && h->use_tc) {
         F.tc_ok = tc_make_maps(reinterpret_cast<Pool<float>*>(&F.D), reinterpret_cast<Pool<float>*>(&F.C),
                                reinterpret_cast<Pool<float>*>(&F.X), reinterpret_cast<Pool<float>*>(&F.GP),
@@ -636,9 +643,10 @@ template <typename T> int factor_impl(fdfd_handle* h) {
                 flops += 8.0 * b3 * ne;
             } else {
                 int ev = prof_begin(h);
-                launch_tri_inverse<T>(h->stream, ne, h->map, h->st, h->scale, F.D, J<int>(h, S.elim), h->derr);
-                prof_end(h, ev, FDFD_PROF_LEVEL1, (double)F.D.planes * sizeof(T) * b * b * ne);
-                h->launches++;
+                launch_tri_inverse<T>(h->stream, ne, h->map, h->st, h->scale, F.D, J<int>(h, S.elim), F.trifac,
+                                      F.tripiv, h->derr);
+                prof_end(h, ev, FDFD_PROF_LEVEL1, 2.0 * sizeof(T) * b * b * ne);
+                h->launches += 2;
                 RET(check_launch(h, "tri_inverse"));
             }
             // bytes: two inverses read (re, im), D written (re, im), both couplings written (all planes)
@@ -1663,7 +1671,7 @@ int debug_gemm_impl(int M, int N, int K, const double* A, const double* B, doubl
             int dev = 0, sms = 0;
             cudaGetDevice(&dev);
             cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-            const int bn = (use_tc == 64 || use_tc == 128 || use_tc == 256) ? use_tc : tc_pick_bn(M, N, 1, sms);
+            const int bn = (use_tc == 64 || use_tc == 128 || use_tc == 256) ? use_tc : tc_pick_bn(M, N, K, 1, sms);
             const int bi = bn == 256 ? 1 : (bn == 128 ? 0 : 2);
             if (rc == FDFD_OK) {
                 cudaEventRecord(e0);

@@ -493,9 +493,13 @@ int tc_gemm_launch_maps(const GemmArgs<float>* g, const int* c_trans_arr, const 
     }
 }
 
-int tc_pick_bn(int M, int N, int njobs, int num_sms) {
+int tc_pick_bn(int M, int N, int K, int njobs, int num_sms) {
     const long long mt = (M + BM - 1) / BM;
     auto tiles = [&](int bn) { return mt * ((N + bn - 1) / bn) * njobs; };
+    // A short-K product (the Gauss-Jordan rank-panel update) is bound by its
+    // β read and C write: 64-column tiles let two CTAs share an SM, so one
+    // CTA's MMAs overlap the other's epilogue.
+    if (K <= 32) return 64;
     if (tiles(256) >= num_sms) return 256;
     if (tiles(128) >= num_sms) return 128;
     return 64;

@@ -25,12 +25,13 @@ bool tc_make_maps(const Pool<float>* D, const Pool<float>* C, const Pool<float>*
 int tc_gemm_launch_maps(const GemmArgs<float>* g, const int* c_trans_arr, const CUtensorMap* mapA,
                         const CUtensorMap* mapB, int bn, int njobs, cudaStream_t stream);
 
-// Widest tile (256, 128 or 64 columns) whose tile count still covers num_sms.
-int tc_pick_bn(int M, int N, int njobs, int num_sms);
+// Tile width for a launch: 64 columns for short-K products (K <= 32), else the
+// widest tile (256, 128 or 64 columns) whose tile count still covers num_sms.
+int tc_pick_bn(int M, int N, int K, int njobs, int num_sms);
 
 inline int tc_gemm_launch(const GemmArgs<float>* g, const int* c_trans_arr, int pa, int pb, int njobs,
                           const TcMaps* maps, int num_sms, cudaStream_t stream) {
-    const int bn = tc_pick_bn(g->M, g->N, njobs, num_sms);
+    const int bn = tc_pick_bn(g->M, g->N, g->K, njobs, num_sms);
     const int bi = bn == 256 ? 1 : (bn == 128 ? 0 : 2);
     return tc_gemm_launch_maps(g, c_trans_arr, &maps->map[pa][0], &maps->map[pb][bi], bn, njobs, stream);
 }

@@ -65,10 +65,11 @@ template <typename T>
 void launch_level1_combine(cudaStream_t s, int njobs, NodeMap m, const cplx<double>* st, double scale, Pool<T> D,
                            Pool<T> C, const L1Job* jobs);
 void launch_perm_init(cudaStream_t s, int njobs, int* perm, int b);
-// D[node] = (cyclic tridiagonal block of node)⁻¹ in O(b²) (first reduction step)
+// D[node] = (cyclic tridiagonal block of node)⁻¹ in O(b²) (first reduction step);
+// fac: 8*b cplx<T> and piv: b ints of workspace per job
 template <typename T>
 void launch_tri_inverse(cudaStream_t s, int njobs, NodeMap m, const cplx<double>* st, double scale, Pool<T> D,
-                        const int* nodes, unsigned* err);
+                        const int* nodes, cplx<T>* fac, int* piv, unsigned* err);
 // Gauss-Jordan panel step with panel width nb on the matrices M[slots[job]]
 // (returns a cudaError_t value).  Writes the panel transformation to GP, the
 // transposed pivot rows to RP, updates perm and writes rowsrc[job][r], the
