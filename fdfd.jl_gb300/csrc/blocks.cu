@@ -69,7 +69,7 @@ template <typename T>
 constexpr size_t level1_combine_smem() { return (size_t)2 * 2 * 128 * 33 * sizeof(T); }
 
 template <typename T>
-__global__ void __launch_bounds__(256) level1_combine_kernel(NodeMap m, const cplx<double>* st, double scale,
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) level1_combine_kernel(NodeMap m, const cplx<double>* st, double scale,
                                                              Pool<T> D, Pool<T> C, const L1Job* jobs) {
     constexpr int CPL = 4;                    // columns per lane
     constexpr int VW = 16 / sizeof(T);
@@ -84,12 +84,13 @@ __global__ void __launch_bounds__(256) level1_combine_kernel(NodeMap m, const cp
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int cl0 = lane * CPL;              // first tile column of this lane
     const int cb0 = c0 + cl0;                // its matrix column
-    const T* Gp = D.slot(J.prev);
-    const T* Gn = D.slot(J.next);
+    // distinct slots: no element is reached through two of these pointers
+    const T* __restrict__ Gp = D.slot(J.prev);
+    const T* __restrict__ Gn = D.slot(J.next);
     const long long pe = D.plane_elems();
-    T* Ds = D.slot(J.s);
-    T* Us = C.slot(J.u_slot);
-    T* Ls = C.slot(J.l_slot);
+    T* __restrict__ Ds = D.slot(J.s);
+    T* __restrict__ Us = C.slot(J.u_slot);
+    T* __restrict__ Ls = C.slot(J.l_slot);
     const long long cpe = C.plane_elems();
     // stencil values are FP64; the arithmetic runs in the factor precision T
     auto tv = [&](cplx<double> v) { return cmk((T)(v.re * scale), (T)(v.im * scale)); };
@@ -111,6 +112,7 @@ __global__ void __launch_bounds__(256) level1_combine_kernel(NodeMap m, const cp
         }
     }
     const bool full = cb0 + CPL <= b;        // all four columns inside the matrix
+#pragma unroll
     for (int q = 0; q < 4; ++q) {
         const int rl = warp + 8 * q;
         const int r = r0 + rl;
@@ -120,6 +122,12 @@ __global__ void __launch_bounds__(256) level1_combine_kernel(NodeMap m, const cp
         }
         const cplx<T> ls = tv(st_at<T>(st, m, m.p_cprev(), J.s, r));
         const cplx<T> us = tv(st_at<T>(st, m, m.p_cnext(), J.s, r));
+        // the cyclic tridiagonal row of D_s: three entries, converted once per row
+        // (b >= 3, so no two of them share a column)
+        const cplx<T> t_d = tv(st_at<T>(st, m, 0, J.s, r));
+        const cplx<T> t_l = tv(st_at<T>(st, m, m.p_inprev(), J.s, r));
+        const cplx<T> t_u = tv(st_at<T>(st, m, m.p_innext(), J.s, r));
+        const int c_l = r == 0 ? b - 1 : r - 1, c_u = r == b - 1 ? 0 : r + 1;
         T gpr[CPL], gpi[CPL], gnr[CPL], gni[CPL];
         const long long o = (long long)r * D.ld + cb0;   // cb0 < b <= ld, cb0 % 4 == 0: vectors stay in the row
 #pragma unroll
@@ -145,11 +153,8 @@ __global__ void __launch_bounds__(256) level1_combine_kernel(NodeMap m, const cp
 #pragma unroll
         for (int e = 0; e < CPL; ++e) {
             const int c = cb0 + e;
-            cplx<double> tri = cmk(0.0, 0.0);
-            if (c == r) tri = st_at<T>(st, m, 0, J.s, r);
-            if (c == (r + b - 1) % b) tri = cadd(tri, st_at<T>(st, m, m.p_inprev(), J.s, r));
-            if (c == (r + 1) % b) tri = cadd(tri, st_at<T>(st, m, m.p_innext(), J.s, r));
-            cplx<T> dv = tv(tri), uv = z, lv = z;
+            cplx<T> dv = c == r ? t_d : (c == c_l ? t_l : (c == c_u ? t_u : z));
+            cplx<T> uv = z, lv = z;
             if (J.prev_elim) {
                 const cplx<T> lg = cmul(ls, cmk(gpr[e], gpi[e]));
                 dv = csub(dv, cmul(lg, ucp[e]));
