@@ -17,16 +17,11 @@ __device__ __forceinline__ cplx<double> st_at(const cplx<double>* st, const Node
 }
 
 template <typename T>
-__device__ __forceinline__ void store_elem(const Pool<T>& P, T* base, int r, int c, cplx<T> v, int trans,
-                                           bool lo = true) {
+__device__ __forceinline__ void store_elem(const Pool<T>& P, T* base, int r, int c, cplx<T> v, int trans) {
     long long off = trans ? (long long)c * P.ld + r : (long long)r * P.ld + c;
     long long pe = P.plane_elems();
     base[off] = v.re;
     base[pe + off] = v.im;
-    if (lo && P.planes == 4) {
-        base[2 * pe + off] = (T)tf32_lo((float)v.re);
-        base[3 * pe + off] = (T)tf32_lo((float)v.im);
-    }
 }
 
 // ---------------------------------------------------------------------------
@@ -171,26 +166,19 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) level1_combine_ke
             }
             dr[e] = dv.re; di[e] = dv.im; ur[e] = uv.re; ui[e] = uv.im; lr[e] = lv.re; li[e] = lv.im;
         }
-        // D_s: re/im only (read as re/im until its inversion writes all planes)
-        auto put_row = [&](T* base, long long ppe, const T* xr, const T* xi, bool lo) {
+        auto put_row = [&](T* base, long long ppe, const T* xr, const T* xi) {
             const long long ob = (long long)r * C.ld + cb0;
             if (full) {
 #pragma unroll
                 for (int v = 0; v < NVL; ++v) {
-                    VT a, c, al, cl;
+                    VT a, c;
 #pragma unroll
                     for (int e = 0; e < VW; ++e) {
                         reinterpret_cast<T*>(&a)[e] = xr[v * VW + e];
                         reinterpret_cast<T*>(&c)[e] = xi[v * VW + e];
-                        reinterpret_cast<T*>(&al)[e] = (T)tf32_lo((float)xr[v * VW + e]);
-                        reinterpret_cast<T*>(&cl)[e] = (T)tf32_lo((float)xi[v * VW + e]);
                     }
                     reinterpret_cast<VT*>(base + ob)[v] = a;
                     reinterpret_cast<VT*>(base + ppe + ob)[v] = c;
-                    if (lo) {
-                        reinterpret_cast<VT*>(base + 2 * ppe + ob)[v] = al;
-                        reinterpret_cast<VT*>(base + 3 * ppe + ob)[v] = cl;
-                    }
                 }
             } else {
 #pragma unroll
@@ -198,17 +186,12 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) level1_combine_ke
                     if (cb0 + e < b) {
                         base[ob + e] = xr[e];
                         base[ppe + ob + e] = xi[e];
-                        if (lo) {
-                            base[2 * ppe + ob + e] = (T)tf32_lo((float)xr[e]);
-                            base[3 * ppe + ob + e] = (T)tf32_lo((float)xi[e]);
-                        }
                     }
                 }
             }
         };
-        put_row(Ds, pe, dr, di, false);
-        const bool clo = C.planes == 4;
-        if (!J.u_trans) put_row(Us, cpe, ur, ui, clo);
+        put_row(Ds, pe, dr, di);
+        if (!J.u_trans) put_row(Us, cpe, ur, ui);
         else {
 #pragma unroll
             for (int e = 0; e < CPL; ++e) {
@@ -216,7 +199,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) level1_combine_ke
                 tU[128 * 33 + (cl0 + e) * 33 + rl] = ui[e];
             }
         }
-        if (!J.l_trans) put_row(Ls, cpe, lr, li, clo);
+        if (!J.l_trans) put_row(Ls, cpe, lr, li);
         else {
 #pragma unroll
             for (int e = 0; e < CPL; ++e) {
@@ -504,7 +487,7 @@ __global__ void __launch_bounds__(512, 1) gj_panel_kernel(Pool<T> M, const int* 
         }
     }
 
-    // 1. G panel (b x GP.cols, zero padded) with its TF32 residual planes.  Rows
+    // 1. G panel (b x GP.cols, zero padded).  Rows
     //    are staged by logical row, 128 at a time, in shared memory (row stride
     //    NB+4 keeps 16-byte accesses conflict-free) and written as whole 16-byte
     //    vectors of consecutive columns, so each warp store covers full rows.
@@ -538,20 +521,21 @@ __global__ void __launch_bounds__(512, 1) gj_panel_kernel(Pool<T> M, const int* 
             const int nr = min(128, b - ch);
             for (int idx = tid; idx < nr * gv; idx += NT) {
                 const int rl = idx / gv, v = idx % gv;
-                VT a = {}, c = {}, al, cl;
+                VT a = {}, c = {};
                 if (v < NB / VW) {
                     a = reinterpret_cast<const VT*>(buf + (size_t)rl * SR)[v];
                     c = reinterpret_cast<const VT*>(buf + (size_t)128 * SR + (size_t)rl * SR)[v];
                 }
-#pragma unroll
-                for (int e = 0; e < VW; ++e) {
-                    reinterpret_cast<T*>(&al)[e] = (T)tf32_lo((float)reinterpret_cast<const T*>(&a)[e]);
-                    reinterpret_cast<T*>(&cl)[e] = (T)tf32_lo((float)reinterpret_cast<const T*>(&c)[e]);
-                }
                 const long long o = (long long)(ch + rl) * GP.ld + v * VW;
                 *reinterpret_cast<VT*>(gp + o) = a;
                 *reinterpret_cast<VT*>(gp + pe + o) = c;
-                if (GP.planes == 4) {
+                if (GP.planes == 4) {   // pre-split tensor-core operand: TF32 residual planes
+                    VT al, cl;
+#pragma unroll
+                    for (int e = 0; e < VW; ++e) {
+                        reinterpret_cast<T*>(&al)[e] = (T)tf32_lo((float)reinterpret_cast<const T*>(&a)[e]);
+                        reinterpret_cast<T*>(&cl)[e] = (T)tf32_lo((float)reinterpret_cast<const T*>(&c)[e]);
+                    }
                     *reinterpret_cast<VT*>(gp + 2 * pe + o) = al;
                     *reinterpret_cast<VT*>(gp + 3 * pe + o) = cl;
                 }
@@ -627,7 +611,7 @@ __global__ void __launch_bounds__(512, 1) gj_panel_kernel(Pool<T> M, const int* 
                 const long long o = (long long)(cb + c) * RP.ld + k;
                 rt[o] = a;
                 rt[pe + o] = d;
-                if (RP.planes == 4) {
+                if (RP.planes == 4) {   // pre-split tensor-core operand
                     rt[2 * pe + o] = (T)tf32_lo((float)a);
                     rt[3 * pe + o] = (T)tf32_lo((float)d);
                 }
@@ -637,8 +621,8 @@ __global__ void __launch_bounds__(512, 1) gj_panel_kernel(Pool<T> M, const int* 
     }
 }
 
-// Dst[r][perm[j]] = Src[r][j] per row (through shared memory, so Src may be Dst);
-// writes the TF32 residual planes.  grid: (ceil(b/8), njobs), block 256
+// Dst[r][perm[j]] = Src[r][j] per row (through shared memory, so Src may be Dst).
+// grid: (ceil(b/8), njobs), block 256
 template <typename T>
 __global__ void gj_unpermute_kernel(Pool<T> Src, const int* sslots, Pool<T> Dst, const int* dslots,
                                     const int* perm) {
@@ -930,8 +914,7 @@ __global__ void __launch_bounds__(128) tri_columns_kernel(int b, Pool<T> D, cons
     // backward: x = U⁻¹ y, each finished row corrected and written with all planes
     auto put = [&](int r, cplx<T> x) {
         const cplx<T> g = csub(csub(x, cmul(s_z0[r], w0)), cmul(s_zN[r], w1));
-        // re/im only: first-step inverses are read by the combine and the sweeps, never as GEMM operands
-        store_elem<T>(D, Gre, r, j, g, 0, false);
+        store_elem<T>(D, Gre, r, j, g, 0);
     };
     cplx<T> x1 = cmul(cur, s_dinv[b - 1]);     // x[b-1]
     put(b - 1, x1);

@@ -55,8 +55,9 @@ __device__ __forceinline__ float tf32_lo(float x) {
 // ---- block pools -----------------------------------------------------------
 // A pool holds `count` complex matrices of `rows` x `cols` (row-major, leading
 // dimension `ld`).  Each slot stores `planes` real planes of rows*ld values:
-// plane 0 = real part, 1 = imaginary part and, for FP32 pools, 2/3 = the
-// TF32 residuals (lo) of planes 0/1 used by the 3xTF32 tensor-core products.
+// plane 0 = real part, 1 = imaginary part and, for the FP32 Gauss-Jordan panel
+// buffers only, 2/3 = the TF32 residuals (lo) of planes 0/1 (pre-split
+// tensor-core operands).
 template <typename T> struct Pool {
     T* base = nullptr;
     int rows = 0, cols = 0, ld = 0, planes = 2;

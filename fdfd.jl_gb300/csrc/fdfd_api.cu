@@ -489,13 +489,15 @@ template <typename T> int alloc_factor(fdfd_handle* h) {
     FactorStore<T>& F = store<T>(h);
     if (F.D.base) return FDFD_OK;
     const int b = h->map.b, n = h->map.n, ld = h->map.ld;
-    const int planes = sizeof(T) == 4 ? 4 : 2;
+    const int planes = 2;   // re, im (the tensor-core GEMM forms the TF32 residuals itself)
     const int pc = sizeof(T) == 4 ? 32 : panel_nb<T>(b);
     RET(alloc_pool<T>(h, F.D, b, b, ld, planes, n));
     RET(alloc_pool<T>(h, F.C, b, b, ld, planes, h->nCslots));
     RET(alloc_pool<T>(h, F.X, b, b, ld, planes, h->nXslots));
-    RET(alloc_pool<T>(h, F.GP, b, pc, pc, planes, h->max_ne));
-    RET(alloc_pool<T>(h, F.RP, b, pc, pc, planes, h->max_ne));
+    // the panel buffers are short-K tensor-core operands: stored pre-split (re, im, re_lo, im_lo)
+    const int pplanes = sizeof(T) == 4 ? 4 : 2;
+    RET(alloc_pool<T>(h, F.GP, b, pc, pc, pplanes, h->max_ne));
+    RET(alloc_pool<T>(h, F.RP, b, pc, pc, pplanes, h->max_ne));
     RET(dev_alloc(h, (void**)&F.perm, (size_t)h->max_ne * b * sizeof(int)));
     RET(dev_alloc(h, (void**)&F.rowsrc, (size_t)h->max_ne * b * sizeof(int)));
     // largest Gauss-Jordan batch: the eliminated nodes of steps >= 2 (and of step 1
@@ -552,7 +554,7 @@ template <typename T> Pool<T>& pool_of(FactorStore<T>& F, int id) {
 template <typename T>
 int gemm(fdfd_handle* h, int pa, int pb, int pc, const int* a_slot, const int* b_slot, const int* c_slot,
          const int* c_trans_arr, int c_trans, int njobs, int M, int N, int K, T alpha, int beta, int mask_c0,
-         int mask_w, int write_lo = 1, int pcin = -1, const int* cin_slot = nullptr,
+         int mask_w, int pcin = -1, const int* cin_slot = nullptr,
          const int* row_src = nullptr, int prof_cls = -1, double prof_work = 0.0) {
     if (njobs == 0) return FDFD_OK;
     FactorStore<T>& F = store<T>(h);
@@ -564,7 +566,6 @@ int gemm(fdfd_handle* h, int pa, int pb, int pc, const int* a_slot, const int* b
     g.M = M; g.N = N; g.K = K; g.alpha = alpha; g.beta = beta;
     g.mask_c0 = mask_c0; g.mask_w = mask_w; g.c_trans = c_trans;
     g.c_trans_arr = nullptr;
-    g.write_lo = write_lo;
     g.err = h->derr;
     const double flops = 8.0 * M * N * K * njobs;
     int ev = prof_begin(h);
@@ -609,9 +610,8 @@ template <typename T> int gj_invert(fdfd_handle* h, const int* d_slots, const in
         prof_end(h, ev, FDFD_PROF_GJ_PANEL, 0.0);
         h->launches++;
         if (e) return set_err(h, FDFD_ECUDA, "gj_panel launch failed: %s", cudaGetErrorString((cudaError_t)e));
-        // no residual planes here: gj_unpermute_kernel rewrites every element of the inverse
         RET(gemm<T>(h, P_GP, P_RP, alt, d_iota, d_iota, alt_slots, nullptr, 0, njobs, b, b, F.GP.cols, (T)1, 1,
-                    c0, w, 0, cur, cur_slots, F.rowsrc, FDFD_PROF_GJ_UPDATE,
+                    c0, w, cur, cur_slots, F.rowsrc, FDFD_PROF_GJ_UPDATE,
                     4.0 * sizeof(T) * (double)b * b * njobs));
         std::swap(cur, alt);
         std::swap(cur_slots, alt_slots);
@@ -660,12 +660,11 @@ template <typename T> int factor_impl(fdfd_handle* h) {
             // Xᵀ = [Lᵀ; Uᵀ] Gᵀ
             RET(gemm<T>(h, P_C, P_D, P_X, J<int>(h, S.xt_a), J<int>(h, S.xt_b), J<int>(h, S.xt_c), nullptr, 0,
                         2 * ne, b, b, b, (T)1, 0, 0, 0));
-            // D_p -= U_p X_L ; D_q -= L_q X_R.  No residual planes: a D block is only
-            // read as re/im until its inversion writes G with all planes.
+            // D_p -= U_p X_L ; D_q -= L_q X_R
             RET(gemm<T>(h, P_C, P_X, P_D, J<int>(h, S.dp_a), J<int>(h, S.dp_b), J<int>(h, S.dp_c), nullptr, 0,
-                        ne, b, b, b, (T)-1, 1, 0, 0, 0));
+                        ne, b, b, b, (T)-1, 1, 0, 0));
             RET(gemm<T>(h, P_C, P_X, P_D, J<int>(h, S.dq_a), J<int>(h, S.dq_b), J<int>(h, S.dq_c), nullptr, 0,
-                        ne, b, b, b, (T)-1, 1, 0, 0, 0));
+                        ne, b, b, b, (T)-1, 1, 0, 0));
             // new couplings U_p' = -U_p X_R, L_q' = -L_q X_L (storage form per node)
             RET(gemm<T>(h, P_C, P_X, P_C, J<int>(h, S.cp_a), J<int>(h, S.cp_b), J<int>(h, S.cp_c),
                         J<int>(h, S.cp_t), 0, S.ncp, b, b, b, (T)-1, 0, 0, 0));
@@ -685,7 +684,7 @@ template <typename T> int factor_impl(fdfd_handle* h) {
     RET(gemm<T>(h, P_C, P_D, P_X, J<int>(h, h->fin_xt_a), J<int>(h, h->fin_xt_b), J<int>(h, h->fin_xt_c), nullptr,
                 0, 1, b, b, b, (T)1, 0, 0, 0));
     RET(gemm<T>(h, P_C, P_X, P_D, J<int>(h, h->fin_da_a), J<int>(h, h->fin_da_b), J<int>(h, h->fin_da_c), nullptr,
-                0, 1, b, b, b, (T)-1, 1, 0, 0, 0));
+                0, 1, b, b, b, (T)-1, 1, 0, 0));
     RET(gj_invert<T>(h, J<int>(h, h->fin_a_slot), J<int>(h, h->fin_iota), 1));
     flops += 8.0 * b3 * 4;
     h->last_factor_flops = flops;
@@ -1610,12 +1609,14 @@ namespace {
 
 template <typename T>
 int debug_gemm_impl(int M, int N, int K, const double* A, const double* B, double* C, int use_tc, double* ms) {
-    const int planes = sizeof(T) == 4 ? 4 : 2;
+    // use_tc < 0: the operands as pre-split four-plane pools (the panel-buffer form)
+    const int planes = (sizeof(T) == 4 && use_tc < 0) ? 4 : 2;
+    use_tc = use_tc < 0 ? -use_tc : use_tc;
     Pool<T> PA, PB, PC;
-    auto setp = [&](Pool<T>& P, int rows, int cols) {
-        P.rows = rows; P.cols = cols; P.ld = (cols + 31) / 32 * 32; P.planes = planes; P.count = 1;
+    auto setp = [&](Pool<T>& P, int rows, int cols, int np) {
+        P.rows = rows; P.cols = cols; P.ld = (cols + 31) / 32 * 32; P.planes = np; P.count = 1;
     };
-    setp(PA, M, K); setp(PB, N, K); setp(PC, M, N);
+    setp(PA, M, K, planes); setp(PB, N, K, planes); setp(PC, M, N, 2);
     auto upload = [&](Pool<T>& P, const double* src) -> int {
         std::vector<T> host((size_t)P.slot_elems(), (T)0);
         long long pe = P.plane_elems();
@@ -1625,7 +1626,7 @@ int debug_gemm_impl(int M, int N, int K, const double* A, const double* B, doubl
                 size_t o = (size_t)r * P.ld + c;
                 host[o] = (T)re;
                 host[pe + o] = (T)im;
-                if (planes == 4) {
+                if (P.planes == 4) {   // TF32 residuals: x minus x with the low 13 mantissa bits cleared
                     float fr = (float)re, fi = (float)im;
                     uint32_t ur, ui;
                     memcpy(&ur, &fr, 4); memcpy(&ui, &fi, 4);
@@ -1659,7 +1660,7 @@ int debug_gemm_impl(int M, int N, int K, const double* A, const double* B, doubl
         g.a_slot = g.b_slot = g.c_slot = slots;
         g.Cin = Pool<T>(); g.cin_slot = nullptr; g.row_src = nullptr;
         g.M = M; g.N = N; g.K = K; g.alpha = (T)1; g.beta = 0; g.mask_c0 = 0; g.mask_w = 0;
-        g.c_trans = 0; g.c_trans_arr = nullptr; g.write_lo = 1; g.err = derr;
+        g.c_trans = 0; g.c_trans_arr = nullptr; g.err = derr;
         cudaEvent_t e0, e1;
         cudaEventCreate(&e0); cudaEventCreate(&e1);
         if (sizeof(T) == 4 && use_tc) {

@@ -91,10 +91,6 @@ __global__ void __launch_bounds__(256) gemm_simt_kernel(GemmArgs<T> g) {
             }
             C[off] = vr;
             C[cpe + off] = vi;
-            if (g.C.planes == 4 && g.write_lo) {
-                C[2 * cpe + off] = (T)tf32_lo((float)vr);
-                C[3 * cpe + off] = (T)tf32_lo((float)vi);
-            }
         }
     }
 }

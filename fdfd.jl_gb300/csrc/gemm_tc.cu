@@ -3,13 +3,17 @@
 //
 //   C[m][n] = beta(m,n)·Cin[src(m)][n] + alpha·Σ_k A[m][k]·B[n][k]      (complex)
 //
-// Operands are FP32 planar pools whose slots hold four planes: re, im and
-// their TF32 residuals lo = x - (x with the low 13 mantissa bits cleared).
-// The tensor core reads only the top 19 bits of an FP32 operand, so the raw
-// plane serves as the "hi" term and
+// Operands are FP32 planar pools.  The tensor core reads only the top 19 bits
+// of an FP32 operand, so the raw plane serves as the "hi" term; with the TF32
+// residual lo = x - (x with the low 13 mantissa bits cleared)
 //   a·b ≈ hi(a)·hi(b) + hi(a)·lo(b) + lo(a)·hi(b)
 // recovers close to FP32 accuracy (the split of Markidis et al., 2018, as used
-// for 3xTF32 GEMMs).  Each complex product is four real products (the im·im
+// for 3xTF32 GEMMs).  Two operand forms: pools of two planes (re, im; the
+// factor blocks), whose lo planes are formed in shared memory as each stage
+// lands, so TMA moves half the bytes; and pools of four planes (re, im, re_lo,
+// im_lo; the small Gauss-Jordan panel buffers), loaded pre-split so that a
+// short-K product has no conversion on its critical path.  A and B of one
+// launch have the same form.  Each complex product is four real products (the im·im
 // term through the instruction's negate-A bit), so one K-step issues 12 MMAs
 // into two TMEM accumulators (real and imaginary, BN columns each).
 //
@@ -17,9 +21,11 @@
 // the widest tile that still fills the GPU, so small batches get more CTAs),
 // K-step 8 (one 32-byte swizzle row per operand row), 4-stage TMA pipeline,
 // 192 threads:
-//   warp 0      TMA producer (one elected lane)
+//   warp 0      TMA producer (one elected lane): the planes of A and B
 //   warp 1      TMEM allocator and MMA issuer (one elected lane)
-//   warps 2..5  epilogue: tcgen05.ld -> registers -> global (N- or T-form)
+//   warps 2..5  during the K loop (two-plane operands): write the lo planes of
+//               each landed stage (bar_full -> bar_conv); then the epilogue:
+//               tcgen05.ld -> registers -> global (N- or T-form)
 // Every mbarrier wait is bounded (2 s of %globaltimer); on timeout the CTA sets
 // FDFD_DEVERR_TIMEOUT, drains its own TMA copies (bounded), frees TMEM and exits.
 #include "gemm_tc.cuh"
@@ -142,7 +148,7 @@ __global__ void __launch_bounds__(192, BN <= 64 ? 2 : 1)
     constexpr int STAGE_BYTES = TcTile<BN>::STAGE_BYTES;
     constexpr uint32_t TMEM_COLS = TcTile<BN>::TMEM_COLS;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
-    __shared__ __align__(8) uint64_t bar_full[STAGES], bar_empty[STAGES], bar_acc;
+    __shared__ __align__(8) uint64_t bar_full[STAGES], bar_conv[STAGES], bar_empty[STAGES], bar_acc;
     __shared__ uint32_t tmem_base_slot;
     __shared__ int s_abort;
 
@@ -151,6 +157,8 @@ __global__ void __launch_bounds__(192, BN <= 64 ? 2 : 1)
     const int job = blockIdx.z;
     const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
     const int nk = (g.K + BK - 1) / BK;
+    const bool presplit = g.A.planes == 4;             // operand form (A and B alike)
+    const int np = presplit ? 4 : 2;                   // planes loaded by TMA
     unsigned char* smem = reinterpret_cast<unsigned char*>(
         (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
     const uint32_t sbase = smem_u32(smem);
@@ -158,6 +166,7 @@ __global__ void __launch_bounds__(192, BN <= 64 ? 2 : 1)
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; ++s) {
             mbar_init(smem_u32(&bar_full[s]), 1);
+            mbar_init(smem_u32(&bar_conv[s]), 128);   // the 128 converter threads
             mbar_init(smem_u32(&bar_empty[s]), 1);
         }
         mbar_init(smem_u32(&bar_acc), 1);
@@ -187,13 +196,13 @@ __global__ void __launch_bounds__(192, BN <= 64 ? 2 : 1)
                     if (!mbar_wait(smem_u32(&bar_empty[s]), ((kt / STAGES) - 1) & 1)) { ok = false; break; }
                 }
                 const uint32_t bar = smem_u32(&bar_full[s]);
-                mbar_expect_tx(bar, STAGE_BYTES);
+                mbar_expect_tx(bar, np * (A_PLANE_BYTES + B_PLANE_BYTES));
                 const uint32_t st = sbase + s * STAGE_BYTES;
                 const int k0 = kt * BK;
-                for (int p = 0; p < 4; ++p)
-                    tma_load_3d(st + p * A_PLANE_BYTES, &mapA, k0, m0, aslot * 4 + p, bar);
-                for (int p = 0; p < 4; ++p)
-                    tma_load_3d(st + 4 * A_PLANE_BYTES + p * B_PLANE_BYTES, &mapB, k0, n0, bslot * 4 + p, bar);
+                for (int p = 0; p < np; ++p)
+                    tma_load_3d(st + p * A_PLANE_BYTES, &mapA, k0, m0, aslot * np + p, bar);
+                for (int p = 0; p < np; ++p)
+                    tma_load_3d(st + 4 * A_PLANE_BYTES + p * B_PLANE_BYTES, &mapB, k0, n0, bslot * np + p, bar);
                 issued = kt + 1;
             }
             if (!ok) {
@@ -214,7 +223,10 @@ __global__ void __launch_bounds__(192, BN <= 64 ? 2 : 1)
             const uint32_t id_pos = idesc_tf32(BM, BN, 0), id_neg = idesc_tf32(BM, BN, 1);
             for (int kt = 0; kt < nk; ++kt) {
                 const int s = kt % STAGES;
-                if (!mbar_wait(smem_u32(&bar_full[s]), (kt / STAGES) & 1)) { ok = false; break; }
+                if (!mbar_wait(smem_u32(presplit ? &bar_full[s] : &bar_conv[s]), (kt / STAGES) & 1)) {
+                    ok = false;
+                    break;
+                }
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                 const uint32_t st = sbase + s * STAGE_BYTES;
                 uint64_t a[4], b[4];
@@ -265,6 +277,35 @@ __global__ void __launch_bounds__(192, BN <= 64 ? 2 : 1)
                 l2_prefetch(src + cipe, (uint32_t)ncols * 4u);
             }
         }
+        // warps 2..5: first the TF32 residual planes of every landed stage
+        // (two-plane operands).  The lo planes have the layout of the raw
+        // planes, so the split is elementwise at equal offsets, whatever the swizzle.
+        if (!presplit) {
+            const int ct = threadIdx.x - 64;                    // 0..127
+            constexpr int NV4 = (2 * A_PLANE_BYTES + 2 * B_PLANE_BYTES) / 16;   // float4s per stage
+            bool okc = true;
+            for (int kt = 0; kt < nk; ++kt) {
+                const int s = kt % STAGES;
+                if (*(volatile int*)&s_abort) { okc = false; break; }
+                if (!mbar_wait(smem_u32(&bar_full[s]), (kt / STAGES) & 1)) { okc = false; break; }
+                unsigned char* st = smem + s * STAGE_BYTES;
+                for (int v = ct; v < NV4; v += 128) {
+                    // A re, A im | B re, B im; each lo plane sits two planes after its raw plane
+                    const int off = v < 2 * A_PLANE_BYTES / 16 ? v * 16 : 4 * A_PLANE_BYTES + (v * 16 - 2 * A_PLANE_BYTES);
+                    const int lo_off = off + (v < 2 * A_PLANE_BYTES / 16 ? 2 * A_PLANE_BYTES : 2 * B_PLANE_BYTES);
+                    const float4 x = *reinterpret_cast<const float4*>(st + off);
+                    *reinterpret_cast<float4*>(st + lo_off) = make_float4(tf32_lo(x.x), tf32_lo(x.y), tf32_lo(x.z),
+                                                                          tf32_lo(x.w));
+                }
+                // make the generic-proxy stores visible to the tensor core (async proxy)
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&bar_conv[s])) : "memory");
+            }
+            if (!okc) {
+                dev_error(g.err, FDFD_DEVERR_TIMEOUT);
+                atomicExch(&s_abort, 1);
+            }
+        }
         const bool ok_l = mbar_wait(smem_u32(&bar_acc), 0);
         const bool ok = __all_sync(0xffffffffu, ok_l);
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -313,10 +354,6 @@ __global__ void __launch_bounds__(192, BN <= 64 ? 2 : 1)
                             const long long off = (long long)n * ld + row;
                             C[off] = xr;
                             C[pe + off] = xi;
-                            if (g.write_lo) {
-                                C[2 * pe + off] = tf32_lo(xr);
-                                C[3 * pe + off] = tf32_lo(xi);
-                            }
                         }
                     }
                 } else {
@@ -370,33 +407,23 @@ __global__ void __launch_bounds__(192, BN <= 64 ? 2 : 1)
                         const float* sip = reinterpret_cast<const float*>(&si);
                         const float* crp = reinterpret_cast<const float*>(&cre[it]);
                         const float* cip = reinterpret_cast<const float*>(&cim[it]);
-                        float xr[4], xi[4], lr[4], li[4];
+                        float xr[4], xi[4];
 #pragma unroll
                         for (int e = 0; e < 4; ++e) {
                             const int col = n + e;
                             const bool keep = g.beta && !(mrow || (col >= g.mask_c0 && col < g.mask_c0 + g.mask_w));
                             xr[e] = g.alpha * srp[e] + (keep ? crp[e] : 0.f);
                             xi[e] = g.alpha * sip[e] + (keep ? cip[e] : 0.f);
-                            lr[e] = tf32_lo(xr[e]);
-                            li[e] = tf32_lo(xi[e]);
                         }
                         const long long off = (long long)r * ld + n;
                         if (full4) {
                             *reinterpret_cast<float4*>(C + off) = make_float4(xr[0], xr[1], xr[2], xr[3]);
                             *reinterpret_cast<float4*>(C + pe + off) = make_float4(xi[0], xi[1], xi[2], xi[3]);
-                            if (g.write_lo) {
-                                *reinterpret_cast<float4*>(C + 2 * pe + off) = make_float4(lr[0], lr[1], lr[2], lr[3]);
-                                *reinterpret_cast<float4*>(C + 3 * pe + off) = make_float4(li[0], li[1], li[2], li[3]);
-                            }
                         } else {
                             for (int e = 0; e < 4; ++e)
                                 if (n + e < g.N) {
                                     C[off + e] = xr[e];
                                     C[pe + off + e] = xi[e];
-                                    if (g.write_lo) {
-                                        C[2 * pe + off + e] = lr[e];
-                                        C[3 * pe + off + e] = li[e];
-                                    }
                                 }
                         }
                     }
@@ -451,7 +478,7 @@ bool encode_pool(const Pool<float>& P, int box_rows, CUtensorMap* out) {
 }  // namespace
 
 bool tc_make_map(const Pool<float>& P, CUtensorMap* box128, CUtensorMap* box256, CUtensorMap* box64) {
-    if (P.planes != 4 || (P.ld % 4) != 0) return false;
+    if ((P.planes != 2 && P.planes != 4) || (P.ld % 4) != 0) return false;
     return encode_pool(P, 128, box128) && encode_pool(P, 256, box256) && encode_pool(P, 64, box64);
 }
 

@@ -77,14 +77,14 @@ void launch_tri_inverse(cudaStream_t s, int njobs, NodeMap m, const cplx<double>
 template <typename T>
 int launch_gj_panel(cudaStream_t s, int nb, int njobs, Pool<T> M, const int* slots, Pool<T> GP, Pool<T> RP,
                     int* perm, int* rowsrc, int c0, unsigned* err);
-// Dst[dslots[job]][r][perm[j]] = Src[sslots[job]][r][j] (Src may equal Dst); writes the TF32 residual planes
+// Dst[dslots[job]][r][perm[j]] = Src[sslots[job]][r][j] (Src may equal Dst)
 template <typename T>
 void launch_gj_unpermute(cudaStream_t s, int njobs, Pool<T> Src, const int* sslots, Pool<T> Dst,
                          const int* dslots, const int* perm);
-// C[dst] = A[s1] + A[s2] (same storage form); also writes lo planes
+// C[dst] = A[s1] + A[s2] (same storage form)
 template <typename T>
 void launch_madd(cudaStream_t s, int njobs, Pool<T> P, const int3* jobs);
-// dst = src (optionally transposed) between pools; writes lo planes
+// dst = src (optionally transposed) between pools
 template <typename T>
 void launch_mcopy(cudaStream_t s, int njobs, Pool<T> S, Pool<T> Dp, const int3* jobs);
 
@@ -106,7 +106,6 @@ template <typename T> struct GemmArgs {
     int mask_c0, mask_w;
     int c_trans;
     const int* c_trans_arr;   // per-job override of c_trans (device, may be null)
-    int write_lo;             // also write the TF32 residual planes of C (FP32 pools)
     unsigned* err;
 };
 template <typename T>
