@@ -20,12 +20,13 @@
 // CTA tile 128 x BN (complex outputs, BN = 256, 128 or 64: the launcher takes
 // the widest tile that still fills the GPU, so small batches get more CTAs),
 // K-step 8 (one 32-byte swizzle row per operand row), 4-stage TMA pipeline,
-// 192 threads:
+// 64 + 32*NEPI threads:
 //   warp 0      TMA producer (one elected lane): the planes of A and B
 //   warp 1      TMEM allocator and MMA issuer (one elected lane)
-//   warps 2..5  during the K loop (two-plane operands): write the lo planes of
+//   warps 2..    during the K loop (two-plane operands): write the lo planes of
 //               each landed stage (bar_full -> bar_conv); then the epilogue:
-//               tcgen05.ld -> registers -> global (N- or T-form)
+//               tcgen05.ld -> registers -> global (N- or T-form).  4 warps, or 8
+//               for BN >= 128 (two per TMEM lane quarter, one per column half)
 // Every mbarrier wait is bounded (2 s of %globaltimer); on timeout the CTA sets
 // FDFD_DEVERR_TIMEOUT, drains its own TMA copies (bounded), frees TMEM and exits.
 #include "gemm_tc.cuh"
@@ -35,12 +36,16 @@ namespace {
 constexpr int BM = 128, BK = 8, STAGES = 4;
 constexpr int A_PLANE_BYTES = BM * BK * 4;                  // 4 KB
 template <int BN> struct TcTile {
+    // epilogue warps: two per TMEM lane quarter (each takes half the columns),
+    // one at BN = 64 (two CTAs share an SM there)
+    static constexpr int NEPI = BN >= 128 ? 8 : 4;
+    static constexpr int THREADS = 64 + 32 * NEPI;
     static constexpr int B_PLANE_BYTES = BN * BK * 4;
     static constexpr int STAGE_BYTES = 4 * A_PLANE_BYTES + 4 * B_PLANE_BYTES;
     static constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024;   // + alignment slack
     static constexpr uint32_t TMEM_COLS = 2 * BN;                     // re and im accumulators
-    // the epilogue stages 4 warps x 2 x 32 x 36 floats in the idle pipeline buffers
-    static_assert(STAGES * STAGE_BYTES >= 4 * 2 * 32 * 36 * 4, "epilogue staging");
+    // the epilogue stages NEPI warps x 2 x 32 x 36 floats in the idle pipeline buffers
+    static_assert(STAGES * STAGE_BYTES >= NEPI * 2 * 32 * 36 * 4, "epilogue staging");
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -141,12 +146,13 @@ struct TcParams {
 };
 
 template <int BN>
-__global__ void __launch_bounds__(192, BN <= 64 ? 2 : 1)
+__global__ void __launch_bounds__(TcTile<BN>::THREADS, BN <= 64 ? 2 : 1)
     gemm_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
                    const TcParams P) {
     constexpr int B_PLANE_BYTES = TcTile<BN>::B_PLANE_BYTES;
     constexpr int STAGE_BYTES = TcTile<BN>::STAGE_BYTES;
     constexpr uint32_t TMEM_COLS = TcTile<BN>::TMEM_COLS;
+    constexpr int NEPI = TcTile<BN>::NEPI;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     __shared__ __align__(8) uint64_t bar_full[STAGES], bar_conv[STAGES], bar_empty[STAGES], bar_acc;
     __shared__ uint32_t tmem_base_slot;
@@ -166,7 +172,7 @@ __global__ void __launch_bounds__(192, BN <= 64 ? 2 : 1)
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; ++s) {
             mbar_init(smem_u32(&bar_full[s]), 1);
-            mbar_init(smem_u32(&bar_conv[s]), 128);   // the 128 converter threads
+            mbar_init(smem_u32(&bar_conv[s]), 32 * NEPI);   // every epilogue thread converts
             mbar_init(smem_u32(&bar_empty[s]), 1);
         }
         mbar_init(smem_u32(&bar_acc), 1);
@@ -259,6 +265,8 @@ __global__ void __launch_bounds__(192, BN <= 64 ? 2 : 1)
     } else {
         // epilogue warps 2..5; TMEM lane quarter = warp % 4
         const int q = warp & 3;
+        const int part = (warp - 2) >> 2;              // column part of this warp (NEPI / 4 parts)
+        constexpr int PARTS = NEPI / 4, PCOLS = BN / PARTS;
         // A short-K product (the Gauss-Jordan rank-panel update) is bound by its β read:
         // each lane pulls its β row (re, im) into L2 while the MMAs run.  Rows are
         // ld-padded, so the range [n0, min(n0 + BN, ld)) is 16-byte aligned and sized.
@@ -269,10 +277,11 @@ __global__ void __launch_bounds__(192, BN <= 64 ? 2 : 1)
             const int cild = sep ? g.Cin.ld : g.C.ld;
             const int* rsrc = (sep && g.row_src) ? g.row_src + (long long)job * g.M : nullptr;
             const int r = m0 + q * 32 + lane;
-            const int ncols = min(BN, cild - n0);
+            const int nlo = n0 + part * PCOLS;
+            const int ncols = min(PCOLS, cild - nlo);
             const bool mrow = (r >= g.mask_c0 && r < g.mask_c0 + g.mask_w);
             if (r < g.M && !mrow && ncols > 0) {
-                const float* src = Ci + (long long)(rsrc ? rsrc[r] : r) * cild + n0;
+                const float* src = Ci + (long long)(rsrc ? rsrc[r] : r) * cild + nlo;
                 l2_prefetch(src, (uint32_t)ncols * 4u);
                 l2_prefetch(src + cipe, (uint32_t)ncols * 4u);
             }
@@ -281,7 +290,7 @@ __global__ void __launch_bounds__(192, BN <= 64 ? 2 : 1)
         // (two-plane operands).  The lo planes have the layout of the raw
         // planes, so the split is elementwise at equal offsets, whatever the swizzle.
         if (!presplit) {
-            const int ct = threadIdx.x - 64;                    // 0..127
+            const int ct = threadIdx.x - 64;                    // 0 .. 32*NEPI-1
             constexpr int NV4 = (2 * A_PLANE_BYTES + 2 * B_PLANE_BYTES) / 16;   // float4s per stage
             bool okc = true;
             for (int kt = 0; kt < nk; ++kt) {
@@ -289,7 +298,7 @@ __global__ void __launch_bounds__(192, BN <= 64 ? 2 : 1)
                 if (*(volatile int*)&s_abort) { okc = false; break; }
                 if (!mbar_wait(smem_u32(&bar_full[s]), (kt / STAGES) & 1)) { okc = false; break; }
                 unsigned char* st = smem + s * STAGE_BYTES;
-                for (int v = ct; v < NV4; v += 128) {
+                for (int v = ct; v < NV4; v += 32 * NEPI) {
                     // A re, A im | B re, B im; each lo plane sits two planes after its raw plane
                     const int off = v < 2 * A_PLANE_BYTES / 16 ? v * 16 : 4 * A_PLANE_BYTES + (v * 16 - 2 * A_PLANE_BYTES);
                     const int lo_off = off + (v < 2 * A_PLANE_BYTES / 16 ? 2 * A_PLANE_BYTES : 2 * B_PLANE_BYTES);
@@ -327,7 +336,7 @@ __global__ void __launch_bounds__(192, BN <= 64 ? 2 : 1)
             const int* rsrc = (sep && g.row_src) ? g.row_src + (long long)job * g.M : nullptr;
             const uint32_t lane_off = (uint32_t)(q * 32) << 16;
             // per-warp staging tile (the pipeline buffers are idle once the accumulator is final)
-            float* stg = reinterpret_cast<float*>(smem) + q * (2 * 32 * 36);
+            float* stg = reinterpret_cast<float*>(smem) + (warp - 2) * (2 * 32 * 36);
             // β-source row offsets of the 8 rows this lane reads in the row-major epilogue
             long long srow[8];
 #pragma unroll
@@ -335,7 +344,7 @@ __global__ void __launch_bounds__(192, BN <= 64 ? 2 : 1)
                 const int r = row0 + 4 * it + (lane >> 3);
                 srow[it] = (long long)(rsrc && r < g.M ? rsrc[r] : r) * cild;
             }
-            for (int ch = 0; ch < BN / 32; ++ch) {
+            for (int ch = part * (PCOLS / 32); ch < (part + 1) * (PCOLS / 32); ++ch) {
                 const int nb = n0 + ch * 32;
                 if (nb >= g.N) break;
                 uint32_t vr[32], vi[32];
@@ -505,7 +514,7 @@ int tc_launch_bn(const GemmArgs<float>* g, const int* c_trans_arr, const CUtenso
     P.g = *g;
     if (c_trans_arr) P.g.c_trans_arr = c_trans_arr;
     dim3 grid((g->N + BN - 1) / BN, (g->M + BM - 1) / BM, njobs);
-    gemm_tc_kernel<BN><<<grid, 192, TcTile<BN>::SMEM_BYTES, stream>>>(*mapA, *mapB, P);
+    gemm_tc_kernel<BN><<<grid, TcTile<BN>::THREADS, TcTile<BN>::SMEM_BYTES, stream>>>(*mapA, *mapB, P);
     return (int)cudaGetLastError();
 }
 }  // namespace
@@ -523,10 +532,6 @@ int tc_gemm_launch_maps(const GemmArgs<float>* g, const int* c_trans_arr, const 
 int tc_pick_bn(int M, int N, int K, int njobs, int num_sms) {
     const long long mt = (M + BM - 1) / BM;
     auto tiles = [&](int bn) { return mt * ((N + bn - 1) / bn) * njobs; };
-    // A short-K product (the Gauss-Jordan rank-panel update) is bound by its
-    // β read and C write: 64-column tiles let two CTAs share an SM, so one
-    // CTA's MMAs overlap the other's epilogue.
-    if (K <= 32) return 64;
     if (tiles(256) >= num_sms) return 256;
     if (tiles(128) >= num_sms) return 128;
     return 64;
