@@ -82,7 +82,8 @@ template <typename T> struct FactorStore {
     T* rv = nullptr; T* xv = nullptr; T* wv = nullptr;
     int vec_nrhs = 0;
     int* perm = nullptr;
-    int* rowsrc = nullptr;      // per-panel composed row exchanges
+    int* rowsrc = nullptr;      // per-panel composed row exchanges (two sets, panel parity)
+    int* gj_slots = nullptr;    // 0 .. 2*max_ne-1: GP/RP slot lists of both parities
     cplx<T>* trifac = nullptr;  // first-step tridiagonal factors (8*b per node)
     int* tripiv = nullptr;      // and their interchanges (b per node)
     bool tc_ok = false;
@@ -108,6 +109,8 @@ struct fdfd_handle {
     double scale = 1;            // factorization scaling of A
     std::string err;
     cudaStream_t stream = nullptr;
+    cudaStream_t stream2 = nullptr;   // Gauss-Jordan look-ahead: the wide part of each panel update
+    cudaEvent_t ev_panel = nullptr, ev_wide = nullptr;
     cudaEvent_t ev[8];
     long long launches = 0;
     long long dev_bytes = 0;
@@ -496,10 +499,17 @@ template <typename T> int alloc_factor(fdfd_handle* h) {
     RET(alloc_pool<T>(h, F.X, b, b, ld, planes, h->nXslots));
     // the panel buffers are short-K tensor-core operands: stored pre-split (re, im, re_lo, im_lo)
     const int pplanes = sizeof(T) == 4 ? 4 : 2;
-    RET(alloc_pool<T>(h, F.GP, b, pc, pc, pplanes, h->max_ne));
-    RET(alloc_pool<T>(h, F.RP, b, pc, pc, pplanes, h->max_ne));
+    // two sets (panel parity) so that a panel can run while the previous panel's update reads the other set
+    RET(alloc_pool<T>(h, F.GP, b, pc, pc, pplanes, 2 * h->max_ne));
+    RET(alloc_pool<T>(h, F.RP, b, pc, pc, pplanes, 2 * h->max_ne));
+    {
+        std::vector<int> sl(2 * h->max_ne);
+        for (int i = 0; i < 2 * h->max_ne; ++i) sl[i] = i;
+        RET(dev_alloc(h, (void**)&F.gj_slots, sl.size() * sizeof(int)));
+        CK(cudaMemcpy(F.gj_slots, sl.data(), sl.size() * sizeof(int), cudaMemcpyHostToDevice));
+    }
     RET(dev_alloc(h, (void**)&F.perm, (size_t)h->max_ne * b * sizeof(int)));
-    RET(dev_alloc(h, (void**)&F.rowsrc, (size_t)h->max_ne * b * sizeof(int)));
+    RET(dev_alloc(h, (void**)&F.rowsrc, (size_t)2 * h->max_ne * b * sizeof(int)));
     // largest Gauss-Jordan batch: the eliminated nodes of steps >= 2 (and of step 1
     // when it inverts by Gauss-Jordan), or the final pair's single matrices
     int gj_max = 1;
@@ -555,9 +565,11 @@ template <typename T>
 int gemm(fdfd_handle* h, int pa, int pb, int pc, const int* a_slot, const int* b_slot, const int* c_slot,
          const int* c_trans_arr, int c_trans, int njobs, int M, int N, int K, T alpha, int beta, int mask_c0,
          int mask_w, int pcin = -1, const int* cin_slot = nullptr,
-         const int* row_src = nullptr, int prof_cls = -1, double prof_work = 0.0) {
+         const int* row_src = nullptr, int prof_cls = -1, double prof_work = 0.0, cudaStream_t stream = nullptr,
+         int n_off = 0, int skip_c0 = 0, int skip_w = 0, int a_pool_slot0 = 0) {
     if (njobs == 0) return FDFD_OK;
     FactorStore<T>& F = store<T>(h);
+    if (!stream) stream = h->stream;
     GemmArgs<T> g;
     g.A = pool_of(F, pa); g.B = pool_of(F, pb); g.C = pool_of(F, pc);
     g.a_slot = a_slot; g.b_slot = b_slot; g.c_slot = c_slot;
@@ -565,21 +577,23 @@ int gemm(fdfd_handle* h, int pa, int pb, int pc, const int* a_slot, const int* b
     g.cin_slot = cin_slot; g.row_src = row_src;
     g.M = M; g.N = N; g.K = K; g.alpha = alpha; g.beta = beta;
     g.mask_c0 = mask_c0; g.mask_w = mask_w; g.c_trans = c_trans;
+    g.n_off = n_off; g.skip_c0 = skip_c0; g.skip_w = skip_w;
     g.c_trans_arr = nullptr;
     g.err = h->derr;
     const double flops = 8.0 * M * N * K * njobs;
     int ev = prof_begin(h);
     if (sizeof(T) == 4 && F.tc_ok) {
         int rc = tc_gemm_launch(reinterpret_cast<GemmArgs<float>*>(&g), c_trans_arr, pa, pb, njobs, &F.tc,
-                                h->num_sms, h->stream);
+                                h->num_sms, stream);
         if (rc != 0) return set_err(h, FDFD_ECUDA, "tcgen05 GEMM launch failed (%d)", rc);
         prof_end(h, ev, prof_cls >= 0 ? prof_cls : FDFD_PROF_GEMM_TC, prof_cls >= 0 ? prof_work : flops);
         h->launches++;
         h->tc_used = 1;
         return check_launch(h, "gemm_tc");
     }
+    if (n_off || skip_w) return set_err(h, FDFD_EINVAL, "column windows need the tensor-core GEMM");
     g.c_trans_arr = c_trans_arr;
-    launch_gemm_simt<T>(h->stream, njobs, g);
+    launch_gemm_simt<T>(stream, njobs, g);
     prof_end(h, ev, prof_cls >= 0 ? prof_cls : FDFD_PROF_GEMM_SIMT, prof_cls >= 0 ? prof_work : flops);
     h->launches++;
     return check_launch(h, "gemm_simt");
@@ -596,26 +610,62 @@ template <typename T> int gj_invert(fdfd_handle* h, const int* d_slots, const in
     if (njobs > F.Tg.count) return set_err(h, FDFD_EINVAL, "Gauss-Jordan batch %d exceeds %lld", njobs, F.Tg.count);
     launch_perm_init(h->stream, njobs, F.perm, b);
     h->launches++;
-    // the matrices alternate between the D slots and the ping-pong buffer: each
+    // The matrices alternate between the D slots and the ping-pong buffer: each
     // panel's update reads the current buffer through the panel's row exchanges
-    // and writes the other one
+    // and writes the other one.
+    //
+    // Look-ahead (FP32 tensor-core path, not while profiling): the update of
+    // panel p is split into the next panel's columns (on the main stream, so
+    // panel p+1 can start right away) and all other columns (on a second
+    // stream, overlapping panel p+1).  The panel buffers, rowsrc and their slot
+    // lists alternate by panel parity, so panel p+1 never overwrites what the
+    // wide update of panel p reads; the wide update of panel p must finish before
+    // the narrow update of panel p+1 writes into the buffer it reads.
+    const bool overlap = sizeof(T) == 4 && F.tc_ok && !h->prof_on && h->stream2;
+    const int npan = ceil_div(b, nb);
     int cur = P_D, alt = P_TG;
     const int* cur_slots = d_slots;
     const int* alt_slots = d_iota;
-    for (int c0 = 0; c0 < b; c0 += nb) {
-        int w = std::min(nb, b - c0);
+    bool wide_pending = false;
+    for (int p = 0; p < npan; ++p) {
+        const int c0 = p * nb, w = std::min(nb, b - c0);
+        const int par = overlap ? (p & 1) : 0;
+        Pool<T> GPp = F.GP, RPp = F.RP;
+        GPp.base += (size_t)par * h->max_ne * F.GP.slot_elems();
+        RPp.base += (size_t)par * h->max_ne * F.RP.slot_elems();
+        int* rs = F.rowsrc + (size_t)par * h->max_ne * b;
+        const int* pslots = F.gj_slots + par * h->max_ne;   // GP/RP slots of this parity
         int ev = prof_begin(h);
-        int e = launch_gj_panel<T>(h->stream, nb, njobs, pool_of(F, cur), cur_slots, F.GP, F.RP, F.perm, F.rowsrc,
-                                   c0, h->derr);
+        int e = launch_gj_panel<T>(h->stream, nb, njobs, pool_of(F, cur), cur_slots, GPp, RPp, F.perm, rs, c0,
+                                   h->derr);
         prof_end(h, ev, FDFD_PROF_GJ_PANEL, 0.0);
         h->launches++;
         if (e) return set_err(h, FDFD_ECUDA, "gj_panel launch failed: %s", cudaGetErrorString((cudaError_t)e));
-        RET(gemm<T>(h, P_GP, P_RP, alt, d_iota, d_iota, alt_slots, nullptr, 0, njobs, b, b, F.GP.cols, (T)1, 1,
-                    c0, w, cur, cur_slots, F.rowsrc, FDFD_PROF_GJ_UPDATE,
-                    4.0 * sizeof(T) * (double)b * b * njobs));
+        const double ubytes = 4.0 * sizeof(T) * (double)b * b * njobs;
+        if (overlap && p + 1 < npan) {
+            const int c1 = c0 + nb, w1 = std::min(nb, b - c1);
+            CK(cudaEventRecord(h->ev_panel, h->stream));
+            if (wide_pending) CK(cudaStreamWaitEvent(h->stream, h->ev_wide, 0));
+            RET(gemm<T>(h, P_GP, P_RP, alt, pslots, pslots, alt_slots, nullptr, 0, njobs, b, w1, F.GP.cols, (T)1, 1,
+                        c0, w, cur, cur_slots, rs, FDFD_PROF_GJ_UPDATE, ubytes * w1 / b, h->stream, c1));
+            CK(cudaStreamWaitEvent(h->stream2, h->ev_panel, 0));
+            RET(gemm<T>(h, P_GP, P_RP, alt, pslots, pslots, alt_slots, nullptr, 0, njobs, b, b, F.GP.cols, (T)1, 1,
+                        c0, w, cur, cur_slots, rs, FDFD_PROF_GJ_UPDATE, ubytes * (b - w1) / b, h->stream2, 0, c1,
+                        w1));
+            CK(cudaEventRecord(h->ev_wide, h->stream2));
+            wide_pending = true;
+        } else {
+            if (wide_pending) {
+                CK(cudaStreamWaitEvent(h->stream, h->ev_wide, 0));
+                wide_pending = false;
+            }
+            RET(gemm<T>(h, P_GP, P_RP, alt, pslots, pslots, alt_slots, nullptr, 0, njobs, b, b, F.GP.cols, (T)1, 1,
+                        c0, w, cur, cur_slots, rs, FDFD_PROF_GJ_UPDATE, ubytes));
+        }
         std::swap(cur, alt);
         std::swap(cur_slots, alt_slots);
     }
+    if (wide_pending) CK(cudaStreamWaitEvent(h->stream, h->ev_wide, 0));
     launch_gj_unpermute<T>(h->stream, njobs, pool_of(F, cur), cur_slots, F.D, d_slots, F.perm);
     h->launches++;
     return check_launch(h, "gj_unpermute");
@@ -1076,6 +1126,12 @@ int fdfd_create(fdfd_handle** out, int Nx, int Ny, int Npx, int Npy, double dx, 
         return FDFD_ECUDA;
     }
     for (auto& e : h->ev) cudaEventCreate(&e);
+    if (cudaStreamCreateWithFlags(&h->stream2, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->ev_panel, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->ev_wide, cudaEventDisableTiming) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(FDFD_ECUDA);
+    }
     {
         int dev = 0;
         cudaGetDevice(&dev);
@@ -1109,6 +1165,9 @@ void fdfd_destroy(fdfd_handle* h) {
     for (auto& e : h->ev) if (e) cudaEventDestroy(e);
     for (auto& e : h->evpool) cudaEventDestroy(e);
     if (h->stream) cudaStreamDestroy(h->stream);
+    if (h->stream2) cudaStreamDestroy(h->stream2);
+    if (h->ev_panel) cudaEventDestroy(h->ev_panel);
+    if (h->ev_wide) cudaEventDestroy(h->ev_wide);
     delete h;
 }
 
@@ -1661,6 +1720,7 @@ int debug_gemm_impl(int M, int N, int K, const double* A, const double* B, doubl
         g.Cin = Pool<T>(); g.cin_slot = nullptr; g.row_src = nullptr;
         g.M = M; g.N = N; g.K = K; g.alpha = (T)1; g.beta = 0; g.mask_c0 = 0; g.mask_w = 0;
         g.c_trans = 0; g.c_trans_arr = nullptr; g.err = derr;
+        g.n_off = 0; g.skip_c0 = 0; g.skip_w = 0;
         cudaEvent_t e0, e1;
         cudaEventCreate(&e0); cudaEventCreate(&e1);
         if (sizeof(T) == 4 && use_tc) {

@@ -3,6 +3,8 @@
 //
 //   C[m][n] = beta(m,n)·Cin[src(m)][n] + alpha·Σ_k A[m][k]·B[n][k]      (complex)
 //
+// over matrix columns n in [n_off, n_off + N) without [skip_c0, skip_c0 + skip_w)
+//
 // Operands are FP32 planar pools.  The tensor core reads only the top 19 bits
 // of an FP32 operand, so the raw plane serves as the "hi" term; with the TF32
 // residual lo = x - (x with the low 13 mantissa bits cleared)
@@ -208,7 +210,7 @@ __global__ void __launch_bounds__(TcTile<BN>::THREADS, BN <= 64 ? 2 : 1)
                 for (int p = 0; p < np; ++p)
                     tma_load_3d(st + p * A_PLANE_BYTES, &mapA, k0, m0, aslot * np + p, bar);
                 for (int p = 0; p < np; ++p)
-                    tma_load_3d(st + 4 * A_PLANE_BYTES + p * B_PLANE_BYTES, &mapB, k0, n0, bslot * np + p, bar);
+                    tma_load_3d(st + 4 * A_PLANE_BYTES + p * B_PLANE_BYTES, &mapB, k0, n0 + g.n_off, bslot * np + p, bar);
                 issued = kt + 1;
             }
             if (!ok) {
@@ -277,8 +279,8 @@ __global__ void __launch_bounds__(TcTile<BN>::THREADS, BN <= 64 ? 2 : 1)
             const int cild = sep ? g.Cin.ld : g.C.ld;
             const int* rsrc = (sep && g.row_src) ? g.row_src + (long long)job * g.M : nullptr;
             const int r = m0 + q * 32 + lane;
-            const int nlo = n0 + part * PCOLS;
-            const int ncols = min(PCOLS, cild - nlo);
+            const int nlo = n0 + g.n_off + part * PCOLS;
+            const int ncols = min(min(PCOLS, cild - nlo), g.n_off + g.N - nlo);
             const bool mrow = (r >= g.mask_c0 && r < g.mask_c0 + g.mask_w);
             if (r < g.M && !mrow && ncols > 0) {
                 const float* src = Ci + (long long)(rsrc ? rsrc[r] : r) * cild + nlo;
@@ -358,9 +360,11 @@ __global__ void __launch_bounds__(TcTile<BN>::THREADS, BN <= 64 ? 2 : 1)
                         for (int j = 0; j < 32; ++j) {
                             const int n = nb + j;
                             if (n >= g.N) break;
+                            const int na = n + g.n_off;      // matrix column
+                            if (na >= g.skip_c0 && na < g.skip_c0 + g.skip_w) continue;
                             const float xr = g.alpha * __uint_as_float(vr[j]);
                             const float xi = g.alpha * __uint_as_float(vi[j]);
-                            const long long off = (long long)n * ld + row;
+                            const long long off = (long long)na * ld + row;
                             C[off] = xr;
                             C[pe + off] = xi;
                         }
@@ -383,7 +387,10 @@ __global__ void __launch_bounds__(TcTile<BN>::THREADS, BN <= 64 ? 2 : 1)
                     __syncwarp();
                     const int sub = lane >> 3, cq = lane & 7;
                     const int n = nb + 4 * cq;
-                    const bool full4 = (n + 3 < g.N);
+                    const int na = n + g.n_off;          // matrix column of the group
+                    // a group touching the skipped columns takes the per-element path
+                    const bool skipg = na + 3 >= g.skip_c0 && na < g.skip_c0 + g.skip_w;
+                    const bool full4 = (n + 3 < g.N) && !skipg;
                     float4 cre[8], cim[8];
 #pragma unroll
                     for (int it = 0; it < 8; ++it) {
@@ -392,7 +399,7 @@ __global__ void __launch_bounds__(TcTile<BN>::THREADS, BN <= 64 ? 2 : 1)
                         cim[it] = cre[it];
                         const bool mrow = (r >= g.mask_c0 && r < g.mask_c0 + g.mask_w);
                         if (g.beta && r < g.M && !mrow) {
-                            const long long off = srow[it] + n;
+                            const long long off = srow[it] + na;
                             if (full4) {
                                 cre[it] = __ldcg(reinterpret_cast<const float4*>(Ci + off));
                                 cim[it] = __ldcg(reinterpret_cast<const float4*>(Ci + cipe + off));
@@ -400,7 +407,10 @@ __global__ void __launch_bounds__(TcTile<BN>::THREADS, BN <= 64 ? 2 : 1)
                                 float* a = reinterpret_cast<float*>(&cre[it]);
                                 float* c = reinterpret_cast<float*>(&cim[it]);
                                 for (int e = 0; e < 4; ++e)
-                                    if (n + e < g.N) { a[e] = __ldcg(Ci + off + e); c[e] = __ldcg(Ci + cipe + off + e); }
+                                    if (n + e < g.N && !(na + e >= g.skip_c0 && na + e < g.skip_c0 + g.skip_w)) {
+                                        a[e] = __ldcg(Ci + off + e);
+                                        c[e] = __ldcg(Ci + cipe + off + e);
+                                    }
                             }
                         }
                     }
@@ -419,18 +429,18 @@ __global__ void __launch_bounds__(TcTile<BN>::THREADS, BN <= 64 ? 2 : 1)
                         float xr[4], xi[4];
 #pragma unroll
                         for (int e = 0; e < 4; ++e) {
-                            const int col = n + e;
+                            const int col = na + e;
                             const bool keep = g.beta && !(mrow || (col >= g.mask_c0 && col < g.mask_c0 + g.mask_w));
                             xr[e] = g.alpha * srp[e] + (keep ? crp[e] : 0.f);
                             xi[e] = g.alpha * sip[e] + (keep ? cip[e] : 0.f);
                         }
-                        const long long off = (long long)r * ld + n;
+                        const long long off = (long long)r * ld + na;
                         if (full4) {
                             *reinterpret_cast<float4*>(C + off) = make_float4(xr[0], xr[1], xr[2], xr[3]);
                             *reinterpret_cast<float4*>(C + pe + off) = make_float4(xi[0], xi[1], xi[2], xi[3]);
                         } else {
                             for (int e = 0; e < 4; ++e)
-                                if (n + e < g.N) {
+                                if (n + e < g.N && !(na + e >= g.skip_c0 && na + e < g.skip_c0 + g.skip_w)) {
                                     C[off + e] = xr[e];
                                     C[pe + off + e] = xi[e];
                                 }

@@ -104,6 +104,9 @@ template <typename T> struct GemmArgs {
     int M, N, K;
     T alpha; int beta;
     int mask_c0, mask_w;
+    // tensor-core kernel only: the product covers matrix columns [n_off, n_off + N)
+    // (B rows likewise); columns [skip_c0, skip_c0 + skip_w) are neither read nor written
+    int n_off, skip_c0, skip_w;
     int c_trans;
     const int* c_trans_arr;   // per-job override of c_trans (device, may be null)
     unsigned* err;
