@@ -189,8 +189,10 @@ def run_extras(L, pkg, W, a):
     """The other benchmark problems, each timed with host-buffer calls after one warm-up:
     adjoint gradients/s on the 1000x600 adjoint problem (300x300 design, Gaussian overlap
     objective), eigenfrequency time on the 12x12 rod-lattice cavity (280x280, 6 modes nearest
-    ωa/2πc = 0.38), and RHS solves/s on a bounded slice of the 400x400 sweep (first 4 of the
-    64 wavelengths, 8 Gaussian sources each; the full sweep repeats this per wavelength)."""
+    ωa/2πc = 0.38), RHS solves/s on a bounded slice of the 400x400 sweep (first 4 of the
+    64 wavelengths, 8 Gaussian sources each; the full sweep repeats this per wavelength),
+    coupled-sideband solves/s of the reference notebook's modulated waveguide (1500x200, three
+    frequencies) and problems/s of the 32-problem mixed-size batch."""
     out = {}
     try:
         p = W.adjoint_problem()
@@ -248,7 +250,80 @@ def run_extras(L, pkg, W, a):
                         "rel_residual": st.rel_residual}
     except Exception as e:
         out["sweep"] = {"error": str(e)}
+    try:
+        p = W.modulated_notebook()
+        e = p.extra
+        h = L.ModulatedHandle(p.Nx, p.Ny, p.npml[0], p.npml[1], p.dx, p.dy, e["nsidebands"], 1e-6, p.pml_m,
+                              p.pml_lnR, e["sharedpml"], L.FDFD_PREC_MIXED)
+        h.set_refinement(1e-10, 80)
+        h.set_eps(p.eps)
+        h.set_deps(e["deps"])
+        h.factor(p.omega, e["Omega"])
+        h.solve(p.src)
+        t0 = time.perf_counter()
+        n = 3
+        for _ in range(n):
+            h.set_eps(p.eps)
+            h.factor(p.omega, e["Omega"])
+            _, _, _, st = h.solve(p.src)
+        t = time.perf_counter() - t0
+        h.close()
+        out["modulated"] = {"solves_per_s": n / t, "workload": "modulated waveguide 1500x200, 1 sideband each side "
+                            "(3 coupled frequencies), host buffers, mixed", "rel_residual": st.rel_residual,
+                            "iterations": st.iterations, "t_factor_ms": st.t_factor_ms, "t_solve_ms": st.t_solve_ms}
+    except Exception as e:   # reported, not hidden
+        out["modulated"] = {"error": str(e)}
+    try:
+        out["mixed_batch"] = run_mixed_batch(L, pkg, W)
+    except Exception as e:
+        out["mixed_batch"] = {"error": str(e)}
     return out
+
+
+def run_mixed_batch(L, pkg, W):
+    """The 32-problem mixed-size batch (square sides drawn from 128, 256, 512, 1024 with a fixed
+    seed; split guide with a centred random design of half the side).  One host thread per side
+    class owns one handle (its own CUDA stream) and solves that class's problems in order, so the
+    classes run concurrently on the GPU; host buffers in and out, each problem refined to 1e-10.
+    Timed after one warm-up problem per class; handle creation is outside the timed region."""
+    import concurrent.futures as cf
+    probs = W.mixed_size_batch()
+    classes = {}
+    for p in probs:
+        classes.setdefault(p.Nx, []).append(p)
+
+    def make(p):
+        h = L.Handle(p.Nx, p.Ny, p.npml[0], p.npml[1], p.dx, p.dy, 1e-6, p.pml_m, p.pml_lnR, pkg.TM,
+                     L.FDFD_PREC_MIXED)
+        h.set_refinement(1e-10, 80)
+        return h
+
+    handles = {s: make(ps[0]) for s, ps in classes.items()}
+
+    def run_class(s, ps):
+        h = handles[s]
+        out = []
+        for p in ps:
+            h.set_eps(p.eps)
+            h.factor(p.omega)
+            _, _, _, st = h.solve(p.src)
+            out.append((st.rel_residual, st.iterations, st.fp64_fallback))
+        return out
+
+    for s, ps in classes.items():          # warm-up: first problem of each class
+        run_class(s, ps[:1])
+    t0 = time.perf_counter()
+    with cf.ThreadPoolExecutor(max_workers=len(classes)) as ex:
+        res = [r for rs in ex.map(lambda kv: run_class(*kv), classes.items()) for r in rs]
+    t = time.perf_counter() - t0
+    for h in handles.values():
+        h.close()
+    return {"problems_per_s": len(probs) / t, "seconds": t, "problems": len(probs),
+            "sides": {int(s): len(ps) for s, ps in sorted(classes.items())},
+            "rel_residual_max": max(r[0] for r in res), "iterations_max": max(r[1] for r in res),
+            "iterations_sum": sum(r[1] for r in res), "fp64_fallbacks": sum(r[2] for r in res),
+            "workload": "32 square problems, sides from {128, 256, 512, 1024} (seed 5), one stream per side "
+                        "class, host buffers, mixed"}
 
 
 def gemm_traffic_bytes():

@@ -24,8 +24,9 @@ import numpy as np
 from . import _lib
 from ._lib import FDFDError, FDFD_PREC_FP64, FDFD_PREC_MIXED  # noqa: F401
 
-__all__ = ["EPS0", "MU0", "C0", "ETA0", "TM", "TE", "Grid", "Device", "Point", "setup_eps", "setup_src",
-           "solve", "eigenfrequency", "FieldTM", "FieldTE", "normalize_parameters", "FDFDError"]
+__all__ = ["EPS0", "MU0", "C0", "ETA0", "TM", "TE", "Grid", "Device", "ModulatedDevice", "Point", "setup_eps",
+           "setup_src", "setup_deps", "solve", "eigenfrequency", "FieldTM", "FieldTE", "normalize_parameters",
+           "FDFDError"]
 
 # src/types.jl:6-9
 EPS0 = 8.85418782e-12
@@ -110,7 +111,33 @@ class Device:
             self.src = np.zeros(self.grid.N, dtype=np.complex128)
 
 
-def _mask(d: Device, region):
+@dataclass
+class ModulatedDevice:
+    """src/solver/modulation.jl:4-28: a Device with a modulation amplitude Δϵᵣ
+    (zero by default), modulation frequency Ω, the number of sidebands on each
+    side of the carrier and whether the sidebands share the carrier's PML."""
+    grid: Grid
+    omega: list
+    Omega: float
+    nsidebands: int
+    sharedpml: bool = True
+    eps: np.ndarray = None
+    deps: np.ndarray = None
+    src: np.ndarray = None
+    modes: list = field(default_factory=list)
+
+    def __post_init__(self):
+        if np.isscalar(self.omega):
+            self.omega = [float(self.omega)]
+        if self.eps is None:
+            self.eps = np.ones(self.grid.N, dtype=np.complex128)
+        if self.deps is None:
+            self.deps = np.zeros(self.grid.N, dtype=np.complex128)
+        if self.src is None:
+            self.src = np.zeros(self.grid.N, dtype=np.complex128)
+
+
+def _mask(d, region):
     X, Y = np.meshgrid(d.grid.xc(), d.grid.yc(), indexing="ij")
     return np.vectorize(region)(X, Y).astype(bool), X, Y
 
@@ -132,7 +159,14 @@ def setup_src(d: Device, where, value=None):
     d.src[m] = np.vectorize(value)(X, Y)[m] if callable(value) else value
 
 
+def setup_deps(d: ModulatedDevice, region, value):
+    """setup_Δϵᵣ!(d, region, value): src/solver/modulation.jl:29-30 (region and value may be callables)."""
+    m, X, Y = _mask(d, region)
+    d.deps[m] = np.vectorize(value)(X, Y)[m] if callable(value) else value
+
+
 globals()["setup_ϵᵣ"] = setup_eps
+globals()["setup_Δϵᵣ"] = setup_deps
 
 
 class _Field:
@@ -186,7 +220,10 @@ def solve(d: Device, pol=TM, precision="mixed", pml_m=3.5, pml_lnR=-12.0, tol=1e
     refined solve for d.src.  ``pml_m``/``pml_lnR`` default to the values the
     reference hard-wires (src/pml.jl:1, S_create does not forward them).
     Returns a FieldTM/FieldTE, or a list when len(d.omega) > 1 (driven.jl:206-207).
+    A ModulatedDevice takes the coupled-sideband path (``solve_modulated``).
     """
+    if isinstance(d, ModulatedDevice):
+        return solve_modulated(d, precision, pml_m, pml_lnR, tol, max_iter, return_stats)
     if d.modes:
         raise FDFDError(_lib.FDFD_EINVAL, "mode sources are not supported by the GPU solve path")
     h = make_handle(d, pol, precision, pml_m, pml_lnR, tol, max_iter)
@@ -204,6 +241,35 @@ def solve(d: Device, pol=TM, precision="mixed", pml_m=3.5, pml_lnR=-12.0, tol=1e
     return (res, stats) if return_stats else res
 
 
+def solve_modulated(d: ModulatedDevice, precision="mixed", pml_m=3.5, pml_lnR=-12.0, tol=1e-10, max_iter=60,
+                    return_stats=False):
+    """solve(d::ModulatedDevice) — src/solver/modulation.jl:35-119 (TM).
+
+    Per carrier ω one factorization of the 2s+1 sideband operators and a
+    refined solve of the coupled system.  Returns an Nω x (2s+1) nested list of
+    FieldTM (the reference's ``Array{FieldTM}(undef, Nω, nfrequencies)``), the
+    field of sideband n = -s..s carrying ωₙ = ω + nΩ."""
+    if d.modes:
+        raise FDFDError(_lib.FDFD_EINVAL, "mode sources are not supported by the GPU solve path")
+    g = d.grid
+    h = _lib.ModulatedHandle(g.N[0], g.N[1], g.Npml[0], g.Npml[1], g.dx(), g.dy(), d.nsidebands, g.L0, pml_m,
+                             pml_lnR, d.sharedpml, _prec(precision))
+    out, stats = [], []
+    try:
+        h.set_refinement(tol, max_iter)
+        h.set_eps(d.eps)
+        h.set_deps(d.deps)
+        for w in d.omega:
+            h.factor(w, d.Omega)
+            ez, hx, hy, st = h.solve(d.src)
+            wn = [w + d.Omega * n for n in range(-d.nsidebands, d.nsidebands + 1)]
+            out.append([FieldTM(g, wn[j], np.stack([ez[j], hx[j], hy[j]], axis=-1)) for j in range(len(wn))])
+            stats.append(st.as_dict())
+    finally:
+        h.close()
+    return (out, stats) if return_stats else out
+
+
 def eigenfrequency(d: Device, pol, nev, which="LM", precision="mixed", pml_m=3.5, pml_lnR=-12.0, tol=1e-10):
     """eigenfrequency(d, pol, nev; which) — src/solver/eigen.jl:318-364."""
     h = make_handle(d, pol, precision, pml_m, pml_lnR, tol)
@@ -214,8 +280,9 @@ def eigenfrequency(d: Device, pol, nev, which="LM", precision="mixed", pml_m=3.5
         flds = np.empty((nev, 3, N), dtype=np.complex128)
         st = _lib.Stats()
         import ctypes as C
-        rc = h.lib.fdfd_eigfreq(h.h, float(d.omega[0]), int(nev), 0, float(tol), _lib.cptr(om), _lib.cptr(lam),
-                                _lib.cptr(flds), C.byref(st))
+        which_code = {"LM": 0, "LR": 1}[which]
+        rc = h.lib.fdfd_eigfreq(h.h, float(d.omega[0]), int(nev), which_code, float(tol), _lib.cptr(om),
+                                _lib.cptr(lam), _lib.cptr(flds), C.byref(st))
         h._check(rc)
         cls = FieldTM if pol == TM else FieldTE
         fields = []

@@ -24,6 +24,8 @@ FDFD_REFINE_GMRES, FDFD_REFINE_CLASSIC = 0, 1
 
 # every symbol include/fdfd_cuda.h declares
 EXPORTS = ["fdfd_version", "fdfd_create", "fdfd_destroy", "fdfd_last_error", "fdfd_set_refinement",
+           "fdfd_set_fallback", "fdfd_set_restart", "fdfd_mf_create", "fdfd_mf_set_deps", "fdfd_mf_factor",
+           "fdfd_mf_solve",
            "fdfd_set_eps", "fdfd_factor", "fdfd_solve", "fdfd_solve_device", "fdfd_adjoint", "fdfd_eigfreq",
            "fdfd_get_stencil", "fdfd_apply", "fdfd_set_profiling", "fdfd_get_profile", "fdfd_residual_noalloc",
            "fdfd_debug_hessenberg_eig", "fdfd_debug_gemm"]
@@ -35,7 +37,8 @@ class Stats(C.Structure):
                 ("t_assemble_ms", C.c_double), ("t_factor_ms", C.c_double), ("t_solve_ms", C.c_double),
                 ("t_recover_ms", C.c_double), ("t_total_ms", C.c_double), ("factor_flops", C.c_double),
                 ("block", C.c_int), ("nblocks", C.c_int), ("levels", C.c_int), ("tc_gemm", C.c_int),
-                ("device_bytes", C.c_longlong), ("gpu_launches", C.c_longlong)]
+                ("device_bytes", C.c_longlong), ("gpu_launches", C.c_longlong),
+                ("factor_precision", C.c_int), ("fp64_fallback", C.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -78,6 +81,19 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.fdfd_last_error.argtypes = [vp]
     lib.fdfd_set_refinement.restype = ip
     lib.fdfd_set_refinement.argtypes = [vp, C.c_double, ip, ip]
+    lib.fdfd_set_fallback.restype = ip
+    lib.fdfd_set_fallback.argtypes = [vp, ip]
+    lib.fdfd_set_restart.restype = ip
+    lib.fdfd_set_restart.argtypes = [vp, ip]
+    lib.fdfd_mf_create.restype = ip
+    lib.fdfd_mf_create.argtypes = [C.POINTER(vp), ip, ip, ip, ip, C.c_double, C.c_double, C.c_double, C.c_double,
+                                   C.c_double, ip, ip, ip]
+    lib.fdfd_mf_set_deps.restype = ip
+    lib.fdfd_mf_set_deps.argtypes = [vp, dp]
+    lib.fdfd_mf_factor.restype = ip
+    lib.fdfd_mf_factor.argtypes = [vp, C.c_double, C.c_double]
+    lib.fdfd_mf_solve.restype = ip
+    lib.fdfd_mf_solve.argtypes = [vp, dp, dp, dp, dp, C.POINTER(Stats)]
     lib.fdfd_set_eps.restype = ip
     lib.fdfd_set_eps.argtypes = [vp, dp]
     lib.fdfd_factor.restype = ip
@@ -160,6 +176,14 @@ class Handle:
     def set_refinement(self, tol=1e-10, max_iter=40, mode=FDFD_REFINE_GMRES):
         self._check(self.lib.fdfd_set_refinement(self.h, float(tol), int(max_iter), int(mode)))
 
+    def set_restart(self, m=0):
+        """FGMRES basis length (0: automatic)."""
+        self._check(self.lib.fdfd_set_restart(self.h, int(m)))
+
+    def set_fallback(self, on=True):
+        """FP64 re-factorization when a MIXED handle's refinement stalls (default on)."""
+        self._check(self.lib.fdfd_set_fallback(self.h, int(bool(on))))
+
     def set_eps(self, eps):
         buf = natural(eps)
         self._check(self.lib.fdfd_set_eps(self.h, cptr(buf)))
@@ -236,6 +260,47 @@ class Handle:
         self._check(self.lib.fdfd_apply(self.h, cptr(buf), x3.shape[0], cptr(out)))
         y = from_natural(out, self.Nx, self.Ny)
         return y[0] if single else y
+
+
+class ModulatedHandle(Handle):
+    """Owning wrapper of a modulated-device handle (fdfd_mf_create): K = 2s+1
+    coupled sidebands, TM (solve(d::ModulatedDevice), modulation.jl:35-119)."""
+
+    def __init__(self, Nx, Ny, Npx, Npy, dx, dy, nsidebands, L0=1e-6, pml_m=3.5, pml_lnR=-12.0,
+                 shared_pml=True, precision=FDFD_PREC_MIXED):
+        self.lib = load()
+        self.h = C.c_void_p()
+        rc = self.lib.fdfd_mf_create(C.byref(self.h), int(Nx), int(Ny), int(Npx), int(Npy), float(dx), float(dy),
+                                     float(L0), float(pml_m), float(pml_lnR), int(nsidebands),
+                                     1 if shared_pml else 0, int(precision))
+        if rc != FDFD_OK:
+            raise FDFDError(rc, "fdfd_mf_create failed")
+        self.Nx, self.Ny, self.pol = int(Nx), int(Ny), FDFD_TM
+        self.K = 2 * int(nsidebands) + 1
+
+    def set_deps(self, deps):
+        buf = natural(deps)
+        self._check(self.lib.fdfd_mf_set_deps(self.h, cptr(buf)))
+
+    def factor(self, omega, Omega):
+        self._check(self.lib.fdfd_mf_factor(self.h, float(omega), float(Omega)))
+
+    def solve(self, src):
+        """src (Nx, Ny) -> (Ez, Hx, Hy, stats), each field (K, Nx, Ny), sideband n = -s..s."""
+        buf = natural(src)
+        outs = [np.empty(self.K * self.Nx * self.Ny, dtype=np.complex128) for _ in range(3)]
+        st = Stats()
+        self._check(self.lib.fdfd_mf_solve(self.h, cptr(buf), cptr(outs[0]), cptr(outs[1]), cptr(outs[2]),
+                                           C.byref(st)))
+        f = [from_natural(o, self.Nx, self.Ny) for o in outs]
+        return f[0], f[1], f[2], st
+
+    def apply(self, x):
+        """Coupled operator product: x (K, Nx, Ny) -> y (K, Nx, Ny)."""
+        buf = natural(x)
+        out = np.empty_like(buf)
+        self._check(self.lib.fdfd_apply(self.h, cptr(buf), 1, cptr(out)))
+        return from_natural(out, self.Nx, self.Ny)
 
 
 def hessenberg_eig(H):

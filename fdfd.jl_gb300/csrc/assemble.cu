@@ -58,6 +58,9 @@ __global__ void sfactor_kernel(SFactorArgs a, cplx<double>* out) {
 //   OP_TE_DRIVEN  A = δxf Tϵxi δxb + δyf Tϵyi δyb + ω² μ₀ I         driven.jl:194
 //   OP_TM_EIGEN   A = Tϵᵣ⁻¹δxf δxb + Tϵᵣ⁻¹δyf δyb - σ I             eigen.jl:333
 //   OP_TE_EIGEN   A = δxf Tϵx⁻¹ δxb + δyf Tϵy⁻¹ δyb - σ I           eigen.jl:351
+//   OP_TM_SIDEBAND  Aₙ = Sxb δxb μ₀⁻¹ Sxf δxf + Syb δyb μ₀⁻¹ Syf δyf + ωₙ² Tϵ
+//                 (one sideband of a modulated device, modulation.jl:80-88:
+//                 backward difference outside, forward inside)
 // with δxf = Sxf·δ(x̂,Forward) etc. (driven.jl:177-180) and the Tϵ averages
 // of grid_average (grid.jl:183-188).
 // ---------------------------------------------------------------------------
@@ -89,7 +92,18 @@ __global__ void stencil_kernel(StencilArgs a, const cplx<double>* __restrict__ e
     cplx<double> bx = cscale_rn(sxb, a.idx), bxp = cscale_rn(sxbp, a.idx);
     cplx<double> by = cscale_rn(syb, a.idy), byp = cscale_rn(sybp, a.idy);
     cplx<double> self, cxm, cxp, cym, cyp;
-    if (a.op == OP_TM_DRIVEN || a.op == OP_TM_EIGEN) {
+    if (a.op == OP_TM_SIDEBAND) {
+        // row i of Sxb δxb μ₀⁻¹ Sxf δxf: (sxb_i/dx)μ₀⁻¹ [sxf_i/dx (v_{i+1} - v_i) - sxf_{i-1}/dx (v_i - v_{i-1})]
+        const int ixm = (ix + a.Nx - 1) % a.Nx, iym = (iy + a.Ny - 1) % a.Ny;
+        cplx<double> ox = cscale_rn(bx, a.imu0), oy = cscale_rn(by, a.imu0);
+        cxp = cmul_rn(ox, cscale_rn(sxf, a.idx));
+        cxm = cmul_rn(ox, cscale_rn(inv[ixm], a.idx));
+        cyp = cmul_rn(oy, cscale_rn(syf, a.idy));
+        cym = cmul_rn(oy, cscale_rn(inv[2 * a.Nx + iym], a.idy));
+        cplx<double> sx = cneg(cadd_rn(cxp, cxm)), sy = cneg(cadd_rn(cyp, cym));
+        cplx<double> e = cscale_rn(eps[k], a.eps0n);
+        self = cadd_rn(cadd_rn(sx, sy), cscale_rn(e, a.omega2));
+    } else if (a.op == OP_TM_DRIVEN || a.op == OP_TM_EIGEN) {
         // forward row factor f = (Sxf δxf)_{i,i+1} = sxf_i/dx, times μ₀⁻¹ (driven) or
         // pre-multiplied by ϵᵣ⁻¹ (eigen: Tϵᵣ⁻¹*δxf).
         cplx<double> fx = cscale_rn(sxf, a.idx), fy = cscale_rn(syf, a.idy);
@@ -189,6 +203,67 @@ __global__ void residual_kernel(int Nx, int Ny, int nrhs, const cplx<double>* __
         if (l == 0) {
             part[((size_t)rhs * gridDim.x + blockIdx.x) * 2 + 0] = rr;
             part[((size_t)rhs * gridDim.x + blockIdx.x) * 2 + 1] = bb;
+        }
+    }
+}
+
+// Residual of the coupled sideband system (modulation.jl:91-99), nrhs = 1:
+// r_n = b_n - (A_n x_n + ½ωₙ²ϵ₀ conj(Δϵ)⊙x_{n+1} + ½ωₙ²ϵ₀ Δϵ⊙x_{n-1}); vectors are
+// sideband-major (x_n at offset n·Nx·Ny).  Grid (blocks, K); partial sums of
+// |r|², |b|² per (sideband, block) in part[n][block][2].
+__global__ void residual_mf_kernel(MfResidualArgs a, const cplx<double>* __restrict__ deps,
+                                   const cplx<double>* __restrict__ x, const cplx<double>* __restrict__ b,
+                                   cplx<double>* __restrict__ r, double* __restrict__ part) {
+    const long long N = (long long)a.Nx * a.Ny;
+    const int n = blockIdx.y;
+    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    double rr = 0.0, bb = 0.0;
+    if (k < N) {
+        const int ix = (int)(k % a.Nx), iy = (int)(k / a.Nx);
+        const long long kxm = (ix == 0) ? k + a.Nx - 1 : k - 1;
+        const long long kxp = (ix == a.Nx - 1) ? k - (a.Nx - 1) : k + 1;
+        const long long kym = (iy == 0) ? k + N - a.Nx : k - a.Nx;
+        const long long kyp = (iy == a.Ny - 1) ? k - (N - a.Nx) : k + a.Nx;
+        const cplx<double>* st = a.st[n];
+        const cplx<double>* xv = x + (size_t)n * N;
+        cplx<double> acc = cmul(st[k], xv[k]);
+        acc = cadd(acc, cmul(st[N + k], xv[kxm]));
+        acc = cadd(acc, cmul(st[2 * N + k], xv[kxp]));
+        acc = cadd(acc, cmul(st[3 * N + k], xv[kym]));
+        acc = cadd(acc, cmul(st[4 * N + k], xv[kyp]));
+        const cplx<double> d = deps[k];
+        const double c = a.half_w2eps0[n];
+        if (n + 1 < a.K) acc = cadd(acc, cmul(cmk(c * d.re, -c * d.im), xv[N + k]));
+        if (n > 0) acc = cadd(acc, cmul(cmk(c * d.re, c * d.im), xv[k - N]));
+        if (b) {
+            const cplx<double> bv = b[(size_t)n * N + k];
+            acc = csub(bv, acc);
+            bb = bv.re * bv.re + bv.im * bv.im;
+        }
+        rr = acc.re * acc.re + acc.im * acc.im;
+        r[(size_t)n * N + k] = acc;
+    }
+    if (!part) return;
+    __shared__ double s_rr[32], s_bb[32];
+    for (int o = 16; o > 0; o >>= 1) {
+        rr += __shfl_down_sync(0xffffffffu, rr, o);
+        bb += __shfl_down_sync(0xffffffffu, bb, o);
+    }
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) { s_rr[w] = rr; s_bb[w] = bb; }
+    __syncthreads();
+    if (w == 0) {
+        const int nw = blockDim.x >> 5;
+        rr = l < nw ? s_rr[l] : 0.0;
+        bb = l < nw ? s_bb[l] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) {
+            rr += __shfl_down_sync(0xffffffffu, rr, o);
+            bb += __shfl_down_sync(0xffffffffu, bb, o);
+        }
+        if (l == 0) {
+            double* p = part + ((size_t)n * gridDim.x + blockIdx.x) * 2;
+            p[0] = rr;
+            p[1] = bb;
         }
     }
 }

@@ -950,20 +950,19 @@ __global__ void __launch_bounds__(128) tri_columns_kernel(int b, Pool<T> D, cons
 template <typename T>
 void launch_tri_inverse(cudaStream_t s, int njobs, NodeMap m, const cplx<double>* st, double scale, Pool<T> D,
                         const int* nodes, cplx<T>* fac, int* piv, unsigned* err) {
+    // both kernels opt in once (thread-safe static initialisation) to the shared memory of
+    // the largest block, b = 1024: above 48 KB they must opt in
+    static const bool opted = [] {
+        const size_t mx = 8 * (size_t)1024 * sizeof(cplx<T>) + (size_t)1024 * sizeof(int);
+        return cudaFuncSetAttribute(tri_factor_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx) ==
+                   cudaSuccess &&
+               cudaFuncSetAttribute(tri_columns_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx) ==
+                   cudaSuccess;
+    }();
+    (void)opted;
     const size_t fsmem = 8 * (size_t)m.b * sizeof(cplx<T>) + (size_t)m.b * sizeof(int);
-    static size_t fopted = 48 * 1024;
-    if (fsmem > fopted &&
-        cudaFuncSetAttribute(tri_factor_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsmem) ==
-            cudaSuccess)
-        fopted = fsmem;
     tri_factor_kernel<T><<<njobs, 32, fsmem, s>>>(m, st, scale, nodes, fac, piv, err);
     const size_t smem = 6 * (size_t)m.b * sizeof(cplx<T>) + (size_t)m.b * sizeof(int);
-    // above 48 KB (FP64 blocks of more than ~500 unknowns) the kernel must opt in
-    static size_t opted = 48 * 1024;
-    if (smem > opted &&
-        cudaFuncSetAttribute(tri_columns_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) ==
-            cudaSuccess)
-        opted = smem;
     tri_columns_kernel<T><<<dim3(ceil_div(m.b, 128), njobs), 128, smem, s>>>(m.b, D, nodes, fac, piv);
 }
 template <typename T>
@@ -975,10 +974,9 @@ template <typename T>
 void launch_level1_combine(cudaStream_t s, int njobs, NodeMap m, const cplx<double>* st, double scale, Pool<T> D,
                            Pool<T> C, const L1Job* jobs) {
     const size_t smem = level1_combine_smem<T>();
-    static bool attr = false;
-    if (!attr && cudaFuncSetAttribute(level1_combine_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)smem) == cudaSuccess)
-        attr = true;
+    static const cudaError_t attr =
+        cudaFuncSetAttribute(level1_combine_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    (void)attr;
     level1_combine_kernel<T><<<dim3(ceil_div(m.b, 128), ceil_div(m.b, 32), njobs), 256, smem, s>>>(m, st, scale, D,
                                                                                                   C, jobs);
 }
@@ -989,13 +987,9 @@ template <typename T, int NB, int R, int C>
 static int gj_panel_launch(cudaStream_t s, int njobs, Pool<T> M, const int* slots, Pool<T> GP, Pool<T> RP,
                            int* perm, int* rowsrc, int c0, unsigned* err) {
     const size_t smem = gj_panel_smem_elems<NB, R>() * sizeof(T);
-    static bool attr = false;
-    if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(gj_panel_kernel<T, NB, R, C>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return (int)e;
-        attr = true;
-    }
+    static const cudaError_t attr =
+        cudaFuncSetAttribute(gj_panel_kernel<T, NB, R, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (attr != cudaSuccess) return (int)attr;
     gj_panel_kernel<T, NB, R, C><<<njobs, 512, smem, s>>>(M, slots, GP, RP, perm, rowsrc, c0, err);
     return (int)cudaGetLastError();
 }

@@ -92,6 +92,19 @@ template <typename T> struct FactorStore {
 
 }  // namespace
 
+// Modulated device (multi-frequency FDFD, modulation.jl): K = 2s+1 sideband
+// operators, each factored by its own handle, coupled through Δϵ.
+struct MfState {
+    int s = 0, K = 1;
+    bool shared_pml = true;
+    double omega = 0, Omega = 0;
+    std::vector<double> wn;              // ωₙ = ω + nΩ, n = -s..s
+    std::vector<fdfd_handle*> sub;       // one handle per sideband (its own stream)
+    cplx<double>* deps = nullptr;        // Δϵᵣ (Nx*Ny, device)
+    cudaEvent_t ev_in = nullptr;
+    std::vector<cudaEvent_t> ev_out;
+};
+
 struct fdfd_handle {
     // problem
     int Nx, Ny, Npx, Npy, pol, precision;
@@ -100,6 +113,13 @@ struct fdfd_handle {
     double tol = 1e-10;
     int max_iter = 40;
     int refine_mode = FDFD_REFINE_GMRES;
+    int fact_prec = FDFD_PREC_FP64;  // precision of the current factor
+    bool fallback = true;            // MIXED: re-factor in FP64 when the refinement would not converge
+    int restart = 0;                 // FGMRES basis length (0: automatic)
+    int nsb = 1;                     // Krylov vector length in units of Nx*Ny (K for a modulated device)
+    MfState* mf = nullptr;           // modulated device state (fdfd_mf_create), else null
+    double mf_factor_ms = 0;         // wall time of the last fdfd_mf_factor
+    bool fell_back = false;          // the current factor is such an FP64 re-factorization
     NodeMap map;
     // state
     bool eps_set = false, factored = false;
@@ -162,6 +182,9 @@ struct fdfd_handle {
 };
 
 namespace {
+
+// length of one refinement vector (unknowns of the solved system)
+long long vlen(const fdfd_handle* h) { return (long long)h->Nx * h->Ny * h->nsb; }
 
 int set_err(fdfd_handle* h, int code, const char* fmt, ...) {
     char buf[512];
@@ -828,8 +851,30 @@ template <typename T> int precond_impl(fdfd_handle* h, const cplx<double>* in, c
     return check_launch(h, "precond");
 }
 
+int precond(fdfd_handle* h, const cplx<double>* in, cplx<double>* out, int nrhs);
+
+// modulated device: block-diagonal preconditioner, sideband n solved by its
+// own factor on its own stream (the K sweeps run concurrently)
+int precond_mf(fdfd_handle* h, const cplx<double>* in, cplx<double>* out) {
+    MfState& M = *h->mf;
+    const long long N = (long long)h->Nx * h->Ny;
+    CK(cudaEventRecord(M.ev_in, h->stream));
+    for (int n = 0; n < M.K; ++n) {
+        fdfd_handle* s = M.sub[n];
+        CK(cudaStreamWaitEvent(s->stream, M.ev_in, 0));
+        const long long l0 = s->launches;
+        int rc = precond(s, in + (size_t)n * N, out + (size_t)n * N, 1);
+        h->launches += s->launches - l0;
+        if (rc != FDFD_OK) return set_err(h, rc, "sideband %d: %s", n, s->err.c_str());
+        CK(cudaEventRecord(M.ev_out[n], s->stream));
+    }
+    for (int n = 0; n < M.K; ++n) CK(cudaStreamWaitEvent(h->stream, M.ev_out[n], 0));
+    return FDFD_OK;
+}
+
 int precond(fdfd_handle* h, const cplx<double>* in, cplx<double>* out, int nrhs) {
-    return h->precision == FDFD_PREC_FP64 ? precond_impl<double>(h, in, out, nrhs)
+    if (h->mf) return precond_mf(h, in, out);
+    return h->fact_prec == FDFD_PREC_FP64 ? precond_impl<double>(h, in, out, nrhs)
                                           : precond_impl<float>(h, in, out, nrhs);
 }
 
@@ -854,8 +899,39 @@ int ensure_red(fdfd_handle* h, size_t doubles) {
 }
 
 // r = b - A x (b may be null: r = A x); optionally ||r||², ||b||² per rhs to host
+int residual_mf(fdfd_handle* h, const cplx<double>* x, const cplx<double>* b, cplx<double>* r,
+                std::vector<double>* norms) {
+    const MfState& M = *h->mf;
+    const long long N = (long long)h->Nx * h->Ny;
+    const int nb = ceil_div(N, 256);
+    RET(ensure_part(h, (size_t)M.K * nb * 2));
+    RET(ensure_red(h, (size_t)M.K * 2));
+    MfResidualArgs a;
+    a.Nx = h->Nx; a.Ny = h->Ny; a.K = M.K;
+    for (int n = 0; n < M.K; ++n) {
+        a.st[n] = M.sub[n]->st;
+        a.half_w2eps0[n] = 0.5 * M.wn[n] * M.wn[n] * (kEPS0 * h->L0);
+    }
+    int ev = prof_begin(h);
+    LAUNCH(residual_mf_kernel, dim3(nb, M.K), 256, 0, a, M.deps, x, b, r, norms ? h->part : nullptr);
+    prof_end(h, ev, FDFD_PROF_RESIDUAL, (double)N * M.K * (96.0 + 16.0 * (b ? 3 : 2)));
+    if (norms) {
+        LAUNCH(reduce_partials_kernel, M.K, 256, 0, h->part, nb, 2, h->red);
+        std::vector<double> per(2 * M.K);
+        CK(cudaMemcpyAsync(per.data(), h->red, per.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+        norms->assign(2, 0.0);
+        for (int n = 0; n < M.K; ++n) {
+            (*norms)[0] += per[2 * n];
+            (*norms)[1] += per[2 * n + 1];
+        }
+    }
+    return check_launch(h, "residual");
+}
+
 int residual(fdfd_handle* h, const cplx<double>* x, const cplx<double>* b, cplx<double>* r, int nrhs,
              std::vector<double>* norms) {
+    if (h->mf) return residual_mf(h, x, b, r, norms);   // nrhs = 1
     long long N = (long long)h->Nx * h->Ny;
     int nb = ceil_div(N, 256);
     RET(ensure_part(h, (size_t)nrhs * nb * 2));
@@ -876,7 +952,7 @@ int residual(fdfd_handle* h, const cplx<double>* x, const cplx<double>* b, cplx<
 // out[rhs*nvec + j] = V_jᴴ w  (complex)
 int dots(fdfd_handle* h, const cplx<double>* V, long long vstride, int nvec, const cplx<double>* w, int nrhs,
          std::vector<zd>& out) {
-    long long N = (long long)h->Nx * h->Ny;
+    long long N = vlen(h);
     const int nb = 152;
     RET(ensure_part(h, (size_t)nrhs * nb * 2 * nvec));
     RET(ensure_red(h, (size_t)nrhs * 2 * nvec));
@@ -893,30 +969,42 @@ int dots(fdfd_handle* h, const cplx<double>* V, long long vstride, int nvec, con
 // y[rhs] += sign Σ_j c[rhs][j] V_j[rhs]
 int combine(fdfd_handle* h, const cplx<double>* V, long long vstride, int nvec, const std::vector<zd>& c, int nrhs,
             double sign, cplx<double>* y) {
-    long long N = (long long)h->Nx * h->Ny;
+    long long N = vlen(h);
     CK(cudaMemcpyAsync(h->kc, c.data(), c.size() * sizeof(zd), cudaMemcpyHostToDevice, h->stream));
     LAUNCH(vcombine_kernel, dim3(ceil_div(N, 256), nrhs), 256, 0, N, nvec, V, vstride, h->kc, nvec, sign, y);
     return check_launch(h, "combine");
 }
 
 int scale_vec(fdfd_handle* h, const cplx<double>* x, const std::vector<zd>& s, int nrhs, cplx<double>* y) {
-    long long N = (long long)h->Nx * h->Ny;
+    long long N = vlen(h);
     CK(cudaMemcpyAsync(h->kc, s.data(), nrhs * sizeof(zd), cudaMemcpyHostToDevice, h->stream));
     LAUNCH(vscale_kernel, dim3(ceil_div(N, 256), nrhs), 256, 0, N, x, h->kc, y);
     return check_launch(h, "scale");
 }
 
+// FGMRES basis length: the handle's setting, else the iteration budget up to
+// 80 solves while the 2m+1 basis vectors fit in 8 GiB, at least 20.  Slowly
+// converging FP32-preconditioned problems (strong resonances at 1024²) stall
+// under restarts every 20 solves and converge unrestarted within ~60.
+int restart_len(const fdfd_handle* h, int nrhs) {
+    if (h->restart > 0) return h->restart;
+    const double vec = (double)vlen(h) * nrhs * sizeof(cplx<double>);
+    const int cap = (int)((8.0 * (1ull << 30) / vec - 1) / 2);
+    return std::max(20, std::min(std::min(h->max_iter, 80), cap));
+}
+
 int ensure_krylov(fdfd_handle* h, int nrhs, int m) {
     if (h->kr_nrhs >= nrhs && h->kr_m >= m) return FDFD_OK;
     dev_free(h->kb); dev_free(h->kx); dev_free(h->kr); dev_free(h->kV); dev_free(h->kZ); dev_free(h->kc);
-    long long N = (long long)h->Nx * h->Ny;
+    long long N = vlen(h);
     size_t v = (size_t)N * nrhs * sizeof(cplx<double>);
     RET(dev_alloc(h, (void**)&h->kb, v));
     RET(dev_alloc(h, (void**)&h->kx, v));
     RET(dev_alloc(h, (void**)&h->kr, v));
     RET(dev_alloc(h, (void**)&h->kV, v * (m + 1)));
     RET(dev_alloc(h, (void**)&h->kZ, v * m));
-    RET(dev_alloc(h, (void**)&h->kc, (size_t)nrhs * (m + 2) * sizeof(cplx<double>) * 2));
+    // coefficients: 2(m+2) per rhs for the refinement, 2 per sideband for the recovery
+    RET(dev_alloc(h, (void**)&h->kc, ((size_t)nrhs * (m + 2) * 2 + 2 * MF_MAX_K) * sizeof(cplx<double>)));
     h->kr_nrhs = nrhs;
     h->kr_m = m;
     return FDFD_OK;
@@ -925,10 +1013,13 @@ int ensure_krylov(fdfd_handle* h, int nrhs, int m) {
 // Solve A x = b (h->kb, nrhs vectors) into h->kx to ||b - A x||/||b|| <= tol.
 // GMRES mode: restarted flexible GMRES (Saad 1993) with classical Gram-Schmidt
 // and one re-orthogonalisation, right-preconditioned by the factorization.
-int refine(fdfd_handle* h, int nrhs, int* iters, double* relres) {
-    long long N = (long long)h->Nx * h->Ny;
-    const int m = 20;
-    RET(ensure_krylov(h, nrhs, m));
+// give_up: stop as soon as the residual reduction measured over the last
+// update projects past max_iter solves (the caller then re-factors).
+int refine(fdfd_handle* h, int nrhs, int* iters, double* relres, bool give_up) {
+    long long N = vlen(h);
+    // the caller sized the workspace (ensure_krylov) before filling h->kb
+    if (h->kr_nrhs < nrhs || h->kr_m < 1) return set_err(h, FDFD_EINVAL, "Krylov workspace not allocated");
+    const int m = std::min(restart_len(h, nrhs), h->kr_m);
     const size_t vs = (size_t)N * nrhs;   // stride between basis vectors
     CK(cudaMemsetAsync(h->kx, 0, vs * sizeof(cplx<double>), h->stream));
     std::vector<double> nrm;
@@ -941,17 +1032,28 @@ int refine(fdfd_handle* h, int nrhs, int* iters, double* relres) {
     }
     int it = 0;
     auto maxrel = [&]() { return *std::max_element(rel.begin(), rel.end()); };
+    // log-linear projection of the solves still needed from the reduction
+    // r0 -> r1 over `used` solves
+    auto hopeless = [&](double r0, double r1, int used) {
+        if (!give_up || r1 <= h->tol || used < 1) return false;
+        if (!(r1 < r0)) return true;
+        const double per = std::log(r1 / r0) / used;
+        return it + std::log(h->tol / r1) / per > h->max_iter;
+    };
     if (h->refine_mode == FDFD_REFINE_CLASSIC) {
         while (maxrel() > h->tol && it < h->max_iter) {
+            const double r0 = maxrel();
             RET(precond(h, h->kr, h->kZ, nrhs));
             ++it;
             std::vector<zd> one(nrhs, zd(1, 0));
             RET(combine(h, h->kZ, 0, 1, one, nrhs, 1.0, h->kx));
             RET(residual(h, h->kx, h->kb, h->kr, nrhs, &nrm));
             for (int r = 0; r < nrhs; ++r) rel[r] = std::sqrt(nrm[2 * r]) / bnorm[r];
+            if (it >= 3 && hopeless(r0, maxrel(), 1)) break;
         }
     } else {
         while (maxrel() > h->tol && it < h->max_iter) {
+            const double r0 = maxrel();
             // start a cycle from the current residual
             std::vector<double> beta(nrhs);
             std::vector<zd> inv(nrhs);
@@ -1026,6 +1128,7 @@ int refine(fdfd_handle* h, int nrhs, int* iters, double* relres) {
             if (k > 0) RET(combine(h, h->kZ, vs, k, coef, nrhs, 1.0, h->kx));
             RET(residual(h, h->kx, h->kb, h->kr, nrhs, &nrm));
             for (int r = 0; r < nrhs; ++r) rel[r] = std::sqrt(nrm[2 * r]) / bnorm[r];
+            if (hopeless(r0, maxrel(), k)) break;
         }
     }
     *iters = it;
@@ -1068,12 +1171,60 @@ int assemble(fdfd_handle* h, int op, double omega_pml, zd sigma, double omega_dr
     return FDFD_OK;
 }
 
-int factor_op(fdfd_handle* h) {
-    int rc = h->precision == FDFD_PREC_FP64 ? factor_impl<double>(h) : factor_impl<float>(h);
-    if (rc != FDFD_OK) return rc;
-    RET(check_device(h, "factor"));
+// factors the assembled operator in precision `prec` (FDFD_PREC_*; -1: the handle's)
+int factor_op(fdfd_handle* h, int prec = -1);
+
+// modulated device: assemble and factor the K sideband operators
+// (modulation.jl:77-89; PML at ω when shared, else at ωₙ)
+int factor_mf(fdfd_handle* h, int prec) {
+    MfState& M = *h->mf;
+    h->factored = false;
+    for (int n = 0; n < M.K; ++n) {
+        fdfd_handle* s = M.sub[n];
+        const long long l0 = s->launches;
+        int rc = assemble(s, OP_TM_SIDEBAND, M.shared_pml ? M.omega : M.wn[n], zd(0, 0), M.wn[n]);
+        if (rc == FDFD_OK) rc = factor_op(s, prec);
+        h->launches += s->launches - l0;
+        if (rc != FDFD_OK) return set_err(h, rc, "sideband %d: %s", n, s->err.c_str());
+    }
+    h->fact_prec = prec;
+    h->fell_back = prec != h->precision;
+    h->op = OP_TM_SIDEBAND;
     h->factored = true;
     return FDFD_OK;
+}
+
+int factor_op(fdfd_handle* h, int prec) {
+    if (prec < 0) prec = h->precision;
+    if (h->mf) return factor_mf(h, prec);
+    h->factored = false;
+    int rc = prec == FDFD_PREC_FP64 ? factor_impl<double>(h) : factor_impl<float>(h);
+    if (rc != FDFD_OK) return rc;
+    RET(check_device(h, "factor"));
+    h->fact_prec = prec;
+    h->fell_back = prec != h->precision;
+    h->factored = true;
+    return FDFD_OK;
+}
+
+// refine() and, for a MIXED handle whose FP32-preconditioned refinement
+// stalls, an FP64 factorization of the same operator followed by a second
+// refinement (the first one's iterations count towards *iters).
+int refine_fb(fdfd_handle* h, int nrhs, int* iters, double* relres) {
+    const bool can = h->fallback && h->fact_prec == FDFD_PREC_MIXED;
+    RET(refine(h, nrhs, iters, relres, can));
+    if (!can || *relres <= h->tol) return FDFD_OK;
+    RET(factor_op(h, FDFD_PREC_FP64));
+    int it2 = 0;
+    RET(refine(h, nrhs, &it2, relres, false));
+    *iters += it2;
+    return FDFD_OK;
+}
+
+template <typename T> void free_store(FactorStore<T>& F) {
+    void* bufs[] = {F.D.base, F.C.base, F.X.base, F.GP.base, F.RP.base, F.Tg.base, F.rv, F.xv, F.wv,
+                    F.perm, F.rowsrc, F.gj_slots, F.trifac, F.tripiv};
+    for (void* p : bufs) dev_free(p);
 }
 
 double elapsed_ms(cudaEvent_t a, cudaEvent_t b) {
@@ -1157,11 +1308,19 @@ int fdfd_create(fdfd_handle** out, int Nx, int Ny, int Npx, int Npy, double dx, 
 void fdfd_destroy(fdfd_handle* h) {
     if (!h) return;
     if (h->stream) cudaStreamSynchronize(h->stream);
+    if (h->mf) {
+        for (fdfd_handle* s : h->mf->sub) fdfd_destroy(s);
+        dev_free(h->mf->deps);
+        if (h->mf->ev_in) cudaEventDestroy(h->mf->ev_in);
+        for (auto& e : h->mf->ev_out) if (e) cudaEventDestroy(e);
+        delete h->mf;
+        h->mf = nullptr;
+    }
     void* bufs[] = {h->eps, h->sf, h->st, h->derr, h->part, h->red, h->kb, h->kx, h->kr, h->kV, h->kZ, h->kc, h->io,
-                    h->djobs, h->f32.D.base, h->f32.C.base, h->f32.X.base, h->f32.GP.base, h->f32.RP.base,
-                    h->f32.rv, h->f32.xv, h->f32.wv, h->f32.perm, h->f64.D.base, h->f64.C.base, h->f64.X.base,
-                    h->f64.GP.base, h->f64.RP.base, h->f64.rv, h->f64.xv, h->f64.wv, h->f64.perm};
+                    h->djobs};
     for (void* p : bufs) dev_free(p);
+    free_store(h->f32);
+    free_store(h->f64);
     for (auto& e : h->ev) if (e) cudaEventDestroy(e);
     for (auto& e : h->evpool) cudaEventDestroy(e);
     if (h->stream) cudaStreamDestroy(h->stream);
@@ -1179,6 +1338,19 @@ int fdfd_set_refinement(fdfd_handle* h, double tol, int max_iter, int mode) {
     return FDFD_OK;
 }
 
+int fdfd_set_restart(fdfd_handle* h, int m) {
+    if (!h) return FDFD_EINVAL;
+    if (m < 0 || m > 512) return set_err(h, FDFD_EINVAL, "restart length must be in [0, 512]");
+    h->restart = m;
+    return FDFD_OK;
+}
+
+int fdfd_set_fallback(fdfd_handle* h, int on) {
+    if (!h) return FDFD_EINVAL;
+    h->fallback = on != 0;
+    return FDFD_OK;
+}
+
 int fdfd_set_eps(fdfd_handle* h, const double* eps_r) {
     if (!h || !eps_r) return h ? set_err(h, FDFD_EINVAL, "eps_r is NULL") : FDFD_EINVAL;
     long long N = (long long)h->Nx * h->Ny;
@@ -1187,6 +1359,12 @@ int fdfd_set_eps(fdfd_handle* h, const double* eps_r) {
     for (long long k = 0; k < N; ++k)
         if (eps_r[2 * k] == 0 && eps_r[2 * k + 1] == 0) return set_err(h, FDFD_EINVAL, "eps_r is zero at %lld", k);
     CK(cudaMemcpyAsync(h->eps, eps_r, N * sizeof(cplx<double>), cudaMemcpyHostToDevice, h->stream));
+    if (h->mf)
+        for (fdfd_handle* s : h->mf->sub) {
+            CK(cudaMemcpyAsync(s->eps, h->eps, N * sizeof(cplx<double>), cudaMemcpyDeviceToDevice, h->stream));
+            s->eps_set = true;
+            s->factored = false;
+        }
     CK(cudaStreamSynchronize(h->stream));
     h->eps_set = true;
     h->factored = false;
@@ -1195,6 +1373,7 @@ int fdfd_set_eps(fdfd_handle* h, const double* eps_r) {
 
 int fdfd_factor(fdfd_handle* h, double omega) {
     if (!h) return FDFD_EINVAL;
+    if (h->mf) return set_err(h, FDFD_EINVAL, "modulated device: use fdfd_mf_factor");
     if (!h->eps_set) return set_err(h, FDFD_EINVAL, "fdfd_set_eps must be called before fdfd_factor");
     if (!(omega > 0) || !std::isfinite(omega)) return set_err(h, FDFD_EINVAL, "omega must be positive and finite");
     h->launches = 0;
@@ -1215,17 +1394,18 @@ namespace {
 // driven solve on device buffers: src (nrhs natural vectors) -> fields
 int solve_core(fdfd_handle* h, const cplx<double>* d_src, int nrhs, cplx<double>* f1, cplx<double>* f2,
                cplx<double>* f3, fdfd_stats* st) {
+    if (h->mf) return set_err(h, FDFD_EINVAL, "modulated device: use fdfd_mf_solve");
     if (!h->factored || (h->op != OP_TM_DRIVEN && h->op != OP_TE_DRIVEN))
         return set_err(h, FDFD_EINVAL, "fdfd_factor must be called before the solve");
     long long N = (long long)h->Nx * h->Ny;
-    RET(ensure_krylov(h, nrhs, 20));
+    RET(ensure_krylov(h, nrhs, restart_len(h, nrhs)));
     cudaEventRecord(h->ev[3], h->stream);
     // b = iω·src   (driven.jl:185,195)
     std::vector<zd> iw(nrhs, zd(0, h->omega));
     RET(scale_vec(h, d_src, iw, nrhs, h->kb));
     int iters = 0;
     double rel = 0;
-    RET(refine(h, nrhs, &iters, &rel));
+    RET(refine_fb(h, nrhs, &iters, &rel));
     cudaEventRecord(h->ev[4], h->stream);
     RET(check_device(h, "solve"));
     if (f1) CK(cudaMemcpyAsync(f1, h->kx, N * nrhs * sizeof(cplx<double>), cudaMemcpyDeviceToDevice, h->stream));
@@ -1266,6 +1446,8 @@ int solve_core(fdfd_handle* h, const cplx<double>* d_src, int nrhs, cplx<double>
         st->nblocks = h->map.n;
         st->levels = (int)h->steps.size() + 1;
         st->tc_gemm = h->tc_used;
+        st->factor_precision = h->fact_prec;
+        st->fp64_fallback = h->fell_back;
         st->device_bytes = h->dev_bytes;
         st->gpu_launches = h->launches;
     }
@@ -1326,6 +1508,168 @@ int fdfd_solve(fdfd_handle* h, const double* src, int nrhs, double* f1, double* 
     return rc;
 }
 
+// ---- modulated device (multi-frequency FDFD), modulation.jl -----------------
+int fdfd_mf_create(fdfd_handle** out, int Nx, int Ny, int Npx, int Npy, double dx, double dy, double L0,
+                   double pml_m, double pml_lnR, int nsidebands, int shared_pml, int precision) {
+    if (!out) return FDFD_EINVAL;
+    *out = nullptr;
+    if (nsidebands < 0 || 2 * nsidebands + 1 > MF_MAX_K) return FDFD_EINVAL;
+    fdfd_handle* h = nullptr;
+    int rc = fdfd_create(&h, Nx, Ny, Npx, Npy, dx, dy, L0, pml_m, pml_lnR, FDFD_TM, precision);
+    if (rc != FDFD_OK) return rc;
+    MfState* M = new MfState();
+    h->mf = M;
+    M->s = nsidebands;
+    M->K = 2 * nsidebands + 1;
+    M->shared_pml = shared_pml != 0;
+    h->nsb = M->K;
+    auto fail = [&](int code) {
+        fdfd_destroy(h);
+        return code;
+    };
+    for (int n = 0; n < M->K; ++n) {
+        fdfd_handle* s = nullptr;
+        rc = fdfd_create(&s, Nx, Ny, Npx, Npy, dx, dy, L0, pml_m, pml_lnR, FDFD_TM, precision);
+        if (rc != FDFD_OK) return fail(rc);
+        M->sub.push_back(s);
+    }
+    M->ev_out.assign(M->K, nullptr);
+    if (cudaEventCreateWithFlags(&M->ev_in, cudaEventDisableTiming) != cudaSuccess) return fail(FDFD_ECUDA);
+    for (auto& e : M->ev_out)
+        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return fail(FDFD_ECUDA);
+    const long long N = (long long)Nx * Ny;
+    rc = dev_alloc(h, (void**)&M->deps, N * sizeof(cplx<double>));
+    if (rc != FDFD_OK) return fail(rc);
+    if (cudaMemset(M->deps, 0, N * sizeof(cplx<double>)) != cudaSuccess) return fail(FDFD_ECUDA);
+    *out = h;
+    return FDFD_OK;
+}
+
+int fdfd_mf_set_deps(fdfd_handle* h, const double* deps_r) {
+    if (!h) return FDFD_EINVAL;
+    if (!h->mf) return set_err(h, FDFD_EINVAL, "not a modulated device handle (fdfd_mf_create)");
+    if (!deps_r) return set_err(h, FDFD_EINVAL, "deps_r is NULL");
+    const long long N = (long long)h->Nx * h->Ny;
+    for (long long k = 0; k < 2 * N; ++k)
+        if (!std::isfinite(deps_r[k])) return set_err(h, FDFD_EINVAL, "deps_r has a non-finite entry at %lld", k / 2);
+    CK(cudaMemcpyAsync(h->mf->deps, deps_r, N * sizeof(cplx<double>), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return FDFD_OK;
+}
+
+int fdfd_mf_factor(fdfd_handle* h, double omega, double Omega) {
+    if (!h) return FDFD_EINVAL;
+    if (!h->mf) return set_err(h, FDFD_EINVAL, "not a modulated device handle (fdfd_mf_create)");
+    if (!h->eps_set) return set_err(h, FDFD_EINVAL, "fdfd_set_eps must be called before fdfd_mf_factor");
+    if (!(omega > 0) || !std::isfinite(omega) || !std::isfinite(Omega))
+        return set_err(h, FDFD_EINVAL, "omega must be positive and finite, Omega finite");
+    MfState& M = *h->mf;
+    M.omega = omega;
+    M.Omega = Omega;
+    M.wn.resize(M.K);
+    for (int j = 0; j < M.K; ++j) {
+        M.wn[j] = omega + Omega * (j - M.s);   // modulation.jl:47
+        if (!(M.wn[j] > 0))
+            return set_err(h, FDFD_EINVAL, "sideband frequency omega + %d*Omega = %g is not positive", j - M.s, M.wn[j]);
+    }
+    h->launches = 0;
+    h->factored = false;
+    auto t0 = std::chrono::steady_clock::now();
+    RET(factor_op(h));
+    h->mf_factor_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    h->omega = omega;
+    return FDFD_OK;
+}
+
+int fdfd_mf_solve(fdfd_handle* h, const double* src, double* ez, double* hx, double* hy, fdfd_stats* stats) {
+    if (!h) return FDFD_EINVAL;
+    if (!h->mf) return set_err(h, FDFD_EINVAL, "not a modulated device handle (fdfd_mf_create)");
+    if (!src) return set_err(h, FDFD_EINVAL, "src is NULL");
+    if (!h->factored) return set_err(h, FDFD_EINVAL, "fdfd_mf_factor must be called before fdfd_mf_solve");
+    auto t0 = std::chrono::steady_clock::now();
+    MfState& M = *h->mf;
+    const long long N = (long long)h->Nx * h->Ny;
+    for (long long k = 0; k < 2 * N; ++k)
+        if (!std::isfinite(src[k])) return set_err(h, FDFD_EINVAL, "src has a non-finite entry");
+    const size_t bytes = (size_t)N * M.K * sizeof(cplx<double>);
+    if (h->io_cap < 4 * bytes) {
+        dev_free(h->io);
+        h->io = nullptr;
+        h->dev_bytes -= (long long)h->io_cap;
+        h->io_cap = 0;
+        RET(dev_alloc(h, (void**)&h->io, 4 * bytes));
+        h->io_cap = 4 * bytes;
+    }
+    cplx<double>* d_src = h->io;
+    cplx<double>* d_hx = h->io + N * M.K;
+    cplx<double>* d_hy = h->io + 2 * N * M.K;
+    RET(ensure_krylov(h, 1, restart_len(h, 1)));
+    CK(cudaMemcpyAsync(d_src, src, N * sizeof(cplx<double>), cudaMemcpyHostToDevice, h->stream));
+    cudaEventRecord(h->ev[3], h->stream);
+    // b = iω·src in the centre sideband, zero elsewhere (modulation.jl:62-64)
+    CK(cudaMemsetAsync(h->kb, 0, bytes, h->stream));
+    const zd iw(0, M.omega);
+    CK(cudaMemcpyAsync(h->kc, &iw, sizeof(zd), cudaMemcpyHostToDevice, h->stream));
+    LAUNCH(vscale_kernel, dim3(ceil_div(N, 256), 1), 256, 0, N, d_src, h->kc, h->kb + (size_t)M.s * N);
+    int iters = 0;
+    double rel = 0;
+    RET(refine_fb(h, 1, &iters, &rel));
+    cudaEventRecord(h->ev[4], h->stream);
+    // H per sideband with forward differences (modulation.jl:110-111)
+    std::vector<zd> coef(2 * M.K);
+    const double mu0 = kMU0 * h->L0;
+    for (int j = 0; j < M.K; ++j) {
+        coef[2 * j] = zd(-0.0, (1.0 / M.wn[j]) / mu0);       // -1/1im/ωₙ/μ₀
+        coef[2 * j + 1] = zd(0.0, (-1.0 / M.wn[j]) / mu0);   //  1/1im/ωₙ/μ₀
+    }
+    CK(cudaMemcpyAsync(h->kc, coef.data(), coef.size() * sizeof(zd), cudaMemcpyHostToDevice, h->stream));
+    RecoverArgs ra;
+    ra.Nx = h->Nx; ra.Ny = h->Ny; ra.mode = REC_TM_EIGEN;
+    ra.idx = 1.0 / h->dx; ra.idy = 1.0 / h->dy; ra.eps0n = kEPS0 * h->L0;
+    for (int j = 0; j < M.K; ++j)
+        LAUNCH(recover_kernel, dim3(ceil_div(N, 256), 1), 256, 0, ra, M.sub[j]->sf, M.sub[j]->eps,
+               h->kx + (size_t)j * N, h->kc + 2 * j, d_hx + (size_t)j * N, d_hy + (size_t)j * N);
+    RET(check_launch(h, "recover"));
+    cudaEventRecord(h->ev[5], h->stream);
+    int rc = FDFD_OK;
+    if (ez && cudaMemcpyAsync(ez, h->kx, bytes, cudaMemcpyDeviceToHost, h->stream) != cudaSuccess) rc = FDFD_ECUDA;
+    if (hx && cudaMemcpyAsync(hx, d_hx, bytes, cudaMemcpyDeviceToHost, h->stream) != cudaSuccess) rc = FDFD_ECUDA;
+    if (hy && cudaMemcpyAsync(hy, d_hy, bytes, cudaMemcpyDeviceToHost, h->stream) != cudaSuccess) rc = FDFD_ECUDA;
+    if (cudaStreamSynchronize(h->stream) != cudaSuccess) rc = FDFD_ECUDA;
+    if (rc != FDFD_OK) return set_err(h, rc, "copy of fields failed");
+    RET(check_device(h, "mf_solve"));
+    if (stats) {
+        fdfd_handle* s0 = M.sub[0];
+        double flops = 0;
+        long long bytes_all = h->dev_bytes;
+        for (fdfd_handle* s : M.sub) {
+            flops += s->last_factor_flops;
+            bytes_all += s->dev_bytes;
+        }
+        stats->iterations = iters;
+        stats->nrhs = 1;
+        stats->rel_residual = rel;
+        stats->t_assemble_ms = 0;
+        stats->t_factor_ms = h->mf_factor_ms;
+        stats->t_solve_ms = elapsed_ms(h->ev[3], h->ev[4]);
+        stats->t_recover_ms = elapsed_ms(h->ev[4], h->ev[5]);
+        stats->factor_flops = flops;
+        stats->block = s0->map.b;
+        stats->nblocks = s0->map.n;
+        stats->levels = (int)s0->steps.size() + 1;
+        stats->tc_gemm = s0->tc_used;
+        stats->device_bytes = bytes_all;
+        stats->gpu_launches = h->launches;
+        stats->factor_precision = h->fact_prec;
+        stats->fp64_fallback = h->fell_back;
+        stats->t_total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    }
+    if (!(rel <= h->tol))
+        return set_err(h, FDFD_ENOCONV, "refinement stopped at relative residual %.3e > tol %.1e after %d iterations",
+                       rel, h->tol, iters);
+    return FDFD_OK;
+}
+
 int fdfd_set_profiling(fdfd_handle* h, int on) {
     if (!h) return FDFD_EINVAL;
     prof_collect(h);
@@ -1344,6 +1688,7 @@ int fdfd_get_profile(fdfd_handle* h, fdfd_profile* out) {
 int fdfd_get_stencil(fdfd_handle* h, double* out) {
     if (!h || !out) return FDFD_EINVAL;
     if (!h->factored) return set_err(h, FDFD_EINVAL, "no assembled operator");
+    if (h->mf) return set_err(h, FDFD_EINVAL, "modulated device: one stencil per sideband, none exported");
     long long N = (long long)h->Nx * h->Ny;
     CK(cudaMemcpyAsync(out, h->st, 5 * N * sizeof(cplx<double>), cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
@@ -1353,7 +1698,8 @@ int fdfd_get_stencil(fdfd_handle* h, double* out) {
 int fdfd_apply(fdfd_handle* h, const double* x, int nrhs, double* y) {
     if (!h || !x || !y || nrhs < 1) return FDFD_EINVAL;
     if (!h->factored) return set_err(h, FDFD_EINVAL, "no assembled operator");
-    long long N = (long long)h->Nx * h->Ny;
+    if (h->mf && nrhs != 1) return set_err(h, FDFD_EINVAL, "modulated device: nrhs must be 1");
+    long long N = vlen(h);
     size_t bytes = (size_t)N * nrhs * sizeof(cplx<double>);
     cplx<double>* buf = nullptr;
     RET(dev_alloc(h, (void**)&buf, 2 * bytes));
@@ -1371,6 +1717,7 @@ int fdfd_apply(fdfd_handle* h, const double* x, int nrhs, double* y) {
 int fdfd_adjoint(fdfd_handle* h, const double* src, const double* mvec, double* J, double* grad, double* ez,
                  fdfd_stats* stats) {
     if (!h) return FDFD_EINVAL;
+    if (h->mf) return set_err(h, FDFD_EINVAL, "fdfd_adjoint: not defined for a modulated device");
     if (!src || !mvec || !J || !grad) return set_err(h, FDFD_EINVAL, "fdfd_adjoint: NULL argument");
     if (!h->factored || h->op != OP_TM_DRIVEN)
         return set_err(h, FDFD_EINVAL, "fdfd_adjoint needs a factored TM driven operator (fdfd_factor, FDFD_TM)");
@@ -1380,7 +1727,7 @@ int fdfd_adjoint(fdfd_handle* h, const double* src, const double* mvec, double* 
         if (!std::isfinite(src[k]) || !std::isfinite(mvec[k]))
             return set_err(h, FDFD_EINVAL, "fdfd_adjoint: non-finite input");
     const size_t bytes = (size_t)N * sizeof(cplx<double>);
-    RET(ensure_krylov(h, 2, 20));
+    RET(ensure_krylov(h, 2, restart_len(h, 2)));
     if (h->io_cap < 4 * bytes) {
         dev_free(h->io);
         h->io = nullptr;
@@ -1404,7 +1751,7 @@ int fdfd_adjoint(fdfd_handle* h, const double* src, const double* mvec, double* 
     LAUNCH(pscale_kernel, nb, 256, 0, h->Nx, h->Ny, h->sf, 0, d_m, h->kb + N);
     int iters = 0;
     double rel = 0;
-    RET(refine(h, 2, &iters, &rel));
+    RET(refine_fb(h, 2, &iters, &rel));
     LAUNCH(pscale_kernel, nb, 256, 0, h->Nx, h->Ny, h->sf, 1, h->kx + N, d_lam);
     // s = mᵀE (no conjugation), reduced on the host from per-block partials
     RET(ensure_part(h, 2 * 152));
@@ -1440,6 +1787,8 @@ int fdfd_adjoint(fdfd_handle* h, const double* src, const double* mvec, double* 
         stats->nblocks = h->map.n;
         stats->levels = (int)h->steps.size() + 1;
         stats->tc_gemm = h->tc_used;
+        stats->factor_precision = h->fact_prec;
+        stats->fp64_fallback = h->fell_back;
         stats->device_bytes = h->dev_bytes;
         stats->gpu_launches = h->launches;
         stats->t_total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
@@ -1453,6 +1802,7 @@ int fdfd_adjoint(fdfd_handle* h, const double* src, const double* mvec, double* 
 int fdfd_eigfreq(fdfd_handle* h, double omega0, int nev, int which, double tol, double* omega, double* lambda,
                  double* fields, fdfd_stats* stats) {
     if (!h) return FDFD_EINVAL;
+    if (h->mf) return set_err(h, FDFD_EINVAL, "fdfd_eigfreq: not defined for a modulated device");
     const long long N = (long long)h->Nx * h->Ny;
     if (!h->eps_set) return set_err(h, FDFD_EINVAL, "fdfd_set_eps must be called before fdfd_eigfreq");
     if (!(omega0 > 0) || nev < 1 || nev > 64 || nev >= N - 1 || !omega)
@@ -1476,7 +1826,7 @@ int fdfd_eigfreq(fdfd_handle* h, double omega0, int nev, int which, double tol, 
 
     // Arnoldi basis (m+1 vectors) on the device
     const int m = (int)std::min<long long>(N - 1, std::max(2 * nev + 24, 48));
-    RET(ensure_krylov(h, 2, 20));
+    RET(ensure_krylov(h, 2, restart_len(h, 2)));
     cplx<double>* V = nullptr;
     const size_t vbytes = (size_t)N * sizeof(cplx<double>);
     RET(dev_alloc(h, (void**)&V, vbytes * (m + 1)));
@@ -1527,7 +1877,7 @@ int fdfd_eigfreq(fdfd_handle* h, double omega0, int nev, int which, double tol, 
             CK(cudaMemcpyAsync(h->kb, V + (size_t)j * N, vbytes, cudaMemcpyDeviceToDevice, h->stream));
             int it = 0;
             double rr = 0;
-            RET(refine(h, 1, &it, &rr));
+            RET(refine_fb(h, 1, &it, &rr));
             iters += it;
             cplx<double>* w = V + (size_t)(j + 1) * N;
             CK(cudaMemcpyAsync(w, h->kx, vbytes, cudaMemcpyDeviceToDevice, h->stream));
@@ -1641,6 +1991,8 @@ int fdfd_eigfreq(fdfd_handle* h, double omega0, int nev, int which, double tol, 
         stats->nblocks = h->map.n;
         stats->levels = (int)h->steps.size() + 1;
         stats->tc_gemm = h->tc_used;
+        stats->factor_precision = h->fact_prec;
+        stats->fp64_fallback = h->fell_back;
         stats->device_bytes = h->dev_bytes;
         stats->gpu_launches = h->launches;
         stats->t_total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();

@@ -465,19 +465,16 @@ typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t,
                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
 EncodeTiledFn get_encode() {
-    static EncodeTiledFn fn = nullptr;
-    static bool tried = false;
-    if (!tried) {
-        tried = true;
+    static const EncodeTiledFn fn = [] {   // thread-safe static initialisation
         void* p = nullptr;
         cudaDriverEntryPointQueryResult q;
         if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
                 cudaSuccess &&
             q == cudaDriverEntryPointSuccess)
-            fn = (EncodeTiledFn)p;
-        else
-            cudaGetLastError();
-    }
+            return (EncodeTiledFn)p;
+        cudaGetLastError();
+        return (EncodeTiledFn) nullptr;
+    }();
     return fn;
 }
 
@@ -513,13 +510,9 @@ namespace {
 template <int BN>
 int tc_launch_bn(const GemmArgs<float>* g, const int* c_trans_arr, const CUtensorMap* mapA, const CUtensorMap* mapB,
                  int njobs, cudaStream_t stream) {
-    static bool attr = false;
-    if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(gemm_tc_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             TcTile<BN>::SMEM_BYTES);
-        if (e != cudaSuccess) return (int)e;
-        attr = true;
-    }
+    static const cudaError_t attr =
+        cudaFuncSetAttribute(gemm_tc_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, TcTile<BN>::SMEM_BYTES);
+    if (attr != cudaSuccess) return (int)attr;
     TcParams P;
     P.g = *g;
     if (c_trans_arr) P.g.c_trans_arr = c_trans_arr;

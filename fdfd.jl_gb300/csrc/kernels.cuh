@@ -2,7 +2,7 @@
 #pragma once
 #include "common.cuh"
 
-enum { OP_TM_DRIVEN = 0, OP_TE_DRIVEN = 1, OP_TM_EIGEN = 2, OP_TE_EIGEN = 3 };
+enum { OP_TM_DRIVEN = 0, OP_TE_DRIVEN = 1, OP_TM_EIGEN = 2, OP_TE_EIGEN = 3, OP_TM_SIDEBAND = 4 };
 enum { REC_TM_DRIVEN = 0, REC_TE_DRIVEN = 1, REC_TM_EIGEN = 2, REC_TE_EIGEN = 3 };
 
 struct SFactorArgs { int Nx, Ny, Npx, Npy; double dx, dy, omega, eps0n, eta0, m, lnR; };
@@ -29,6 +29,17 @@ __global__ void sfactor_kernel(SFactorArgs a, cplx<double>* out);
 __global__ void stencil_kernel(StencilArgs a, const cplx<double>* eps, const cplx<double>* sf, cplx<double>* st);
 __global__ void residual_kernel(int Nx, int Ny, int nrhs, const cplx<double>* st, const cplx<double>* x,
                                 const cplx<double>* b, cplx<double>* r, double* part);
+// Coupled sideband system of a modulated device: K = 2s+1 stencils (one per
+// sideband, each an OP_TM_SIDEBAND operator) and the couplings
+// ½ωₙ²ϵ₀ conj(Δϵ) (to sideband n+1) and ½ωₙ²ϵ₀ Δϵ (to n-1).
+#define MF_MAX_K 33
+struct MfResidualArgs {
+    int Nx, Ny, K;
+    const cplx<double>* st[MF_MAX_K];
+    double half_w2eps0[MF_MAX_K];   // ½ ωₙ² ϵ₀L₀
+};
+__global__ void residual_mf_kernel(MfResidualArgs a, const cplx<double>* deps, const cplx<double>* x,
+                                   const cplx<double>* b, cplx<double>* r, double* part);
 __global__ void reduce_partials_kernel(const double* part, int nblocks, int nvals, double* out);
 __global__ void recover_kernel(RecoverArgs a, const cplx<double>* sf, const cplx<double>* eps,
                                const cplx<double>* f, const cplx<double>* coef, cplx<double>* g1,

@@ -273,15 +273,14 @@ size_t gemv_smem(int tr, int b) {
 template <typename T, int R>
 int gemv_launch_r(cudaStream_t s, int tr, int njobs, const GemvArgs<T>& g) {
     constexpr int VW = 16 / sizeof(T);
-    static bool attr = false;
-    if (!attr) {
+    static const cudaError_t attr = [] {   // thread-safe static initialisation
         cudaError_t e = cudaFuncSetAttribute(gemv_n_kernel<T, R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              200 * 1024);
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(gemv_t_kernel<T, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        if (e != cudaSuccess) return (int)e;
-        attr = true;
-    }
+        return e;
+    }();
+    if (attr != cudaSuccess) return (int)attr;
     const size_t smem = gemv_smem<T, R>(tr, g.b);
     // Launch shape: the widest per-block tile that still gives about four blocks
     // per SM.  Small batches (the deep reduction levels) get narrow tiles, so

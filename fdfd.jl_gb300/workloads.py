@@ -194,3 +194,43 @@ def phc_cavity(n_cells=12, res=20, eps_rod=8.9, radius=0.2, npml=NPML, a_um=1.0,
     p = Problem("phc_cavity", N, N, dx, dx, (npml, npml), eps, src, omega0,
                 extra={"x0": x0})
     return p, omega0
+
+
+def modulated_waveguide(dh=0.02, L=5.0, nsidebands=1, npml=(15, 15), waist_um=0.2, sharedpml=True,
+                        mod_range=None):
+    """Interband photonic transition in a modulated waveguide, the setup of the
+    reference's own modulated-device test (test/runtests.jl:41-63): x ∈ [0, L],
+    y ∈ [-1, 1] µm at cell size dh, 15 PML cells, carrier ω = 2π·193.9 THz,
+    modulation Ω = 4.541e14 rad/s, a guide of width a = 0.2202 µm (ϵᵣ = 12.25)
+    and Δϵᵣ = exp(i q x), q = 2.9263 µm⁻¹, on the lower half of the guide for
+    x in ``mod_range`` (default [1, L-1]).  The reference drives the guide with a
+    mode source; here a Gaussian line source of waist ``waist_um`` across the
+    guide at x = 0.2 µm stands in.  PML grading is the reference default
+    (m = 3.5, lnR = -12).  ``extra`` holds deps, Omega, nsidebands, sharedpml."""
+    if np.isscalar(npml):
+        npml = (int(npml), int(npml))
+    x0, x1 = mod_range if mod_range is not None else (1.0, L - 1.0)
+    Nx, Ny = int(round(L / dh)), int(round(2.0 / dh))
+    xc = 0.0 + dh * (np.arange(Nx) + 0.5)
+    yc = -1.0 + dh * (np.arange(Ny) + 0.5)
+    X, Y = np.meshgrid(xc, yc, indexing="ij")
+    a, q = 0.2202, 2.9263
+    eps = np.ones((Nx, Ny), dtype=np.complex128)
+    eps[(-a / 2 <= Y) & (Y <= a / 2)] = 12.25
+    deps = np.zeros((Nx, Ny), dtype=np.complex128)
+    reg = (x0 <= X) & (X <= x1) & (-a / 2 <= Y) & (Y <= 0.0)
+    deps[reg] = np.exp(1j * q * X[reg])
+    src = np.zeros((Nx, Ny), dtype=np.complex128)
+    ix = int(round(0.2 / dh))
+    src[ix, :] = np.exp(-(yc / waist_um) ** 2)
+    return Problem(f"modulated_waveguide_{Nx}x{Ny}", Nx, Ny, dh, dh, tuple(npml), eps, src,
+                   2 * math.pi * 1.939e14, pml_m=3.5, pml_lnR=-12.0,
+                   extra={"deps": deps, "Omega": 4.541e14, "nsidebands": nsidebands, "sharedpml": sharedpml})
+
+
+def modulated_notebook(nsidebands=1):
+    """The modulated-waveguide example of the reference's notebook
+    (notebooks/Example_simulations.ipynb, the ModulatedDevice cell): dh = 0.01 µm,
+    x ∈ [0, 15], y ∈ [-1, 1] (1500 x 200 cells), PML 15 x 10 cells, modulation on
+    1.5 ≤ x ≤ 11.7, one sideband on each side of the carrier."""
+    return modulated_waveguide(dh=0.01, L=15.0, nsidebands=nsidebands, npml=(15, 10), mod_range=(1.5, 11.7))

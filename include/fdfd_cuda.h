@@ -68,6 +68,10 @@ typedef struct {
     int    tc_gemm;          /* 1 when the tcgen05 3xTF32 GEMM ran                   */
     long long device_bytes;  /* device memory held by the handle                     */
     long long gpu_launches;  /* kernels this library launched during the call        */
+    int    factor_precision; /* FDFD_PREC_* of the factor the refinement finished with */
+    int    fp64_fallback;    /* 1 when that factor is an FP64 re-factorization of an
+                                FDFD_PREC_MIXED handle (fdfd_set_fallback); its time
+                                counts in t_solve_ms                               */
 } fdfd_stats;
 
 /* Version string of the library. */
@@ -86,8 +90,20 @@ void fdfd_destroy(fdfd_handle* h);
 const char* fdfd_last_error(const fdfd_handle* h);
 
 /* Refinement stopping rule: ||b - A x||/||b|| <= tol within max_iter factor
- * solves (FDFD_REFINE_GMRES restarts every max_iter/… internally). */
+ * solves (FDFD_REFINE_GMRES restarts its Krylov basis every 20 solves). */
 int  fdfd_set_refinement(fdfd_handle* h, double tol, int max_iter, int mode);
+
+/* Basis length m of the restarted FGMRES refinement (0: automatic, the
+ * default).  The refinement holds 2m+1 FP64 vectors per right-hand side. */
+int  fdfd_set_restart(fdfd_handle* h, int m);
+
+/* FP64 fallback of an FDFD_PREC_MIXED handle (on by default).  When the
+ * refinement preconditioned by the FP32 factor is projected to miss tol
+ * within max_iter solves (measured rate per restart cycle), or stops above
+ * tol, the handle factors the same operator in FP64 and refines again; the
+ * FP64 factor then serves the following solves until the next factorization.
+ * Off: the call returns FDFD_ENOCONV instead.  No effect on FP64 handles. */
+int  fdfd_set_fallback(fdfd_handle* h, int on);
 
 /* Relative permittivity ϵᵣ (Device.ϵᵣ, src/device.jl:19-25), Nx*Ny complex.
  * Rejects NaN/Inf.  Invalidates any existing factorization. */
@@ -137,6 +153,39 @@ int  fdfd_adjoint(fdfd_handle* h, const double* src, const double* mvec,
 int  fdfd_eigfreq(fdfd_handle* h, double omega0, int nev, int which,
                   double tol, double* omega, double* lambda, double* fields,
                   fdfd_stats* stats);
+
+/* Modulated device (multi-frequency FDFD): replaces solve(d::ModulatedDevice)
+ * (src/solver/modulation.jl:35-119, TM only as the reference).  The handle
+ * holds K = 2*nsidebands+1 sideband operators
+ *   Aₙ = Sxb δxb μ₀⁻¹ Sxf δxf + Syb δyb μ₀⁻¹ Syf δyf + ωₙ² ϵ₀ϵᵣ,  ωₙ = ω + nΩ,
+ * n = -s..s, with the PML at ω (shared_pml != 0, the reference default) or at
+ * ωₙ, coupled by ½ωₙ² ϵ₀ conj(Δϵᵣ) to sideband n+1 and ½ωₙ² ϵ₀ Δϵᵣ to n-1
+ * (modulation.jl:91-99).  The coupled system is refined in FP64 (FGMRES) to
+ * the handle's tol, preconditioned by the K sideband factorizations, which
+ * are solved concurrently.  fdfd_set_eps, fdfd_set_refinement,
+ * fdfd_set_restart, fdfd_set_fallback, fdfd_apply (nrhs 1, K*Nx*Ny values,
+ * sideband-major) and fdfd_destroy accept the handle; fdfd_factor,
+ * fdfd_solve, fdfd_adjoint and fdfd_eigfreq reject it (FDFD_EINVAL).
+ * nsidebands in [0, 16]. */
+int  fdfd_mf_create(fdfd_handle** h, int Nx, int Ny, int Npx, int Npy, double dx,
+                    double dy, double L0, double pml_m, double pml_lnR,
+                    int nsidebands, int shared_pml, int precision);
+
+/* Modulation amplitude Δϵᵣ (ModulatedDevice.Δϵᵣ, setup_Δϵᵣ!,
+ * modulation.jl:26-30), Nx*Ny complex; zero after fdfd_mf_create. */
+int  fdfd_mf_set_deps(fdfd_handle* h, const double* deps_r);
+
+/* Assemble and factor the K sideband operators for carrier ω and modulation
+ * frequency Ω (ModulatedDevice.ω, .Ω); every ωₙ must be positive. */
+int  fdfd_mf_factor(fdfd_handle* h, double omega, double Omega);
+
+/* One source (Nx*Ny complex): b = iω·src in the centre sideband
+ * (modulation.jl:62-64).  Outputs (each may be NULL) hold K*Nx*Ny complex
+ * values, sideband n = -s..s in order: Ez and the forward-difference
+ * H = (-Syf δyf Ez, Sxf δxf Ez)/(iωₙμ₀) (modulation.jl:108-114).  Stats:
+ * iterations are applications of the block preconditioner. */
+int  fdfd_mf_solve(fdfd_handle* h, const double* src, double* ez, double* hx,
+                   double* hy, fdfd_stats* stats);
 
 /* Debug/parity: copy the assembled FP64 5-point stencil of the last factored
  * operator to the host: 5*Nx*Ny complex, planes [self, x-1, x+1, y-1, y+1]

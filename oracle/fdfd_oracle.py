@@ -354,5 +354,64 @@ def objective(g: Grid, eps_r, src, omega, mvec, m=3.5, lnR=-12.0):
     return abs(vec(mvec).astype(np.complex128) @ E) ** 2
 
 
+# --- multi-frequency (modulated) driven solve: src/solver/modulation.jl ------
+
+def modulated_system(g: Grid, eps_r, deps_r, omega: float, Omega: float, nsidebands: int,
+                     sharedpml=True, m=3.5, lnR=-12.0):
+    """Coupled sideband system of ``solve(d::ModulatedDevice)``:
+    src/solver/modulation.jl:35-119 (TM only, as the reference).
+
+    Frequencies ωₙ = ω + nΩ, n = -s..s (:44-50).  Per sideband
+    Aₙ = Sxb δxb μ₀⁻¹ Sxf δxf + Syb δyb μ₀⁻¹ Syf δyf + ωₙ² Tϵ with the PML at ω
+    (shared, :77-83) or at ωₙ (:85-89).  Couplings: block (n, n+1) =
+    ½ωₙ² conj(TΔϵ), block (n+1, n) = ½ωₙ₊₁² TΔϵ (:91-99).  Returns
+    (A, omegas, S) with S = [(Sxf, Syf)] per sideband (one entry when shared)."""
+    eps0, mu0, _ = normalize_parameters(g.L0)
+    K = 2 * nsidebands + 1
+    wn = omega + Omega * np.arange(-nsidebands, nsidebands + 1)
+    Te = sp.diags(eps0 * vec(np.asarray(eps_r, dtype=np.complex128)), 0)
+    TDe = sp.diags(eps0 * vec(np.asarray(deps_r, dtype=np.complex128)), 0)
+    dxb, dxf = delta(X, BACKWARD, g), delta(X, FORWARD, g)
+    dyb, dyf = delta(Y, BACKWARD, g), delta(Y, FORWARD, g)
+    blocks, S = [], []
+    for j in range(K if not sharedpml else 1):
+        Sxf, Sxb, Syf, Syb = S_create(g, omega if sharedpml else wn[j], m, lnR)
+        S.append((Sxf, Syf, Sxb @ dxb * (1 / mu0) @ Sxf @ dxf + Syb @ dyb * (1 / mu0) @ Syf @ dyf))
+    for j in range(K):
+        A1 = S[0 if sharedpml else j][2]
+        blocks.append(A1 + wn[j] ** 2 * Te)
+    A = sp.block_diag(blocks, format="csr")
+    if nsidebands > 0:
+        Cp = sp.kron(sp.diags(0.5 * wn[:-1] ** 2, 1), TDe.conj())
+        Cm = sp.kron(sp.diags(0.5 * wn[1:] ** 2, -1), TDe)
+        A = A + Cp + Cm
+    return A.tocsc(), wn, [(a, b) for a, b, _ in S]
+
+
+def solve_modulated(g: Grid, eps_r, deps_r, src, omega: float, Omega: float, nsidebands: int,
+                    sharedpml=True, m=3.5, lnR=-12.0):
+    """``solve(d::ModulatedDevice)`` for one ω: src/solver/modulation.jl:35-119.
+
+    b = iω·src in the centre sideband block (:62-64); Ez per sideband and
+    H with forward differences, hx = -Syf δyf ez/(iωₙμ₀), hy = Sxf δxf ez/(iωₙμ₀)
+    (:108-114).  Returns a list of K (Ez, Hx, Hy) triples, n = -s..s."""
+    eps0, mu0, _ = normalize_parameters(g.L0)
+    A, wn, S = modulated_system(g, eps_r, deps_r, omega, Omega, nsidebands, sharedpml, m, lnR)
+    N = g.N[0] * g.N[1]
+    K = len(wn)
+    b = np.zeros(K * N, dtype=np.complex128)
+    b[nsidebands * N:(nsidebands + 1) * N] = 1j * omega * vec(np.asarray(src, dtype=np.complex128))
+    ez = dolinearsolve(A, b)
+    dxf, dyf = delta(X, FORWARD, g), delta(Y, FORWARD, g)
+    out = []
+    for j in range(K):
+        e = ez[j * N:(j + 1) * N]
+        Sxf, Syf = S[0 if sharedpml else j]
+        hx = -1 / 1j / wn[j] / mu0 * (Syf @ (dyf @ e))
+        hy = 1 / 1j / wn[j] / mu0 * (Sxf @ (dxf @ e))
+        out.append((unvec(e, g.N), unvec(hx, g.N), unvec(hy, g.N)))
+    return out
+
+
 def relative_residual(A, x, b):
     return np.linalg.norm(b - A @ x) / np.linalg.norm(b)

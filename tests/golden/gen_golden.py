@@ -58,12 +58,24 @@ def eigen_case(name, p, omega0, pol, nev):
                         omega=w[order], lam=lam[order])
 
 
+def modulated_case(name, p):
+    g = grid_of(p)
+    e = p.extra
+    out = O.solve_modulated(g, p.eps, e["deps"], p.src, p.omega, e["Omega"], e["nsidebands"], e["sharedpml"],
+                            p.pml_m, p.pml_lnR)
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), Nx=p.Nx, Ny=p.Ny, npml=np.array(p.npml), dx=p.dx,
+                        dy=p.dy, omega=p.omega, Omega=e["Omega"], nsidebands=e["nsidebands"],
+                        sharedpml=e["sharedpml"], pml_m=p.pml_m, pml_lnR=p.pml_lnR, eps=p.eps, deps=e["deps"],
+                        src=p.src, ez=np.stack([o[0] for o in out]))
+
+
 def main():
     driven_case("tm_point_guide_60x40", W.point_source_guide(60, 40, npml=8), O.TM)
     driven_case("tm_design_48x72", W.design_guide(48, 72, design=(16, 20), seed=7, npml=8), O.TM)
     driven_case("te_design_64x40", W.design_guide(64, 40, design=(20, 12), seed=11, npml=8), O.TE)
     p, w0 = W.phc_cavity(n_cells=5, res=8, npml=8)
     eigen_case("tm_phc_eigen_56", p, w0, O.TM, 4)
+    modulated_case("tm_modulated_125x50", W.modulated_waveguide(dh=0.04, nsidebands=1))
     print("golden fixtures written to", HERE)
 
 

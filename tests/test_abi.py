@@ -53,4 +53,6 @@ def test_null_handle_calls_fail_cleanly(lib, fdfd):
     assert lib.fdfd_factor(None, 1.0) == E
     assert lib.fdfd_solve(None, None, 1, None, None, None, None) == E
     assert lib.fdfd_set_refinement(None, 1e-10, 10, 0) == E
+    assert lib.fdfd_set_fallback(None, 1) == E
+    assert lib.fdfd_set_restart(None, 20) == E
     lib.fdfd_destroy(None)

@@ -133,6 +133,36 @@ def test_point_guide_200x120(lib, fdfd, oracle):
         assert max(rel(f1, ref[0]), rel(f2, ref[1]), rel(f3, ref[2])) <= tol
 
 
+def test_fp64_fallback(lib, fdfd, oracle):
+    """A MIXED handle whose refinement cannot reach tol within max_iter solves
+    (one fewer than the FP32 factor needs) factors the operator again in FP64
+    and finishes with it; with the fallback off the call reports
+    FDFD_ENOCONV, and the next factorization is FP32 again."""
+    from fdfd_gb300 import workloads as W
+    p = W.point_source_guide()
+    ref = oracle_solve(oracle, p, oracle.TM)
+    h = handle_for(fdfd, p.Nx, p.Ny, p.npml, p.dx, p.dy, p.pml_m, p.pml_lnR, fdfd.TM, fdfd.FDFD_PREC_MIXED)
+    h.set_eps(p.eps)
+    h.factor(p.omega)
+    _, _, _, st = h.solve(p.src)
+    n_mixed = st.iterations
+    assert st.fp64_fallback == 0 and st.factor_precision == fdfd.FDFD_PREC_MIXED and n_mixed >= 3
+    h.set_refinement(TOL_RES, n_mixed - 1)
+    f1, f2, f3, st = h.solve(p.src)
+    assert st.fp64_fallback == 1 and st.factor_precision == fdfd.FDFD_PREC_FP64
+    assert st.rel_residual <= TOL_RES
+    assert max(rel(f1, ref[0]), rel(f2, ref[1]), rel(f3, ref[2])) <= TOL_FIELD_FP64
+    h.set_fallback(False)
+    h.factor(p.omega)
+    with pytest.raises(fdfd.FDFDError) as e:
+        h.solve(p.src)
+    assert e.value.code == fdfd._lib.FDFD_ENOCONV
+    h.set_refinement(TOL_RES, 40)
+    _, _, _, st = h.solve(p.src)
+    h.close()
+    assert st.fp64_fallback == 0 and st.factor_precision == fdfd.FDFD_PREC_MIXED and st.rel_residual <= TOL_RES
+
+
 def test_block_size_above_512(lib, fdfd):
     """Blocks of more than 512 unknowns take the two-rows-per-thread panel
     kernels (FP32 panel width 16, FP64 width 8).  Both factorizations must

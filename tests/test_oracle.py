@@ -155,3 +155,88 @@ def test_adjoint_gradient_matches_fd(oracle):
         fd = (oracle.objective(g, ep, src, w, m, 4.0, np.log(1e-8)) -
               oracle.objective(g, em, src, w, m, 4.0, np.log(1e-8))) / 2e-4
         assert abs(fd - grad[i, j]) <= 1e-5 * abs(grad[i, j]) + 1e-12 * J
+
+
+# ---------------------------------------------------------------------------
+# modulated device (src/solver/modulation.jl)
+# ---------------------------------------------------------------------------
+def test_modulated_blocks(oracle):
+    """Block structure of the coupled sideband matrix (modulation.jl:77-99):
+    diagonal blocks differ only by (ωₙ² - ω₀²)Tϵ under a shared PML, block
+    (n, n+1) is ½ωₙ² conj(TΔϵ), block (n+1, n) is ½ωₙ₊₁² TΔϵ."""
+    g = small_grid(oracle, N=(6, 5), npml=(1, 1), d=(0.1, 0.2))
+    rng = np.random.default_rng(1)
+    eps = rng.uniform(1, 4, g.N) + 0j
+    deps = rng.standard_normal(g.N) + 1j * rng.standard_normal(g.N)
+    w, W = 2.0e15, 3.0e14
+    A, wn, _ = oracle.modulated_system(g, eps, deps, w, W, 1, True, 4.0, -18.0)
+    A = A.toarray()
+    N = 30
+    eps0 = oracle.EPS0 * g.L0
+    blk = lambda i, j: A[i * N:(i + 1) * N, j * N:(j + 1) * N]
+    Te = np.diag(eps0 * oracle.vec(eps))
+    TDe = np.diag(eps0 * oracle.vec(deps))
+    assert np.allclose(wn, [w - W, w, w + W])
+    for n in range(3):
+        assert np.allclose(blk(n, n) - wn[n] ** 2 * Te, blk(1, 1) - wn[1] ** 2 * Te, rtol=0, atol=1e-9 * abs(A).max())
+    for n in range(2):
+        assert np.allclose(blk(n, n + 1), 0.5 * wn[n] ** 2 * TDe.conj(), rtol=1e-14, atol=0)
+        assert np.allclose(blk(n + 1, n), 0.5 * wn[n + 1] ** 2 * TDe, rtol=1e-14, atol=0)
+    assert not blk(0, 2).any() and not blk(2, 0).any()
+
+
+def test_sideband_operator_entries(oracle):
+    """Row of Sxb δxb μ₀⁻¹ Sxf δxf (modulation.jl:80): x-neighbour entries
+    sxb_i sxf_i/(dx²μ₀) (i+1) and sxb_i sxf_{i-1}/(dx²μ₀) (i-1), diagonal minus
+    their sum, with 1/s factors of S_create."""
+    g = small_grid(oracle, N=(6, 5), npml=(2, 1), d=(0.1, 0.2))
+    w = 2.0e15
+    eps = np.ones(g.N) + 0j
+    A, _, _ = oracle.modulated_system(g, eps, np.zeros(g.N), w, 0.0, 0, True, 4.0, -18.0)
+    A = A.tocsr()
+    _, mu0, _ = oracle.normalize_parameters(g.L0)
+    eps0 = oracle.EPS0 * g.L0
+    sxf = 1 / oracle.create_sfactor(oracle.X, oracle.FORWARD, g, w, 4.0, -18.0)
+    sxb = 1 / oracle.create_sfactor(oracle.X, oracle.BACKWARD, g, w, 4.0, -18.0)
+    syf = 1 / oracle.create_sfactor(oracle.Y, oracle.FORWARD, g, w, 4.0, -18.0)
+    syb = 1 / oracle.create_sfactor(oracle.Y, oracle.BACKWARD, g, w, 4.0, -18.0)
+    dx, dy = g.dx(), g.dy()
+    Nx, Ny = g.N
+    for ix, iy in [(0, 0), (2, 3), (5, 4), (1, 2)]:
+        k = ix + Nx * iy
+        kp, km = (ix + 1) % Nx + Nx * iy, (ix - 1) % Nx + Nx * iy
+        kyp, kym = ix + Nx * ((iy + 1) % Ny), ix + Nx * ((iy - 1) % Ny)
+        cxp = sxb[ix] * sxf[ix] / dx ** 2 / mu0
+        cxm = sxb[ix] * sxf[ix - 1] / dx ** 2 / mu0
+        cyp = syb[iy] * syf[iy] / dy ** 2 / mu0
+        cym = syb[iy] * syf[iy - 1] / dy ** 2 / mu0
+        assert np.isclose(A[k, kp], cxp, rtol=1e-13) and np.isclose(A[k, km], cxm, rtol=1e-13)
+        assert np.isclose(A[k, kyp], cyp, rtol=1e-13) and np.isclose(A[k, kym], cym, rtol=1e-13)
+        assert np.isclose(A[k, k], -(cxp + cxm + cyp + cym) + w ** 2 * eps0, rtol=1e-12)
+
+
+def test_modulated_without_pml_or_modulation_is_driven(oracle):
+    """Without PML the backward-outer sideband operator equals the driven TM
+    operator (periodic differences commute); with Δϵ = 0 the centre sideband
+    of solve(::ModulatedDevice) is then the driven field and the other
+    sidebands vanish."""
+    g = oracle.Grid((24, 18), (0, 0), ((0.0, 0.0), (24 * 0.08, 18 * 0.08)))
+    rng = np.random.default_rng(3)
+    eps = rng.uniform(1, 4, g.N) + 1j * rng.uniform(0.01, 0.1, g.N)
+    src = np.zeros(g.N, complex)
+    src[7, 9] = 1j
+    w = 2 * np.pi * oracle.C0 / 1.55e-6
+    out = oracle.solve_modulated(g, eps, np.zeros(g.N), src, w, 0.2 * w, 1, True)
+    ref = oracle.solve(g, eps, src, w, oracle.TM)
+    assert np.linalg.norm(out[1][0] - ref[0]) <= 1e-10 * np.linalg.norm(ref[0])
+    assert np.abs(out[0][0]).max() == 0 and np.abs(out[2][0]).max() == 0
+
+
+def test_modulated_golden_regression(oracle):
+    g = np.load(os.path.join(GOLD, "tm_modulated_125x50.npz"))
+    Nx, Ny = int(g["Nx"]), int(g["Ny"])
+    grid = oracle.Grid((Nx, Ny), tuple(g["npml"]), ((0.0, 0.0), (Nx * float(g["dx"]), Ny * float(g["dy"]))))
+    out = oracle.solve_modulated(grid, g["eps"], g["deps"], g["src"], float(g["omega"]), float(g["Omega"]),
+                                 int(g["nsidebands"]), bool(g["sharedpml"]), float(g["pml_m"]), float(g["pml_lnR"]))
+    ez = np.stack([o[0] for o in out])
+    assert np.linalg.norm(ez - g["ez"]) <= 1e-12 * np.linalg.norm(g["ez"])
