@@ -274,10 +274,53 @@ def run_extras(L, pkg, W, a):
     except Exception as e:   # reported, not hidden
         out["modulated"] = {"error": str(e)}
     try:
+        out["mode_sources"] = run_mode_sources(L, pkg, W)
+    except Exception as e:   # reported, not hidden
+        out["mode_sources"] = {"error": str(e)}
+    try:
         out["mixed_batch"] = run_mixed_batch(L, pkg, W)
     except Exception as e:
         out["mixed_batch"] = {"error": str(e)}
     return out
+
+
+def run_mode_sources(L, pkg, W):
+    """Mode sources for the 64 wavelengths of the sweep band (λ ∈ [1.45, 1.65] µm) on the reference's
+    waveguide test grid (500x100 at dh = 0.02 µm, guide ϵᵣ = 12 of 0.3 µm): one TM mode (slice width
+    0.8 µm, n_eff 3.5) per wavelength, all 64 mode problems and source arrays in one call; the same
+    64 mode problems with the oracle (scipy ARPACK shift-invert) on one host core beside it."""
+    import numpy as np
+    Nx, Ny, dh = 500, 100, 0.02
+    yc = -1.0 + dh * (np.arange(Ny) + 0.5)
+    eps = np.ones((Nx, Ny), dtype=np.complex128)
+    eps[:, np.abs(yc) <= 0.15] = 12.0
+    lams = np.linspace(1.45, 1.65, 64)
+    omegas = np.array([W.omega_of(l) for l in lams])
+    mode = (L.FDFD_TM, L.FDFD_X, 50, Ny // 2, 0.8, 3.5)
+    h = L.Handle(Nx, Ny, 15, 15, dh, dh, 1e-6, 3.5, -12.0, pkg.TM, L.FDFD_PREC_MIXED)
+    h.set_eps(eps)
+    h.mode_sources(omegas, [mode])
+    n = 5
+    t0 = time.perf_counter()
+    for _ in range(n):
+        h.mode_sources(omegas, [mode])
+    t = (time.perf_counter() - t0) / n
+    h.close()
+    res = {"modes_per_s": len(omegas) / t, "ms_per_call": 1e3 * t, "modes_per_call": len(omegas),
+           "workload": "64 TM modes (41-cell slices) of the 500x100 waveguide test grid, sources in and out of "
+                       "host memory, one call"}
+    try:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import fdfd_oracle as O
+        g = O.Grid((Nx, Ny), (15, 15), ((0.0, -1.0), (Nx * dh, 1.0)))
+        t0 = time.perf_counter()
+        for w in omegas[:16]:
+            O.get_modes(g, eps, 1, w, 3.5, 1, 50, Ny // 2, O.X, 0.8)
+        tc = (time.perf_counter() - t0) / 16
+        res["cpu_oracle_modes_per_s"] = 1.0 / tc
+    except Exception as e:   # reported, not hidden
+        res["cpu_oracle_modes_per_s"] = {"error": str(e)}
+    return res
 
 
 def run_mixed_batch(L, pkg, W):

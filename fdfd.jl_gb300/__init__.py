@@ -24,9 +24,9 @@ import numpy as np
 from . import _lib
 from ._lib import FDFDError, FDFD_PREC_FP64, FDFD_PREC_MIXED  # noqa: F401
 
-__all__ = ["EPS0", "MU0", "C0", "ETA0", "TM", "TE", "Grid", "Device", "ModulatedDevice", "Point", "setup_eps",
-           "setup_src", "setup_deps", "solve", "eigenfrequency", "FieldTM", "FieldTE", "normalize_parameters",
-           "FDFDError"]
+__all__ = ["EPS0", "MU0", "C0", "ETA0", "TM", "TE", "X", "Y", "Grid", "Device", "ModulatedDevice", "Point", "Mode",
+           "setup_eps", "setup_src", "setup_deps", "add_mode", "setup_mode", "get_modes", "solve", "eigenfrequency",
+           "FieldTM", "FieldTE", "normalize_parameters", "FDFDError"]
 
 # src/types.jl:6-9
 EPS0 = 8.85418782e-12
@@ -35,6 +35,7 @@ C0 = math.sqrt(1 / EPS0 / MU0)
 ETA0 = math.sqrt(MU0 / EPS0)
 DEFAULT_L0 = 1e-6          # src/grid.jl:31
 TM, TE = _lib.FDFD_TM, _lib.FDFD_TE   # src/types.jl:20
+X, Y = _lib.FDFD_X, _lib.FDFD_Y       # src/types.jl:18 (x̂, ŷ)
 
 
 @dataclass
@@ -86,6 +87,17 @@ class Grid:
         ix = int(round((pt.x - self.bounds[0][0]) / self.L[0] * self.N[0]) + 1)
         iy = int(round((pt.y - self.bounds[0][1]) / self.L[1] * self.N[1]) + 1)
         return min(max(ix, 1), self.N[0]) - 1, min(max(iy, 1), self.N[1]) - 1
+
+
+@dataclass
+class Mode:
+    """src/device.jl:7-13: polarization, slice normal (X or Y), effective-index
+    guess, centre point and slice width (L₀ units)."""
+    pol: int
+    dir: int
+    neff: complex
+    pt: Point
+    width: float
 
 
 def normalize_parameters(g: Grid):
@@ -165,6 +177,51 @@ def setup_deps(d: ModulatedDevice, region, value):
     d.deps[m] = np.vectorize(value)(X, Y)[m] if callable(value) else value
 
 
+def add_mode(d, mode: Mode):
+    """add_mode!(d, mode): src/device.jl:111-114."""
+    d.modes.append(mode)
+
+
+def _mode_spec(d, m: Mode, pol=None):
+    ix, iy = d.grid.coord2ind(m.pt if isinstance(m.pt, Point) else Point(*m.pt))
+    return (m.pol if pol is None else pol, m.dir, ix, iy, m.width, m.neff)
+
+
+def _mode_handle(d):
+    g = d.grid
+    h = _lib.Handle(g.N[0], g.N[1], g.Npml[0], g.Npml[1], g.dx(), g.dy(), g.L0, 3.5, -12.0, TM, FDFD_PREC_MIXED)
+    h.set_eps(d.eps)
+    return h
+
+
+def get_modes(d, pol, omega, neff, nmodes, pt: Point, slicenormal, slicewidth):
+    """get_modes(d, pol, ω, neff, nmodes, pt, slicenormal, slicewidth): src/device.jl:122-149, computed on
+    the GPU (nmodes = 1).  Returns (β, vector, indx, indy) with 0-based slice indices."""
+    if nmodes != 1:
+        raise FDFDError(_lib.FDFD_EINVAL, "get_modes: the GPU mode solver returns one mode (nmodes = 1)")
+    h = _mode_handle(d)
+    try:
+        ix, iy = d.grid.coord2ind(pt if isinstance(pt, Point) else Point(*pt))
+        beta, v = h.get_mode(omega, pol, slicenormal, ix, iy, slicewidth, neff)
+    finally:
+        h.close()
+    M = (v.size - 1) // 2
+    if slicenormal == X:
+        return beta, v, ix, np.arange(iy - M, iy + M + 1)
+    return beta, v, np.arange(ix - M, ix + M + 1), iy
+
+
+def setup_mode(d, pol, omega, neff, pt: Point, srcnormal, srcwidth):
+    """setup_mode!(d, pol, ω, neff, pt, srcnormal, srcwidth): src/device.jl:116-120 — adds
+    normalize(abs.(v)) to d.src on the slice."""
+    h = _mode_handle(d)
+    try:
+        m = Mode(pol, srcnormal, neff, pt, srcwidth)
+        d.src = d.src + h.mode_sources([omega], [_mode_spec(d, m)])[0]
+    finally:
+        h.close()
+
+
 globals()["setup_ϵᵣ"] = setup_eps
 globals()["setup_Δϵᵣ"] = setup_deps
 
@@ -224,12 +281,16 @@ def solve(d: Device, pol=TM, precision="mixed", pml_m=3.5, pml_lnR=-12.0, tol=1e
     """
     if isinstance(d, ModulatedDevice):
         return solve_modulated(d, precision, pml_m, pml_lnR, tol, max_iter, return_stats)
-    if d.modes:
-        raise FDFDError(_lib.FDFD_EINVAL, "mode sources are not supported by the GPU solve path")
     h = make_handle(d, pol, precision, pml_m, pml_lnR, tol, max_iter)
     out, stats = [], []
     try:
-        for w in d.omega:
+        if d.modes:
+            # driven.jl:15-19: per ω the source is reset and rebuilt from the modes
+            # (TM profiles, as the reference's loop passes TM); all ω in one launch
+            srcs = h.mode_sources(d.omega, [_mode_spec(d, m, TM) for m in d.modes])
+        for i, w in enumerate(d.omega):
+            if d.modes:
+                d.src = srcs[i].copy()
             h.factor(w)
             f1, f2, f3, st = h.solve(d.src)
             cls = FieldTM if pol == TM else FieldTE
@@ -249,8 +310,6 @@ def solve_modulated(d: ModulatedDevice, precision="mixed", pml_m=3.5, pml_lnR=-1
     refined solve of the coupled system.  Returns an Nω x (2s+1) nested list of
     FieldTM (the reference's ``Array{FieldTM}(undef, Nω, nfrequencies)``), the
     field of sideband n = -s..s carrying ωₙ = ω + nΩ."""
-    if d.modes:
-        raise FDFDError(_lib.FDFD_EINVAL, "mode sources are not supported by the GPU solve path")
     g = d.grid
     h = _lib.ModulatedHandle(g.N[0], g.N[1], g.Npml[0], g.Npml[1], g.dx(), g.dy(), d.nsidebands, g.L0, pml_m,
                              pml_lnR, d.sharedpml, _prec(precision))
@@ -259,7 +318,11 @@ def solve_modulated(d: ModulatedDevice, precision="mixed", pml_m=3.5, pml_lnR=-1
         h.set_refinement(tol, max_iter)
         h.set_eps(d.eps)
         h.set_deps(d.deps)
-        for w in d.omega:
+        if d.modes:
+            srcs = h.mode_sources(d.omega, [_mode_spec(d, m, TM) for m in d.modes])   # modulation.jl:51-56
+        for i, w in enumerate(d.omega):
+            if d.modes:
+                d.src = srcs[i].copy()
             h.factor(w, d.Omega)
             ez, hx, hy, st = h.solve(d.src)
             wn = [w + d.Omega * n for n in range(-d.nsidebands, d.nsidebands + 1)]

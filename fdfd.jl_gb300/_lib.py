@@ -21,11 +21,13 @@ STATUS_NAMES = {0: "FDFD_OK", 1: "FDFD_EINVAL", 2: "FDFD_ENOMEM", 3: "FDFD_ESING
 FDFD_TM, FDFD_TE = 1, 2
 FDFD_PREC_FP64, FDFD_PREC_MIXED = 0, 1
 FDFD_REFINE_GMRES, FDFD_REFINE_CLASSIC = 0, 1
+FDFD_X, FDFD_Y = 1, 2
+FDFD_MODE_MAX_POINTS = 1023
 
 # every symbol include/fdfd_cuda.h declares
 EXPORTS = ["fdfd_version", "fdfd_create", "fdfd_destroy", "fdfd_last_error", "fdfd_set_refinement",
            "fdfd_set_fallback", "fdfd_set_restart", "fdfd_mf_create", "fdfd_mf_set_deps", "fdfd_mf_factor",
-           "fdfd_mf_solve",
+           "fdfd_mf_solve", "fdfd_get_mode", "fdfd_mode_sources",
            "fdfd_set_eps", "fdfd_factor", "fdfd_solve", "fdfd_solve_device", "fdfd_adjoint", "fdfd_eigfreq",
            "fdfd_get_stencil", "fdfd_apply", "fdfd_set_profiling", "fdfd_get_profile", "fdfd_residual_noalloc",
            "fdfd_debug_hessenberg_eig", "fdfd_debug_gemm"]
@@ -42,6 +44,12 @@ class Stats(C.Structure):
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class Mode(C.Structure):
+    """fdfd_mode: one mode source (Mode, src/device.jl:7-13)."""
+    _fields_ = [("pol", C.c_int), ("normal", C.c_int), ("ix", C.c_int), ("iy", C.c_int), ("width", C.c_double),
+                ("neff_re", C.c_double), ("neff_im", C.c_double)]
 
 
 class Profile(C.Structure):
@@ -94,6 +102,10 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.fdfd_mf_factor.argtypes = [vp, C.c_double, C.c_double]
     lib.fdfd_mf_solve.restype = ip
     lib.fdfd_mf_solve.argtypes = [vp, dp, dp, dp, dp, C.POINTER(Stats)]
+    lib.fdfd_get_mode.restype = ip
+    lib.fdfd_get_mode.argtypes = [vp, C.c_double, C.POINTER(Mode), ip, dp, dp, C.POINTER(C.c_int)]
+    lib.fdfd_mode_sources.restype = ip
+    lib.fdfd_mode_sources.argtypes = [vp, ip, dp, ip, C.POINTER(Mode), dp]
     lib.fdfd_set_eps.restype = ip
     lib.fdfd_set_eps.argtypes = [vp, dp]
     lib.fdfd_factor.restype = ip
@@ -230,6 +242,25 @@ class Handle:
         f = np.stack([np.stack([from_natural(flds[i, c], self.Nx, self.Ny)[0] for c in range(3)])
                       for i in range(nev)])
         return om, lam, f, st
+
+    def get_mode(self, omega, pol, normal, ix, iy, width, neff):
+        """Guided mode of the slice -> (beta (complex), vector (npts,) complex)."""
+        m = Mode(int(pol), int(normal), int(ix), int(iy), float(width), float(np.real(neff)), float(np.imag(neff)))
+        vec = np.empty(FDFD_MODE_MAX_POINTS, dtype=np.complex128)
+        beta = np.empty(1, dtype=np.complex128)
+        npts = C.c_int(0)
+        self._check(self.lib.fdfd_get_mode(self.h, float(omega), C.byref(m), vec.size, cptr(beta), cptr(vec),
+                                           C.byref(npts)))
+        return complex(beta[0]), vec[:npts.value].copy()
+
+    def mode_sources(self, omegas, modes):
+        """modes: sequence of (pol, normal, ix, iy, width, neff) -> src (nw, Nx, Ny) complex."""
+        om = np.ascontiguousarray(np.atleast_1d(np.asarray(omegas, dtype=np.float64)))
+        arr = (Mode * len(modes))(*[Mode(int(p), int(nrm), int(ix), int(iy), float(w), float(np.real(n)),
+                                         float(np.imag(n))) for p, nrm, ix, iy, w, n in modes])
+        out = np.empty(om.size * self.Nx * self.Ny, dtype=np.complex128)
+        self._check(self.lib.fdfd_mode_sources(self.h, om.size, cptr(om), len(modes), arr, cptr(out)))
+        return from_natural(out, self.Nx, self.Ny)
 
     def set_profiling(self, on=True):
         self._check(self.lib.fdfd_set_profiling(self.h, 1 if on else 0))

@@ -119,6 +119,8 @@ struct fdfd_handle {
     int nsb = 1;                     // Krylov vector length in units of Nx*Ny (K for a modulated device)
     MfState* mf = nullptr;           // modulated device state (fdfd_mf_create), else null
     double mf_factor_ms = 0;         // wall time of the last fdfd_mf_factor
+    unsigned char* mode_buf = nullptr;   // guided-mode scratch (jobs, vectors, sources)
+    size_t mode_cap = 0;
     bool fell_back = false;          // the current factor is such an FP64 re-factorization
     NodeMap map;
     // state
@@ -1317,7 +1319,7 @@ void fdfd_destroy(fdfd_handle* h) {
         h->mf = nullptr;
     }
     void* bufs[] = {h->eps, h->sf, h->st, h->derr, h->part, h->red, h->kb, h->kx, h->kr, h->kV, h->kZ, h->kc, h->io,
-                    h->djobs};
+                    h->djobs, h->mode_buf};
     for (void* p : bufs) dev_free(p);
     free_store(h->f32);
     free_store(h->f64);
@@ -1668,6 +1670,135 @@ int fdfd_mf_solve(fdfd_handle* h, const double* src, double* ez, double* hx, dou
         return set_err(h, FDFD_ENOCONV, "refinement stopped at relative residual %.3e > tol %.1e after %d iterations",
                        rel, h->tol, iters);
     return FDFD_OK;
+}
+
+// ---- guided modes and mode sources (get_modes, setup_mode!, eigenmode) ------
+namespace {
+
+// slice of one Mode (device.jl:122-143): srcpoints = round(width/dh), made odd,
+// centred on (ix, iy) across the slice normal; shift σ = (ω n_eff/c₀)² (eigen.jl:22)
+int mode_job(fdfd_handle* h, const fdfd_mode* md, double omega, ModeJob* J) {
+    if (!md) return set_err(h, FDFD_EINVAL, "mode is NULL");
+    if (md->normal != FDFD_X && md->normal != FDFD_Y) return set_err(h, FDFD_EINVAL, "mode normal must be FDFD_X or FDFD_Y");
+    if (md->pol != FDFD_TM && md->pol != FDFD_TE) return set_err(h, FDFD_EINVAL, "mode polarization must be TM or TE");
+    if (!(md->width > 0) || !std::isfinite(md->width) || !std::isfinite(md->neff_re) || !std::isfinite(md->neff_im))
+        return set_err(h, FDFD_EINVAL, "mode width must be positive, n_eff finite");
+    if (!(omega > 0) || !std::isfinite(omega)) return set_err(h, FDFD_EINVAL, "omega must be positive and finite");
+    if (md->ix < 0 || md->ix >= h->Nx || md->iy < 0 || md->iy >= h->Ny)
+        return set_err(h, FDFD_EINVAL, "mode centre (%d, %d) outside the grid", md->ix, md->iy);
+    const bool xn = md->normal == FDFD_X;
+    const double dh = xn ? h->dy : h->dx;
+    long long pts = (long long)std::nearbyint(md->width / dh);   // round half to even, as Julia's round
+    if (pts % 2 == 0) pts += 1;
+    const long long M = (pts - 1) / 2;
+    if (pts < 3 || pts > FDFD_MODE_MAX_POINTS)
+        return set_err(h, FDFD_EINVAL, "mode slice of %lld cells (3..%d)", pts, FDFD_MODE_MAX_POINTS);
+    const int c = xn ? md->iy : md->ix, lim = xn ? h->Ny : h->Nx;
+    if (c - M < 0 || c + M >= lim) return set_err(h, FDFD_EINVAL, "mode slice leaves the grid");
+    J->pol = md->pol;
+    J->n = (int)pts;
+    J->k0 = xn ? md->ix + (long long)h->Nx * (c - M) : (c - M) + (long long)h->Nx * md->iy;
+    J->stride = xn ? h->Nx : 1;
+    J->dh = dh;
+    J->omega = omega;
+    const double k = omega / (std::sqrt(1.0 / kEPS0 / kMU0) / h->L0);
+    const zd sb = zd(k * md->neff_re, k * md->neff_im);
+    const zd sg = sb * sb;
+    J->sig_re = sg.real();
+    J->sig_im = sg.imag();
+    J->out_off = 0;
+    J->pad = 0;
+    return FDFD_OK;
+}
+
+// solves the jobs (one per (frequency, mode)); optionally builds nw source arrays
+int run_modes(fdfd_handle* h, std::vector<ModeJob>& jobs, const std::vector<int>& job_start, bool want_src,
+              std::vector<zd>* beta, std::vector<zd>* vecs, double* src_host) {
+    if (!h->eps_set) return set_err(h, FDFD_EINVAL, "fdfd_set_eps must be called before the mode solve");
+    const int nj = (int)jobs.size();
+    const int nw = (int)job_start.size() - 1;
+    int tot = 0, nmax = 0;
+    for (ModeJob& J : jobs) {
+        J.out_off = tot;
+        tot += J.n;
+        nmax = std::max(nmax, J.n);
+    }
+    const long long N = (long long)h->Nx * h->Ny;
+    auto al = [](size_t b) { return (b + 255) / 256 * 256; };
+    const size_t o_jobs = 0, o_start = al(o_jobs + nj * sizeof(ModeJob)), o_beta = al(o_start + (nw + 1) * sizeof(int)),
+                 o_it = al(o_beta + nj * sizeof(zd)), o_vec = al(o_it + nj * sizeof(int)),
+                 o_src = al(o_vec + (size_t)tot * sizeof(zd)),
+                 need = o_src + (want_src ? (size_t)nw * N * sizeof(zd) : 0);
+    if (h->mode_cap < need) {
+        dev_free(h->mode_buf);
+        h->mode_buf = nullptr;
+        h->dev_bytes -= (long long)h->mode_cap;
+        h->mode_cap = 0;
+        RET(dev_alloc(h, (void**)&h->mode_buf, need));
+        h->mode_cap = need;
+    }
+    unsigned char* B = h->mode_buf;
+    CK(cudaMemcpyAsync(B + o_jobs, jobs.data(), nj * sizeof(ModeJob), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(B + o_start, job_start.data(), (nw + 1) * sizeof(int), cudaMemcpyHostToDevice, h->stream));
+    int rc = launch_modes(h->stream, nj, nmax, (const ModeJob*)(B + o_jobs), h->eps, kEPS0 * h->L0, kMU0 * h->L0,
+                          (cplx<double>*)(B + o_beta), (cplx<double>*)(B + o_vec), (int*)(B + o_it), h->derr);
+    h->launches++;
+    if (rc != 0) return set_err(h, FDFD_ECUDA, "mode kernel launch: %s", cudaGetErrorString((cudaError_t)rc));
+    if (want_src) {
+        CK(cudaMemsetAsync(B + o_src, 0, (size_t)nw * N * sizeof(zd), h->stream));
+        launch_mode_src(h->stream, nw, (const ModeJob*)(B + o_jobs), (const int*)(B + o_start),
+                        (const cplx<double>*)(B + o_vec), N, (cplx<double>*)(B + o_src));
+        h->launches++;
+        RET(check_launch(h, "mode sources"));
+        CK(cudaMemcpyAsync(src_host, B + o_src, (size_t)nw * N * sizeof(zd), cudaMemcpyDeviceToHost, h->stream));
+    }
+    std::vector<int> its(nj);
+    CK(cudaMemcpyAsync(its.data(), B + o_it, nj * sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    if (beta) {
+        beta->resize(nj);
+        CK(cudaMemcpyAsync(beta->data(), B + o_beta, nj * sizeof(zd), cudaMemcpyDeviceToHost, h->stream));
+    }
+    if (vecs) {
+        vecs->resize(tot);
+        CK(cudaMemcpyAsync(vecs->data(), B + o_vec, (size_t)tot * sizeof(zd), cudaMemcpyDeviceToHost, h->stream));
+    }
+    RET(check_device(h, "mode solve"));   // synchronises
+    for (int j = 0; j < nj; ++j)
+        if (its[j] < 0)
+            return set_err(h, FDFD_ENOCONV, "mode job %d: inverse iteration did not converge in %d steps", j, -its[j]);
+    return FDFD_OK;
+}
+
+}  // namespace
+
+int fdfd_get_mode(fdfd_handle* h, double omega, const fdfd_mode* mode, int cap, double* beta, double* vec,
+                  int* npts) {
+    if (!h) return FDFD_EINVAL;
+    if (!beta || !vec || !npts) return set_err(h, FDFD_EINVAL, "fdfd_get_mode: NULL argument");
+    std::vector<ModeJob> jobs(1);
+    RET(mode_job(h, mode, omega, &jobs[0]));
+    *npts = jobs[0].n;
+    if (cap < jobs[0].n) return set_err(h, FDFD_EINVAL, "vec holds %d values, the slice has %d", cap, jobs[0].n);
+    std::vector<zd> b, v;
+    RET(run_modes(h, jobs, std::vector<int>{0, 1}, false, &b, &v, nullptr));
+    beta[0] = b[0].real();
+    beta[1] = b[0].imag();
+    memcpy(vec, v.data(), v.size() * sizeof(zd));
+    return FDFD_OK;
+}
+
+int fdfd_mode_sources(fdfd_handle* h, int nw, const double* omegas, int nmodes, const fdfd_mode* modes, double* src) {
+    if (!h) return FDFD_EINVAL;
+    if (nw < 1 || nmodes < 1 || !omegas || !modes || !src)
+        return set_err(h, FDFD_EINVAL, "fdfd_mode_sources: invalid arguments");
+    std::vector<ModeJob> jobs((size_t)nw * nmodes);
+    std::vector<int> start(nw + 1);
+    for (int w = 0; w < nw; ++w) {
+        start[w] = w * nmodes;
+        for (int m = 0; m < nmodes; ++m) RET(mode_job(h, &modes[m], omegas[w], &jobs[(size_t)w * nmodes + m]));
+    }
+    start[nw] = nw * nmodes;
+    return run_modes(h, jobs, start, true, nullptr, nullptr, src);
 }
 
 int fdfd_set_profiling(fdfd_handle* h, int on) {

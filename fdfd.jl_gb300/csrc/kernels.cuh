@@ -99,6 +99,26 @@ void launch_madd(cudaStream_t s, int njobs, Pool<T> P, const int3* jobs);
 template <typename T>
 void launch_mcopy(cudaStream_t s, int njobs, Pool<T> S, Pool<T> Dp, const int3* jobs);
 
+// ---- modes.cu -------------------------------------------------------------------
+// One guided-mode job: the 1-D slice of n cells starting at natural index k0,
+// step `stride`, cell size dh, polarization pol (1 TM, 2 TE), shift σ =
+// (ω n_eff/c₀)²; its unit vector goes to vecs[out_off .. out_off+n).
+#define FDFD_MODE_MAX_POINTS 1023
+struct ModeJob {
+    int pol, n;
+    long long k0, stride;
+    double dh, omega, sig_re, sig_im;
+    int out_off, pad;
+};
+size_t mode_smem_bytes(int nmax);
+// beta[job] = √λ, vecs: unit eigenvectors, iters[job]: inverse-iteration steps
+// (negative: no convergence).  Returns a cudaError_t value.
+int launch_modes(cudaStream_t s, int njobs, int nmax, const ModeJob* jobs, const cplx<double>* eps, double eps0n,
+                 double mu0n, cplx<double>* beta, cplx<double>* vecs, int* iters, unsigned* err);
+// src[w] += |v| of the jobs job_start[w] .. job_start[w+1]-1 (nw frequencies, N cells each)
+void launch_mode_src(cudaStream_t s, int nw, const ModeJob* jobs, const int* job_start, const cplx<double>* vecs,
+                     long long N, cplx<double>* src);
+
 // ---- gemm_simt.cu / gemm_tc.cu --------------------------------------------
 // Batched complex "TN" GEMM on planar pools:
 //   C[m][n] = beta(m,n)·Cin[src(m)][n] + alpha·Σ_k A[m][k]·B[n][k]

@@ -46,6 +46,9 @@ extern "C" {
 #define FDFD_REFINE_GMRES   0  /* flexible GMRES in FP64, factor as preconditioner */
 #define FDFD_REFINE_CLASSIC 1  /* x += M^-1 (b - A x)                              */
 
+#define FDFD_X 1           /* src/types.jl:18 (@enum Direction x̂=1 ŷ=2) */
+#define FDFD_Y 2
+
 #define FDFD_WHICH_LM 0    /* eigenvalues of A nearest sigma (ARPACK :LM in shift-invert) */
 #define FDFD_WHICH_LR 1    /* largest real part of 1/(λ-σ) (ARPACK :LR in shift-invert)  */
 
@@ -153,6 +156,38 @@ int  fdfd_adjoint(fdfd_handle* h, const double* src, const double* mvec,
 int  fdfd_eigfreq(fdfd_handle* h, double omega0, int nev, int which,
                   double tol, double* omega, double* lambda, double* fields,
                   fdfd_stats* stats);
+
+/* A mode source (Mode, src/device.jl:7-13): polarization, slice normal
+ * (FDFD_X: the slice runs along y at column ix; FDFD_Y: along x at row iy),
+ * centre cell (0-based: coord2ind(grid, Mode.pt) - 1), slice width in L0
+ * units and the effective-index guess n_eff. */
+typedef struct {
+    int    pol;
+    int    normal;
+    int    ix, iy;
+    double width;
+    double neff_re, neff_im;
+} fdfd_mode;
+
+/* Guided mode of a grid slice: get_modes with nmodes = 1 (src/device.jl:122-149)
+ * and the 1-D eigenmode it calls (src/solver/eigen.jl:6-29).  The slice has
+ * round(width/dh) cells, made odd (*npts), of the handle's ϵᵣ; the periodic
+ * 1-D operator A = ω²μ₀Tϵ + δxf δxb (TM) or ω²μ₀Tϵ + Tϵ δxf Tϵxinv δxb (TE)
+ * gives the eigenpair nearest (ω n_eff/c₀)², found by shift-invert
+ * iteration on the GPU.  beta: 1 complex (√λ, principal branch); vec: *npts
+ * complex values (cap = its capacity), unit 2-norm, largest entry real and
+ * positive.  A slice leaving the grid, or of fewer than 3 or more than 1023
+ * cells, is FDFD_EINVAL. */
+int  fdfd_get_mode(fdfd_handle* h, double omega, const fdfd_mode* mode, int cap,
+                   double* beta, double* vec, int* npts);
+
+/* Mode sources for nw frequencies (driven.jl:15-19 with setup_mode!,
+ * device.jl:116-120): src (nw*Nx*Ny complex, host) is overwritten with, per
+ * frequency, the sum over the nmodes modes of normalize(abs.(v)) on each
+ * mode's slice.  All nw*nmodes mode problems run in one launch (a warp each).
+ * Like the reference's solve loop, callers pass pol = FDFD_TM for sources. */
+int  fdfd_mode_sources(fdfd_handle* h, int nw, const double* omegas, int nmodes,
+                       const fdfd_mode* modes, double* src);
 
 /* Modulated device (multi-frequency FDFD): replaces solve(d::ModulatedDevice)
  * (src/solver/modulation.jl:35-119, TM only as the reference).  The handle

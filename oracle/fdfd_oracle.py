@@ -354,6 +354,71 @@ def objective(g: Grid, eps_r, src, omega, mvec, m=3.5, lnR=-12.0):
     return abs(vec(mvec).astype(np.complex128) @ E) ** 2
 
 
+# --- mode sources: src/device.jl:111-149, src/solver/eigen.jl:6-29 ----------
+
+def eigenmode_1d(eps_slice, dh: float, omega: float, pol: int, neff, nev: int = 1, L0: float = DEFAULT_L0,
+                 dense=False):
+    """eigenmode(d::AbstractDevice{1}, pol, neff, nev): src/solver/eigen.jl:6-29.
+
+    1-D periodic grid of len(eps_slice) cells of size dh, no PML (the
+    ``Grid(N, xrange)`` constructor, grid.jl:51-59).  TM: A = ω²μ₀Tϵ + δxf δxb;
+    TE: A = ω²μ₀Tϵ + Tϵ δxf Tϵxinv δxb.  ARPACK's shift-invert eigs(A, nev,
+    sigma=(ω n_eff/c₀)²) (scipy's ARPACK-ng here; ``dense`` picks the nearest
+    eigenvalues of a dense eig instead).  Returns (β = √λ, vectors (n, nev))."""
+    eps0, mu0, c0 = normalize_parameters(L0)
+    e = np.asarray(eps_slice, dtype=np.complex128).ravel()
+    n = e.size
+    g = Grid((n, 1), (0, 0), ((0.0, 0.0), (n * dh, dh)), L0)
+    Te = sp.diags(eps0 * e, 0)
+    dxb, dxf = delta(X, BACKWARD, g), delta(X, FORWARD, g)
+    if pol == TM:
+        A = omega ** 2 * mu0 * Te + dxf @ dxb
+    else:
+        Txi = sp.diags(1 / (eps0 * grid_average(e, X)), 0)
+        A = omega ** 2 * mu0 * Te + Te @ dxf @ Txi @ dxb
+    sigma = (omega / c0 * neff) ** 2
+    if dense:
+        w, v = np.linalg.eig(A.toarray())
+        idx = np.argsort(np.abs(w - sigma))[:nev]
+        vals, vecs = w[idx], v[:, idx]
+    else:
+        vals, vecs = spla.eigs(A.astype(np.complex128).tocsc(), k=nev, sigma=sigma,
+                               v0=np.ones(n, dtype=np.complex128))
+    return np.sqrt(vals.astype(np.complex128)), vecs
+
+
+def mode_slice(g: Grid, ix: int, iy: int, normal: int, width: float):
+    """Slice indices of get_modes (device.jl:125-143), 0-based: srcpoints =
+    round(width/dh) made odd, M = (srcpoints-1)/2 cells each side of (ix, iy)."""
+    dh = g.dy() if normal == X else g.dx()
+    pts = int(round(width / dh))
+    if pts % 2 == 0:
+        pts += 1
+    M = (pts - 1) // 2
+    if normal == X:
+        return ix, np.arange(iy - M, iy + M + 1), dh
+    return np.arange(ix - M, ix + M + 1), iy, dh
+
+
+def get_modes(g: Grid, eps_r, pol: int, omega: float, neff, nmodes: int, ix: int, iy: int, normal: int,
+              width: float, dense=False):
+    """get_modes(d, pol, ω, neff, nmodes, pt, slicenormal, slicewidth): src/device.jl:122-149
+    with (ix, iy) = coord2ind(grid, pt) - 1.  Returns (β, vectors, indx, indy)."""
+    indx, indy, dh = mode_slice(g, ix, iy, normal, width)
+    e = np.asarray(eps_r)[indx, indy]
+    beta, vecs = eigenmode_1d(e, dh, omega, pol, neff, nmodes, g.L0, dense)
+    return beta, vecs, indx, indy
+
+
+def setup_mode(src, g: Grid, eps_r, pol: int, omega: float, neff, ix: int, iy: int, normal: int, width: float):
+    """setup_mode!(d, pol, ω, neff, pt, srcnormal, srcwidth): src/device.jl:116-120,
+    src[indx, indy] += normalize(abs.(vector[:])) (in place)."""
+    _, vecs, indx, indy = get_modes(g, eps_r, pol, omega, neff, 1, ix, iy, normal, width)
+    a = np.abs(vecs[:, 0])
+    src[indx, indy] += a / np.linalg.norm(a)
+    return src
+
+
 # --- multi-frequency (modulated) driven solve: src/solver/modulation.jl ------
 
 def modulated_system(g: Grid, eps_r, deps_r, omega: float, Omega: float, nsidebands: int,

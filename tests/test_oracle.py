@@ -240,3 +240,54 @@ def test_modulated_golden_regression(oracle):
                                  int(g["nsidebands"]), bool(g["sharedpml"]), float(g["pml_m"]), float(g["pml_lnR"]))
     ez = np.stack([o[0] for o in out])
     assert np.linalg.norm(ez - g["ez"]) <= 1e-12 * np.linalg.norm(g["ez"])
+
+
+# ---------------------------------------------------------------------------
+# mode sources (src/device.jl:111-149, src/solver/eigen.jl:6-29)
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("pol", [1, 2])
+def test_eigenmode_arpack_matches_dense(oracle, pol):
+    """The ARPACK shift-invert restatement of eigenmode returns the eigenpair
+    of the dense eigendecomposition nearest the shift."""
+    rng = np.random.default_rng(4 + pol)
+    e = rng.uniform(1, 12, 41) + 1j * rng.uniform(0, 0.2, 41)
+    w = 2 * np.pi * oracle.C0 / 1.55e-6
+    b1, v1 = oracle.eigenmode_1d(e, 0.03, w, pol, 2.5)
+    b2, v2 = oracle.eigenmode_1d(e, 0.03, w, pol, 2.5, dense=True)
+    assert abs(b1[0] - b2[0]) <= 1e-12 * abs(b2[0])
+    a1, a2 = np.abs(v1[:, 0]), np.abs(v2[:, 0])
+    assert np.linalg.norm(a1 / np.linalg.norm(a1) - a2 / np.linalg.norm(a2)) <= 1e-9
+
+
+def test_eigenmode_slab_dispersion(oracle):
+    """Known answer: the fundamental TM (Ez) mode of a symmetric slab of index
+    n1 = 3.5, width d = 0.22 µm in n2 = 1 satisfies κ tan(κd/2) = γ with
+    κ² = k₀²n1² − β², γ² = β² − k₀²n2²; the second-order finite differences
+    reach it to O(dh²)."""
+    from scipy.optimize import brentq
+    lam, d, n1, n2, dh = 1.55, 0.22, 3.5, 1.0, 0.002
+    k0 = 2 * np.pi / lam
+    f = lambda b: np.sqrt(k0 ** 2 * n1 ** 2 - b ** 2) * np.tan(np.sqrt(k0 ** 2 * n1 ** 2 - b ** 2) * d / 2) \
+        - np.sqrt(b ** 2 - k0 ** 2 * n2 ** 2)
+    lo = max(k0 * n2, np.sqrt(max(k0 ** 2 * n1 ** 2 - (np.pi / d) ** 2, 0))) + 1e-9
+    b_exact = brentq(f, lo, k0 * n1 - 1e-9)
+    y = (np.arange(1000) + 0.5) * dh - 1.0
+    e = np.where(np.abs(y) <= d / 2, n1 ** 2, n2 ** 2).astype(complex)
+    w = 2 * np.pi * oracle.C0 / (lam * 1e-6)
+    b, _ = oracle.eigenmode_1d(e, dh, w, 1, 3.0)
+    assert abs(b[0].real - b_exact) <= 2e-3 * b_exact and abs(b[0].imag) <= 1e-9 * b_exact
+
+
+def test_setup_mode_adds_normalized_abs(oracle):
+    """setup_mode! adds normalize(abs.(v)) on the slice and nothing elsewhere."""
+    g = oracle.Grid((30, 40), (4, 4), ((0.0, 0.0), (30 * 0.05, 40 * 0.05)))
+    e = np.ones(g.N, complex)
+    e[:, 17:23] = 12.25
+    src = np.zeros(g.N, complex)
+    w = 2 * np.pi * oracle.C0 / 1.55e-6
+    oracle.setup_mode(src, g, e, 1, w, 3.0, 6, 20, oracle.X, 0.8)
+    indx, indy, _ = oracle.mode_slice(g, 6, 20, oracle.X, 0.8)
+    assert len(indy) == 17 and np.isclose(np.linalg.norm(src), 1.0)
+    mask = np.zeros(g.N, bool)
+    mask[indx, indy] = True
+    assert not src[~mask].any() and np.all(src[mask].real > 0)
