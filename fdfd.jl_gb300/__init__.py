@@ -26,7 +26,7 @@ from ._lib import FDFDError, FDFD_PREC_FP64, FDFD_PREC_MIXED  # noqa: F401
 
 __all__ = ["EPS0", "MU0", "C0", "ETA0", "TM", "TE", "X", "Y", "Grid", "Device", "ModulatedDevice", "Point", "Mode",
            "setup_eps", "setup_src", "setup_deps", "add_mode", "setup_mode", "get_modes", "solve", "eigenfrequency",
-           "FieldTM", "FieldTE", "normalize_parameters", "FDFDError"]
+           "FieldTM", "FieldTE", "Flux", "poynting", "flux_surface_integral", "normalize_parameters", "FDFDError"]
 
 # src/types.jl:6-9
 EPS0 = 8.85418782e-12
@@ -252,6 +252,58 @@ class FieldTM(_Field):
 class FieldTE(_Field):
     """src/data.jl:65-78: Nx x Ny x 3 with components [:Hz, :Ex, :Ey]."""
     components = ("Hz", "Ex", "Ey")
+
+
+@dataclass
+class Flux:
+    """src/data.jl (Flux): grid, ω and the Poynting components Sx, Sy (Nx x Ny)."""
+    grid: Grid
+    omega: complex
+    Sx: np.ndarray
+    Sy: np.ndarray
+
+
+def _field_handle(field):
+    g = field.grid
+    return _lib.Handle(g.N[0], g.N[1], g.Npml[0], g.Npml[1], g.dx(), g.dy(), g.L0, 3.5, -12.0, TM, FDFD_PREC_MIXED)
+
+
+def _pol_of(field):
+    return TM if isinstance(field, FieldTM) else TE
+
+
+def poynting(field):
+    """poynting(field::Field): src/flux.jl:15-29, on the GPU."""
+    h = _field_handle(field)
+    try:
+        Sx, Sy = h.poynting(_pol_of(field), field.data[:, :, 0], field.data[:, :, 1], field.data[:, :, 2])
+    finally:
+        h.close()
+    return Flux(field.grid, field.omega, Sx, Sy)
+
+
+def flux_surface_integral(field, center: Point, width, normal):
+    """flux_surface_integral(field, center, width, normal): src/flux.jl:37-66, on the GPU.
+    The column is the one whose centre lies within dx/2 of center.x; the rows are
+    those whose centres lie in [center.y - width, center.y + width]."""
+    g = field.grid
+    if normal == Y:
+        raise FDFDError(_lib.FDFD_EINVAL, "ŷ normal %s calculation not yet implemented" %
+                        ("TM" if _pol_of(field) == TM else "TE"))
+    xc, yc = g.xc(), g.yc()
+    hit = np.nonzero(np.abs(xc - center.x) <= g.dx() / 2)[0]
+    if hit.size == 0:
+        raise FDFDError(_lib.FDFD_EINVAL, "no grid column at center.x")
+    rows = np.nonzero((yc >= center.y - width) & (yc <= center.y + width))[0]
+    if rows.size == 0:
+        raise FDFDError(_lib.FDFD_EINVAL, "no grid row in the interval")
+    h = _field_handle(field)
+    try:
+        out = h.flux_integral(_pol_of(field), field.data[:, :, 0], field.data[:, :, 2],
+                              [(int(hit[0]), int(rows[0]), int(rows[-1]))], normal)
+    finally:
+        h.close()
+    return float(out[0])
 
 
 def _prec(precision):

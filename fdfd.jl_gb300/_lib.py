@@ -27,7 +27,8 @@ FDFD_MODE_MAX_POINTS = 1023
 # every symbol include/fdfd_cuda.h declares
 EXPORTS = ["fdfd_version", "fdfd_create", "fdfd_destroy", "fdfd_last_error", "fdfd_set_refinement",
            "fdfd_set_fallback", "fdfd_set_restart", "fdfd_mf_create", "fdfd_mf_set_deps", "fdfd_mf_factor",
-           "fdfd_mf_solve", "fdfd_get_mode", "fdfd_mode_sources",
+           "fdfd_mf_solve", "fdfd_get_mode", "fdfd_mode_sources", "fdfd_poynting", "fdfd_poynting_device",
+           "fdfd_flux_integral",
            "fdfd_set_eps", "fdfd_factor", "fdfd_solve", "fdfd_solve_device", "fdfd_adjoint", "fdfd_eigfreq",
            "fdfd_get_stencil", "fdfd_apply", "fdfd_set_profiling", "fdfd_get_profile", "fdfd_residual_noalloc",
            "fdfd_debug_hessenberg_eig", "fdfd_debug_gemm"]
@@ -106,6 +107,12 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.fdfd_get_mode.argtypes = [vp, C.c_double, C.POINTER(Mode), ip, dp, dp, C.POINTER(C.c_int)]
     lib.fdfd_mode_sources.restype = ip
     lib.fdfd_mode_sources.argtypes = [vp, ip, dp, ip, C.POINTER(Mode), dp]
+    lib.fdfd_poynting.restype = ip
+    lib.fdfd_poynting.argtypes = [vp, ip, dp, dp, dp, dp, dp]
+    lib.fdfd_poynting_device.restype = ip
+    lib.fdfd_poynting_device.argtypes = [vp, ip, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    lib.fdfd_flux_integral.restype = ip
+    lib.fdfd_flux_integral.argtypes = [vp, ip, dp, dp, ip, ip, C.POINTER(C.c_int), dp]
     lib.fdfd_set_eps.restype = ip
     lib.fdfd_set_eps.argtypes = [vp, dp]
     lib.fdfd_factor.restype = ip
@@ -261,6 +268,23 @@ class Handle:
         out = np.empty(om.size * self.Nx * self.Ny, dtype=np.complex128)
         self._check(self.lib.fdfd_mode_sources(self.h, om.size, cptr(om), len(modes), arr, cptr(out)))
         return from_natural(out, self.Nx, self.Ny)
+
+    def poynting(self, pol, f1, f2, f3):
+        """(Sx, Sy), each (Nx, Ny), of the field (f1, f2, f3)."""
+        b = [natural(f) for f in (f1, f2, f3)]
+        Sx = np.empty((self.Ny, self.Nx), dtype=np.float64)
+        Sy = np.empty_like(Sx)
+        self._check(self.lib.fdfd_poynting(self.h, int(pol), *[cptr(x) for x in b], cptr(Sx), cptr(Sy)))
+        return Sx.T.copy(), Sy.T.copy()
+
+    def flux_integral(self, pol, f1, f3, lines, normal=FDFD_X):
+        """x̂-normal line integrals; lines: sequence of (xind, iy0, iy1) -> array of fluxes."""
+        b1, b3 = natural(f1), natural(f3)
+        ln = np.ascontiguousarray(np.asarray(lines, dtype=np.int32).reshape(-1, 3))
+        out = np.empty(ln.shape[0], dtype=np.float64)
+        self._check(self.lib.fdfd_flux_integral(self.h, int(pol), cptr(b1), cptr(b3), int(normal), ln.shape[0],
+                                                ln.ctypes.data_as(C.POINTER(C.c_int)), cptr(out)))
+        return out
 
     def set_profiling(self, on=True):
         self._check(self.lib.fdfd_set_profiling(self.h, 1 if on else 0))

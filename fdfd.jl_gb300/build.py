@@ -21,8 +21,8 @@ LIB = os.path.join(HERE, "libfdfd_cuda.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
          "-I" + CSRC, "-I" + INCLUDE]
-SOURCES = ["assemble.cu", "blocks.cu", "gemm_simt.cu", "gemm_tc.cu", "sweep.cu", "modes.cu", "fdfd_api.cu",
-           "noalloc.cu"]
+SOURCES = ["assemble.cu", "blocks.cu", "gemm_simt.cu", "gemm_tc.cu", "sweep.cu", "modes.cu", "flux.cu",
+           "fdfd_api.cu", "noalloc.cu"]
 
 
 def nvcc() -> str:

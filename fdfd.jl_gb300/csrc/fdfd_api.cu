@@ -1801,6 +1801,87 @@ int fdfd_mode_sources(fdfd_handle* h, int nw, const double* omegas, int nmodes, 
     return run_modes(h, jobs, start, true, nullptr, nullptr, src);
 }
 
+// ---- Poynting flux (src/flux.jl) ------------------------------------------------
+int fdfd_poynting_device(fdfd_handle* h, int pol, const double* d_f1, const double* d_f2, const double* d_f3,
+                         double* d_Sx, double* d_Sy) {
+    if (!h) return FDFD_EINVAL;
+    if (pol != FDFD_TM && pol != FDFD_TE) return set_err(h, FDFD_EINVAL, "pol must be FDFD_TM or FDFD_TE");
+    if (!d_f1 || !d_f2 || !d_f3 || !d_Sx || !d_Sy) return set_err(h, FDFD_EINVAL, "fdfd_poynting: NULL argument");
+    launch_poynting(h->stream, h->Nx, h->Ny, pol, (const cplx<double>*)d_f1, (const cplx<double>*)d_f2,
+                    (const cplx<double>*)d_f3, d_Sx, d_Sy);
+    h->launches++;
+    RET(check_launch(h, "poynting"));
+    CK(cudaStreamSynchronize(h->stream));
+    return FDFD_OK;
+}
+
+int fdfd_poynting(fdfd_handle* h, int pol, const double* f1, const double* f2, const double* f3, double* Sx,
+                  double* Sy) {
+    if (!h) return FDFD_EINVAL;
+    if (!f1 || !f2 || !f3 || !Sx || !Sy) return set_err(h, FDFD_EINVAL, "fdfd_poynting: NULL argument");
+    const long long N = (long long)h->Nx * h->Ny;
+    const size_t fb = (size_t)N * sizeof(cplx<double>), sb = (size_t)N * sizeof(double);
+    if (h->io_cap < 3 * fb + 2 * sb) {
+        dev_free(h->io);
+        h->io = nullptr;
+        h->dev_bytes -= (long long)h->io_cap;
+        h->io_cap = 0;
+        RET(dev_alloc(h, (void**)&h->io, 3 * fb + 2 * sb));
+        h->io_cap = 3 * fb + 2 * sb;
+    }
+    unsigned char* B = reinterpret_cast<unsigned char*>(h->io);
+    CK(cudaMemcpyAsync(B, f1, fb, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(B + fb, f2, fb, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(B + 2 * fb, f3, fb, cudaMemcpyHostToDevice, h->stream));
+    double* dS = reinterpret_cast<double*>(B + 3 * fb);
+    RET(fdfd_poynting_device(h, pol, (const double*)B, (const double*)(B + fb), (const double*)(B + 2 * fb), dS,
+                             dS + N));
+    CK(cudaMemcpyAsync(Sx, dS, sb, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(Sy, dS + N, sb, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return FDFD_OK;
+}
+
+int fdfd_flux_integral(fdfd_handle* h, int pol, const double* f1, const double* f3, int normal, int nlines,
+                       const int* lines, double* flux) {
+    if (!h) return FDFD_EINVAL;
+    if (pol != FDFD_TM && pol != FDFD_TE) return set_err(h, FDFD_EINVAL, "pol must be FDFD_TM or FDFD_TE");
+    if (normal == FDFD_Y)   // flux.jl:59-66
+        return set_err(h, FDFD_EINVAL, "%s normal %s calculation not yet implemented", "y",
+                       pol == FDFD_TM ? "TM" : "TE");
+    if (normal != FDFD_X) return set_err(h, FDFD_EINVAL, "normal must be FDFD_X or FDFD_Y");
+    if (!f1 || !f3 || !lines || !flux || nlines < 1) return set_err(h, FDFD_EINVAL, "fdfd_flux_integral: bad argument");
+    for (int l = 0; l < nlines; ++l) {
+        const int x = lines[3 * l], y0 = lines[3 * l + 1], y1 = lines[3 * l + 2];
+        if (x < 0 || x + 1 >= h->Nx || y0 < 0 || y1 >= h->Ny || y0 > y1)
+            return set_err(h, FDFD_EINVAL, "flux line %d (column %d, rows %d..%d) outside the grid", l, x, y0, y1);
+    }
+    const long long N = (long long)h->Nx * h->Ny;
+    const size_t fb = (size_t)N * sizeof(cplx<double>);
+    const size_t need = 2 * fb + (size_t)nlines * (sizeof(int3) + sizeof(double)) + 64;
+    if (h->io_cap < need) {
+        dev_free(h->io);
+        h->io = nullptr;
+        h->dev_bytes -= (long long)h->io_cap;
+        h->io_cap = 0;
+        RET(dev_alloc(h, (void**)&h->io, need));
+        h->io_cap = need;
+    }
+    unsigned char* B = reinterpret_cast<unsigned char*>(h->io);
+    int3* dl = reinterpret_cast<int3*>(B + 2 * fb);
+    double* dout = reinterpret_cast<double*>(B + ((2 * fb + (size_t)nlines * sizeof(int3) + 15) / 16 * 16));
+    CK(cudaMemcpyAsync(B, f1, fb, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(B + fb, f3, fb, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(dl, lines, (size_t)nlines * sizeof(int3), cudaMemcpyHostToDevice, h->stream));
+    launch_flux_lines(h->stream, nlines, h->Nx, pol, h->dy, dl, (const cplx<double>*)B,
+                      (const cplx<double>*)(B + fb), dout);
+    h->launches++;
+    RET(check_launch(h, "flux lines"));
+    CK(cudaMemcpyAsync(flux, dout, (size_t)nlines * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return FDFD_OK;
+}
+
 int fdfd_set_profiling(fdfd_handle* h, int on) {
     if (!h) return FDFD_EINVAL;
     prof_collect(h);

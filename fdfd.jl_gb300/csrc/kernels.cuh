@@ -119,6 +119,14 @@ int launch_modes(cudaStream_t s, int njobs, int nmax, const ModeJob* jobs, const
 void launch_mode_src(cudaStream_t s, int nw, const ModeJob* jobs, const int* job_start, const cplx<double>* vecs,
                      long long N, cplx<double>* src);
 
+// ---- flux.cu --------------------------------------------------------------------
+// Poynting flux Sx, Sy per cell (flux.jl:15-29); pol 1 TM (Ez, Hx, Hy), 2 TE (Hz, Ex, Ey)
+void launch_poynting(cudaStream_t s, int Nx, int Ny, int pol, const cplx<double>* f1, const cplx<double>* f2,
+                     const cplx<double>* f3, double* Sx, double* Sy);
+// x̂-normal line integrals (flux.jl:37-57): lines (xind, iy0, iy1), out[l] (one block per line)
+void launch_flux_lines(cudaStream_t s, int nlines, int Nx, int pol, double dy, const int3* lines,
+                       const cplx<double>* f1, const cplx<double>* f3, double* out);
+
 // ---- gemm_simt.cu / gemm_tc.cu --------------------------------------------
 // Batched complex "TN" GEMM on planar pools:
 //   C[m][n] = beta(m,n)·Cin[src(m)][n] + alpha·Σ_k A[m][k]·B[n][k]

@@ -189,6 +189,29 @@ int  fdfd_get_mode(fdfd_handle* h, double omega, const fdfd_mode* mode, int cap,
 int  fdfd_mode_sources(fdfd_handle* h, int nw, const double* omegas, int nmodes,
                        const fdfd_mode* modes, double* src);
 
+/* Poynting flux of a field (poynting, src/flux.jl:15-29) on the handle's grid:
+ * f1, f2, f3 = (Ez, Hx, Hy) for FDFD_TM or (Hz, Ex, Ey) for FDFD_TE, Nx*Ny
+ * complex each (host); Sx, Sy: Nx*Ny doubles.  TM: Sx = -½Re(avgx(Ez) Hy*),
+ * Sy = ½Re(avgy(Ez) Hx*); TE: Sx = ½Re(Ey avgx(Hz)*), Sy = -½Re(Ex avgy(Hz)*),
+ * avg the periodic grid_average (grid.jl:183-188).  The reference's TE branch
+ * reads fields a FieldTE lacks (flux.jl:26-27); the averaged Hz is used. */
+int  fdfd_poynting(fdfd_handle* h, int pol, const double* f1, const double* f2,
+                   const double* f3, double* Sx, double* Sy);
+/* The same on device pointers (e.g. the outputs of fdfd_solve_device), with
+ * no host copies. */
+int  fdfd_poynting_device(fdfd_handle* h, int pol, const double* d_f1, const double* d_f2,
+                          const double* d_f3, double* d_Sx, double* d_Sy);
+
+/* flux_surface_integral(field, center, width, normal) (src/flux.jl:37-66) for
+ * nlines lines (x̂ normal): lines holds (xind, iy0, iy1) per line, 0-based:
+ * the column of center.x and the rows whose centres lie in
+ * [center.y - width, center.y + width].  flux[l] = Σ -½Re(½(f1[xind]+f1[xind+1])
+ * f3[xind]*)·dy, f1/f3 = Ez/Hy (TM) or Hz/Ey (TE; the reference's TE branch
+ * names an undefined `pt` and reads :Hy, flux.jl:49,54 — the column of center
+ * and :Ey are used).  FDFD_Y is FDFD_EINVAL, as in the reference. */
+int  fdfd_flux_integral(fdfd_handle* h, int pol, const double* f1, const double* f3,
+                        int normal, int nlines, const int* lines, double* flux);
+
 /* Modulated device (multi-frequency FDFD): replaces solve(d::ModulatedDevice)
  * (src/solver/modulation.jl:35-119, TM only as the reference).  The handle
  * holds K = 2*nsidebands+1 sideband operators

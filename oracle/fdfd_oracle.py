@@ -419,6 +419,108 @@ def setup_mode(src, g: Grid, eps_r, pol: int, omega: float, neff, ix: int, iy: i
     return src
 
 
+# --- χ³ nonlinear driven solve: src/solver/nonlinear.jl --------------------------
+
+def chi3_coeff(g: Grid, chi, omega: float):
+    """coeff = ω²ϵ₀·3χ/L₀ with ϵ₀ normalised (nonlinear.jl:74)."""
+    eps0, _, _ = normalize_parameters(g.L0)
+    return omega ** 2 * eps0 * 3 * vec(np.asarray(chi, dtype=np.float64)) / g.L0
+
+
+def born(A, b, coeff, ez, tol=1e-12, maxiterations=50):
+    """_doborn (nonlinear.jl:94-108): ez ← (A + diag(coeff·|ez|²))⁻¹ b until
+    ||ez_new − ez||/||ez|| ≤ tol.  The reference misplaces a parenthesis in
+    the solve call (``sparse(Diagonal(...), b, CNSym)``); the evident intent,
+    dolinearsolve(A + Diagonal(coeff.*ez.*conj.(ez)), b), is restated."""
+    err = [1.0]
+    i = 1
+    while err[-1] > tol and i <= maxiterations:
+        new = dolinearsolve((A + sp.diags(coeff * ez * np.conj(ez))).tocsc(), b)
+        err.append(np.linalg.norm(new - ez) / np.linalg.norm(ez))
+        ez = new
+        i += 1
+    return ez, err
+
+
+def newton(A, b, coeff, ez, tol=1e-12, maxiterations=50):
+    """_donewton (nonlinear.jl:110-129): Newton on the stacked unknown [ez; conj(ez)]
+    with F = (A + diag(coeff|ez|²))ez − b, J = [J1 J2; conj(J2) conj(J1)],
+    J1 = A + diag(2coeff|ez|²), J2 = diag(coeff ez²); err = ||δ||/||[ez; conj ez]||."""
+    M = ez.size
+    z = np.concatenate([ez, np.conj(ez)])
+    err = [1.0]
+    i = 1
+    while err[-1] > tol and i <= maxiterations:
+        e1 = z[:M]
+        F = (A + sp.diags(coeff * e1 * np.conj(e1))) @ e1 - b
+        J1 = A + sp.diags(2 * coeff * np.conj(e1) * e1)
+        J2 = sp.diags(coeff * e1 * e1)
+        J = sp.bmat([[J1, J2], [J2.conj(), J1.conj()]], format="csc")
+        d = dolinearsolve(J, np.concatenate([F, np.conj(F)]))
+        nz = np.linalg.norm(z)
+        z = z - d
+        err.append(np.linalg.norm(d) / nz)
+        i += 1
+    return z[:M], err
+
+
+def solve_chi3(g: Grid, eps_r, chi, src, omega: float, method: str, m=3.5, lnR=-12.0, tol=1e-12,
+               maxiterations=50):
+    """solve(d::χ3Device, which_method): src/solver/nonlinear.jl:36-91 (TM): the
+    linear solve, then Born (``"born"``) or Gauss-Newton (``"newton"``), then
+    the driven H recovery.  Returns ((Ez, Hx, Hy), err history)."""
+    A = assemble(g, eps_r, omega, TM, m, lnR)
+    b = 1j * omega * vec(np.asarray(src, dtype=np.complex128))
+    ez = dolinearsolve(A, b)
+    coeff = chi3_coeff(g, chi, omega)
+    if method == "born":
+        ez, err = born(A, b, coeff, ez, tol, maxiterations)
+    else:
+        ez, err = newton(A, b, coeff, ez, tol, maxiterations)
+    return recover_driven(g, eps_r, omega, ez, TM, m, lnR), err
+
+
+# --- Poynting flux: src/flux.jl -------------------------------------------------
+
+def poynting(f1, f2, f3, pol: int):
+    """poynting(field): src/flux.jl:15-29.  TM (Ez, Hx, Hy): Sx = -½Re(avgx(Ez)·Hy*),
+    Sy = ½Re(avgy(Ez)·Hx*).  TE (Hz, Ex, Ey): Sx = ½Re(Ey·avgx(Hz)*),
+    Sy = -½Re(Ex·avgy(Hz)*) — the reference reads ``field.Hz_x``/``field.Hz_y``
+    (flux.jl:26-27), which a FieldTE does not have; the averages computed on the
+    lines before are meant."""
+    ax, ay = grid_average(f1, X), grid_average(f1, Y)
+    if pol == TM:
+        return -0.5 * np.real(ax * np.conj(f3)), 0.5 * np.real(ay * np.conj(f2))
+    return 0.5 * np.real(f3 * np.conj(ax)), -0.5 * np.real(f2 * np.conj(ay))
+
+
+def flux_line_indices(g: Grid, center, width):
+    """Indices of flux_surface_integral (flux.jl:39-42), 0-based: the column whose
+    centre lies within dx/2 of center.x (AxisArrays ``atvalue``), and the rows
+    whose centres lie in the closed interval [center.y - width, center.y + width]."""
+    xc, yc = g.xc(), g.yc()
+    hit = np.nonzero(np.abs(xc - center[0]) <= g.dx() / 2)[0]
+    if hit.size == 0:
+        raise ValueError("no grid column at center.x")
+    rows = np.nonzero((yc >= center[1] - width) & (yc <= center[1] + width))[0]
+    return int(hit[0]), rows
+
+
+def flux_surface_integral(g: Grid, f1, f3, pol: int, center, width, normal: int):
+    """flux_surface_integral(field, center, width, normal): src/flux.jl:37-66.
+    x̂ normal: Σ -½Re(½(f1[x]+f1[x+1])·f3[x]*)·dy over the rows, f1/f3 = Ez/Hy
+    (TM) or Hz/Ey (TE: the reference names an undefined ``pt`` and reads :Hy,
+    flux.jl:49,54; the column of ``center`` and :Ey are meant; its sign is kept).
+    ŷ normal raises, as the reference."""
+    if normal == Y:
+        raise NotImplementedError("ŷ normal %s calculation not yet implemented" % ("TM" if pol == TM else "TE"))
+    x, rows = flux_line_indices(g, center, width)
+    av = 0.5 * (f1[x, rows] + f1[x + 1, rows])
+    if pol == TM:
+        return float(np.sum(-0.5 * np.real(av * np.conj(f3[x, rows]))) * g.dy())
+    return float(np.sum(-0.5 * np.real(f3[x, rows] * np.conj(av))) * g.dy())
+
+
 # --- multi-frequency (modulated) driven solve: src/solver/modulation.jl ------
 
 def modulated_system(g: Grid, eps_r, deps_r, omega: float, Omega: float, nsidebands: int,
