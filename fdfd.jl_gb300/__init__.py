@@ -26,7 +26,8 @@ from ._lib import FDFDError, FDFD_PREC_FP64, FDFD_PREC_MIXED  # noqa: F401
 
 __all__ = ["EPS0", "MU0", "C0", "ETA0", "TM", "TE", "X", "Y", "Grid", "Device", "ModulatedDevice", "Point", "Mode",
            "setup_eps", "setup_src", "setup_deps", "add_mode", "setup_mode", "get_modes", "solve", "eigenfrequency",
-           "FieldTM", "FieldTE", "Flux", "poynting", "flux_surface_integral", "normalize_parameters", "FDFDError"]
+           "FieldTM", "FieldTE", "Flux", "poynting", "flux_surface_integral", "Chi3Device", "setup_chi",
+           "IterativeMethodGN", "IterativeMethodB", "normalize_parameters", "FDFDError"]
 
 # src/types.jl:6-9
 EPS0 = 8.85418782e-12
@@ -36,6 +37,7 @@ ETA0 = math.sqrt(MU0 / EPS0)
 DEFAULT_L0 = 1e-6          # src/grid.jl:31
 TM, TE = _lib.FDFD_TM, _lib.FDFD_TE   # src/types.jl:20
 X, Y = _lib.FDFD_X, _lib.FDFD_Y       # src/types.jl:18 (x̂, ŷ)
+IterativeMethodGN, IterativeMethodB = _lib.FDFD_CHI3_NEWTON, _lib.FDFD_CHI3_BORN   # src/solver/nonlinear.jl:5
 
 
 @dataclass
@@ -149,6 +151,27 @@ class ModulatedDevice:
             self.src = np.zeros(self.grid.N, dtype=np.complex128)
 
 
+@dataclass
+class Chi3Device:
+    """src/solver/nonlinear.jl:9-27: a Device with a real χ⁽³⁾ array (zero by default)."""
+    grid: Grid
+    omega: list
+    eps: np.ndarray = None
+    chi: np.ndarray = None
+    src: np.ndarray = None
+    modes: list = field(default_factory=list)
+
+    def __post_init__(self):
+        if np.isscalar(self.omega):
+            self.omega = [float(self.omega)]
+        if self.eps is None:
+            self.eps = np.ones(self.grid.N, dtype=np.complex128)
+        if self.chi is None:
+            self.chi = np.zeros(self.grid.N, dtype=np.float64)
+        if self.src is None:
+            self.src = np.zeros(self.grid.N, dtype=np.complex128)
+
+
 def _mask(d, region):
     X, Y = np.meshgrid(d.grid.xc(), d.grid.yc(), indexing="ij")
     return np.vectorize(region)(X, Y).astype(bool), X, Y
@@ -175,6 +198,15 @@ def setup_deps(d: ModulatedDevice, region, value):
     """setup_Δϵᵣ!(d, region, value): src/solver/modulation.jl:29-30 (region and value may be callables)."""
     m, X, Y = _mask(d, region)
     d.deps[m] = np.vectorize(value)(X, Y)[m] if callable(value) else value
+
+
+def setup_chi(d: Chi3Device, region, value):
+    """setup_χ!(d, region, value): src/solver/nonlinear.jl:32-33."""
+    m, X_, Y_ = _mask(d, region)
+    d.chi[m] = np.vectorize(value)(X_, Y_)[m] if callable(value) else value
+
+
+globals()["setup_χ"] = setup_chi
 
 
 def add_mode(d, mode: Mode):
@@ -333,6 +365,9 @@ def solve(d: Device, pol=TM, precision="mixed", pml_m=3.5, pml_lnR=-12.0, tol=1e
     """
     if isinstance(d, ModulatedDevice):
         return solve_modulated(d, precision, pml_m, pml_lnR, tol, max_iter, return_stats)
+    if isinstance(d, Chi3Device):
+        # solve(d::χ3Device, which_method): the second argument is the iterative method
+        return solve_chi3(d, pol, precision, pml_m, pml_lnR, max_iter=max_iter, return_stats=return_stats)
     h = make_handle(d, pol, precision, pml_m, pml_lnR, tol, max_iter)
     out, stats = [], []
     try:
@@ -348,6 +383,32 @@ def solve(d: Device, pol=TM, precision="mixed", pml_m=3.5, pml_lnR=-12.0, tol=1e
             cls = FieldTM if pol == TM else FieldTE
             out.append(cls(d.grid, w, np.stack([f1, f2, f3], axis=-1)))
             stats.append(st.as_dict())
+    finally:
+        h.close()
+    res = out[0] if len(out) == 1 else out
+    return (res, stats) if return_stats else res
+
+
+def solve_chi3(d: Chi3Device, method=IterativeMethodGN, precision="mixed", pml_m=3.5, pml_lnR=-12.0,
+               tol=1e-12, maxiterations=50, max_iter=40, return_stats=False):
+    """solve(d::χ3Device, which_method) — src/solver/nonlinear.jl:36-91 (TM): per ω one
+    factorization of the linear operator, reused by every Born or Newton step."""
+    g = d.grid
+    h = _lib.Handle(g.N[0], g.N[1], g.Npml[0], g.Npml[1], g.dx(), g.dy(), g.L0, pml_m, pml_lnR, TM,
+                    _prec(precision))
+    out, stats = [], []
+    try:
+        h.set_refinement(1e-10, max_iter)
+        h.set_eps(d.eps)
+        if d.modes:
+            srcs = h.mode_sources(d.omega, [_mode_spec(d, m, TM) for m in d.modes])
+        for i, w in enumerate(d.omega):
+            if d.modes:
+                d.src = srcs[i].copy()
+            h.factor(w)
+            ez, hx, hy, err, st = h.chi3_solve(d.chi, d.src, method, tol, maxiterations)
+            out.append(FieldTM(g, w, np.stack([ez, hx, hy], axis=-1)))
+            stats.append(dict(st.as_dict(), step_errors=err.tolist()))
     finally:
         h.close()
     res = out[0] if len(out) == 1 else out

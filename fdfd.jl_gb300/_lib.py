@@ -22,13 +22,14 @@ FDFD_TM, FDFD_TE = 1, 2
 FDFD_PREC_FP64, FDFD_PREC_MIXED = 0, 1
 FDFD_REFINE_GMRES, FDFD_REFINE_CLASSIC = 0, 1
 FDFD_X, FDFD_Y = 1, 2
+FDFD_CHI3_NEWTON, FDFD_CHI3_BORN = 1, 2
 FDFD_MODE_MAX_POINTS = 1023
 
 # every symbol include/fdfd_cuda.h declares
 EXPORTS = ["fdfd_version", "fdfd_create", "fdfd_destroy", "fdfd_last_error", "fdfd_set_refinement",
            "fdfd_set_fallback", "fdfd_set_restart", "fdfd_mf_create", "fdfd_mf_set_deps", "fdfd_mf_factor",
            "fdfd_mf_solve", "fdfd_get_mode", "fdfd_mode_sources", "fdfd_poynting", "fdfd_poynting_device",
-           "fdfd_flux_integral",
+           "fdfd_flux_integral", "fdfd_chi3_solve",
            "fdfd_set_eps", "fdfd_factor", "fdfd_solve", "fdfd_solve_device", "fdfd_adjoint", "fdfd_eigfreq",
            "fdfd_get_stencil", "fdfd_apply", "fdfd_set_profiling", "fdfd_get_profile", "fdfd_residual_noalloc",
            "fdfd_debug_hessenberg_eig", "fdfd_debug_gemm"]
@@ -113,6 +114,9 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.fdfd_poynting_device.argtypes = [vp, ip, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
     lib.fdfd_flux_integral.restype = ip
     lib.fdfd_flux_integral.argtypes = [vp, ip, dp, dp, ip, ip, C.POINTER(C.c_int), dp]
+    lib.fdfd_chi3_solve.restype = ip
+    lib.fdfd_chi3_solve.argtypes = [vp, dp, dp, ip, C.c_double, ip, dp, dp, dp, dp, C.POINTER(C.c_int),
+                                    C.POINTER(Stats)]
     lib.fdfd_set_eps.restype = ip
     lib.fdfd_set_eps.argtypes = [vp, dp]
     lib.fdfd_factor.restype = ip
@@ -285,6 +289,19 @@ class Handle:
         self._check(self.lib.fdfd_flux_integral(self.h, int(pol), cptr(b1), cptr(b3), int(normal), ln.shape[0],
                                                 ln.ctypes.data_as(C.POINTER(C.c_int)), cptr(out)))
         return out
+
+    def chi3_solve(self, chi, src, method=FDFD_CHI3_NEWTON, tol=1e-12, maxit=50):
+        """χ³ solve of the factored TM operator -> (Ez, Hx, Hy, err history, stats)."""
+        c = np.ascontiguousarray(np.asarray(chi, dtype=np.float64).T)
+        b = natural(src)
+        outs = [np.empty_like(b) for _ in range(3)]
+        err = np.empty(maxit + 1, dtype=np.float64)
+        nerr = C.c_int(0)
+        st = Stats()
+        self._check(self.lib.fdfd_chi3_solve(self.h, cptr(c), cptr(b), int(method), float(tol), int(maxit),
+                                             *[cptr(o) for o in outs], cptr(err), C.byref(nerr), C.byref(st)))
+        f = [from_natural(o, self.Nx, self.Ny)[0] for o in outs]
+        return f[0], f[1], f[2], err[:min(nerr.value, maxit + 1)].copy(), st
 
     def set_profiling(self, on=True):
         self._check(self.lib.fdfd_set_profiling(self.h, 1 if on else 0))

@@ -268,6 +268,100 @@ __global__ void residual_mf_kernel(MfResidualArgs a, const cplx<double>* __restr
     }
 }
 
+// ---------------------------------------------------------------------------
+// χ³ systems of the nonlinear driven solve (src/solver/nonlinear.jl:94-129).
+// mode 1 (Born): r = b − (A + diag d1) x on one N-vector;
+// mode 2 (Newton on the stacked unknown [x1; x2]):
+//   r1 = b1 − (A x1 + d1⊙x1 + d2⊙x2),  r2 = b2 − (conj(A) x2 + conj(d2)⊙x1 + conj(d1)⊙x2).
+// Grid (blocks, 1 or 2 halves); partial sums of |r|², |b|² per half.
+// ---------------------------------------------------------------------------
+__global__ void residual_nl_kernel(int Nx, int Ny, int mode, const cplx<double>* __restrict__ st,
+                                   const cplx<double>* __restrict__ d1, const cplx<double>* __restrict__ d2,
+                                   const cplx<double>* __restrict__ x, const cplx<double>* __restrict__ b,
+                                   cplx<double>* __restrict__ r, double* __restrict__ part) {
+    const long long N = (long long)Nx * Ny;
+    const int half = blockIdx.y;
+    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    double rr = 0.0, bb = 0.0;
+    if (k < N) {
+        const int ix = (int)(k % Nx), iy = (int)(k / Nx);
+        const long long kxm = (ix == 0) ? k + Nx - 1 : k - 1;
+        const long long kxp = (ix == Nx - 1) ? k - (Nx - 1) : k + 1;
+        const long long kym = (iy == 0) ? k + N - Nx : k - Nx;
+        const long long kyp = (iy == Ny - 1) ? k - (N - Nx) : k + Nx;
+        const cplx<double>* xs = x + (size_t)half * N;
+        const double cj = half ? -1.0 : 1.0;   // conjugate the coefficients in the second half
+        auto c = [&](cplx<double> v) { return cmk(v.re, cj * v.im); };
+        cplx<double> acc = cmul(c(st[k]), xs[k]);
+        acc = cadd(acc, cmul(c(st[N + k]), xs[kxm]));
+        acc = cadd(acc, cmul(c(st[2 * N + k]), xs[kxp]));
+        acc = cadd(acc, cmul(c(st[3 * N + k]), xs[kym]));
+        acc = cadd(acc, cmul(c(st[4 * N + k]), xs[kyp]));
+        acc = cadd(acc, cmul(c(d1[k]), xs[k]));
+        if (mode == 2) acc = cadd(acc, cmul(c(d2[k]), x[(size_t)(1 - half) * N + k]));
+        if (b) {
+            const cplx<double> bv = b[(size_t)half * N + k];
+            acc = csub(bv, acc);
+            bb = bv.re * bv.re + bv.im * bv.im;
+        }
+        rr = acc.re * acc.re + acc.im * acc.im;
+        r[(size_t)half * N + k] = acc;
+    }
+    if (!part) return;
+    __shared__ double s_rr[32], s_bb[32];
+    for (int o = 16; o > 0; o >>= 1) {
+        rr += __shfl_down_sync(0xffffffffu, rr, o);
+        bb += __shfl_down_sync(0xffffffffu, bb, o);
+    }
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) { s_rr[w] = rr; s_bb[w] = bb; }
+    __syncthreads();
+    if (w == 0) {
+        const int nw = blockDim.x >> 5;
+        rr = l < nw ? s_rr[l] : 0.0;
+        bb = l < nw ? s_bb[l] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) {
+            rr += __shfl_down_sync(0xffffffffu, rr, o);
+            bb += __shfl_down_sync(0xffffffffu, bb, o);
+        }
+        if (l == 0) {
+            double* p = part + ((size_t)half * gridDim.x + blockIdx.x) * 2;
+            p[0] = rr;
+            p[1] = bb;
+        }
+    }
+}
+
+// χ³ diagonals from the field e (coeff = ω²ϵ₀·3χ/L₀, nonlinear.jl:74):
+// mode 1: d1 = coeff|e|²;  mode 2 (Newton Jacobian): d1 = 2coeff|e|², d2 = coeff·e².
+__global__ void chi3_diag_kernel(long long N, int mode, const double* __restrict__ coeff,
+                                 const cplx<double>* __restrict__ e, cplx<double>* __restrict__ d1,
+                                 cplx<double>* __restrict__ d2) {
+    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= N) return;
+    const cplx<double> v = e[k];
+    const double c = coeff[k], m2 = v.re * v.re + v.im * v.im;
+    if (mode == 1) {
+        d1[k] = cmk(c * m2, 0.0);
+    } else {
+        d1[k] = cmk(2.0 * c * m2, 0.0);
+        d2[k] = cmk(c * (v.re * v.re - v.im * v.im), c * 2.0 * v.re * v.im);
+    }
+}
+
+// out = conj(in)  (n values; in may equal out)
+__global__ void vconj_kernel(long long n, const cplx<double>* in, cplx<double>* out) {
+    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) out[k] = cmk(in[k].re, -in[k].im);
+}
+
+// y += alpha·x  (n values)
+__global__ void vaxpy_kernel(long long n, double alpha, const cplx<double>* __restrict__ x,
+                             cplx<double>* __restrict__ y) {
+    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) y[k] = cmk(y[k].re + alpha * x[k].re, y[k].im + alpha * x[k].im);
+}
+
 // out[rhs*nvals + v] = Σ_blocks part[rhs][block][v]   (fixed order: deterministic)
 // grid: nrhs, block 256
 __global__ void reduce_partials_kernel(const double* __restrict__ part, int nblocks, int nvals,

@@ -117,6 +117,13 @@ struct fdfd_handle {
     bool fallback = true;            // MIXED: re-factor in FP64 when the refinement would not converge
     int restart = 0;                 // FGMRES basis length (0: automatic)
     int nsb = 1;                     // Krylov vector length in units of Nx*Ny (K for a modulated device)
+    long long kr_vlen = 0;           // vector length the Krylov workspace was sized for
+    bool warm_start = false;         // next refine() starts from h->kx instead of 0 (consumed)
+    // χ³ solve (nonlinear.jl): 0 off, 1 Born operator A + diag d1, 2 Newton's stacked system
+    int nl_mode = 0;
+    cplx<double>* nl_d1 = nullptr;
+    cplx<double>* nl_d2 = nullptr;
+    cplx<double>* nl_tmp = nullptr;  // 2N: conjugated preconditioner input (Newton)
     MfState* mf = nullptr;           // modulated device state (fdfd_mf_create), else null
     double mf_factor_ms = 0;         // wall time of the last fdfd_mf_factor
     unsigned char* mode_buf = nullptr;   // guided-mode scratch (jobs, vectors, sources)
@@ -876,6 +883,18 @@ int precond_mf(fdfd_handle* h, const cplx<double>* in, cplx<double>* out) {
 
 int precond(fdfd_handle* h, const cplx<double>* in, cplx<double>* out, int nrhs) {
     if (h->mf) return precond_mf(h, in, out);
+    if (h->nl_mode == 2) {
+        // Newton's stacked system: blockdiag(A⁻¹, conj(A)⁻¹), conj(A)⁻¹v = conj(A⁻¹ conj(v)),
+        // both halves through one two-right-hand-side sweep
+        const long long N = (long long)h->Nx * h->Ny;
+        CK(cudaMemcpyAsync(h->nl_tmp, in, N * sizeof(cplx<double>), cudaMemcpyDeviceToDevice, h->stream));
+        LAUNCH(vconj_kernel, ceil_div(N, 256), 256, 0, N, in + N, h->nl_tmp + N);
+        int rc = h->fact_prec == FDFD_PREC_FP64 ? precond_impl<double>(h, h->nl_tmp, out, 2)
+                                                : precond_impl<float>(h, h->nl_tmp, out, 2);
+        if (rc != FDFD_OK) return rc;
+        LAUNCH(vconj_kernel, ceil_div(N, 256), 256, 0, N, out + N, out + N);
+        return check_launch(h, "precond");
+    }
     return h->fact_prec == FDFD_PREC_FP64 ? precond_impl<double>(h, in, out, nrhs)
                                           : precond_impl<float>(h, in, out, nrhs);
 }
@@ -931,9 +950,35 @@ int residual_mf(fdfd_handle* h, const cplx<double>* x, const cplx<double>* b, cp
     return check_launch(h, "residual");
 }
 
+// χ³ operators (nl_mode 1: A + diag d1; 2: Newton's stacked system), nrhs = 1
+int residual_nl(fdfd_handle* h, const cplx<double>* x, const cplx<double>* b, cplx<double>* r,
+                std::vector<double>* norms) {
+    const long long N = (long long)h->Nx * h->Ny;
+    const int nb = ceil_div(N, 256), halves = h->nl_mode == 2 ? 2 : 1;
+    RET(ensure_part(h, (size_t)halves * nb * 2));
+    RET(ensure_red(h, (size_t)halves * 2));
+    int ev = prof_begin(h);
+    LAUNCH(residual_nl_kernel, dim3(nb, halves), 256, 0, h->Nx, h->Ny, h->nl_mode, h->st, h->nl_d1, h->nl_d2, x, b,
+           r, norms ? h->part : nullptr);
+    prof_end(h, ev, FDFD_PROF_RESIDUAL, (double)N * halves * (112.0 + 16.0 * (b ? 3 : 2)));
+    if (norms) {
+        LAUNCH(reduce_partials_kernel, halves, 256, 0, h->part, nb, 2, h->red);
+        std::vector<double> per(2 * halves);
+        CK(cudaMemcpyAsync(per.data(), h->red, per.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+        norms->assign(2, 0.0);
+        for (int i = 0; i < halves; ++i) {
+            (*norms)[0] += per[2 * i];
+            (*norms)[1] += per[2 * i + 1];
+        }
+    }
+    return check_launch(h, "residual");
+}
+
 int residual(fdfd_handle* h, const cplx<double>* x, const cplx<double>* b, cplx<double>* r, int nrhs,
              std::vector<double>* norms) {
     if (h->mf) return residual_mf(h, x, b, r, norms);   // nrhs = 1
+    if (h->nl_mode) return residual_nl(h, x, b, r, norms);   // nrhs = 1
     long long N = (long long)h->Nx * h->Ny;
     int nb = ceil_div(N, 256);
     RET(ensure_part(h, (size_t)nrhs * nb * 2));
@@ -996,7 +1041,7 @@ int restart_len(const fdfd_handle* h, int nrhs) {
 }
 
 int ensure_krylov(fdfd_handle* h, int nrhs, int m) {
-    if (h->kr_nrhs >= nrhs && h->kr_m >= m) return FDFD_OK;
+    if (h->kr_nrhs >= nrhs && h->kr_m >= m && h->kr_vlen == vlen(h)) return FDFD_OK;
     dev_free(h->kb); dev_free(h->kx); dev_free(h->kr); dev_free(h->kV); dev_free(h->kZ); dev_free(h->kc);
     long long N = vlen(h);
     size_t v = (size_t)N * nrhs * sizeof(cplx<double>);
@@ -1009,6 +1054,7 @@ int ensure_krylov(fdfd_handle* h, int nrhs, int m) {
     RET(dev_alloc(h, (void**)&h->kc, ((size_t)nrhs * (m + 2) * 2 + 2 * MF_MAX_K) * sizeof(cplx<double>)));
     h->kr_nrhs = nrhs;
     h->kr_m = m;
+    h->kr_vlen = vlen(h);
     return FDFD_OK;
 }
 
@@ -1023,7 +1069,8 @@ int refine(fdfd_handle* h, int nrhs, int* iters, double* relres, bool give_up) {
     if (h->kr_nrhs < nrhs || h->kr_m < 1) return set_err(h, FDFD_EINVAL, "Krylov workspace not allocated");
     const int m = std::min(restart_len(h, nrhs), h->kr_m);
     const size_t vs = (size_t)N * nrhs;   // stride between basis vectors
-    CK(cudaMemsetAsync(h->kx, 0, vs * sizeof(cplx<double>), h->stream));
+    if (!h->warm_start) CK(cudaMemsetAsync(h->kx, 0, vs * sizeof(cplx<double>), h->stream));
+    h->warm_start = false;
     std::vector<double> nrm;
     RET(residual(h, h->kx, h->kb, h->kr, nrhs, &nrm));
     std::vector<double> bnorm(nrhs), rel(nrhs);
@@ -1319,7 +1366,7 @@ void fdfd_destroy(fdfd_handle* h) {
         h->mf = nullptr;
     }
     void* bufs[] = {h->eps, h->sf, h->st, h->derr, h->part, h->red, h->kb, h->kx, h->kr, h->kV, h->kZ, h->kc, h->io,
-                    h->djobs, h->mode_buf};
+                    h->djobs, h->mode_buf, h->nl_d1};
     for (void* p : bufs) dev_free(p);
     free_store(h->f32);
     free_store(h->f64);
@@ -1879,6 +1926,172 @@ int fdfd_flux_integral(fdfd_handle* h, int pol, const double* f1, const double* 
     RET(check_launch(h, "flux lines"));
     CK(cudaMemcpyAsync(flux, dout, (size_t)nlines * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
+    return FDFD_OK;
+}
+
+// ---- χ³ nonlinear driven solve (src/solver/nonlinear.jl) -------------------------
+namespace {
+
+double vnorm(fdfd_handle* h, const cplx<double>* x, long long n) {
+    if (ensure_part(h, 152 * 2) != FDFD_OK || ensure_red(h, 2) != FDFD_OK) return NAN;
+    vdots_kernel<<<dim3(152, 1), 256, 0, h->stream>>>(n, 1, x, 0, x, h->part);
+    reduce_partials_kernel<<<1, 256, 0, h->stream>>>(h->part, 152, 2, h->red);
+    h->launches += 2;
+    double v[2] = {0, 0};
+    if (cudaMemcpyAsync(v, h->red, sizeof v, cudaMemcpyDeviceToHost, h->stream) != cudaSuccess ||
+        cudaStreamSynchronize(h->stream) != cudaSuccess)
+        return NAN;
+    return std::sqrt(std::max(v[0], 0.0));
+}
+
+// restores the handle's single-system state on every exit of fdfd_chi3_solve
+struct NlGuard {
+    fdfd_handle* h;
+    double tol;
+    ~NlGuard() {
+        h->nl_mode = 0;
+        h->nsb = 1;
+        h->tol = tol;
+        h->warm_start = false;
+    }
+};
+
+}  // namespace
+
+int fdfd_chi3_solve(fdfd_handle* h, const double* chi, const double* src, int method, double tol, int maxit,
+                    double* f1, double* f2, double* f3, double* err_hist, int* nerr, fdfd_stats* stats) {
+    if (!h) return FDFD_EINVAL;
+    if (h->mf) return set_err(h, FDFD_EINVAL, "fdfd_chi3_solve: not defined for a modulated device");
+    if (!h->factored || h->op != OP_TM_DRIVEN)
+        return set_err(h, FDFD_EINVAL, "fdfd_chi3_solve needs a factored TM driven operator (fdfd_factor, FDFD_TM)");
+    if (!chi || !src) return set_err(h, FDFD_EINVAL, "fdfd_chi3_solve: NULL argument");
+    if (method != FDFD_CHI3_NEWTON && method != FDFD_CHI3_BORN)
+        return set_err(h, FDFD_EINVAL, "method must be FDFD_CHI3_NEWTON or FDFD_CHI3_BORN");
+    if (!(tol > 0) || maxit < 0) return set_err(h, FDFD_EINVAL, "tol must be positive, maxit >= 0");
+    const long long N = (long long)h->Nx * h->Ny;
+    for (long long k = 0; k < N; ++k)
+        if (!std::isfinite(chi[k])) return set_err(h, FDFD_EINVAL, "chi has a non-finite entry at %lld", k);
+    for (long long k = 0; k < 2 * N; ++k)
+        if (!std::isfinite(src[k])) return set_err(h, FDFD_EINVAL, "src has a non-finite entry");
+    auto t0 = std::chrono::steady_clock::now();
+    const size_t vb = (size_t)N * sizeof(cplx<double>);
+    // scratch: d1 | d2 | tmp (2N) | Z (2N) | B (N) | coeff (N doubles)
+    if (!h->nl_d1) {
+        RET(dev_alloc(h, (void**)&h->nl_d1, 8 * vb + (size_t)N * sizeof(double)));
+        h->nl_d2 = h->nl_d1 + N;
+        h->nl_tmp = h->nl_d2 + N;
+    }
+    cplx<double>* Z = h->nl_tmp + 2 * N;
+    cplx<double>* B = Z + 2 * N;
+    double* dco = reinterpret_cast<double*>(B + N);
+    if (h->io_cap < 4 * vb) {
+        dev_free(h->io);
+        h->io = nullptr;
+        h->dev_bytes -= (long long)h->io_cap;
+        h->io_cap = 0;
+        RET(dev_alloc(h, (void**)&h->io, 4 * vb));
+        h->io_cap = 4 * vb;
+    }
+    cplx<double>* d_src = h->io;
+    // coeff = ω²ϵ₀·3χ/L₀ (nonlinear.jl:74, ϵ₀ normalised)
+    std::vector<double> coeff(N);
+    const double w = h->omega;
+    for (long long k = 0; k < N; ++k) coeff[k] = w * w * (kEPS0 * h->L0) * 3 * chi[k] / h->L0;
+    CK(cudaMemcpyAsync(dco, coeff.data(), N * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(d_src, src, vb, cudaMemcpyHostToDevice, h->stream));
+    NlGuard guard{h, h->tol};
+    // inner linear solves a decade below the nonlinear tolerance (the reference solves them directly)
+    h->tol = std::max(std::min(h->tol, 0.1 * tol), 1e-14);
+    h->nl_mode = 0;
+    h->nsb = 1;
+    cudaEventRecord(h->ev[3], h->stream);
+    RET(ensure_krylov(h, 1, restart_len(h, 1)));
+    RET(scale_vec(h, d_src, std::vector<zd>(1, zd(0, w)), 1, h->kb));   // b = iω·src
+    CK(cudaMemcpyAsync(B, h->kb, vb, cudaMemcpyDeviceToDevice, h->stream));
+    int iters = 0, it = 0;
+    double rel = 0;
+    RET(refine_fb(h, 1, &it, &rel));   // linear solve (nonlinear.jl:71-72)
+    iters += it;
+    CK(cudaMemcpyAsync(Z, h->kx, vb, cudaMemcpyDeviceToDevice, h->stream));
+    std::vector<double> errs(1, 1.0);
+    const int nb = ceil_div(N, 256);
+    if (method == FDFD_CHI3_BORN) {
+        // _doborn (nonlinear.jl:94-108)
+        for (int i = 1; errs.back() > tol && i <= maxit; ++i) {
+            LAUNCH(chi3_diag_kernel, nb, 256, 0, N, 1, dco, Z, h->nl_d1, h->nl_d2);
+            h->nl_mode = 1;
+            h->warm_start = true;   // kx holds the previous iterate
+            RET(refine_fb(h, 1, &it, &rel));
+            iters += it;
+            CK(cudaMemcpyAsync(h->nl_tmp, h->kx, vb, cudaMemcpyDeviceToDevice, h->stream));
+            LAUNCH(vaxpy_kernel, nb, 256, 0, N, -1.0, Z, h->nl_tmp);
+            const double nz = vnorm(h, Z, N), nd = vnorm(h, h->nl_tmp, N);
+            CK(cudaMemcpyAsync(Z, h->kx, vb, cudaMemcpyDeviceToDevice, h->stream));
+            errs.push_back(nd / nz);
+        }
+    } else {
+        // _donewton (nonlinear.jl:110-129) on [e; conj(e)]: J δ = [F; conj F], e ← e − δ.  With
+        // r = b − (A + diag(coeff|e|²)) e = −F the system is solved for δ' = −δ and e += δ'.
+        LAUNCH(vconj_kernel, nb, 256, 0, N, Z, Z + N);
+        h->nsb = 2;
+        RET(ensure_krylov(h, 1, restart_len(h, 1)));
+        for (int i = 1; errs.back() > tol && i <= maxit; ++i) {
+            LAUNCH(chi3_diag_kernel, nb, 256, 0, N, 1, dco, Z, h->nl_d1, h->nl_d2);
+            LAUNCH(residual_nl_kernel, dim3(nb, 1), 256, 0, h->Nx, h->Ny, 1, h->st, h->nl_d1, h->nl_d2, Z, B, h->kb,
+                   nullptr);
+            LAUNCH(vconj_kernel, nb, 256, 0, N, h->kb, h->kb + N);
+            LAUNCH(chi3_diag_kernel, nb, 256, 0, N, 2, dco, Z, h->nl_d1, h->nl_d2);
+            h->nl_mode = 2;
+            RET(refine_fb(h, 1, &it, &rel));
+            iters += it;
+            const double nz = vnorm(h, Z, 2 * N), nd = vnorm(h, h->kx, 2 * N);
+            LAUNCH(vaxpy_kernel, ceil_div(2 * N, 256), 256, 0, 2 * N, 1.0, h->kx, Z);
+            errs.push_back(nd / nz);
+        }
+    }
+    RET(check_launch(h, "chi3"));
+    cudaEventRecord(h->ev[4], h->stream);
+    // H recovery (nonlinear.jl:86-87): the driven TM recovery of the final field
+    std::vector<zd> coef(2);
+    const double mu0 = kMU0 * h->L0;
+    coef[0] = zd(-0.0, (1.0 / w) / mu0);
+    coef[1] = zd(0.0, (-1.0 / w) / mu0);
+    CK(cudaMemcpyAsync(h->kc, coef.data(), 2 * sizeof(zd), cudaMemcpyHostToDevice, h->stream));
+    RecoverArgs ra;
+    ra.Nx = h->Nx; ra.Ny = h->Ny; ra.mode = REC_TM_DRIVEN;
+    ra.idx = 1.0 / h->dx; ra.idy = 1.0 / h->dy; ra.eps0n = kEPS0 * h->L0;
+    LAUNCH(recover_kernel, dim3(nb, 1), 256, 0, ra, h->sf, h->eps, Z, h->kc, h->io + N, h->io + 2 * N);
+    RET(check_launch(h, "recover"));
+    if (f1) CK(cudaMemcpyAsync(f1, Z, vb, cudaMemcpyDeviceToHost, h->stream));
+    if (f2) CK(cudaMemcpyAsync(f2, h->io + N, vb, cudaMemcpyDeviceToHost, h->stream));
+    if (f3) CK(cudaMemcpyAsync(f3, h->io + 2 * N, vb, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    RET(check_device(h, "chi3"));
+    if (err_hist)
+        for (size_t i = 0; i < errs.size() && i <= (size_t)maxit; ++i) err_hist[i] = errs[i];
+    if (nerr) *nerr = (int)errs.size();
+    if (stats) {
+        stats->iterations = iters;
+        stats->nrhs = 1;
+        stats->rel_residual = rel;
+        stats->t_assemble_ms = elapsed_ms(h->ev[0], h->ev[1]);
+        stats->t_factor_ms = elapsed_ms(h->ev[1], h->ev[2]);
+        stats->t_solve_ms = elapsed_ms(h->ev[3], h->ev[4]);
+        stats->t_recover_ms = 0;
+        stats->factor_flops = h->last_factor_flops;
+        stats->block = h->map.b;
+        stats->nblocks = h->map.n;
+        stats->levels = (int)h->steps.size() + 1;
+        stats->tc_gemm = h->tc_used;
+        stats->device_bytes = h->dev_bytes;
+        stats->gpu_launches = h->launches;
+        stats->factor_precision = h->fact_prec;
+        stats->fp64_fallback = h->fell_back;
+        stats->t_total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    }
+    if (errs.back() > tol)
+        return set_err(h, FDFD_ENOCONV, "chi3 %s iteration stopped at step error %.3e > tol %.1e after %d steps",
+                       method == FDFD_CHI3_BORN ? "Born" : "Newton", errs.back(), tol, (int)errs.size() - 1);
     return FDFD_OK;
 }
 

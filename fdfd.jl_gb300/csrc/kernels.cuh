@@ -40,6 +40,13 @@ struct MfResidualArgs {
 };
 __global__ void residual_mf_kernel(MfResidualArgs a, const cplx<double>* deps, const cplx<double>* x,
                                    const cplx<double>* b, cplx<double>* r, double* part);
+__global__ void residual_nl_kernel(int Nx, int Ny, int mode, const cplx<double>* st, const cplx<double>* d1,
+                                   const cplx<double>* d2, const cplx<double>* x, const cplx<double>* b,
+                                   cplx<double>* r, double* part);
+__global__ void chi3_diag_kernel(long long N, int mode, const double* coeff, const cplx<double>* e,
+                                 cplx<double>* d1, cplx<double>* d2);
+__global__ void vconj_kernel(long long n, const cplx<double>* in, cplx<double>* out);
+__global__ void vaxpy_kernel(long long n, double alpha, const cplx<double>* x, cplx<double>* y);
 __global__ void reduce_partials_kernel(const double* part, int nblocks, int nvals, double* out);
 __global__ void recover_kernel(RecoverArgs a, const cplx<double>* sf, const cplx<double>* eps,
                                const cplx<double>* f, const cplx<double>* coef, cplx<double>* g1,

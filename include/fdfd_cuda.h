@@ -49,6 +49,9 @@ extern "C" {
 #define FDFD_X 1           /* src/types.jl:18 (@enum Direction x̂=1 ŷ=2) */
 #define FDFD_Y 2
 
+#define FDFD_CHI3_NEWTON 1 /* src/solver/nonlinear.jl:5 (IterativeMethodGN=1 IterativeMethodB=2) */
+#define FDFD_CHI3_BORN   2
+
 #define FDFD_WHICH_LM 0    /* eigenvalues of A nearest sigma (ARPACK :LM in shift-invert) */
 #define FDFD_WHICH_LR 1    /* largest real part of 1/(λ-σ) (ARPACK :LR in shift-invert)  */
 
@@ -211,6 +214,25 @@ int  fdfd_poynting_device(fdfd_handle* h, int pol, const double* d_f1, const dou
  * and :Ey are used).  FDFD_Y is FDFD_EINVAL, as in the reference. */
 int  fdfd_flux_integral(fdfd_handle* h, int pol, const double* f1, const double* f3,
                         int normal, int nlines, const int* lines, double* flux);
+
+/* χ³ nonlinear TM solve, solve(d::χ3Device, method) (src/solver/nonlinear.jl:36-129)
+ * for the handle's factored TM operator A (fdfd_factor) and one source:
+ * the linear field, then
+ *   FDFD_CHI3_BORN:   e ← (A + diag(c|e|²))⁻¹ b until ||Δe||/||e|| <= tol,
+ *   FDFD_CHI3_NEWTON: Newton on [e; conj e] with J = [A + 2c|e|², c e²;
+ *                     conj(c e²), conj(A + 2c|e|²)] until ||δ||/||[e; conj e]|| <= tol,
+ * c = ω²ϵ₀·3χ/L₀ (chi: Nx*Ny real), at most maxit steps (the reference uses
+ * tol 1e-12, 50).  Each linear system is refined by FGMRES to a decade below
+ * tol, preconditioned by the factor of A (Newton: by blockdiag(A⁻¹, conj(A)⁻¹)
+ * through one two-right-hand-side sweep), so the factorization is reused by
+ * every step.  Outputs Ez, Hx, Hy (driven recovery, may be NULL), the step
+ * errors err_hist[0..*nerr-1] (err_hist[0] = 1 as the reference's history;
+ * capacity maxit+1).  FDFD_ENOCONV when tol is not reached.  The reference's
+ * Born step misplaces a parenthesis in its solve call (nonlinear.jl:99); its
+ * evident intent is implemented. */
+int  fdfd_chi3_solve(fdfd_handle* h, const double* chi, const double* src, int method,
+                     double tol, int maxit, double* f1, double* f2, double* f3,
+                     double* err_hist, int* nerr, fdfd_stats* stats);
 
 /* Modulated device (multi-frequency FDFD): replaces solve(d::ModulatedDevice)
  * (src/solver/modulation.jl:35-119, TM only as the reference).  The handle
