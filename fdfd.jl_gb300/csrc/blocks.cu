@@ -454,13 +454,32 @@ __global__ void __launch_bounds__(512, 1) gj_panel_kernel(Pool<T> M, const int* 
                     f[j] = isp[j] ? cmk((T)0, (T)0) : fi;
                 }
             }
+            if constexpr (sizeof(T) == 4 && C % 2 == 0) {
+                // packed FP32 FMAs (two lanes per instruction, each lane an IEEE fma:
+                // the same results as the scalar form below)
 #pragma unroll
-            for (int j = 0; j < R; ++j)
+                for (int j = 0; j < R; ++j) {
+                    const float2 fi = make_float2(f[j].im, f[j].im), nfr = make_float2(-f[j].re, -f[j].re);
+                    const float2 nfi = make_float2(-f[j].im, -f[j].im);
 #pragma unroll
-                for (int k = 0; k < C; ++k) {
-                    vr[j][k] = fma(-f[j].re, xr[k], fma(f[j].im, xi[k], vr[j][k]));
-                    vi[j][k] = fma(-f[j].re, xi[k], fma(-f[j].im, xr[k], vi[j][k]));
+                    for (int k = 0; k < C; k += 2) {
+                        const float2 x_r = make_float2(xr[k], xr[k + 1]), x_i = make_float2(xi[k], xi[k + 1]);
+                        float2 a = make_float2(vr[j][k], vr[j][k + 1]), c = make_float2(vi[j][k], vi[j][k + 1]);
+                        a = __ffma2_rn(nfr, x_r, __ffma2_rn(fi, x_i, a));
+                        c = __ffma2_rn(nfr, x_i, __ffma2_rn(nfi, x_r, c));
+                        vr[j][k] = a.x; vr[j][k + 1] = a.y;
+                        vi[j][k] = c.x; vi[j][k + 1] = c.y;
+                    }
                 }
+            } else {
+#pragma unroll
+                for (int j = 0; j < R; ++j)
+#pragma unroll
+                    for (int k = 0; k < C; ++k) {
+                        vr[j][k] = fma(-f[j].re, xr[k], fma(f[j].im, xi[k], vr[j][k]));
+                        vi[j][k] = fma(-f[j].re, xi[k], fma(-f[j].im, xr[k], vi[j][k]));
+                    }
+            }
 #pragma unroll
             for (int j = 0; j < R; ++j) {
                 if (cb == g) {
