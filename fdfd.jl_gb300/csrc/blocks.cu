@@ -49,33 +49,37 @@ __global__ void build_tridiag_kernel(NodeMap m, const cplx<double>* st, double s
 //   D_s  = tri_s - [prev elim] diag(l_s) G_prev diag(u_prev) - [next elim] diag(u_s) G_next diag(l_next)
 //   U_s' = next elim ? -diag(u_s) G_next diag(u_next) : diag(u_s)
 //   L_s' = prev elim ? -diag(l_s) G_prev diag(l_prev) : diag(l_s)
-// Tiles of 32 rows x 128 columns, block 256: warp w takes rows w, w+8, ..,
+// Tiles of L1_TR = 16 rows x 128 columns, block 256: warp w takes rows w, w+8,
 // each lane 4 consecutive columns, so block loads and row-major stores are
 // 16-byte vectors and the per-row stencil factors are loaded once per lane.
-// Transposed stores are staged in shared memory and written 32 elements
-// (one transposed row segment) per warp instruction.
-// grid: (ceil(b/128), ceil(b/32), njobs), dynamic smem level1_combine_smem<T>()
+// Transposed stores are staged in shared memory and written as 16-element
+// transposed row segments, two per warp instruction.  The short tile keeps the
+// staging at 34 KB, so five CTAs share an SM (the kernel waits on memory:
+// resident warps are what keeps HBM busy).
+// grid: (ceil(b/128), ceil(b/L1_TR), njobs), dynamic smem level1_combine_smem<T>()
 // ---------------------------------------------------------------------------
 template <typename T> struct Vec16;
 template <> struct Vec16<float> { typedef float4 type; };
 template <> struct Vec16<double> { typedef double2 type; };
 
+constexpr int L1_TR = 16;   // tile rows
 template <typename T>
-constexpr size_t level1_combine_smem() { return (size_t)2 * 2 * 128 * 33 * sizeof(T); }
+constexpr size_t level1_combine_smem() { return (size_t)2 * 2 * 128 * (L1_TR + 1) * sizeof(T) + 4 * 128 * 2 * sizeof(T); }
 
 template <typename T>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) level1_combine_kernel(NodeMap m, const cplx<double>* st, double scale,
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 5 : 1) level1_combine_kernel(NodeMap m, const cplx<double>* st, double scale,
                                                              Pool<T> D, Pool<T> C, const L1Job* jobs) {
     constexpr int CPL = 4;                    // columns per lane
     constexpr int VW = 16 / sizeof(T);
     constexpr int NVL = CPL / VW;             // 16-byte vectors per lane and plane
     typedef typename Vec16<T>::type VT;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    T* tU = reinterpret_cast<T*>(smem_raw);  // [plane][tile column][tile row], row stride 33
-    T* tL = tU + 2 * 128 * 33;
+    constexpr int SR = L1_TR + 1;            // staging row stride
+    T* tU = reinterpret_cast<T*>(smem_raw);  // [plane][tile column][tile row]
+    T* tL = tU + 2 * 128 * SR;
     const L1Job J = jobs[blockIdx.z];
     const int b = m.b;
-    const int c0 = blockIdx.x * 128, r0 = blockIdx.y * 32;
+    const int c0 = blockIdx.x * 128, r0 = blockIdx.y * L1_TR;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int cl0 = lane * CPL;              // first tile column of this lane
     const int cb0 = c0 + cl0;                // its matrix column
@@ -90,25 +94,22 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) level1_combine_ke
     // stencil values are FP64; the arithmetic runs in the factor precision T
     auto tv = [&](cplx<double> v) { return cmk((T)(v.re * scale), (T)(v.im * scale)); };
     const cplx<T> z = cmk((T)0, (T)0);
-    cplx<T> lcn[CPL], ucn[CPL], ucp[CPL], lcp[CPL];
-#pragma unroll
-    for (int e = 0; e < CPL; ++e) {
-        const int c = cb0 + e;
-        lcn[e] = ucn[e] = ucp[e] = lcp[e] = z;
+    // per-column coupling factors of the neighbours, shared by the tile's rows:
+    // [0] l_next, [1] u_next, [2] u_prev, [3] l_prev for the 128 tile columns
+    cplx<T>* fac = reinterpret_cast<cplx<T>*>(tL + 2 * 128 * SR);
+    for (int t = threadIdx.x; t < 4 * 128; t += 256) {
+        const int k = t / 128, c = c0 + t % 128;
+        cplx<T> v = z;
         if (c < b) {
-            if (J.next_elim) {
-                lcn[e] = tv(st_at<T>(st, m, m.p_cprev(), J.next, c));
-                ucn[e] = tv(st_at<T>(st, m, m.p_cnext(), J.next, c));
-            }
-            if (J.prev_elim) {
-                ucp[e] = tv(st_at<T>(st, m, m.p_cnext(), J.prev, c));
-                lcp[e] = tv(st_at<T>(st, m, m.p_cprev(), J.prev, c));
-            }
+            if (k < 2 && J.next_elim) v = tv(st_at<T>(st, m, k == 0 ? m.p_cprev() : m.p_cnext(), J.next, c));
+            if (k >= 2 && J.prev_elim) v = tv(st_at<T>(st, m, k == 2 ? m.p_cnext() : m.p_cprev(), J.prev, c));
         }
+        fac[t] = v;
     }
+    __syncthreads();
     const bool full = cb0 + CPL <= b;        // all four columns inside the matrix
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
+    for (int q = 0; q < L1_TR / 8; ++q) {
         const int rl = warp + 8 * q;
         const int r = r0 + rl;
         if (r >= b || cb0 >= b) {
@@ -152,15 +153,15 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) level1_combine_ke
             cplx<T> uv = z, lv = z;
             if (J.prev_elim) {
                 const cplx<T> lg = cmul(ls, cmk(gpr[e], gpi[e]));
-                dv = csub(dv, cmul(lg, ucp[e]));
-                lv = cneg(cmul(lg, lcp[e]));
+                dv = csub(dv, cmul(lg, fac[2 * 128 + cl0 + e]));
+                lv = cneg(cmul(lg, fac[3 * 128 + cl0 + e]));
             } else if (c == r) {
                 lv = ls;
             }
             if (J.next_elim) {
                 const cplx<T> ug = cmul(us, cmk(gnr[e], gni[e]));
-                dv = csub(dv, cmul(ug, lcn[e]));
-                uv = cneg(cmul(ug, ucn[e]));
+                dv = csub(dv, cmul(ug, fac[cl0 + e]));
+                uv = cneg(cmul(ug, fac[128 + cl0 + e]));
             } else if (c == r) {
                 uv = us;
             }
@@ -195,29 +196,31 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) level1_combine_ke
         else {
 #pragma unroll
             for (int e = 0; e < CPL; ++e) {
-                tU[(cl0 + e) * 33 + rl] = ur[e];
-                tU[128 * 33 + (cl0 + e) * 33 + rl] = ui[e];
+                tU[(cl0 + e) * SR + rl] = ur[e];
+                tU[128 * SR + (cl0 + e) * SR + rl] = ui[e];
             }
         }
         if (!J.l_trans) put_row(Ls, cpe, lr, li);
         else {
 #pragma unroll
             for (int e = 0; e < CPL; ++e) {
-                tL[(cl0 + e) * 33 + rl] = lr[e];
-                tL[128 * 33 + (cl0 + e) * 33 + rl] = li[e];
+                tL[(cl0 + e) * SR + rl] = lr[e];
+                tL[128 * SR + (cl0 + e) * SR + rl] = li[e];
             }
         }
     }
     if (J.u_trans || J.l_trans) {
         __syncthreads();
-        // transposed store: element (r, c) -> position (c, r); warp w writes the
-        // transposed rows c0+w, c0+w+8, ..., lane = tile row
-        const int rr = r0 + lane;
-        for (int cl = warp; cl < 128; cl += 8) {
+        // transposed store: element (r, c) -> position (c, r); a warp instruction
+        // writes two transposed row segments (tile columns cl, cl+1), lane % 16 =
+        // tile row
+        const int tr = lane % L1_TR;
+        const int rr = r0 + tr;
+        for (int cl = 2 * warp + lane / L1_TR; cl < 128; cl += 16) {
             const int cc = c0 + cl;
             if (cc >= b || rr >= b) continue;
-            if (J.u_trans) store_elem<T>(C, Us, cc, rr, cmk(tU[cl * 33 + lane], tU[128 * 33 + cl * 33 + lane]), 0);
-            if (J.l_trans) store_elem<T>(C, Ls, cc, rr, cmk(tL[cl * 33 + lane], tL[128 * 33 + cl * 33 + lane]), 0);
+            if (J.u_trans) store_elem<T>(C, Us, cc, rr, cmk(tU[cl * SR + tr], tU[128 * SR + cl * SR + tr]), 0);
+            if (J.l_trans) store_elem<T>(C, Ls, cc, rr, cmk(tL[cl * SR + tr], tL[128 * SR + cl * SR + tr]), 0);
         }
     }
 }
@@ -996,8 +999,8 @@ void launch_level1_combine(cudaStream_t s, int njobs, NodeMap m, const cplx<doub
     static const cudaError_t attr =
         cudaFuncSetAttribute(level1_combine_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     (void)attr;
-    level1_combine_kernel<T><<<dim3(ceil_div(m.b, 128), ceil_div(m.b, 32), njobs), 256, smem, s>>>(m, st, scale, D,
-                                                                                                  C, jobs);
+    level1_combine_kernel<T><<<dim3(ceil_div(m.b, 128), ceil_div(m.b, L1_TR), njobs), 256, smem, s>>>(m, st, scale,
+                                                                                                     D, C, jobs);
 }
 void launch_perm_init(cudaStream_t s, int njobs, int* perm, int b) {
     perm_init_kernel<int><<<dim3(ceil_div(b, 256), njobs), 256, 0, s>>>(perm, b);
