@@ -916,7 +916,12 @@ __global__ void __launch_bounds__(128) tri_columns_kernel(int b, Pool<T> D, cons
     const long long pe = D.plane_elems();
     T* Gim = Gre + pe;
     const int ld = D.ld;
-    const int i0 = j > 0 ? j - 1 : 0;          // rows above j-1 of T0⁻¹ e_j are zero after L⁻¹
+    // rows above j-1 of L⁻¹ e_j are zero.  The forward recurrence starts at the
+    // same row for the whole warp (its first column's j-1): a lane whose unit
+    // entry comes later carries zeros until then, and the warp's stores of a
+    // row stay one coalesced segment.
+    const int jw = j & ~31;
+    const int i0 = jw > 0 ? jw - 1 : 0;
     // forward: y = L⁻¹ e_j, rows i0 .. b-2 stored in G (as scratch)
     cplx<T> cur = cmk((T)(j == i0 ? 1 : 0), (T)0);
     for (int i = i0; i + 1 < b; ++i) {
