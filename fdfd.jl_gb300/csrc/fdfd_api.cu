@@ -195,6 +195,39 @@ namespace {
 // length of one refinement vector (unknowns of the solved system)
 long long vlen(const fdfd_handle* h) { return (long long)h->Nx * h->Ny * h->nsb; }
 
+// index of the first NaN/Inf in x[0..n), or -1.  Input validation runs on every
+// host-buffer call, so each 4096-value chunk is first tested by a branch-free
+// exponent test (vectorised by the compiler) and searched only if it fails.
+long long first_nonfinite(const double* x, long long n) {
+    constexpr uint64_t kExp = 0x7ff0000000000000ull;
+    for (long long c = 0; c < n; c += 4096) {
+        const long long e = std::min(n, c + 4096);
+        uint64_t bad = 0;
+        for (long long k = c; k < e; ++k) {
+            uint64_t u;
+            memcpy(&u, x + k, sizeof u);
+            bad |= (uint64_t)((u & kExp) == kExp);
+        }
+        if (bad)
+            for (long long k = c; k < e; ++k)
+                if (!std::isfinite(x[k])) return k;
+    }
+    return -1;
+}
+
+// index of the first complex zero among the n interleaved values z, or -1
+long long first_zero(const double* z, long long n) {
+    for (long long c = 0; c < n; c += 4096) {
+        const long long e = std::min(n, c + 4096);
+        int any = 0;
+        for (long long k = c; k < e; ++k) any |= (z[2 * k] == 0.0) & (z[2 * k + 1] == 0.0);
+        if (any)
+            for (long long k = c; k < e; ++k)
+                if (z[2 * k] == 0.0 && z[2 * k + 1] == 0.0) return k;
+    }
+    return -1;
+}
+
 int set_err(fdfd_handle* h, int code, const char* fmt, ...) {
     char buf[512];
     va_list ap;
@@ -1403,10 +1436,9 @@ int fdfd_set_fallback(fdfd_handle* h, int on) {
 int fdfd_set_eps(fdfd_handle* h, const double* eps_r) {
     if (!h || !eps_r) return h ? set_err(h, FDFD_EINVAL, "eps_r is NULL") : FDFD_EINVAL;
     long long N = (long long)h->Nx * h->Ny;
-    for (long long k = 0; k < 2 * N; ++k)
-        if (!std::isfinite(eps_r[k])) return set_err(h, FDFD_EINVAL, "eps_r has a non-finite entry at %lld", k / 2);
-    for (long long k = 0; k < N; ++k)
-        if (eps_r[2 * k] == 0 && eps_r[2 * k + 1] == 0) return set_err(h, FDFD_EINVAL, "eps_r is zero at %lld", k);
+    if (const long long k = first_nonfinite(eps_r, 2 * N); k >= 0)
+        return set_err(h, FDFD_EINVAL, "eps_r has a non-finite entry at %lld", k / 2);
+    if (const long long k = first_zero(eps_r, N); k >= 0) return set_err(h, FDFD_EINVAL, "eps_r is zero at %lld", k);
     CK(cudaMemcpyAsync(h->eps, eps_r, N * sizeof(cplx<double>), cudaMemcpyHostToDevice, h->stream));
     if (h->mf)
         for (fdfd_handle* s : h->mf->sub) {
@@ -1526,8 +1558,7 @@ int fdfd_solve(fdfd_handle* h, const double* src, int nrhs, double* f1, double* 
     if (!src || nrhs < 1) return set_err(h, FDFD_EINVAL, "invalid source arguments");
     auto t0 = std::chrono::steady_clock::now();
     long long N = (long long)h->Nx * h->Ny;
-    for (long long k = 0; k < 2 * N * nrhs; ++k)
-        if (!std::isfinite(src[k])) return set_err(h, FDFD_EINVAL, "src has a non-finite entry");
+    if (first_nonfinite(src, 2 * N * nrhs) >= 0) return set_err(h, FDFD_EINVAL, "src has a non-finite entry");
     size_t bytes = (size_t)N * nrhs * sizeof(cplx<double>);
     // staging: [src | f1 | f2 | f3], kept by the handle between calls
     if (h->io_cap < 4 * bytes) {
@@ -1599,8 +1630,8 @@ int fdfd_mf_set_deps(fdfd_handle* h, const double* deps_r) {
     if (!h->mf) return set_err(h, FDFD_EINVAL, "not a modulated device handle (fdfd_mf_create)");
     if (!deps_r) return set_err(h, FDFD_EINVAL, "deps_r is NULL");
     const long long N = (long long)h->Nx * h->Ny;
-    for (long long k = 0; k < 2 * N; ++k)
-        if (!std::isfinite(deps_r[k])) return set_err(h, FDFD_EINVAL, "deps_r has a non-finite entry at %lld", k / 2);
+    if (const long long k = first_nonfinite(deps_r, 2 * N); k >= 0)
+        return set_err(h, FDFD_EINVAL, "deps_r has a non-finite entry at %lld", k / 2);
     CK(cudaMemcpyAsync(h->mf->deps, deps_r, N * sizeof(cplx<double>), cudaMemcpyHostToDevice, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     return FDFD_OK;
@@ -1638,8 +1669,7 @@ int fdfd_mf_solve(fdfd_handle* h, const double* src, double* ez, double* hx, dou
     auto t0 = std::chrono::steady_clock::now();
     MfState& M = *h->mf;
     const long long N = (long long)h->Nx * h->Ny;
-    for (long long k = 0; k < 2 * N; ++k)
-        if (!std::isfinite(src[k])) return set_err(h, FDFD_EINVAL, "src has a non-finite entry");
+    if (first_nonfinite(src, 2 * N) >= 0) return set_err(h, FDFD_EINVAL, "src has a non-finite entry");
     const size_t bytes = (size_t)N * M.K * sizeof(cplx<double>);
     if (h->io_cap < 4 * bytes) {
         dev_free(h->io);
@@ -1969,10 +1999,9 @@ int fdfd_chi3_solve(fdfd_handle* h, const double* chi, const double* src, int me
         return set_err(h, FDFD_EINVAL, "method must be FDFD_CHI3_NEWTON or FDFD_CHI3_BORN");
     if (!(tol > 0) || maxit < 0) return set_err(h, FDFD_EINVAL, "tol must be positive, maxit >= 0");
     const long long N = (long long)h->Nx * h->Ny;
-    for (long long k = 0; k < N; ++k)
-        if (!std::isfinite(chi[k])) return set_err(h, FDFD_EINVAL, "chi has a non-finite entry at %lld", k);
-    for (long long k = 0; k < 2 * N; ++k)
-        if (!std::isfinite(src[k])) return set_err(h, FDFD_EINVAL, "src has a non-finite entry");
+    if (const long long k = first_nonfinite(chi, N); k >= 0)
+        return set_err(h, FDFD_EINVAL, "chi has a non-finite entry at %lld", k);
+    if (first_nonfinite(src, 2 * N) >= 0) return set_err(h, FDFD_EINVAL, "src has a non-finite entry");
     auto t0 = std::chrono::steady_clock::now();
     const size_t vb = (size_t)N * sizeof(cplx<double>);
     // scratch: d1 | d2 | tmp (2N) | Z (2N) | B (N) | coeff (N doubles)
@@ -2148,9 +2177,8 @@ int fdfd_adjoint(fdfd_handle* h, const double* src, const double* mvec, double* 
         return set_err(h, FDFD_EINVAL, "fdfd_adjoint needs a factored TM driven operator (fdfd_factor, FDFD_TM)");
     auto t0 = std::chrono::steady_clock::now();
     const long long N = (long long)h->Nx * h->Ny;
-    for (long long k = 0; k < 2 * N; ++k)
-        if (!std::isfinite(src[k]) || !std::isfinite(mvec[k]))
-            return set_err(h, FDFD_EINVAL, "fdfd_adjoint: non-finite input");
+    if (first_nonfinite(src, 2 * N) >= 0 || first_nonfinite(mvec, 2 * N) >= 0)
+        return set_err(h, FDFD_EINVAL, "fdfd_adjoint: non-finite input");
     const size_t bytes = (size_t)N * sizeof(cplx<double>);
     RET(ensure_krylov(h, 2, restart_len(h, 2)));
     if (h->io_cap < 4 * bytes) {
