@@ -243,9 +243,9 @@ __global__ void perm_init_kernel(int* perm, int b) {
 //     -M[i,j]·(scaled pivot row) with its pivot-column entry set to -M[i,j]/p.
 //     The result G (b x w) holds the panel's block transformation;
 //  2. composes the panel's row exchanges into rowsrc (row r of the exchanged
-//     matrix is row rowsrc[r] of M) and into perm; no row of M moves;
-//  3. writes Rᵀ: the exchanged panel rows M[rowsrc[c0:c0+w], :] transposed,
-//     with the panel columns replaced by the identity.
+//     matrix is row rowsrc[r] of M) and into perm; no row of M moves.
+// gj_rt_kernel then writes Rᵀ: the exchanged panel rows M[rowsrc[c0:c0+w], :]
+// transposed, with the panel columns replaced by the identity.
 // The rank-w update M' = mask(M[rowsrc]) + G·R is then one TN GEMM
 // (gemm_*_kernel with mask [c0, c0+w) reading its β term through rowsrc into
 // a second buffer).  After the last panel M holds (P M₀)⁻¹, and
@@ -282,19 +282,18 @@ template <typename T> __device__ __forceinline__ cplx<T> cinv_pow2(cplx<T> z) {
     return cmk(ldexp(a * r, -e), ldexp(-b * r, -e));
 }
 
-// dynamic shared memory of gj_panel_kernel (elements of T): the largest of the
-// G staging tile (128 rows x NB+4, re and im), the Rᵀ transpose tile (NB x 129,
-// re and im) and the double-buffered pivot column (2 x 2 planes x 128*R)
+// dynamic shared memory of gj_panel_kernel (elements of T): the larger of the
+// G staging tile (128 rows x NB+4, re and im) and the double-buffered pivot
+// column (2 x 2 planes x 128*R)
 template <int NB, int R>
 __host__ __device__ constexpr size_t gj_panel_smem_elems() {
-    return (size_t)2 * (128 * (NB + 4) > NB * 129 ? (128 * (NB + 4) > 2 * 128 * R ? 128 * (NB + 4) : 2 * 128 * R)
-                                                  : (NB * 129 > 2 * 128 * R ? NB * 129 : 2 * 128 * R));
+    return (size_t)2 * (128 * (NB + 4) > 2 * 128 * R ? 128 * (NB + 4) : 2 * 128 * R);
 }
 
 
 template <typename T, int NB, int R, int C>
-__global__ void __launch_bounds__(512, 1) gj_panel_kernel(Pool<T> M, const int* slots, Pool<T> GP, Pool<T> RP,
-                                                          int* perm, int* rowsrc, int c0, unsigned* err) {
+__global__ void __launch_bounds__(512, 1) gj_panel_kernel(Pool<T> M, const int* slots, Pool<T> GP, int* perm,
+                                                          int* rowsrc, int c0, unsigned* err) {
     constexpr int NT = 512;
     constexpr int NCB = NB / C;                        // column blocks
     constexpr int TPB = NT / NCB;                      // threads per column block
@@ -590,55 +589,66 @@ __global__ void __launch_bounds__(512, 1) gj_panel_kernel(Pool<T> M, const int* 
             if (i < b) { pp[i] = pv[t]; rs[i] = rsm[i]; }
         }
     }
-    // 3. Rᵀ (b x RP.cols): RT[c][k] = (row c0+k after the exchanges)[c], identity on the
-    //    panel columns; staged through shared memory so reads and writes coalesce.
-    //    Each thread issues all of its loads of a tile before its shared-memory stores.
-    {
-        T* rt = RP.slot(job);
-        const int rc = RP.cols;
-        const long long pe = RP.plane_elems();
-        constexpr int TW = 128;                        // columns per staging tile
-        constexpr int IT = NB * TW / NT;               // loads per thread per tile
-        static_assert((NB * TW) % NT == 0, "tile split");
-        for (int cb = 0; cb < b; cb += TW) {
-            const int cw = min(TW, b - cb);
-            T la[IT], lb[IT];
+}
+
+// Rᵀ of a panel (b x RP.cols): RT[c][k] = (row c0+k after the panel's exchanges)[c],
+// the identity on the panel columns, read through rowsrc (row r of the exchanged
+// matrix is row rowsrc[r] of M).  A separate launch from the panel kernel: the
+// rows it reads outside the panel are written by the previous panel's wide
+// update, which the look-ahead runs concurrently with this panel's column steps.
+// One CTA per 128 columns and matrix; the tile is staged through shared memory so
+// reads and writes coalesce.  grid: (ceil(b/128), njobs), block 512
+template <typename T, int NB>
+__global__ void __launch_bounds__(512) gj_rt_kernel(Pool<T> M, const int* slots, Pool<T> RP, const int* rowsrc,
+                                                    int c0) {
+    constexpr int NT = 512, TW = 128;
+    constexpr int IT = NB * TW / NT;               // loads per thread
+    static_assert((NB * TW) % NT == 0, "tile split");
+    __shared__ T buf[2 * NB * (TW + 1)];
+    const int b = M.rows, tid = threadIdx.x, job = blockIdx.y;
+    const int cb = blockIdx.x * TW, cw = min(TW, b - cb);
+    const int w = min(NB, b - c0);
+    const T* Mre = M.slot(slots[job]);
+    const T* Mim = Mre + M.plane_elems();
+    const int ld = M.ld;
+    const int* rs = rowsrc + (size_t)job * b;
+    T* rt = RP.slot(job);
+    const int rc = RP.cols;
+    const long long pe = RP.plane_elems();
+    T la[IT], lb[IT];
 #pragma unroll
-            for (int u = 0; u < IT; ++u) {
-                const int idx = tid + u * NT;
-                const int k = idx / TW, c = idx % TW;
-                const int cc = cb + c;
-                la[u] = 0; lb[u] = 0;
-                if (k < w && c < cw) {
-                    if (cc >= c0 && cc < c0 + w) la[u] = (T)((cc - c0) == k ? 1 : 0);
-                    else {
-                        const int sr = rsm[c0 + k];
-                        la[u] = Mre[(size_t)sr * ld + cc];
-                        lb[u] = Mim[(size_t)sr * ld + cc];
-                    }
-                }
+    for (int u = 0; u < IT; ++u) {
+        const int idx = tid + u * NT;
+        const int k = idx / TW, c = idx % TW;
+        const int cc = cb + c;
+        la[u] = 0; lb[u] = 0;
+        if (k < w && c < cw) {
+            if (cc >= c0 && cc < c0 + w) la[u] = (T)((cc - c0) == k ? 1 : 0);
+            else {
+                const int sr = rs[c0 + k];
+                la[u] = Mre[(size_t)sr * ld + cc];
+                lb[u] = Mim[(size_t)sr * ld + cc];
             }
+        }
+    }
 #pragma unroll
-            for (int u = 0; u < IT; ++u) {
-                const int idx = tid + u * NT;
-                const int k = idx / TW, c = idx % TW;
-                buf[2 * (k * (TW + 1) + c)] = la[u];
-                buf[2 * (k * (TW + 1) + c) + 1] = lb[u];
-            }
-            __syncthreads();
-            for (int idx = tid; idx < cw * rc; idx += NT) {
-                const int c = idx / rc, k = idx % rc;
-                T a = 0, d = 0;
-                if (k < NB) { a = buf[2 * (k * (TW + 1) + c)]; d = buf[2 * (k * (TW + 1) + c) + 1]; }
-                const long long o = (long long)(cb + c) * RP.ld + k;
-                rt[o] = a;
-                rt[pe + o] = d;
-                if (RP.planes == 4) {   // pre-split tensor-core operand
-                    rt[2 * pe + o] = (T)tf32_lo((float)a);
-                    rt[3 * pe + o] = (T)tf32_lo((float)d);
-                }
-            }
-            __syncthreads();
+    for (int u = 0; u < IT; ++u) {
+        const int idx = tid + u * NT;
+        const int k = idx / TW, c = idx % TW;
+        buf[2 * (k * (TW + 1) + c)] = la[u];
+        buf[2 * (k * (TW + 1) + c) + 1] = lb[u];
+    }
+    __syncthreads();
+    for (int idx = tid; idx < cw * rc; idx += NT) {
+        const int c = idx / rc, k = idx % rc;
+        T a = 0, d = 0;
+        if (k < NB) { a = buf[2 * (k * (TW + 1) + c)]; d = buf[2 * (k * (TW + 1) + c) + 1]; }
+        const long long o = (long long)(cb + c) * RP.ld + k;
+        rt[o] = a;
+        rt[pe + o] = d;
+        if (RP.planes == 4) {   // pre-split tensor-core operand
+            rt[2 * pe + o] = (T)tf32_lo((float)a);
+            rt[3 * pe + o] = (T)tf32_lo((float)d);
         }
     }
 }
@@ -1011,29 +1021,39 @@ void launch_perm_init(cudaStream_t s, int njobs, int* perm, int b) {
     perm_init_kernel<int><<<dim3(ceil_div(b, 256), njobs), 256, 0, s>>>(perm, b);
 }
 template <typename T, int NB, int R, int C>
-static int gj_panel_launch(cudaStream_t s, int njobs, Pool<T> M, const int* slots, Pool<T> GP, Pool<T> RP,
-                           int* perm, int* rowsrc, int c0, unsigned* err) {
+static int gj_panel_launch(cudaStream_t s, int njobs, Pool<T> M, const int* slots, Pool<T> GP, int* perm,
+                           int* rowsrc, int c0, unsigned* err) {
     const size_t smem = gj_panel_smem_elems<NB, R>() * sizeof(T);
     static const cudaError_t attr =
         cudaFuncSetAttribute(gj_panel_kernel<T, NB, R, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (attr != cudaSuccess) return (int)attr;
-    gj_panel_kernel<T, NB, R, C><<<njobs, 512, smem, s>>>(M, slots, GP, RP, perm, rowsrc, c0, err);
+    gj_panel_kernel<T, NB, R, C><<<njobs, 512, smem, s>>>(M, slots, GP, perm, rowsrc, c0, err);
     return (int)cudaGetLastError();
 }
 
 template <typename T>
-int launch_gj_panel(cudaStream_t s, int nb, int njobs, Pool<T> M, const int* slots, Pool<T> GP, Pool<T> RP,
-                    int* perm, int* rowsrc, int c0, unsigned* err) {
+int launch_gj_panel(cudaStream_t s, int nb, int njobs, Pool<T> M, const int* slots, Pool<T> GP, int* perm,
+                    int* rowsrc, int c0, unsigned* err) {
     const bool two = M.rows > 512;
     if (M.rows > 1024) return (int)cudaErrorInvalidValue;
     if constexpr (sizeof(T) == 4) {
-        if (nb == 32 && !two) return gj_panel_launch<T, 32, 4, 8>(s, njobs, M, slots, GP, RP, perm, rowsrc, c0, err);
-        if (nb == 16 && two) return gj_panel_launch<T, 16, 8, 4>(s, njobs, M, slots, GP, RP, perm, rowsrc, c0, err);
+        if (nb == 32 && !two) return gj_panel_launch<T, 32, 4, 8>(s, njobs, M, slots, GP, perm, rowsrc, c0, err);
+        if (nb == 16 && two) return gj_panel_launch<T, 16, 8, 4>(s, njobs, M, slots, GP, perm, rowsrc, c0, err);
     } else {
-        if (nb == 16 && !two) return gj_panel_launch<T, 16, 4, 4>(s, njobs, M, slots, GP, RP, perm, rowsrc, c0, err);
-        if (nb == 8 && two) return gj_panel_launch<T, 8, 8, 2>(s, njobs, M, slots, GP, RP, perm, rowsrc, c0, err);
+        if (nb == 16 && !two) return gj_panel_launch<T, 16, 4, 4>(s, njobs, M, slots, GP, perm, rowsrc, c0, err);
+        if (nb == 8 && two) return gj_panel_launch<T, 8, 8, 2>(s, njobs, M, slots, GP, perm, rowsrc, c0, err);
     }
     return (int)cudaErrorInvalidValue;
+}
+template <typename T>
+int launch_gj_rt(cudaStream_t s, int nb, int njobs, Pool<T> M, const int* slots, Pool<T> RP, const int* rowsrc,
+                 int c0) {
+    const dim3 grid(ceil_div(M.rows, 128), njobs);
+    if (nb == 32) gj_rt_kernel<T, 32><<<grid, 512, 0, s>>>(M, slots, RP, rowsrc, c0);
+    else if (nb == 16) gj_rt_kernel<T, 16><<<grid, 512, 0, s>>>(M, slots, RP, rowsrc, c0);
+    else if (nb == 8) gj_rt_kernel<T, 8><<<grid, 512, 0, s>>>(M, slots, RP, rowsrc, c0);
+    else return (int)cudaErrorInvalidValue;
+    return (int)cudaGetLastError();
 }
 template <typename T>
 void launch_gj_unpermute(cudaStream_t s, int njobs, Pool<T> Src, const int* sslots, Pool<T> Dst,
@@ -1055,8 +1075,9 @@ void launch_mcopy(cudaStream_t s, int njobs, Pool<T> S, Pool<T> Dp, const int3* 
                                           const int*);                                                       \
     template void launch_level1_combine<T>(cudaStream_t, int, NodeMap, const cplx<double>*, double, Pool<T>,  \
                                            Pool<T>, const L1Job*);                                           \
-    template int launch_gj_panel<T>(cudaStream_t, int, int, Pool<T>, const int*, Pool<T>, Pool<T>, int*, int*,\
-                                    int, unsigned*);                                                         \
+    template int launch_gj_panel<T>(cudaStream_t, int, int, Pool<T>, const int*, Pool<T>, int*, int*, int,    \
+                                    unsigned*);                                                              \
+    template int launch_gj_rt<T>(cudaStream_t, int, int, Pool<T>, const int*, Pool<T>, const int*, int);    \
     template void launch_gj_unpermute<T>(cudaStream_t, int, Pool<T>, const int*, Pool<T>, const int*,        \
                                          const int*);                                                       \
     template void launch_madd<T>(cudaStream_t, int, Pool<T>, const int3*);                                    \

@@ -701,16 +701,23 @@ template <typename T> int gj_invert(fdfd_handle* h, const int* d_slots, const in
         int* rs = F.rowsrc + (size_t)par * h->max_ne * b;
         const int* pslots = F.gj_slots + par * h->max_ne;   // GP/RP slots of this parity
         int ev = prof_begin(h);
-        int e = launch_gj_panel<T>(h->stream, nb, njobs, pool_of(F, cur), cur_slots, GPp, RPp, F.perm, rs, c0,
-                                   h->derr);
-        prof_end(h, ev, FDFD_PROF_GJ_PANEL, 0.0);
+        int e = launch_gj_panel<T>(h->stream, nb, njobs, pool_of(F, cur), cur_slots, GPp, F.perm, rs, c0, h->derr);
         h->launches++;
         if (e) return set_err(h, FDFD_ECUDA, "gj_panel launch failed: %s", cudaGetErrorString((cudaError_t)e));
+        // Rᵀ reads the pivot rows in full: the previous panel's wide update, which ran
+        // concurrently with this panel's column steps, must have finished
+        if (wide_pending) {
+            CK(cudaStreamWaitEvent(h->stream, h->ev_wide, 0));
+            wide_pending = false;
+        }
+        e = launch_gj_rt<T>(h->stream, nb, njobs, pool_of(F, cur), cur_slots, RPp, rs, c0);
+        prof_end(h, ev, FDFD_PROF_GJ_PANEL, 0.0);
+        h->launches++;
+        if (e) return set_err(h, FDFD_ECUDA, "gj_rt launch failed: %s", cudaGetErrorString((cudaError_t)e));
         const double ubytes = 4.0 * sizeof(T) * (double)b * b * njobs;
         if (overlap && p + 1 < npan) {
             const int c1 = c0 + nb, w1 = std::min(nb, b - c1);
             CK(cudaEventRecord(h->ev_panel, h->stream));
-            if (wide_pending) CK(cudaStreamWaitEvent(h->stream, h->ev_wide, 0));
             RET(gemm<T>(h, P_GP, P_RP, alt, pslots, pslots, alt_slots, nullptr, 0, njobs, b, w1, F.GP.cols, (T)1, 1,
                         c0, w, cur, cur_slots, rs, FDFD_PROF_GJ_UPDATE, ubytes * w1 / b, h->stream, c1));
             CK(cudaStreamWaitEvent(h->stream2, h->ev_panel, 0));
@@ -720,10 +727,6 @@ template <typename T> int gj_invert(fdfd_handle* h, const int* d_slots, const in
             CK(cudaEventRecord(h->ev_wide, h->stream2));
             wide_pending = true;
         } else {
-            if (wide_pending) {
-                CK(cudaStreamWaitEvent(h->stream, h->ev_wide, 0));
-                wide_pending = false;
-            }
             RET(gemm<T>(h, P_GP, P_RP, alt, pslots, pslots, alt_slots, nullptr, 0, njobs, b, b, F.GP.cols, (T)1, 1,
                         c0, w, cur, cur_slots, rs, FDFD_PROF_GJ_UPDATE, ubytes));
         }

@@ -89,12 +89,17 @@ template <typename T>
 void launch_tri_inverse(cudaStream_t s, int njobs, NodeMap m, const cplx<double>* st, double scale, Pool<T> D,
                         const int* nodes, cplx<T>* fac, int* piv, unsigned* err);
 // Gauss-Jordan panel step with panel width nb on the matrices M[slots[job]]
-// (returns a cudaError_t value).  Writes the panel transformation to GP, the
-// transposed pivot rows to RP, updates perm and writes rowsrc[job][r], the
-// row of M that lands at row r after this panel's interchanges.
+// (returns a cudaError_t value).  Writes the panel transformation to GP,
+// updates perm and writes rowsrc[job][r], the row of M that lands at row r
+// after this panel's interchanges.
 template <typename T>
-int launch_gj_panel(cudaStream_t s, int nb, int njobs, Pool<T> M, const int* slots, Pool<T> GP, Pool<T> RP,
-                    int* perm, int* rowsrc, int c0, unsigned* err);
+int launch_gj_panel(cudaStream_t s, int nb, int njobs, Pool<T> M, const int* slots, Pool<T> GP, int* perm,
+                    int* rowsrc, int c0, unsigned* err);
+// The panel's transposed pivot rows (identity on the panel columns) into RP,
+// read from M through rowsrc; M must hold the rows after the previous update.
+template <typename T>
+int launch_gj_rt(cudaStream_t s, int nb, int njobs, Pool<T> M, const int* slots, Pool<T> RP, const int* rowsrc,
+                 int c0);
 // Dst[dslots[job]][r][perm[j]] = Src[sslots[job]][r][j] (Src may equal Dst)
 template <typename T>
 void launch_gj_unpermute(cudaStream_t s, int njobs, Pool<T> Src, const int* sslots, Pool<T> Dst,
