@@ -653,6 +653,251 @@ __global__ void __launch_bounds__(512) gj_rt_kernel(Pool<T> M, const int* slots,
     }
 }
 
+// Gauss-Jordan panel step, lane-quad form (b <= 512, 16-byte vectors of NB/4
+// columns).  The four lanes 4q..4q+3 of a warp share rows: lane c of the quad
+// holds columns [c*C, c*C+C) (C = NB/4) of the quad's R = 4 rows (rows
+// 4*(8*warp + q) .. +3).  Every row therefore lives inside one warp, which
+// gives a column step one block-wide barrier: the warp's best candidate row is
+// published whole by its quad before the barrier; after it, every thread picks
+// the winner among the 16 warp candidates, reads its C columns of the winning
+// row (shared memory) and gets the pivot-column values of its rows from the
+// quad lane that holds that column (shuffles).  The arithmetic is that of
+// gj_panel_kernel (same pivot keys, same reciprocal, same fma sequence,
+// deferred pivot-row scale), so both forms give identical results.  Candidate
+// slots alternate by step parity.  grid: njobs, block 512; requires b <= 512.
+template <typename T, int NB>
+__global__ void __launch_bounds__(512, 1) gj_panel_quad_kernel(Pool<T> M, const int* slots, Pool<T> GP, int* perm,
+                                                               int* rowsrc, int c0, unsigned* err) {
+    constexpr int NT = 512, NW = NT / 32, R = 4, C = NB / 4;
+    constexpr int VW = 16 / sizeof(T);
+    static_assert(C % VW == 0 && NT / 4 * R >= 512, "quad tiling");
+    typedef typename Vec16<T>::type VT;
+    __shared__ __align__(16) T cand_row[2][NW][2 * NB];   // [parity][warp][re | im]
+    __shared__ unsigned cand_key[2][NW];
+    __shared__ cplx<T> cand_inv[2][NW];
+    __shared__ int cand_lrow[2][NW];
+    __shared__ int rsm[NT];
+    const int b = M.rows;
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const int qc = lane & 3;                         // column block of this lane
+    const int qbase = lane & ~3;                     // first lane of the quad
+    const int row0 = (warp * 8 + (lane >> 2)) * R;   // first of the quad's rows
+    const int job = blockIdx.x;
+    const T* Mre = M.slot(slots[job]);
+    const T* Mim = Mre + M.plane_elems();
+    const int ld = M.ld;
+    const int w = min(NB, b - c0);
+    T vr[R][C], vi[R][C];
+    int lrow[R];
+    cplx<T> alpha[R];                                // deferred pivot-row scales
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+        const int i = row0 + j;
+        lrow[j] = i < b ? i : INT_MAX;
+        alpha[j] = cmk((T)1, (T)0);
+#pragma unroll
+        for (int v = 0; v < C / VW; ++v) {
+            const int col = qc * C + v * VW;
+            VT a = {}, c = {};
+            if (i < b && col < w) {   // c0 + NB <= ld: the vector stays in the row
+                a = *reinterpret_cast<const VT*>(Mre + (size_t)i * ld + c0 + col);
+                c = *reinterpret_cast<const VT*>(Mim + (size_t)i * ld + c0 + col);
+            }
+#pragma unroll
+            for (int e = 0; e < VW; ++e) {
+                const bool ok = i < b && col + e < w;
+                vr[j][v * VW + e] = ok ? reinterpret_cast<const T*>(&a)[e] : (T)0;
+                vi[j][v * VW + e] = ok ? reinterpret_cast<const T*>(&c)[e] : (T)0;
+            }
+        }
+    }
+#pragma unroll 1
+    for (int g = 0; g * C < w; ++g) {
+#pragma unroll
+        for (int sp = 0; sp < C; ++sp) {
+            const int jj = g * C + sp;
+            if (jj < w) {   // uniform
+                const int r0 = c0 + jj;
+                const int par = jj & 1;
+                // A: keys of the rows held by the pivot column's lanes; warp maximum
+                unsigned key = 0;
+                int jbest = 0;
+                if (qc == g) {
+#pragma unroll
+                    for (int j = 0; j < R; ++j)
+                        if (lrow[j] >= r0 && lrow[j] < b) {
+                            const unsigned k = pivot_key((float)(fabs(vr[j][sp]) + fabs(vi[j][sp])), row0 + j);
+                            if (k > key) { key = k; jbest = j; }
+                        }
+                }
+                const unsigned wkey = __reduce_max_sync(0xffffffffu, key);
+                const unsigned hit = __ballot_sync(0xffffffffu, key != 0u && key == wkey);
+                if (hit) {
+                    // the winning lane's quad publishes the row (each lane its C columns)
+                    const int wl = __ffs(hit) - 1;
+                    const int jsel = __shfl_sync(0xffffffffu, jbest, wl);
+                    if ((lane & ~3) == (wl & ~3)) {
+                        T* cr = cand_row[par][warp];
+#pragma unroll
+                        for (int j = 0; j < R; ++j) {
+                            if (j == jsel) {
+#pragma unroll
+                                for (int v = 0; v < C / VW; ++v) {
+                                    VT a, c;
+#pragma unroll
+                                    for (int e = 0; e < VW; ++e) {
+                                        reinterpret_cast<T*>(&a)[e] = vr[j][v * VW + e];
+                                        reinterpret_cast<T*>(&c)[e] = vi[j][v * VW + e];
+                                    }
+                                    reinterpret_cast<VT*>(cr + qc * C)[v] = a;
+                                    reinterpret_cast<VT*>(cr + NB + qc * C)[v] = c;
+                                }
+                                if (lane == wl) {
+                                    cand_inv[par][warp] = cinv_pow2(cmk(vr[j][sp], vi[j][sp]));
+                                    cand_lrow[par][warp] = lrow[j];
+                                }
+                            }
+                        }
+                    }
+                }
+                if (lane == 0) cand_key[par][warp] = wkey;
+                __syncthreads();
+                // B: the winner among the warp candidates (the holder of logical row r0
+                // is always a candidate, so there is one)
+                const unsigned ck = lane < NW ? cand_key[par][lane] : 0u;
+                const unsigned gkey = __reduce_max_sync(0xffffffffu, ck);
+                const int ww = __ffs(__ballot_sync(0xffffffffu, ck == gkey && lane < NW)) - 1;
+                const T* pr = cand_row[par][ww];
+                const int pl = cand_lrow[par][ww];
+                const cplx<T> p = cmk(pr[jj], pr[NB + jj]);
+                const bool bad = !(fabs(p.re) + fabs(p.im) > (T)0) || !isfinite(p.re) || !isfinite(p.im);
+                if (bad && t == 0) dev_error(err, FDFD_DEVERR_SINGULAR);
+                const cplx<T> inv = bad ? cmk((T)0, (T)0) : cand_inv[par][ww];
+                // C: the pivot-column values of this lane's rows (held by quad lane g)
+                cplx<T> f[R];
+                bool isp[R];
+#pragma unroll
+                for (int j = 0; j < R; ++j) {
+                    const T cr_ = __shfl_sync(0xffffffffu, vr[j][sp], qbase + g);
+                    const T ci_ = __shfl_sync(0xffffffffu, vi[j][sp], qbase + g);
+                    isp[j] = lrow[j] == pl;
+                    const cplx<T> fi = cmul(cmk(cr_, ci_), inv);
+                    f[j] = isp[j] ? cmk((T)0, (T)0) : fi;
+                }
+                T xr[C], xi[C];
+#pragma unroll
+                for (int v = 0; v < C / VW; ++v) {
+                    const VT a = reinterpret_cast<const VT*>(pr + qc * C)[v];
+                    const VT c = reinterpret_cast<const VT*>(pr + NB + qc * C)[v];
+#pragma unroll
+                    for (int e = 0; e < VW; ++e) {
+                        xr[v * VW + e] = reinterpret_cast<const T*>(&a)[e];
+                        xi[v * VW + e] = reinterpret_cast<const T*>(&c)[e];
+                    }
+                }
+                if constexpr (sizeof(T) == 4 && C % 2 == 0) {
+#pragma unroll
+                    for (int j = 0; j < R; ++j) {
+                        const float2 fim = make_float2(f[j].im, f[j].im), nfr = make_float2(-f[j].re, -f[j].re);
+                        const float2 nfi = make_float2(-f[j].im, -f[j].im);
+#pragma unroll
+                        for (int k = 0; k < C; k += 2) {
+                            const float2 x_r = make_float2(xr[k], xr[k + 1]), x_i = make_float2(xi[k], xi[k + 1]);
+                            float2 a = make_float2(vr[j][k], vr[j][k + 1]), c = make_float2(vi[j][k], vi[j][k + 1]);
+                            a = __ffma2_rn(nfr, x_r, __ffma2_rn(fim, x_i, a));
+                            c = __ffma2_rn(nfr, x_i, __ffma2_rn(nfi, x_r, c));
+                            vr[j][k] = a.x; vr[j][k + 1] = a.y;
+                            vi[j][k] = c.x; vi[j][k + 1] = c.y;
+                        }
+                    }
+                } else {
+#pragma unroll
+                    for (int j = 0; j < R; ++j)
+#pragma unroll
+                        for (int k = 0; k < C; ++k) {
+                            vr[j][k] = fma(-f[j].re, xr[k], fma(f[j].im, xi[k], vr[j][k]));
+                            vi[j][k] = fma(-f[j].re, xi[k], fma(-f[j].im, xr[k], vi[j][k]));
+                        }
+                }
+#pragma unroll
+                for (int j = 0; j < R; ++j) {
+                    if (qc == g) {
+                        vr[j][sp] = isp[j] ? (T)1 : -f[j].re;
+                        vi[j][sp] = isp[j] ? (T)0 : -f[j].im;
+                    }
+                    if (isp[j]) alpha[j] = inv;
+                    // exchange of logical rows r0 and pl between their holders
+                    lrow[j] = (lrow[j] == r0) ? pl : (isp[j] ? r0 : lrow[j]);
+                }
+            }
+        }
+    }
+    // apply the deferred pivot-row scales
+#pragma unroll
+    for (int j = 0; j < R; ++j)
+#pragma unroll
+        for (int k = 0; k < C; ++k) {
+            const cplx<T> x = cmul(alpha[j], cmk(vr[j][k], vi[j][k]));
+            vr[j][k] = x.re;
+            vi[j][k] = x.im;
+        }
+    // G (b x GP.cols, zero padded): row j of this lane goes to G row lrow[j],
+    // columns [qc*C, qc*C+C) as whole 16-byte vectors; lane 0 of the quad zero-fills
+    // the padding columns [NB, GP.cols)
+    {
+        T* gp = GP.slot(job);
+        const long long pe = GP.plane_elems();
+#pragma unroll
+        for (int j = 0; j < R; ++j) {
+            if (lrow[j] >= b) continue;
+            const long long o = (long long)lrow[j] * GP.ld;
+#pragma unroll
+            for (int v = 0; v < C / VW; ++v) {
+                VT a, c;
+#pragma unroll
+                for (int e = 0; e < VW; ++e) {
+                    reinterpret_cast<T*>(&a)[e] = vr[j][v * VW + e];
+                    reinterpret_cast<T*>(&c)[e] = vi[j][v * VW + e];
+                }
+                const int col = qc * C + v * VW;
+                *reinterpret_cast<VT*>(gp + o + col) = a;
+                *reinterpret_cast<VT*>(gp + pe + o + col) = c;
+                if (GP.planes == 4) {   // pre-split tensor-core operand: TF32 residual planes
+                    VT al, cl;
+#pragma unroll
+                    for (int e = 0; e < VW; ++e) {
+                        reinterpret_cast<T*>(&al)[e] = (T)tf32_lo((float)reinterpret_cast<const T*>(&a)[e]);
+                        reinterpret_cast<T*>(&cl)[e] = (T)tf32_lo((float)reinterpret_cast<const T*>(&c)[e]);
+                    }
+                    *reinterpret_cast<VT*>(gp + 2 * pe + o + col) = al;
+                    *reinterpret_cast<VT*>(gp + 3 * pe + o + col) = cl;
+                }
+            }
+            if (qc == 0)
+                for (int col = NB; col < GP.cols; col += VW) {
+                    const VT z = {};
+                    for (int pl2 = 0; pl2 < GP.planes; ++pl2) *reinterpret_cast<VT*>(gp + pl2 * pe + o + col) = z;
+                }
+        }
+    }
+    // the panel's row exchanges, composed (row r of the exchanged matrix is row
+    // rsm[r] of M), into rowsrc and perm
+    if (qc == 0) {
+#pragma unroll
+        for (int j = 0; j < R; ++j)
+            if (lrow[j] < b) rsm[lrow[j]] = row0 + j;
+    }
+    __syncthreads();
+    {
+        int* rs = rowsrc + (size_t)job * b;
+        int* pp = perm + (size_t)job * b;
+        int pv = 0;
+        if (t < b) pv = pp[rsm[t]];
+        __syncthreads();   // every old perm entry is read before any is overwritten
+        if (t < b) { pp[t] = pv; rs[t] = rsm[t]; }
+    }
+}
+
 // Dst[r][perm[j]] = Src[r][j] per row (through shared memory, so Src may be Dst).
 // grid: (ceil(b/8), njobs), block 256
 template <typename T>
@@ -1036,6 +1281,11 @@ int launch_gj_panel(cudaStream_t s, int nb, int njobs, Pool<T> M, const int* slo
                     int* rowsrc, int c0, unsigned* err) {
     const bool two = M.rows > 512;
     if (M.rows > 1024) return (int)cudaErrorInvalidValue;
+    if (!two && nb == (sizeof(T) == 4 ? 32 : 16)) {
+        // lane-quad form: one barrier per column step
+        gj_panel_quad_kernel<T, sizeof(T) == 4 ? 32 : 16><<<njobs, 512, 0, s>>>(M, slots, GP, perm, rowsrc, c0, err);
+        return (int)cudaGetLastError();
+    }
     if constexpr (sizeof(T) == 4) {
         if (nb == 32 && !two) return gj_panel_launch<T, 32, 4, 8>(s, njobs, M, slots, GP, perm, rowsrc, c0, err);
         if (nb == 16 && two) return gj_panel_launch<T, 16, 8, 4>(s, njobs, M, slots, GP, perm, rowsrc, c0, err);
