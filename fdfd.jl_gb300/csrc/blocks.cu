@@ -658,10 +658,11 @@ __global__ void __launch_bounds__(512) gj_rt_kernel(Pool<T> M, const int* slots,
 // holds columns [c*C, c*C+C) (C = NB/4) of the quad's R = 4 rows (rows
 // 4*(8*warp + q) .. +3).  Every row therefore lives inside one warp, which
 // gives a column step one block-wide barrier: the warp's best candidate row is
-// published whole by its quad before the barrier; after it, every thread picks
-// the winner among the 16 warp candidates, reads its C columns of the winning
-// row (shared memory) and gets the pivot-column values of its rows from the
-// quad lane that holds that column (shuffles).  The arithmetic is that of
+// published whole by its quad before the barrier; after it, every thread takes
+// the largest of the 16 warp keys (the key names the physical row, hence the
+// warp), reads its C columns of the winning row (shared memory) and gets the
+// pivot-column values of its rows from the quad lane that holds that column
+// (shuffles).  The arithmetic is that of
 // gj_panel_kernel (same pivot keys, same reciprocal, same fma sequence,
 // deferred pivot-row scale), so both forms give identical results.  Candidate
 // slots alternate by step parity.  grid: njobs, block 512; requires b <= 512.
@@ -673,7 +674,7 @@ __global__ void __launch_bounds__(512, 1) gj_panel_quad_kernel(Pool<T> M, const 
     static_assert(C % VW == 0 && NT / 4 * R >= 512, "quad tiling");
     typedef typename Vec16<T>::type VT;
     __shared__ __align__(16) T cand_row[2][NW][2 * NB];   // [parity][warp][re | im]
-    __shared__ unsigned cand_key[2][NW];
+    __shared__ __align__(16) unsigned cand_key[2][NW];
     __shared__ cplx<T> cand_inv[2][NW];
     __shared__ int cand_lrow[2][NW];
     __shared__ int rsm[NT];
@@ -719,24 +720,22 @@ __global__ void __launch_bounds__(512, 1) gj_panel_quad_kernel(Pool<T> M, const 
             if (jj < w) {   // uniform
                 const int r0 = c0 + jj;
                 const int par = jj & 1;
-                // A: keys of the rows held by the pivot column's lanes; warp maximum
+                // A: keys of the rows held by the pivot column's lanes; warp maximum.
+                // The key encodes the physical row, so the winning quad and row follow
+                // from the maximum directly; the quad publishes the row, and its lane
+                // in the pivot column adds the reciprocal of the pivot.
                 unsigned key = 0;
-                int jbest = 0;
                 if (qc == g) {
 #pragma unroll
                     for (int j = 0; j < R; ++j)
-                        if (lrow[j] >= r0 && lrow[j] < b) {
-                            const unsigned k = pivot_key((float)(fabs(vr[j][sp]) + fabs(vi[j][sp])), row0 + j);
-                            if (k > key) { key = k; jbest = j; }
-                        }
+                        if (lrow[j] >= r0 && lrow[j] < b)
+                            key = max(key, pivot_key((float)(fabs(vr[j][sp]) + fabs(vi[j][sp])), row0 + j));
                 }
                 const unsigned wkey = __reduce_max_sync(0xffffffffu, key);
-                const unsigned hit = __ballot_sync(0xffffffffu, key != 0u && key == wkey);
-                if (hit) {
-                    // the winning lane's quad publishes the row (each lane its C columns)
-                    const int wl = __ffs(hit) - 1;
-                    const int jsel = __shfl_sync(0xffffffffu, jbest, wl);
-                    if ((lane & ~3) == (wl & ~3)) {
+                if (wkey != 0u) {
+                    const int wphys = pivot_key_row(wkey);
+                    const int wq = (wphys >> 2) & 7, jsel = wphys & 3;
+                    if ((lane >> 2) == wq) {
                         T* cr = cand_row[par][warp];
 #pragma unroll
                         for (int j = 0; j < R; ++j) {
@@ -752,7 +751,7 @@ __global__ void __launch_bounds__(512, 1) gj_panel_quad_kernel(Pool<T> M, const 
                                     reinterpret_cast<VT*>(cr + qc * C)[v] = a;
                                     reinterpret_cast<VT*>(cr + NB + qc * C)[v] = c;
                                 }
-                                if (lane == wl) {
+                                if (qc == g) {
                                     cand_inv[par][warp] = cinv_pow2(cmk(vr[j][sp], vi[j][sp]));
                                     cand_lrow[par][warp] = lrow[j];
                                 }
@@ -764,9 +763,13 @@ __global__ void __launch_bounds__(512, 1) gj_panel_quad_kernel(Pool<T> M, const 
                 __syncthreads();
                 // B: the winner among the warp candidates (the holder of logical row r0
                 // is always a candidate, so there is one)
-                const unsigned ck = lane < NW ? cand_key[par][lane] : 0u;
-                const unsigned gkey = __reduce_max_sync(0xffffffffu, ck);
-                const int ww = __ffs(__ballot_sync(0xffffffffu, ck == gkey && lane < NW)) - 1;
+                unsigned gkey = 0u;
+#pragma unroll
+                for (int q = 0; q < NW / 4; ++q) {
+                    const uint4 kv = reinterpret_cast<const uint4*>(cand_key[par])[q];
+                    gkey = max(gkey, max(max(kv.x, kv.y), max(kv.z, kv.w)));
+                }
+                const int ww = pivot_key_row(gkey) >> 5;   // a warp holds 32 consecutive physical rows
                 const T* pr = cand_row[par][ww];
                 const int pl = cand_lrow[par][ww];
                 const cplx<T> p = cmk(pr[jj], pr[NB + jj]);
@@ -841,6 +844,19 @@ __global__ void __launch_bounds__(512, 1) gj_panel_quad_kernel(Pool<T> M, const 
             vr[j][k] = x.re;
             vi[j][k] = x.im;
         }
+    // the panel's row exchanges, composed (row r of the exchanged matrix is row
+    // rsm[r] of M); the perm gather is issued before the G stores so that its
+    // latency overlaps them
+    if (qc == 0) {
+#pragma unroll
+        for (int j = 0; j < R; ++j)
+            if (lrow[j] < b) rsm[lrow[j]] = row0 + j;
+    }
+    __syncthreads();
+    int* rs = rowsrc + (size_t)job * b;
+    int* pp = perm + (size_t)job * b;
+    const int rsv = t < b ? rsm[t] : 0;
+    const int pv = t < b ? pp[rsv] : 0;
     // G (b x GP.cols, zero padded): row j of this lane goes to G row lrow[j],
     // columns [qc*C, qc*C+C) as whole 16-byte vectors; lane 0 of the quad zero-fills
     // the padding columns [NB, GP.cols)
@@ -880,22 +896,8 @@ __global__ void __launch_bounds__(512, 1) gj_panel_quad_kernel(Pool<T> M, const 
                 }
         }
     }
-    // the panel's row exchanges, composed (row r of the exchanged matrix is row
-    // rsm[r] of M), into rowsrc and perm
-    if (qc == 0) {
-#pragma unroll
-        for (int j = 0; j < R; ++j)
-            if (lrow[j] < b) rsm[lrow[j]] = row0 + j;
-    }
-    __syncthreads();
-    {
-        int* rs = rowsrc + (size_t)job * b;
-        int* pp = perm + (size_t)job * b;
-        int pv = 0;
-        if (t < b) pv = pp[rsm[t]];
-        __syncthreads();   // every old perm entry is read before any is overwritten
-        if (t < b) { pp[t] = pv; rs[t] = rsm[t]; }
-    }
+    __syncthreads();   // every old perm entry is read before any is overwritten
+    if (t < b) { pp[t] = pv; rs[t] = rsv; }
 }
 
 // Dst[r][perm[j]] = Src[r][j] per row (through shared memory, so Src may be Dst).
