@@ -124,12 +124,38 @@ def _cpu_solve(kind):
     return t, float(O.relative_residual(A, O.vec(f[0]), b))
 
 
+_BLAS_THREAD_VARS = ("OPENBLAS_NUM_THREADS", "OMP_NUM_THREADS", "MKL_NUM_THREADS")
+
+
+class _single_threaded_children:
+    """Spawned worker processes inherit one BLAS thread each (scipy's BLAS is multithreaded by
+    default: concurrent workers would oversubscribe the host, and a single 'one core' solve
+    would not be one core)."""
+
+    def __enter__(self):
+        self.saved = {k: os.environ.get(k) for k in _BLAS_THREAD_VARS}
+        for k in _BLAS_THREAD_VARS:
+            os.environ[k] = "1"
+
+    def __exit__(self, *exc):
+        for k, v in self.saved.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+
+
 def cpu_baseline_single():
-    """One full solve, single thread (SuperLU factors sequentially)."""
-    t, res = _cpu_solve("full")
+    """One full solve on one host thread, in a spawned process whose BLAS runs one thread
+    (SuperLU itself factors sequentially)."""
+    import concurrent.futures as cf
+    import multiprocessing as mp
+    with _single_threaded_children():
+        with cf.ProcessPoolExecutor(max_workers=1, mp_context=mp.get_context("spawn")) as ex:
+            t, res = ex.submit(_cpu_solve, "full").result()
     return {"value": 1.0 / t, "unit": "solves/s", "cores": 1, "kind": "port",
-            "sample": f"1 full solve of the workload with the scipy/SuperLU FP64 oracle ({t:.1f} s, "
-                      f"rel. residual {res:.1e})"}
+            "sample": f"1 full solve of the workload with the scipy/SuperLU FP64 oracle, one thread "
+                      f"({t:.1f} s, rel. residual {res:.1e})"}
 
 
 def run_reference(a):
@@ -137,7 +163,7 @@ def run_reference(a):
     import multiprocessing as mp
     cores = min(os.cpu_count() or 1, 16)
     ctx = mp.get_context("spawn")
-    with cf.ProcessPoolExecutor(max_workers=cores, mp_context=ctx) as ex:
+    with _single_threaded_children(), cf.ProcessPoolExecutor(max_workers=cores, mp_context=ctx) as ex:
         for _ in range(a.warmup):   # warm the workers: small solve each
             list(ex.map(_cpu_solve, ["small"] * cores))
         times = []
@@ -152,7 +178,7 @@ def run_reference(a):
             "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 * total / a.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
             "config": {"workload": WORKLOAD, "solver": "scipy SuperLU FP64 (restatement of lu(A)\\b)",
-                       "step": f"{cores} concurrent full solves, one per host core"},
+                       "step": f"{cores} concurrent full solves, one per host core, one BLAS thread each"},
             "cpu_baseline": {"value": value, "unit": "solves/s", "cores": cores, "kind": "port",
                              "sample": f"{a.steps} steps x {cores} concurrent full solves"},
             "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
