@@ -653,10 +653,11 @@ __global__ void __launch_bounds__(512) gj_rt_kernel(Pool<T> M, const int* slots,
     }
 }
 
-// Gauss-Jordan panel step, lane-quad form (b <= 512, 16-byte vectors of NB/4
+// Gauss-Jordan panel step, lane-quad form (b <= 128*R, 16-byte vectors of NB/4
 // columns).  The four lanes 4q..4q+3 of a warp share rows: lane c of the quad
-// holds columns [c*C, c*C+C) (C = NB/4) of the quad's R = 4 rows (rows
-// 4*(8*warp + q) .. +3).  Every row therefore lives inside one warp, which
+// holds columns [c*C, c*C+C) (C = NB/4) of the quad's R rows (rows
+// R*(8*warp + q) .. +R-1; R = 4 for b <= 512, 8 up to 1024, with the narrower
+// panel there).  Every row therefore lives inside one warp, which
 // gives a column step one block-wide barrier: the warp's best candidate row is
 // published whole by its quad before the barrier; after it, every thread takes
 // the largest of the 16 warp keys (the key names the physical row, hence the
@@ -665,19 +666,19 @@ __global__ void __launch_bounds__(512) gj_rt_kernel(Pool<T> M, const int* slots,
 // (shuffles).  The arithmetic is that of
 // gj_panel_kernel (same pivot keys, same reciprocal, same fma sequence,
 // deferred pivot-row scale), so both forms give identical results.  Candidate
-// slots alternate by step parity.  grid: njobs, block 512; requires b <= 512.
-template <typename T, int NB>
+// slots alternate by step parity.  grid: njobs, block 512; requires b <= 128*R.
+template <typename T, int NB, int R>
 __global__ void __launch_bounds__(512, 1) gj_panel_quad_kernel(Pool<T> M, const int* slots, Pool<T> GP, int* perm,
                                                                int* rowsrc, int c0, unsigned* err) {
-    constexpr int NT = 512, NW = NT / 32, R = 4, C = NB / 4;
+    constexpr int NT = 512, NW = NT / 32, C = NB / 4;
     constexpr int VW = 16 / sizeof(T);
-    static_assert(C % VW == 0 && NT / 4 * R >= 512, "quad tiling");
+    static_assert(C % VW == 0 && (R & (R - 1)) == 0, "quad tiling");
     typedef typename Vec16<T>::type VT;
     __shared__ __align__(16) T cand_row[2][NW][2 * NB];   // [parity][warp][re | im]
     __shared__ __align__(16) unsigned cand_key[2][NW];
     __shared__ cplx<T> cand_inv[2][NW];
     __shared__ int cand_lrow[2][NW];
-    __shared__ int rsm[NT];
+    __shared__ int rsm[128 * R];                      // composed row exchanges, every row of the block
     const int b = M.rows;
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
     const int qc = lane & 3;                         // column block of this lane
@@ -734,7 +735,7 @@ __global__ void __launch_bounds__(512, 1) gj_panel_quad_kernel(Pool<T> M, const 
                 const unsigned wkey = __reduce_max_sync(0xffffffffu, key);
                 if (wkey != 0u) {
                     const int wphys = pivot_key_row(wkey);
-                    const int wq = (wphys >> 2) & 7, jsel = wphys & 3;
+                    const int wq = (wphys / R) & 7, jsel = wphys & (R - 1);
                     if ((lane >> 2) == wq) {
                         T* cr = cand_row[par][warp];
 #pragma unroll
@@ -769,7 +770,7 @@ __global__ void __launch_bounds__(512, 1) gj_panel_quad_kernel(Pool<T> M, const 
                     const uint4 kv = reinterpret_cast<const uint4*>(cand_key[par])[q];
                     gkey = max(gkey, max(max(kv.x, kv.y), max(kv.z, kv.w)));
                 }
-                const int ww = pivot_key_row(gkey) >> 5;   // a warp holds 32 consecutive physical rows
+                const int ww = pivot_key_row(gkey) / (8 * R);   // a warp holds 8*R consecutive physical rows
                 const T* pr = cand_row[par][ww];
                 const int pl = cand_lrow[par][ww];
                 const cplx<T> p = cmk(pr[jj], pr[NB + jj]);
@@ -855,8 +856,15 @@ __global__ void __launch_bounds__(512, 1) gj_panel_quad_kernel(Pool<T> M, const 
     __syncthreads();
     int* rs = rowsrc + (size_t)job * b;
     int* pp = perm + (size_t)job * b;
-    const int rsv = t < b ? rsm[t] : 0;
-    const int pv = t < b ? pp[rsv] : 0;
+    constexpr int PPT = 128 * R / NT;                // rows per thread in the bookkeeping
+    static_assert(128 * R % NT == 0, "rows per thread");
+    int rsv[PPT], pv[PPT];
+#pragma unroll
+    for (int u = 0; u < PPT; ++u) {
+        const int i = t + u * NT;
+        rsv[u] = i < b ? rsm[i] : 0;
+        pv[u] = i < b ? pp[rsv[u]] : 0;
+    }
     // G (b x GP.cols, zero padded): row j of this lane goes to G row lrow[j],
     // columns [qc*C, qc*C+C) as whole 16-byte vectors; lane 0 of the quad zero-fills
     // the padding columns [NB, GP.cols)
@@ -897,7 +905,11 @@ __global__ void __launch_bounds__(512, 1) gj_panel_quad_kernel(Pool<T> M, const 
         }
     }
     __syncthreads();   // every old perm entry is read before any is overwritten
-    if (t < b) { pp[t] = pv; rs[t] = rsv; }
+#pragma unroll
+    for (int u = 0; u < PPT; ++u) {
+        const int i = t + u * NT;
+        if (i < b) { pp[i] = pv[u]; rs[i] = rsv[u]; }
+    }
 }
 
 // Dst[r][perm[j]] = Src[r][j] per row (through shared memory, so Src may be Dst).
@@ -1283,17 +1295,22 @@ int launch_gj_panel(cudaStream_t s, int nb, int njobs, Pool<T> M, const int* slo
                     int* rowsrc, int c0, unsigned* err) {
     const bool two = M.rows > 512;
     if (M.rows > 1024) return (int)cudaErrorInvalidValue;
-    if (!two && nb == (sizeof(T) == 4 ? 32 : 16)) {
-        // lane-quad form: one barrier per column step
-        gj_panel_quad_kernel<T, sizeof(T) == 4 ? 32 : 16><<<njobs, 512, 0, s>>>(M, slots, GP, perm, rowsrc, c0, err);
+    // lane-quad form: one barrier per column step; four rows per quad up to b = 512,
+    // eight (with the half-width panel) up to 1024 in FP32
+    constexpr int NB1 = sizeof(T) == 4 ? 32 : 16;
+    if (!two && nb == NB1) {
+        gj_panel_quad_kernel<T, NB1, 4><<<njobs, 512, 0, s>>>(M, slots, GP, perm, rowsrc, c0, err);
         return (int)cudaGetLastError();
     }
     if constexpr (sizeof(T) == 4) {
-        if (nb == 32 && !two) return gj_panel_launch<T, 32, 4, 8>(s, njobs, M, slots, GP, perm, rowsrc, c0, err);
-        if (nb == 16 && two) return gj_panel_launch<T, 16, 8, 4>(s, njobs, M, slots, GP, perm, rowsrc, c0, err);
+        if (two && nb == 16) {
+            gj_panel_quad_kernel<T, 16, 8><<<njobs, 512, 0, s>>>(M, slots, GP, perm, rowsrc, c0, err);
+            return (int)cudaGetLastError();
+        }
     } else {
-        if (nb == 16 && !two) return gj_panel_launch<T, 16, 4, 4>(s, njobs, M, slots, GP, perm, rowsrc, c0, err);
-        if (nb == 8 && two) return gj_panel_launch<T, 8, 8, 2>(s, njobs, M, slots, GP, perm, rowsrc, c0, err);
+        // FP64 with eight rows per quad would spill (its per-row scale factors alone take 32
+        // registers): the 2-D tiled kernel keeps those in shared memory
+        if (two && nb == 8) return gj_panel_launch<T, 8, 8, 2>(s, njobs, M, slots, GP, perm, rowsrc, c0, err);
     }
     return (int)cudaErrorInvalidValue;
 }
