@@ -56,3 +56,27 @@ def test_null_handle_calls_fail_cleanly(lib, fdfd):
     assert lib.fdfd_set_fallback(None, 1) == E
     assert lib.fdfd_set_restart(None, 20) == E
     lib.fdfd_destroy(None)
+
+
+def test_extension_entry_points_reject_bad_arguments(lib, fdfd):
+    """The modulated-device, mode, flux and χ³ entry points validate their
+    arguments before any device work (no GPU needed)."""
+    import ctypes as C
+    L = fdfd._lib
+    E = L.FDFD_EINVAL
+    h = C.c_void_p()
+    assert lib.fdfd_mf_create(None, 40, 30, 4, 4, 0.05, 0.05, 1e-6, 4.0, -18.4, 1, 1, 1) == E
+    assert lib.fdfd_mf_create(C.byref(h), 40, 30, 4, 4, 0.05, 0.05, 1e-6, 4.0, -18.4, -1, 1, 1) == E   # sidebands
+    assert lib.fdfd_mf_create(C.byref(h), 40, 30, 4, 4, 0.05, 0.05, 1e-6, 4.0, -18.4, 17, 1, 1) == E   # K > 33
+    assert lib.fdfd_mf_set_deps(None, None) == E
+    assert lib.fdfd_mf_factor(None, 1.0, 0.1) == E
+    assert lib.fdfd_mf_solve(None, None, None, None, None, None) == E
+    m = L.Mode(1, 1, 5, 5, 0.5, 3.0, 0.0)
+    beta = (C.c_double * 2)()
+    npts = C.c_int(0)
+    assert lib.fdfd_get_mode(None, 1.0, C.byref(m), 0, beta, beta, C.byref(npts)) == E
+    assert lib.fdfd_mode_sources(None, 1, beta, 1, C.byref(m), beta) == E
+    assert lib.fdfd_poynting(None, 1, None, None, None, None, None) == E
+    assert lib.fdfd_poynting_device(None, 1, None, None, None, None, None) == E
+    assert lib.fdfd_flux_integral(None, 1, None, None, 1, 1, None, None) == E
+    assert lib.fdfd_chi3_solve(None, None, None, 1, 1e-12, 10, None, None, None, None, None, None) == E
