@@ -514,7 +514,16 @@ __global__ void vcombine_kernel(long long N, int nvec, const cplx<double>* __res
     int rhs = blockIdx.y;
     if (k >= N) return;
     cplx<double> acc = y[(size_t)rhs * N + k];
-    for (int j = 0; j < nvec; ++j) {
+    // the loads of four vectors are issued before their products (the sum keeps its order)
+    int j = 0;
+    for (; j + 4 <= nvec; j += 4) {
+        cplx<double> v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) v[u] = V[(j + u) * vstride + (size_t)rhs * N + k];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) acc = cadd(acc, cscale(cmul(c[rhs * ldc + j + u], v[u]), sign));
+    }
+    for (; j < nvec; ++j) {
         cplx<double> cj = c[rhs * ldc + j];
         cplx<double> v = V[j * vstride + (size_t)rhs * N + k];
         acc = cadd(acc, cscale(cmul(cj, v), sign));

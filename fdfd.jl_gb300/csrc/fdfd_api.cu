@@ -1036,7 +1036,7 @@ int residual(fdfd_handle* h, const cplx<double>* x, const cplx<double>* b, cplx<
 int dots(fdfd_handle* h, const cplx<double>* V, long long vstride, int nvec, const cplx<double>* w, int nrhs,
          std::vector<zd>& out) {
     long long N = vlen(h);
-    const int nb = 152;
+    const int nb = 4 * h->num_sms;   // four blocks per SM: enough loads in flight for HBM
     RET(ensure_part(h, (size_t)nrhs * nb * 2 * nvec));
     RET(ensure_red(h, (size_t)nrhs * 2 * nvec));
     LAUNCH(vdots_kernel, dim3(nb, nrhs), 256, 0, N, nvec, V, vstride, w, h->part);
