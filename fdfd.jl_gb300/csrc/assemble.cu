@@ -506,29 +506,51 @@ __global__ void vscale_kernel(long long N, const cplx<double>* __restrict__ x, c
     y[(size_t)rhs * N + k] = cmul(s[rhs], x[(size_t)rhs * N + k]);
 }
 
-// y[rhs] += Σ_j c[rhs*ldc + j] * V_j[rhs]   (V_j = V + j*vstride)
+// acc ± c·v in four FMAs (FP64 issue, not HBM, bounds these vector kernels on
+// this part; the negations are free operand modifiers)
+template <bool kSub>
+__device__ __forceinline__ void cmac(cplx<double>& acc, cplx<double> c, cplx<double> v) {
+    if (kSub) {
+        acc.re = fma(-c.re, v.re, acc.re);
+        acc.re = fma(c.im, v.im, acc.re);
+        acc.im = fma(-c.re, v.im, acc.im);
+        acc.im = fma(-c.im, v.re, acc.im);
+    } else {
+        acc.re = fma(c.re, v.re, acc.re);
+        acc.re = fma(-c.im, v.im, acc.re);
+        acc.im = fma(c.re, v.im, acc.im);
+        acc.im = fma(c.im, v.re, acc.im);
+    }
+}
+
+template <bool kSub>
+__device__ __forceinline__ cplx<double> vcombine_elem(const cplx<double>* __restrict__ V, long long vstride,
+                                                      const cplx<double>* __restrict__ c, int nvec, size_t o,
+                                                      cplx<double> acc) {
+    // the loads of four vectors are issued before their products (the sum keeps its order)
+    int j = 0;
+    for (; j + 4 <= nvec; j += 4) {
+        cplx<double> v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) v[u] = V[(j + u) * vstride + o];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) cmac<kSub>(acc, c[j + u], v[u]);
+    }
+    for (; j < nvec; ++j) cmac<kSub>(acc, c[j], V[j * vstride + o]);
+    return acc;
+}
+
+// y[rhs] += sign Σ_j c[rhs*ldc + j] * V_j[rhs]   (V_j = V + j*vstride, sign = ±1)
 __global__ void vcombine_kernel(long long N, int nvec, const cplx<double>* __restrict__ V, long long vstride,
                                 const cplx<double>* __restrict__ c, int ldc, double sign,
                                 cplx<double>* __restrict__ y) {
     long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     int rhs = blockIdx.y;
     if (k >= N) return;
-    cplx<double> acc = y[(size_t)rhs * N + k];
-    // the loads of four vectors are issued before their products (the sum keeps its order)
-    int j = 0;
-    for (; j + 4 <= nvec; j += 4) {
-        cplx<double> v[4];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) v[u] = V[(j + u) * vstride + (size_t)rhs * N + k];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) acc = cadd(acc, cscale(cmul(c[rhs * ldc + j + u], v[u]), sign));
-    }
-    for (; j < nvec; ++j) {
-        cplx<double> cj = c[rhs * ldc + j];
-        cplx<double> v = V[j * vstride + (size_t)rhs * N + k];
-        acc = cadd(acc, cscale(cmul(cj, v), sign));
-    }
-    y[(size_t)rhs * N + k] = acc;
+    const size_t o = (size_t)rhs * N + k;
+    const cplx<double>* cr = c + (size_t)rhs * ldc;
+    y[o] = sign < 0 ? vcombine_elem<true>(V, vstride, cr, nvec, o, y[o])
+                    : vcombine_elem<false>(V, vstride, cr, nvec, o, y[o]);
 }
 
 // part[rhs][block][j] = Σ_k conj(V_j[rhs][k]) * w[rhs][k]  for j < nvec (≤ 64)
@@ -546,8 +568,11 @@ __global__ void vdots_kernel(long long N, int nvec, const cplx<double>* __restri
             cplx<double> wv = w[(size_t)rhs * N + k];
             for (int j = 0; j < nj; ++j) {
                 cplx<double> v = V[(j0 + j) * vstride + (size_t)rhs * N + k];
-                acc_re[j] += v.re * wv.re + v.im * wv.im;
-                acc_im[j] += v.re * wv.im - v.im * wv.re;
+                // conj(v)·w in four FMAs
+                acc_re[j] = fma(v.re, wv.re, acc_re[j]);
+                acc_re[j] = fma(v.im, wv.im, acc_re[j]);
+                acc_im[j] = fma(v.re, wv.im, acc_im[j]);
+                acc_im[j] = fma(-v.im, wv.re, acc_im[j]);
             }
         }
         for (int j = 0; j < nj; ++j)
@@ -567,6 +592,18 @@ __global__ void vdots_kernel(long long N, int nvec, const cplx<double>* __restri
         }
         __syncthreads();
     }
+}
+
+// y[rhs] = x[rhs] / ‖x[rhs]‖ with ‖x‖² read from nrm[2*rhs] (0 where ‖x‖ ≤ 1e-300)
+// (x may be y: each thread reads its element before writing it)
+__global__ void vnormalize_kernel(long long N, const cplx<double>* x, const double* __restrict__ nrm,
+                                  cplx<double>* y) {
+    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int rhs = blockIdx.y;
+    if (k >= N) return;
+    const double hn = sqrt(fmax(0.0, nrm[2 * rhs]));
+    const cplx<double> sc = cmk(hn > 1e-300 ? 1.0 / hn : 0.0, 0.0);
+    y[(size_t)rhs * N + k] = cmul(sc, x[(size_t)rhs * N + k]);
 }
 
 // Adjoint helpers (TM): v = P⁻¹ g  or  v = P g with P_k = s_xf[ix]·s_yf[iy]

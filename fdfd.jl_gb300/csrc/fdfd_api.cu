@@ -1058,6 +1058,48 @@ int combine(fdfd_handle* h, const cplx<double>* V, long long vstride, int nvec, 
     return check_launch(h, "combine");
 }
 
+// One Arnoldi orthogonalisation on the device: two classical Gram-Schmidt
+// passes of w against V_0..V_{nvec-1}, then w /= ‖w‖:
+//   h1 = Vᴴw, w -= V h1, h2 = Vᴴw, w -= V h2, nn = ‖w‖², w /= √nn.
+// The coefficients stay on the device between the passes, and one read-back
+// returns h1, h2 (out[rhs*nvec + j]) and nn (per rhs) for the Hessenberg column.
+int arnoldi_orth(fdfd_handle* h, const cplx<double>* V, long long vstride, int nvec, cplx<double>* w, int nrhs,
+                 std::vector<zd>& h1, std::vector<zd>& h2, std::vector<double>& nn) {
+    long long N = vlen(h);
+    const int nb = 4 * h->num_sms;
+    const size_t nc = (size_t)nrhs * 2 * nvec;   // doubles per coefficient set
+    RET(ensure_part(h, (size_t)nrhs * nb * 2 * nvec));
+    RET(ensure_red(h, 2 * nc + 2 * (size_t)nrhs));
+    double* r1 = h->red;
+    double* r2 = h->red + nc;
+    double* r3 = h->red + 2 * nc;
+    LAUNCH(vdots_kernel, dim3(nb, nrhs), 256, 0, N, nvec, V, vstride, w, h->part);
+    LAUNCH(reduce_partials_kernel, nrhs, 256, 0, h->part, nb, 2 * nvec, r1);
+    const dim3 ge(ceil_div(N, 256), nrhs);
+    LAUNCH(vcombine_kernel, ge, 256, 0, N, nvec, V, vstride, reinterpret_cast<const cplx<double>*>(r1), nvec,
+           -1.0, w);
+    LAUNCH(vdots_kernel, dim3(nb, nrhs), 256, 0, N, nvec, V, vstride, w, h->part);
+    LAUNCH(reduce_partials_kernel, nrhs, 256, 0, h->part, nb, 2 * nvec, r2);
+    LAUNCH(vcombine_kernel, ge, 256, 0, N, nvec, V, vstride, reinterpret_cast<const cplx<double>*>(r2), nvec,
+           -1.0, w);
+    LAUNCH(vdots_kernel, dim3(nb, nrhs), 256, 0, N, 1, w, 0, w, h->part);
+    LAUNCH(reduce_partials_kernel, nrhs, 256, 0, h->part, nb, 2, r3);
+    LAUNCH(vnormalize_kernel, dim3(ceil_div(N, 256), nrhs), 256, 0, N, w, r3, w);
+    std::vector<double> tmp(2 * nc + 2 * (size_t)nrhs);
+    CK(cudaMemcpyAsync(tmp.data(), h->red, tmp.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    const size_t nv = (size_t)nrhs * nvec;
+    h1.resize(nv);
+    h2.resize(nv);
+    nn.resize(nrhs);
+    for (size_t i = 0; i < nv; ++i) {
+        h1[i] = zd(tmp[2 * i], tmp[2 * i + 1]);
+        h2[i] = zd(tmp[nc + 2 * i], tmp[nc + 2 * i + 1]);
+    }
+    for (int r = 0; r < nrhs; ++r) nn[r] = tmp[2 * nc + 2 * r];
+    return check_launch(h, "arnoldi");
+}
+
 int scale_vec(fdfd_handle* h, const cplx<double>* x, const std::vector<zd>& s, int nrhs, cplx<double>* y) {
     long long N = vlen(h);
     CK(cudaMemcpyAsync(h->kc, s.data(), nrhs * sizeof(zd), cudaMemcpyHostToDevice, h->stream));
@@ -1160,21 +1202,16 @@ int refine(fdfd_handle* h, int nrhs, int* iters, double* relres, bool give_up) {
                 RET(precond(h, Vj, Zj, nrhs));
                 ++it;
                 RET(residual(h, Zj, nullptr, Vn, nrhs, nullptr));   // Vn = A Zj
+                // Vn ⟂ V_0..V_j, normalised (the device applies 1/hn, or 0 where hn ≤ 1e-300)
                 std::vector<zd> hc, hc2;
-                RET(dots(h, h->kV, vs, j + 1, Vn, nrhs, hc));
-                RET(combine(h, h->kV, vs, j + 1, hc, nrhs, -1.0, Vn));
-                RET(dots(h, h->kV, vs, j + 1, Vn, nrhs, hc2));
-                RET(combine(h, h->kV, vs, j + 1, hc2, nrhs, -1.0, Vn));
-                std::vector<zd> nn;
-                RET(dots(h, Vn, 0, 1, Vn, nrhs, nn));
-                std::vector<zd> sc(nrhs);
+                std::vector<double> nn;
+                RET(arnoldi_orth(h, h->kV, vs, j + 1, Vn, nrhs, hc, hc2, nn));
                 bool all = true;
                 for (int r = 0; r < nrhs; ++r) {
                     std::vector<zd>& Hr = H[r];
                     for (int i = 0; i <= j; ++i) Hr[i * m + j] = hc[r * (j + 1) + i] + hc2[r * (j + 1) + i];
-                    double hn = std::sqrt(std::max(0.0, nn[r].real()));
+                    double hn = std::sqrt(std::max(0.0, nn[r]));
                     Hr[(j + 1) * m + j] = hn;
-                    sc[r] = hn > 1e-300 ? zd(1.0 / hn, 0) : zd(0, 0);
                     // apply previous Givens rotations
                     for (int i = 0; i < j; ++i) {
                         zd a = Hr[i * m + j], bb = Hr[(i + 1) * m + j];
@@ -1194,7 +1231,6 @@ int refine(fdfd_handle* h, int nrhs, int* iters, double* relres, bool give_up) {
                     if (est <= 0.5 * h->tol || hn <= 1e-300 * bnorm[r]) done[r] = 1;
                     if (!done[r]) all = false;
                 }
-                RET(scale_vec(h, Vn, sc, nrhs, Vn));
                 if (all) { ++j; break; }
             }
             // x += Z y  with H y = g (upper triangular, j columns)

@@ -61,6 +61,7 @@ __global__ void vcombine_kernel(long long N, int nvec, const cplx<double>* V, lo
                                 const cplx<double>* c, int ldc, double sign, cplx<double>* y);
 __global__ void vdots_kernel(long long N, int nvec, const cplx<double>* V, long long vstride,
                              const cplx<double>* w, double* part);
+__global__ void vnormalize_kernel(long long N, const cplx<double>* x, const double* nrm, cplx<double>* y);
 __global__ void pscale_kernel(int Nx, int Ny, const cplx<double>* sf, int mode, const cplx<double>* in,
                               cplx<double>* out);
 __global__ void adjoint_grad_kernel(long long N, cplx<double> coef, const cplx<double>* lam,
