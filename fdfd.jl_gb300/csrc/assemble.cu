@@ -169,11 +169,12 @@ __global__ void residual_kernel(int Nx, int Ny, int nrhs, const cplx<double>* __
         long long kym = (iy == 0) ? k + N - Nx : k - Nx;
         long long kyp = (iy == Ny - 1) ? k - (N - Nx) : k + Nx;
         const cplx<double>* xv = x + (size_t)rhs * N;
+        // four FMAs per term: FP64 issue, not HBM, bounds this kernel on this part
         cplx<double> acc = cmul(st[k], xv[k]);
-        acc = cadd(acc, cmul(st[N + k], xv[kxm]));
-        acc = cadd(acc, cmul(st[2 * N + k], xv[kxp]));
-        acc = cadd(acc, cmul(st[3 * N + k], xv[kym]));
-        acc = cadd(acc, cmul(st[4 * N + k], xv[kyp]));
+        cmac<false>(acc, st[N + k], xv[kxm]);
+        cmac<false>(acc, st[2 * N + k], xv[kxp]);
+        cmac<false>(acc, st[3 * N + k], xv[kym]);
+        cmac<false>(acc, st[4 * N + k], xv[kyp]);
         if (b) {
             cplx<double> bv = b[(size_t)rhs * N + k];
             acc = csub(bv, acc);
@@ -226,11 +227,12 @@ __global__ void residual_mf_kernel(MfResidualArgs a, const cplx<double>* __restr
         const long long kyp = (iy == a.Ny - 1) ? k - (N - a.Nx) : k + a.Nx;
         const cplx<double>* st = a.st[n];
         const cplx<double>* xv = x + (size_t)n * N;
+        // four FMAs per term: FP64 issue, not HBM, bounds this kernel on this part
         cplx<double> acc = cmul(st[k], xv[k]);
-        acc = cadd(acc, cmul(st[N + k], xv[kxm]));
-        acc = cadd(acc, cmul(st[2 * N + k], xv[kxp]));
-        acc = cadd(acc, cmul(st[3 * N + k], xv[kym]));
-        acc = cadd(acc, cmul(st[4 * N + k], xv[kyp]));
+        cmac<false>(acc, st[N + k], xv[kxm]);
+        cmac<false>(acc, st[2 * N + k], xv[kxp]);
+        cmac<false>(acc, st[3 * N + k], xv[kym]);
+        cmac<false>(acc, st[4 * N + k], xv[kyp]);
         const cplx<double> d = deps[k];
         const double c = a.half_w2eps0[n];
         if (n + 1 < a.K) acc = cadd(acc, cmul(cmk(c * d.re, -c * d.im), xv[N + k]));
@@ -363,12 +365,13 @@ __global__ void vaxpy_kernel(long long n, double alpha, const cplx<double>* __re
 }
 
 // out[rhs*nvals + v] = Σ_blocks part[rhs][block][v]   (fixed order: deterministic)
-// grid: nrhs, block 256
+// grid: (nrhs, any number ≤ nvals), block 256
 __global__ void reduce_partials_kernel(const double* __restrict__ part, int nblocks, int nvals,
                                        double* __restrict__ out) {
     int rhs = blockIdx.x;
     __shared__ double s[32];
-    for (int v = 0; v < nvals; ++v) {
+    // values spread over grid y (one value per block when gridDim.y == nvals)
+    for (int v = blockIdx.y; v < nvals; v += gridDim.y) {
         double acc = 0.0;
         for (int i = threadIdx.x; i < nblocks; i += blockDim.x)
             acc += part[((size_t)rhs * nblocks + i) * nvals + v];
@@ -506,23 +509,6 @@ __global__ void vscale_kernel(long long N, const cplx<double>* __restrict__ x, c
     y[(size_t)rhs * N + k] = cmul(s[rhs], x[(size_t)rhs * N + k]);
 }
 
-// acc ± c·v in four FMAs (FP64 issue, not HBM, bounds these vector kernels on
-// this part; the negations are free operand modifiers)
-template <bool kSub>
-__device__ __forceinline__ void cmac(cplx<double>& acc, cplx<double> c, cplx<double> v) {
-    if (kSub) {
-        acc.re = fma(-c.re, v.re, acc.re);
-        acc.re = fma(c.im, v.im, acc.re);
-        acc.im = fma(-c.re, v.im, acc.im);
-        acc.im = fma(-c.im, v.re, acc.im);
-    } else {
-        acc.re = fma(c.re, v.re, acc.re);
-        acc.re = fma(-c.im, v.im, acc.re);
-        acc.im = fma(c.re, v.im, acc.im);
-        acc.im = fma(c.im, v.re, acc.im);
-    }
-}
-
 template <bool kSub>
 __device__ __forceinline__ cplx<double> vcombine_elem(const cplx<double>* __restrict__ V, long long vstride,
                                                       const cplx<double>* __restrict__ c, int nvec, size_t o,
@@ -600,10 +586,16 @@ __global__ void vnormalize_kernel(long long N, const cplx<double>* x, const doub
                                   cplx<double>* y) {
     const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const int rhs = blockIdx.y;
+    // one FP64 square root and division per block (both are long FP64 sequences)
+    __shared__ double sc;
+    if (threadIdx.x == 0) {
+        const double hn = sqrt(fmax(0.0, nrm[2 * rhs]));
+        sc = hn > 1e-300 ? 1.0 / hn : 0.0;
+    }
+    __syncthreads();
     if (k >= N) return;
-    const double hn = sqrt(fmax(0.0, nrm[2 * rhs]));
-    const cplx<double> sc = cmk(hn > 1e-300 ? 1.0 / hn : 0.0, 0.0);
-    y[(size_t)rhs * N + k] = cmul(sc, x[(size_t)rhs * N + k]);
+    const cplx<double> v = x[(size_t)rhs * N + k];
+    y[(size_t)rhs * N + k] = cmk(sc * v.re, sc * v.im);
 }
 
 // Adjoint helpers (TM): v = P⁻¹ g  or  v = P g with P_k = s_xf[ix]·s_yf[iy]

@@ -32,6 +32,22 @@ template <typename T> __host__ __device__ __forceinline__ cplx<T> cinv(cplx<T> z
     }
 }
 template <typename T> __host__ __device__ __forceinline__ T cabs1(cplx<T> a) { return fabs(a.re) + fabs(a.im); }
+// acc ± c·v in four FMAs (the negations are free operand modifiers).  The FP64
+// vector and stencil kernels are bound by FP64 issue on this part, not by HBM.
+template <bool kSub, typename T>
+__device__ __forceinline__ void cmac(cplx<T>& acc, cplx<T> c, cplx<T> v) {
+    if (kSub) {
+        acc.re = fma(-c.re, v.re, acc.re);
+        acc.re = fma(c.im, v.im, acc.re);
+        acc.im = fma(-c.re, v.im, acc.im);
+        acc.im = fma(-c.im, v.re, acc.im);
+    } else {
+        acc.re = fma(c.re, v.re, acc.re);
+        acc.re = fma(-c.im, v.im, acc.re);
+        acc.im = fma(c.re, v.im, acc.im);
+        acc.im = fma(c.im, v.re, acc.im);
+    }
+}
 
 // ---- FP64 arithmetic without FMA contraction (mirrors Julia's rounding) ----
 __device__ __forceinline__ cplx<double> cmul_rn(cplx<double> a, cplx<double> b) {

@@ -1024,7 +1024,7 @@ int residual(fdfd_handle* h, const cplx<double>* x, const cplx<double>* b, cplx<
     // algorithmic bytes per unknown: 5 stencil coefficients (80 B), x, r and b (16 B each)
     prof_end(h, ev, FDFD_PROF_RESIDUAL, (double)N * nrhs * (80.0 + 16.0 * (b ? 3 : 2)));
     if (norms) {
-        LAUNCH(reduce_partials_kernel, nrhs, 256, 0, h->part, nb, 2, h->red);
+        LAUNCH(reduce_partials_kernel, dim3(nrhs, 2), 256, 0, h->part, nb, 2, h->red);
         norms->resize(2 * nrhs);
         CK(cudaMemcpyAsync(norms->data(), h->red, 2 * nrhs * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
         CK(cudaStreamSynchronize(h->stream));
@@ -1040,7 +1040,7 @@ int dots(fdfd_handle* h, const cplx<double>* V, long long vstride, int nvec, con
     RET(ensure_part(h, (size_t)nrhs * nb * 2 * nvec));
     RET(ensure_red(h, (size_t)nrhs * 2 * nvec));
     LAUNCH(vdots_kernel, dim3(nb, nrhs), 256, 0, N, nvec, V, vstride, w, h->part);
-    LAUNCH(reduce_partials_kernel, nrhs, 256, 0, h->part, nb, 2 * nvec, h->red);
+    LAUNCH(reduce_partials_kernel, dim3(nrhs, 2 * nvec), 256, 0, h->part, nb, 2 * nvec, h->red);
     std::vector<double> tmp(2 * nvec * nrhs);
     CK(cudaMemcpyAsync(tmp.data(), h->red, tmp.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
@@ -1074,16 +1074,16 @@ int arnoldi_orth(fdfd_handle* h, const cplx<double>* V, long long vstride, int n
     double* r2 = h->red + nc;
     double* r3 = h->red + 2 * nc;
     LAUNCH(vdots_kernel, dim3(nb, nrhs), 256, 0, N, nvec, V, vstride, w, h->part);
-    LAUNCH(reduce_partials_kernel, nrhs, 256, 0, h->part, nb, 2 * nvec, r1);
+    LAUNCH(reduce_partials_kernel, dim3(nrhs, 2 * nvec), 256, 0, h->part, nb, 2 * nvec, r1);
     const dim3 ge(ceil_div(N, 256), nrhs);
     LAUNCH(vcombine_kernel, ge, 256, 0, N, nvec, V, vstride, reinterpret_cast<const cplx<double>*>(r1), nvec,
            -1.0, w);
     LAUNCH(vdots_kernel, dim3(nb, nrhs), 256, 0, N, nvec, V, vstride, w, h->part);
-    LAUNCH(reduce_partials_kernel, nrhs, 256, 0, h->part, nb, 2 * nvec, r2);
+    LAUNCH(reduce_partials_kernel, dim3(nrhs, 2 * nvec), 256, 0, h->part, nb, 2 * nvec, r2);
     LAUNCH(vcombine_kernel, ge, 256, 0, N, nvec, V, vstride, reinterpret_cast<const cplx<double>*>(r2), nvec,
            -1.0, w);
     LAUNCH(vdots_kernel, dim3(nb, nrhs), 256, 0, N, 1, w, 0, w, h->part);
-    LAUNCH(reduce_partials_kernel, nrhs, 256, 0, h->part, nb, 2, r3);
+    LAUNCH(reduce_partials_kernel, dim3(nrhs, 2), 256, 0, h->part, nb, 2, r3);
     LAUNCH(vnormalize_kernel, dim3(ceil_div(N, 256), nrhs), 256, 0, N, w, r3, w);
     std::vector<double> tmp(2 * nc + 2 * (size_t)nrhs);
     CK(cudaMemcpyAsync(tmp.data(), h->red, tmp.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
