@@ -56,6 +56,23 @@ def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)), int(os.environ.get("WORLD_SIZE", 1))
 
 
+def max_over_ranks(t: float, world: int, device: str = "cuda") -> float:
+    """The slowest rank's time: the job of N independent replicas ends with its last one.
+    `device` is where the process group's backend reduces ("cuda" for NCCL, "cpu" for gloo)."""
+    if world <= 1:
+        return t
+    import torch
+    import torch.distributed as dist
+    tt = torch.tensor([t], device=device, dtype=torch.float64)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    return float(tt.item())
+
+
+def job_rate(world: int, steps: int, t: float) -> float:
+    """Whole-job throughput: every rank ran `steps` steps of its own replica in at most t seconds."""
+    return world * steps / t
+
+
 # ---------------------------------------------------------------------------
 # clocks sampler (nvidia-smi during the timed region)
 # ---------------------------------------------------------------------------
@@ -477,12 +494,8 @@ def main():
     if world > 1:
         torch.distributed.barrier()
     clk = clocks.stop()
-    t = e0.elapsed_time(e1) / 1e3
-    if world > 1:
-        tt = torch.tensor([t], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t = float(tt.item())
-    value = world * a.steps / t
+    t = max_over_ranks(e0.elapsed_time(e1) / 1e3, world)
+    value = job_rate(world, a.steps, t)
     # per-class device times for the rooflines: separate steps with profiling on (the library then
     # brackets every launch with events and runs the Gauss-Jordan updates on one stream)
     prof_steps = min(a.steps, 3)
@@ -535,12 +548,15 @@ def main():
 
         e2e_step()
         torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
         t0 = time.perf_counter()
         for _ in range(a.steps):
             e2e_step()
-        te = time.perf_counter() - t0
+        torch.cuda.synchronize()
+        te = max_over_ranks(time.perf_counter() - t0, world)
         he.close()
-        e2e = {"value": world * a.steps / te, "unit": "solves/s", "h2d_bytes_per_step": h2d,
+        e2e = {"value": job_rate(world, a.steps, te), "unit": "solves/s", "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": d2h}
 
     # rooflines: the factorization's tensor-core GEMM (tensor-bound) and the solve sweeps (HBM-bound),
