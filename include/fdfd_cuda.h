@@ -96,7 +96,8 @@ void fdfd_destroy(fdfd_handle* h);
 const char* fdfd_last_error(const fdfd_handle* h);
 
 /* Refinement stopping rule: ||b - A x||/||b|| <= tol within max_iter factor
- * solves (FDFD_REFINE_GMRES restarts its Krylov basis every 20 solves). */
+ * solves (FDFD_REFINE_GMRES restarts its Krylov basis every m solves, m from
+ * fdfd_set_restart). */
 int  fdfd_set_refinement(fdfd_handle* h, double tol, int max_iter, int mode);
 
 /* Basis length m of the restarted FGMRES refinement (0: automatic, the
