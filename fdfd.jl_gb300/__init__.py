@@ -34,7 +34,7 @@ EPS0 = 8.85418782e-12
 MU0 = 1.25663706e-6
 C0 = math.sqrt(1 / EPS0 / MU0)
 ETA0 = math.sqrt(MU0 / EPS0)
-DEFAULT_L0 = 1e-6          # src/grid.jl:31
+DEFAULT_L0 = 1e-6          # src/grid.jl:5
 TM, TE = _lib.FDFD_TM, _lib.FDFD_TE   # src/types.jl:20
 X, Y = _lib.FDFD_X, _lib.FDFD_Y       # src/types.jl:18 (x̂, ŷ)
 IterativeMethodGN, IterativeMethodB = _lib.FDFD_CHI3_NEWTON, _lib.FDFD_CHI3_BORN   # src/solver/nonlinear.jl:5
@@ -48,7 +48,7 @@ class Point:
 
 
 class Grid:
-    """2-D grid (src/grid.jl:33-59): N = round(L/dh) cells per axis, Npml PML
+    """2-D grid (src/grid.jl:7-33): N = round(L/dh) cells per axis, Npml PML
     cells per side, bounds ((x1, y1), (x2, y2)) in units of L₀."""
 
     def __init__(self, dh, Npml, xrange, yrange, L0=DEFAULT_L0):
@@ -72,20 +72,20 @@ class Grid:
     def size(self):
         return self.N
 
-    def dx(self):  # src/grid.jl:94-96
+    def dx(self):  # src/grid.jl:68-70
         return (self.bounds[1][0] - self.bounds[0][0]) / self.N[0]
 
-    def dy(self):  # src/grid.jl:98-100
+    def dy(self):  # src/grid.jl:72-74
         return (self.bounds[1][1] - self.bounds[0][1]) / self.N[1]
 
-    def xc(self):  # src/grid.jl:102-104
+    def xc(self):  # src/grid.jl:76-78
         return self.bounds[0][0] + self.dx() * (np.arange(self.N[0]) + 0.5)
 
-    def yc(self):  # src/grid.jl:106-108
+    def yc(self):  # src/grid.jl:80-82
         return self.bounds[0][1] + self.dy() * (np.arange(self.N[1]) + 0.5)
 
     def coord2ind(self, pt: Point):
-        """0-based (ix, iy), src/grid.jl:129-151."""
+        """0-based (ix, iy), src/grid.jl:103-125."""
         ix = int(round((pt.x - self.bounds[0][0]) / self.L[0] * self.N[0]) + 1)
         iy = int(round((pt.y - self.bounds[0][1]) / self.L[1] * self.N[1]) + 1)
         return min(max(ix, 1), self.N[0]) - 1, min(max(iy, 1), self.N[1]) - 1
@@ -93,7 +93,7 @@ class Grid:
 
 @dataclass
 class Mode:
-    """src/device.jl:7-13: polarization, slice normal (X or Y), effective-index
+    """src/device.jl:5-11: polarization, slice normal (X or Y), effective-index
     guess, centre point and slice width (L₀ units)."""
     pol: int
     dir: int
@@ -127,7 +127,7 @@ class Device:
 
 @dataclass
 class ModulatedDevice:
-    """src/solver/modulation.jl:4-28: a Device with a modulation amplitude Δϵᵣ
+    """src/solver/modulation.jl:4-26: a Device with a modulation amplitude Δϵᵣ
     (zero by default), modulation frequency Ω, the number of sidebands on each
     side of the carrier and whether the sidebands share the carrier's PML."""
     grid: Grid
@@ -195,7 +195,7 @@ def setup_src(d: Device, where, value=None):
 
 
 def setup_deps(d: ModulatedDevice, region, value):
-    """setup_Δϵᵣ!(d, region, value): src/solver/modulation.jl:29-30 (region and value may be callables)."""
+    """setup_Δϵᵣ!(d, region, value): src/solver/modulation.jl:31-32 (region and value may be callables)."""
     m, X, Y = _mask(d, region)
     d.deps[m] = np.vectorize(value)(X, Y)[m] if callable(value) else value
 
@@ -210,7 +210,7 @@ globals()["setup_χ"] = setup_chi
 
 
 def add_mode(d, mode: Mode):
-    """add_mode!(d, mode): src/device.jl:111-114."""
+    """add_mode!(d, mode): src/device.jl:112-115."""
     d.modes.append(mode)
 
 
@@ -227,7 +227,7 @@ def _mode_handle(d):
 
 
 def get_modes(d, pol, omega, neff, nmodes, pt: Point, slicenormal, slicewidth):
-    """get_modes(d, pol, ω, neff, nmodes, pt, slicenormal, slicewidth): src/device.jl:122-149, computed on
+    """get_modes(d, pol, ω, neff, nmodes, pt, slicenormal, slicewidth): src/device.jl:124-149, computed on
     the GPU (nmodes = 1).  Returns (β, vector, indx, indy) with 0-based slice indices."""
     if nmodes != 1:
         raise FDFDError(_lib.FDFD_EINVAL, "get_modes: the GPU mode solver returns one mode (nmodes = 1)")
@@ -244,7 +244,7 @@ def get_modes(d, pol, omega, neff, nmodes, pt: Point, slicenormal, slicewidth):
 
 
 def setup_mode(d, pol, omega, neff, pt: Point, srcnormal, srcwidth):
-    """setup_mode!(d, pol, ω, neff, pt, srcnormal, srcwidth): src/device.jl:116-120 — adds
+    """setup_mode!(d, pol, ω, neff, pt, srcnormal, srcwidth): src/device.jl:118-121 — adds
     normalize(abs.(v)) to d.src on the slice."""
     h = _mode_handle(d)
     try:
@@ -355,12 +355,12 @@ def make_handle(d: Device, pol=TM, precision="mixed", pml_m=3.5, pml_lnR=-12.0, 
 
 def solve(d: Device, pol=TM, precision="mixed", pml_m=3.5, pml_lnR=-12.0, tol=1e-10, max_iter=40,
           return_stats=False):
-    """solve(d::Device, pol) — src/solver/driven.jl:153-208.
+    """solve(d::Device, pol) — src/solver/driven.jl:4-59.
 
     One factorization per frequency (as the reference re-factors per ω) and a
     refined solve for d.src.  ``pml_m``/``pml_lnR`` default to the values the
     reference hard-wires (src/pml.jl:1, S_create does not forward them).
-    Returns a FieldTM/FieldTE, or a list when len(d.omega) > 1 (driven.jl:206-207).
+    Returns a FieldTM/FieldTE, or a list when len(d.omega) > 1 (driven.jl:57-58).
     A ModulatedDevice takes the coupled-sideband path (``solve_modulated``).
     """
     if isinstance(d, ModulatedDevice):
@@ -391,7 +391,7 @@ def solve(d: Device, pol=TM, precision="mixed", pml_m=3.5, pml_lnR=-12.0, tol=1e
 
 def solve_chi3(d: Chi3Device, method=IterativeMethodGN, precision="mixed", pml_m=3.5, pml_lnR=-12.0,
                tol=1e-12, maxiterations=50, max_iter=40, return_stats=False):
-    """solve(d::χ3Device, which_method) — src/solver/nonlinear.jl:36-91 (TM): per ω one
+    """solve(d::χ3Device, which_method) — src/solver/nonlinear.jl:36-90 (TM): per ω one
     factorization of the linear operator, reused by every Born or Newton step."""
     g = d.grid
     h = _lib.Handle(g.N[0], g.N[1], g.Npml[0], g.Npml[1], g.dx(), g.dy(), g.L0, pml_m, pml_lnR, TM,
@@ -432,7 +432,7 @@ def solve_modulated(d: ModulatedDevice, precision="mixed", pml_m=3.5, pml_lnR=-1
         h.set_eps(d.eps)
         h.set_deps(d.deps)
         if d.modes:
-            srcs = h.mode_sources(d.omega, [_mode_spec(d, m, TM) for m in d.modes])   # modulation.jl:51-56
+            srcs = h.mode_sources(d.omega, [_mode_spec(d, m, TM) for m in d.modes])   # modulation.jl:51-55
         for i, w in enumerate(d.omega):
             if d.modes:
                 d.src = srcs[i].copy()
@@ -447,7 +447,7 @@ def solve_modulated(d: ModulatedDevice, precision="mixed", pml_m=3.5, pml_lnR=-1
 
 
 def eigenfrequency(d: Device, pol, nev, which="LM", precision="mixed", pml_m=3.5, pml_lnR=-12.0, tol=1e-10):
-    """eigenfrequency(d, pol, nev; which) — src/solver/eigen.jl:318-364."""
+    """eigenfrequency(d, pol, nev; which) — src/solver/eigen.jl:69-115."""
     h = make_handle(d, pol, precision, pml_m, pml_lnR, tol)
     try:
         N = d.grid.N[0] * d.grid.N[1]

@@ -49,7 +49,7 @@ class Stats(C.Structure):
 
 
 class Mode(C.Structure):
-    """fdfd_mode: one mode source (Mode, src/device.jl:7-13)."""
+    """fdfd_mode: one mode source (Mode, src/device.jl:5-11)."""
     _fields_ = [("pol", C.c_int), ("normal", C.c_int), ("ix", C.c_int), ("iy", C.c_int), ("width", C.c_double),
                 ("neff_re", C.c_double), ("neff_im", C.c_double)]
 

@@ -2,8 +2,8 @@
 //
 // The operator is the reference's 5-point FDFD matrix, assembled per unknown
 // instead of as sparse products.  Unknown k = ix + Nx*iy (x fastest, the
-// column-major `A[:]` ordering of src/solver/driven.jl:170).  All neighbours are
-// periodic, exactly as the reference's difference matrices (src/grid.jl:164-177,
+// column-major `A[:]` ordering of src/solver/driven.jl:21).  All neighbours are
+// periodic, exactly as the reference's difference matrices (src/grid.jl:138-151,
 // the ±(N-1) corner entries).
 #include "common.cuh"
 #include "kernels.cuh"
@@ -17,7 +17,7 @@
 __device__ cplx<double> sfactor_value(int i1, int Nw, int Npml, double dw, bool forward,
                                       double omega, double eps0n, double eta0,
                                       double m, double lnR) {
-    // i1 is the 1-based index of the reference loop (pml.jl:202-216).
+    // i1 is the 1-based index of the reference loop (pml.jl:14-28).
     if (Npml == 0) return cmk(1.0, 0.0);
     double Tw = Npml * dw;
     double sigmax = -(m + 1) * lnR / (2 * eta0 * Tw);
@@ -32,7 +32,7 @@ __device__ cplx<double> sfactor_value(int i1, int Nw, int Npml, double dw, bool 
         else return cmk(1.0, 0.0);
     }
     double sig = sigmax * pow(l / Tw, m);
-    // S(l) = 1 - 1im*σ(l)/(ω ϵ₀)  (pml.jl:198)
+    // S(l) = 1 - 1im*σ(l)/(ω ϵ₀)  (pml.jl:10)
     return cmk(1.0, -(sig / (omega * eps0n)));
 }
 
@@ -54,15 +54,15 @@ __global__ void sfactor_kernel(SFactorArgs a, cplx<double>* out) {
 // [self, (ix-1,iy), (ix+1,iy), (ix,iy-1), (ix,iy+1)] of the operator selected
 // by `op`, evaluated in the order the reference's sparse products evaluate them
 // (products without FMA contraction, as Julia does).
-//   OP_TM_DRIVEN  A = δxf μ₀⁻¹ δxb + δyf μ₀⁻¹ δyb + ω² Tϵ          driven.jl:184
-//   OP_TE_DRIVEN  A = δxf Tϵxi δxb + δyf Tϵyi δyb + ω² μ₀ I         driven.jl:194
-//   OP_TM_EIGEN   A = Tϵᵣ⁻¹δxf δxb + Tϵᵣ⁻¹δyf δyb - σ I             eigen.jl:333
-//   OP_TE_EIGEN   A = δxf Tϵx⁻¹ δxb + δyf Tϵy⁻¹ δyb - σ I           eigen.jl:351
+//   OP_TM_DRIVEN  A = δxf μ₀⁻¹ δxb + δyf μ₀⁻¹ δyb + ω² Tϵ          driven.jl:35
+//   OP_TE_DRIVEN  A = δxf Tϵxi δxb + δyf Tϵyi δyb + ω² μ₀ I         driven.jl:45
+//   OP_TM_EIGEN   A = Tϵᵣ⁻¹δxf δxb + Tϵᵣ⁻¹δyf δyb - σ I             eigen.jl:84
+//   OP_TE_EIGEN   A = δxf Tϵx⁻¹ δxb + δyf Tϵy⁻¹ δyb - σ I           eigen.jl:102
 //   OP_TM_SIDEBAND  Aₙ = Sxb δxb μ₀⁻¹ Sxf δxf + Syb δyb μ₀⁻¹ Syf δyf + ωₙ² Tϵ
-//                 (one sideband of a modulated device, modulation.jl:80-88:
+//                 (one sideband of a modulated device, modulation.jl:82-90:
 //                 backward difference outside, forward inside)
-// with δxf = Sxf·δ(x̂,Forward) etc. (driven.jl:177-180) and the Tϵ averages
-// of grid_average (grid.jl:183-188).
+// with δxf = Sxf·δ(x̂,Forward) etc. (driven.jl:28-31) and the Tϵ averages
+// of grid_average (grid.jl:157-162).
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ cplx<double> eps_avg_inv(const cplx<double>* eps, int ix, int iy, int Nx, int Ny,
                                                     bool alongx, double eps0n) {
@@ -208,7 +208,7 @@ __global__ void residual_kernel(int Nx, int Ny, int nrhs, const cplx<double>* __
     }
 }
 
-// Residual of the coupled sideband system (modulation.jl:91-99), nrhs = 1:
+// Residual of the coupled sideband system (modulation.jl:93-101), nrhs = 1:
 // r_n = b_n - (A_n x_n + ½ωₙ²ϵ₀ conj(Δϵ)⊙x_{n+1} + ½ωₙ²ϵ₀ Δϵ⊙x_{n-1}); vectors are
 // sideband-major (x_n at offset n·Nx·Ny).  Grid (blocks, K); partial sums of
 // |r|², |b|² per (sideband, block) in part[n][block][2].
@@ -271,7 +271,7 @@ __global__ void residual_mf_kernel(MfResidualArgs a, const cplx<double>* __restr
 }
 
 // ---------------------------------------------------------------------------
-// χ³ systems of the nonlinear driven solve (src/solver/nonlinear.jl:94-129).
+// χ³ systems of the nonlinear driven solve (src/solver/nonlinear.jl:92-129).
 // mode 1 (Born): r = b − (A + diag d1) x on one N-vector;
 // mode 2 (Newton on the stacked unknown [x1; x2]):
 //   r1 = b1 − (A x1 + d1⊙x1 + d2⊙x2),  r2 = b2 − (conj(A) x2 + conj(d2)⊙x1 + conj(d1)⊙x2).
@@ -334,7 +334,7 @@ __global__ void residual_nl_kernel(int Nx, int Ny, int mode, const cplx<double>*
     }
 }
 
-// χ³ diagonals from the field e (coeff = ω²ϵ₀·3χ/L₀, nonlinear.jl:74):
+// χ³ diagonals from the field e (coeff = ω²ϵ₀·3χ/L₀, nonlinear.jl:71):
 // mode 1: d1 = coeff|e|²;  mode 2 (Newton Jacobian): d1 = 2coeff|e|², d2 = coeff·e².
 __global__ void chi3_diag_kernel(long long N, int mode, const double* __restrict__ coeff,
                                  const cplx<double>* __restrict__ e, cplx<double>* __restrict__ d1,
@@ -390,10 +390,10 @@ __global__ void reduce_partials_kernel(const double* __restrict__ part, int nblo
 
 // ---------------------------------------------------------------------------
 // Field recovery (FP64), following the reference's expression order:
-//   REC_TM_DRIVEN  hx = c_x·(δyb ez), hy = c_y·(δxb ez)        driven.jl:189-190
-//   REC_TM_EIGEN   hx = c_x·(δyf ez), hy = c_y·(δxf ez)        eigen.jl:339-340
-//   REC_TE_DRIVEN  ex = (c·Tϵyi)(δyb hz), ey = (c·Tϵxi)(-δxb hz) driven.jl:199-200
-//   REC_TE_EIGEN   ex = (c·Tϵx⁻¹)(δyb hz), ey = (c·Tϵy⁻¹)(-δxb hz) eigen.jl:357-358
+//   REC_TM_DRIVEN  hx = c_x·(δyb ez), hy = c_y·(δxb ez)        driven.jl:40-41
+//   REC_TM_EIGEN   hx = c_x·(δyf ez), hy = c_y·(δxf ez)        eigen.jl:90-91
+//   REC_TE_DRIVEN  ex = (c·Tϵyi)(δyb hz), ey = (c·Tϵxi)(-δxb hz) driven.jl:50-51
+//   REC_TE_EIGEN   ex = (c·Tϵx⁻¹)(δyb hz), ey = (c·Tϵy⁻¹)(-δxb hz) eigen.jl:108-109
 // TM: the scalar multiplies the matrix entries before the product (Julia
 // evaluates coef*δ first), c_x = -1/1im/ω/μ₀, c_y = 1/1im/ω/μ₀.
 // TE: c = 1/1im/ω.  Coefficients are per right-hand side (complex ω for eigen).

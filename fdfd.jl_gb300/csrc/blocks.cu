@@ -4,7 +4,7 @@
 // With unknowns grouped into n "nodes" (grid lines) of b unknowns each, the
 // 5-point operator is block-cyclic-tridiagonal: node j couples to itself
 // through a cyclic tridiagonal D_j and to its ring neighbours j∓1 through
-// diagonal matrices L_j, U_j (the periodic ±(N-1) corners of src/grid.jl:164-177
+// diagonal matrices L_j, U_j (the periodic ±(N-1) corners of src/grid.jl:138-151
 // close both the in-line and the node ring).
 #include "common.cuh"
 #include "kernels.cuh"

@@ -1296,7 +1296,7 @@ int assemble(fdfd_handle* h, int op, double omega_pml, zd sigma, double omega_dr
 int factor_op(fdfd_handle* h, int prec = -1);
 
 // modulated device: assemble and factor the K sideband operators
-// (modulation.jl:77-89; PML at ω when shared, else at ωₙ)
+// (modulation.jl:79-92; PML at ω when shared, else at ωₙ)
 int factor_mf(fdfd_handle* h, int prec) {
     MfState& M = *h->mf;
     h->factored = false;
@@ -1520,7 +1520,7 @@ int solve_core(fdfd_handle* h, const cplx<double>* d_src, int nrhs, cplx<double>
     long long N = (long long)h->Nx * h->Ny;
     RET(ensure_krylov(h, nrhs, restart_len(h, nrhs)));
     cudaEventRecord(h->ev[3], h->stream);
-    // b = iω·src   (driven.jl:185,195)
+    // b = iω·src   (driven.jl:36,46)
     std::vector<zd> iw(nrhs, zd(0, h->omega));
     RET(scale_vec(h, d_src, iw, nrhs, h->kb));
     int iters = 0;
@@ -1530,7 +1530,7 @@ int solve_core(fdfd_handle* h, const cplx<double>* d_src, int nrhs, cplx<double>
     RET(check_device(h, "solve"));
     if (f1) CK(cudaMemcpyAsync(f1, h->kx, N * nrhs * sizeof(cplx<double>), cudaMemcpyDeviceToDevice, h->stream));
     if (f2 || f3) {
-        // coefficients per rhs (driven.jl:189-190, 199-200)
+        // coefficients per rhs (driven.jl:40-41, 199-200)
         std::vector<zd> coef(2 * nrhs);
         const double w = h->omega, mu0 = kMU0 * h->L0;
         for (int r = 0; r < nrhs; ++r) {
@@ -1687,7 +1687,7 @@ int fdfd_mf_factor(fdfd_handle* h, double omega, double Omega) {
     M.Omega = Omega;
     M.wn.resize(M.K);
     for (int j = 0; j < M.K; ++j) {
-        M.wn[j] = omega + Omega * (j - M.s);   // modulation.jl:47
+        M.wn[j] = omega + Omega * (j - M.s);   // modulation.jl:49
         if (!(M.wn[j] > 0))
             return set_err(h, FDFD_EINVAL, "sideband frequency omega + %d*Omega = %g is not positive", j - M.s, M.wn[j]);
     }
@@ -1724,7 +1724,7 @@ int fdfd_mf_solve(fdfd_handle* h, const double* src, double* ez, double* hx, dou
     RET(ensure_krylov(h, 1, restart_len(h, 1)));
     CK(cudaMemcpyAsync(d_src, src, N * sizeof(cplx<double>), cudaMemcpyHostToDevice, h->stream));
     cudaEventRecord(h->ev[3], h->stream);
-    // b = iω·src in the centre sideband, zero elsewhere (modulation.jl:62-64)
+    // b = iω·src in the centre sideband, zero elsewhere (modulation.jl:67-69)
     CK(cudaMemsetAsync(h->kb, 0, bytes, h->stream));
     const zd iw(0, M.omega);
     CK(cudaMemcpyAsync(h->kc, &iw, sizeof(zd), cudaMemcpyHostToDevice, h->stream));
@@ -1733,7 +1733,7 @@ int fdfd_mf_solve(fdfd_handle* h, const double* src, double* ez, double* hx, dou
     double rel = 0;
     RET(refine_fb(h, 1, &iters, &rel));
     cudaEventRecord(h->ev[4], h->stream);
-    // H per sideband with forward differences (modulation.jl:110-111)
+    // H per sideband with forward differences (modulation.jl:112-113)
     std::vector<zd> coef(2 * M.K);
     const double mu0 = kMU0 * h->L0;
     for (int j = 0; j < M.K; ++j) {
@@ -1791,8 +1791,8 @@ int fdfd_mf_solve(fdfd_handle* h, const double* src, double* ez, double* hx, dou
 // ---- guided modes and mode sources (get_modes, setup_mode!, eigenmode) ------
 namespace {
 
-// slice of one Mode (device.jl:122-143): srcpoints = round(width/dh), made odd,
-// centred on (ix, iy) across the slice normal; shift σ = (ω n_eff/c₀)² (eigen.jl:22)
+// slice of one Mode (device.jl:124-142): srcpoints = round(width/dh), made odd,
+// centred on (ix, iy) across the slice normal; shift σ = (ω n_eff/c₀)² (eigen.jl:23-25)
 int mode_job(fdfd_handle* h, const fdfd_mode* md, double omega, ModeJob* J) {
     if (!md) return set_err(h, FDFD_EINVAL, "mode is NULL");
     if (md->normal != FDFD_X && md->normal != FDFD_Y) return set_err(h, FDFD_EINVAL, "mode normal must be FDFD_X or FDFD_Y");
@@ -2061,7 +2061,7 @@ int fdfd_chi3_solve(fdfd_handle* h, const double* chi, const double* src, int me
         h->io_cap = 4 * vb;
     }
     cplx<double>* d_src = h->io;
-    // coeff = ω²ϵ₀·3χ/L₀ (nonlinear.jl:74, ϵ₀ normalised)
+    // coeff = ω²ϵ₀·3χ/L₀ (nonlinear.jl:71, ϵ₀ normalised)
     std::vector<double> coeff(N);
     const double w = h->omega;
     for (long long k = 0; k < N; ++k) coeff[k] = w * w * (kEPS0 * h->L0) * 3 * chi[k] / h->L0;
@@ -2078,13 +2078,13 @@ int fdfd_chi3_solve(fdfd_handle* h, const double* chi, const double* src, int me
     CK(cudaMemcpyAsync(B, h->kb, vb, cudaMemcpyDeviceToDevice, h->stream));
     int iters = 0, it = 0;
     double rel = 0;
-    RET(refine_fb(h, 1, &it, &rel));   // linear solve (nonlinear.jl:71-72)
+    RET(refine_fb(h, 1, &it, &rel));   // linear solve (nonlinear.jl:66-69)
     iters += it;
     CK(cudaMemcpyAsync(Z, h->kx, vb, cudaMemcpyDeviceToDevice, h->stream));
     std::vector<double> errs(1, 1.0);
     const int nb = ceil_div(N, 256);
     if (method == FDFD_CHI3_BORN) {
-        // _doborn (nonlinear.jl:94-108)
+        // _doborn (nonlinear.jl:92-106)
         for (int i = 1; errs.back() > tol && i <= maxit; ++i) {
             LAUNCH(chi3_diag_kernel, nb, 256, 0, N, 1, dco, Z, h->nl_d1, h->nl_d2);
             h->nl_mode = 1;
@@ -2098,7 +2098,7 @@ int fdfd_chi3_solve(fdfd_handle* h, const double* chi, const double* src, int me
             errs.push_back(nd / nz);
         }
     } else {
-        // _donewton (nonlinear.jl:110-129) on [e; conj(e)]: J δ = [F; conj F], e ← e − δ.  With
+        // _donewton (nonlinear.jl:108-129) on [e; conj(e)]: J δ = [F; conj F], e ← e − δ.  With
         // r = b − (A + diag(coeff|e|²)) e = −F the system is solved for δ' = −δ and e += δ'.
         LAUNCH(vconj_kernel, nb, 256, 0, N, Z, Z + N);
         h->nsb = 2;
@@ -2119,7 +2119,7 @@ int fdfd_chi3_solve(fdfd_handle* h, const double* chi, const double* src, int me
     }
     RET(check_launch(h, "chi3"));
     cudaEventRecord(h->ev[4], h->stream);
-    // H recovery (nonlinear.jl:86-87): the driven TM recovery of the final field
+    // H recovery (nonlinear.jl:82-83): the driven TM recovery of the final field
     std::vector<zd> coef(2);
     const double mu0 = kMU0 * h->L0;
     coef[0] = zd(-0.0, (1.0 / w) / mu0);
@@ -2305,7 +2305,7 @@ int fdfd_eigfreq(fdfd_handle* h, double omega0, int nev, int which, double tol, 
     auto t0 = std::chrono::steady_clock::now();
     h->launches = 0;
     const double eps0 = kEPS0 * h->L0, mu0 = kMU0 * h->L0;
-    // eigen.jl:335 (TM) and :353 (TE): shift σ = -ω₀²μ₀ϵ₀ resp. -ω₀²μ₀, PML frozen at ω₀
+    // eigen.jl:86 (TM) and :104 (TE): shift σ = -ω₀²μ₀ϵ₀ resp. -ω₀²μ₀, PML frozen at ω₀
     const zd sigma = h->pol == FDFD_TM ? zd(-omega0 * omega0 * mu0 * eps0, 0) : zd(-omega0 * omega0 * mu0, 0);
     cudaEventRecord(h->ev[0], h->stream);
     h->factored = false;
@@ -2421,7 +2421,7 @@ int fdfd_eigfreq(fdfd_handle* h, double omega0, int nev, int which, double tol, 
     for (int q = 0; q < nev; ++q) {
         const zd th = theta[order[q]];
         lam[q] = sigma + 1.0 / th;
-        om[q] = h->pol == FDFD_TM ? std::sqrt(-lam[q] / mu0 / eps0) : std::sqrt(-lam[q] / mu0);   // eigen.jl:336,354
+        om[q] = h->pol == FDFD_TM ? std::sqrt(-lam[q] / mu0 / eps0) : std::sqrt(-lam[q] / mu0);   // eigen.jl:87,105
         omega[2 * q] = om[q].real();
         omega[2 * q + 1] = om[q].imag();
         if (lambda) { lambda[2 * q] = lam[q].real(); lambda[2 * q + 1] = lam[q].imag(); }
@@ -2449,7 +2449,7 @@ int fdfd_eigfreq(fdfd_handle* h, double omega0, int nev, int which, double tol, 
             double* f1 = fields + (size_t)q * 3 * 2 * N;
             memcpy(f1, host.data(), vbytes);
             CK(cudaMemcpyAsync(y, host.data(), vbytes, cudaMemcpyHostToDevice, h->stream));
-            // eigen.jl:339-340 (TM, forward differences) / :357-358 (TE)
+            // eigen.jl:90-91 (TM, forward differences) / :108-109 (TE)
             std::vector<zd> coef(2);
             if (h->pol == FDFD_TM) {
                 coef[0] = zd(-0.0, 1.0) / om[q] / mu0;    // -1/1im/ω/μ₀

@@ -1,7 +1,7 @@
 // Field post-processing: Poynting flux and its line integral (src/flux.jl).
 //
 //   poynting (flux.jl:15-29), per cell, with grid_average(a, w) = (a + a shifted
-//   by one cell along w)/2 (periodic, grid.jl:183-188):
+//   by one cell along w)/2 (periodic, grid.jl:157-162):
 //     TM: Sx = -½ Re(avgx(Ez)·conj(Hy)),  Sy = ½ Re(avgy(Ez)·conj(Hx))
 //     TE: Sx =  ½ Re(Ey·conj(avgx(Hz))),  Sy = -½ Re(Ex·conj(avgy(Hz)))
 //   (the reference's TE branch reads `field.Hz_x`/`field.Hz_y`, fields a FieldTE

@@ -1,12 +1,12 @@
 // Guided modes of 1-D grid slices and the mode sources built from them.
 //
 // The reference computes a mode source per frequency before each driven solve
-// (src/solver/driven.jl:15-19): get_modes (src/device.jl:122-149) cuts the ϵᵣ
+// (src/solver/driven.jl:15-19): get_modes (src/device.jl:124-149) cuts the ϵᵣ
 // slice of a Mode, eigenmode (src/solver/eigen.jl:6-29) builds the periodic 1-D
 // operator
 //   TM: A = ω²μ₀Tϵ + δxf δxb            TE: A = ω²μ₀Tϵ + Tϵ δxf Tϵxinv δxb
 // and ARPACK's shift-invert `eigs(A, nev=1, sigma=(ω n_eff/c₀)²)` returns the
-// eigenpair nearest the shift; setup_mode! (device.jl:116-120) adds
+// eigenpair nearest the shift; setup_mode! (device.jl:118-121) adds
 // normalize(abs.(v)) to the source on the slice.
 //
 // Here every (frequency, mode) pair is one job of one warp, in FP64, all in
@@ -77,7 +77,7 @@ __global__ void __launch_bounds__(32) mode_kernel(const ModeJob* __restrict__ jo
     const double h2 = 1.0 / (J.dh * J.dh);
     const double w2mu = J.omega * J.omega * mu0n;
 
-    // ---- the 1-D operator (eigen.jl:14-20) ----
+    // ---- the 1-D operator (eigen.jl:16-21) ----
     for (int i = lane; i < n; i += 32) {
         const cplx<double> e = eps[J.k0 + (long long)i * J.stride];
         const cplx<double> te = cscale(e, eps0n);                                 // Tϵ_i
@@ -265,7 +265,7 @@ __global__ void __launch_bounds__(32) mode_kernel(const ModeJob* __restrict__ jo
     }
 }
 
-// Mode sources (device.jl:116-120, driven.jl:15-19): src[w] = Σ over the modes of
+// Mode sources (device.jl:118-121, driven.jl:15-19): src[w] = Σ over the modes of
 // frequency w of |v| on the slice (v has unit norm, so |v| is normalize(abs.(v))).
 // One block per frequency; modes are added in order, a block-wide barrier
 // between modes (slices may overlap).

@@ -199,7 +199,7 @@ def phc_cavity(n_cells=12, res=20, eps_rod=8.9, radius=0.2, npml=NPML, a_um=1.0,
 def modulated_waveguide(dh=0.02, L=5.0, nsidebands=1, npml=(15, 15), waist_um=0.2, sharedpml=True,
                         mod_range=None):
     """Interband photonic transition in a modulated waveguide, the setup of the
-    reference's own modulated-device test (test/runtests.jl:41-63): x ∈ [0, L],
+    reference's own modulated-device test (test/runtests.jl:40-63): x ∈ [0, L],
     y ∈ [-1, 1] µm at cell size dh, 15 PML cells, carrier ω = 2π·193.9 THz,
     modulation Ω = 4.541e14 rad/s, a guide of width a = 0.2202 µm (ϵᵣ = 12.25)
     and Δϵᵣ = exp(i q x), q = 2.9263 µm⁻¹, on the lower half of the guide for

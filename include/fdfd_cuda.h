@@ -6,14 +6,14 @@
  * (src/solver/solver.jl:4-41), which sees only a CSC matrix.  This library
  * sits one level up and replaces, per frequency, the assembly, the linear
  * solve and the field recovery of
- *   solve(d::Device, pol)                       src/solver/driven.jl:153-208
- *   eigenfrequency(d, pol, nev; which)          src/solver/eigen.jl:318-364
+ *   solve(d::Device, pol)                       src/solver/driven.jl:4-59
+ *   eigenfrequency(d, pol, nev; which)          src/solver/eigen.jl:69-115
  * so that Julia's `solve`/`eigenfrequency` can `ccall` it when
  * ENV["FDFD_SOLVER"] == "cuda".
  *
  * Array conventions (all entry points): complex arrays are interleaved
  * {re, im} doubles (Julia ComplexF64 / C `double _Complex`), Nx*Ny values per
- * field, x fastest (Julia column-major `A[:]`, driven.jl:170).  Host arrays
+ * field, x fastest (Julia column-major `A[:]`, driven.jl:21).  Host arrays
  * belong to the caller and are only read/written during the call.  Every call
  * blocks until its results are in the caller's arrays.  A handle is used by one
  * thread at a time; distinct handles are independent.
@@ -83,8 +83,8 @@ typedef struct {
 /* Version string of the library. */
 const char* fdfd_version(void);
 
-/* Create a handle for an Nx x Ny grid (Grid, src/grid.jl:33-59) with Npx/Npy
- * PML cells per side, cell sizes dx, dy in units of L0 metres (grid.jl:94-100),
+/* Create a handle for an Nx x Ny grid (Grid, src/grid.jl:7-33) with Npx/Npy
+ * PML cells per side, cell sizes dx, dy in units of L0 metres (grid.jl:68-74),
  * PML grading m and ln(R) (create_sfactor, src/pml.jl:1-31; the reference
  * hard-wires m=3.5, lnR=-12 because S_create does not forward them,
  * pml.jl:35-38), polarization FDFD_TM/FDFD_TE and precision FDFD_PREC_*.
@@ -118,14 +118,14 @@ int  fdfd_set_eps(fdfd_handle* h, const double* eps_r);
 
 /* Assemble the driven operator of solve() at angular frequency omega (SI
  * rad/s) and factor it:  TM A = δxf μ₀⁻¹ δxb + δyf μ₀⁻¹ δyb + ω² Tϵ,
- * TE A = δxf Tϵxi δxb + δyf Tϵyi δyb + ω² μ₀ I  (driven.jl:170-194). */
+ * TE A = δxf Tϵxi δxb + δyf Tϵyi δyb + ω² μ₀ I  (driven.jl:21-45). */
 int  fdfd_factor(fdfd_handle* h, double omega);
 
 /* Driven solve with the current factorization for nrhs current sources
- * (Device.src, b = iω·src, driven.jl:185,195), each Nx*Ny complex, stacked.
+ * (Device.src, b = iω·src, driven.jl:36,46), each Nx*Ny complex, stacked.
  * Outputs (each nrhs*Nx*Ny complex, any may be NULL):
- *   TM: f1 = Ez, f2 = Hx, f3 = Hy  (driven.jl:187-191)
- *   TE: f1 = Hz, f2 = Ex, f3 = Ey  (driven.jl:197-202)
+ *   TM: f1 = Ez, f2 = Hx, f3 = Hy  (driven.jl:38-42)
+ *   TE: f1 = Hz, f2 = Ex, f3 = Ey  (driven.jl:48-53)
  * Replaces dolinearsolve (solver.jl:4-41) plus the recovery SpMVs. */
 int  fdfd_solve(fdfd_handle* h, const double* src, int nrhs, double* f1,
                 double* f2, double* f3, fdfd_stats* stats);
@@ -145,7 +145,7 @@ int  fdfd_solve_device(fdfd_handle* h, const double* d_src, int nrhs,
 int  fdfd_adjoint(fdfd_handle* h, const double* src, const double* mvec,
                   double* J, double* grad, double* ez, fdfd_stats* stats);
 
-/* Shift-invert eigenfrequencies (eigenfrequency, src/solver/eigen.jl:318-364):
+/* Shift-invert eigenfrequencies (eigenfrequency, src/solver/eigen.jl:69-115):
  * with the PML frozen at omega0, TM finds eigenpairs of
  * A = Tϵᵣ⁻¹(δxf δxb + δyf δyb) nearest σ = -ω₀²μ₀ϵ₀, TE of
  * A = δxf Tϵx⁻¹ δxb + δyf Tϵy⁻¹ δyb nearest σ = -ω₀²μ₀, by Arnoldi on
@@ -161,7 +161,7 @@ int  fdfd_eigfreq(fdfd_handle* h, double omega0, int nev, int which,
                   double tol, double* omega, double* lambda, double* fields,
                   fdfd_stats* stats);
 
-/* A mode source (Mode, src/device.jl:7-13): polarization, slice normal
+/* A mode source (Mode, src/device.jl:5-11): polarization, slice normal
  * (FDFD_X: the slice runs along y at column ix; FDFD_Y: along x at row iy),
  * centre cell (0-based: coord2ind(grid, Mode.pt) - 1), slice width in L0
  * units and the effective-index guess n_eff. */
@@ -173,7 +173,7 @@ typedef struct {
     double neff_re, neff_im;
 } fdfd_mode;
 
-/* Guided mode of a grid slice: get_modes with nmodes = 1 (src/device.jl:122-149)
+/* Guided mode of a grid slice: get_modes with nmodes = 1 (src/device.jl:124-149)
  * and the 1-D eigenmode it calls (src/solver/eigen.jl:6-29).  The slice has
  * round(width/dh) cells, made odd (*npts), of the handle's ϵᵣ; the periodic
  * 1-D operator A = ω²μ₀Tϵ + δxf δxb (TM) or ω²μ₀Tϵ + Tϵ δxf Tϵxinv δxb (TE)
@@ -186,7 +186,7 @@ int  fdfd_get_mode(fdfd_handle* h, double omega, const fdfd_mode* mode, int cap,
                    double* beta, double* vec, int* npts);
 
 /* Mode sources for nw frequencies (driven.jl:15-19 with setup_mode!,
- * device.jl:116-120): src (nw*Nx*Ny complex, host) is overwritten with, per
+ * device.jl:118-121): src (nw*Nx*Ny complex, host) is overwritten with, per
  * frequency, the sum over the nmodes modes of normalize(abs.(v)) on each
  * mode's slice.  All nw*nmodes mode problems run in one launch (a warp each).
  * Like the reference's solve loop, callers pass pol = FDFD_TM for sources. */
@@ -197,7 +197,7 @@ int  fdfd_mode_sources(fdfd_handle* h, int nw, const double* omegas, int nmodes,
  * f1, f2, f3 = (Ez, Hx, Hy) for FDFD_TM or (Hz, Ex, Ey) for FDFD_TE, Nx*Ny
  * complex each (host); Sx, Sy: Nx*Ny doubles.  TM: Sx = -½Re(avgx(Ez) Hy*),
  * Sy = ½Re(avgy(Ez) Hx*); TE: Sx = ½Re(Ey avgx(Hz)*), Sy = -½Re(Ex avgy(Hz)*),
- * avg the periodic grid_average (grid.jl:183-188).  The reference's TE branch
+ * avg the periodic grid_average (grid.jl:157-162).  The reference's TE branch
  * reads fields a FieldTE lacks (flux.jl:26-27); the averaged Hz is used. */
 int  fdfd_poynting(fdfd_handle* h, int pol, const double* f1, const double* f2,
                    const double* f3, double* Sx, double* Sy);
@@ -229,7 +229,7 @@ int  fdfd_flux_integral(fdfd_handle* h, int pol, const double* f1, const double*
  * every step.  Outputs Ez, Hx, Hy (driven recovery, may be NULL), the step
  * errors err_hist[0..*nerr-1] (err_hist[0] = 1 as the reference's history;
  * capacity maxit+1).  FDFD_ENOCONV when tol is not reached.  The reference's
- * Born step misplaces a parenthesis in its solve call (nonlinear.jl:99); its
+ * Born step misplaces a parenthesis in its solve call (nonlinear.jl:97); its
  * evident intent is implemented. */
 int  fdfd_chi3_solve(fdfd_handle* h, const double* chi, const double* src, int method,
                      double tol, int maxit, double* f1, double* f2, double* f3,
@@ -241,7 +241,7 @@ int  fdfd_chi3_solve(fdfd_handle* h, const double* chi, const double* src, int m
  *   Aₙ = Sxb δxb μ₀⁻¹ Sxf δxf + Syb δyb μ₀⁻¹ Syf δyf + ωₙ² ϵ₀ϵᵣ,  ωₙ = ω + nΩ,
  * n = -s..s, with the PML at ω (shared_pml != 0, the reference default) or at
  * ωₙ, coupled by ½ωₙ² ϵ₀ conj(Δϵᵣ) to sideband n+1 and ½ωₙ² ϵ₀ Δϵᵣ to n-1
- * (modulation.jl:91-99).  The coupled system is refined in FP64 (FGMRES) to
+ * (modulation.jl:93-101).  The coupled system is refined in FP64 (FGMRES) to
  * the handle's tol, preconditioned by the K sideband factorizations, which
  * are solved concurrently.  fdfd_set_eps, fdfd_set_refinement,
  * fdfd_set_restart, fdfd_set_fallback, fdfd_apply (nrhs 1, K*Nx*Ny values,
@@ -253,7 +253,7 @@ int  fdfd_mf_create(fdfd_handle** h, int Nx, int Ny, int Npx, int Npy, double dx
                     int nsidebands, int shared_pml, int precision);
 
 /* Modulation amplitude Δϵᵣ (ModulatedDevice.Δϵᵣ, setup_Δϵᵣ!,
- * modulation.jl:26-30), Nx*Ny complex; zero after fdfd_mf_create. */
+ * modulation.jl:7,28-32), Nx*Ny complex; zero after fdfd_mf_create. */
 int  fdfd_mf_set_deps(fdfd_handle* h, const double* deps_r);
 
 /* Assemble and factor the K sideband operators for carrier ω and modulation
@@ -261,7 +261,7 @@ int  fdfd_mf_set_deps(fdfd_handle* h, const double* deps_r);
 int  fdfd_mf_factor(fdfd_handle* h, double omega, double Omega);
 
 /* One source (Nx*Ny complex): b = iω·src in the centre sideband
- * (modulation.jl:62-64).  Outputs (each may be NULL) hold K*Nx*Ny complex
+ * (modulation.jl:67-69).  Outputs (each may be NULL) hold K*Nx*Ny complex
  * values, sideband n = -s..s in order: Ez and the forward-difference
  * H = (-Syf δyf Ez, Sxf δxf Ez)/(iωₙμ₀) (modulation.jl:108-114).  Stats:
  * iterations are applications of the block preconditioner. */

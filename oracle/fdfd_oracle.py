@@ -26,7 +26,7 @@ and there is no Manifest):
   * SparseArrays ``lu(A)\\b`` -> SuiteSparse UMFPACK (``src/solver/solver.jl:35``),
     MKL Pardiso ``COMPLEX_NONSYM`` (``solver.jl:19-32``): restated with
     ``scipy.sparse.linalg.splu`` (SuperLU), another FP64 sparse direct LU.
-  * Arpack.jl ``eigs(A, nev, sigma, which)`` (``src/solver/eigen.jl:335,353``):
+  * Arpack.jl ``eigs(A, nev, sigma, which)`` (``src/solver/eigen.jl:86,104``):
     restated with ``scipy.sparse.linalg.eigs`` (ARPACK-ng shift-invert).
 """
 from __future__ import annotations
@@ -57,7 +57,7 @@ def normalize_parameters(L0: float = DEFAULT_L0):
 
 @dataclass
 class Grid:
-    """2-D grid: src/grid.jl:33-39 (fields), :52-59 (constructor)."""
+    """2-D grid: src/grid.jl:7-13 (fields), :52-59 (constructor)."""
     N: tuple       # (Nx, Ny)
     Npml: tuple    # (Npx, Npy)
     bounds: tuple  # ((x1, y1), (x2, y2))
@@ -65,7 +65,7 @@ class Grid:
 
     @classmethod
     def from_ranges(cls, dh, Npml, xrange, yrange, L0=DEFAULT_L0):
-        """src/grid.jl:52-59: N = round(L/dh) (round-half-even, as Julia)."""
+        """src/grid.jl:26-33: N = round(L/dh) (round-half-even, as Julia)."""
         L = (float(xrange[1] - xrange[0]), float(yrange[1] - yrange[0]))
         N = (int(round(L[0] / dh)), int(round(L[1] / dh)))
         return cls(N, (int(Npml[0]), int(Npml[1])),
@@ -77,36 +77,36 @@ class Grid:
         return (self.bounds[1][0] - self.bounds[0][0],
                 self.bounds[1][1] - self.bounds[0][1])
 
-    def dx(self):  # src/grid.jl:94-96
+    def dx(self):  # src/grid.jl:68-70
         return (self.bounds[1][0] - self.bounds[0][0]) / self.N[0]
 
-    def dy(self):  # src/grid.jl:98-100
+    def dy(self):  # src/grid.jl:72-74
         return (self.bounds[1][1] - self.bounds[0][1]) / self.N[1]
 
-    def dh(self, w):  # src/grid.jl:89-92
+    def dh(self, w):  # src/grid.jl:63-66
         return self.dx() if w == X else self.dy()
 
-    def xc(self):  # src/grid.jl:102-104
+    def xc(self):  # src/grid.jl:76-78
         return self.bounds[0][0] + self.dx() * (np.arange(self.N[0]) + 0.5)
 
-    def yc(self):  # src/grid.jl:106-108
+    def yc(self):  # src/grid.jl:80-82
         return self.bounds[0][1] + self.dy() * (np.arange(self.N[1]) + 0.5)
 
     def x2ind(self, x):
-        """src/grid.jl:138-143, returned 0-based."""
+        """src/grid.jl:112-117, returned 0-based."""
         ind = int(round((x - self.bounds[0][0]) / self.L[0] * self.N[0]) + 1)
         ind = min(max(ind, 1), self.N[0])
         return ind - 1
 
     def y2ind(self, y):
-        """src/grid.jl:146-151, returned 0-based."""
+        """src/grid.jl:120-125, returned 0-based."""
         ind = int(round((y - self.bounds[0][1]) / self.L[1] * self.N[1]) + 1)
         ind = min(max(ind, 1), self.N[1])
         return ind - 1
 
 
 def vec(a: np.ndarray) -> np.ndarray:
-    """Julia ``a[:]``: column-major flatten, x fastest (driven.jl:170)."""
+    """Julia ``a[:]``: column-major flatten, x fastest (driven.jl:21)."""
     return np.asarray(a).reshape(-1, order="F")
 
 
@@ -115,7 +115,7 @@ def unvec(v: np.ndarray, shape) -> np.ndarray:
 
 
 def delta(w: int, s: int, g: Grid) -> sp.csr_matrix:
-    """Periodic first differences: src/grid.jl:154-180.
+    """Periodic first differences: src/grid.jl:128-154.
 
     x: kron(I_Ny, δx), y: kron(δy, I_Nx); forward has +1 on the super-diagonal
     and at (N,1); backward has -1 on the sub-diagonal and at (1,N).
@@ -137,7 +137,7 @@ def delta(w: int, s: int, g: Grid) -> sp.csr_matrix:
 
 
 def grid_average(center: np.ndarray, w: int) -> np.ndarray:
-    """src/grid.jl:183-188: (a + circshift(a, 1 along w))/2, periodic."""
+    """src/grid.jl:157-162: (a + circshift(a, 1 along w))/2, periodic."""
     if center.ndim == 1:
         return (center + np.roll(center, 1)) / 2
     if w == X:
@@ -195,17 +195,17 @@ def S_create(g: Grid, omega: float, m: float = 3.5, lnR: float = -12.0):
 
 
 def stretched_deltas(g: Grid, omega: float, m=3.5, lnR=-12.0):
-    """δxb, δxf, δyb, δyf with PML rows applied: src/solver/driven.jl:174-180."""
+    """δxb, δxf, δyb, δyf with PML rows applied: src/solver/driven.jl:25-31."""
     Sxf, Sxb, Syf, Syb = S_create(g, omega, m, lnR)
     return (Sxb @ delta(X, BACKWARD, g), Sxf @ delta(X, FORWARD, g),
             Syb @ delta(Y, BACKWARD, g), Syf @ delta(Y, FORWARD, g))
 
 
 def assemble(g: Grid, eps_r: np.ndarray, omega: float, pol: int, m=3.5, lnR=-12.0):
-    """Driven system matrix A (CSC): src/solver/driven.jl:170-194.
+    """Driven system matrix A (CSC): src/solver/driven.jl:21-45.
 
-    TM: A = δxf μ₀⁻¹ δxb + δyf μ₀⁻¹ δyb + ω² Tϵ               (driven.jl:184)
-    TE: A = δxf Tϵxi δxb + δyf Tϵyi δyb + ω² μ₀ I              (driven.jl:194;
+    TM: A = δxf μ₀⁻¹ δxb + δyf μ₀⁻¹ δyb + ω² Tϵ               (driven.jl:35)
+    TE: A = δxf Tϵxi δxb + δyf Tϵyi δyb + ω² μ₀ I              (driven.jl:45;
         the reference's ``speye`` is restated as a sparse identity)
     """
     eps0, mu0, _ = normalize_parameters(g.L0)
@@ -223,19 +223,19 @@ def assemble(g: Grid, eps_r: np.ndarray, omega: float, pol: int, m=3.5, lnR=-12.
 
 
 def dolinearsolve(A: sp.spmatrix, b: np.ndarray) -> np.ndarray:
-    """``lu(A)\\b``: src/solver/solver.jl:243 (SuperLU stands in for UMFPACK)."""
+    """``lu(A)\\b``: src/solver/solver.jl:35 (SuperLU stands in for UMFPACK)."""
     lu = spla.splu(sp.csc_matrix(A))
     return lu.solve(np.asarray(b, dtype=np.complex128))
 
 
 def solve(g: Grid, eps_r, src, omega: float, pol: int = TM, m=3.5, lnR=-12.0,
           return_system=False):
-    """Driven solve for one frequency: src/solver/driven.jl:153-208.
+    """Driven solve for one frequency: src/solver/driven.jl:4-59.
 
     ``src`` is the current array J (Nx x Ny); the right-hand side is
-    b = iω·src (driven.jl:185,195).  Returns (f1, f2, f3) as Nx x Ny arrays:
-    TM -> (Ez, Hx, Hy) with backward-difference H recovery (driven.jl:189-190);
-    TE -> (Hz, Ex, Ey) (driven.jl:199-200).
+    b = iω·src (driven.jl:36,46).  Returns (f1, f2, f3) as Nx x Ny arrays:
+    TM -> (Ez, Hx, Hy) with backward-difference H recovery (driven.jl:40-41);
+    TE -> (Hz, Ex, Ey) (driven.jl:50-51).
     """
     eps0, mu0, _ = normalize_parameters(g.L0)
     eps_r = np.asarray(eps_r, dtype=np.complex128)
@@ -249,7 +249,7 @@ def solve(g: Grid, eps_r, src, omega: float, pol: int = TM, m=3.5, lnR=-12.0,
 
 
 def recover_driven(g: Grid, eps_r, omega, x, pol, m=3.5, lnR=-12.0):
-    """H (TM) or E (TE) recovery of the driven solve: src/solver/driven.jl:189-200."""
+    """H (TM) or E (TE) recovery of the driven solve: src/solver/driven.jl:40-51."""
     eps0, mu0, _ = normalize_parameters(g.L0)
     dxb, dxf, dyb, dyf = stretched_deltas(g, omega, m, lnR)
     shp = g.N
@@ -266,10 +266,10 @@ def recover_driven(g: Grid, eps_r, omega, x, pol, m=3.5, lnR=-12.0):
 
 
 def eigen_operator(g: Grid, eps_r, omega0: float, pol: int, m=3.5, lnR=-12.0):
-    """Eigen-operator A and shift σ: src/solver/eigen.jl:318-353.
+    """Eigen-operator A and shift σ: src/solver/eigen.jl:69-104.
 
-    TM: A = Tϵᵣ⁻¹ δxf δxb + Tϵᵣ⁻¹ δyf δyb, σ = -ω₀² μ₀ ϵ₀   (eigen.jl:332-335)
-    TE: A = δxf Tϵx⁻¹ δxb + δyf Tϵy⁻¹ δyb, σ = -ω₀² μ₀      (eigen.jl:349-353)
+    TM: A = Tϵᵣ⁻¹ δxf δxb + Tϵᵣ⁻¹ δyf δyb, σ = -ω₀² μ₀ ϵ₀   (eigen.jl:83-86)
+    TE: A = δxf Tϵx⁻¹ δxb + δyf Tϵy⁻¹ δyb, σ = -ω₀² μ₀      (eigen.jl:100-104)
     """
     eps0, mu0, _ = normalize_parameters(g.L0)
     eps_r = np.asarray(eps_r, dtype=np.complex128)
@@ -288,11 +288,11 @@ def eigen_operator(g: Grid, eps_r, omega0: float, pol: int, m=3.5, lnR=-12.0):
 
 def eigenfrequency(g: Grid, eps_r, omega0: float, pol: int, nev: int, which="LM",
                    m=3.5, lnR=-12.0, tol=0.0, v0=None):
-    """Shift-invert eigenfrequencies and fields: src/solver/eigen.jl:318-364.
+    """Shift-invert eigenfrequencies and fields: src/solver/eigen.jl:69-115.
 
-    Returns (omega, fields) with omega = sqrt(-λ/(μ₀ϵ₀)) for TM (eigen.jl:336)
-    or sqrt(-λ/μ₀) for TE (eigen.jl:354); fields use FORWARD differences for
-    TM H recovery (eigen.jl:339-340) and Tϵx⁻¹/Tϵy⁻¹ for TE (eigen.jl:357-358).
+    Returns (omega, fields) with omega = sqrt(-λ/(μ₀ϵ₀)) for TM (eigen.jl:87)
+    or sqrt(-λ/μ₀) for TE (eigen.jl:105); fields use FORWARD differences for
+    TM H recovery (eigen.jl:90-91) and Tϵx⁻¹/Tϵy⁻¹ for TE (eigen.jl:108-109).
     """
     eps0, mu0, _ = normalize_parameters(g.L0)
     eps_r = np.asarray(eps_r, dtype=np.complex128)
@@ -354,14 +354,14 @@ def objective(g: Grid, eps_r, src, omega, mvec, m=3.5, lnR=-12.0):
     return abs(vec(mvec).astype(np.complex128) @ E) ** 2
 
 
-# --- mode sources: src/device.jl:111-149, src/solver/eigen.jl:6-29 ----------
+# --- mode sources: src/device.jl:112-149, src/solver/eigen.jl:6-29 ----------
 
 def eigenmode_1d(eps_slice, dh: float, omega: float, pol: int, neff, nev: int = 1, L0: float = DEFAULT_L0,
                  dense=False):
     """eigenmode(d::AbstractDevice{1}, pol, neff, nev): src/solver/eigen.jl:6-29.
 
     1-D periodic grid of len(eps_slice) cells of size dh, no PML (the
-    ``Grid(N, xrange)`` constructor, grid.jl:51-59).  TM: A = ω²μ₀Tϵ + δxf δxb;
+    ``Grid(N, xrange)`` constructor, grid.jl:53-59).  TM: A = ω²μ₀Tϵ + δxf δxb;
     TE: A = ω²μ₀Tϵ + Tϵ δxf Tϵxinv δxb.  ARPACK's shift-invert eigs(A, nev,
     sigma=(ω n_eff/c₀)²) (scipy's ARPACK-ng here; ``dense`` picks the nearest
     eigenvalues of a dense eig instead).  Returns (β = √λ, vectors (n, nev))."""
@@ -388,7 +388,7 @@ def eigenmode_1d(eps_slice, dh: float, omega: float, pol: int, neff, nev: int = 
 
 
 def mode_slice(g: Grid, ix: int, iy: int, normal: int, width: float):
-    """Slice indices of get_modes (device.jl:125-143), 0-based: srcpoints =
+    """Slice indices of get_modes (device.jl:125-142), 0-based: srcpoints =
     round(width/dh) made odd, M = (srcpoints-1)/2 cells each side of (ix, iy)."""
     dh = g.dy() if normal == X else g.dx()
     pts = int(round(width / dh))
@@ -402,7 +402,7 @@ def mode_slice(g: Grid, ix: int, iy: int, normal: int, width: float):
 
 def get_modes(g: Grid, eps_r, pol: int, omega: float, neff, nmodes: int, ix: int, iy: int, normal: int,
               width: float, dense=False):
-    """get_modes(d, pol, ω, neff, nmodes, pt, slicenormal, slicewidth): src/device.jl:122-149
+    """get_modes(d, pol, ω, neff, nmodes, pt, slicenormal, slicewidth): src/device.jl:124-149
     with (ix, iy) = coord2ind(grid, pt) - 1.  Returns (β, vectors, indx, indy)."""
     indx, indy, dh = mode_slice(g, ix, iy, normal, width)
     e = np.asarray(eps_r)[indx, indy]
@@ -411,7 +411,7 @@ def get_modes(g: Grid, eps_r, pol: int, omega: float, neff, nmodes: int, ix: int
 
 
 def setup_mode(src, g: Grid, eps_r, pol: int, omega: float, neff, ix: int, iy: int, normal: int, width: float):
-    """setup_mode!(d, pol, ω, neff, pt, srcnormal, srcwidth): src/device.jl:116-120,
+    """setup_mode!(d, pol, ω, neff, pt, srcnormal, srcwidth): src/device.jl:118-121,
     src[indx, indy] += normalize(abs.(vector[:])) (in place)."""
     _, vecs, indx, indy = get_modes(g, eps_r, pol, omega, neff, 1, ix, iy, normal, width)
     a = np.abs(vecs[:, 0])
@@ -422,13 +422,13 @@ def setup_mode(src, g: Grid, eps_r, pol: int, omega: float, neff, ix: int, iy: i
 # --- χ³ nonlinear driven solve: src/solver/nonlinear.jl --------------------------
 
 def chi3_coeff(g: Grid, chi, omega: float):
-    """coeff = ω²ϵ₀·3χ/L₀ with ϵ₀ normalised (nonlinear.jl:74)."""
+    """coeff = ω²ϵ₀·3χ/L₀ with ϵ₀ normalised (nonlinear.jl:71)."""
     eps0, _, _ = normalize_parameters(g.L0)
     return omega ** 2 * eps0 * 3 * vec(np.asarray(chi, dtype=np.float64)) / g.L0
 
 
 def born(A, b, coeff, ez, tol=1e-12, maxiterations=50):
-    """_doborn (nonlinear.jl:94-108): ez ← (A + diag(coeff·|ez|²))⁻¹ b until
+    """_doborn (nonlinear.jl:92-106): ez ← (A + diag(coeff·|ez|²))⁻¹ b until
     ||ez_new − ez||/||ez|| ≤ tol.  The reference misplaces a parenthesis in
     the solve call (``sparse(Diagonal(...), b, CNSym)``); the evident intent,
     dolinearsolve(A + Diagonal(coeff.*ez.*conj.(ez)), b), is restated."""
@@ -443,7 +443,7 @@ def born(A, b, coeff, ez, tol=1e-12, maxiterations=50):
 
 
 def newton(A, b, coeff, ez, tol=1e-12, maxiterations=50):
-    """_donewton (nonlinear.jl:110-129): Newton on the stacked unknown [ez; conj(ez)]
+    """_donewton (nonlinear.jl:108-129): Newton on the stacked unknown [ez; conj(ez)]
     with F = (A + diag(coeff|ez|²))ez − b, J = [J1 J2; conj(J2) conj(J1)],
     J1 = A + diag(2coeff|ez|²), J2 = diag(coeff ez²); err = ||δ||/||[ez; conj ez]||."""
     M = ez.size
@@ -466,7 +466,7 @@ def newton(A, b, coeff, ez, tol=1e-12, maxiterations=50):
 
 def solve_chi3(g: Grid, eps_r, chi, src, omega: float, method: str, m=3.5, lnR=-12.0, tol=1e-12,
                maxiterations=50):
-    """solve(d::χ3Device, which_method): src/solver/nonlinear.jl:36-91 (TM): the
+    """solve(d::χ3Device, which_method): src/solver/nonlinear.jl:36-90 (TM): the
     linear solve, then Born (``"born"``) or Gauss-Newton (``"newton"``), then
     the driven H recovery.  Returns ((Ez, Hx, Hy), err history)."""
     A = assemble(g, eps_r, omega, TM, m, lnR)
@@ -528,10 +528,10 @@ def modulated_system(g: Grid, eps_r, deps_r, omega: float, Omega: float, nsideba
     """Coupled sideband system of ``solve(d::ModulatedDevice)``:
     src/solver/modulation.jl:35-119 (TM only, as the reference).
 
-    Frequencies ωₙ = ω + nΩ, n = -s..s (:44-50).  Per sideband
+    Frequencies ωₙ = ω + nΩ, n = -s..s (:41,49).  Per sideband
     Aₙ = Sxb δxb μ₀⁻¹ Sxf δxf + Syb δyb μ₀⁻¹ Syf δyf + ωₙ² Tϵ with the PML at ω
-    (shared, :77-83) or at ωₙ (:85-89).  Couplings: block (n, n+1) =
-    ½ωₙ² conj(TΔϵ), block (n+1, n) = ½ωₙ₊₁² TΔϵ (:91-99).  Returns
+    (shared, :79-85) or at ωₙ (:86-91).  Couplings: block (n, n+1) =
+    ½ωₙ² conj(TΔϵ), block (n+1, n) = ½ωₙ₊₁² TΔϵ (:93-101).  Returns
     (A, omegas, S) with S = [(Sxf, Syf)] per sideband (one entry when shared)."""
     eps0, mu0, _ = normalize_parameters(g.L0)
     K = 2 * nsidebands + 1
@@ -559,9 +559,9 @@ def solve_modulated(g: Grid, eps_r, deps_r, src, omega: float, Omega: float, nsi
                     sharedpml=True, m=3.5, lnR=-12.0):
     """``solve(d::ModulatedDevice)`` for one ω: src/solver/modulation.jl:35-119.
 
-    b = iω·src in the centre sideband block (:62-64); Ez per sideband and
+    b = iω·src in the centre sideband block (:67-69); Ez per sideband and
     H with forward differences, hx = -Syf δyf ez/(iωₙμ₀), hy = Sxf δxf ez/(iωₙμ₀)
-    (:108-114).  Returns a list of K (Ez, Hx, Hy) triples, n = -s..s."""
+    (:110-114).  Returns a list of K (Ez, Hx, Hy) triples, n = -s..s."""
     eps0, mu0, _ = normalize_parameters(g.L0)
     A, wn, S = modulated_system(g, eps_r, deps_r, omega, Omega, nsidebands, sharedpml, m, lnR)
     N = g.N[0] * g.N[1]

@@ -1,5 +1,5 @@
 """GPU parity of the guided-mode solver and the mode sources
-(get_modes / setup_mode!, src/device.jl:111-149; eigenmode, src/solver/eigen.jl:6-29)
+(get_modes / setup_mode!, src/device.jl:112-149; eigenmode, src/solver/eigen.jl:6-29)
 through the C ABI against the FP64 oracle."""
 import numpy as np
 import pytest
@@ -74,7 +74,7 @@ def test_mode_sources_match_oracle(lib, fdfd, oracle):
 
 
 def test_solve_with_mode_source(lib, fdfd, oracle):
-    """The reference's waveguide test setup (test/runtests.jl:24-39): a guide
+    """The reference's waveguide test setup (test/runtests.jl:23-38): a guide
     (ϵᵣ = 12, 0.3 µm wide) driven by a TM mode source at x = 1 µm, solved
     through the host mirror's solve() against the oracle."""
     g = fdfd.Grid(0.02, (15, 15), (0.0, 10.0), (-1.0, 1.0))

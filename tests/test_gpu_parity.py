@@ -306,7 +306,7 @@ def test_eigfreq_golden(lib, fdfd, prec):
     om, lam, f, st = h.eigfreq(float(g["omega0"]), nev)
     assert match_eigs(om, g["omega"]) <= 1e-8
     # eigenvectors: (A - σI) y = (λ - σ) y with the assembled shifted operator
-    sigma = -float(g["omega0"]) ** 2 * (fdfd.MU0 * 1e-6) * (fdfd.EPS0 * 1e-6)   # eigen.jl:335
+    sigma = -float(g["omega0"]) ** 2 * (fdfd.MU0 * 1e-6) * (fdfd.EPS0 * 1e-6)   # eigen.jl:86
     ay = h.apply(f[:, 0])
     for q in range(nev):
         r = ay[q] - (lam[q] - sigma) * f[q, 0]

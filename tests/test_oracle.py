@@ -27,7 +27,7 @@ def test_constants(oracle):
 
 
 def test_grid_round_half_even(oracle):
-    # src/grid.jl:54: N = round(L/dh), Julia rounds half to even
+    # src/grid.jl:28: N = round(L/dh), Julia rounds half to even
     g = oracle.Grid.from_ranges(1.0, [0, 0], [0.0, 2.5], [0.0, 3.5])
     assert g.N == (2, 4)
     assert np.allclose(g.xc(), [0.625, 1.875])
@@ -62,7 +62,7 @@ def test_sfactor_hand_values(oracle):
     g = oracle.Grid((10, 10), (3, 3), ((0.0, 0.0), (1.0, 1.0)))
     w = 2e15
     eps0 = oracle.EPS0 * 1e-6
-    T = 3 * 0.1   # Npml * dw, as pml.jl:192 computes it
+    T = 3 * 0.1   # Npml * dw, as pml.jl:4 computes it
     smax = -(3.5 + 1) * (-12) / (2 * oracle.ETA0 * T)
     S = lambda l: 1 - 1j * smax * (l / T) ** 3.5 / (w * eps0)
     f = oracle.create_sfactor(oracle.X, oracle.FORWARD, g, w)
@@ -106,7 +106,7 @@ def test_solver_agreement(oracle, pol):
 def test_dipole_matches_greens_function(oracle):
     """Known answer: a point current 1im in free space radiates
     Ez = -(i/4)·ω·μ₀·dx·dy·H0⁽²⁾(k r) (outgoing under the e^{+iωt} convention
-    implied by the PML stretch s = 1 - iσ/(ωϵ₀), pml.jl:198)."""
+    implied by the PML stretch s = 1 - iσ/(ωϵ₀), pml.jl:10)."""
     dx = 0.025
     N = 240
     g = oracle.Grid((N, N), (20, 20), ((-N * dx / 2, -N * dx / 2), (N * dx / 2, N * dx / 2)))
@@ -161,7 +161,7 @@ def test_adjoint_gradient_matches_fd(oracle):
 # modulated device (src/solver/modulation.jl)
 # ---------------------------------------------------------------------------
 def test_modulated_blocks(oracle):
-    """Block structure of the coupled sideband matrix (modulation.jl:77-99):
+    """Block structure of the coupled sideband matrix (modulation.jl:79-101):
     diagonal blocks differ only by (ωₙ² - ω₀²)Tϵ under a shared PML, block
     (n, n+1) is ½ωₙ² conj(TΔϵ), block (n+1, n) is ½ωₙ₊₁² TΔϵ."""
     g = small_grid(oracle, N=(6, 5), npml=(1, 1), d=(0.1, 0.2))
@@ -186,7 +186,7 @@ def test_modulated_blocks(oracle):
 
 
 def test_sideband_operator_entries(oracle):
-    """Row of Sxb δxb μ₀⁻¹ Sxf δxf (modulation.jl:80): x-neighbour entries
+    """Row of Sxb δxb μ₀⁻¹ Sxf δxf (modulation.jl:82): x-neighbour entries
     sxb_i sxf_i/(dx²μ₀) (i+1) and sxb_i sxf_{i-1}/(dx²μ₀) (i-1), diagonal minus
     their sum, with 1/s factors of S_create."""
     g = small_grid(oracle, N=(6, 5), npml=(2, 1), d=(0.1, 0.2))
@@ -243,7 +243,7 @@ def test_modulated_golden_regression(oracle):
 
 
 # ---------------------------------------------------------------------------
-# mode sources (src/device.jl:111-149, src/solver/eigen.jl:6-29)
+# mode sources (src/device.jl:112-149, src/solver/eigen.jl:6-29)
 # ---------------------------------------------------------------------------
 @pytest.mark.parametrize("pol", [1, 2])
 def test_eigenmode_arpack_matches_dense(oracle, pol):
