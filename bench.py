@@ -46,6 +46,7 @@ def args():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the adjoint / eigenfrequency / frequency-sweep measurements")
+    ap.add_argument("--seed", type=int, default=2, help="seed of the random design region (2: the benchmark's)")
     ap.add_argument("--size", default=None,
                     help="NXxNY: same problem family at another size (profiling runs); design region = "
                          "a quarter of the smaller side squared")
@@ -449,14 +450,14 @@ def main():
     pkg = G.load_package()
     from fdfd_gb300 import workloads as W
     L = pkg._lib
-    workload = WORKLOAD
+    workload = WORKLOAD.replace("(seed 2)", f"(seed {a.seed})")
     if a.size:
         nx, ny = (int(v) for v in a.size.lower().split("x"))
         dsz = min(nx, ny) // 4
-        p = W.design_guide(nx, ny, design=(dsz, dsz))
-        workload = f"design_guide {nx}x{ny} (profiling size), {dsz}x{dsz} design"
+        p = W.design_guide(nx, ny, design=(dsz, dsz), seed=a.seed)
+        workload = f"design_guide {nx}x{ny} (profiling size), {dsz}x{dsz} design (seed {a.seed})"
     else:
-        p = W.design_guide()
+        p = W.design_guide(seed=a.seed)
     N = p.Nx * p.Ny
 
     def make(prec):
