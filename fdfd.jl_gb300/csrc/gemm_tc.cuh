@@ -10,7 +10,7 @@ struct TcMaps {
     CUtensorMap map[5][3];
 };
 
-// Encodes the three descriptors of one pool; false if the driver refuses.
+// Encodes the three descriptors of one pool; false if cuTensorMapEncodeTiled rejects one.
 bool tc_make_map(const Pool<float>& P, CUtensorMap* box128, CUtensorMap* box256, CUtensorMap* box64);
 
 // Encodes the descriptors of the five pools; false if any is refused (the
