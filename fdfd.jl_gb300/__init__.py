@@ -26,7 +26,7 @@ from ._lib import FDFDError, FDFD_PREC_FP64, FDFD_PREC_MIXED  # noqa: F401
 
 __all__ = ["EPS0", "MU0", "C0", "ETA0", "TM", "TE", "X", "Y", "Grid", "Device", "ModulatedDevice", "Point", "Mode",
            "setup_eps", "setup_src", "setup_deps", "add_mode", "setup_mode", "get_modes", "solve", "eigenfrequency",
-           "FieldTM", "FieldTE", "Flux", "poynting", "flux_surface_integral", "Chi3Device", "setup_chi",
+           "FieldTM", "FieldTE", "Flux", "probe_field", "poynting", "flux_surface_integral", "Chi3Device", "setup_chi",
            "IterativeMethodGN", "IterativeMethodB", "normalize_parameters", "FDFDError"]
 
 # src/types.jl:6-9
@@ -302,6 +302,23 @@ def _field_handle(field):
 
 def _pol_of(field):
     return TM if isinstance(field, FieldTM) else TE
+
+
+def probe_field(field, component: str, pt: Point):
+    """probe_field(field, component, pt): src/flux.jl:6-12.  The value of
+    `component` ("Ez", "Hx", "Hy" for TM; "Hz", "Ex", "Ey" for TE) in the cell
+    whose centre lies within half a cell of pt on each axis, as AxisArrays'
+    atvalue(…, atol = dh/2) selects it; the first such cell on a tie."""
+    g = field.grid
+    ix = np.nonzero(np.abs(g.xc() - pt.x) <= g.dx() / 2)[0]
+    iy = np.nonzero(np.abs(g.yc() - pt.y) <= g.dy() / 2)[0]
+    if ix.size == 0 or iy.size == 0:
+        raise FDFDError(_lib.FDFD_EINVAL, f"no grid cell centre within half a cell of ({pt.x}, {pt.y})")
+    if component not in field.components:
+        raise FDFDError(_lib.FDFD_EINVAL, "%s is invalid for the %s polarization. Valid options are %s" %
+                        (component, "TM" if isinstance(field, FieldTM) else "TE",
+                         ", ".join(":" + c for c in field.components)))
+    return complex(field[component][ix[0], iy[0]])
 
 
 def poynting(field):
