@@ -26,7 +26,7 @@ from ._lib import FDFDError, FDFD_PREC_FP64, FDFD_PREC_MIXED  # noqa: F401
 
 __all__ = ["EPS0", "MU0", "C0", "ETA0", "TM", "TE", "X", "Y", "Grid", "Device", "ModulatedDevice", "Point", "Mode",
            "setup_eps", "setup_src", "setup_deps", "add_mode", "setup_mode", "get_modes", "solve", "eigenfrequency",
-           "FieldTM", "FieldTE", "Flux", "probe_field", "poynting", "flux_surface_integral", "Chi3Device", "setup_chi",
+           "FieldTM", "FieldTE", "Flux", "probe_field", "poynting", "flux_surface_integral", "unwrap", "Chi3Device", "setup_chi",
            "IterativeMethodGN", "IterativeMethodB", "normalize_parameters", "FDFDError"]
 
 # src/types.jl:6-9
@@ -84,11 +84,28 @@ class Grid:
     def yc(self):  # src/grid.jl:80-82
         return self.bounds[0][1] + self.dy() * (np.arange(self.N[1]) + 0.5)
 
+    def dh(self, w):  # src/grid.jl:63-66
+        return self.dx() if w == X else self.dy()
+
+    def xe(self):  # src/grid.jl:89-91: the N+1 cell edges along x
+        return self.bounds[0][0] + self.dx() * np.arange(self.N[0] + 1)
+
+    def ye(self):  # src/grid.jl:93-95
+        return self.bounds[0][1] + self.dy() * np.arange(self.N[1] + 1)
+
+    def x2ind(self, x):
+        """0-based index of the cell nearest x, clamped to the grid (src/grid.jl:112-117;
+        Julia's round and Python's both round half to even)."""
+        i = int(round((x - self.bounds[0][0]) / self.L[0] * self.N[0]) + 1)
+        return min(max(i, 1), self.N[0]) - 1
+
+    def y2ind(self, y):  # src/grid.jl:120-125, 0-based
+        i = int(round((y - self.bounds[0][1]) / self.L[1] * self.N[1]) + 1)
+        return min(max(i, 1), self.N[1]) - 1
+
     def coord2ind(self, pt: Point):
         """0-based (ix, iy), src/grid.jl:103-125."""
-        ix = int(round((pt.x - self.bounds[0][0]) / self.L[0] * self.N[0]) + 1)
-        iy = int(round((pt.y - self.bounds[0][1]) / self.L[1] * self.N[1]) + 1)
-        return min(max(ix, 1), self.N[0]) - 1, min(max(iy, 1), self.N[1]) - 1
+        return self.x2ind(pt.x), self.y2ind(pt.y)
 
 
 @dataclass
@@ -185,13 +202,22 @@ def setup_eps(d: Device, region, value):
 
 def setup_src(d: Device, where, value=None):
     """setup_src!(d, pt) puts 1im at the point (src/device.jl:95-98);
+    setup_src!(d, pt, srcnormal) puts 1im on the whole grid line through the
+    point normal to srcnormal, X or Y (device.jl:101-108);
     setup_src!(d, region, value) fills a region (device.jl:92)."""
     if isinstance(where, Point):
         ix, iy = d.grid.coord2ind(where)
-        d.src[ix, iy] = 1j
+        if value is None:
+            d.src[ix, iy] = 1j
+        elif value == X:
+            d.src[ix, :] = 1j
+        elif value == Y:
+            d.src[:, iy] = 1j
+        else:
+            raise FDFDError(_lib.FDFD_EINVAL, "srcnormal must be X or Y")
         return
-    m, X, Y = _mask(d, where)
-    d.src[m] = np.vectorize(value)(X, Y)[m] if callable(value) else value
+    m, xs, ys = _mask(d, where)
+    d.src[m] = np.vectorize(value)(xs, ys)[m] if callable(value) else value
 
 
 def setup_deps(d: ModulatedDevice, region, value):
@@ -302,6 +328,22 @@ def _field_handle(field):
 
 def _pol_of(field):
     return TM if isinstance(field, FieldTM) else TE
+
+
+def unwrap(v, inplace=False):
+    """unwrap(v, inplace=false): src/FDFD.jl:19-31.  Phase unwrapping in the
+    reference's order: each entry is shifted by 2π while it differs from the
+    already unwrapped previous entry by ≥ π (then ≤ -π).  Non-finite entries are
+    left as they are (the reference's loops would not end on ±Inf)."""
+    u = v if inplace else np.array(v, dtype=np.float64, copy=True)
+    for i in range(1, len(u)):
+        if not (math.isfinite(u[i]) and math.isfinite(u[i - 1])):
+            continue
+        while u[i] - u[i - 1] >= math.pi:
+            u[i] -= 2 * math.pi
+        while u[i] - u[i - 1] <= -math.pi:
+            u[i] += 2 * math.pi
+    return u
 
 
 def probe_field(field, component: str, pt: Point):

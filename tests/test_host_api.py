@@ -34,3 +34,38 @@ def test_grid_and_indices_follow_the_reference(fdfd):
     assert np.isclose(g.xc()[0], -5.0 + 0.025) and np.isclose(g.yc()[-1], 3.0 - 0.025)
     assert g.coord2ind(fdfd.Point(-3.0, 0.0)) == (40, 60)
     assert g.coord2ind(fdfd.Point(-99.0, 99.0)) == (0, 119)
+
+
+def test_grid_edges_and_axis_indices(fdfd):
+    """dh, xe/ye (src/grid.jl:63-66, 89-95) and x2ind/y2ind (:112-125)."""
+    g = fdfd.Grid(0.1, (2, 2), (-1.0, 1.0), (0.0, 1.5))
+    assert g.dh(fdfd.X) == g.dx() and g.dh(fdfd.Y) == g.dy()
+    assert len(g.xe()) == g.N[0] + 1 and np.isclose(g.xe()[-1], 1.0)
+    assert len(g.ye()) == g.N[1] + 1 and np.isclose(g.ye()[0], 0.0)
+    assert g.x2ind(-1.0) == 0 and g.x2ind(0.0) == 10 and g.x2ind(7.0) == g.N[0] - 1
+    assert g.y2ind(0.26) == 3 and g.y2ind(-3.0) == 0
+
+
+def test_line_source(fdfd):
+    """setup_src!(d, pt, srcnormal) (src/device.jl:101-108): 1im on the grid line normal to srcnormal."""
+    g = fdfd.Grid(0.1, (2, 2), (-1.0, 1.0), (0.0, 1.5))
+    d = fdfd.Device(g, 1e15)
+    fdfd.setup_src(d, fdfd.Point(-0.5, 0.7), fdfd.X)
+    ix, iy = g.coord2ind(fdfd.Point(-0.5, 0.7))
+    assert np.all(d.src[ix, :] == 1j) and np.count_nonzero(d.src) == g.N[1]
+    d2 = fdfd.Device(g, 1e15)
+    fdfd.setup_src(d2, fdfd.Point(-0.5, 0.7), fdfd.Y)
+    assert np.all(d2.src[:, iy] == 1j) and np.count_nonzero(d2.src) == g.N[0]
+
+
+def test_unwrap_follows_the_reference_loop(fdfd):
+    """unwrap (src/FDFD.jl:19-31): shifts by 2π against the already unwrapped previous entry."""
+    import math
+    v = np.array([0.0, 3.0, -3.0, 0.5, 3.1416, -3.1416])
+    u = fdfd.unwrap(v)
+    assert np.all(v == np.array([0.0, 3.0, -3.0, 0.5, 3.1416, -3.1416]))   # not in place
+    # 0.5 - 3.28 > -π: no shift at index 3, as the reference's loop decides it
+    assert np.allclose(u, [0.0, 3.0, -3.0 + 2 * math.pi, 0.5, 3.1416, -3.1416 + 2 * math.pi])
+    assert np.all(np.abs(np.diff(u)) < math.pi)
+    w = v.copy()
+    assert fdfd.unwrap(w, True) is w and np.allclose(w, u)
