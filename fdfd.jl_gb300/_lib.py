@@ -196,6 +196,13 @@ class Handle:
         except Exception:
             pass
 
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+        return False
+
     def set_refinement(self, tol=1e-10, max_iter=40, mode=FDFD_REFINE_GMRES):
         self._check(self.lib.fdfd_set_refinement(self.h, float(tol), int(max_iter), int(mode)))
 

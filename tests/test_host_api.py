@@ -69,3 +69,16 @@ def test_unwrap_follows_the_reference_loop(fdfd):
     assert np.all(np.abs(np.diff(u)) < math.pi)
     w = v.copy()
     assert fdfd.unwrap(w, True) is w and np.allclose(w, u)
+
+
+def test_handle_is_a_context_manager(fdfd):
+    """`with Handle(...)` releases the library handle on exit (a closed handle is a NULL pointer)."""
+    H = fdfd._lib.Handle
+    assert hasattr(H, "__enter__") and hasattr(H, "__exit__")
+    h = H.__new__(H)               # no GPU here: exercise the protocol on an unopened handle
+    import ctypes
+    h.h = ctypes.c_void_p()
+    h.lib = None
+    with h as same:
+        assert same is h
+    assert not h.h
