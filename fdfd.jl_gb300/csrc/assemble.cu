@@ -539,7 +539,7 @@ __global__ void vcombine_kernel(long long N, int nvec, const cplx<double>* __res
                     : vcombine_elem<false>(V, vstride, cr, nvec, o, y[o]);
 }
 
-// part[rhs][block][j] = Σ_k conj(V_j[rhs][k]) * w[rhs][k]  for j < nvec (≤ 64)
+// part[rhs][block][j] = Σ_k conj(V_j[rhs][k]) * w[rhs][k]  for j < nvec (eight vectors per pass)
 __global__ void vdots_kernel(long long N, int nvec, const cplx<double>* __restrict__ V, long long vstride,
                              const cplx<double>* __restrict__ w, double* __restrict__ part) {
     int rhs = blockIdx.y;
