@@ -57,7 +57,7 @@ def normalize_parameters(L0: float = DEFAULT_L0):
 
 @dataclass
 class Grid:
-    """2-D grid: src/grid.jl:7-13 (fields), :52-59 (constructor)."""
+    """2-D grid: src/grid.jl:7-13 (fields), :26-33 (constructor)."""
     N: tuple       # (Nx, Ny)
     Npml: tuple    # (Npx, Npy)
     bounds: tuple  # ((x1, y1), (x2, y2))

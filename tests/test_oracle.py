@@ -242,6 +242,24 @@ def test_modulated_golden_regression(oracle):
     assert np.linalg.norm(ez - g["ez"]) <= 1e-12 * np.linalg.norm(g["ez"])
 
 
+@pytest.mark.parametrize("pol", [1, 2])
+def test_eigenfrequency_discrete_dispersion(oracle, pol):
+    """eigenfrequency (src/solver/eigen.jl:69-115) on a periodic grid without PML and with
+    uniform ϵᵣ: the 5-point operator's eigenvalues are known in closed form,
+    k² = (2/dx·sin(πm/Nx))² + (2/dy·sin(πn/Ny))², ω = c₀k/(L₀√ϵᵣ), for TM (ω = √(-λ/μ₀ϵ₀))
+    and TE (ω = √(-λ/μ₀)) alike.  The four modes nearest ω₀ must be on that set."""
+    Nx, Ny, dh, er = 24, 18, 0.05, 2.25
+    g = oracle.Grid((Nx, Ny), (0, 0), ((0.0, 0.0), (Nx * dh, Ny * dh)))
+    _, _, c0n = oracle.normalize_parameters(g.L0)
+    m, n = np.arange(Nx)[:, None], np.arange(Ny)[None, :]
+    k2 = (2 / dh * np.sin(np.pi * m / Nx)) ** 2 + (2 / dh * np.sin(np.pi * n / Ny)) ** 2
+    w_an = np.sort(np.sqrt(k2.ravel()) * c0n / np.sqrt(er))
+    w, _, _ = oracle.eigenfrequency(g, np.full((Nx, Ny), er, dtype=complex), 1.02 * w_an[5], pol, 4)
+    for x in w:
+        assert np.min(np.abs(w_an - x)) <= 1e-12 * abs(x)
+    assert np.allclose(w, w_an[5], rtol=1e-12)   # the (±m, ±n) mode nearest ω₀ is four-fold
+
+
 # ---------------------------------------------------------------------------
 # mode sources (src/device.jl:112-149, src/solver/eigen.jl:6-29)
 # ---------------------------------------------------------------------------
