@@ -103,6 +103,33 @@ def test_solver_agreement(oracle, pol):
     assert np.linalg.norm(x1 - x2) <= 1e-12 * np.linalg.norm(x2)
 
 
+@pytest.mark.parametrize("pol", [1, 2])
+def test_driven_plane_wave_closed_form(oracle, pol):
+    """Driven solve (src/solver/driven.jl:4-59) without PML, uniform ϵᵣ, source e^{i(θx·i + θy·j)}:
+    the operator is diagonal in that discrete Fourier mode, so
+      TM: Ez = iω·src / (-k²/μ₀ + ω²ϵ₀ϵᵣ),  Hx = -δyb Ez/(iωμ₀),  Hy = δxb Ez/(iωμ₀)   (:35-41)
+      TE: Hz = iω·src / (-k²/(ϵ₀ϵᵣ) + ω²μ₀), Ex = Tϵyi δyb Hz/(iω), Ey = -Tϵxi δxb Hz/(iω)   (:45-51)
+    with k² = (2/dx·sin(θx/2))² + (2/dy·sin(θy/2))² and δb e^{iθj} = e^{iθj}(1 - e^{-iθ})/dh."""
+    Nx, Ny, dx, dy, er = 20, 16, 0.05, 0.04, 2.25
+    g = oracle.Grid((Nx, Ny), (0, 0), ((0.0, 0.0), (Nx * dx, Ny * dy)))
+    eps0, mu0, _ = oracle.normalize_parameters(g.L0)
+    w = 2 * np.pi * oracle.C0 / 1.55e-6
+    I, J = np.meshgrid(np.arange(Nx), np.arange(Ny), indexing="ij")
+    tx, ty = 2 * np.pi * 3 / Nx, 2 * np.pi * 2 / Ny
+    src = np.exp(1j * (tx * I + ty * J))
+    k2 = (2 / dx * np.sin(tx / 2)) ** 2 + (2 / dy * np.sin(ty / 2)) ** 2
+    bx, by = (1 - np.exp(-1j * tx)) / dx, (1 - np.exp(-1j * ty)) / dy
+    f = oracle.solve(g, np.full((Nx, Ny), er, dtype=complex), src, w, pol)
+    if pol == oracle.TM:
+        ez = 1j * w * src / (-k2 / mu0 + w ** 2 * eps0 * er)
+        want = (ez, -ez * by / (1j * w * mu0), ez * bx / (1j * w * mu0))
+    else:
+        hz = 1j * w * src / (-k2 / (eps0 * er) + w ** 2 * mu0)
+        want = (hz, hz * by / (1j * w * eps0 * er), -hz * bx / (1j * w * eps0 * er))
+    for got, ref in zip(f, want):
+        assert np.abs(got - ref).max() <= 1e-11 * np.abs(ref).max()
+
+
 def test_dipole_matches_greens_function(oracle):
     """Known answer: a point current 1im in free space radiates
     Ez = -(i/4)·ω·μ₀·dx·dy·H0⁽²⁾(k r) (outgoing under the e^{+iωt} convention
