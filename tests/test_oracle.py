@@ -259,6 +259,42 @@ def test_modulated_without_pml_or_modulation_is_driven(oracle):
     assert np.abs(out[0][0]).max() == 0 and np.abs(out[2][0]).max() == 0
 
 
+def test_modulated_plane_wave_closed_form(oracle):
+    """solve(d::ModulatedDevice) (src/solver/modulation.jl:35-119) without PML, with uniform ϵᵣ and
+    Δϵᵣ and a discrete plane-wave source: each sideband field is c_n·src, where c solves the
+    K x K tridiagonal system of that Fourier mode:
+      diagonal -k²/μ₀ + ωₙ²ϵ₀ϵᵣ, (n, n+1) = ½ωₙ²ϵ₀ conj(Δϵᵣ), (n+1, n) = ½ωₙ₊₁²ϵ₀ Δϵᵣ   (:79-101),
+      right-hand side iω in the centre sideband (:67-69);
+    H is the forward-difference recovery at ωₙ (:110-114), δf e^{iθj} = e^{iθj}(e^{iθ} - 1)/dh."""
+    Nx, Ny, dx, dy, er, de = 20, 16, 0.05, 0.04, 2.25, 0.3 + 0.2j
+    g = oracle.Grid((Nx, Ny), (0, 0), ((0.0, 0.0), (Nx * dx, Ny * dy)))
+    eps0, mu0, _ = oracle.normalize_parameters(g.L0)
+    w = 2 * np.pi * oracle.C0 / 1.55e-6
+    Om, s = 0.05 * w, 2
+    K = 2 * s + 1
+    I, J = np.meshgrid(np.arange(Nx), np.arange(Ny), indexing="ij")
+    tx, ty = 2 * np.pi * 3 / Nx, 2 * np.pi * 2 / Ny
+    src = np.exp(1j * (tx * I + ty * J))
+    k2 = (2 / dx * np.sin(tx / 2)) ** 2 + (2 / dy * np.sin(ty / 2)) ** 2
+    wn = w + Om * np.arange(-s, s + 1)
+    M = np.diag(-k2 / mu0 + wn ** 2 * eps0 * er).astype(complex)
+    for j in range(K - 1):
+        M[j, j + 1] = 0.5 * wn[j] ** 2 * eps0 * np.conj(de)
+        M[j + 1, j] = 0.5 * wn[j + 1] ** 2 * eps0 * de
+    rhs = np.zeros(K, dtype=complex)
+    rhs[s] = 1j * w
+    c = np.linalg.solve(M, rhs)
+    out = oracle.solve_modulated(g, np.full((Nx, Ny), er, dtype=complex), np.full((Nx, Ny), de), src, w, Om, s)
+    fx, fy = (np.exp(1j * tx) - 1) / dx, (np.exp(1j * ty) - 1) / dy
+    got = [np.stack(f) for f in out]
+    ref = [np.stack((c[j] * src, -c[j] * src * fy / (1j * wn[j] * mu0), c[j] * src * fx / (1j * wn[j] * mu0)))
+           for j in range(K)]
+    for comp in range(3):
+        a = np.stack([x[comp] for x in got])
+        b = np.stack([x[comp] for x in ref])
+        assert np.linalg.norm(a - b) <= 1e-11 * np.linalg.norm(b)
+
+
 def test_modulated_golden_regression(oracle):
     g = np.load(os.path.join(GOLD, "tm_modulated_125x50.npz"))
     Nx, Ny = int(g["Nx"]), int(g["Ny"])
