@@ -410,3 +410,32 @@ def test_flux_integral_matches_poynting_columns(oracle):
     assert np.isclose(v, ref, rtol=1e-13)
     with pytest.raises(NotImplementedError):
         oracle.flux_surface_integral(g, f[0], f[2], oracle.TM, (0.41, 0.0), 0.1, oracle.Y)
+
+
+@pytest.mark.parametrize("method", ["born", "newton"])
+def test_chi3_plane_wave_closed_form(oracle, method):
+    """solve(d::χ3Device, method) (src/solver/nonlinear.jl:36-129) without PML, with uniform ϵᵣ
+    and χ and a unit-modulus plane-wave source: |e|² stays uniform, so the field is a·src with
+    the scalar fixed point (L + c|a|²)a = iω, L = -k²/μ₀ + ω²ϵ₀ϵᵣ, c = ω²ϵ₀·3χ/L₀ (:71).
+    χ is set so that c|a|² ≈ 0.01|L|: the amplitude moves 1 % from the linear a₀ = iω/L, which
+    both iterations must reproduce (Born on this grid diverges at 0.1: other Fourier modes lie
+    near resonance, and the Born map amplifies them; Newton does not)."""
+    Nx, Ny, dx, dy, er = 20, 16, 0.05, 0.04, 2.25
+    g = oracle.Grid((Nx, Ny), (0, 0), ((0.0, 0.0), (Nx * dx, Ny * dy)))
+    eps0, mu0, _ = oracle.normalize_parameters(g.L0)
+    w = 2 * np.pi * oracle.C0 / 1.55e-6
+    I, J = np.meshgrid(np.arange(Nx), np.arange(Ny), indexing="ij")
+    tx, ty = 2 * np.pi * 3 / Nx, 2 * np.pi * 2 / Ny
+    src = np.exp(1j * (tx * I + ty * J))
+    L = -((2 / dx * np.sin(tx / 2)) ** 2 + (2 / dy * np.sin(ty / 2)) ** 2) / mu0 + w ** 2 * eps0 * er
+    a0 = 1j * w / L
+    chi = 0.01 * abs(L) / (abs(a0) ** 2 * w ** 2 * eps0 * 3 / g.L0)
+    c = w ** 2 * eps0 * 3 * chi / g.L0
+    a = a0
+    for _ in range(200):
+        a = 1j * w / (L + c * abs(a) ** 2)
+    assert abs(a - a0) > 5e-3 * abs(a0)
+    (ez, _, _), err = oracle.solve_chi3(g, np.full((Nx, Ny), er, dtype=complex), np.full((Nx, Ny), chi), src, w,
+                                        method)
+    assert err[-1] <= 1e-12
+    assert np.abs(ez - a * src).max() <= 1e-10 * abs(a)
