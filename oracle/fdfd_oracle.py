@@ -17,8 +17,11 @@ checks that two FP64 direct solvers agree to sqrt(eps)).  Parity of this
 restatement with the reference is therefore UNPINNED at the level of exact
 field values.  It is cross-checked instead against (a) hand-derived operator
 entries on tiny grids, (b) an independent dense FP64 solve, mirroring the
-reference's own solver-agreement test, and (c) the analytic 2-D free-space
-Green's function for the reference's dipole test problem.
+reference's own solver-agreement test, (c) the analytic 2-D free-space
+Green's function for the reference's dipole test problem, and (d) closed-form
+discrete solutions on periodic grids without PML (plane-wave driven TM/TE
+fields, the sideband system per Fourier mode, the χ³ scalar fixed point, and
+the eigenfrequencies of a uniform grid).
 
 Third-party arithmetic that the reference delegates (not vendored in the
 reference tree, and unpinned there: ``Project.toml`` has no [compat] section
