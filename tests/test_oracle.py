@@ -439,3 +439,25 @@ def test_chi3_plane_wave_closed_form(oracle, method):
                                         method)
     assert err[-1] <= 1e-12
     assert np.abs(ez - a * src).max() <= 1e-10 * abs(a)
+
+
+@pytest.mark.parametrize("pol", [1, 2])
+def test_poynting_plane_wave_closed_form(oracle, pol):
+    """poynting (src/flux.jl:15-29) of a discrete plane wave f1 = a·e^{i(θx·i + θy·j)} with
+    f2 = α·f1, f3 = β·f1: grid_average over the previous cell multiplies f1 by (1 + e^{-iθ})/2, so
+      TM: Sx = -½|a|²Re(½(1 + e^{-iθx})·conj(β)),  Sy = ½|a|²Re(½(1 + e^{-iθy})·conj(α))
+      TE: Sx = ½|a|²Re(β·conj(½(1 + e^{-iθx}))),  Sy = -½|a|²Re(α·conj(½(1 + e^{-iθy})))
+    uniform over the grid (the average wraps periodically, grid.jl:157-162)."""
+    Nx, Ny = 12, 10
+    I, J = np.meshgrid(np.arange(Nx), np.arange(Ny), indexing="ij")
+    tx, ty = 2 * np.pi * 2 / Nx, 2 * np.pi * 3 / Ny
+    a, al, be = 0.7 - 1.1j, 0.3 + 2.0j, -1.4 + 0.6j
+    f1 = a * np.exp(1j * (tx * I + ty * J))
+    Sx, Sy = oracle.poynting(f1, al * f1, be * f1, pol)
+    hx, hy = (1 + np.exp(-1j * tx)) / 2, (1 + np.exp(-1j * ty)) / 2
+    a2 = abs(a) ** 2
+    if pol == oracle.TM:
+        want = (-0.5 * a2 * (hx * np.conj(be)).real, 0.5 * a2 * (hy * np.conj(al)).real)
+    else:
+        want = (0.5 * a2 * (be * np.conj(hx)).real, -0.5 * a2 * (al * np.conj(hy)).real)
+    assert np.allclose(Sx, want[0], rtol=1e-13, atol=0) and np.allclose(Sy, want[1], rtol=1e-13, atol=0)
