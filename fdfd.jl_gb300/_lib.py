@@ -27,7 +27,7 @@ FDFD_MODE_MAX_POINTS = 1023
 
 # every symbol include/fdfd_cuda.h declares
 EXPORTS = ["fdfd_version", "fdfd_create", "fdfd_destroy", "fdfd_last_error", "fdfd_set_refinement",
-           "fdfd_set_fallback", "fdfd_set_restart", "fdfd_mf_create", "fdfd_mf_set_deps", "fdfd_mf_factor",
+           "fdfd_set_fallback", "fdfd_set_restart", "fdfd_set_wait_limit", "fdfd_set_device_budget", "fdfd_mf_create", "fdfd_mf_set_deps", "fdfd_mf_factor",
            "fdfd_mf_solve", "fdfd_get_mode", "fdfd_mode_sources", "fdfd_poynting", "fdfd_poynting_device",
            "fdfd_flux_integral", "fdfd_chi3_solve",
            "fdfd_set_eps", "fdfd_factor", "fdfd_solve", "fdfd_solve_device", "fdfd_adjoint", "fdfd_eigfreq",
@@ -95,6 +95,10 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.fdfd_set_fallback.argtypes = [vp, ip]
     lib.fdfd_set_restart.restype = ip
     lib.fdfd_set_restart.argtypes = [vp, ip]
+    lib.fdfd_set_wait_limit.restype = ip
+    lib.fdfd_set_wait_limit.argtypes = [vp, C.c_longlong]
+    lib.fdfd_set_device_budget.restype = ip
+    lib.fdfd_set_device_budget.argtypes = [vp, C.c_longlong]
     lib.fdfd_mf_create.restype = ip
     lib.fdfd_mf_create.argtypes = [C.POINTER(vp), ip, ip, ip, ip, C.c_double, C.c_double, C.c_double, C.c_double,
                                    C.c_double, ip, ip, ip]
@@ -213,6 +217,14 @@ class Handle:
     def set_fallback(self, on=True):
         """FP64 re-factorization when a MIXED handle's refinement stalls (default on)."""
         self._check(self.lib.fdfd_set_fallback(self.h, int(bool(on))))
+
+    def set_wait_limit(self, ns=0):
+        """Pipeline wait limit of the tensor-core GEMM in ns (0: the default, 2 s)."""
+        self._check(self.lib.fdfd_set_wait_limit(self.h, int(ns)))
+
+    def set_device_budget(self, nbytes=0):
+        """Device bytes the handle may hold (0: no limit); beyond it allocations fail with FDFD_ENOMEM."""
+        self._check(self.lib.fdfd_set_device_budget(self.h, int(nbytes)))
 
     def set_eps(self, eps):
         buf = natural(eps)

@@ -32,6 +32,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #define FDFD_VERSION_STR "fdfd_cuda 0.1.0 (sm_103a)"
@@ -74,6 +75,7 @@ struct StepJobs {     // offsets into the job blob
     size_t f2 = 0, f2y = 0, bw = 0, bwy = 0;
     size_t iota = 0;
     int ne = 0, ns = 0, nl1 = 0, ncp = 0, ncpy = 0, nf2 = 0;
+    int nf2b = 0;         // coupling blocks the forward survivor jobs (f2) reference
 };
 
 template <typename T> struct FactorStore {
@@ -88,6 +90,7 @@ template <typename T> struct FactorStore {
     int* tripiv = nullptr;      // and their interchanges (b per node)
     bool tc_ok = false;
     TcMaps tc;       // TMA descriptors (FP32 only)
+    bool complete = false;   // every pool above allocated
 };
 
 }  // namespace
@@ -143,6 +146,9 @@ struct fdfd_handle {
     cudaEvent_t ev[8];
     long long launches = 0;
     long long dev_bytes = 0;
+    long long dev_budget = 0;            // device bytes the handle may hold (0: no limit)
+    std::unordered_map<void*, size_t> alloc_bytes;   // live dev_alloc buffers and their sizes
+    unsigned long long wait_ns = 0;      // pipeline wait limit of the tensor-core GEMM (0: default)
     // FP64 device buffers (natural layout)
     cplx<double>* eps = nullptr;     // Nx*Ny
     cplx<double>* sf = nullptr;      // 2*(2Nx+2Ny)
@@ -266,17 +272,31 @@ int check_launch(fdfd_handle* h, const char* where) {
 
 int dev_alloc(fdfd_handle* h, void** p, size_t bytes) {
     if (bytes == 0) bytes = 16;
+    if (h->dev_budget > 0 && h->dev_bytes + (long long)bytes > h->dev_budget) {
+        *p = nullptr;
+        return set_err(h, FDFD_ENOMEM, "device budget of %lld bytes exceeded: %lld held, %zu more requested",
+                       h->dev_budget, h->dev_bytes, bytes);
+    }
     cudaError_t e = cudaMalloc(p, bytes);
     if (e != cudaSuccess) {
+        *p = nullptr;
         cudaGetLastError();
         return set_err(h, FDFD_ENOMEM, "cudaMalloc(%zu bytes) failed: %s", bytes, cudaGetErrorString(e));
     }
     h->dev_bytes += (long long)bytes;
+    h->alloc_bytes[*p] = bytes;
     return FDFD_OK;
 }
 
-void dev_free(void* p) {
-    if (p) cudaFree(p);
+// frees a dev_alloc'd buffer and returns its bytes to the handle's count
+void dev_free(fdfd_handle* h, void* p) {
+    if (!p) return;
+    auto it = h->alloc_bytes.find(p);
+    if (it != h->alloc_bytes.end()) {
+        h->dev_bytes -= (long long)it->second;
+        h->alloc_bytes.erase(it);
+    }
+    cudaFree(p);
 }
 
 // ---- profiling -------------------------------------------------------------
@@ -491,6 +511,7 @@ void build_jobs(fdfd_handle* h, JobBlob& B) {
                     f2.push_back(make_int4(sp.snext_elim[i] ? h->Uslot[e - 1][s] : -1, sp.snext[i],
                                            sp.sprev_elim[i] ? h->Lslot[e - 1][s] : -1, sp.sprev[i]));
                     f2y.push_back(make_int2(s, s));
+                    J.nf2b += (sp.snext_elim[i] ? 1 : 0) + (sp.sprev_elim[i] ? 1 : 0);
                 }
             }
             J.cpy = B.add(cpy.data(), cpy.size() * sizeof(int3));
@@ -553,9 +574,30 @@ template <typename T> int alloc_pool(fdfd_handle* h, Pool<T>& P, int rows, int c
     return FDFD_OK;
 }
 
+template <typename T> void free_store(fdfd_handle* h, FactorStore<T>& F) {
+    void* bufs[] = {F.D.base, F.C.base, F.X.base, F.GP.base, F.RP.base, F.Tg.base, F.rv, F.xv, F.wv,
+                    F.perm, F.rowsrc, F.gj_slots, F.trifac, F.tripiv};
+    for (void* p : bufs) dev_free(h, p);
+    F = FactorStore<T>();
+}
+
+template <typename T> int alloc_factor_pools(fdfd_handle* h);
+
+// factor storage of precision T: all of it, or (on failure) none of it
 template <typename T> int alloc_factor(fdfd_handle* h) {
     FactorStore<T>& F = store<T>(h);
-    if (F.D.base) return FDFD_OK;
+    if (F.complete) return FDFD_OK;
+    const int rc = alloc_factor_pools<T>(h);
+    if (rc != FDFD_OK) {
+        free_store(h, F);
+        return rc;
+    }
+    F.complete = true;
+    return FDFD_OK;
+}
+
+template <typename T> int alloc_factor_pools(fdfd_handle* h) {
+    FactorStore<T>& F = store<T>(h);
     const int b = h->map.b, n = h->map.n, ld = h->map.ld;
     const int planes = 2;   // re, im (the tensor-core GEMM forms the TF32 residuals itself)
     const int pc = sizeof(T) == 4 ? 32 : panel_nb<T>(b);
@@ -597,8 +639,9 @@ template <typename T> int alloc_factor(fdfd_handle* h) {
 template <typename T> int alloc_vectors(fdfd_handle* h, int nrhs) {
     FactorStore<T>& F = store<T>(h);
     if (F.vec_nrhs >= nrhs) return FDFD_OK;
-    dev_free(F.rv); dev_free(F.xv); dev_free(F.wv);
+    dev_free(h, F.rv); dev_free(h, F.xv); dev_free(h, F.wv);
     F.rv = F.xv = F.wv = nullptr;
+    F.vec_nrhs = 0;   // stays 0 unless all three allocations succeed
     size_t bytes = (size_t)h->map.n * nrhs * 2 * h->map.ld * sizeof(T);
     RET(dev_alloc(h, (void**)&F.rv, bytes));
     RET(dev_alloc(h, (void**)&F.xv, bytes));
@@ -645,6 +688,7 @@ int gemm(fdfd_handle* h, int pa, int pb, int pc, const int* a_slot, const int* b
     g.n_off = n_off; g.skip_c0 = skip_c0; g.skip_w = skip_w;
     g.c_trans_arr = nullptr;
     g.err = h->derr;
+    g.wait_ns = h->wait_ns;
     const double flops = 8.0 * M * N * K * njobs;
     int ev = prof_begin(h);
     if (sizeof(T) == 4 && F.tc_ok) {
@@ -813,8 +857,9 @@ template <typename T> int factor_impl(fdfd_handle* h) {
 // Solve sweeps: F.rv holds the (scaled) right-hand sides in node layout on
 // entry; F.xv holds the solution on exit.
 // ---------------------------------------------------------------------------
+// nblk: factor blocks the njobs jobs reference (a job's second block may be absent)
 template <typename T> int gemv(fdfd_handle* h, int tr, int p1, int p2, const T* V1, const T* V2, const T* Y0, T* Y,
-                               const int4* jobs, const int2* yjobs, int njobs, int nrhs, T alpha) {
+                               const int4* jobs, const int2* yjobs, int njobs, int nblk, int nrhs, T alpha) {
     if (njobs == 0) return FDFD_OK;
     FactorStore<T>& F = store<T>(h);
     const int b = h->map.b;
@@ -826,11 +871,13 @@ template <typename T> int gemv(fdfd_handle* h, int tr, int p1, int p2, const T* 
         g.jobs = jobs; g.yjobs = yjobs;
         g.b = b; g.ld = h->map.ld; g.nrhs = std::min(rmax, nrhs - r0); g.rtot = nrhs; g.r0 = r0;
         g.alpha = alpha;
+        g.nsm = h->num_sms;
         int ev = prof_begin(h);
         int e = launch_gemv<T>(h->stream, tr, njobs, g);
-        // algorithmic bytes: every referenced block (re + im planes) read once, vectors in and out
+        // algorithmic bytes: every referenced block (re + im planes) read once; per job and
+        // right-hand side the input vectors of its blocks, y0 and y (each b complex values)
         prof_end(h, ev, FDFD_PROF_SWEEP,
-                 (double)njobs * (2.0 * b * b * 2 * sizeof(T) + 3.0 * g.nrhs * 2 * b * sizeof(T)));
+                 (double)nblk * 2.0 * b * b * sizeof(T) + (double)(nblk + 2 * njobs) * g.nrhs * 2.0 * b * sizeof(T));
         h->launches++;
         if (e) return set_err(h, FDFD_ECUDA, "gemv launch failed: %s", cudaGetErrorString((cudaError_t)e));
     }
@@ -843,7 +890,7 @@ template <typename T> int sweep_impl(fdfd_handle* h, int nrhs) {
     // forward
     for (int e = 1; e <= E; ++e) {
         const StepJobs& S = h->sj[e];
-        RET(gemv<T>(h, 0, P_D, P_D, F.rv, F.rv, nullptr, F.xv, J<int4>(h, S.fwd1), J<int2>(h, S.fwd1y), S.ne, nrhs,
+        RET(gemv<T>(h, 0, P_D, P_D, F.rv, F.rv, nullptr, F.xv, J<int4>(h, S.fwd1), J<int2>(h, S.fwd1y), S.ne, S.ne, nrhs,
                     (T)1));
         if (e == 1) {
             if (S.nf2) {
@@ -852,18 +899,18 @@ template <typename T> int sweep_impl(fdfd_handle* h, int nrhs) {
                 h->launches++;
             }
         } else {
-            RET(gemv<T>(h, 0, P_C, P_C, F.xv, F.xv, F.rv, F.rv, J<int4>(h, S.f2), J<int2>(h, S.f2y), S.nf2, nrhs,
+            RET(gemv<T>(h, 0, P_C, P_C, F.xv, F.xv, F.rv, F.rv, J<int4>(h, S.f2), J<int2>(h, S.f2y), S.nf2, S.nf2b, nrhs,
                         (T)-1));
         }
     }
     // final pair
-    RET(gemv<T>(h, 0, P_D, P_D, F.rv, F.rv, nullptr, F.xv, J<int4>(h, h->fin_g1), J<int2>(h, h->fin_g1y), 1, nrhs,
+    RET(gemv<T>(h, 0, P_D, P_D, F.rv, F.rv, nullptr, F.xv, J<int4>(h, h->fin_g1), J<int2>(h, h->fin_g1y), 1, 1, nrhs,
                 (T)1));
-    RET(gemv<T>(h, 0, P_C, P_C, F.xv, F.xv, F.rv, F.rv, J<int4>(h, h->fin_ra), J<int2>(h, h->fin_ray), 1, nrhs,
+    RET(gemv<T>(h, 0, P_C, P_C, F.xv, F.xv, F.rv, F.rv, J<int4>(h, h->fin_ra), J<int2>(h, h->fin_ray), 1, 1, nrhs,
                 (T)-1));
-    RET(gemv<T>(h, 0, P_D, P_D, F.rv, F.rv, nullptr, F.xv, J<int4>(h, h->fin_g0), J<int2>(h, h->fin_g0y), 1, nrhs,
+    RET(gemv<T>(h, 0, P_D, P_D, F.rv, F.rv, nullptr, F.xv, J<int4>(h, h->fin_g0), J<int2>(h, h->fin_g0y), 1, 1, nrhs,
                 (T)1));
-    RET(gemv<T>(h, 1, P_X, P_X, F.xv, F.xv, F.xv, F.xv, J<int4>(h, h->fin_bx), J<int2>(h, h->fin_bxy), 1, nrhs,
+    RET(gemv<T>(h, 1, P_X, P_X, F.xv, F.xv, F.xv, F.xv, J<int4>(h, h->fin_bx), J<int2>(h, h->fin_bxy), 1, 1, nrhs,
                 (T)-1));
     // backward
     for (int e = E; e >= 1; --e) {
@@ -872,10 +919,10 @@ template <typename T> int sweep_impl(fdfd_handle* h, int nrhs) {
             launch_diag_sweep<T>(h->stream, S.ne, h->map, h->st, h->scale, nrhs, J<int4>(h, S.dswb), 1,
                                  (const T*)F.xv, F.wv);
             h->launches++;
-            RET(gemv<T>(h, 0, P_D, P_D, F.wv, F.wv, F.xv, F.xv, J<int4>(h, S.bwd1), J<int2>(h, S.bwd1y), S.ne, nrhs,
+            RET(gemv<T>(h, 0, P_D, P_D, F.wv, F.wv, F.xv, F.xv, J<int4>(h, S.bwd1), J<int2>(h, S.bwd1y), S.ne, S.ne, nrhs,
                         (T)-1));
         } else {
-            RET(gemv<T>(h, 1, P_X, P_X, F.xv, F.xv, F.xv, F.xv, J<int4>(h, S.bw), J<int2>(h, S.bwy), S.ne, nrhs,
+            RET(gemv<T>(h, 1, P_X, P_X, F.xv, F.xv, F.xv, F.xv, J<int4>(h, S.bw), J<int2>(h, S.bwy), S.ne, 2 * S.ne, nrhs,
                         (T)-1));
         }
     }
@@ -940,16 +987,18 @@ int precond(fdfd_handle* h, const cplx<double>* in, cplx<double>* out, int nrhs)
 // ---------------------------------------------------------------------------
 int ensure_part(fdfd_handle* h, size_t doubles) {
     if (h->part_cap >= doubles) return FDFD_OK;
-    dev_free(h->part);
+    dev_free(h, h->part);
     h->part = nullptr;
+    h->part_cap = 0;
     RET(dev_alloc(h, (void**)&h->part, doubles * sizeof(double)));
     h->part_cap = doubles;
     return FDFD_OK;
 }
 int ensure_red(fdfd_handle* h, size_t doubles) {
     if (h->red_cap >= doubles) return FDFD_OK;
-    dev_free(h->red);
+    dev_free(h, h->red);
     h->red = nullptr;
+    h->red_cap = 0;
     RET(dev_alloc(h, (void**)&h->red, doubles * sizeof(double)));
     h->red_cap = doubles;
     return FDFD_OK;
@@ -1120,7 +1169,10 @@ int restart_len(const fdfd_handle* h, int nrhs) {
 
 int ensure_krylov(fdfd_handle* h, int nrhs, int m) {
     if (h->kr_nrhs >= nrhs && h->kr_m >= m && h->kr_vlen == vlen(h)) return FDFD_OK;
-    dev_free(h->kb); dev_free(h->kx); dev_free(h->kr); dev_free(h->kV); dev_free(h->kZ); dev_free(h->kc);
+    dev_free(h, h->kb); dev_free(h, h->kx); dev_free(h, h->kr); dev_free(h, h->kV); dev_free(h, h->kZ); dev_free(h, h->kc);
+    h->kb = h->kx = h->kr = h->kV = h->kZ = h->kc = nullptr;
+    h->kr_nrhs = h->kr_m = 0;   // stay 0 unless every allocation succeeds
+    h->kr_vlen = 0;
     long long N = vlen(h);
     size_t v = (size_t)N * nrhs * sizeof(cplx<double>);
     RET(dev_alloc(h, (void**)&h->kb, v));
@@ -1342,12 +1394,6 @@ int refine_fb(fdfd_handle* h, int nrhs, int* iters, double* relres) {
     return FDFD_OK;
 }
 
-template <typename T> void free_store(FactorStore<T>& F) {
-    void* bufs[] = {F.D.base, F.C.base, F.X.base, F.GP.base, F.RP.base, F.Tg.base, F.rv, F.xv, F.wv,
-                    F.perm, F.rowsrc, F.gj_slots, F.trifac, F.tripiv};
-    for (void* p : bufs) dev_free(p);
-}
-
 double elapsed_ms(cudaEvent_t a, cudaEvent_t b) {
     float ms = 0;
     cudaEventElapsedTime(&ms, a, b);
@@ -1431,7 +1477,7 @@ void fdfd_destroy(fdfd_handle* h) {
     if (h->stream) cudaStreamSynchronize(h->stream);
     if (h->mf) {
         for (fdfd_handle* s : h->mf->sub) fdfd_destroy(s);
-        dev_free(h->mf->deps);
+        dev_free(h, h->mf->deps);
         if (h->mf->ev_in) cudaEventDestroy(h->mf->ev_in);
         for (auto& e : h->mf->ev_out) if (e) cudaEventDestroy(e);
         delete h->mf;
@@ -1439,9 +1485,9 @@ void fdfd_destroy(fdfd_handle* h) {
     }
     void* bufs[] = {h->eps, h->sf, h->st, h->derr, h->part, h->red, h->kb, h->kx, h->kr, h->kV, h->kZ, h->kc, h->io,
                     h->djobs, h->mode_buf, h->nl_d1};
-    for (void* p : bufs) dev_free(p);
-    free_store(h->f32);
-    free_store(h->f64);
+    for (void* p : bufs) dev_free(h, p);
+    free_store(h, h->f32);
+    free_store(h, h->f64);
     for (auto& e : h->ev) if (e) cudaEventDestroy(e);
     for (auto& e : h->evpool) cudaEventDestroy(e);
     if (h->stream) cudaStreamDestroy(h->stream);
@@ -1469,6 +1515,22 @@ int fdfd_set_restart(fdfd_handle* h, int m) {
 int fdfd_set_fallback(fdfd_handle* h, int on) {
     if (!h) return FDFD_EINVAL;
     h->fallback = on != 0;
+    return FDFD_OK;
+}
+
+int fdfd_set_wait_limit(fdfd_handle* h, long long ns) {
+    if (!h) return FDFD_EINVAL;
+    if (h->mf)
+        for (fdfd_handle* s : h->mf->sub) s->wait_ns = ns > 0 ? (unsigned long long)ns : 0ull;
+    h->wait_ns = ns > 0 ? (unsigned long long)ns : 0ull;
+    return FDFD_OK;
+}
+
+int fdfd_set_device_budget(fdfd_handle* h, long long bytes) {
+    if (!h || bytes < 0) return FDFD_EINVAL;
+    if (h->mf)
+        for (fdfd_handle* s : h->mf->sub) s->dev_budget = bytes;
+    h->dev_budget = bytes;
     return FDFD_OK;
 }
 
@@ -1601,9 +1663,8 @@ int fdfd_solve(fdfd_handle* h, const double* src, int nrhs, double* f1, double* 
     size_t bytes = (size_t)N * nrhs * sizeof(cplx<double>);
     // staging: [src | f1 | f2 | f3], kept by the handle between calls
     if (h->io_cap < 4 * bytes) {
-        dev_free(h->io);
+        dev_free(h, h->io);
         h->io = nullptr;
-        h->dev_bytes -= (long long)h->io_cap;
         h->io_cap = 0;
         RET(dev_alloc(h, (void**)&h->io, 4 * bytes));
         h->io_cap = 4 * bytes;
@@ -1711,9 +1772,8 @@ int fdfd_mf_solve(fdfd_handle* h, const double* src, double* ez, double* hx, dou
     if (first_nonfinite(src, 2 * N) >= 0) return set_err(h, FDFD_EINVAL, "src has a non-finite entry");
     const size_t bytes = (size_t)N * M.K * sizeof(cplx<double>);
     if (h->io_cap < 4 * bytes) {
-        dev_free(h->io);
+        dev_free(h, h->io);
         h->io = nullptr;
-        h->dev_bytes -= (long long)h->io_cap;
         h->io_cap = 0;
         RET(dev_alloc(h, (void**)&h->io, 4 * bytes));
         h->io_cap = 4 * bytes;
@@ -1846,9 +1906,8 @@ int run_modes(fdfd_handle* h, std::vector<ModeJob>& jobs, const std::vector<int>
                  o_src = al(o_vec + (size_t)tot * sizeof(zd)),
                  need = o_src + (want_src ? (size_t)nw * N * sizeof(zd) : 0);
     if (h->mode_cap < need) {
-        dev_free(h->mode_buf);
+        dev_free(h, h->mode_buf);
         h->mode_buf = nullptr;
-        h->dev_bytes -= (long long)h->mode_cap;
         h->mode_cap = 0;
         RET(dev_alloc(h, (void**)&h->mode_buf, need));
         h->mode_cap = need;
@@ -1938,9 +1997,8 @@ int fdfd_poynting(fdfd_handle* h, int pol, const double* f1, const double* f2, c
     const long long N = (long long)h->Nx * h->Ny;
     const size_t fb = (size_t)N * sizeof(cplx<double>), sb = (size_t)N * sizeof(double);
     if (h->io_cap < 3 * fb + 2 * sb) {
-        dev_free(h->io);
+        dev_free(h, h->io);
         h->io = nullptr;
-        h->dev_bytes -= (long long)h->io_cap;
         h->io_cap = 0;
         RET(dev_alloc(h, (void**)&h->io, 3 * fb + 2 * sb));
         h->io_cap = 3 * fb + 2 * sb;
@@ -1976,9 +2034,8 @@ int fdfd_flux_integral(fdfd_handle* h, int pol, const double* f1, const double* 
     const size_t fb = (size_t)N * sizeof(cplx<double>);
     const size_t need = 2 * fb + (size_t)nlines * (sizeof(int3) + sizeof(double)) + 64;
     if (h->io_cap < need) {
-        dev_free(h->io);
+        dev_free(h, h->io);
         h->io = nullptr;
-        h->dev_bytes -= (long long)h->io_cap;
         h->io_cap = 0;
         RET(dev_alloc(h, (void**)&h->io, need));
         h->io_cap = need;
@@ -2002,9 +2059,10 @@ int fdfd_flux_integral(fdfd_handle* h, int pol, const double* f1, const double* 
 namespace {
 
 double vnorm(fdfd_handle* h, const cplx<double>* x, long long n) {
-    if (ensure_part(h, 152 * 2) != FDFD_OK || ensure_red(h, 2) != FDFD_OK) return NAN;
-    vdots_kernel<<<dim3(152, 1), 256, 0, h->stream>>>(n, 1, x, 0, x, h->part);
-    reduce_partials_kernel<<<1, 256, 0, h->stream>>>(h->part, 152, 2, h->red);
+    const int nb = h->num_sms;   // one partial per SM
+    if (ensure_part(h, (size_t)nb * 2) != FDFD_OK || ensure_red(h, 2) != FDFD_OK) return NAN;
+    vdots_kernel<<<dim3(nb, 1), 256, 0, h->stream>>>(n, 1, x, 0, x, h->part);
+    reduce_partials_kernel<<<1, 256, 0, h->stream>>>(h->part, nb, 2, h->red);
     h->launches += 2;
     double v[2] = {0, 0};
     if (cudaMemcpyAsync(v, h->red, sizeof v, cudaMemcpyDeviceToHost, h->stream) != cudaSuccess ||
@@ -2053,9 +2111,8 @@ int fdfd_chi3_solve(fdfd_handle* h, const double* chi, const double* src, int me
     cplx<double>* B = Z + 2 * N;
     double* dco = reinterpret_cast<double*>(B + N);
     if (h->io_cap < 4 * vb) {
-        dev_free(h->io);
+        dev_free(h, h->io);
         h->io = nullptr;
-        h->dev_bytes -= (long long)h->io_cap;
         h->io_cap = 0;
         RET(dev_alloc(h, (void**)&h->io, 4 * vb));
         h->io_cap = 4 * vb;
@@ -2202,8 +2259,7 @@ int fdfd_apply(fdfd_handle* h, const double* x, int nrhs, double* y) {
     if (rc == FDFD_OK && cudaMemcpyAsync(y, buf + N * nrhs, bytes, cudaMemcpyDeviceToHost, h->stream) != cudaSuccess)
         rc = FDFD_ECUDA;
     cudaStreamSynchronize(h->stream);
-    cudaFree(buf);
-    h->dev_bytes -= 2 * (long long)bytes;
+    dev_free(h, buf);
     return rc == FDFD_ECUDA ? set_err(h, rc, "fdfd_apply copy failed") : rc;
 }
 
@@ -2221,9 +2277,8 @@ int fdfd_adjoint(fdfd_handle* h, const double* src, const double* mvec, double* 
     const size_t bytes = (size_t)N * sizeof(cplx<double>);
     RET(ensure_krylov(h, 2, restart_len(h, 2)));
     if (h->io_cap < 4 * bytes) {
-        dev_free(h->io);
+        dev_free(h, h->io);
         h->io = nullptr;
-        h->dev_bytes -= (long long)h->io_cap;
         h->io_cap = 0;
         RET(dev_alloc(h, (void**)&h->io, 4 * bytes));
         h->io_cap = 4 * bytes;
@@ -2246,13 +2301,14 @@ int fdfd_adjoint(fdfd_handle* h, const double* src, const double* mvec, double* 
     RET(refine_fb(h, 2, &iters, &rel));
     LAUNCH(pscale_kernel, nb, 256, 0, h->Nx, h->Ny, h->sf, 1, h->kx + N, d_lam);
     // s = mᵀE (no conjugation), reduced on the host from per-block partials
-    RET(ensure_part(h, 2 * 152));
-    LAUNCH(vdotu_kernel, 152, 256, 0, N, d_m, h->kx, h->part);
-    std::vector<double> part(2 * 152);
+    const int nparts = h->num_sms;   // one partial per SM
+    RET(ensure_part(h, 2 * (size_t)nparts));
+    LAUNCH(vdotu_kernel, nparts, 256, 0, N, d_m, h->kx, h->part);
+    std::vector<double> part(2 * (size_t)nparts);
     CK(cudaMemcpyAsync(part.data(), h->part, part.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     zd s(0, 0);
-    for (int i = 0; i < 152; ++i) s += zd(part[2 * i], part[2 * i + 1]);
+    for (int i = 0; i < nparts; ++i) s += zd(part[2 * i], part[2 * i + 1]);
     // dJ/dϵᵣ_k = -2 Re(conj(s)·ω²ϵ₀·λ_k·E_k)
     const zd coef = std::conj(s) * (h->omega * h->omega * kEPS0 * h->L0);
     cplx<double> c;
@@ -2324,7 +2380,7 @@ int fdfd_eigfreq(fdfd_handle* h, double omega0, int nev, int which, double tol, 
     RET(dev_alloc(h, (void**)&V, vbytes * (m + 1)));
     struct Free {
         fdfd_handle* h; void* p; size_t b;
-        ~Free() { cudaFree(p); h->dev_bytes -= (long long)b; }
+        ~Free() { dev_free(h, p); }
     } free_v{h, V, vbytes * (m + 1)};
     // deterministic start vector (splitmix64 hash of the index), unit norm
     {
@@ -2563,7 +2619,7 @@ int debug_gemm_impl(int M, int N, int K, const double* A, const double* B, doubl
         g.a_slot = g.b_slot = g.c_slot = slots;
         g.Cin = Pool<T>(); g.cin_slot = nullptr; g.row_src = nullptr;
         g.M = M; g.N = N; g.K = K; g.alpha = (T)1; g.beta = 0; g.mask_c0 = 0; g.mask_w = 0;
-        g.c_trans = 0; g.c_trans_arr = nullptr; g.err = derr;
+        g.c_trans = 0; g.c_trans_arr = nullptr; g.err = derr; g.wait_ns = 0;
         g.n_off = 0; g.skip_c0 = 0; g.skip_w = 0;
         cudaEvent_t e0, e1;
         cudaEventCreate(&e0); cudaEventCreate(&e1);

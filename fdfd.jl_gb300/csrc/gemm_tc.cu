@@ -69,13 +69,17 @@ __device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
         : "memory");
     return ok != 0;
 }
-// bounded wait: false after FDFD_WAIT_LIMIT_NS
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+// bounded wait: false once limit_ns of %globaltimer have passed.  The pipeline
+// waits take the launch's limit (GemmArgs::wait_ns, settable per handle); the
+// waits that drain a CTA's own copies and MMAs in flight before it frees TMEM
+// and exits always take FDFD_WAIT_LIMIT_NS, so a short pipeline limit never
+// lets a CTA leave with asynchronous work outstanding.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, uint64_t limit_ns) {
     if (mbar_try(bar, parity)) return true;
     uint64_t t0 = globaltimer_ns();
     while (true) {
         if (mbar_try(bar, parity)) return true;
-        if (globaltimer_ns() - t0 > FDFD_WAIT_LIMIT_NS) return false;
+        if (globaltimer_ns() - t0 > limit_ns) return false;
         __nanosleep(64);
     }
 }
@@ -161,6 +165,7 @@ __global__ void __launch_bounds__(TcTile<BN>::THREADS, BN <= 64 ? 2 : 1)
     __shared__ int s_abort;
 
     const GemmArgs<float>& g = P.g;
+    const uint64_t wait_ns = g.wait_ns ? g.wait_ns : FDFD_WAIT_LIMIT_NS;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int job = blockIdx.z;
     const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
@@ -201,7 +206,7 @@ __global__ void __launch_bounds__(TcTile<BN>::THREADS, BN <= 64 ? 2 : 1)
             for (int kt = 0; kt < nk; ++kt) {
                 const int s = kt % STAGES;
                 if (kt >= STAGES) {
-                    if (!mbar_wait(smem_u32(&bar_empty[s]), ((kt / STAGES) - 1) & 1)) { ok = false; break; }
+                    if (!mbar_wait(smem_u32(&bar_empty[s]), ((kt / STAGES) - 1) & 1, wait_ns)) { ok = false; break; }
                 }
                 const uint32_t bar = smem_u32(&bar_full[s]);
                 mbar_expect_tx(bar, np * (A_PLANE_BYTES + B_PLANE_BYTES));
@@ -219,7 +224,7 @@ __global__ void __launch_bounds__(TcTile<BN>::THREADS, BN <= 64 ? 2 : 1)
             }
             // drain this CTA's copies in flight (bounded)
             for (int kt = (issued > STAGES ? issued - STAGES : 0); kt < issued; ++kt)
-                if (!mbar_wait(smem_u32(&bar_full[kt % STAGES]), (kt / STAGES) & 1)) {
+                if (!mbar_wait(smem_u32(&bar_full[kt % STAGES]), (kt / STAGES) & 1, FDFD_WAIT_LIMIT_NS)) {
                     dev_error(g.err, FDFD_DEVERR_TIMEOUT);
                     break;
                 }
@@ -231,7 +236,7 @@ __global__ void __launch_bounds__(TcTile<BN>::THREADS, BN <= 64 ? 2 : 1)
             const uint32_t id_pos = idesc_tf32(BM, BN, 0), id_neg = idesc_tf32(BM, BN, 1);
             for (int kt = 0; kt < nk; ++kt) {
                 const int s = kt % STAGES;
-                if (!mbar_wait(smem_u32(presplit ? &bar_full[s] : &bar_conv[s]), (kt / STAGES) & 1)) {
+                if (!mbar_wait(smem_u32(presplit ? &bar_full[s] : &bar_conv[s]), (kt / STAGES) & 1, wait_ns)) {
                     ok = false;
                     break;
                 }
@@ -298,7 +303,7 @@ __global__ void __launch_bounds__(TcTile<BN>::THREADS, BN <= 64 ? 2 : 1)
             for (int kt = 0; kt < nk; ++kt) {
                 const int s = kt % STAGES;
                 if (*(volatile int*)&s_abort) { okc = false; break; }
-                if (!mbar_wait(smem_u32(&bar_full[s]), (kt / STAGES) & 1)) { okc = false; break; }
+                if (!mbar_wait(smem_u32(&bar_full[s]), (kt / STAGES) & 1, wait_ns)) { okc = false; break; }
                 unsigned char* st = smem + s * STAGE_BYTES;
                 for (int v = ct; v < NV4; v += 32 * NEPI) {
                     // A re, A im | B re, B im; each lo plane sits two planes after its raw plane
@@ -317,7 +322,8 @@ __global__ void __launch_bounds__(TcTile<BN>::THREADS, BN <= 64 ? 2 : 1)
                 atomicExch(&s_abort, 1);
             }
         }
-        const bool ok_l = mbar_wait(smem_u32(&bar_acc), 0);
+        // the accumulator barrier also drains the MMAs in flight: full limit
+        const bool ok_l = mbar_wait(smem_u32(&bar_acc), 0, FDFD_WAIT_LIMIT_NS);
         const bool ok = __all_sync(0xffffffffu, ok_l);
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         const int abort = __shfl_sync(0xffffffffu, *(volatile int*)&s_abort, 0);

@@ -162,6 +162,9 @@ template <typename T> struct GemmArgs {
     int c_trans;
     const int* c_trans_arr;   // per-job override of c_trans (device, may be null)
     unsigned* err;
+    // tensor-core kernel only: limit of each pipeline wait in ns of %globaltimer
+    // (0: FDFD_WAIT_LIMIT_NS); the drain waits before exit always take the full limit
+    unsigned long long wait_ns;
 };
 template <typename T>
 void launch_gemm_simt(cudaStream_t s, int njobs, const GemmArgs<T>& g);
@@ -180,6 +183,7 @@ template <typename T> struct GemvArgs {
     T alpha;
     int rpw, og;        // launch shape, set by launch_gemv: rows per warp (N form),
                         // lanes per output group (T form)
+    int nsm;            // streaming multiprocessors of the device (launch shape)
 };
 // TR = 1: matrices stored transposed.  Returns a cudaError_t value.
 template <typename T>

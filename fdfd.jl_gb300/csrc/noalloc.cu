@@ -7,16 +7,20 @@
 // imply.  fdfd_residual_noalloc computes the same FP64 residual and norms as
 // the handle path (residual_kernel + reduce_partials_kernel) from caller-owned
 // buffers only.  Its one piece of scratch — the per-block partial sums of
-// |r|² and |b|² — lives in the file-scope device array below, which every GPU
-// that loads this library holds until the process exits.
+// |r|² and |b|² — lives in the file-scope device array below.  The array comes
+// into being when this library's module is loaded on a device (with lazy module
+// loading, the CUDA default, at its first use there) and every GPU that loads
+// it holds it until the process exits.
 #include "fdfd_cuda.h"
 #include "kernels.cuh"
 
 #include <mutex>
 
 // (thread block, right-hand side) pairs whose partial sums fit the array:
-// 65536 pairs x 2 doubles = 1 MiB per device.
+// 65536 pairs x 2 doubles = 1 MiB per device.  The right-hand sides form the
+// grid's y dimension, so nrhs is also bounded by 65535.
 #define FDFD_NOALLOC_MAX_PARTIALS 65536
+#define FDFD_NOALLOC_MAX_RHS 65535
 #define FDFD_NOALLOC_BLOCK 256
 #define FDFD_NOALLOC_MAX_DEVICES 64
 
@@ -32,6 +36,7 @@ extern "C" int fdfd_residual_noalloc(int Nx, int Ny, int nrhs, const double* ste
     if (Nx < 1 || Ny < 1 || nrhs < 1 || !stencil || !x || !r || !norms) return FDFD_EINVAL;
     const long long N = (long long)Nx * Ny;
     const long long nblocks = (N + FDFD_NOALLOC_BLOCK - 1) / FDFD_NOALLOC_BLOCK;
+    if (nrhs > FDFD_NOALLOC_MAX_RHS) return FDFD_EINVAL;                  // grid y limit
     if (nblocks * nrhs > FDFD_NOALLOC_MAX_PARTIALS) return FDFD_EINVAL;   // scratch too small
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= FDFD_NOALLOC_MAX_DEVICES) {
@@ -41,7 +46,9 @@ extern "C" int fdfd_residual_noalloc(int Nx, int Ny, int nrhs, const double* ste
     double* part = nullptr;
     {
         // set-up, once per device, with that device current: the host-side name
-        // of the array is not a device address, so resolve it here
+        // of the array is not a device address, so resolve it here.  The cached
+        // address belongs to the device's primary context: it must not outlive a
+        // cudaDeviceReset (or a release and re-creation of that context)
         std::lock_guard<std::mutex> lock(g_mu);
         if (!g_partials_ptr[dev]) {
             void* p = nullptr;

@@ -285,7 +285,7 @@ int gemv_launch_r(cudaStream_t s, int tr, int njobs, const GemvArgs<T>& g) {
     // Launch shape: the widest per-block tile that still gives about four blocks
     // per SM.  Small batches (the deep reduction levels) get narrow tiles, so
     // their few blocks are still spread over the whole GPU.
-    const long long want = 4LL * 152;
+    const long long want = 4LL * (g.nsm > 0 ? g.nsm : 1);
     GemvArgs<T> a = g;
     if (tr) {
         a.og = 32;

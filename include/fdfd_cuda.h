@@ -112,6 +112,23 @@ int  fdfd_set_restart(fdfd_handle* h, int m);
  * Off: the call returns FDFD_ENOCONV instead.  No effect on FP64 handles. */
 int  fdfd_set_fallback(fdfd_handle* h, int on);
 
+/* Watchdog of the tensor-core GEMM (no counterpart in the reference, whose
+ * solvers have no device waits).  Every pipeline wait of that kernel
+ * (mbarrier, on TMA copies and MMAs) gives up after ns nanoseconds of
+ * %globaltimer; the CTA then records the timeout, lets its own copies and
+ * MMAs in flight finish (those waits keep the default limit), frees its
+ * tensor memory and exits, and the call returns FDFD_ETIMEOUT with the
+ * context still usable.  ns <= 0 restores the default, 2 s.  A limit far
+ * below a kernel's run time makes every factorization time out: a
+ * failure-path check, not a tuning knob. */
+int  fdfd_set_wait_limit(fdfd_handle* h, long long ns);
+
+/* Device-memory budget of the handle in bytes (no counterpart in the
+ * reference; 0, the default, means no limit).  An allocation that would take
+ * the handle's device memory above the budget fails with FDFD_ENOMEM and the
+ * sizes in the message, as a failed cudaMalloc does. */
+int  fdfd_set_device_budget(fdfd_handle* h, long long bytes);
+
 /* Relative permittivity ϵᵣ (Device.ϵᵣ, src/device.jl:19-25), Nx*Ny complex.
  * Rejects NaN/Inf.  Invalidates any existing factorization. */
 int  fdfd_set_eps(fdfd_handle* h, const double* eps_r);
@@ -311,12 +328,17 @@ int  fdfd_get_profile(fdfd_handle* h, fdfd_profile* out);
  * fdfd_get_stencil, x/b/r hold nrhs*Nx*Ny complex values, norms 2*nrhs
  * doubles.  stream is a cudaStream_t (NULL = default stream); the call
  * returns after the stream has finished its work.  Scratch: a fixed 1 MiB
- * device array of the library (block partial sums), allocated when the
- * library is loaded and held by every GPU that loads it until exit; sizes with
- * ceil(Nx*Ny/256)*nrhs > 65536 are rejected with FDFD_EINVAL.  The first call
- * on a device resolves that array's device address (cudaGetSymbolAddress) and
- * should come before any stream capture.  All calls share the array, so calls
- * that overlap on the GPU (other streams or threads) race; serialise them. */
+ * device array of the library (block partial sums).  It is created when the
+ * library's module loads on a device (with CUDA's default lazy loading, at the
+ * first use there, which may allocate and synchronise once) and is held by
+ * every GPU that loads it until exit; a caller that must never see an
+ * allocation makes one warm-up call per device first.  Sizes with
+ * ceil(Nx*Ny/256)*nrhs > 65536, or nrhs > 65535, are rejected with
+ * FDFD_EINVAL.  The first call on a device resolves that array's device
+ * address (cudaGetSymbolAddress) and should come before any stream capture;
+ * the address is cached for the device's primary context and must not
+ * outlive a cudaDeviceReset.  All calls share the array, so calls that
+ * overlap on the GPU (other streams or threads) race; serialise them. */
 int  fdfd_residual_noalloc(int Nx, int Ny, int nrhs, const double* stencil,
                            const double* x, const double* b, double* r,
                            double* norms, void* stream);

@@ -52,6 +52,8 @@ int main(void) {
     CHECK(fdfd_set_refinement(NULL, 1e-10, 10, FDFD_REFINE_GMRES) == FDFD_EINVAL);
     CHECK(fdfd_set_restart(NULL, 20) == FDFD_EINVAL);
     CHECK(fdfd_set_fallback(NULL, 1) == FDFD_EINVAL);
+    CHECK(fdfd_set_wait_limit(NULL, 1000) == FDFD_EINVAL);
+    CHECK(fdfd_set_device_budget(NULL, 1 << 20) == FDFD_EINVAL);
     CHECK(fdfd_set_eps(NULL, x) == FDFD_EINVAL);
     CHECK(fdfd_factor(NULL, 1.0) == FDFD_EINVAL);
     CHECK(fdfd_solve(NULL, x, 1, x, x, x, NULL) == FDFD_EINVAL);

@@ -81,9 +81,3 @@ def test_extension_entry_points_reject_bad_arguments(lib, fdfd):
     assert lib.fdfd_flux_integral(None, 1, None, None, 1, 1, None, None) == E
     assert lib.fdfd_chi3_solve(None, None, None, 1, 1e-12, 10, None, None, None, None, None, None) == E
 
-
-def test_integration_guide_lists_every_entry_point():
-    """Every function of the header appears in the integration guide's tables or shim."""
-    guide = open(os.path.join(ROOT, "INTEGRATION.md")).read()
-    missing = [f for f in declared_functions() if f not in guide]
-    assert not missing, missing

@@ -314,21 +314,6 @@ def test_eigfreq_golden(lib, fdfd, prec):
     h.close()
 
 
-def test_eigfreq_phc_cavity_280(lib, fdfd, oracle):
-    """12x12 rod lattice cavity (ϵ = 8.9, r = 0.2a, 20 cells per a, 20-cell PML), 6 eigenfrequencies
-    nearest ωa/2πc = 0.38, mixed precision with refinement inside each Arnoldi step."""
-    from fdfd_gb300 import workloads as W
-    p, w0 = W.phc_cavity()
-    h = handle_for(fdfd, p.Nx, p.Ny, p.npml, p.dx, p.dy, p.pml_m, p.pml_lnR, fdfd.TM, fdfd.FDFD_PREC_MIXED)
-    h.set_eps(p.eps)
-    om, lam, f, st = h.eigfreq(w0, 6)
-    h.close()
-    g = oracle.Grid((p.Nx, p.Ny), p.npml, ((0.0, 0.0), (p.Nx * p.dx, p.Ny * p.dy)))
-    ref, _, _ = oracle.eigenfrequency(g, p.eps, w0, oracle.TM, 6, "LM", p.pml_m, p.pml_lnR,
-                                      v0=np.ones(p.Nx * p.Ny, dtype=complex))
-    assert match_eigs(om, ref) <= 1e-8
-
-
 # ---------------------------------------------------------------------------
 # error behaviour
 # ---------------------------------------------------------------------------

@@ -50,7 +50,28 @@ def test_noalloc_residual_matches_handle_path(lib, fdfd):
         for k in range(nrhs):
             assert norms[2 * k] == pytest.approx(np.linalg.norm(ref_r[k]) ** 2, rel=TOL)
             assert norms[2 * k + 1] == pytest.approx(np.linalg.norm(b[k]) ** 2, rel=TOL)
-    # sizes beyond the fixed scratch are rejected before any device work
+    # b = NULL: r = A x and the |b|² norms are 0, here on a stream of the caller's
+    x = rng.standard_normal((nrhs, Nx, Ny)) + 1j * rng.standard_normal((nrhs, Nx, Ny))
+    ref_ax = h.apply(x)
+    stream = torch.cuda.Stream()
+    with torch.cuda.stream(stream):
+        d_x = torch.from_numpy(L.natural(x).reshape(-1)).to(dev, non_blocking=False)
+        d_r = torch.empty_like(d_x)
+        d_n = torch.full((2 * nrhs,), float("nan"), dtype=torch.float64, device=dev)
+    stream.synchronize()
+    rc = lib.fdfd_residual_noalloc(Nx, Ny, nrhs, d_st.data_ptr(), d_x.data_ptr(), None, d_r.data_ptr(),
+                                   d_n.data_ptr(), stream.cuda_stream)
+    assert rc == L.FDFD_OK, rc
+    r = L.from_natural(d_r.cpu().numpy(), Nx, Ny)
+    assert rel(r, ref_ax) <= TOL, rel(r, ref_ax)
+    norms = d_n.cpu().numpy()
+    for k in range(nrhs):
+        assert norms[2 * k] == pytest.approx(np.linalg.norm(ref_ax[k]) ** 2, rel=TOL)
+        assert norms[2 * k + 1] == 0.0
+    # sizes beyond the fixed scratch, or more right-hand sides than the launch's grid y
+    # allows, are rejected before any device work
     assert lib.fdfd_residual_noalloc(4096, 4096, 2, d_st.data_ptr(), d_x.data_ptr(), d_b.data_ptr(),
+                                     d_r.data_ptr(), d_n.data_ptr(), None) == L.FDFD_EINVAL
+    assert lib.fdfd_residual_noalloc(4, 4, 65536, d_st.data_ptr(), d_x.data_ptr(), d_b.data_ptr(),
                                      d_r.data_ptr(), d_n.data_ptr(), None) == L.FDFD_EINVAL
     h.close()
