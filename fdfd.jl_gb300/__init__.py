@@ -515,7 +515,7 @@ def eigenfrequency(d: Device, pol, nev, which="LM", precision="mixed", pml_m=3.5
         flds = np.empty((nev, 3, N), dtype=np.complex128)
         st = _lib.Stats()
         import ctypes as C
-        which_code = {"LM": 0, "LR": 1}[which]
+        which_code = {"LM": 0, "LR": 1, "SM": 2, "SR": 3, "LI": 4, "SI": 5}[str(which).lstrip(":")]
         rc = h.lib.fdfd_eigfreq(h.h, float(d.omega[0]), int(nev), which_code, float(tol), _lib.cptr(om),
                                 _lib.cptr(lam), _lib.cptr(flds), C.byref(st))
         h._check(rc)

@@ -30,7 +30,7 @@ EXPORTS = ["fdfd_version", "fdfd_create", "fdfd_destroy", "fdfd_last_error", "fd
            "fdfd_set_fallback", "fdfd_set_restart", "fdfd_set_wait_limit", "fdfd_set_device_budget", "fdfd_mf_create", "fdfd_mf_set_deps", "fdfd_mf_factor",
            "fdfd_mf_solve", "fdfd_get_mode", "fdfd_mode_sources", "fdfd_poynting", "fdfd_poynting_device",
            "fdfd_flux_integral", "fdfd_chi3_solve",
-           "fdfd_set_eps", "fdfd_factor", "fdfd_solve", "fdfd_solve_device", "fdfd_adjoint", "fdfd_eigfreq",
+           "fdfd_set_eps", "fdfd_factor", "fdfd_solve", "fdfd_solve_device", "fdfd_adjoint", "fdfd_adjoint_vjp", "fdfd_eigfreq",
            "fdfd_get_stencil", "fdfd_apply", "fdfd_set_profiling", "fdfd_get_profile", "fdfd_residual_noalloc",
            "fdfd_debug_hessenberg_eig", "fdfd_debug_gemm"]
 PROF_CLASSES = ["gemm_tc", "gemm_simt", "gj_panel", "sweep", "residual", "other", "gj_update", "level1"]
@@ -131,6 +131,8 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.fdfd_solve_device.argtypes = [vp, C.c_void_p, ip, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(Stats)]
     lib.fdfd_adjoint.restype = ip
     lib.fdfd_adjoint.argtypes = [vp, dp, dp, dp, dp, dp, C.POINTER(Stats)]
+    lib.fdfd_adjoint_vjp.restype = ip
+    lib.fdfd_adjoint_vjp.argtypes = [vp, dp, dp, dp, dp, C.POINTER(Stats)]
     lib.fdfd_eigfreq.restype = ip
     lib.fdfd_eigfreq.argtypes = [vp, C.c_double, ip, ip, C.c_double, dp, dp, dp, C.POINTER(Stats)]
     lib.fdfd_get_stencil.restype = ip
@@ -259,6 +261,17 @@ class Handle:
         st = Stats()
         self._check(self.lib.fdfd_adjoint(self.h, cptr(s), cptr(m), C.byref(J), cptr(grad), cptr(ez), C.byref(st)))
         return J.value, grad.T.copy(), from_natural(ez, self.Nx, self.Ny)[0], st
+
+    def adjoint_vjp(self, src, g):
+        """Pullback of Ez = solve(ϵᵣ) for the conjugated cotangent g = conj(ΔEz):
+        -> (grad (Nx, Ny) = -Re(ω²ϵ₀ λ⊙E) with λ = A⁻ᵀ g, Ez (Nx, Ny), stats)."""
+        s = natural(src)
+        gv = natural(g)
+        grad = np.empty((self.Ny, self.Nx), dtype=np.float64)
+        ez = np.empty_like(s)
+        st = Stats()
+        self._check(self.lib.fdfd_adjoint_vjp(self.h, cptr(s), cptr(gv), cptr(grad), cptr(ez), C.byref(st)))
+        return grad.T.copy(), from_natural(ez, self.Nx, self.Ny)[0], st
 
     def eigfreq(self, omega0, nev, which=0, tol=1e-10):
         """Shift-invert eigenfrequencies -> (omega[nev], lambda[nev], fields (nev, 3, Nx, Ny), stats)."""

@@ -2263,17 +2263,24 @@ int fdfd_apply(fdfd_handle* h, const double* x, int nrhs, double* y) {
     return rc == FDFD_ECUDA ? set_err(h, rc, "fdfd_apply copy failed") : rc;
 }
 
-int fdfd_adjoint(fdfd_handle* h, const double* src, const double* mvec, double* J, double* grad, double* ez,
-                 fdfd_stats* stats) {
+}  // extern "C"
+
+namespace {
+
+// Shared core of fdfd_adjoint (objective form: g = m, the gradient of J = |mᵀE|²)
+// and fdfd_adjoint_vjp (g is the caller's cotangent, grad_k = -Re(ω²ϵ₀ λ_k E_k)).
+int adjoint_core(fdfd_handle* h, const double* src, const double* mvec, bool objective, double* J, double* grad,
+                 double* ez, fdfd_stats* stats) {
+    const char* fn = objective ? "fdfd_adjoint" : "fdfd_adjoint_vjp";
     if (!h) return FDFD_EINVAL;
-    if (h->mf) return set_err(h, FDFD_EINVAL, "fdfd_adjoint: not defined for a modulated device");
-    if (!src || !mvec || !J || !grad) return set_err(h, FDFD_EINVAL, "fdfd_adjoint: NULL argument");
+    if (h->mf) return set_err(h, FDFD_EINVAL, "%s: not defined for a modulated device", fn);
+    if (!src || !mvec || (objective && !J) || !grad) return set_err(h, FDFD_EINVAL, "%s: NULL argument", fn);
     if (!h->factored || h->op != OP_TM_DRIVEN)
-        return set_err(h, FDFD_EINVAL, "fdfd_adjoint needs a factored TM driven operator (fdfd_factor, FDFD_TM)");
+        return set_err(h, FDFD_EINVAL, "%s needs a factored TM driven operator (fdfd_factor, FDFD_TM)", fn);
     auto t0 = std::chrono::steady_clock::now();
     const long long N = (long long)h->Nx * h->Ny;
     if (first_nonfinite(src, 2 * N) >= 0 || first_nonfinite(mvec, 2 * N) >= 0)
-        return set_err(h, FDFD_EINVAL, "fdfd_adjoint: non-finite input");
+        return set_err(h, FDFD_EINVAL, "%s: non-finite input", fn);
     const size_t bytes = (size_t)N * sizeof(cplx<double>);
     RET(ensure_krylov(h, 2, restart_len(h, 2)));
     if (h->io_cap < 4 * bytes) {
@@ -2300,17 +2307,21 @@ int fdfd_adjoint(fdfd_handle* h, const double* src, const double* mvec, double* 
     double rel = 0;
     RET(refine_fb(h, 2, &iters, &rel));
     LAUNCH(pscale_kernel, nb, 256, 0, h->Nx, h->Ny, h->sf, 1, h->kx + N, d_lam);
-    // s = mᵀE (no conjugation), reduced on the host from per-block partials
-    const int nparts = h->num_sms;   // one partial per SM
-    RET(ensure_part(h, 2 * (size_t)nparts));
-    LAUNCH(vdotu_kernel, nparts, 256, 0, N, d_m, h->kx, h->part);
-    std::vector<double> part(2 * (size_t)nparts);
-    CK(cudaMemcpyAsync(part.data(), h->part, part.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
-    CK(cudaStreamSynchronize(h->stream));
     zd s(0, 0);
-    for (int i = 0; i < nparts; ++i) s += zd(part[2 * i], part[2 * i + 1]);
-    // dJ/dϵᵣ_k = -2 Re(conj(s)·ω²ϵ₀·λ_k·E_k)
-    const zd coef = std::conj(s) * (h->omega * h->omega * kEPS0 * h->L0);
+    const double w2e0 = h->omega * h->omega * kEPS0 * h->L0;
+    zd coef(0.5 * w2e0, 0.0);   // vjp: grad_k = -2 Re(½ω²ϵ₀·λ_k·E_k)
+    if (objective) {
+        // s = mᵀE (no conjugation), reduced on the host from per-block partials
+        const int nparts = h->num_sms;   // one partial per SM
+        RET(ensure_part(h, 2 * (size_t)nparts));
+        LAUNCH(vdotu_kernel, nparts, 256, 0, N, d_m, h->kx, h->part);
+        std::vector<double> part(2 * (size_t)nparts);
+        CK(cudaMemcpyAsync(part.data(), h->part, part.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+        for (int i = 0; i < nparts; ++i) s += zd(part[2 * i], part[2 * i + 1]);
+        // dJ/dϵᵣ_k = -2 Re(conj(s)·ω²ϵ₀·λ_k·E_k)
+        coef = std::conj(s) * w2e0;
+    }
     cplx<double> c;
     c.re = coef.real();
     c.im = coef.imag();
@@ -2321,7 +2332,7 @@ int fdfd_adjoint(fdfd_handle* h, const double* src, const double* mvec, double* 
     cudaEventRecord(h->ev[4], h->stream);
     CK(cudaStreamSynchronize(h->stream));
     RET(check_device(h, "adjoint"));
-    *J = std::norm(s);
+    if (J) *J = std::norm(s);
     if (stats) {
         stats->iterations = iters;
         stats->nrhs = 2;
@@ -2347,6 +2358,20 @@ int fdfd_adjoint(fdfd_handle* h, const double* src, const double* mvec, double* 
     return FDFD_OK;
 }
 
+}  // namespace
+
+extern "C" {
+
+int fdfd_adjoint(fdfd_handle* h, const double* src, const double* mvec, double* J, double* grad, double* ez,
+                 fdfd_stats* stats) {
+    return adjoint_core(h, src, mvec, true, J, grad, ez, stats);
+}
+
+int fdfd_adjoint_vjp(fdfd_handle* h, const double* src, const double* g, double* grad, double* ez,
+                     fdfd_stats* stats) {
+    return adjoint_core(h, src, g, false, nullptr, grad, ez, stats);
+}
+
 int fdfd_eigfreq(fdfd_handle* h, double omega0, int nev, int which, double tol, double* omega, double* lambda,
                  double* fields, fdfd_stats* stats) {
     if (!h) return FDFD_EINVAL;
@@ -2355,8 +2380,8 @@ int fdfd_eigfreq(fdfd_handle* h, double omega0, int nev, int which, double tol, 
     if (!h->eps_set) return set_err(h, FDFD_EINVAL, "fdfd_set_eps must be called before fdfd_eigfreq");
     if (!(omega0 > 0) || nev < 1 || nev > 64 || nev >= N - 1 || !omega)
         return set_err(h, FDFD_EINVAL, "fdfd_eigfreq: invalid arguments");
-    if (which != FDFD_WHICH_LM && which != FDFD_WHICH_LR)
-        return set_err(h, FDFD_EINVAL, "fdfd_eigfreq: which must be FDFD_WHICH_LM or FDFD_WHICH_LR");
+    if (which < FDFD_WHICH_LM || which > FDFD_WHICH_SI)
+        return set_err(h, FDFD_EINVAL, "fdfd_eigfreq: which must be one of FDFD_WHICH_LM/LR/SM/SR/LI/SI");
     if (!(tol > 0)) tol = 1e-10;
     auto t0 = std::chrono::steady_clock::now();
     h->launches = 0;
@@ -2398,6 +2423,17 @@ int fdfd_eigfreq(fdfd_handle* h, double omega0, int nev, int which, double tol, 
         CK(cudaMemcpyAsync(V, v0.data(), vbytes, cudaMemcpyHostToDevice, h->stream));
     }
     cudaEventRecord(h->ev[3], h->stream);
+    // ARPACK's `which` in shift-invert mode ranks the eigenvalues θ = 1/(λ - σ) of the operator
+    auto before = [which](const zd& a, const zd& b) {
+        switch (which) {
+            case FDFD_WHICH_LR: return a.real() > b.real();
+            case FDFD_WHICH_SM: return std::abs(a) < std::abs(b);
+            case FDFD_WHICH_SR: return a.real() < b.real();
+            case FDFD_WHICH_LI: return a.imag() > b.imag();
+            case FDFD_WHICH_SI: return a.imag() < b.imag();
+            default: return std::abs(a) > std::abs(b);
+        }
+    };
     std::vector<zd> Hm((size_t)(m + 1) * m, zd(0, 0));
     std::vector<zd> theta, S;
     std::vector<int> pick;
@@ -2412,9 +2448,7 @@ int fdfd_eigfreq(fdfd_handle* h, double omega0, int nev, int which, double tol, 
         if (!hess::eig(kk, Hk, theta, S)) return false;
         std::vector<int> idx(kk);
         for (int i = 0; i < kk; ++i) idx[i] = i;
-        std::sort(idx.begin(), idx.end(), [&](int a, int b) {
-            return which == FDFD_WHICH_LM ? std::abs(theta[a]) > std::abs(theta[b]) : theta[a].real() > theta[b].real();
-        });
+        std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return before(theta[a], theta[b]); });
         pick.assign(idx.begin(), idx.begin() + std::min(nev, kk));
         return true;
     };
@@ -2471,9 +2505,7 @@ int fdfd_eigfreq(fdfd_handle* h, double omega0, int nev, int which, double tol, 
     // eigenvalues of A (λ = σ + 1/θ), eigenfrequencies, Ritz vectors and fields
     std::vector<zd> lam(nev), om(nev);
     std::vector<int> order(pick);
-    std::sort(order.begin(), order.end(), [&](int a, int b) {
-        return which == FDFD_WHICH_LM ? std::abs(theta[a]) > std::abs(theta[b]) : theta[a].real() > theta[b].real();
-    });
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return before(theta[a], theta[b]); });
     for (int q = 0; q < nev; ++q) {
         const zd th = theta[order[q]];
         lam[q] = sigma + 1.0 / th;

@@ -52,8 +52,14 @@ extern "C" {
 #define FDFD_CHI3_NEWTON 1 /* src/solver/nonlinear.jl:5 (IterativeMethodGN=1 IterativeMethodB=2) */
 #define FDFD_CHI3_BORN   2
 
-#define FDFD_WHICH_LM 0    /* eigenvalues of A nearest sigma (ARPACK :LM in shift-invert) */
-#define FDFD_WHICH_LR 1    /* largest real part of 1/(λ-σ) (ARPACK :LR in shift-invert)  */
+/* eigfreq selection, as Arpack's `which` (src/solver/eigen.jl:69,86,104) in
+ * shift-invert mode: it ranks θ = 1/(λ-σ), the eigenvalues of (A - σI)⁻¹ */
+#define FDFD_WHICH_LM 0    /* largest |θ|: eigenvalues of A nearest sigma (:LM)     */
+#define FDFD_WHICH_LR 1    /* largest real part of θ (:LR)                          */
+#define FDFD_WHICH_SM 2    /* smallest |θ|: farthest from sigma (:SM)               */
+#define FDFD_WHICH_SR 3    /* smallest real part of θ (:SR)                         */
+#define FDFD_WHICH_LI 4    /* largest imaginary part of θ (:LI)                     */
+#define FDFD_WHICH_SI 5    /* smallest imaginary part of θ (:SI)                    */
 
 typedef struct fdfd_handle fdfd_handle;
 
@@ -154,13 +160,24 @@ int  fdfd_solve_device(fdfd_handle* h, const double* d_src, int nrhs,
                        fdfd_stats* stats);
 
 /* Adjoint gradient of J = |Σ_k m_k Ez_k|² with respect to real ϵᵣ for the
- * current TM factorization and one source (no counterpart in the reference,
+ * current factorization of a TM driven operator (fdfd_factor on an FDFD_TM
+ * handle; a TE handle is FDFD_EINVAL) and one source (no counterpart in the reference,
  * which has no gradient code).  Solves A E = iω·src and Aᵀ λ = m by reusing
  * the forward factors (P·A is complex symmetric for the diagonal PML scaling
  * P, so Aᵀ = P A P⁻¹), then dJ/dϵᵣ_k = -2 Re(conj(mᵀE)·ω²ϵ₀·λ_k·E_k).
  * Outputs: J (scalar), grad (Nx*Ny doubles), ez (Nx*Ny complex, may be NULL). */
 int  fdfd_adjoint(fdfd_handle* h, const double* src, const double* mvec,
                   double* J, double* grad, double* ez, fdfd_stats* stats);
+
+/* Vector-Jacobian product of the TM solve with respect to real ϵᵣ (no
+ * counterpart in the reference; the pullback of a ChainRulesCore.rrule on
+ * solve): E = A⁻¹(iω·src), λ = A⁻ᵀ g with g (Nx*Ny complex) the conjugated
+ * cotangent of Ez (ChainRules convention: dL = Re(Σ conj(ΔEz)·dEz), so
+ * g = conj(ΔEz)), and grad_k = -Re(ω²ϵ₀·λ_k·E_k) = dL/dϵᵣ_k.  Same
+ * factorization reuse and requirements as fdfd_adjoint, which is this
+ * product for g = 2·conj(mᵀE)·m. */
+int  fdfd_adjoint_vjp(fdfd_handle* h, const double* src, const double* g,
+                      double* grad, double* ez, fdfd_stats* stats);
 
 /* Shift-invert eigenfrequencies (eigenfrequency, src/solver/eigen.jl:69-115):
  * with the PML frozen at omega0, TM finds eigenpairs of

@@ -59,6 +59,7 @@ int main(void) {
     CHECK(fdfd_solve(NULL, x, 1, x, x, x, NULL) == FDFD_EINVAL);
     CHECK(fdfd_solve_device(NULL, x, 1, x, x, x, NULL) == FDFD_EINVAL);
     CHECK(fdfd_adjoint(NULL, x, x, x, x, x, NULL) == FDFD_EINVAL);
+    CHECK(fdfd_adjoint_vjp(NULL, x, x, x, x, NULL) == FDFD_EINVAL);
     CHECK(fdfd_eigfreq(NULL, 1.0, 1, FDFD_WHICH_LM, 1e-10, x, x, x, NULL) == FDFD_EINVAL);
     CHECK(fdfd_get_mode(NULL, 1.0, &mode, 1, x, x, &npts) == FDFD_EINVAL);
     CHECK(fdfd_mode_sources(NULL, 1, x, 1, &mode, x) == FDFD_EINVAL);

@@ -173,3 +173,21 @@ def test_eigfreq_and_fields_vs_oracle(lib, fdfd, oracle, pol, prec):
         ref = phase_normalised(*f_ref[k])
         errs = [rel(a, b) for a, b in zip(got, ref)]
         assert max(errs) <= 1e-8, (q, errs)
+
+
+@pytest.mark.parametrize("which", ["LR", "SR", "LI"])
+def test_eigfreq_which_vs_oracle(lib, fdfd, oracle, which):
+    """Arpack's `which` in shift-invert mode ranks θ = 1/(λ - σ): the selections
+    other than :LM against scipy's ARPACK with the same `which` and shift."""
+    Nx, Ny, npml, dx, eps, w0 = eigen_problem("TM")
+    h = fdfd._lib.Handle(Nx, Ny, npml, npml, dx, dx, 1e-6, 4.0, np.log(1e-8), oracle.TM, fdfd.FDFD_PREC_FP64)
+    h.set_refinement(1e-12, 80)
+    h.set_eps(eps)
+    code = {"LM": 0, "LR": 1, "SM": 2, "SR": 3, "LI": 4, "SI": 5}[which]
+    nev = 3
+    om, lam, f, st = h.eigfreq(w0, nev, which=code, tol=1e-12)
+    h.close()
+    g = oracle.Grid((Nx, Ny), (npml, npml), ((0.0, 0.0), (Nx * dx, Ny * dx)))
+    w_ref, _, _ = oracle.eigenfrequency(g, eps, w0, oracle.TM, nev, which, 4.0, np.log(1e-8),
+                                        v0=np.ones(Nx * Ny, dtype=complex))
+    assert match_eigs(om, w_ref) <= 1e-10
