@@ -632,7 +632,8 @@ def main():
             "class_ms_per_solve": {k: round(v["ms"] / prof_steps, 3) for k, v in prof.items()},
             "dominant_class": max(prof, key=lambda k: prof[k]["ms"])}
     # HBM-bound classes: achieved = algorithmic bytes / device time
-    hbm_units = {"sweep": "factor blocks (re, im planes) read once per sweep + node vectors",
+    hbm_units = {"sweep": "dense factor blocks each product references (re, im planes) and the first step's "
+                          "tridiagonal factors (8b complex + b pivots per node), read once per sweep, + node vectors",
                  "gj_update": "each matrix read and written once per Gauss-Jordan panel (re, im planes)",
                  "level1": "first-step inverses written; two inverses read, three blocks written per survivor"}
     roof_hbm = {}

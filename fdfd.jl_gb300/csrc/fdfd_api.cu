@@ -187,6 +187,7 @@ struct fdfd_handle {
     int tc_used = 0;
     bool use_tc = true;
     bool level1_gj = false;     // invert first-step blocks by Gauss-Jordan instead of the O(b²) kernel
+    bool tri_sweep = true;      // first-step sweep products through the tridiagonal factors, not the dense inverses
     // profiling (CUDA events around launches on the handle's stream)
     struct ProfRec { int cls, e0, e1; double work; };
     bool prof_on = false;
@@ -884,14 +885,37 @@ template <typename T> int gemv(fdfd_handle* h, int tr, int p1, int p2, const T* 
     return FDFD_OK;
 }
 
+// First-step products through the tridiagonal factors (launch_tri_apply):
+// Y = Y0 + alpha·D_k⁻¹ V for the step's eliminated nodes
+template <typename T> int tri_apply(fdfd_handle* h, const T* V, const T* Y0, T* Y, int nrhs, T alpha) {
+    FactorStore<T>& F = store<T>(h);
+    const StepJobs& S = h->sj[1];
+    const int b = h->map.b;
+    int ev = prof_begin(h);
+    int e = launch_tri_apply<T>(h->stream, b, h->map.ld, S.ne, nrhs, J<int>(h, S.elim), F.trifac, F.tripiv, V, Y0, Y,
+                                alpha);
+    // factor workspace (8b complex + b pivots) per node; per node and right-hand side V read,
+    // Y written (and Y0 read) once
+    prof_end(h, ev, FDFD_PROF_SWEEP,
+             (double)S.ne * (8.0 * b * sizeof(cplx<T>) + 4.0 * b + (2.0 + (Y0 ? 1 : 0)) * nrhs * 2.0 * b * sizeof(T)));
+    h->launches++;
+    if (e) return set_err(h, FDFD_ECUDA, "tri_apply launch failed: %s", cudaGetErrorString((cudaError_t)e));
+    return FDFD_OK;
+}
+
 template <typename T> int sweep_impl(fdfd_handle* h, int nrhs) {
     FactorStore<T>& F = store<T>(h);
     const int E = (int)h->steps.size();
+    const bool tri1 = F.trifac && !h->level1_gj && h->tri_sweep;
     // forward
     for (int e = 1; e <= E; ++e) {
         const StepJobs& S = h->sj[e];
-        RET(gemv<T>(h, 0, P_D, P_D, F.rv, F.rv, nullptr, F.xv, J<int4>(h, S.fwd1), J<int2>(h, S.fwd1y), S.ne, S.ne, nrhs,
-                    (T)1));
+        if (e == 1 && tri1) {
+            RET(tri_apply<T>(h, F.rv, nullptr, F.xv, nrhs, (T)1));
+        } else {
+            RET(gemv<T>(h, 0, P_D, P_D, F.rv, F.rv, nullptr, F.xv, J<int4>(h, S.fwd1), J<int2>(h, S.fwd1y), S.ne, S.ne,
+                        nrhs, (T)1));
+        }
         if (e == 1) {
             if (S.nf2) {
                 launch_diag_sweep<T>(h->stream, S.nf2, h->map, h->st, h->scale, nrhs, J<int4>(h, S.dswf), 0,
@@ -919,8 +943,12 @@ template <typename T> int sweep_impl(fdfd_handle* h, int nrhs) {
             launch_diag_sweep<T>(h->stream, S.ne, h->map, h->st, h->scale, nrhs, J<int4>(h, S.dswb), 1,
                                  (const T*)F.xv, F.wv);
             h->launches++;
-            RET(gemv<T>(h, 0, P_D, P_D, F.wv, F.wv, F.xv, F.xv, J<int4>(h, S.bwd1), J<int2>(h, S.bwd1y), S.ne, S.ne, nrhs,
-                        (T)-1));
+            if (tri1) {
+                RET(tri_apply<T>(h, F.wv, F.xv, F.xv, nrhs, (T)-1));
+            } else {
+                RET(gemv<T>(h, 0, P_D, P_D, F.wv, F.wv, F.xv, F.xv, J<int4>(h, S.bwd1), J<int2>(h, S.bwd1y), S.ne, S.ne,
+                            nrhs, (T)-1));
+            }
         } else {
             RET(gemv<T>(h, 1, P_X, P_X, F.xv, F.xv, F.xv, F.xv, J<int4>(h, S.bw), J<int2>(h, S.bwy), S.ne, 2 * S.ne, nrhs,
                         (T)-1));
@@ -1428,6 +1456,8 @@ int fdfd_create(fdfd_handle** out, int Nx, int Ny, int Npx, int Npy, double dx, 
     if (env && env[0] == '1') h->use_tc = false;
     const char* env1 = getenv("FDFD_LEVEL1_GJ");
     if (env1 && env1[0] == '1') h->level1_gj = true;
+    const char* env2 = getenv("FDFD_DENSE_L1_SWEEP");
+    if (env2 && env2[0] == '1') h->tri_sweep = false;
     NodeMap& m = h->map;
     m.Nx = Nx; m.Ny = Ny;
     m.transposed = Nx > Ny ? 1 : 0;

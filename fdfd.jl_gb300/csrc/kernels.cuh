@@ -191,6 +191,13 @@ int launch_gemv(cudaStream_t s, int tr, int njobs, const GemvArgs<T>& g);
 // right-hand sides one launch_gemv call may take for block size b
 template <typename T>
 int gemv_max_rhs(int b);
+// Y[node] = Y0[node] + alpha·D_node⁻¹ V[node] for the first reduction step's
+// nodes jobs[0..njobs) from their tridiagonal factor workspaces (fac, piv as
+// written by launch_tri_inverse, workspace j for jobs[j]).  Y0 may be null or
+// equal to Y.  Returns a cudaError_t value.
+template <typename T>
+int launch_tri_apply(cudaStream_t s, int b, int ld, int njobs, int nrhs, const int* jobs, const cplx<T>* fac,
+                     const int* piv, const T* V, const T* Y0, T* Y, T alpha);
 // r[s] -= u_s ⊙ z[next] + l_s ⊙ z[prev]  (first reduction step, diagonal couplings)
 // mode 0: survivors update r from eliminated neighbours (jobs: L1Job-like int4 (s, prev, next, flags))
 // mode 1: eliminated k: w[k] = l_k ⊙ x[prev] + u_k ⊙ x[next]

@@ -3,6 +3,8 @@
 // They stream every factor block once per sweep, so they are HBM-bound; both
 // kernels issue all of a thread's 16-byte loads for a row (or a group of rows)
 // before the first FMA so that enough bytes are in flight per SM.
+#include <algorithm>
+
 #include "common.cuh"
 #include "kernels.cuh"
 
@@ -258,6 +260,94 @@ __global__ void diag_sweep_kernel(NodeMap m, const cplx<double>* st, double scal
     }
 }
 
+// First-step sweep products y = y0 + alpha·D_k⁻¹ v without the dense inverse:
+// D_k = T0 + corners (the first reduction step's cyclic tridiagonal block) is
+// applied through its stored factorization (tri_factor_kernel's workspace:
+// the xGTTRF factors of T0 and the Sherman-Morrison-Woodbury terms),
+//     D_k⁻¹ v = T0⁻¹ v − z0 (w0·v) − zN (w1·v),
+// with the xGTTRS recurrences for T0⁻¹.  That reads 8b complex factor values
+// per node instead of the b² of the dense inverse.  One warp per node: the
+// node's factors and up to `rc` right-hand sides are staged in shared memory
+// with coalesced loads, lane r runs the serial recurrences of right-hand side
+// r out of shared memory (the dots with the original v are formed in the
+// forward pass), and the warp writes y back coalesced.
+// jobs[j] = node of factor workspace j; grid: njobs, block 32,
+// dynamic smem (8b + rc·b) cplx<T> + b ints
+template <typename T>
+__global__ void __launch_bounds__(32) tri_apply_kernel(int b, int ld, int nrhs, int rc, const int* jobs,
+                                                       const cplx<T>* __restrict__ fac, const int* __restrict__ piv,
+                                                       const T* V, const T* Y0, T* Y, T alpha) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    cplx<T>* sf = reinterpret_cast<cplx<T>*>(smem_raw);      // dl du du2 dinv z0 zN w0 w1
+    cplx<T>* sv = sf + 8 * (size_t)b;                          // rc vectors of b
+    int* sp = reinterpret_cast<int*>(sv + (size_t)rc * b);
+    const int j = blockIdx.x, lane = threadIdx.x;
+    const int node = jobs[j];
+    const cplx<T>* f = fac + (size_t)j * 8 * b;
+    for (int i = lane; i < 8 * b; i += 32) sf[i] = f[i];
+    for (int i = lane; i < b; i += 32) sp[i] = piv[(size_t)j * b + i];
+    const cplx<T>* dl = sf;
+    const cplx<T>* du = sf + b;
+    const cplx<T>* du2 = sf + 2 * b;
+    const cplx<T>* dinv = sf + 3 * b;
+    const cplx<T>* z0 = sf + 4 * b;
+    const cplx<T>* zN = sf + 5 * b;
+    const cplx<T>* w0 = sf + 6 * b;
+    const cplx<T>* w1 = sf + 7 * b;
+    for (int r0 = 0; r0 < nrhs; r0 += rc) {
+        const int nr = min(rc, nrhs - r0);
+        for (int q = 0; q < nr; ++q) {
+            const T* v = V + ((size_t)node * nrhs + r0 + q) * 2 * ld;
+            for (int i = lane; i < b; i += 32) sv[(size_t)q * b + i] = cmk(v[i], v[ld + i]);
+        }
+        __syncwarp();
+        if (lane < nr) {
+            cplx<T>* x = sv + (size_t)lane * b;
+            // L y = P v in place (interchanges between neighbours), dots with the original v
+            cplx<T> xi = x[0];
+            cplx<T> c0 = cmul(w0[0], xi), c1 = cmul(w1[0], xi);
+#pragma unroll 4
+            for (int i = 0; i + 1 < b; ++i) {
+                const cplx<T> xn = x[i + 1];
+                c0 = cadd(c0, cmul(w0[i + 1], xn));
+                c1 = cadd(c1, cmul(w1[i + 1], xn));
+                const cplx<T> l = dl[i];
+                if (sp[i] == i) {
+                    x[i] = xi;
+                    xi = csub(xn, cmul(l, xi));
+                } else {
+                    x[i] = xn;
+                    xi = csub(xi, cmul(l, xn));
+                }
+            }
+            // U x = y, then x − z0 c0 − zN c1, row b-1 first (in place)
+            cplx<T> x1 = cmul(xi, dinv[b - 1]), x2 = cmk((T)0, (T)0);
+            x[b - 1] = csub(csub(x1, cmul(z0[b - 1], c0)), cmul(zN[b - 1], c1));
+#pragma unroll 4
+            for (int i = b - 2; i >= 0; --i) {
+                const cplx<T> xv = cmul(csub(csub(x[i], cmul(du[i], x1)), cmul(du2[i], x2)), dinv[i]);
+                x[i] = csub(csub(xv, cmul(z0[i], c0)), cmul(zN[i], c1));
+                x2 = x1;
+                x1 = xv;
+            }
+        }
+        __syncwarp();
+        for (int q = 0; q < nr; ++q) {
+            const size_t vo = ((size_t)node * nrhs + r0 + q) * 2 * ld;
+            const T* y0 = Y0 ? Y0 + vo : nullptr;
+            T* y = Y + vo;
+            for (int i = lane; i < b; i += 32) {
+                const cplx<T> g = sv[(size_t)q * b + i];
+                T o_r = alpha * g.re, o_i = alpha * g.im;
+                if (y0) { o_r += y0[i]; o_i += y0[ld + i]; }
+                y[i] = o_r;
+                y[ld + i] = o_i;
+            }
+        }
+        __syncwarp();
+    }
+}
+
 namespace {
 template <typename T, int R>
 size_t gemv_smem(int tr, int b) {
@@ -323,6 +413,25 @@ void launch_diag_sweep(cudaStream_t s, int njobs, NodeMap m, const cplx<double>*
                        const int4* jobs, int mode, const T* src, T* dst) {
     diag_sweep_kernel<T><<<dim3(ceil_div(m.b, 256), njobs), 256, 0, s>>>(m, st, scale, nrhs, jobs, mode, src, dst);
 }
+template <typename T>
+int launch_tri_apply(cudaStream_t s, int b, int ld, int njobs, int nrhs, const int* jobs, const cplx<T>* fac,
+                     const int* piv, const T* V, const T* Y0, T* Y, T alpha) {
+    if (njobs == 0 || nrhs == 0) return 0;
+    constexpr size_t kMaxSmem = 200 * 1024;
+    static const cudaError_t attr = cudaFuncSetAttribute(tri_apply_kernel<T>,
+                                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem);
+    if (attr != cudaSuccess) return (int)attr;
+    const size_t fixed = 8 * (size_t)b * sizeof(cplx<T>) + (size_t)b * sizeof(int);
+    const size_t per = (size_t)b * sizeof(cplx<T>);
+    if (fixed + per > kMaxSmem) return (int)cudaErrorInvalidValue;
+    const int rc = (int)std::min<size_t>(std::min(nrhs, 32), (kMaxSmem - fixed) / per);
+    tri_apply_kernel<T><<<njobs, 32, fixed + (size_t)rc * per, s>>>(b, ld, nrhs, rc, jobs, fac, piv, V, Y0, Y, alpha);
+    return (int)cudaGetLastError();
+}
+template int launch_tri_apply<float>(cudaStream_t, int, int, int, int, const int*, const cplx<float>*, const int*,
+                                     const float*, const float*, float*, float);
+template int launch_tri_apply<double>(cudaStream_t, int, int, int, int, const int*, const cplx<double>*, const int*,
+                                      const double*, const double*, double*, double);
 template int launch_gemv<float>(cudaStream_t, int, int, const GemvArgs<float>&);
 template int launch_gemv<double>(cudaStream_t, int, int, const GemvArgs<double>&);
 template int gemv_max_rhs<float>(int);
