@@ -600,7 +600,7 @@ __global__ void __launch_bounds__(512, 1) gj_panel_kernel(Pool<T> M, const int* 
 // reads and writes coalesce.  grid: (ceil(b/128), njobs), block 512
 template <typename T, int NB>
 __global__ void __launch_bounds__(512) gj_rt_kernel(Pool<T> M, const int* slots, Pool<T> RP, const int* rowsrc,
-                                                    int c0) {
+                                                    int c0, int rcw) {
     constexpr int NT = 512, TW = 128;
     constexpr int IT = NB * TW / NT;               // loads per thread
     static_assert((NB * TW) % NT == 0, "tile split");
@@ -613,7 +613,7 @@ __global__ void __launch_bounds__(512) gj_rt_kernel(Pool<T> M, const int* slots,
     const int ld = M.ld;
     const int* rs = rowsrc + (size_t)job * b;
     T* rt = RP.slot(job);
-    const int rc = RP.cols;
+    const int rc = rcw;     // RT columns written (zero beyond the panel)
     const long long pe = RP.plane_elems();
     T la[IT], lb[IT];
 #pragma unroll
@@ -669,7 +669,7 @@ __global__ void __launch_bounds__(512) gj_rt_kernel(Pool<T> M, const int* slots,
 // slots alternate by step parity.  grid: njobs, block 512; requires b <= 128*R.
 template <typename T, int NB, int R>
 __global__ void __launch_bounds__(512, 1) gj_panel_quad_kernel(Pool<T> M, const int* slots, Pool<T> GP, int* perm,
-                                                               int* rowsrc, int c0, unsigned* err) {
+                                                               int* rowsrc, int c0, unsigned* err, GjFuse fz) {
     constexpr int NT = 512, NW = NT / 32, C = NB / 4;
     constexpr int VW = 16 / sizeof(T);
     static_assert(C % VW == 0 && (R & (R - 1)) == 0, "quad tiling");
@@ -865,16 +865,19 @@ __global__ void __launch_bounds__(512, 1) gj_panel_quad_kernel(Pool<T> M, const 
         rsv[u] = i < b ? rsm[i] : 0;
         pv[u] = i < b ? pp[rsv[u]] : 0;
     }
-    // G (b x GP.cols, zero padded): row j of this lane goes to G row lrow[j],
-    // columns [qc*C, qc*C+C) as whole 16-byte vectors; lane 0 of the quad zero-fills
-    // the padding columns [NB, GP.cols)
+    // G (b x NB; the update reads K = NB columns): row j of this lane goes to G row
+    // lrow[j], columns [qc*C, qc*C+C) as whole 16-byte vectors.  Fused super-panels
+    // (fz.fused): the columns start at fz.gcol0 and the row is the super-panel's
+    // input row of this physical row (fz.tot_in, identity when null).
+    const int* tin = fz.tot_in ? fz.tot_in + (size_t)job * b : nullptr;
     {
         T* gp = GP.slot(job);
         const long long pe = GP.plane_elems();
 #pragma unroll
         for (int j = 0; j < R; ++j) {
             if (lrow[j] >= b) continue;
-            const long long o = (long long)lrow[j] * GP.ld;
+            const int grow = fz.fused ? (tin ? tin[row0 + j] : row0 + j) : lrow[j];
+            const long long o = (long long)grow * GP.ld + fz.gcol0;
 #pragma unroll
             for (int v = 0; v < C / VW; ++v) {
                 VT a, c;
@@ -897,18 +900,46 @@ __global__ void __launch_bounds__(512, 1) gj_panel_quad_kernel(Pool<T> M, const 
                     *reinterpret_cast<VT*>(gp + 3 * pe + o + col) = cl;
                 }
             }
-            if (qc == 0)
-                for (int col = NB; col < GP.cols; col += VW) {
-                    const VT z = {};
-                    for (int pl2 = 0; pl2 < GP.planes; ++pl2) *reinterpret_cast<VT*>(gp + pl2 * pe + o + col) = z;
-                }
         }
     }
-    __syncthreads();   // every old perm entry is read before any is overwritten
+    // fused: rowsrc becomes the composed map tot_out[r] = tot_in[rsm[r]] (row of the
+    // super-panel's input matrix that lands at logical row r)
+    if (tin) {
+#pragma unroll
+        for (int u = 0; u < PPT; ++u) {
+            const int i = t + u * NT;
+            if (i < b) rsv[u] = tin[rsv[u]];
+        }
+    }
+    __syncthreads();   // every old perm (and tot_in) entry is read before any is overwritten
 #pragma unroll
     for (int u = 0; u < PPT; ++u) {
         const int i = t + u * NT;
-        if (i < b) { pp[i] = pv[u]; rs[i] = rsv[u]; }
+        if (i < b) {
+            pp[i] = pv[u];
+            rs[i] = rsv[u];
+            if (fz.fused) {
+                fz.inv_out[(size_t)job * b + rsv[u]] = i;
+                rsm[i] = rsv[u];
+            }
+        }
+    }
+    if (fz.fused && fz.gcol0 > 0) {
+        // The earlier sub-panels' G columns of this panel's pivot rows (input rows
+        // tot_out[c0 .. c0+w)): copied to gsub for the pivot-row product, then zeroed
+        // (rows of this panel's pivots take no earlier update).
+        __syncthreads();
+        T* gp = GP.slot(job);
+        const long long pe = GP.plane_elems();
+        T* gs = static_cast<T*>(fz.gsub) + (size_t)job * 2 * NB * GP.cols;
+        const int n = w * fz.gcol0;
+        for (int idx = t; idx < n; idx += NT) {
+            const int jj = idx / fz.gcol0, c = idx % fz.gcol0;
+            const long long o = (long long)rsm[c0 + jj] * GP.ld + c;
+            gs[(size_t)jj * GP.cols + c] = gp[o];
+            gs[(size_t)(NB + jj) * GP.cols + c] = gp[pe + o];
+            for (int pl2 = 0; pl2 < GP.planes; ++pl2) gp[pl2 * pe + o] = (T)0;
+        }
     }
 }
 
@@ -1292,36 +1323,179 @@ static int gj_panel_launch(cudaStream_t s, int njobs, Pool<T> M, const int* slot
 
 template <typename T>
 int launch_gj_panel(cudaStream_t s, int nb, int njobs, Pool<T> M, const int* slots, Pool<T> GP, int* perm,
-                    int* rowsrc, int c0, unsigned* err) {
+                    int* rowsrc, int c0, unsigned* err, GjFuse fz) {
     const bool two = M.rows > 512;
     if (M.rows > 1024) return (int)cudaErrorInvalidValue;
     // lane-quad form: one barrier per column step; four rows per quad up to b = 512,
     // eight (with the half-width panel) up to 1024 in FP32
     constexpr int NB1 = sizeof(T) == 4 ? 32 : 16;
     if (!two && nb == NB1) {
-        gj_panel_quad_kernel<T, NB1, 4><<<njobs, 512, 0, s>>>(M, slots, GP, perm, rowsrc, c0, err);
+        gj_panel_quad_kernel<T, NB1, 4><<<njobs, 512, 0, s>>>(M, slots, GP, perm, rowsrc, c0, err, fz);
         return (int)cudaGetLastError();
     }
     if constexpr (sizeof(T) == 4) {
         if (two && nb == 16) {
-            gj_panel_quad_kernel<T, 16, 8><<<njobs, 512, 0, s>>>(M, slots, GP, perm, rowsrc, c0, err);
+            gj_panel_quad_kernel<T, 16, 8><<<njobs, 512, 0, s>>>(M, slots, GP, perm, rowsrc, c0, err, fz);
             return (int)cudaGetLastError();
         }
     } else {
         // FP64 with eight rows per quad would spill (its per-row scale factors alone take 32
         // registers): the 2-D tiled kernel keeps those in shared memory
+        if (fz.fused) return (int)cudaErrorInvalidValue;   // fused super-panels: lane-quad kernels only
         if (two && nb == 8) return gj_panel_launch<T, 8, 8, 2>(s, njobs, M, slots, GP, perm, rowsrc, c0, err);
     }
     return (int)cudaErrorInvalidValue;
 }
 template <typename T>
 int launch_gj_rt(cudaStream_t s, int nb, int njobs, Pool<T> M, const int* slots, Pool<T> RP, const int* rowsrc,
-                 int c0) {
+                 int c0, int rcw) {
     const dim3 grid(ceil_div(M.rows, 128), njobs);
-    if (nb == 32) gj_rt_kernel<T, 32><<<grid, 512, 0, s>>>(M, slots, RP, rowsrc, c0);
-    else if (nb == 16) gj_rt_kernel<T, 16><<<grid, 512, 0, s>>>(M, slots, RP, rowsrc, c0);
-    else if (nb == 8) gj_rt_kernel<T, 8><<<grid, 512, 0, s>>>(M, slots, RP, rowsrc, c0);
+    if (rcw <= 0 || rcw > RP.cols) rcw = RP.cols;
+    if (nb == 32) gj_rt_kernel<T, 32><<<grid, 512, 0, s>>>(M, slots, RP, rowsrc, c0, rcw);
+    else if (nb == 16) gj_rt_kernel<T, 16><<<grid, 512, 0, s>>>(M, slots, RP, rowsrc, c0, rcw);
+    else if (nb == 8) gj_rt_kernel<T, 8><<<grid, 512, 0, s>>>(M, slots, RP, rowsrc, c0, rcw);
     else return (int)cudaErrorInvalidValue;
+    return (int)cudaGetLastError();
+}
+
+// Pivot rows of sub-panel s >= 1 of a fused super-panel, transposed into RP
+// columns [kp, kp + NB) with kp = s·NB:
+//   RT[n][kp + k] = δ(n − c0, k)                                    n in the panel's columns,
+//                 = [n ∉ [c0q, c0)]·M0[tot[c0 + k]][n] + Σ_{t<kp} gsub[k][t]·RT[n][t]   otherwise,
+// for k < w (zero beyond), M0 the super-panel's input matrix (it starts at column
+// c0q), gsub the earlier G columns of the panel's pivot rows (written by the panel
+// kernel).  The sum applies the earlier sub-panels' update to the pivot rows only,
+// so the super-panel's single update is the only pass over the matrix.  The
+// earlier RT columns of the panel's own columns, RT[n ∈ [c0, c0+w)][t < kp], are
+// then zeroed.  FP32 CUDA-core FMAs: a small correction of b x NB x kp per matrix.
+// grid: (ceil(b/64), njobs), block 256, dynamic smem gj_rs_smem<NB>(kp)
+template <int NB>
+__host__ __device__ constexpr size_t gj_rs_smem_elems(int kp) {
+    // G transposed [t][NB] (re, im), RT tile [64][kp + 1] (re, im), β tile [NB][64] (re, im)
+    return (size_t)2 * NB * kp + (size_t)2 * 64 * (kp + 1) + (size_t)2 * NB * 64;
+}
+template <typename T, int NB>
+__global__ void __launch_bounds__(256) gj_rs_kernel(Pool<T> M, const int* slots, Pool<T> RP, const int* tot,
+                                                    const T* gsub, int kp, int c0, int c0q) {
+    constexpr int TN = 64, NT = 256;
+    constexpr int KG = NB / 4;                       // groups of four k per n pair
+    constexpr int NPT = TN * KG / NT;                // n values per thread (2 for NB = 32, 1 for 16)
+    static_assert(NPT >= 1 && TN * KG % NT == 0, "rs tiling");
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int KP = kp + 1;
+    T* gtr = reinterpret_cast<T*>(smem_raw);         // [t][NB]
+    T* gti = gtr + NB * kp;
+    T* rre = gti + NB * kp;                          // [n][KP]
+    T* rim = rre + TN * KP;
+    T* bre = rim + TN * KP;                          // [k][TN]
+    T* bim = bre + NB * TN;
+    const int b = M.rows, job = blockIdx.y, n0 = blockIdx.x * TN, tid = threadIdx.x;
+    const int w = min(NB, b - c0);
+    const T* gs = gsub + (size_t)job * 2 * NB * RP.cols;
+    T* rt = RP.slot(job);
+    const long long pe = RP.plane_elems();
+    const T* Mre = M.slot(slots[job]);
+    const T* Mim = Mre + M.plane_elems();
+    const int* tj = tot + (size_t)job * b;
+    for (int idx = tid; idx < NB * kp; idx += NT) {
+        const int k = idx / kp, t = idx % kp;
+        gtr[t * NB + k] = gs[(size_t)k * RP.cols + t];
+        gti[t * NB + k] = gs[(size_t)(NB + k) * RP.cols + t];
+    }
+    for (int idx = tid; idx < TN * kp; idx += NT) {
+        const int nn = idx / kp, t = idx % kp, n = n0 + nn;
+        const long long o = (long long)n * RP.ld + t;
+        rre[nn * KP + t] = n < b ? rt[o] : (T)0;
+        rim[nn * KP + t] = n < b ? rt[pe + o] : (T)0;
+    }
+    // β rows of M0 (the pivot rows before the super-panel), coalesced along n
+    for (int idx = tid; idx < NB * TN; idx += NT) {
+        const int k = idx / TN, nn = idx % TN, n = n0 + nn;
+        T a = 0, d = 0;
+        if (k < w && n < b && !(n >= c0q && n < c0 + w)) {
+            const long long o = (long long)tj[c0 + k] * M.ld + n;
+            a = Mre[o];
+            d = Mim[o];
+        }
+        bre[k * TN + nn] = a;
+        bim[k * TN + nn] = d;
+    }
+    __syncthreads();
+    // thread: four consecutive k (one 16-byte G load per plane and t) for NPT values of n
+    const int kg = tid % KG, k0 = 4 * kg;
+    int nl[NPT];
+    T ar[NPT][4], ai[NPT][4];
+#pragma unroll
+    for (int u = 0; u < NPT; ++u) {
+        nl[u] = tid / KG + u * (NT / KG);
+#pragma unroll
+        for (int e = 0; e < 4; ++e) { ar[u][e] = bre[(k0 + e) * TN + nl[u]]; ai[u][e] = bim[(k0 + e) * TN + nl[u]]; }
+    }
+    for (int t = 0; t < kp; ++t) {
+        const float4 gr4 = *reinterpret_cast<const float4*>(gtr + t * NB + k0);
+        const float4 gi4 = *reinterpret_cast<const float4*>(gti + t * NB + k0);
+        const T gr[4] = {gr4.x, gr4.y, gr4.z, gr4.w}, gi[4] = {gi4.x, gi4.y, gi4.z, gi4.w};
+#pragma unroll
+        for (int u = 0; u < NPT; ++u) {
+            const T xr = rre[nl[u] * KP + t], xi = rim[nl[u] * KP + t];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                ar[u][e] = fma(gr[e], xr, fma(-gi[e], xi, ar[u][e]));
+                ai[u][e] = fma(gr[e], xi, fma(gi[e], xr, ai[u][e]));
+            }
+        }
+    }
+#pragma unroll
+    for (int u = 0; u < NPT; ++u) {
+        const int n = n0 + nl[u];
+        if (n >= b) continue;
+        const bool own = n >= c0 && n < c0 + w;   // the panel's own columns: identity
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            const int k = k0 + e;
+            T ore = 0, oim = 0;
+            if (k < w) {
+                if (own) ore = (T)(n - c0 == k ? 1 : 0);
+                else { ore = ar[u][e]; oim = ai[u][e]; }
+            }
+            const long long o = (long long)n * RP.ld + kp + k;
+            rt[o] = ore;
+            rt[pe + o] = oim;
+            if (RP.planes == 4) {
+                rt[2 * pe + o] = (T)tf32_lo((float)ore);
+                rt[3 * pe + o] = (T)tf32_lo((float)oim);
+            }
+        }
+    }
+    // the panel's own rows take no earlier update: zero their earlier RT columns
+    const int z0 = max(c0, n0), z1 = min(c0 + w, min(n0 + TN, b));
+    for (int idx = tid; idx < (z1 > z0 ? (z1 - z0) * kp : 0); idx += NT) {
+        const int n = z0 + idx / kp, t = idx % kp;
+        const long long o = (long long)n * RP.ld + t;
+        for (int pl = 0; pl < RP.planes; ++pl) rt[pl * pe + o] = (T)0;
+    }
+}
+
+template <typename T>
+int launch_gj_rs(cudaStream_t s, int nb, int njobs, Pool<T> M, const int* slots, Pool<T> RP, const int* tot,
+                 const T* gsub, int kp, int c0, int c0q) {
+    if (kp <= 0 || kp + nb > RP.cols) return (int)cudaErrorInvalidValue;
+    const dim3 grid(ceil_div(M.rows, 64), njobs);
+    if (nb == 32) {
+        const size_t smem = gj_rs_smem_elems<32>(kp) * sizeof(T);
+        static const cudaError_t attr = cudaFuncSetAttribute(
+            gj_rs_kernel<T, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(gj_rs_smem_elems<32>(128) * sizeof(T)));
+        if (attr != cudaSuccess) return (int)attr;
+        gj_rs_kernel<T, 32><<<grid, 256, smem, s>>>(M, slots, RP, tot, gsub, kp, c0, c0q);
+    } else if (nb == 16) {
+        const size_t smem = gj_rs_smem_elems<16>(kp) * sizeof(T);
+        static const cudaError_t attr = cudaFuncSetAttribute(
+            gj_rs_kernel<T, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(gj_rs_smem_elems<16>(128) * sizeof(T)));
+        if (attr != cudaSuccess) return (int)attr;
+        gj_rs_kernel<T, 16><<<grid, 256, smem, s>>>(M, slots, RP, tot, gsub, kp, c0, c0q);
+    } else {
+        return (int)cudaErrorInvalidValue;
+    }
     return (int)cudaGetLastError();
 }
 template <typename T>
@@ -1345,8 +1519,8 @@ void launch_mcopy(cudaStream_t s, int njobs, Pool<T> S, Pool<T> Dp, const int3* 
     template void launch_level1_combine<T>(cudaStream_t, int, NodeMap, const cplx<double>*, double, Pool<T>,  \
                                            Pool<T>, const L1Job*);                                           \
     template int launch_gj_panel<T>(cudaStream_t, int, int, Pool<T>, const int*, Pool<T>, int*, int*, int,    \
-                                    unsigned*);                                                              \
-    template int launch_gj_rt<T>(cudaStream_t, int, int, Pool<T>, const int*, Pool<T>, const int*, int);    \
+                                    unsigned*, GjFuse);                                                      \
+    template int launch_gj_rt<T>(cudaStream_t, int, int, Pool<T>, const int*, Pool<T>, const int*, int, int); \
     template void launch_gj_unpermute<T>(cudaStream_t, int, Pool<T>, const int*, Pool<T>, const int*,        \
                                          const int*);                                                       \
     template void launch_madd<T>(cudaStream_t, int, Pool<T>, const int3*);                                    \
@@ -1355,3 +1529,6 @@ void launch_mcopy(cudaStream_t s, int njobs, Pool<T> S, Pool<T> Dp, const int3* 
                                         const int*, cplx<T>*, int*, unsigned*);
 INST(float)
 INST(double)
+// fused super-panels run on the FP32 tensor-core path only
+template int launch_gj_rs<float>(cudaStream_t, int, int, Pool<float>, const int*, Pool<float>, const int*,
+                                 const float*, int, int, int);

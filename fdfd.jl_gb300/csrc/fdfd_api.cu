@@ -37,6 +37,7 @@
 
 #define FDFD_VERSION_STR "fdfd_cuda 0.1.0 (sm_103a)"
 
+
 namespace {
 
 constexpr double kEPS0 = 8.85418782e-12;   // src/types.jl:6
@@ -85,6 +86,8 @@ template <typename T> struct FactorStore {
     int vec_nrhs = 0;
     int* perm = nullptr;
     int* rowsrc = nullptr;      // per-panel composed row exchanges (two sets, panel parity)
+    int* inv = nullptr;         // fused super-panels: inverse of the composed map (two sets)
+    T* gsub = nullptr;          // fused super-panels: earlier G columns of a panel's pivot rows
     int* gj_slots = nullptr;    // 0 .. 2*max_ne-1: GP/RP slot lists of both parities
     cplx<T>* trifac = nullptr;  // first-step tridiagonal factors (8*b per node)
     int* tripiv = nullptr;      // and their interchanges (b per node)
@@ -188,6 +191,9 @@ struct fdfd_handle {
     bool use_tc = true;
     bool level1_gj = false;     // invert first-step blocks by Gauss-Jordan instead of the O(b²) kernel
     bool tri_sweep = true;      // first-step sweep products through the tridiagonal factors, not the dense inverses
+    int gj_fused_k = 0;            // FP32 tensor-core Gauss-Jordan: columns of the panels that share one
+                                   // update (0: one update per panel, the default; FDFD_GJ_FUSED_K)
+    int gj_fused_min = 1;          // ... for batches of at least this many matrices
     // profiling (CUDA events around launches on the handle's stream)
     struct ProfRec { int cls, e0, e1; double work; };
     bool prof_on = false;
@@ -577,7 +583,7 @@ template <typename T> int alloc_pool(fdfd_handle* h, Pool<T>& P, int rows, int c
 
 template <typename T> void free_store(fdfd_handle* h, FactorStore<T>& F) {
     void* bufs[] = {F.D.base, F.C.base, F.X.base, F.GP.base, F.RP.base, F.Tg.base, F.rv, F.xv, F.wv,
-                    F.perm, F.rowsrc, F.gj_slots, F.trifac, F.tripiv};
+                    F.perm, F.rowsrc, F.inv, F.gsub, F.gj_slots, F.trifac, F.tripiv};
     for (void* p : bufs) dev_free(h, p);
     F = FactorStore<T>();
 }
@@ -601,7 +607,10 @@ template <typename T> int alloc_factor_pools(fdfd_handle* h) {
     FactorStore<T>& F = store<T>(h);
     const int b = h->map.b, n = h->map.n, ld = h->map.ld;
     const int planes = 2;   // re, im (the tensor-core GEMM forms the TF32 residuals itself)
-    const int pc = sizeof(T) == 4 ? 32 : panel_nb<T>(b);
+    // panel buffer width: one panel, or (fused super-panels, FP32 tensor-core path) the
+    // gj_fused_k columns of the panels that share one update
+    const bool fused = sizeof(T) == 4 && h->use_tc && h->gj_fused_k > panel_nb<T>(b);
+    const int pc = fused ? (h->gj_fused_k + 31) / 32 * 32 : (sizeof(T) == 4 ? 32 : panel_nb<T>(b));
     RET(alloc_pool<T>(h, F.D, b, b, ld, planes, n));
     RET(alloc_pool<T>(h, F.C, b, b, ld, planes, h->nCslots));
     RET(alloc_pool<T>(h, F.X, b, b, ld, planes, h->nXslots));
@@ -618,6 +627,10 @@ template <typename T> int alloc_factor_pools(fdfd_handle* h) {
     }
     RET(dev_alloc(h, (void**)&F.perm, (size_t)h->max_ne * b * sizeof(int)));
     RET(dev_alloc(h, (void**)&F.rowsrc, (size_t)2 * h->max_ne * b * sizeof(int)));
+    if (fused) {
+        RET(dev_alloc(h, (void**)&F.inv, (size_t)2 * h->max_ne * b * sizeof(int)));
+        RET(dev_alloc(h, (void**)&F.gsub, (size_t)h->max_ne * 2 * panel_nb<T>(b) * pc * sizeof(T)));
+    }
     // largest Gauss-Jordan batch: the eliminated nodes of steps >= 2 (and of step 1
     // when it inverts by Gauss-Jordan), or the final pair's single matrices
     int gj_max = 1;
@@ -675,7 +688,7 @@ int gemm(fdfd_handle* h, int pa, int pb, int pc, const int* a_slot, const int* b
          const int* c_trans_arr, int c_trans, int njobs, int M, int N, int K, T alpha, int beta, int mask_c0,
          int mask_w, int pcin = -1, const int* cin_slot = nullptr,
          const int* row_src = nullptr, int prof_cls = -1, double prof_work = 0.0, cudaStream_t stream = nullptr,
-         int n_off = 0, int skip_c0 = 0, int skip_w = 0, int a_pool_slot0 = 0) {
+         int n_off = 0, int skip_c0 = 0, int skip_w = 0, int a_pool_slot0 = 0, const int* row_dst = nullptr) {
     if (njobs == 0) return FDFD_OK;
     FactorStore<T>& F = store<T>(h);
     if (!stream) stream = h->stream;
@@ -688,6 +701,7 @@ int gemm(fdfd_handle* h, int pa, int pb, int pc, const int* a_slot, const int* b
     g.mask_c0 = mask_c0; g.mask_w = mask_w; g.c_trans = c_trans;
     g.n_off = n_off; g.skip_c0 = skip_c0; g.skip_w = skip_w;
     g.c_trans_arr = nullptr;
+    g.row_dst = row_dst;
     g.err = h->derr;
     g.wait_ns = h->wait_ns;
     const double flops = 8.0 * M * N * K * njobs;
@@ -701,7 +715,7 @@ int gemm(fdfd_handle* h, int pa, int pb, int pc, const int* a_slot, const int* b
         h->tc_used = 1;
         return check_launch(h, "gemm_tc");
     }
-    if (n_off || skip_w) return set_err(h, FDFD_EINVAL, "column windows need the tensor-core GEMM");
+    if (n_off || skip_w || row_dst) return set_err(h, FDFD_EINVAL, "column windows need the tensor-core GEMM");
     g.c_trans_arr = c_trans_arr;
     launch_gemm_simt<T>(stream, njobs, g);
     prof_end(h, ev, prof_cls >= 0 ? prof_cls : FDFD_PROF_GEMM_SIMT, prof_cls >= 0 ? prof_work : flops);
@@ -712,9 +726,13 @@ int gemm(fdfd_handle* h, int pa, int pb, int pc, const int* a_slot, const int* b
 // ---------------------------------------------------------------------------
 // Gauss-Jordan inversion of D-pool slots (batched)
 // ---------------------------------------------------------------------------
+int gj_invert_fused(fdfd_handle* h, const int* d_slots, const int* d_iota, int njobs);
+
 template <typename T> int gj_invert(fdfd_handle* h, const int* d_slots, const int* d_iota, int njobs) {
     if (njobs == 0) return FDFD_OK;
     FactorStore<T>& F = store<T>(h);
+    if constexpr (sizeof(T) == 4)
+        if (F.tc_ok && F.inv && njobs >= h->gj_fused_min) return gj_invert_fused(h, d_slots, d_iota, njobs);
     const int b = h->map.b;
     const int nb = panel_nb<T>(b);
     if (njobs > F.Tg.count) return set_err(h, FDFD_EINVAL, "Gauss-Jordan batch %d exceeds %lld", njobs, F.Tg.count);
@@ -746,7 +764,8 @@ template <typename T> int gj_invert(fdfd_handle* h, const int* d_slots, const in
         int* rs = F.rowsrc + (size_t)par * h->max_ne * b;
         const int* pslots = F.gj_slots + par * h->max_ne;   // GP/RP slots of this parity
         int ev = prof_begin(h);
-        int e = launch_gj_panel<T>(h->stream, nb, njobs, pool_of(F, cur), cur_slots, GPp, F.perm, rs, c0, h->derr);
+        int e = launch_gj_panel<T>(h->stream, nb, njobs, pool_of(F, cur), cur_slots, GPp, F.perm, rs, c0, h->derr,
+                                   GjFuse{});
         h->launches++;
         if (e) return set_err(h, FDFD_ECUDA, "gj_panel launch failed: %s", cudaGetErrorString((cudaError_t)e));
         // Rᵀ reads the pivot rows in full: the previous panel's wide update, which ran
@@ -755,7 +774,7 @@ template <typename T> int gj_invert(fdfd_handle* h, const int* d_slots, const in
             CK(cudaStreamWaitEvent(h->stream, h->ev_wide, 0));
             wide_pending = false;
         }
-        e = launch_gj_rt<T>(h->stream, nb, njobs, pool_of(F, cur), cur_slots, RPp, rs, c0);
+        e = launch_gj_rt<T>(h->stream, nb, njobs, pool_of(F, cur), cur_slots, RPp, rs, c0, nb);
         prof_end(h, ev, FDFD_PROF_GJ_PANEL, 0.0);
         h->launches++;
         if (e) return set_err(h, FDFD_ECUDA, "gj_rt launch failed: %s", cudaGetErrorString((cudaError_t)e));
@@ -763,16 +782,16 @@ template <typename T> int gj_invert(fdfd_handle* h, const int* d_slots, const in
         if (overlap && p + 1 < npan) {
             const int c1 = c0 + nb, w1 = std::min(nb, b - c1);
             CK(cudaEventRecord(h->ev_panel, h->stream));
-            RET(gemm<T>(h, P_GP, P_RP, alt, pslots, pslots, alt_slots, nullptr, 0, njobs, b, w1, F.GP.cols, (T)1, 1,
+            RET(gemm<T>(h, P_GP, P_RP, alt, pslots, pslots, alt_slots, nullptr, 0, njobs, b, w1, nb, (T)1, 1,
                         c0, w, cur, cur_slots, rs, FDFD_PROF_GJ_UPDATE, ubytes * w1 / b, h->stream, c1));
             CK(cudaStreamWaitEvent(h->stream2, h->ev_panel, 0));
-            RET(gemm<T>(h, P_GP, P_RP, alt, pslots, pslots, alt_slots, nullptr, 0, njobs, b, b, F.GP.cols, (T)1, 1,
+            RET(gemm<T>(h, P_GP, P_RP, alt, pslots, pslots, alt_slots, nullptr, 0, njobs, b, b, nb, (T)1, 1,
                         c0, w, cur, cur_slots, rs, FDFD_PROF_GJ_UPDATE, ubytes * (b - w1) / b, h->stream2, 0, c1,
                         w1));
             CK(cudaEventRecord(h->ev_wide, h->stream2));
             wide_pending = true;
         } else {
-            RET(gemm<T>(h, P_GP, P_RP, alt, pslots, pslots, alt_slots, nullptr, 0, njobs, b, b, F.GP.cols, (T)1, 1,
+            RET(gemm<T>(h, P_GP, P_RP, alt, pslots, pslots, alt_slots, nullptr, 0, njobs, b, b, nb, (T)1, 1,
                         c0, w, cur, cur_slots, rs, FDFD_PROF_GJ_UPDATE, ubytes));
         }
         std::swap(cur, alt);
@@ -780,6 +799,112 @@ template <typename T> int gj_invert(fdfd_handle* h, const int* d_slots, const in
     }
     if (wide_pending) CK(cudaStreamWaitEvent(h->stream, h->ev_wide, 0));
     launch_gj_unpermute<T>(h->stream, njobs, pool_of(F, cur), cur_slots, F.D, d_slots, F.perm);
+    h->launches++;
+    return check_launch(h, "gj_unpermute");
+}
+
+// Fused super-panels (FP32 tensor-core path, FDFD_GJ_FUSED_K = 64 or 128; off by
+// default: on the 800 x 480 workload K = 64 saved 0.7 ms of the 26.7 ms factor but
+// its rounding took FGMRES from 8 to 9 iterations, +1.3 ms).  The S = K / nb panels of
+// a super-panel share one rank-(S·nb) update of the matrix, so each matrix is
+// read and written once per super-panel instead of once per panel.  With M0 the
+// super-panel's input matrix, P the composed row exchanges of its panels so far
+// and J their columns, the matrix after them is
+//     M = mask_J(P M0) + P·Ĝ·R,
+// where Ĝ holds the panels' G columns in M0's row order (each panel writes its
+// rows there, so no earlier column is ever permuted; its pivot rows' earlier
+// columns are zeroed) and R their pivot rows.  A later panel's pivot rows are
+// formed from M0 and the earlier G and R (gj_rs), the next panel's columns by a
+// narrow product (K = panels so far × nb), and the rest of the matrix by one
+// wide product at the end; both GEMMs scatter the rows of Ĝ·R to their logical
+// places (row_dst = P's inverse) and read β from M0 directly.  Look-ahead (not
+// while profiling): the wide product runs on the second stream, overlapping the
+// next super-panel's first panel; the panel buffers and maps alternate by
+// super-panel parity.
+int gj_invert_fused(fdfd_handle* h, const int* d_slots, const int* d_iota, int njobs) {
+    FactorStore<float>& F = h->f32;
+    const int b = h->map.b;
+    const int nb = panel_nb<float>(b);
+    const int S = F.GP.cols / nb;
+    if (njobs > F.Tg.count) return set_err(h, FDFD_EINVAL, "Gauss-Jordan batch %d exceeds %lld", njobs, F.Tg.count);
+    launch_perm_init(h->stream, njobs, F.perm, b);
+    h->launches++;
+    const bool overlap = !h->prof_on && h->stream2;
+    const int npan = ceil_div(b, nb), nsup = ceil_div(npan, S);
+    int cur = P_D, alt = P_TG;
+    const int* cur_slots = d_slots;
+    const int* alt_slots = d_iota;
+    bool wide_pending = false;
+    const double ubytes = 4.0 * sizeof(float) * (double)b * b * njobs;   // each matrix read and written once
+    for (int q = 0; q < nsup; ++q) {
+        const int par = overlap ? (q & 1) : 0;
+        Pool<float> GPq = F.GP, RPq = F.RP;
+        GPq.base += (size_t)par * h->max_ne * F.GP.slot_elems();
+        RPq.base += (size_t)par * h->max_ne * F.RP.slot_elems();
+        int* tot = F.rowsrc + (size_t)par * h->max_ne * b;
+        int* inv = F.inv + (size_t)par * h->max_ne * b;
+        const int* pslots = F.gj_slots + par * h->max_ne;   // GP/RP slots of this parity
+        const int p0 = q * S, pans = std::min(S, npan - p0), c0q = p0 * nb;
+        for (int si = 0; si < pans; ++si) {
+            const int c0 = (p0 + si) * nb, kp = si * nb, K = kp + nb;
+            GjFuse fz;
+            fz.fused = 1;
+            fz.gcol0 = kp;
+            fz.tot_in = si == 0 ? nullptr : tot;
+            fz.inv_out = inv;
+            fz.gsub = F.gsub;
+            // the panel reads its columns of the matrix after the previous panels: the
+            // super-panel's input for the first, the narrow product's output after that
+            int ev = prof_begin(h);
+            int e = launch_gj_panel<float>(h->stream, nb, njobs, pool_of(F, si == 0 ? cur : alt),
+                                           si == 0 ? cur_slots : alt_slots, GPq, F.perm, tot, c0, h->derr, fz);
+            h->launches++;
+            if (e) return set_err(h, FDFD_ECUDA, "gj_panel launch failed: %s", cudaGetErrorString((cudaError_t)e));
+            if (si == 0) {
+                // pivot rows in full: the previous super-panel's wide product must have finished
+                if (wide_pending) {
+                    CK(cudaStreamWaitEvent(h->stream, h->ev_wide, 0));
+                    wide_pending = false;
+                }
+                e = launch_gj_rt<float>(h->stream, nb, njobs, pool_of(F, cur), cur_slots, RPq, tot, c0, nb);
+            } else {
+                e = launch_gj_rs<float>(h->stream, nb, njobs, pool_of(F, cur), cur_slots, RPq, tot, F.gsub, kp, c0,
+                                        c0q);
+            }
+            prof_end(h, ev, FDFD_PROF_GJ_PANEL, 0.0);
+            h->launches++;
+            if (e) return set_err(h, FDFD_ECUDA, "gj pivot-row launch failed: %s", cudaGetErrorString((cudaError_t)e));
+            const bool last = si == pans - 1;
+            const int c1 = c0 + nb, w1 = std::min(nb, b - c1);
+            const bool has_next = c1 < b;
+            if (has_next && (!last || overlap)) {
+                // the next panel's columns, on the main stream
+                RET(gemm<float>(h, P_GP, P_RP, alt, pslots, pslots, alt_slots, nullptr, 0, njobs, b, w1, K, 1.0f, 1,
+                                c0q, K, cur, cur_slots, nullptr, FDFD_PROF_GJ_UPDATE, ubytes * w1 / b, h->stream, c1,
+                                0, 0, 0, inv));
+            }
+            if (last) {
+                if (has_next && overlap) {
+                    // every other column on the second stream, overlapping the next panel
+                    CK(cudaEventRecord(h->ev_panel, h->stream));
+                    CK(cudaStreamWaitEvent(h->stream2, h->ev_panel, 0));
+                    RET(gemm<float>(h, P_GP, P_RP, alt, pslots, pslots, alt_slots, nullptr, 0, njobs, b, b, K, 1.0f, 1,
+                                    c0q, K, cur, cur_slots, nullptr, FDFD_PROF_GJ_UPDATE, ubytes * (b - w1) / b,
+                                    h->stream2, 0, c1, w1, 0, inv));
+                    CK(cudaEventRecord(h->ev_wide, h->stream2));
+                    wide_pending = true;
+                } else {
+                    RET(gemm<float>(h, P_GP, P_RP, alt, pslots, pslots, alt_slots, nullptr, 0, njobs, b, b, K, 1.0f, 1,
+                                    c0q, K, cur, cur_slots, nullptr, FDFD_PROF_GJ_UPDATE, ubytes, h->stream, 0, 0, 0,
+                                    0, inv));
+                }
+            }
+        }
+        std::swap(cur, alt);
+        std::swap(cur_slots, alt_slots);
+    }
+    if (wide_pending) CK(cudaStreamWaitEvent(h->stream, h->ev_wide, 0));
+    launch_gj_unpermute<float>(h->stream, njobs, pool_of(F, cur), cur_slots, F.D, d_slots, F.perm);
     h->launches++;
     return check_launch(h, "gj_unpermute");
 }
@@ -1458,6 +1583,8 @@ int fdfd_create(fdfd_handle** out, int Nx, int Ny, int Npx, int Npy, double dx, 
     if (env1 && env1[0] == '1') h->level1_gj = true;
     const char* env2 = getenv("FDFD_DENSE_L1_SWEEP");
     if (env2 && env2[0] == '1') h->tri_sweep = false;
+    if (const char* e = getenv("FDFD_GJ_FUSED_K")) h->gj_fused_k = std::max(0, atoi(e));
+    if (const char* e = getenv("FDFD_GJ_FUSED_MIN")) h->gj_fused_min = std::max(1, atoi(e));
     NodeMap& m = h->map;
     m.Nx = Nx; m.Ny = Ny;
     m.transposed = Nx > Ny ? 1 : 0;
@@ -2681,7 +2808,7 @@ int debug_gemm_impl(int M, int N, int K, const double* A, const double* B, doubl
         g.a_slot = g.b_slot = g.c_slot = slots;
         g.Cin = Pool<T>(); g.cin_slot = nullptr; g.row_src = nullptr;
         g.M = M; g.N = N; g.K = K; g.alpha = (T)1; g.beta = 0; g.mask_c0 = 0; g.mask_w = 0;
-        g.c_trans = 0; g.c_trans_arr = nullptr; g.err = derr; g.wait_ns = 0;
+        g.c_trans = 0; g.c_trans_arr = nullptr; g.row_dst = nullptr; g.err = derr; g.wait_ns = 0;
         g.n_off = 0; g.skip_c0 = 0; g.skip_w = 0;
         cudaEvent_t e0, e1;
         cudaEventCreate(&e0); cudaEventCreate(&e1);

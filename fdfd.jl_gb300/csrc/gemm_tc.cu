@@ -286,7 +286,8 @@ __global__ void __launch_bounds__(TcTile<BN>::THREADS, BN <= 64 ? 2 : 1)
             const int r = m0 + q * 32 + lane;
             const int nlo = n0 + g.n_off + part * PCOLS;
             const int ncols = min(min(PCOLS, cild - nlo), g.n_off + g.N - nlo);
-            const bool mrow = (r >= g.mask_c0 && r < g.mask_c0 + g.mask_w);
+            const int rd = (g.row_dst && r < g.M) ? g.row_dst[(long long)job * g.M + r] : r;   // output row
+            const bool mrow = (rd >= g.mask_c0 && rd < g.mask_c0 + g.mask_w);
             if (r < g.M && !mrow && ncols > 0) {
                 const float* src = Ci + (long long)(rsrc ? rsrc[r] : r) * cild + nlo;
                 l2_prefetch(src, (uint32_t)ncols * 4u);
@@ -342,15 +343,19 @@ __global__ void __launch_bounds__(TcTile<BN>::THREADS, BN <= 64 ? 2 : 1)
             const long long cipe = sep ? g.Cin.plane_elems() : pe;
             const long long cild = sep ? (long long)g.Cin.ld : ld;
             const int* rsrc = (sep && g.row_src) ? g.row_src + (long long)job * g.M : nullptr;
+            const int* rdst = g.row_dst ? g.row_dst + (long long)job * g.M : nullptr;
             const uint32_t lane_off = (uint32_t)(q * 32) << 16;
             // per-warp staging tile (the pipeline buffers are idle once the accumulator is final)
             float* stg = reinterpret_cast<float*>(smem) + (warp - 2) * (2 * 32 * 36);
-            // β-source row offsets of the 8 rows this lane reads in the row-major epilogue
+            // β-source row offsets and output rows of the 8 rows this lane handles in the
+            // row-major epilogue
             long long srow[8];
+            int drow[8];
 #pragma unroll
             for (int it = 0; it < 8; ++it) {
                 const int r = row0 + 4 * it + (lane >> 3);
                 srow[it] = (long long)(rsrc && r < g.M ? rsrc[r] : r) * cild;
+                drow[it] = (rdst && r < g.M) ? rdst[r] : r;
             }
             for (int ch = part * (PCOLS / 32); ch < (part + 1) * (PCOLS / 32); ++ch) {
                 const int nb = n0 + ch * 32;
@@ -403,7 +408,7 @@ __global__ void __launch_bounds__(TcTile<BN>::THREADS, BN <= 64 ? 2 : 1)
                         const int r = row0 + 4 * it + sub;
                         cre[it] = make_float4(0.f, 0.f, 0.f, 0.f);
                         cim[it] = cre[it];
-                        const bool mrow = (r >= g.mask_c0 && r < g.mask_c0 + g.mask_w);
+                        const bool mrow = (drow[it] >= g.mask_c0 && drow[it] < g.mask_c0 + g.mask_w);
                         if (g.beta && r < g.M && !mrow) {
                             const long long off = srow[it] + na;
                             if (full4) {
@@ -425,7 +430,8 @@ __global__ void __launch_bounds__(TcTile<BN>::THREADS, BN <= 64 ? 2 : 1)
                         const int rl = 4 * it + sub;
                         const int r = row0 + rl;
                         if (r >= g.M) continue;
-                        const bool mrow = (r >= g.mask_c0 && r < g.mask_c0 + g.mask_w);
+                        const int rd = drow[it];
+                        const bool mrow = (rd >= g.mask_c0 && rd < g.mask_c0 + g.mask_w);
                         const float4 sr = *reinterpret_cast<const float4*>(&stg[rl * 36 + 4 * cq]);
                         const float4 si = *reinterpret_cast<const float4*>(&stg[32 * 36 + rl * 36 + 4 * cq]);
                         const float* srp = reinterpret_cast<const float*>(&sr);
@@ -440,7 +446,7 @@ __global__ void __launch_bounds__(TcTile<BN>::THREADS, BN <= 64 ? 2 : 1)
                             xr[e] = g.alpha * srp[e] + (keep ? crp[e] : 0.f);
                             xi[e] = g.alpha * sip[e] + (keep ? cip[e] : 0.f);
                         }
-                        const long long off = (long long)r * ld + na;
+                        const long long off = (long long)rd * ld + na;
                         if (full4) {
                             *reinterpret_cast<float4*>(C + off) = make_float4(xr[0], xr[1], xr[2], xr[3]);
                             *reinterpret_cast<float4*>(C + pe + off) = make_float4(xi[0], xi[1], xi[2], xi[3]);
@@ -541,7 +547,8 @@ int tc_gemm_launch_maps(const GemmArgs<float>* g, const int* c_trans_arr, const 
 int tc_pick_bn(int M, int N, int K, int njobs, int num_sms) {
     const long long mt = (M + BM - 1) / BM;
     auto tiles = [&](int bn) { return mt * ((N + bn - 1) / bn) * njobs; };
-    if (tiles(256) >= num_sms) return 256;
-    if (tiles(128) >= num_sms) return 128;
+    // no wider than the product (a narrow column window would idle most of a wide tile)
+    if (N > 128 && tiles(256) >= num_sms) return 256;
+    if (N > 64 && tiles(128) >= num_sms) return 128;
     return 64;
 }

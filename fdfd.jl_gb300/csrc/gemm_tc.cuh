@@ -25,8 +25,8 @@ bool tc_make_maps(const Pool<float>* D, const Pool<float>* C, const Pool<float>*
 int tc_gemm_launch_maps(const GemmArgs<float>* g, const int* c_trans_arr, const CUtensorMap* mapA,
                         const CUtensorMap* mapB, int bn, int njobs, cudaStream_t stream);
 
-// Tile width for a launch: the widest tile (256, 128 or 64 columns) whose tile
-// count still covers num_sms.
+// Tile width for a launch: the widest tile (256, 128 or 64 columns, no wider
+// than the product needs) whose tile count still covers num_sms.
 int tc_pick_bn(int M, int N, int K, int njobs, int num_sms);
 
 inline int tc_gemm_launch(const GemmArgs<float>* g, const int* c_trans_arr, int pa, int pb, int njobs,

@@ -89,18 +89,40 @@ void launch_perm_init(cudaStream_t s, int njobs, int* perm, int b);
 template <typename T>
 void launch_tri_inverse(cudaStream_t s, int njobs, NodeMap m, const cplx<double>* st, double scale, Pool<T> D,
                         const int* nodes, cplx<T>* fac, int* piv, unsigned* err);
+// Fused super-panels of the Gauss-Jordan inversion (FP32 tensor-core path):
+// several consecutive panels share one rank-(panels x nb) update of the matrix.
+// Their G columns are kept in the row order of the super-panel's input matrix
+// M0, so no earlier column is ever permuted; rowsrc carries the composed map
+// tot[r] (row of M0 that lands at logical row r) and inv_out its inverse.
+struct GjFuse {
+    int fused;             // 0: single-panel form (the fields below unused)
+    int gcol0;             // first GP column of this panel (sub-panel index x nb)
+    const int* tot_in;     // composed map before this panel (per job b), null: identity
+    int* inv_out;          // per job b: inv_out[tot_out[r]] = r
+    void* gsub;            // per job 2 x nb x GP.cols: earlier G columns of the pivot rows (re | im)
+};
+
 // Gauss-Jordan panel step with panel width nb on the matrices M[slots[job]]
 // (returns a cudaError_t value).  Writes the panel transformation to GP,
 // updates perm and writes rowsrc[job][r], the row of M that lands at row r
-// after this panel's interchanges.
+// after this panel's interchanges (fused: of the super-panel's input matrix).
 template <typename T>
 int launch_gj_panel(cudaStream_t s, int nb, int njobs, Pool<T> M, const int* slots, Pool<T> GP, int* perm,
-                    int* rowsrc, int c0, unsigned* err);
-// The panel's transposed pivot rows (identity on the panel columns) into RP,
-// read from M through rowsrc; M must hold the rows after the previous update.
+                    int* rowsrc, int c0, unsigned* err, GjFuse fz);
+// The panel's transposed pivot rows (identity on the panel columns) into RP
+// columns [0, rcw) (zero beyond the panel; rcw <= 0: all of RP.cols), read
+// from M through rowsrc; M must hold the rows after the previous update.
 template <typename T>
 int launch_gj_rt(cudaStream_t s, int nb, int njobs, Pool<T> M, const int* slots, Pool<T> RP, const int* rowsrc,
-                 int c0);
+                 int c0, int rcw);
+// Pivot rows of a later sub-panel of a fused super-panel into RP columns
+// [kp, kp+nb): M0's rows through tot (masked on the super-panel's earlier
+// columns [c0q, c0)) plus the earlier sub-panels' update of those rows (gsub
+// times RP columns [0, kp)); identity on the panel's columns [c0, c0+nb), whose
+// earlier RP columns are zeroed.  nb = 16 or 32.  Returns a cudaError_t value.
+template <typename T>
+int launch_gj_rs(cudaStream_t s, int nb, int njobs, Pool<T> M, const int* slots, Pool<T> RP, const int* tot,
+                 const T* gsub, int kp, int c0, int c0q);
 // Dst[dslots[job]][r][perm[j]] = Src[sslots[job]][r][j] (Src may equal Dst)
 template <typename T>
 void launch_gj_unpermute(cudaStream_t s, int njobs, Pool<T> Src, const int* sslots, Pool<T> Dst,
@@ -142,7 +164,7 @@ void launch_flux_lines(cudaStream_t s, int nlines, int Nx, int pol, double dy, c
 
 // ---- gemm_simt.cu / gemm_tc.cu --------------------------------------------
 // Batched complex "TN" GEMM on planar pools:
-//   C[m][n] = beta(m,n)·Cin[src(m)][n] + alpha·Σ_k A[m][k]·B[n][k]
+//   C[dst(m)][n] = beta(dst(m),n)·Cin[src(m)][n] + alpha·Σ_k A[m][k]·B[n][k]
 // with A, B, C row-major slots; beta(m,n) = beta unless m or n lies in
 // [mask_c0, mask_c0 + mask_w), where it is 0; c_trans stores Cᵀ instead.
 // Cin is C itself (src(m) = m) unless Cin.base is set; then src(m) =
@@ -161,6 +183,11 @@ template <typename T> struct GemmArgs {
     int n_off, skip_c0, skip_w;
     int c_trans;
     const int* c_trans_arr;   // per-job override of c_trans (device, may be null)
+    // tensor-core kernel only (N-form C, Cin set): when set, A row m is output row
+    // row_dst[job*M + m] (the β term is read from Cin row m, and the row mask tests
+    // the output row) -- the fused Gauss-Jordan updates, whose G rows stay in the
+    // order of the super-panel's input matrix
+    const int* row_dst;
     unsigned* err;
     // tensor-core kernel only: limit of each pipeline wait in ns of %globaltimer
     // (0: FDFD_WAIT_LIMIT_NS); the drain waits before exit always take the full limit
