@@ -31,7 +31,8 @@ EXPORTS = ["fdfd_version", "fdfd_create", "fdfd_destroy", "fdfd_last_error", "fd
            "fdfd_mf_solve", "fdfd_get_mode", "fdfd_mode_sources", "fdfd_poynting", "fdfd_poynting_device",
            "fdfd_flux_integral", "fdfd_chi3_solve",
            "fdfd_set_eps", "fdfd_factor", "fdfd_solve", "fdfd_solve_device", "fdfd_adjoint", "fdfd_adjoint_vjp", "fdfd_eigfreq",
-           "fdfd_get_stencil", "fdfd_apply", "fdfd_set_profiling", "fdfd_get_profile", "fdfd_residual_noalloc",
+           "fdfd_batch_create", "fdfd_batch_factor", "fdfd_batch_stats", "fdfd_batch_last_error",
+           "fdfd_batch_destroy", "fdfd_autotune", "fdfd_get_tuning", "fdfd_get_stencil", "fdfd_apply", "fdfd_set_profiling", "fdfd_get_profile", "fdfd_residual_noalloc",
            "fdfd_debug_hessenberg_eig", "fdfd_debug_gemm"]
 PROF_CLASSES = ["gemm_tc", "gemm_simt", "gj_panel", "sweep", "residual", "other", "gj_update", "level1"]
 
@@ -135,6 +136,20 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.fdfd_adjoint_vjp.argtypes = [vp, dp, dp, dp, dp, C.POINTER(Stats)]
     lib.fdfd_eigfreq.restype = ip
     lib.fdfd_eigfreq.argtypes = [vp, C.c_double, ip, ip, C.c_double, dp, dp, dp, C.POINTER(Stats)]
+    lib.fdfd_batch_create.restype = ip
+    lib.fdfd_batch_create.argtypes = [C.POINTER(vp), ip, C.POINTER(vp)]
+    lib.fdfd_batch_factor.restype = ip
+    lib.fdfd_batch_factor.argtypes = [vp, dp, C.POINTER(C.c_int)]
+    lib.fdfd_batch_stats.restype = ip
+    lib.fdfd_batch_stats.argtypes = [vp, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong), dp]
+    lib.fdfd_batch_last_error.restype = C.c_char_p
+    lib.fdfd_batch_last_error.argtypes = [vp]
+    lib.fdfd_batch_destroy.restype = None
+    lib.fdfd_batch_destroy.argtypes = [vp]
+    lib.fdfd_autotune.restype = ip
+    lib.fdfd_autotune.argtypes = [vp]
+    lib.fdfd_get_tuning.restype = ip
+    lib.fdfd_get_tuning.argtypes = [vp, C.c_char_p, ip]
     lib.fdfd_get_stencil.restype = ip
     lib.fdfd_get_stencil.argtypes = [vp, dp]
     lib.fdfd_apply.restype = ip
@@ -227,6 +242,18 @@ class Handle:
     def set_device_budget(self, nbytes=0):
         """Device bytes the handle may hold (0: no limit); beyond it allocations fail with FDFD_ENOMEM."""
         self._check(self.lib.fdfd_set_device_budget(self.h, int(nbytes)))
+
+    def autotune(self):
+        """Time the candidate launch shapes of this handle's GEMMs and sweep products and keep the
+        fastest; overwrites the factor storage.  Returns the record of the choices (text)."""
+        self._check(self.lib.fdfd_autotune(self.h))
+        return self.tuning()
+
+    def tuning(self):
+        n = self.lib.fdfd_get_tuning(self.h, None, 0)
+        buf = C.create_string_buffer(n + 1)
+        self.lib.fdfd_get_tuning(self.h, buf, n + 1)
+        return buf.value.decode()
 
     def set_eps(self, eps):
         buf = natural(eps)
@@ -433,3 +460,45 @@ def debug_gemm(A, B, precision=FDFD_PREC_MIXED, use_tc=1):
     if rc != FDFD_OK:
         raise FDFDError(rc, "fdfd_debug_gemm failed")
     return Cm, ms.value
+
+
+class Batch:
+    """Handles factored together: one CUDA graph launch per fdfd_batch_factor after the first
+    call (which factors them one by one and captures the graph).  The handles must outlive it."""
+
+    def __init__(self, handles):
+        self.lib = load()
+        self.handles = list(handles)
+        self.b = C.c_void_p()
+        arr = (C.c_void_p * len(self.handles))(*[h.h for h in self.handles])
+        rc = self.lib.fdfd_batch_create(C.byref(self.b), len(self.handles), arr)
+        if rc != FDFD_OK:
+            raise FDFDError(rc, "fdfd_batch_create failed")
+
+    def factor(self, omegas):
+        """Factor handle i at omegas[i]; returns the per-handle status codes (raises on error)."""
+        om = np.ascontiguousarray(np.asarray(omegas, dtype=np.float64))
+        if om.size != len(self.handles):
+            raise ValueError("one frequency per handle")
+        st = (C.c_int * len(self.handles))()
+        rc = self.lib.fdfd_batch_factor(self.b, om.ctypes.data_as(C.POINTER(C.c_double)), st)
+        if rc != FDFD_OK:
+            raise FDFDError(rc, self.lib.fdfd_batch_last_error(self.b).decode())
+        return list(st)
+
+    def stats(self):
+        k, n, ms = C.c_longlong(0), C.c_longlong(0), C.c_double(0)
+        self.lib.fdfd_batch_stats(self.b, C.byref(k), C.byref(n), C.byref(ms))
+        return {"graph_kernels": k.value, "graph_launches": n.value, "last_graph_ms": ms.value}
+
+    def close(self):
+        if self.b:
+            self.lib.fdfd_batch_destroy(self.b)
+            self.b = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+        return False

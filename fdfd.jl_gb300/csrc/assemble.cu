@@ -36,7 +36,10 @@ __device__ cplx<double> sfactor_value(int i1, int Nw, int Npml, double dw, bool 
     return cmk(1.0, -(sig / (omega * eps0n)));
 }
 
-__global__ void sfactor_kernel(SFactorArgs a, cplx<double>* out) {
+// the arguments live in device memory, so that a captured factorization is replayed
+// for another frequency by rewriting them before the launch
+__global__ void sfactor_kernel(const SFactorArgs* __restrict__ pa, cplx<double>* out) {
+    const SFactorArgs a = *pa;
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     int tot = 2 * a.Nx + 2 * a.Ny;
     if (t >= tot) return;
@@ -76,8 +79,9 @@ __device__ __forceinline__ cplx<double> eps_avg_inv(const cplx<double>* eps, int
     return cinv(s);
 }
 
-__global__ void stencil_kernel(StencilArgs a, const cplx<double>* __restrict__ eps,
+__global__ void stencil_kernel(const StencilArgs* __restrict__ pa, const cplx<double>* __restrict__ eps,
                                const cplx<double>* __restrict__ sf, cplx<double>* __restrict__ st) {
+    const StencilArgs a = *pa;
     long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     long long N = (long long)a.Nx * a.Ny;
     if (k >= N) return;

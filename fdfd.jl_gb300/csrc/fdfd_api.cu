@@ -32,6 +32,8 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <map>
+#include <tuple>
 #include <unordered_map>
 #include <vector>
 
@@ -150,6 +152,8 @@ struct fdfd_handle {
     long long launches = 0;
     long long dev_bytes = 0;
     long long dev_budget = 0;            // device bytes the handle may hold (0: no limit)
+    AssembleArgs hargs;                  // assembly arguments (host copy) ...
+    AssembleArgs* dargs = nullptr;       // ... and the device block the assembly kernels read
     std::unordered_map<void*, size_t> alloc_bytes;   // live dev_alloc buffers and their sizes
     unsigned long long wait_ns = 0;      // pipeline wait limit of the tensor-core GEMM (0: default)
     // FP64 device buffers (natural layout)
@@ -194,6 +198,12 @@ struct fdfd_handle {
     int gj_fused_k = 0;            // FP32 tensor-core Gauss-Jordan: columns of the panels that share one
                                    // update (0: one update per panel, the default; FDFD_GJ_FUSED_K)
     int gj_fused_min = 1;          // ... for batches of at least this many matrices
+    // autotuner (fdfd_autotune): tile width per tensor-core GEMM shape (M, N, K, jobs, pre-split
+    // operands) and launch shape per sweep product (form, jobs, right-hand sides per launch)
+    std::map<std::tuple<int, int, int, int, int>, int> tune_gemm;
+    std::map<std::tuple<int, int, int>, int> tune_gemv;
+    std::string tune_log;
+    int force_bn = 0, force_shape = 0;   // set while the autotuner times a candidate
     // profiling (CUDA events around launches on the handle's stream)
     struct ProfRec { int cls, e0, e1; double work; };
     bool prof_on = false;
@@ -707,8 +717,13 @@ int gemm(fdfd_handle* h, int pa, int pb, int pc, const int* a_slot, const int* b
     const double flops = 8.0 * M * N * K * njobs;
     int ev = prof_begin(h);
     if (sizeof(T) == 4 && F.tc_ok) {
+        int bn = h->force_bn;
+        if (!bn) {
+            auto it = h->tune_gemm.find(std::make_tuple(M, N, K, njobs, (int)(g.A.planes == 4)));
+            if (it != h->tune_gemm.end()) bn = it->second;
+        }
         int rc = tc_gemm_launch(reinterpret_cast<GemmArgs<float>*>(&g), c_trans_arr, pa, pb, njobs, &F.tc,
-                                h->num_sms, stream);
+                                h->num_sms, stream, bn);
         if (rc != 0) return set_err(h, FDFD_ECUDA, "tcgen05 GEMM launch failed (%d)", rc);
         prof_end(h, ev, prof_cls >= 0 ? prof_cls : FDFD_PROF_GEMM_TC, prof_cls >= 0 ? prof_work : flops);
         h->launches++;
@@ -998,6 +1013,11 @@ template <typename T> int gemv(fdfd_handle* h, int tr, int p1, int p2, const T* 
         g.b = b; g.ld = h->map.ld; g.nrhs = std::min(rmax, nrhs - r0); g.rtot = nrhs; g.r0 = r0;
         g.alpha = alpha;
         g.nsm = h->num_sms;
+        g.shape = h->force_shape;
+        if (!g.shape) {
+            auto it = h->tune_gemv.find(std::make_tuple(tr, njobs, g.nrhs));
+            if (it != h->tune_gemv.end()) g.shape = it->second;
+        }
         int ev = prof_begin(h);
         int e = launch_gemv<T>(h->stream, tr, njobs, g);
         // algorithmic bytes: every referenced block (re + im planes) read once; per job and
@@ -1465,14 +1485,13 @@ int refine(fdfd_handle* h, int nrhs, int* iters, double* relres, bool give_up) {
 // ---------------------------------------------------------------------------
 // Assembly + factorization of the operator `op`
 // ---------------------------------------------------------------------------
-int assemble(fdfd_handle* h, int op, double omega_pml, zd sigma, double omega_drv) {
-    SFactorArgs sa;
+// the operator's assembly arguments, copied to the handle's device argument block on `s`
+int assemble_args(fdfd_handle* h, int op, double omega_pml, zd sigma, double omega_drv, cudaStream_t s) {
+    SFactorArgs& sa = h->hargs.sf;
     sa.Nx = h->Nx; sa.Ny = h->Ny; sa.Npx = h->Npx; sa.Npy = h->Npy;
     sa.dx = h->dx; sa.dy = h->dy; sa.omega = omega_pml; sa.eps0n = kEPS0 * h->L0;
     sa.eta0 = std::sqrt(kMU0 / kEPS0); sa.m = h->pml_m; sa.lnR = h->pml_lnR;
-    int tot = 2 * h->Nx + 2 * h->Ny;
-    LAUNCH(sfactor_kernel, ceil_div(tot, 128), 128, 0, sa, h->sf);
-    StencilArgs a;
+    StencilArgs& a = h->hargs.st;
     a.Nx = h->Nx; a.Ny = h->Ny; a.op = op;
     a.idx = 1.0 / h->dx; a.idy = 1.0 / h->dy;
     a.imu0 = 1.0 / (kMU0 * h->L0);
@@ -1480,9 +1499,23 @@ int assemble(fdfd_handle* h, int op, double omega_pml, zd sigma, double omega_dr
     a.omega2 = omega_drv * omega_drv;
     a.omega2mu0 = omega_drv * omega_drv * (kMU0 * h->L0);
     a.sigma_re = sigma.real(); a.sigma_im = sigma.imag();
+    CK(cudaMemcpyAsync(h->dargs, &h->hargs, sizeof(AssembleArgs), cudaMemcpyHostToDevice, s));
+    return FDFD_OK;
+}
+
+// the assembly kernels (device arguments), on the handle's stream
+int assemble_kernels(fdfd_handle* h) {
+    int tot = 2 * h->Nx + 2 * h->Ny;
+    LAUNCH(sfactor_kernel, ceil_div(tot, 128), 128, 0, &h->dargs->sf, h->sf);
     long long N = (long long)h->Nx * h->Ny;
-    LAUNCH(stencil_kernel, ceil_div(N, 256), 256, 0, a, h->eps, h->sf, h->st);
-    RET(check_launch(h, "assemble"));
+    LAUNCH(stencil_kernel, ceil_div(N, 256), 256, 0, &h->dargs->st, h->eps, h->sf, h->st);
+    return check_launch(h, "assemble");
+}
+
+int assemble(fdfd_handle* h, int op, double omega_pml, zd sigma, double omega_drv) {
+    RET(assemble_args(h, op, omega_pml, sigma, omega_drv, h->stream));
+    RET(assemble_kernels(h));
+    long long N = (long long)h->Nx * h->Ny;
     // factorization scale: power of two nearest 1/Σ|off-diagonal| at the grid centre
     long long kc = h->Nx / 2 + (long long)h->Nx * (h->Ny / 2);
     cplx<double> c[5];
@@ -1619,6 +1652,7 @@ int fdfd_create(fdfd_handle** out, int Nx, int Ny, int Npx, int Npy, double dx, 
     if ((rc = dev_alloc(h, (void**)&h->sf, 2 * (2 * Nx + 2 * Ny) * sizeof(cplx<double>)))) return fail(rc);
     if ((rc = dev_alloc(h, (void**)&h->st, 5 * N * sizeof(cplx<double>)))) return fail(rc);
     if ((rc = dev_alloc(h, (void**)&h->derr, sizeof(unsigned)))) return fail(rc);
+    if ((rc = dev_alloc(h, (void**)&h->dargs, sizeof(AssembleArgs)))) return fail(rc);
     cudaMemsetAsync(h->derr, 0, sizeof(unsigned), h->stream);
     build_plan(h);
     JobBlob B;
@@ -1640,8 +1674,8 @@ void fdfd_destroy(fdfd_handle* h) {
         delete h->mf;
         h->mf = nullptr;
     }
-    void* bufs[] = {h->eps, h->sf, h->st, h->derr, h->part, h->red, h->kb, h->kx, h->kr, h->kV, h->kZ, h->kc, h->io,
-                    h->djobs, h->mode_buf, h->nl_d1};
+    void* bufs[] = {h->eps, h->sf, h->st, h->derr, h->dargs, h->part, h->red, h->kb, h->kx, h->kr, h->kV, h->kZ,
+                    h->kc, h->io, h->djobs, h->mode_buf, h->nl_d1};
     for (void* p : bufs) dev_free(h, p);
     free_store(h, h->f32);
     free_store(h, h->f64);
@@ -1846,6 +1880,221 @@ int fdfd_solve(fdfd_handle* h, const double* src, int nrhs, double* f1, double* 
 }
 
 // ---- modulated device (multi-frequency FDFD), modulation.jl -----------------
+// ---- batched factorizations in one CUDA graph ------------------------------
+// Many frequencies, or independent problems of uneven sizes, each on its own
+// handle: their assemblies and factorizations become the parallel branches of one
+// captured graph, so a batch is one cudaGraphLaunch and the GPU runs the
+// factorizations side by side (the deep, few-matrix levels of one leave most of
+// the GPU to the others).  The first fdfd_batch_factor factors every handle the
+// ordinary way (allocating its storage and fixing its scaling), then captures the
+// work; later calls rewrite each handle's assembly arguments (frequency) and
+// replay the graph.  The captured work is the factorization only: solves run on
+// each handle afterwards (they are ordered after the graph on the handle's stream).
+}  // extern "C"
+
+struct fdfd_batch {
+    std::vector<fdfd_handle*> hs;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_done = nullptr, ev_t0 = nullptr, ev_t1 = nullptr;
+    std::vector<cudaEvent_t> ev_join, ev_in;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    long long kernels = 0;        // kernel launches captured in the graph
+    std::vector<long long> hkernels;   // ... per handle
+    long long graph_launches = 0; // cudaGraphLaunch calls
+    double last_ms = 0;           // device time of the last graph launch
+    std::string err;
+};
+
+namespace {
+
+int batch_err(fdfd_batch* B, int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    B->err = buf;
+    return code;
+}
+
+// the device work of one handle's driven factorization (assembly kernels from the
+// device argument block, then the block cyclic reduction), on its stream
+int factor_work(fdfd_handle* h) {
+    RET(assemble_kernels(h));
+    return h->precision == FDFD_PREC_FP64 ? factor_impl<double>(h) : factor_impl<float>(h);
+}
+
+int batch_capture(fdfd_batch* B) {
+    cudaGraph_t g = nullptr;
+    if (cudaStreamBeginCapture(B->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        cudaGetLastError();
+        return batch_err(B, FDFD_ECUDA, "cudaStreamBeginCapture failed");
+    }
+    int rc = FDFD_OK;
+    long long k0 = 0;
+    for (fdfd_handle* h : B->hs) k0 += h->launches;
+    B->hkernels.assign(B->hs.size(), 0);
+    if (cudaEventRecord(B->ev_fork, B->stream) != cudaSuccess) rc = FDFD_ECUDA;
+    for (size_t i = 0; i < B->hs.size() && rc == FDFD_OK; ++i) {
+        fdfd_handle* h = B->hs[i];
+        if (cudaStreamWaitEvent(h->stream, B->ev_fork, 0) != cudaSuccess) { rc = FDFD_ECUDA; break; }
+        const long long l0 = h->launches;
+        rc = factor_work(h);
+        B->hkernels[i] = h->launches - l0;
+        if (rc != FDFD_OK) { B->err = h->err; break; }
+        if (cudaEventRecord(B->ev_join[i], h->stream) != cudaSuccess ||
+            cudaStreamWaitEvent(B->stream, B->ev_join[i], 0) != cudaSuccess)
+            rc = FDFD_ECUDA;
+    }
+    const cudaError_t ee = cudaStreamEndCapture(B->stream, &g);
+    if (rc == FDFD_OK && (ee != cudaSuccess || !g)) rc = FDFD_ECUDA;
+    long long k1 = 0;
+    for (fdfd_handle* h : B->hs) k1 += h->launches;
+    if (rc == FDFD_OK && cudaGraphInstantiate(&B->exec, g, 0) != cudaSuccess) rc = FDFD_ECUDA;
+    if (rc != FDFD_OK) {
+        cudaGetLastError();
+        if (g) cudaGraphDestroy(g);
+        B->exec = nullptr;
+        if (B->err.empty()) B->err = "graph capture of the batch factorization failed";
+        return rc;
+    }
+    B->graph = g;
+    B->kernels = k1 - k0;
+    return FDFD_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fdfd_batch_create(fdfd_batch** out, int n, fdfd_handle* const* handles) {
+    if (!out || n < 1 || !handles) return FDFD_EINVAL;
+    *out = nullptr;
+    for (int i = 0; i < n; ++i) {
+        if (!handles[i] || handles[i]->mf) return FDFD_EINVAL;
+        for (int j = 0; j < i; ++j)
+            if (handles[j] == handles[i]) return FDFD_EINVAL;
+    }
+    fdfd_batch* B = new fdfd_batch();
+    B->hs.assign(handles, handles + n);
+    bool ok = cudaStreamCreateWithFlags(&B->stream, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaEventCreateWithFlags(&B->ev_fork, cudaEventDisableTiming) == cudaSuccess &&
+              cudaEventCreateWithFlags(&B->ev_done, cudaEventDisableTiming) == cudaSuccess &&
+              cudaEventCreate(&B->ev_t0) == cudaSuccess && cudaEventCreate(&B->ev_t1) == cudaSuccess;
+    B->ev_join.assign(n, nullptr);
+    B->ev_in.assign(n, nullptr);
+    for (int i = 0; i < n && ok; ++i)
+        ok = cudaEventCreateWithFlags(&B->ev_join[i], cudaEventDisableTiming) == cudaSuccess &&
+             cudaEventCreateWithFlags(&B->ev_in[i], cudaEventDisableTiming) == cudaSuccess;
+    if (!ok) {
+        cudaGetLastError();
+        fdfd_batch_destroy(B);
+        return FDFD_ECUDA;
+    }
+    *out = B;
+    return FDFD_OK;
+}
+
+void fdfd_batch_destroy(fdfd_batch* B) {
+    if (!B) return;
+    if (B->stream) cudaStreamSynchronize(B->stream);
+    if (B->exec) cudaGraphExecDestroy(B->exec);
+    if (B->graph) cudaGraphDestroy(B->graph);
+    for (cudaEvent_t e : B->ev_join) if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : B->ev_in) if (e) cudaEventDestroy(e);
+    cudaEvent_t evs[] = {B->ev_fork, B->ev_done, B->ev_t0, B->ev_t1};
+    for (cudaEvent_t e : evs) if (e) cudaEventDestroy(e);
+    if (B->stream) cudaStreamDestroy(B->stream);
+    delete B;
+}
+
+const char* fdfd_batch_last_error(const fdfd_batch* B) { return B ? B->err.c_str() : "null batch"; }
+
+int fdfd_batch_factor(fdfd_batch* B, const double* omegas, int* status) {
+    if (!B) return FDFD_EINVAL;
+    if (!omegas) return batch_err(B, FDFD_EINVAL, "fdfd_batch_factor: NULL omegas");
+    const int n = (int)B->hs.size();
+    for (int i = 0; i < n; ++i) {
+        fdfd_handle* h = B->hs[i];
+        if (!(omegas[i] > 0) || !std::isfinite(omegas[i]))
+            return batch_err(B, FDFD_EINVAL, "fdfd_batch_factor: omega[%d] must be positive and finite", i);
+        if (!h->eps_set) return batch_err(B, FDFD_EINVAL, "fdfd_batch_factor: handle %d has no permittivity", i);
+        if (h->prof_on) return batch_err(B, FDFD_EINVAL, "fdfd_batch_factor: handle %d is profiling", i);
+    }
+    int first = FDFD_OK;
+    if (!B->exec) {
+        // the ordinary factorizations: storage, scaling, and this call's results
+        for (int i = 0; i < n; ++i) {
+            const int rc = fdfd_factor(B->hs[i], omegas[i]);
+            if (status) status[i] = rc;
+            if (rc != FDFD_OK && first == FDFD_OK) {
+                first = rc;
+                B->err = B->hs[i]->err;
+            }
+        }
+        if (first != FDFD_OK) return first;
+        for (int i = 0; i < n; ++i)
+            if (B->hs[i]->fact_prec != B->hs[i]->precision) return batch_err(B, FDFD_EINVAL, "handle %d: mixed factor unavailable", i);
+        return batch_capture(B);
+    }
+    // replay: new assembly arguments on the batch stream, after each handle's own
+    // pending work (its permittivity copy)
+    for (int i = 0; i < n; ++i) {
+        fdfd_handle* h = B->hs[i];
+        const int op = h->pol == FDFD_TM ? OP_TM_DRIVEN : OP_TE_DRIVEN;
+        h->launches = 0;
+        h->factored = false;
+        if (cudaEventRecord(B->ev_in[i], h->stream) != cudaSuccess ||
+            cudaStreamWaitEvent(B->stream, B->ev_in[i], 0) != cudaSuccess)
+            return batch_err(B, FDFD_ECUDA, "batch: stream ordering failed");
+        const int rc = assemble_args(h, op, omegas[i], zd(0, 0), omegas[i], B->stream);
+        if (rc != FDFD_OK) return batch_err(B, rc, "%s", h->err.c_str());
+    }
+    if (cudaEventRecord(B->ev_t0, B->stream) != cudaSuccess || cudaGraphLaunch(B->exec, B->stream) != cudaSuccess ||
+        cudaEventRecord(B->ev_t1, B->stream) != cudaSuccess || cudaEventRecord(B->ev_done, B->stream) != cudaSuccess) {
+        cudaGetLastError();
+        return batch_err(B, FDFD_ECUDA, "cudaGraphLaunch of the batch factorization failed");
+    }
+    B->graph_launches++;
+    for (int i = 0; i < n; ++i)
+        if (cudaStreamWaitEvent(B->hs[i]->stream, B->ev_done, 0) != cudaSuccess)
+            return batch_err(B, FDFD_ECUDA, "batch: stream ordering failed");
+    if (cudaStreamSynchronize(B->stream) != cudaSuccess) {
+        cudaGetLastError();
+        return batch_err(B, FDFD_ECUDA, "batch factorization failed on the device");
+    }
+    float ms = 0;
+    cudaEventElapsedTime(&ms, B->ev_t0, B->ev_t1);
+    B->last_ms = ms;
+    for (int i = 0; i < n; ++i) {
+        fdfd_handle* h = B->hs[i];
+        int rc = check_device(h, "batch factor");
+        if (rc == FDFD_OK) {
+            h->launches = B->hkernels[i];
+            h->op = h->pol == FDFD_TM ? OP_TM_DRIVEN : OP_TE_DRIVEN;
+            h->omega = omegas[i];
+            h->fact_prec = h->precision;
+            h->fell_back = false;
+            h->factored = true;
+        }
+        if (status) status[i] = rc;
+        if (rc != FDFD_OK && first == FDFD_OK) {
+            first = rc;
+            B->err = h->err;
+        }
+    }
+    return first;
+}
+
+int fdfd_batch_stats(const fdfd_batch* B, long long* kernels, long long* graph_launches, double* last_ms) {
+    if (!B) return FDFD_EINVAL;
+    if (kernels) *kernels = B->kernels;
+    if (graph_launches) *graph_launches = B->graph_launches;
+    if (last_ms) *last_ms = B->last_ms;
+    return FDFD_OK;
+}
+
 int fdfd_mf_create(fdfd_handle** out, int Nx, int Ny, int Npx, int Npy, double dx, double dy, double L0,
                    double pml_m, double pml_lnR, int nsidebands, int shared_pml, int precision) {
     if (!out) return FDFD_EINVAL;
@@ -2375,6 +2624,180 @@ int fdfd_chi3_solve(fdfd_handle* h, const double* chi, const double* src, int me
         return set_err(h, FDFD_ENOCONV, "chi3 %s iteration stopped at step error %.3e > tol %.1e after %d steps",
                        method == FDFD_CHI3_BORN ? "Born" : "Newton", errs.back(), tol, (int)errs.size() - 1);
     return FDFD_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// device time (ms) of fn() on the handle's stream: one untimed run, then the mean of three
+template <typename F> int time_launch(fdfd_handle* h, F fn, double* ms) {
+    RET(fn());
+    CK(cudaEventRecord(h->ev[5], h->stream));
+    for (int r = 0; r < 3; ++r) RET(fn());
+    CK(cudaEventRecord(h->ev[6], h->stream));
+    CK(cudaEventSynchronize(h->ev[6]));
+    float t = 0;
+    CK(cudaEventElapsedTime(&t, h->ev[5], h->ev[6]));
+    *ms = t / 3.0;
+    return FDFD_OK;
+}
+
+// zeroes a pool (so that the candidates run on finite data)
+template <typename T> int zero_pool(fdfd_handle* h, const Pool<T>& P) {
+    if (P.base) CK(cudaMemsetAsync(P.base, 0, (size_t)P.slot_elems() * P.count * sizeof(T), h->stream));
+    return FDFD_OK;
+}
+
+// The autotuner: every tensor-core GEMM shape of the factorization and every
+// sweep product of the plan is timed with each candidate launch shape, on the
+// handle's own storage and job lists (zeroed first, row maps the identity), and
+// the fastest is recorded for the handle's later launches.
+template <typename T> int autotune_impl(fdfd_handle* h) {
+    RET(alloc_factor<T>(h));
+    const int nrhs_max = std::min(8, gemv_max_rhs<T>(h->map.b));
+    RET(alloc_vectors<T>(h, nrhs_max));
+    FactorStore<T>& F = store<T>(h);
+    const int b = h->map.b, E = (int)h->steps.size();
+    RET(zero_pool<T>(h, F.D)); RET(zero_pool<T>(h, F.C)); RET(zero_pool<T>(h, F.X));
+    RET(zero_pool<T>(h, F.GP)); RET(zero_pool<T>(h, F.RP)); RET(zero_pool<T>(h, F.Tg));
+    launch_perm_init(h->stream, 2 * h->max_ne, F.rowsrc, b);   // in-range rows for the β gathers
+    h->launches++;
+    h->tune_gemm.clear();
+    h->tune_gemv.clear();
+    std::string log;
+    char line[256];
+    const bool prof = h->prof_on;
+    h->prof_on = false;
+    // ---- tensor-core GEMM tile widths
+    if (sizeof(T) == 4 && F.tc_ok) {
+        auto tune = [&](int M, int N, int K, int njobs, int presplit, const char* role, auto launch) -> int {
+            const auto key = std::make_tuple(M, N, K, njobs, presplit);
+            if (njobs == 0 || h->tune_gemm.count(key)) return FDFD_OK;
+            int best = 0;
+            double tbest = 1e30;
+            std::string cand;
+            for (int bn : {64, 128, 256}) {
+                if ((bn == 256 && N <= 128) || (bn == 128 && N <= 64)) continue;   // no wider than the product
+                h->force_bn = bn;
+                double ms = 0;
+                const int rc = time_launch(h, launch, &ms);
+                h->force_bn = 0;
+                RET(rc);
+                snprintf(line, sizeof line, " %d:%.4f", bn, ms);
+                cand += line;
+                if (ms < tbest) { tbest = ms; best = bn; }
+            }
+            h->tune_gemm[key] = best;
+            snprintf(line, sizeof line, "gemm %-10s M=%d N=%d K=%d jobs=%d -> BN=%d  (ms%s)\n", role, M, N, K, njobs,
+                     best, cand.c_str());
+            log += line;
+            return FDFD_OK;
+        };
+        const int nb = panel_nb<T>(b);
+        for (int e = 2; e <= E; ++e) {
+            const StepJobs& S = h->sj[e];
+            const int ne = S.ne;
+            RET(tune(b, b, b, 2 * ne, 0, "schur-2n", [&] {
+                return gemm<T>(h, P_C, P_D, P_X, J<int>(h, S.xt_a), J<int>(h, S.xt_b), J<int>(h, S.xt_c), nullptr, 0,
+                               2 * ne, b, b, b, (T)1, 0, 0, 0);
+            }));
+            RET(tune(b, b, b, ne, 0, "schur-n", [&] {
+                return gemm<T>(h, P_C, P_X, P_D, J<int>(h, S.dp_a), J<int>(h, S.dp_b), J<int>(h, S.dp_c), nullptr, 0,
+                               ne, b, b, b, (T)-1, 1, 0, 0);
+            }));
+            const int w1 = std::min(nb, b - nb);
+            RET(tune(b, w1, nb, ne, 1, "gj-narrow", [&] {
+                return gemm<T>(h, P_GP, P_RP, P_TG, F.gj_slots, F.gj_slots, J<int>(h, S.iota), nullptr, 0, ne, b, w1,
+                               nb, (T)1, 1, 0, nb, P_D, J<int>(h, S.elim), F.rowsrc, -1, 0.0, h->stream, nb);
+            }));
+            RET(tune(b, b, nb, ne, 1, "gj-wide", [&] {
+                return gemm<T>(h, P_GP, P_RP, P_TG, F.gj_slots, F.gj_slots, J<int>(h, S.iota), nullptr, 0, ne, b, b,
+                               nb, (T)1, 1, 0, nb, P_D, J<int>(h, S.elim), F.rowsrc, -1, 0.0, h->stream, 0, nb, w1);
+            }));
+        }
+        // the final pair's single-matrix products
+        RET(tune(b, b, b, 1, 0, "schur-1", [&] {
+            return gemm<T>(h, P_C, P_D, P_X, J<int>(h, h->fin_xt_a), J<int>(h, h->fin_xt_b), J<int>(h, h->fin_xt_c),
+                           nullptr, 0, 1, b, b, b, (T)1, 0, 0, 0);
+        }));
+    }
+    // ---- sweep product launch shapes
+    auto tune_v = [&](int tr, int p1, int p2, const T* V1, const T* V2, const T* Y0, T* Y, const int4* jobs,
+                      const int2* yjobs, int njobs, int nrhs, const char* role) -> int {
+        const auto key = std::make_tuple(tr, njobs, nrhs);
+        if (njobs == 0 || h->tune_gemv.count(key)) return FDFD_OK;
+        int best = 0;
+        double tbest = 1e30;
+        std::string cand;
+        const int cands[2][3] = {{1, 2, 4}, {8, 16, 32}};
+        for (int c : cands[tr]) {
+            h->force_shape = c;
+            double ms = 0;
+            const int rc = time_launch(h, [&] { return gemv<T>(h, tr, p1, p2, V1, V2, Y0, Y, jobs, yjobs, njobs,
+                                                               njobs, nrhs, (T)1); }, &ms);
+            h->force_shape = 0;
+            RET(rc);
+            snprintf(line, sizeof line, " %d:%.4f", c, ms);
+            cand += line;
+            if (ms < tbest) { tbest = ms; best = c; }
+        }
+        h->tune_gemv[key] = best;
+        snprintf(line, sizeof line, "gemv %-10s %s jobs=%d rhs=%d -> %s=%d  (ms%s)\n", role, tr ? "T" : "N", njobs,
+                 nrhs, tr ? "og" : "rpw", best, cand.c_str());
+        log += line;
+        return FDFD_OK;
+    };
+    CK(cudaMemsetAsync(F.rv, 0, (size_t)h->map.n * F.vec_nrhs * 2 * h->map.ld * sizeof(T), h->stream));
+    CK(cudaMemsetAsync(F.xv, 0, (size_t)h->map.n * F.vec_nrhs * 2 * h->map.ld * sizeof(T), h->stream));
+    const int rhs_set[2] = {1, nrhs_max};
+    for (int nr : rhs_set) {
+        for (int e = 1; e <= E; ++e) {
+            const StepJobs& S = h->sj[e];
+            if (e == 1 && !(F.trifac && h->tri_sweep && !h->level1_gj))
+                RET(tune_v(0, P_D, P_D, F.rv, F.rv, nullptr, F.xv, J<int4>(h, S.fwd1), J<int2>(h, S.fwd1y), S.ne, nr,
+                           "inverse"));
+            if (e >= 2) {
+                RET(tune_v(0, P_D, P_D, F.rv, F.rv, nullptr, F.xv, J<int4>(h, S.fwd1), J<int2>(h, S.fwd1y), S.ne, nr,
+                           "inverse"));
+                RET(tune_v(0, P_C, P_C, F.xv, F.xv, F.rv, F.rv, J<int4>(h, S.f2), J<int2>(h, S.f2y), S.nf2, nr,
+                           "coupling"));
+                RET(tune_v(1, P_X, P_X, F.xv, F.xv, F.xv, F.xv, J<int4>(h, S.bw), J<int2>(h, S.bwy), S.ne, nr,
+                           "back"));
+            }
+        }
+        RET(tune_v(0, P_D, P_D, F.rv, F.rv, nullptr, F.xv, J<int4>(h, h->fin_g1), J<int2>(h, h->fin_g1y), 1, nr,
+                   "inverse"));
+        RET(tune_v(1, P_X, P_X, F.xv, F.xv, F.xv, F.xv, J<int4>(h, h->fin_bx), J<int2>(h, h->fin_bxy), 1, nr,
+                   "back"));
+    }
+    h->prof_on = prof;
+    CK(cudaStreamSynchronize(h->stream));
+    RET(check_device(h, "autotune"));
+    h->tune_log = log;
+    h->factored = false;   // the factor storage now holds the candidates' output
+    return FDFD_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fdfd_autotune(fdfd_handle* h) {
+    if (!h) return FDFD_EINVAL;
+    if (h->mf) return set_err(h, FDFD_EINVAL, "fdfd_autotune: tune the sideband handles of a modulated device");
+    return h->precision == FDFD_PREC_FP64 ? autotune_impl<double>(h) : autotune_impl<float>(h);
+}
+
+int fdfd_get_tuning(const fdfd_handle* h, char* buf, int cap) {
+    if (!h || cap < 0 || (cap > 0 && !buf)) return -1;
+    const int n = (int)h->tune_log.size();
+    if (cap > 0) {
+        const int m = std::min(n, cap - 1);
+        memcpy(buf, h->tune_log.data(), (size_t)m);
+        buf[m] = 0;
+    }
+    return n;
 }
 
 int fdfd_set_profiling(fdfd_handle* h, int on) {

@@ -29,9 +29,10 @@ int tc_gemm_launch_maps(const GemmArgs<float>* g, const int* c_trans_arr, const 
 // than the product needs) whose tile count still covers num_sms.
 int tc_pick_bn(int M, int N, int K, int njobs, int num_sms);
 
+// bn > 0 forces the tile width (the autotuner's choice), 0 takes tc_pick_bn's
 inline int tc_gemm_launch(const GemmArgs<float>* g, const int* c_trans_arr, int pa, int pb, int njobs,
-                          const TcMaps* maps, int num_sms, cudaStream_t stream) {
-    const int bn = tc_pick_bn(g->M, g->N, g->K, njobs, num_sms);
+                          const TcMaps* maps, int num_sms, cudaStream_t stream, int bn = 0) {
+    if (bn != 64 && bn != 128 && bn != 256) bn = tc_pick_bn(g->M, g->N, g->K, njobs, num_sms);
     const int bi = bn == 256 ? 1 : (bn == 128 ? 0 : 2);
     return tc_gemm_launch_maps(g, c_trans_arr, &maps->map[pa][0], &maps->map[pb][bi], bn, njobs, stream);
 }

@@ -25,8 +25,11 @@ struct NodeMap {
 };
 
 // ---- assemble.cu -----------------------------------------------------------
-__global__ void sfactor_kernel(SFactorArgs a, cplx<double>* out);
-__global__ void stencil_kernel(StencilArgs a, const cplx<double>* eps, const cplx<double>* sf, cplx<double>* st);
+// assembly arguments are read from device memory (a captured factorization is
+// replayed for another frequency by rewriting them)
+struct AssembleArgs { SFactorArgs sf; StencilArgs st; };
+__global__ void sfactor_kernel(const SFactorArgs* a, cplx<double>* out);
+__global__ void stencil_kernel(const StencilArgs* a, const cplx<double>* eps, const cplx<double>* sf, cplx<double>* st);
 __global__ void residual_kernel(int Nx, int Ny, int nrhs, const cplx<double>* st, const cplx<double>* x,
                                 const cplx<double>* b, cplx<double>* r, double* part);
 // Coupled sideband system of a modulated device: K = 2s+1 stencils (one per
@@ -211,6 +214,8 @@ template <typename T> struct GemvArgs {
     int rpw, og;        // launch shape, set by launch_gemv: rows per warp (N form),
                         // lanes per output group (T form)
     int nsm;            // streaming multiprocessors of the device (launch shape)
+    int shape;          // launch shape chosen by the caller (autotuner): rpw in {1, 2, 4} (N form)
+                        // or og in {8, 16, 32} (T form); 0: launch_gemv's rule
 };
 // TR = 1: matrices stored transposed.  Returns a cudaError_t value.
 template <typename T>

@@ -380,10 +380,12 @@ int gemv_launch_r(cudaStream_t s, int tr, int njobs, const GemvArgs<T>& g) {
     if (tr) {
         a.og = 32;
         while (a.og > 8 && (long long)ceil_div(g.b, a.og * VW) * njobs < want) a.og >>= 1;
+        if (g.shape == 8 || g.shape == 16 || g.shape == 32) a.og = g.shape;
         gemv_t_kernel<T, R><<<dim3(ceil_div(g.b, a.og * VW), njobs), 256, smem, s>>>(a);
     } else {
         a.rpw = 4;
         while (a.rpw > 1 && (long long)ceil_div(g.b, 8 * a.rpw) * njobs < want) a.rpw >>= 1;
+        if (g.shape == 1 || g.shape == 2 || g.shape == 4) a.rpw = g.shape;
         gemv_n_kernel<T, R><<<dim3(ceil_div(g.b, 8 * a.rpw), njobs), 256, smem, s>>>(a);
     }
     return (int)cudaGetLastError();

@@ -302,6 +302,44 @@ int  fdfd_mf_factor(fdfd_handle* h, double omega, double Omega);
 int  fdfd_mf_solve(fdfd_handle* h, const double* src, double* ez, double* hx,
                    double* hy, fdfd_stats* stats);
 
+/* Batched factorizations in one CUDA graph (no counterpart in the reference,
+ * whose solve loop re-assembles and re-factors each frequency in turn,
+ * src/solver/driven.jl:11-55).  A batch groups n existing driven handles
+ * (TM or TE, any grid sizes and precisions; not modulated devices; each handle
+ * in at most one batch).  fdfd_batch_factor(B, omegas, status) assembles and
+ * factors every handle at its omegas[i] (SI rad/s) with the permittivity last
+ * given to fdfd_set_eps: the first call does so handle by handle and then
+ * captures the device work of all of them as the parallel branches of one
+ * CUDA graph; every later call is one cudaGraphLaunch of that graph (the
+ * handles' factorizations run concurrently on the GPU).  status[i] (may be
+ * NULL) receives each handle's code; the call returns the first error.  The
+ * handles are then factored as after fdfd_factor (fdfd_solve, fdfd_adjoint on
+ * each).  The handles must outlive the batch and not profile
+ * (fdfd_set_profiling) while batched; a handle may belong to several batches
+ * used one at a time; its power-of-two operator scaling is the one of the
+ * first call.  fdfd_batch_stats: kernels captured
+ * in the graph, graph launches so far, device time of the last launch (ms). */
+typedef struct fdfd_batch fdfd_batch;
+int  fdfd_batch_create(fdfd_batch** B, int n, fdfd_handle* const* handles);
+int  fdfd_batch_factor(fdfd_batch* B, const double* omegas, int* status);
+int  fdfd_batch_stats(const fdfd_batch* B, long long* kernels,
+                      long long* graph_launches, double* last_ms);
+const char* fdfd_batch_last_error(const fdfd_batch* B);
+void fdfd_batch_destroy(fdfd_batch* B);
+
+/* Autotuner of the launch shapes (no counterpart in the reference).  Times,
+ * on the handle's own storage and job lists, every tensor-core GEMM shape of
+ * its factorization (tile width 64, 128 or 256 columns) and every sweep product
+ * of its plan for 1 and for the largest right-hand-side count per launch (rows
+ * per warp 1/2/4, or output-group width 8/16/32 for the transposed form), and
+ * keeps the fastest for the handle's later factorizations, solves and batch
+ * graphs.  It overwrites the factor storage (call it before fdfd_factor, or
+ * factor again after it).  fdfd_get_tuning copies the record of the choices
+ * (one line per shape with each candidate's time) into buf (cap bytes, NUL
+ * terminated) and returns its full length (-1 on bad arguments). */
+int  fdfd_autotune(fdfd_handle* h);
+int  fdfd_get_tuning(const fdfd_handle* h, char* buf, int cap);
+
 /* Debug/parity: copy the assembled FP64 5-point stencil of the last factored
  * operator to the host: 5*Nx*Ny complex, planes [self, x-1, x+1, y-1, y+1]
  * (periodic neighbours, unscaled, reference units). */

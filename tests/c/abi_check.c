@@ -53,6 +53,16 @@ int main(void) {
     CHECK(fdfd_set_restart(NULL, 20) == FDFD_EINVAL);
     CHECK(fdfd_set_fallback(NULL, 1) == FDFD_EINVAL);
     CHECK(fdfd_set_wait_limit(NULL, 1000) == FDFD_EINVAL);
+    CHECK(fdfd_autotune(NULL) == FDFD_EINVAL);
+    CHECK(fdfd_get_tuning(NULL, NULL, 0) == -1);
+    {
+        fdfd_batch* bt = NULL;
+        CHECK(fdfd_batch_create(&bt, 0, NULL) == FDFD_EINVAL && bt == NULL);
+        CHECK(fdfd_batch_create(NULL, 1, NULL) == FDFD_EINVAL);
+        CHECK(fdfd_batch_factor(NULL, x, NULL) == FDFD_EINVAL);
+        CHECK(fdfd_batch_stats(NULL, NULL, NULL, NULL) == FDFD_EINVAL);
+        fdfd_batch_destroy(NULL);
+    }
     CHECK(fdfd_set_device_budget(NULL, 1 << 20) == FDFD_EINVAL);
     CHECK(fdfd_set_eps(NULL, x) == FDFD_EINVAL);
     CHECK(fdfd_factor(NULL, 1.0) == FDFD_EINVAL);
