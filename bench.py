@@ -282,10 +282,10 @@ def run_extras(L, pkg, W, a):
     """The other benchmark problems, each timed with host-buffer calls after one warm-up:
     adjoint gradients/s on the 1000x600 adjoint problem (300x300 design, Gaussian overlap
     objective), eigenfrequency time on the 12x12 rod-lattice cavity (280x280, 6 modes nearest
-    ωa/2πc = 0.38), RHS solves/s on a bounded slice of the 400x400 sweep (first 4 of the
-    64 wavelengths, 8 Gaussian sources each; the full sweep repeats this per wavelength),
-    coupled-sideband solves/s of the reference notebook's modulated waveguide (1500x200, three
-    frequencies) and problems/s of the 32-problem mixed-size batch."""
+    ωa/2πc = 0.38), the 400x400 frequency sweep (all 64 wavelengths x 8 Gaussian sources, batched
+    factorizations in CUDA graphs), coupled-sideband solves/s of the reference notebook's
+    modulated waveguide (1500x200, three frequencies) and problems/s of the 32-problem mixed-size
+    batch."""
     out = {}
     try:
         p = W.adjoint_problem()
@@ -296,7 +296,7 @@ def run_extras(L, pkg, W, a):
         h.factor(p.omega)
         h.adjoint(p.src, p.extra["mvec"])
         t0 = time.perf_counter()
-        n = 2
+        n = 5
         for _ in range(n):
             h.set_eps(p.eps)
             h.factor(p.omega)
@@ -324,24 +324,8 @@ def run_extras(L, pkg, W, a):
     except Exception as e:
         out["eigfreq"] = {"error": str(e)}
     try:
-        p, lams = W.frequency_sweep()
-        h = L.Handle(p.Nx, p.Ny, p.npml[0], p.npml[1], p.dx, p.dy, 1e-6, p.pml_m, p.pml_lnR, pkg.TM,
-                     L.FDFD_PREC_MIXED)
-        h.set_refinement(1e-10, 80)
-        h.set_eps(p.eps)
-        h.factor(W.omega_of(lams[0]))
-        h.solve(p.src)
-        nl = 4
-        t0 = time.perf_counter()
-        for lam in lams[:nl]:
-            h.factor(W.omega_of(lam))
-            _, _, _, st = h.solve(p.src)
-        t = time.perf_counter() - t0
-        h.close()
-        out["sweep"] = {"rhs_solves_per_s": nl * p.src.shape[0] / t, "wavelengths_per_s": nl / t,
-                        "workload": f"frequency sweep 400x400, {nl} of 64 wavelengths x 8 sources, mixed",
-                        "rel_residual": st.rel_residual}
-    except Exception as e:
+        out["sweep"] = run_sweep(L, pkg, W)
+    except Exception as e:   # reported, not hidden
         out["sweep"] = {"error": str(e)}
     try:
         p = W.modulated_notebook()
@@ -416,50 +400,130 @@ def run_mode_sources(L, pkg, W):
     return res
 
 
+def tuning_summary(logs):
+    """Autotuner choices across handles: per product role, how often each launch shape won."""
+    out = {}
+    for log in logs:
+        for line in log.splitlines():
+            f = line.split()
+            if len(f) < 4 or "->" not in f:
+                continue
+            role = f"{f[0]} {f[1]}"
+            choice = f[f.index("->") + 1]
+            d = out.setdefault(role, {})
+            d[choice] = d.get(choice, 0) + 1
+    return out
+
+
+def run_sweep(L, pkg, W, width=8):
+    """The batched frequency sweep: 400x400 with a 160x160 seeded random design, all 64 wavelengths
+    (uniform in [1.45, 1.65] um, seeded), each with its 8 Gaussian line sources.  `width` handles of
+    the same problem (each autotuned) are factored together, one wavelength each, by one CUDA-graph
+    launch (fdfd_batch_factor); their 8-source solves (host buffers, refined to 1e-10) then run
+    concurrently, one host thread per handle.  64 wavelengths = 64/width launches.  Timed after one
+    untimed pass (which captures the graph); handle creation and tuning are outside the timed region."""
+    import concurrent.futures as cf
+    import numpy as np
+    p, lams = W.frequency_sweep()
+    hs = []
+    for _ in range(width):
+        h = L.Handle(p.Nx, p.Ny, p.npml[0], p.npml[1], p.dx, p.dy, 1e-6, p.pml_m, p.pml_lnR, pkg.TM,
+                     L.FDFD_PREC_MIXED)
+        h.set_refinement(1e-10, 80)
+        h.set_eps(p.eps)
+        hs.append(h)
+    logs = [h.autotune() for h in hs]
+    batch = L.Batch(hs)
+    omegas = np.array([W.omega_of(l) for l in lams])
+
+    def one_pass():
+        res = []
+        with cf.ThreadPoolExecutor(max_workers=width) as ex:
+            for w0 in range(0, len(omegas), width):
+                batch.factor(omegas[w0:w0 + width])
+                res += list(ex.map(lambda h: h.solve(p.src)[3], hs))
+        return res
+
+    one_pass()
+    t0 = time.perf_counter()
+    res = one_pass()
+    t = time.perf_counter() - t0
+    st = batch.stats()
+    batch.close()
+    for h in hs:
+        h.close()
+    nsrc = p.src.shape[0]
+    return {"wavelengths_per_s": len(omegas) / t, "rhs_solves_per_s": len(omegas) * nsrc / t, "seconds": t,
+            "wavelengths": len(omegas), "sources_per_wavelength": nsrc,
+            "rel_residual_max": max(r.rel_residual for r in res), "iterations_max": max(r.iterations for r in res),
+            "fp64_fallbacks": sum(r.fp64_fallback for r in res),
+            "graph": {"handles_per_launch": width, "graph_launches_timed": len(omegas) // width,
+                      "kernels_per_graph": st["graph_kernels"], "last_graph_ms": st["last_graph_ms"]},
+            "tuned_shapes": tuning_summary(logs),
+            "workload": f"frequency sweep 400x400, 64 of 64 wavelengths x {nsrc} sources, {width} frequencies per "
+                        f"CUDA-graph launch, autotuned launch shapes, host buffers, mixed"}
+
+
 def run_mixed_batch(L, pkg, W):
     """The 32-problem mixed-size batch (square sides drawn from 128, 256, 512, 1024 with a fixed
-    seed; split guide with a centred random design of half the side).  One host thread per side
-    class owns one handle (its own CUDA stream) and solves that class's problems in order, so the
-    classes run concurrently on the GPU; host buffers in and out, each problem refined to 1e-10.
-    Timed after one warm-up problem per class; handle creation is outside the timed region."""
+    seed; split guide with a centred random design of half the side).  One autotuned handle per side
+    class; the batch runs in waves, each wave taking the next problem of every class that has one:
+    the wave's permittivities are copied in, all its factorizations run as one CUDA-graph launch
+    (fdfd_batch_factor over that wave's handles), then its solves run concurrently, one host thread
+    per handle (host buffers, refined to 1e-10).  All 32 factor sets at once would not fit in HBM
+    (nine 1024^2 problems hold ~32 GB each), hence the waves.  Timed after one untimed pass (which
+    captures the graphs); handle creation and tuning are outside the timed region."""
     import concurrent.futures as cf
     probs = W.mixed_size_batch()
     classes = {}
     for p in probs:
         classes.setdefault(p.Nx, []).append(p)
-
-    def make(p):
+    sides = sorted(classes)
+    handles = {}
+    for sd in sides:
+        p = classes[sd][0]
         h = L.Handle(p.Nx, p.Ny, p.npml[0], p.npml[1], p.dx, p.dy, 1e-6, p.pml_m, p.pml_lnR, pkg.TM,
                      L.FDFD_PREC_MIXED)
         h.set_refinement(1e-10, 80)
-        return h
+        handles[sd] = h
+    logs = [h.autotune() for h in handles.values()]
+    nwaves = max(len(v) for v in classes.values())
+    waves = [[sd for sd in sides if w < len(classes[sd])] for w in range(nwaves)]
+    batches = {}
+    for wv in waves:
+        key = tuple(wv)
+        if key not in batches:
+            batches[key] = L.Batch([handles[sd] for sd in wv])
 
-    handles = {s: make(ps[0]) for s, ps in classes.items()}
+    def one_pass():
+        res = []
+        with cf.ThreadPoolExecutor(max_workers=len(sides)) as ex:
+            for w, wv in enumerate(waves):
+                ps = [classes[sd][w] for sd in wv]
+                for sd, p in zip(wv, ps):
+                    handles[sd].set_eps(p.eps)
+                batches[tuple(wv)].factor([p.omega for p in ps])
+                res += list(ex.map(lambda a: handles[a[0]].solve(a[1].src)[3], zip(wv, ps)))
+        return res
 
-    def run_class(s, ps):
-        h = handles[s]
-        out = []
-        for p in ps:
-            h.set_eps(p.eps)
-            h.factor(p.omega)
-            _, _, _, st = h.solve(p.src)
-            out.append((st.rel_residual, st.iterations, st.fp64_fallback))
-        return out
-
-    for s, ps in classes.items():          # warm-up: first problem of each class
-        run_class(s, ps[:1])
+    one_pass()
     t0 = time.perf_counter()
-    with cf.ThreadPoolExecutor(max_workers=len(classes)) as ex:
-        res = [r for rs in ex.map(lambda kv: run_class(*kv), classes.items()) for r in rs]
+    res = one_pass()
     t = time.perf_counter() - t0
+    kernels = sum(b.stats()["graph_kernels"] for b in batches.values())
+    for b in batches.values():
+        b.close()
     for h in handles.values():
         h.close()
     return {"problems_per_s": len(probs) / t, "seconds": t, "problems": len(probs),
-            "sides": {int(s): len(ps) for s, ps in sorted(classes.items())},
-            "rel_residual_max": max(r[0] for r in res), "iterations_max": max(r[1] for r in res),
-            "iterations_sum": sum(r[1] for r in res), "fp64_fallbacks": sum(r[2] for r in res),
-            "workload": "32 square problems, sides from {128, 256, 512, 1024} (seed 5), one stream per side "
-                        "class, host buffers, mixed"}
+            "sides": {int(sd): len(classes[sd]) for sd in sides},
+            "rel_residual_max": max(r.rel_residual for r in res), "iterations_max": max(r.iterations for r in res),
+            "iterations_sum": sum(r.iterations for r in res), "fp64_fallbacks": sum(r.fp64_fallback for r in res),
+            "graph": {"waves": len(waves), "graph_launches_timed": len(waves), "distinct_graphs": len(batches),
+                      "kernels_in_graphs": kernels},
+            "tuned_shapes": tuning_summary(logs),
+            "workload": "32 square problems, sides from {128, 256, 512, 1024} (seed 5), one autotuned handle per side "
+                        "class, one CUDA-graph launch factoring each wave, concurrent solves, host buffers, mixed"}
 
 
 def gemm_traffic_bytes():
