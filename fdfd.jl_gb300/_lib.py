@@ -27,7 +27,8 @@ FDFD_MODE_MAX_POINTS = 1023
 
 # every symbol include/fdfd_cuda.h declares
 EXPORTS = ["fdfd_version", "fdfd_create", "fdfd_destroy", "fdfd_last_error", "fdfd_set_refinement",
-           "fdfd_set_fallback", "fdfd_set_restart", "fdfd_set_wait_limit", "fdfd_set_device_budget", "fdfd_mf_create", "fdfd_mf_set_deps", "fdfd_mf_factor",
+           "fdfd_set_fallback", "fdfd_set_restart", "fdfd_set_wait_limit", "fdfd_set_device_budget",
+           "fdfd_set_checkpoint", "fdfd_checkpoint_info", "fdfd_mf_create", "fdfd_mf_set_deps", "fdfd_mf_factor",
            "fdfd_mf_solve", "fdfd_get_mode", "fdfd_mode_sources", "fdfd_poynting", "fdfd_poynting_device",
            "fdfd_flux_integral", "fdfd_chi3_solve",
            "fdfd_set_eps", "fdfd_factor", "fdfd_solve", "fdfd_solve_device", "fdfd_adjoint", "fdfd_adjoint_vjp", "fdfd_eigfreq",
@@ -100,6 +101,10 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.fdfd_set_wait_limit.argtypes = [vp, C.c_longlong]
     lib.fdfd_set_device_budget.restype = ip
     lib.fdfd_set_device_budget.argtypes = [vp, C.c_longlong]
+    lib.fdfd_set_checkpoint.restype = ip
+    lib.fdfd_set_checkpoint.argtypes = [vp, ip]
+    lib.fdfd_checkpoint_info.restype = ip
+    lib.fdfd_checkpoint_info.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]
     lib.fdfd_mf_create.restype = ip
     lib.fdfd_mf_create.argtypes = [C.POINTER(vp), ip, ip, ip, ip, C.c_double, C.c_double, C.c_double, C.c_double,
                                    C.c_double, ip, ip, ip]
@@ -254,6 +259,15 @@ class Handle:
         buf = C.create_string_buffer(n + 1)
         self.lib.fdfd_get_tuning(self.h, buf, n + 1)
         return buf.value.decode()
+
+    def set_checkpoint(self, mode=0):
+        """Block factors in pinned host memory: 0 automatic (default), 1 always, -1 never."""
+        self._check(self.lib.fdfd_set_checkpoint(self.h, int(mode)))
+
+    def checkpoint_info(self):
+        a, hb, cb = C.c_int(0), C.c_longlong(0), C.c_longlong(0)
+        self._check(self.lib.fdfd_checkpoint_info(self.h, C.byref(a), C.byref(hb), C.byref(cb)))
+        return {"active": bool(a.value), "host_bytes": hb.value, "copied_bytes": cb.value}
 
     def set_eps(self, eps):
         buf = natural(eps)

@@ -96,6 +96,8 @@ template <typename T> struct FactorStore {
     bool tc_ok = false;
     TcMaps tc;       // TMA descriptors (FP32 only)
     bool complete = false;   // every pool above allocated
+    T* hC = nullptr;         // checkpoint mode: pinned host copies of every coupling ring ...
+    T* hX = nullptr;         // ... and of every level's X blocks (original slot numbering)
 };
 
 }  // namespace
@@ -182,6 +184,16 @@ struct fdfd_handle {
     std::vector<int> XL, XR;                        // [node]
     int Xf = -1, C01 = -1, C10 = -1;
     int nCslots = 0, nXslots = 0, max_ne = 0;
+    // per ring e: first coupling slot and slot count; per level e >= 2: first X slot and count
+    // (the plan's own numbering, kept as the host layout of checkpoint mode)
+    std::vector<int> cring0, cringn, xlev0, xlevn;
+    // checkpoint mode: coupling rings alternate between two device buffers and every level's X
+    // blocks share one device window; completed rings and levels live in pinned host memory
+    int ckpt_mode = 0;           // 0 automatic (when the resident factor storage does not fit), 1 on, -1 off
+    bool ckpt = false;           // engaged (the slot tables are remapped to the windows)
+    int ckpt_nA = 0;             // slots of the odd-ring coupling buffer (the even one follows)
+    int orig_nC = 0, orig_nX = 0;   // slot counts of the resident layout
+    long long host_bytes = 0, ckpt_copied = 0;
     std::vector<StepJobs> sj;
     size_t fin_mrg = 0, fin_c_slot = 0, fin_a_slot = 0, fin_xt_a = 0, fin_xt_b = 0, fin_xt_c = 0,
            fin_da_a = 0, fin_da_b = 0, fin_da_c = 0, fin_g1 = 0, fin_g1y = 0, fin_ra = 0, fin_ray = 0,
@@ -414,8 +426,13 @@ void build_plan(fdfd_handle* h) {
     h->Lslot.assign(E + 1, std::vector<int>(n, -1));
     h->Uslot.assign(E + 1, std::vector<int>(n, -1));
     int cs = 0;
-    for (int e = 1; e <= E; ++e)
+    h->cring0.assign(E + 1, 0);
+    h->cringn.assign(E + 1, 0);
+    for (int e = 1; e <= E; ++e) {
+        h->cring0[e] = cs;
         for (int s : rings[e]) { h->Lslot[e][s] = cs++; h->Uslot[e][s] = cs++; }
+        h->cringn[e] = cs - h->cring0[e];
+    }
     h->C01 = cs++;
     h->C10 = cs++;
     h->nCslots = cs;
@@ -423,11 +440,15 @@ void build_plan(fdfd_handle* h) {
     h->XR.assign(n, -1);
     int xs = 0;
     h->max_ne = 1;
+    h->xlev0.assign(E + 1, 0);
+    h->xlevn.assign(E + 1, 0);
     for (int e = 1; e <= E; ++e) {
         const StepPlan& sp = h->steps[e - 1];
         h->max_ne = std::max(h->max_ne, (int)sp.elim.size());
+        h->xlev0[e] = xs;
         if (e >= 2)
             for (int k : sp.elim) { h->XL[k] = xs++; h->XR[k] = xs++; }
+        h->xlevn[e] = xs - h->xlev0[e];
     }
     h->Xf = xs++;
     h->nXslots = xs;
@@ -595,7 +616,124 @@ template <typename T> void free_store(fdfd_handle* h, FactorStore<T>& F) {
     void* bufs[] = {F.D.base, F.C.base, F.X.base, F.GP.base, F.RP.base, F.Tg.base, F.rv, F.xv, F.wv,
                     F.perm, F.rowsrc, F.inv, F.gsub, F.gj_slots, F.trifac, F.tripiv};
     for (void* p : bufs) dev_free(h, p);
+    if (F.hC || F.hX) {
+        const long long se = F.C.slot_elems();
+        h->host_bytes -= (long long)sizeof(T) * se * ((F.hC ? h->orig_nC - 2 : 0) + (F.hX ? h->orig_nX - 1 : 0));
+    }
+    if (F.hC) cudaFreeHost(F.hC);
+    if (F.hX) cudaFreeHost(F.hX);
     F = FactorStore<T>();
+}
+
+// ---------------------------------------------------------------------------
+// Checkpoint mode: block factors beyond HBM.  Resident, the factor storage is
+// n D blocks, about 2n coupling blocks (two per survivor of every ring) and
+// about n X blocks.  The couplings of ring e are written at step e and read at
+// step e+1; the X blocks of step e are read only within step e; after that both
+// serve only the solve sweeps.  In checkpoint mode the rings alternate between
+// two device buffers (odd and even e) and all steps' X blocks share one device
+// window; when step e ends, its X blocks and ring e-1 are copied to pinned host
+// memory (one cudaMemcpyAsync each, in the plan's slot order), and each sweep
+// copies them back step by step before the products that read them.  The device
+// then holds n + ~1.5n + ~n/2 blocks instead of ~4n; the sweeps move the
+// couplings and X blocks over the host link every time.
+// ---------------------------------------------------------------------------
+int restart_len(const fdfd_handle* h, int nrhs);
+
+// device bytes the factorization and a one-source solve will add, resident and in
+// checkpoint mode: D, C and X blocks, the Gauss-Jordan and first-step work space,
+// the sweep vectors and the FP64 Krylov basis (estimates of the later allocations)
+template <typename T> void factor_bytes(const fdfd_handle* h, double* resident, double* windowed) {
+    const int b = h->map.b, n = h->map.n, ld = h->map.ld;
+    const double sb = (double)b * ld * 2 * sizeof(T);
+    int nA = 0, nB = 0, nXw = 0, gj_max = 1;
+    for (int e = 1; e < (int)h->cringn.size(); ++e) {
+        if (e & 1) nA = std::max(nA, h->cringn[e]);
+        else nB = std::max(nB, h->cringn[e]);
+        nXw = std::max(nXw, h->xlevn[e]);
+        if (e >= 2 && e < (int)h->sj.size()) gj_max = std::max(gj_max, h->sj[e].ne);
+    }
+    const int nC = h->ckpt ? h->orig_nC : h->nCslots, nX = h->ckpt ? h->orig_nX : h->nXslots;
+    const double N = (double)h->Nx * h->Ny;
+    const double work = sb * gj_max + 2.0 * 2 * h->max_ne * b * 32 * 4 * sizeof(T) + 3.0 * h->max_ne * b * 4 +
+                        (double)n * 9 * b * sizeof(cplx<T>) + 3.0 * n * 2 * ld * sizeof(T) +
+                        (2.0 * restart_len(h, 1) + 4) * N * sizeof(cplx<double>);
+    *resident = sb * (n + nC + nX) + work;
+    *windowed = sb * (n + nA + nB + 2 + nXw + 1) + work;
+}
+
+// remaps the coupling and X slot tables onto the device windows and rebuilds the job lists
+int ckpt_engage(fdfd_handle* h) {
+    const int E = (int)h->steps.size();
+    int nA = 0, nB = 0, nXw = 0;
+    for (int e = 1; e <= E; ++e) {
+        if (e & 1) nA = std::max(nA, h->cringn[e]);
+        else nB = std::max(nB, h->cringn[e]);
+        nXw = std::max(nXw, h->xlevn[e]);
+    }
+    h->orig_nC = h->nCslots;
+    h->orig_nX = h->nXslots;
+    for (int e = 1; e <= E; ++e) {
+        const int base = (e & 1) ? 0 : nA;
+        for (int& v : h->Lslot[e]) if (v >= 0) v = v - h->cring0[e] + base;
+        for (int& v : h->Uslot[e]) if (v >= 0) v = v - h->cring0[e] + base;
+        if (e >= 2)
+            for (int k : h->steps[e - 1].elim) { h->XL[k] -= h->xlev0[e]; h->XR[k] -= h->xlev0[e]; }
+    }
+    h->C01 = nA + nB;
+    h->C10 = nA + nB + 1;
+    h->nCslots = nA + nB + 2;
+    h->Xf = nXw;
+    h->nXslots = nXw + 1;
+    h->ckpt_nA = nA;
+    JobBlob B;
+    build_jobs(h, B);
+    CK(cudaMemcpy(h->djobs, B.host.data(), B.host.size(), cudaMemcpyHostToDevice));
+    h->ckpt = true;
+    return FDFD_OK;
+}
+
+// device buffer of ring e's couplings in checkpoint mode
+template <typename T> T* ckpt_ring_dev(fdfd_handle* h, int e) {
+    FactorStore<T>& F = store<T>(h);
+    return F.C.slot((e & 1) ? 0 : h->ckpt_nA);
+}
+
+// end of step e: its X blocks and ring e-1 to the host
+template <typename T> int ckpt_offload(fdfd_handle* h, int e) {
+    if (!h->ckpt || e < 2) return FDFD_OK;
+    FactorStore<T>& F = store<T>(h);
+    const size_t se = (size_t)F.C.slot_elems();
+    if (h->xlevn[e]) {
+        const size_t bytes = se * h->xlevn[e] * sizeof(T);
+        CK(cudaMemcpyAsync(F.hX + se * h->xlev0[e], F.X.slot(0), bytes, cudaMemcpyDeviceToHost, h->stream));
+        h->ckpt_copied += (long long)bytes;
+    }
+    if (h->cringn[e - 1]) {
+        const size_t bytes = se * h->cringn[e - 1] * sizeof(T);
+        CK(cudaMemcpyAsync(F.hC + se * h->cring0[e - 1], ckpt_ring_dev<T>(h, e - 1), bytes, cudaMemcpyDeviceToHost,
+                           h->stream));
+        h->ckpt_copied += (long long)bytes;
+    }
+    return FDFD_OK;
+}
+
+// sweeps: ring e back to its device buffer, or step e's X blocks back to the window
+template <typename T> int ckpt_reload_ring(fdfd_handle* h, int e) {
+    if (!h->ckpt || !h->cringn[e]) return FDFD_OK;
+    FactorStore<T>& F = store<T>(h);
+    const size_t se = (size_t)F.C.slot_elems(), bytes = se * h->cringn[e] * sizeof(T);
+    CK(cudaMemcpyAsync(ckpt_ring_dev<T>(h, e), F.hC + se * h->cring0[e], bytes, cudaMemcpyHostToDevice, h->stream));
+    h->ckpt_copied += (long long)bytes;
+    return FDFD_OK;
+}
+template <typename T> int ckpt_reload_x(fdfd_handle* h, int e) {
+    if (!h->ckpt || !h->xlevn[e]) return FDFD_OK;
+    FactorStore<T>& F = store<T>(h);
+    const size_t se = (size_t)F.C.slot_elems(), bytes = se * h->xlevn[e] * sizeof(T);
+    CK(cudaMemcpyAsync(F.X.slot(0), F.hX + se * h->xlev0[e], bytes, cudaMemcpyHostToDevice, h->stream));
+    h->ckpt_copied += (long long)bytes;
+    return FDFD_OK;
 }
 
 template <typename T> int alloc_factor_pools(fdfd_handle* h);
@@ -616,6 +754,21 @@ template <typename T> int alloc_factor(fdfd_handle* h) {
 template <typename T> int alloc_factor_pools(fdfd_handle* h) {
     FactorStore<T>& F = store<T>(h);
     const int b = h->map.b, n = h->map.n, ld = h->map.ld;
+    // checkpoint mode: forced, or automatic when the resident storage would not fit what is
+    // left of the device budget (or of the device's free memory) but the windowed one does
+    if (!h->ckpt && h->ckpt_mode >= 0 && h->steps.size() >= 2) {
+        double resident = 0, windowed = 0;
+        factor_bytes<T>(h, &resident, &windowed);
+        double avail = 0;
+        if (h->dev_budget > 0) {
+            avail = (double)(h->dev_budget - h->dev_bytes);
+        } else {
+            size_t fr = 0, tot = 0;
+            if (cudaMemGetInfo(&fr, &tot) == cudaSuccess) avail = 0.95 * (double)fr;
+            else cudaGetLastError();
+        }
+        if (h->ckpt_mode == 1 || (avail > 0 && resident > avail && windowed < avail)) RET(ckpt_engage(h));
+    }
     const int planes = 2;   // re, im (the tensor-core GEMM forms the TF32 residuals itself)
     // panel buffer width: one panel, or (fused super-panels, FP32 tensor-core path) the
     // gj_fused_k columns of the panels that share one update
@@ -651,6 +804,22 @@ template <typename T> int alloc_factor_pools(fdfd_handle* h) {
         const size_t n1 = (size_t)std::max(1, h->sj[1].ne);
         RET(dev_alloc(h, (void**)&F.trifac, n1 * 8 * b * sizeof(cplx<T>)));
         RET(dev_alloc(h, (void**)&F.tripiv, n1 * b * sizeof(int)));
+    }
+    if (h->ckpt) {
+        const size_t se = (size_t)F.C.slot_elems() * sizeof(T);
+        const size_t bc = se * (h->orig_nC - 2), bx = se * (h->orig_nX - 1);
+        if (cudaHostAlloc((void**)&F.hC, std::max<size_t>(bc, 16), cudaHostAllocDefault) != cudaSuccess) {
+            cudaGetLastError();
+            F.hC = nullptr;
+            return set_err(h, FDFD_ENOMEM, "pinned host memory for the checkpointed couplings (%zu bytes) failed", bc);
+        }
+        h->host_bytes += (long long)bc;
+        if (cudaHostAlloc((void**)&F.hX, std::max<size_t>(bx, 16), cudaHostAllocDefault) != cudaSuccess) {
+            cudaGetLastError();
+            F.hX = nullptr;
+            return set_err(h, FDFD_ENOMEM, "pinned host memory for the checkpointed X blocks (%zu bytes) failed", bx);
+        }
+        h->host_bytes += (long long)bx;
     }
     if (sizeof(T) == 4 && h->use_tc) {
         F.tc_ok = tc_make_maps(reinterpret_cast<Pool<float>*>(&F.D), reinterpret_cast<Pool<float>*>(&F.C),
@@ -978,6 +1147,7 @@ template <typename T> int factor_impl(fdfd_handle* h) {
             }
             flops += 8.0 * b3 * ne * 7;   // inversion + 2 (Xᵀ) + 4 (updates)
         }
+        RET(ckpt_offload<T>(h, e));
     }
     // final pair (a, c)
     launch_madd<T>(h->stream, 2, F.C, J<int3>(h, h->fin_mrg));
@@ -1068,6 +1238,7 @@ template <typename T> int sweep_impl(fdfd_handle* h, int nrhs) {
                 h->launches++;
             }
         } else {
+            RET(ckpt_reload_ring<T>(h, e - 1));
             RET(gemv<T>(h, 0, P_C, P_C, F.xv, F.xv, F.rv, F.rv, J<int4>(h, S.f2), J<int2>(h, S.f2y), S.nf2, S.nf2b, nrhs,
                         (T)-1));
         }
@@ -1095,6 +1266,7 @@ template <typename T> int sweep_impl(fdfd_handle* h, int nrhs) {
                             nrhs, (T)-1));
             }
         } else {
+            RET(ckpt_reload_x<T>(h, e));
             RET(gemv<T>(h, 1, P_X, P_X, F.xv, F.xv, F.xv, F.xv, J<int4>(h, S.bw), J<int2>(h, S.bwy), S.ne, 2 * S.ne, nrhs,
                         (T)-1));
         }
@@ -1714,6 +1886,28 @@ int fdfd_set_wait_limit(fdfd_handle* h, long long ns) {
     if (h->mf)
         for (fdfd_handle* s : h->mf->sub) s->wait_ns = ns > 0 ? (unsigned long long)ns : 0ull;
     h->wait_ns = ns > 0 ? (unsigned long long)ns : 0ull;
+    return FDFD_OK;
+}
+
+int fdfd_set_checkpoint(fdfd_handle* h, int mode) {
+    if (!h || mode < -1 || mode > 1) return FDFD_EINVAL;
+    if (h->mf) {
+        for (fdfd_handle* s : h->mf->sub) RET(fdfd_set_checkpoint(s, mode));
+        h->ckpt_mode = mode;
+        return FDFD_OK;
+    }
+    if (h->ckpt && mode < 0) return set_err(h, FDFD_EINVAL, "checkpoint mode is engaged for the handle's lifetime");
+    if (!h->ckpt && mode == 1 && (h->f32.complete || h->f64.complete))
+        return set_err(h, FDFD_EINVAL, "fdfd_set_checkpoint(1) must come before the first factorization");
+    h->ckpt_mode = mode;
+    return FDFD_OK;
+}
+
+int fdfd_checkpoint_info(const fdfd_handle* h, int* active, long long* host_bytes, long long* copied_bytes) {
+    if (!h) return FDFD_EINVAL;
+    if (active) *active = h->ckpt ? 1 : 0;
+    if (host_bytes) *host_bytes = h->host_bytes;
+    if (copied_bytes) *copied_bytes = h->ckpt_copied;
     return FDFD_OK;
 }
 

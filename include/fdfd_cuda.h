@@ -135,6 +135,24 @@ int  fdfd_set_wait_limit(fdfd_handle* h, long long ns);
  * sizes in the message, as a failed cudaMalloc does. */
 int  fdfd_set_device_budget(fdfd_handle* h, long long bytes);
 
+/* Checkpointing of block factors to host memory (no counterpart in the
+ * reference, whose sparse factors live in host memory).  mode 0 (default):
+ * engaged at the first factorization when the resident factor storage would
+ * not fit the handle's device budget (fdfd_set_device_budget) or, without a
+ * budget, 95% of the device's free memory, while the checkpointed storage
+ * does; 1: always (before the first factorization); -1: never.  Engaged, the
+ * coupling blocks of each reduction step and its X blocks move to pinned host
+ * memory as soon as the factorization no longer needs them (one copy per
+ * step), and every solve sweep copies them back step by step: the device holds
+ * about 3n instead of 4n blocks of b x b (n = max(Nx, Ny), b = min(Nx, Ny)),
+ * at the price of host-link traffic in every sweep.  Results are identical to
+ * the resident layout.  Engaged mode lasts for the handle's lifetime.
+ * fdfd_checkpoint_info: engaged flag, pinned host bytes held, bytes copied
+ * between device and host so far. */
+int  fdfd_set_checkpoint(fdfd_handle* h, int mode);
+int  fdfd_checkpoint_info(const fdfd_handle* h, int* active, long long* host_bytes,
+                          long long* copied_bytes);
+
 /* Relative permittivity ϵᵣ (Device.ϵᵣ, src/device.jl:19-25), Nx*Ny complex.
  * Rejects NaN/Inf.  Invalidates any existing factorization. */
 int  fdfd_set_eps(fdfd_handle* h, const double* eps_r);

@@ -54,6 +54,8 @@ int main(void) {
     CHECK(fdfd_set_fallback(NULL, 1) == FDFD_EINVAL);
     CHECK(fdfd_set_wait_limit(NULL, 1000) == FDFD_EINVAL);
     CHECK(fdfd_autotune(NULL) == FDFD_EINVAL);
+    CHECK(fdfd_set_checkpoint(NULL, 1) == FDFD_EINVAL);
+    CHECK(fdfd_checkpoint_info(NULL, NULL, NULL, NULL) == FDFD_EINVAL);
     CHECK(fdfd_get_tuning(NULL, NULL, 0) == -1);
     {
         fdfd_batch* bt = NULL;

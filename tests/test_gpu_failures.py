@@ -90,3 +90,65 @@ def test_device_budget_reports_enomem(lib, fdfd):
     _, _, _, st = h.solve(p.src)
     h.close()
     assert st.rel_residual <= TOL_RES
+
+
+# ---------------------------------------------------------------------------
+# checkpointing of block factors to host memory (capacity beyond HBM)
+# ---------------------------------------------------------------------------
+def ckpt_problem():
+    from fdfd_gb300 import workloads as W
+    return W.design_guide(300, 200, design=(60, 60), seed=8, npml=12)
+
+
+@pytest.mark.parametrize("prec", ["mixed", "fp64"])
+def test_checkpoint_mode_matches_resident(lib, fdfd, prec):
+    """Forced checkpoint mode (couplings and X blocks in pinned host memory, copied back by every
+    sweep) gives the same fields as the resident layout, with less device memory."""
+    p = ckpt_problem()
+    P = fdfd.FDFD_PREC_FP64 if prec == "fp64" else fdfd.FDFD_PREC_MIXED
+    out = {}
+    for mode in (-1, 1):
+        h = handle(fdfd, p, P)
+        h.set_checkpoint(mode)
+        h.set_eps(p.eps)
+        h.factor(p.omega)
+        f1, f2, f3, st = h.solve(p.src)
+        out[mode] = (f1, f2, f3, st.device_bytes, h.checkpoint_info(), st.rel_residual)
+        h.close()
+    res, ck = out[-1], out[1]
+    assert not res[4]["active"] and ck[4]["active"]
+    assert ck[4]["host_bytes"] > 0 and ck[4]["copied_bytes"] > ck[4]["host_bytes"]
+    assert ck[3] < res[3]
+    assert ck[5] <= TOL_RES
+    for a, c in zip(res[:3], ck[:3]):
+        assert rel(c, a) <= 1e-14
+
+
+def test_checkpoint_engages_under_device_budget(lib, fdfd):
+    """Automatic mode: with a device budget between the checkpointed and the resident footprint
+    the handle checkpoints by itself and solves; below the checkpointed footprint it reports
+    FDFD_ENOMEM."""
+    p = ckpt_problem()
+    tot = {}
+    for mode in (-1, 1):
+        h = handle(fdfd, p, fdfd.FDFD_PREC_MIXED)
+        h.set_checkpoint(mode)
+        h.set_eps(p.eps)
+        h.factor(p.omega)
+        _, _, _, st = h.solve(p.src)
+        tot[mode] = st.device_bytes
+        h.close()
+    h = handle(fdfd, p, fdfd.FDFD_PREC_MIXED)
+    h.set_device_budget((tot[-1] + tot[1]) // 2)
+    h.set_eps(p.eps)
+    h.factor(p.omega)
+    _, _, _, st = h.solve(p.src)
+    assert h.checkpoint_info()["active"] and st.rel_residual <= TOL_RES
+    h.close()
+    h = handle(fdfd, p, fdfd.FDFD_PREC_MIXED)
+    h.set_device_budget(tot[1] // 2)
+    h.set_eps(p.eps)
+    with pytest.raises(fdfd.FDFDError) as e:
+        h.factor(p.omega)
+    assert e.value.code == fdfd._lib.FDFD_ENOMEM
+    h.close()
