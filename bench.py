@@ -351,6 +351,10 @@ def run_extras(L, pkg, W, a):
     except Exception as e:   # reported, not hidden
         out["modulated"] = {"error": str(e)}
     try:
+        out["checkpoint"] = run_checkpoint(L, pkg, W)
+    except Exception as e:   # reported, not hidden
+        out["checkpoint"] = {"error": str(e)}
+    try:
         out["mode_sources"] = run_mode_sources(L, pkg, W)
     except Exception as e:   # reported, not hidden
         out["mode_sources"] = {"error": str(e)}
@@ -358,6 +362,39 @@ def run_extras(L, pkg, W, a):
         out["mixed_batch"] = run_mixed_batch(L, pkg, W)
     except Exception as e:
         out["mixed_batch"] = {"error": str(e)}
+    return out
+
+
+def run_checkpoint(L, pkg, W):
+    """The benchmark workload (800x480) with its block factors checkpointed to pinned host memory
+    (fdfd_set_checkpoint(1)) next to the resident layout: solves/s, device bytes, host bytes and
+    the bytes moved over the host link per solve.  Three timed solves each after one warm-up."""
+    import numpy as np
+    p = W.design_guide()
+    out = {}
+    for mode, name in ((-1, "resident"), (1, "checkpointed")):
+        h = L.Handle(p.Nx, p.Ny, p.npml[0], p.npml[1], p.dx, p.dy, 1e-6, p.pml_m, p.pml_lnR, pkg.TM,
+                     L.FDFD_PREC_MIXED)
+        h.set_refinement(1e-10, 80)
+        h.set_checkpoint(mode)
+        h.set_eps(p.eps)
+        h.factor(p.omega)
+        f = h.solve(p.src)
+        c0 = h.checkpoint_info()["copied_bytes"]
+        n = 3
+        t0 = time.perf_counter()
+        for _ in range(n):
+            h.factor(p.omega)
+            f = h.solve(p.src)
+        t = time.perf_counter() - t0
+        info = h.checkpoint_info()
+        out[name] = {"solves_per_s": n / t, "device_bytes": f[3].device_bytes, "host_bytes": info["host_bytes"],
+                     "host_link_bytes_per_solve": (info["copied_bytes"] - c0) / n,
+                     "rel_residual": f[3].rel_residual, "ez": f[0]}
+        h.close()
+    out["field_diff"] = float(np.linalg.norm(out["checkpointed"].pop("ez") - out["resident"]["ez"]) /
+                              np.linalg.norm(out["resident"].pop("ez")))
+    out["workload"] = "design_guide 800x480, mixed, block factors resident vs checkpointed to pinned host memory"
     return out
 
 
