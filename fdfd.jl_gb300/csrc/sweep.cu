@@ -266,21 +266,49 @@ __global__ void diag_sweep_kernel(NodeMap m, const cplx<double>* st, double scal
 // the xGTTRF factors of T0 and the Sherman-Morrison-Woodbury terms),
 //     D_k⁻¹ v = T0⁻¹ v − z0 (w0·v) − zN (w1·v),
 // with the xGTTRS recurrences for T0⁻¹.  That reads 8b complex factor values
-// per node instead of the b² of the dense inverse.  One warp per node: the
-// node's factors and up to `rc` right-hand sides are staged in shared memory
-// with coalesced loads, lane r runs the serial recurrences of right-hand side
-// r out of shared memory (the dots with the original v are formed in the
-// forward pass), and the warp writes y back coalesced.
+// per node instead of the b² of the dense inverse.
+//
+// One warp per node, the node's factors in shared memory.  Both recurrences
+// are affine in their carried state, so the warp runs them as scans: each
+// lane composes the maps of a contiguous chunk of steps, a shuffle scan of the
+// 32 composed maps gives every lane the state entering its chunk, and the
+// lanes replay their chunks.  Forward (L y = P v, interchanges between
+// neighbours): the state is the pending entry s, and step i maps
+//     no interchange:  y_i = s,       s ← −l_i s + v_{i+1}
+//     interchange:     y_i = v_{i+1}, s ← s − l_i v_{i+1}
+// with y_{b−1} the final state.  Backward (U x = y): the state is
+// (x_i, x_{i+1}), and step i (from b−2 down to 0) maps it by
+//     x_i = dinv_i (y_i − du_i x_{i+1} − du2_i x_{i+2}),
+// a 2 x 2 complex matrix and a 2-vector.  The chain of one right-hand side
+// is then about 2·b/32 steps per lane plus two 5-round scans instead of 2·b
+// dependent steps on one lane.  The multipliers l_i of a partially pivoted
+// factorization are at most one in magnitude, so the composed forward maps
+// stay bounded.  The Woodbury dots come from a warp reduction over v.
 // jobs[j] = node of factor workspace j; grid: njobs, block 32,
-// dynamic smem (8b + rc·b) cplx<T> + b ints
+// dynamic smem 10b cplx<T> + b ints
+template <typename T>
+__device__ __forceinline__ cplx<T> shfl_up_c(cplx<T> z, int d) {
+    return cmk(__shfl_up_sync(0xffffffffu, z.re, d), __shfl_up_sync(0xffffffffu, z.im, d));
+}
+template <typename T>
+__device__ __forceinline__ cplx<T> shfl_idx_c(cplx<T> z, int src) {
+    return cmk(__shfl_sync(0xffffffffu, z.re, src), __shfl_sync(0xffffffffu, z.im, src));
+}
+template <typename T>
+__device__ __forceinline__ cplx<T> shfl_xor_c(cplx<T> z, int m) {
+    return cmk(__shfl_xor_sync(0xffffffffu, z.re, m), __shfl_xor_sync(0xffffffffu, z.im, m));
+}
+
 template <typename T>
 __global__ void __launch_bounds__(32) tri_apply_kernel(int b, int ld, int nrhs, int rc, const int* jobs,
                                                        const cplx<T>* __restrict__ fac, const int* __restrict__ piv,
                                                        const T* V, const T* Y0, T* Y, T alpha) {
+    (void)rc;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cplx<T>* sf = reinterpret_cast<cplx<T>*>(smem_raw);      // dl du du2 dinv z0 zN w0 w1
-    cplx<T>* sv = sf + 8 * (size_t)b;                          // rc vectors of b
-    int* sp = reinterpret_cast<int*>(sv + (size_t)rc * b);
+    cplx<T>* sv = sf + 8 * (size_t)b;                          // v of the current right-hand side
+    cplx<T>* sy = sv + b;                                      // y, then the output
+    int* sp = reinterpret_cast<int*>(sy + b);
     const int j = blockIdx.x, lane = threadIdx.x;
     const int node = jobs[j];
     const cplx<T>* f = fac + (size_t)j * 8 * b;
@@ -294,57 +322,119 @@ __global__ void __launch_bounds__(32) tri_apply_kernel(int b, int ld, int nrhs, 
     const cplx<T>* zN = sf + 5 * b;
     const cplx<T>* w0 = sf + 6 * b;
     const cplx<T>* w1 = sf + 7 * b;
-    for (int r0 = 0; r0 < nrhs; r0 += rc) {
-        const int nr = min(rc, nrhs - r0);
-        for (int q = 0; q < nr; ++q) {
-            const T* v = V + ((size_t)node * nrhs + r0 + q) * 2 * ld;
-            for (int i = lane; i < b; i += 32) sv[(size_t)q * b + i] = cmk(v[i], v[ld + i]);
-        }
+    const cplx<T> one = cmk((T)1, (T)0), zero = cmk((T)0, (T)0);
+    const int steps = b - 1;                      // both recurrences have b − 1 steps
+    const int ch = (steps + 31) / 32;
+    const int k0 = min(steps, lane * ch), k1 = min(steps, k0 + ch);
+    for (int r = 0; r < nrhs; ++r) {
+        const size_t vo = ((size_t)node * nrhs + r) * 2 * ld;
+        const T* v = V + vo;
         __syncwarp();
-        if (lane < nr) {
-            cplx<T>* x = sv + (size_t)lane * b;
-            // L y = P v in place (interchanges between neighbours), dots with the original v
-            cplx<T> xi = x[0];
-            cplx<T> c0 = cmul(w0[0], xi), c1 = cmul(w1[0], xi);
-#pragma unroll 4
-            for (int i = 0; i + 1 < b; ++i) {
-                const cplx<T> xn = x[i + 1];
-                c0 = cadd(c0, cmul(w0[i + 1], xn));
-                c1 = cadd(c1, cmul(w1[i + 1], xn));
-                const cplx<T> l = dl[i];
+        for (int i = lane; i < b; i += 32) sv[i] = cmk(v[i], v[ld + i]);
+        __syncwarp();
+        // Woodbury dots with the original v
+        cplx<T> c0 = zero, c1 = zero;
+        for (int i = lane; i < b; i += 32) {
+            c0 = cadd(c0, cmul(w0[i], sv[i]));
+            c1 = cadd(c1, cmul(w1[i], sv[i]));
+        }
+#pragma unroll
+        for (int m = 16; m > 0; m >>= 1) {
+            c0 = cadd(c0, shfl_xor_c(c0, m));
+            c1 = cadd(c1, shfl_xor_c(c1, m));
+        }
+        // ---- forward: compose this lane's maps s ← a s + c
+        cplx<T> A = one, C = zero;
+        for (int i = k0; i < k1; ++i) {
+            const cplx<T> xn = sv[i + 1];
+            const bool keep = sp[i] == i;
+            const cplx<T> a = keep ? cneg(dl[i]) : one;
+            const cplx<T> c = keep ? xn : cneg(cmul(dl[i], xn));
+            A = cmul(a, A);
+            C = cadd(cmul(a, C), c);
+        }
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const cplx<T> Ap = shfl_up_c(A, d), Cp = shfl_up_c(C, d);
+            if (lane >= d) {
+                C = cadd(cmul(A, Cp), C);
+                A = cmul(A, Ap);
+            }
+        }
+        const cplx<T> v0 = sv[0];
+        {
+            const cplx<T> Ae = shfl_up_c(A, 1), Ce = shfl_up_c(C, 1);
+            const cplx<T> last = cadd(cmul(shfl_idx_c(A, 31), v0), shfl_idx_c(C, 31));
+            cplx<T> st = lane == 0 ? v0 : cadd(cmul(Ae, v0), Ce);
+            for (int i = k0; i < k1; ++i) {
+                const cplx<T> xn = sv[i + 1];
                 if (sp[i] == i) {
-                    x[i] = xi;
-                    xi = csub(xn, cmul(l, xi));
+                    sy[i] = st;
+                    st = csub(xn, cmul(dl[i], st));
                 } else {
-                    x[i] = xn;
-                    xi = csub(xi, cmul(l, xn));
+                    sy[i] = xn;
+                    st = csub(st, cmul(dl[i], xn));
                 }
             }
-            // U x = y, then x − z0 c0 − zN c1, row b-1 first (in place)
-            cplx<T> x1 = cmul(xi, dinv[b - 1]), x2 = cmk((T)0, (T)0);
-            x[b - 1] = csub(csub(x1, cmul(z0[b - 1], c0)), cmul(zN[b - 1], c1));
-#pragma unroll 4
-            for (int i = b - 2; i >= 0; --i) {
-                const cplx<T> xv = cmul(csub(csub(x[i], cmul(du[i], x1)), cmul(du2[i], x2)), dinv[i]);
-                x[i] = csub(csub(xv, cmul(z0[i], c0)), cmul(zN[i], c1));
-                x2 = x1;
-                x1 = xv;
-            }
+            if (lane == 0) sy[b - 1] = last;
         }
         __syncwarp();
-        for (int q = 0; q < nr; ++q) {
-            const size_t vo = ((size_t)node * nrhs + r0 + q) * 2 * ld;
-            const T* y0 = Y0 ? Y0 + vo : nullptr;
-            T* y = Y + vo;
-            for (int i = lane; i < b; i += 32) {
-                const cplx<T> g = sv[(size_t)q * b + i];
-                T o_r = alpha * g.re, o_i = alpha * g.im;
-                if (y0) { o_r += y0[i]; o_i += y0[ld + i]; }
-                y[i] = o_r;
-                y[ld + i] = o_i;
+        // ---- backward: compose this lane's maps (x_i, x_{i+1}) ← M (x_{i+1}, x_{i+2}) + t, i = b−2−k
+        cplx<T> m00 = one, m01 = zero, m10 = zero, m11 = one, t0 = zero, t1 = zero;
+        for (int k = k0; k < k1; ++k) {
+            const int i = b - 2 - k;
+            const cplx<T> g = dinv[i];
+            const cplx<T> p = cneg(cmul(g, du[i])), q = cneg(cmul(g, du2[i]));   // row 0 of the step's matrix
+            const cplx<T> u = cmul(g, sy[i]);
+            // step ∘ current: [[p, q], [1, 0]]·M and [[p, q], [1, 0]]·t + (u, 0)
+            const cplx<T> n00 = cadd(cmul(p, m00), cmul(q, m10)), n01 = cadd(cmul(p, m01), cmul(q, m11));
+            const cplx<T> nt0 = cadd(cadd(cmul(p, t0), cmul(q, t1)), u);
+            m10 = m00; m11 = m01; t1 = t0;
+            m00 = n00; m01 = n01; t0 = nt0;
+        }
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const cplx<T> a00 = shfl_up_c(m00, d), a01 = shfl_up_c(m01, d), a10 = shfl_up_c(m10, d),
+                          a11 = shfl_up_c(m11, d), s0 = shfl_up_c(t0, d), s1 = shfl_up_c(t1, d);
+            if (lane >= d) {
+                // this lane's maps after the earlier lanes': M·A and M·s + t
+                const cplx<T> n00 = cadd(cmul(m00, a00), cmul(m01, a10)), n01 = cadd(cmul(m00, a01), cmul(m01, a11));
+                const cplx<T> n10 = cadd(cmul(m10, a00), cmul(m11, a10)), n11 = cadd(cmul(m10, a01), cmul(m11, a11));
+                const cplx<T> nt0 = cadd(cadd(cmul(m00, s0), cmul(m01, s1)), t0);
+                const cplx<T> nt1 = cadd(cadd(cmul(m10, s0), cmul(m11, s1)), t1);
+                m00 = n00; m01 = n01; m10 = n10; m11 = n11; t0 = nt0; t1 = nt1;
             }
         }
+        {
+            const cplx<T> e00 = shfl_up_c(m00, 1), e01 = shfl_up_c(m01, 1), e10 = shfl_up_c(m10, 1),
+                          e11 = shfl_up_c(m11, 1), f0 = shfl_up_c(t0, 1), f1 = shfl_up_c(t1, 1);
+            const cplx<T> xl = cmul(sy[b - 1], dinv[b - 1]);      // state (x_{b−1}, 0) entering step b−2
+            cplx<T> x0 = xl, x1 = zero;
+            if (lane > 0) {
+                x0 = cadd(cmul(e00, xl), f0);
+                x1 = cadd(cmul(e10, xl), f1);
+                (void)e01; (void)e11;
+            }
+            __syncwarp();
+            for (int k = k0; k < k1; ++k) {
+                const int i = b - 2 - k;
+                const cplx<T> xv = cmul(csub(csub(sy[i], cmul(du[i], x0)), cmul(du2[i], x1)), dinv[i]);
+                sy[i] = csub(csub(xv, cmul(z0[i], c0)), cmul(zN[i], c1));
+                x1 = x0;
+                x0 = xv;
+            }
+            if (lane == 0) sy[b - 1] = csub(csub(xl, cmul(z0[b - 1], c0)), cmul(zN[b - 1], c1));
+        }
         __syncwarp();
+        const T* y0 = Y0 ? Y0 + vo : nullptr;
+        T* y = Y + vo;
+        for (int i = lane; i < b; i += 32) {
+            const cplx<T> g = sy[i];
+            T o_r = alpha * g.re, o_i = alpha * g.im;
+            if (y0) { o_r += y0[i]; o_i += y0[ld + i]; }
+            y[i] = o_r;
+            y[ld + i] = o_i;
+        }
     }
 }
 
@@ -419,15 +509,12 @@ template <typename T>
 int launch_tri_apply(cudaStream_t s, int b, int ld, int njobs, int nrhs, const int* jobs, const cplx<T>* fac,
                      const int* piv, const T* V, const T* Y0, T* Y, T alpha) {
     if (njobs == 0 || nrhs == 0) return 0;
-    constexpr size_t kMaxSmem = 200 * 1024;
+    const size_t smem = 10 * (size_t)b * sizeof(cplx<T>) + (size_t)b * sizeof(int);
+    if (smem > 200 * 1024) return (int)cudaErrorInvalidValue;
     static const cudaError_t attr = cudaFuncSetAttribute(tri_apply_kernel<T>,
-                                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem);
+                                                         cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     if (attr != cudaSuccess) return (int)attr;
-    const size_t fixed = 8 * (size_t)b * sizeof(cplx<T>) + (size_t)b * sizeof(int);
-    const size_t per = (size_t)b * sizeof(cplx<T>);
-    if (fixed + per > kMaxSmem) return (int)cudaErrorInvalidValue;
-    const int rc = (int)std::min<size_t>(std::min(nrhs, 32), (kMaxSmem - fixed) / per);
-    tri_apply_kernel<T><<<njobs, 32, fixed + (size_t)rc * per, s>>>(b, ld, nrhs, rc, jobs, fac, piv, V, Y0, Y, alpha);
+    tri_apply_kernel<T><<<njobs, 32, smem, s>>>(b, ld, nrhs, 1, jobs, fac, piv, V, Y0, Y, alpha);
     return (int)cudaGetLastError();
 }
 template int launch_tri_apply<float>(cudaStream_t, int, int, int, int, const int*, const cplx<float>*, const int*,
