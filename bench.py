@@ -47,6 +47,8 @@ def args():
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the adjoint / eigenfrequency / frequency-sweep measurements")
     ap.add_argument("--seed", type=int, default=2, help="seed of the random design region (2: the benchmark's)")
+    ap.add_argument("--autotune", type=int, default=1, choices=[0, 1],
+                    help="1: run the launch-shape autotuner on the timed handles first (outside the timed region)")
     ap.add_argument("--size", default=None,
                     help="NXxNY: same problem family at another size (profiling runs); design region = "
                          "a quarter of the smaller side squared")
@@ -626,6 +628,7 @@ def main():
         return h.solve_device(d_src.data_ptr(), 1, d_f[0].data_ptr(), d_f[1].data_ptr(), d_f[2].data_ptr())
 
     h = make(L.FDFD_PREC_MIXED)
+    tuned = h.autotune() if a.autotune else None
     for _ in range(a.warmup):
         step_device(h)
     torch.cuda.synchronize()
@@ -689,6 +692,8 @@ def main():
     if not a.no_e2e:
         import ctypes
         he = make(L.FDFD_PREC_MIXED)
+        if a.autotune:
+            he.autotune()
         h2d = N * 16 * 2
         d2h = N * 16 * 3
         eps_c, src_c = L.natural(p.eps), L.natural(p.src)
@@ -774,7 +779,10 @@ def main():
                 "config": {"workload": workload, "precision": "mixed: FP32 factors, 3xTF32 tcgen05 products, "
                                                             "FP64 FGMRES refinement",
                            "l2": "inputs larger than L2 (factor storage ~6 GB per solve, no flush needed)",
-                           "parallelism": f"replicas x{world}"},
+                           "parallelism": f"replicas x{world}",
+                           "launch_shapes": ("autotuned (fdfd_autotune, before the warm-up): " +
+                                             json.dumps(tuning_summary([tuned])) if tuned else
+                                             "the library's rule (widest tile that fills the GPU)")},
                 "e2e": e2e, "gpu_launches": launches, "roofline": roof, "roofline_hbm": roof_hbm,
                 "cpu_baseline": cpu, "clocks": clk,
                 "rel_residual_max": maxres, "refine_iterations": iters, "field_err_vs_oracle": vs_oracle,
