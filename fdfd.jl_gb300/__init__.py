@@ -413,7 +413,7 @@ def make_handle(d: Device, pol=TM, precision="mixed", pml_m=3.5, pml_lnR=-12.0, 
 
 
 def solve(d: Device, pol=TM, precision="mixed", pml_m=3.5, pml_lnR=-12.0, tol=1e-10, max_iter=40,
-          return_stats=False):
+          return_stats=False, frequencies_per_launch=1, autotune=False):
     """solve(d::Device, pol) — src/solver/driven.jl:4-59.
 
     One factorization per frequency (as the reference re-factors per ω) and a
@@ -421,13 +421,23 @@ def solve(d: Device, pol=TM, precision="mixed", pml_m=3.5, pml_lnR=-12.0, tol=1e
     reference hard-wires (src/pml.jl:1, S_create does not forward them).
     Returns a FieldTM/FieldTE, or a list when len(d.omega) > 1 (driven.jl:57-58).
     A ModulatedDevice takes the coupled-sideband path (``solve_modulated``).
+
+    ``frequencies_per_launch`` > 1 (several frequencies, no mode sources): that many
+    handles are factored together, one frequency each, by one CUDA-graph launch
+    (fdfd_batch_factor), and their solves run concurrently.  ``autotune`` runs the
+    launch-shape autotuner on every handle first.
     """
     if isinstance(d, ModulatedDevice):
         return solve_modulated(d, precision, pml_m, pml_lnR, tol, max_iter, return_stats)
     if isinstance(d, Chi3Device):
         # solve(d::χ3Device, which_method): the second argument is the iterative method
         return solve_chi3(d, pol, precision, pml_m, pml_lnR, max_iter=max_iter, return_stats=return_stats)
+    if frequencies_per_launch > 1 and len(d.omega) > 1 and not d.modes:
+        return _solve_batched(d, pol, precision, pml_m, pml_lnR, tol, max_iter, return_stats,
+                              int(frequencies_per_launch), autotune)
     h = make_handle(d, pol, precision, pml_m, pml_lnR, tol, max_iter)
+    if autotune:
+        h.autotune()
     out, stats = [], []
     try:
         if d.modes:
@@ -444,6 +454,43 @@ def solve(d: Device, pol=TM, precision="mixed", pml_m=3.5, pml_lnR=-12.0, tol=1e
             stats.append(st.as_dict())
     finally:
         h.close()
+    res = out[0] if len(out) == 1 else out
+    return (res, stats) if return_stats else res
+
+
+def _solve_batched(d, pol, precision, pml_m, pml_lnR, tol, max_iter, return_stats, width, autotune):
+    """solve() for many frequencies: `width` handles, one CUDA-graph launch factoring a wave of
+    `width` frequencies, then their solves concurrently (the driver's threads wait in the library,
+    outside the interpreter lock)."""
+    import concurrent.futures as cf
+    omegas = list(d.omega)
+    width = min(width, len(omegas))
+    hs = [make_handle(d, pol, precision, pml_m, pml_lnR, tol, max_iter) for _ in range(width)]
+    cls = FieldTM if pol == TM else FieldTE
+    out, stats = [None] * len(omegas), [None] * len(omegas)
+    batch = None
+    try:
+        if autotune:
+            for h in hs:
+                h.autotune()
+        batch = _lib.Batch(hs)
+        with cf.ThreadPoolExecutor(max_workers=width) as ex:
+            for w0 in range(0, len(omegas), width):
+                wave = omegas[w0:w0 + width]
+                if len(wave) == width:
+                    batch.factor(wave)
+                else:                        # a short last wave: its handles factor one by one
+                    for h, w in zip(hs, wave):
+                        h.factor(w)
+                res = list(ex.map(lambda h: h.solve(d.src), hs[:len(wave)]))
+                for k, (w, (f1, f2, f3, st)) in enumerate(zip(wave, res)):
+                    out[w0 + k] = cls(d.grid, w, np.stack([f1, f2, f3], axis=-1))
+                    stats[w0 + k] = st.as_dict()
+    finally:
+        if batch is not None:
+            batch.close()
+        for h in hs:
+            h.close()
     res = out[0] if len(out) == 1 else out
     return (res, stats) if return_stats else res
 

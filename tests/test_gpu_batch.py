@@ -107,3 +107,20 @@ def test_autotune_records_choices_and_keeps_results(lib, fdfd, oracle, prec):
     tol = 1e-8 if prec == "mixed" else 1e-10
     assert st.rel_residual <= TOL_RES
     assert max(rel(f1, ref[0]), rel(f2, ref[1]), rel(f3, ref[2])) <= tol
+
+
+def test_mirror_solve_batches_frequencies(lib, fdfd):
+    """solve(d, TM, frequencies_per_launch=4) on a device with six frequencies (one graph wave
+    of four, a short wave of two) gives the fields of the frequency-by-frequency solve."""
+    g = fdfd.Grid(0.05, (10, 10), (-3.0, 3.0), (-2.0, 2.0))
+    lams = np.linspace(1.45, 1.65, 6)
+    d = fdfd.Device(g, [2 * np.pi * 299792458.0 / (l * 1e-6) for l in lams])
+    fdfd.setup_eps(d, lambda x, y: abs(y) < 0.25, 12.25)
+    fdfd.setup_src(d, fdfd.Point(-2.0, 0.0))
+    ref = fdfd.solve(d, fdfd.TM)
+    got, st = fdfd.solve(d, fdfd.TM, frequencies_per_launch=4, autotune=True, return_stats=True)
+    assert len(got) == 6
+    for a, b in zip(got, ref):
+        for c in ("Ez", "Hx", "Hy"):
+            assert rel(a[c], b[c]) <= 1e-8
+    assert max(s["rel_residual"] for s in st) <= TOL_RES
