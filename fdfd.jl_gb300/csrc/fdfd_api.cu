@@ -2871,20 +2871,20 @@ template <typename T> int autotune_impl(fdfd_handle* h) {
             int best = 0;
             double tbest = 1e30;
             std::string cand;
-            for (int bn : {64, 128, 256}) {
-                if ((bn == 256 && N <= 128) || (bn == 128 && N <= 64)) continue;   // no wider than the product
+            for (int bn : {64, 128, TC_BN128_TWO, 256}) {
+                if ((bn == 256 && N <= 128) || (bn != 64 && N <= 64)) continue;   // no wider than the product
                 h->force_bn = bn;
                 double ms = 0;
                 const int rc = time_launch(h, launch, &ms);
                 h->force_bn = 0;
                 RET(rc);
-                snprintf(line, sizeof line, " %d:%.4f", bn, ms);
+                snprintf(line, sizeof line, " %s:%.4f", tc_tile_name(bn), ms);
                 cand += line;
                 if (ms < tbest) { tbest = ms; best = bn; }
             }
             h->tune_gemm[key] = best;
-            snprintf(line, sizeof line, "gemm %-10s M=%d N=%d K=%d jobs=%d -> BN=%d  (ms%s)\n", role, M, N, K, njobs,
-                     best, cand.c_str());
+            snprintf(line, sizeof line, "gemm %-10s M=%d N=%d K=%d jobs=%d -> BN=%s  (ms%s)\n", role, M, N, K, njobs,
+                     tc_tile_name(best), cand.c_str());
             log += line;
             return FDFD_OK;
         };
@@ -3438,8 +3438,10 @@ int debug_gemm_impl(int M, int N, int K, const double* A, const double* B, doubl
             int dev = 0, sms = 0;
             cudaGetDevice(&dev);
             cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-            const int bn = (use_tc == 64 || use_tc == 128 || use_tc == 256) ? use_tc : tc_pick_bn(M, N, K, 1, sms);
-            const int bi = bn == 256 ? 1 : (bn == 128 ? 0 : 2);
+            const int bn = (use_tc == 64 || use_tc == 128 || use_tc == 256 || use_tc == TC_BN128_TWO)
+                               ? use_tc
+                               : tc_pick_bn(M, N, K, 1, sms);
+            const int bi = bn == 256 ? 1 : ((bn == 128 || bn == TC_BN128_TWO) ? 0 : 2);
             if (rc == FDFD_OK) {
                 cudaEventRecord(e0);
                 if (tc_gemm_launch_maps(reinterpret_cast<GemmArgs<float>*>(&g), nullptr, &ma[0], &mb[bi], bn, 1, 0) !=

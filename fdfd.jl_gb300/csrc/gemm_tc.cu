@@ -35,19 +35,25 @@
 
 namespace {
 
-constexpr int BM = 128, BK = 8, STAGES = 4;
+constexpr int BM = 128, BK = 8;
 constexpr int A_PLANE_BYTES = BM * BK * 4;                  // 4 KB
-template <int BN> struct TcTile {
+// TWO = 1: a 128-column tile sized so that two CTAs share an SM (three pipeline
+// stages, one epilogue warp per TMEM lane quarter), so one CTA's epilogue overlaps
+// the other's MMAs; an autotuner candidate beside the one-CTA tiles.
+template <int BN, int TWO = 0> struct TcTile {
+    static constexpr int STAGES = TWO ? 3 : 4;
     // epilogue warps: two per TMEM lane quarter (each takes half the columns),
-    // one at BN = 64 (two CTAs share an SM there)
-    static constexpr int NEPI = BN >= 128 ? 8 : 4;
+    // one at BN = 64 and in the two-CTA form (two CTAs share an SM there)
+    static constexpr int NEPI = (BN >= 128 && !TWO) ? 8 : 4;
     static constexpr int THREADS = 64 + 32 * NEPI;
+    static constexpr int MIN_BLOCKS = (BN <= 64 || TWO) ? 2 : 1;
     static constexpr int B_PLANE_BYTES = BN * BK * 4;
     static constexpr int STAGE_BYTES = 4 * A_PLANE_BYTES + 4 * B_PLANE_BYTES;
     static constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024;   // + alignment slack
     static constexpr uint32_t TMEM_COLS = 2 * BN;                     // re and im accumulators
     // the epilogue stages NEPI warps x 2 x 32 x 36 floats in the idle pipeline buffers
     static_assert(STAGES * STAGE_BYTES >= NEPI * 2 * 32 * 36 * 4, "epilogue staging");
+    static_assert(MIN_BLOCKS * (SMEM_BYTES + 1024) <= 227 * 1024, "shared memory per SM");
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -151,14 +157,15 @@ struct TcParams {
     GemmArgs<float> g;
 };
 
-template <int BN>
-__global__ void __launch_bounds__(TcTile<BN>::THREADS, BN <= 64 ? 2 : 1)
+template <int BN, int TWO>
+__global__ void __launch_bounds__(TcTile<BN, TWO>::THREADS, TcTile<BN, TWO>::MIN_BLOCKS)
     gemm_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
                    const TcParams P) {
-    constexpr int B_PLANE_BYTES = TcTile<BN>::B_PLANE_BYTES;
-    constexpr int STAGE_BYTES = TcTile<BN>::STAGE_BYTES;
-    constexpr uint32_t TMEM_COLS = TcTile<BN>::TMEM_COLS;
-    constexpr int NEPI = TcTile<BN>::NEPI;
+    constexpr int STAGES = TcTile<BN, TWO>::STAGES;
+    constexpr int B_PLANE_BYTES = TcTile<BN, TWO>::B_PLANE_BYTES;
+    constexpr int STAGE_BYTES = TcTile<BN, TWO>::STAGE_BYTES;
+    constexpr uint32_t TMEM_COLS = TcTile<BN, TWO>::TMEM_COLS;
+    constexpr int NEPI = TcTile<BN, TWO>::NEPI;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     __shared__ __align__(8) uint64_t bar_full[STAGES], bar_conv[STAGES], bar_empty[STAGES], bar_acc;
     __shared__ uint32_t tmem_base_slot;
@@ -519,17 +526,18 @@ bool tc_make_maps(const Pool<float>* D, const Pool<float>* C, const Pool<float>*
 }
 
 namespace {
-template <int BN>
+template <int BN, int TWO = 0>
 int tc_launch_bn(const GemmArgs<float>* g, const int* c_trans_arr, const CUtensorMap* mapA, const CUtensorMap* mapB,
                  int njobs, cudaStream_t stream) {
+    typedef TcTile<BN, TWO> Tile;
     static const cudaError_t attr =
-        cudaFuncSetAttribute(gemm_tc_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, TcTile<BN>::SMEM_BYTES);
+        cudaFuncSetAttribute(gemm_tc_kernel<BN, TWO>, cudaFuncAttributeMaxDynamicSharedMemorySize, Tile::SMEM_BYTES);
     if (attr != cudaSuccess) return (int)attr;
     TcParams P;
     P.g = *g;
     if (c_trans_arr) P.g.c_trans_arr = c_trans_arr;
     dim3 grid((g->N + BN - 1) / BN, (g->M + BM - 1) / BM, njobs);
-    gemm_tc_kernel<BN><<<grid, TcTile<BN>::THREADS, TcTile<BN>::SMEM_BYTES, stream>>>(*mapA, *mapB, P);
+    gemm_tc_kernel<BN, TWO><<<grid, Tile::THREADS, Tile::SMEM_BYTES, stream>>>(*mapA, *mapB, P);
     return (int)cudaGetLastError();
 }
 }  // namespace
@@ -539,6 +547,7 @@ int tc_gemm_launch_maps(const GemmArgs<float>* g, const int* c_trans_arr, const 
     switch (bn) {
         case 256: return tc_launch_bn<256>(g, c_trans_arr, mapA, mapB, njobs, stream);
         case 128: return tc_launch_bn<128>(g, c_trans_arr, mapA, mapB, njobs, stream);
+        case TC_BN128_TWO: return tc_launch_bn<128, 1>(g, c_trans_arr, mapA, mapB, njobs, stream);
         case 64: return tc_launch_bn<64>(g, c_trans_arr, mapA, mapB, njobs, stream);
         default: return (int)cudaErrorInvalidValue;
     }

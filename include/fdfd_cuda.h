@@ -427,7 +427,8 @@ int  fdfd_debug_hessenberg_eig(int n, const double* H, double* w, double* V);
  * the library's block GEMM: precision FDFD_PREC_FP64 (CUDA-core FP64) or
  * FDFD_PREC_MIXED (FP32 storage; use_tc = 1 selects the tcgen05 3xTF32
  * kernel with the library's tile choice, 64, 128 or 256 that kernel with
- * 128 x use_tc tiles, 0 the CUDA-core FP32 kernel; a negative use_tc passes
+ * 128 x use_tc tiles, 129 its 128 x 128 tile sized for two CTAs per SM, 0
+ * the CUDA-core FP32 kernel; a negative use_tc passes
  * the operands pre-split, as the Gauss-Jordan panel buffers are).  *ms (may
  * be NULL) receives the kernel time in milliseconds. */
 int  fdfd_debug_gemm(int M, int N, int K, const double* A, const double* B,

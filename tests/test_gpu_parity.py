@@ -34,17 +34,20 @@ def oracle_solve(oracle, p, pol):
 # block GEMM kernels
 # ---------------------------------------------------------------------------
 @pytest.mark.parametrize("M,N,K", [(100, 70, 40), (128, 256, 32), (480, 480, 480), (300, 520, 96)])
-@pytest.mark.parametrize("kind", ["tc", "tc64", "tc128", "tc256", "tcs", "tcs64", "tcs256", "simt32", "simt64"])
+@pytest.mark.parametrize("kind", ["tc", "tc64", "tc128", "tc128x2", "tc256", "tcs", "tcs64", "tcs128x2", "tcs256",
+                                  "simt32", "simt64"])
 def test_block_gemm(lib, fdfd, M, N, K, kind):
     """tc: the tensor-core kernel with the launcher's tile width, residual
-    planes formed in shared memory; tcNN forces 128 x NN tiles; tcs*: operands
+    planes formed in shared memory; tcNN forces 128 x NN tiles (tc128x2: the 128-column
+    tile sized for two CTAs per SM); tcs*: operands
     passed pre-split (four planes); simt32/simt64: the CUDA-core kernels."""
     rng = np.random.default_rng(M * 7 + N * 3 + K)
     A = rng.standard_normal((M, K)) + 1j * rng.standard_normal((M, K))
     B = rng.standard_normal((N, K)) + 1j * rng.standard_normal((N, K))
     ref = A @ B.T
     prec = fdfd.FDFD_PREC_FP64 if kind == "simt64" else fdfd.FDFD_PREC_MIXED
-    use_tc = {"tc": 1, "tc64": 64, "tc128": 128, "tc256": 256, "tcs": -1, "tcs64": -64, "tcs256": -256}.get(kind, 0)
+    use_tc = {"tc": 1, "tc64": 64, "tc128": 128, "tc128x2": 129, "tc256": 256, "tcs": -1, "tcs64": -64,
+              "tcs128x2": -129, "tcs256": -256}.get(kind, 0)
     C, ms = fdfd._lib.debug_gemm(A, B, prec, use_tc)
     err = rel(C, ref)
     # FP32 inputs carry 6e-8 relative rounding; 3xTF32 products keep ~2^-21 per
