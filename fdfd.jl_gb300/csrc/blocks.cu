@@ -943,6 +943,620 @@ __global__ void __launch_bounds__(512, 1) gj_panel_quad_kernel(Pool<T> M, const 
     }
 }
 
+// Gauss-Jordan panel step, row form: thread t holds the R physical rows t·R ..
+// t·R + R - 1 in all NB columns of the panel (registers), so the pivot column of
+// a step is in every thread's own registers and the per-row bookkeeping (pivot
+// key, exchange tracking, deferred scale) runs once per row.  The panel comes in
+// and G goes out through shared memory (rows padded by 16 bytes, so a warp's
+// row reads are conflict-free), with whole 16-byte vectors of consecutive
+// columns per lane in global memory.  Steps run in groups of GS = min(8, NB):
+// the GS steps of a group are unrolled and the register columns rotate by GS
+// after each group, so the columns of the current group always sit in
+// registers 0 .. GS-1 (static indices) while the code stays one group long.
+// The step loop is software-pipelined: step s's pivot search runs
+// before step s-1's rank-1 update of the bulk columns, so the FMA work of one
+// step overlaps the latency chain (warp maximum, publication, block wait,
+// broadcast read) of the next.  Iteration s:
+//   1. column s and the bookkeeping (exchange, deferred scale, the Gauss-Jordan
+//      column s-1) take step s-1's transformation;
+//   2. warp maximum of the pivot keys of column s;
+//   3. the owning lane publishes its row, still lacking step s-1 in the columns
+//      other than s and s-1, with its step s-1 factor; the warp's lanes then
+//      apply step s-1 to it, one column per lane, with the fma sequence the
+//      owner applies to its registers, so the published row is the row the
+//      sequential order would publish; the warp's key; one mbarrier arrival;
+//   4. step s-1 on this thread's other columns (pivot row streamed from shared
+//      memory);
+//   5. bounded wait for every warp's arrival; the winner of step s and the
+//      factors of this thread's rows.
+// Iteration w (the panel width) only applies step w-1 (after the loop when w = NB).  Every element sees the
+// operations of gj_panel_quad_kernel in the same order with the same pivots, so
+// both forms give identical results.  Published rows rotate through three
+// slots: a step's pivot row is read until step s+1's update, and its slot is
+// written again at step s+3, after every warp has arrived at s+2.  A wait that
+// runs past wait_ns sets FDFD_DEVERR_TIMEOUT (the results are then void).
+// grid: njobs, block ceil(b / R / 32)·32 <= 512 threads, dynamic shared memory
+// gj_panel_row_smem<T, NB>(block · R).
+template <typename T, int NB> __host__ __device__ constexpr int gj_row_stride() { return NB * (int)sizeof(T) + 16; }
+template <typename T, int NB> __host__ __device__ constexpr size_t gj_panel_row_smem(int rows) {
+    return (size_t)2 * rows * gj_row_stride<T, NB>();
+}
+
+template <typename T, int NB, int R>
+__global__ void __launch_bounds__(512, 1) gj_panel_row_kernel(Pool<T> M, const int* slots, Pool<T> GP, int* perm,
+                                                              int* rowsrc, int c0, unsigned* err, uint64_t wait_ns) {
+    constexpr int NWM = 16, VW = 16 / sizeof(T), NS = 3;
+    constexpr int RSB = gj_row_stride<T, NB>();           // staging row stride, bytes
+    constexpr int CPR = NB / VW;                          // 16-byte vectors per row and plane
+    constexpr int GS = NB < 8 ? NB : 8, NG = NB / GS;     // steps per group, groups
+    static_assert(NB % VW == 0 && NB <= 32, "row tiling");
+    typedef typename Vec16<T>::type VT;
+    extern __shared__ __align__(16) unsigned char stage[];  // [plane][row] x RSB bytes
+    __shared__ __align__(16) T cand_row[NS][NWM][2 * NB];   // [slot][warp][re | im]
+    __shared__ __align__(16) unsigned cand_key[NS][NWM];
+    __shared__ cplx<T> cand_inv[NS][NWM];
+    __shared__ int cand_lrow[NS][NWM];
+    __shared__ cplx<T> cand_f[NWM];                         // step s-1 factor of the warp's published row
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ int rsm[512 * R];                            // composed row exchanges, every row of the block
+    const int b = M.rows, NT = blockDim.x, NW = NT / 32, NR = NT * R;
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const int row0 = t * R;
+    const int job = blockIdx.x;
+    const T* Mre = M.slot(slots[job]);
+    const T* Mim = Mre + M.plane_elems();
+    const int ld = M.ld;
+    const int w = min(NB, b - c0);
+    const uint32_t bar_a = smem_u32(&bar);
+    auto srow = [&](int plane, int r) { return reinterpret_cast<T*>(stage + ((size_t)plane * NR + r) * RSB); };
+    if (t < NS * NWM) cand_key[t / NWM][t % NWM] = 0u;     // warps beyond the block never publish
+    if (t == 0) mbar_init(bar_a, NW);
+    // the panel, coalesced: consecutive threads take consecutive vectors of a row
+    for (int idx = t; idx < 2 * b * CPR; idx += NT) {
+        const int plane = idx / (b * CPR), rem = idx - plane * b * CPR;
+        const int r = rem / CPR, col = (rem % CPR) * VW;
+        VT a = {};
+        if (col < w) {   // c0 + NB <= ld: the vector stays in the row
+            a = *reinterpret_cast<const VT*>((plane ? Mim : Mre) + (size_t)r * ld + c0 + col);
+#pragma unroll
+            for (int e = 0; e < VW; ++e)
+                if (col + e >= w) reinterpret_cast<T*>(&a)[e] = (T)0;
+        }
+        reinterpret_cast<VT*>(srow(plane, r))[col / VW] = a;
+    }
+    __syncthreads();
+    T vr[R][NB], vi[R][NB];
+    int lrow[R];
+    cplx<T> alpha[R];                                       // deferred pivot-row scales
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+        const int i = row0 + j;
+        lrow[j] = i < b ? i : INT_MAX;
+        alpha[j] = cmk((T)1, (T)0);
+#pragma unroll
+        for (int v = 0; v < CPR; ++v) {
+            VT a = {}, c = {};
+            if (i < b) {
+                a = reinterpret_cast<const VT*>(srow(0, i))[v];
+                c = reinterpret_cast<const VT*>(srow(1, i))[v];
+            }
+#pragma unroll
+            for (int e = 0; e < VW; ++e) {
+                vr[j][v * VW + e] = reinterpret_cast<const T*>(&a)[e];
+                vi[j][v * VW + e] = reinterpret_cast<const T*>(&c)[e];
+            }
+        }
+    }
+    // the previous step: its pivot row (shared memory), reciprocal, logical row and
+    // this thread's factors
+    const T* xp = cand_row[0][0];
+    cplx<T> inv_p = cmk((T)0, (T)0);
+    int pl_p = -1;
+    cplx<T> f[R];
+    bool isp[R];
+#pragma unroll
+    for (int j = 0; j < R; ++j) { f[j] = cmk((T)0, (T)0); isp[j] = false; }
+    bool timed_out = false;
+    // step s-1's transformation of element (j, k)
+    auto upd = [&](int j, int k, T xr_, T xi_) {
+        vr[j][k] = fma(-f[j].re, xr_, fma(f[j].im, xi_, vr[j][k]));
+        vi[j][k] = fma(-f[j].re, xi_, fma(-f[j].im, xr_, vi[j][k]));
+    };
+    // one step of the pipeline; register column sp holds column s = g·GS + sp, and
+    // register (sp + NB - 1) % NB column s - 1 (the registers rotate by GS per group)
+    auto step = [&](const int g, const int sp, const bool last) {
+        const int s = g * GS + sp;
+        const int rprev = (sp + NB - 1) % NB;
+        const bool prev = s > 0 && s - 1 < w;   // step s-1 to apply (uniform)
+        const bool cur = !last && s < w;        // step s to search (uniform)
+        const int slot = s % NS;
+        const int cbase = g * GS;               // absolute column of register 0
+        // 1. column s and the bookkeeping through step s-1
+        if (prev) {
+            if (!last) {
+                const T xs_r = xp[s], xs_i = xp[NB + s];
+#pragma unroll
+                for (int j = 0; j < R; ++j) upd(j, sp, xs_r, xs_i);
+            }
+            const int rp = c0 + s - 1;
+#pragma unroll
+            for (int j = 0; j < R; ++j) {
+                vr[j][rprev] = isp[j] ? (T)1 : -f[j].re;
+                vi[j][rprev] = isp[j] ? (T)0 : -f[j].im;
+                if (isp[j]) alpha[j] = inv_p;
+                lrow[j] = (lrow[j] == rp) ? pl_p : (isp[j] ? rp : lrow[j]);
+            }
+        }
+        if (cur) {
+            // 2. pivot keys of column s
+            const int r0 = c0 + s;
+            unsigned key = 0;
+#pragma unroll
+            for (int j = 0; j < R; ++j)
+                if (lrow[j] >= r0 && lrow[j] < b)
+                    key = max(key, pivot_key((float)(fabs(vr[j][sp]) + fabs(vi[j][sp])), row0 + j));
+            const unsigned wkey = __reduce_max_sync(0xffffffffu, key);
+            // 3. publication (register k is column (cbase + k) mod NB)
+            T* crow = cand_row[slot][warp];
+            if (wkey != 0u) {
+                const int wphys = pivot_key_row(wkey);
+                if (lane == (wphys / R) % 32) {
+                    const int jsel = wphys % R;
+#pragma unroll
+                    for (int j = 0; j < R; ++j) {
+                        if (j == jsel) {
+#pragma unroll
+                            for (int v = 0; v < CPR; ++v) {
+                                VT a, c;
+#pragma unroll
+                                for (int e = 0; e < VW; ++e) {
+                                    reinterpret_cast<T*>(&a)[e] = vr[j][v * VW + e];
+                                    reinterpret_cast<T*>(&c)[e] = vi[j][v * VW + e];
+                                }
+                                const int col = (cbase + v * VW) % NB;
+                                *reinterpret_cast<VT*>(crow + col) = a;
+                                *reinterpret_cast<VT*>(crow + NB + col) = c;
+                            }
+                            cand_inv[slot][warp] = cinv_pow2(cmk(vr[j][sp], vi[j][sp]));
+                            cand_lrow[slot][warp] = lrow[j];
+                            if (s > 0) cand_f[warp] = f[j];
+                        }
+                    }
+                }
+                if (s > 0) {
+                    __syncwarp();
+                    if (lane < NB && lane != s && lane != s - 1) {
+                        const cplx<T> fw = cand_f[warp];
+                        const T xr_ = xp[lane], xi_ = xp[NB + lane];
+                        const T a = crow[lane], c = crow[NB + lane];
+                        crow[lane] = fma(-fw.re, xr_, fma(fw.im, xi_, a));
+                        crow[NB + lane] = fma(-fw.re, xi_, fma(-fw.im, xr_, c));
+                    }
+                }
+            }
+            if (lane == 0) cand_key[slot][warp] = wkey;
+            __syncwarp();
+            if (lane == 0) mbar_arrive(bar_a);
+        }
+        // 4. step s-1 on the other columns
+        if (prev) {
+#pragma unroll
+            for (int v = 0; v < CPR; ++v) {
+                const int col = (cbase + v * VW) % NB;
+                const VT a = *reinterpret_cast<const VT*>(xp + col);
+                const VT c = *reinterpret_cast<const VT*>(xp + NB + col);
+                const T* ar = reinterpret_cast<const T*>(&a);
+                const T* ci = reinterpret_cast<const T*>(&c);
+#pragma unroll
+                for (int e = 0; e < VW; e += 2) {
+                    const int k = v * VW + e;
+                    const bool u0 = (last || k != sp) && k != rprev;
+                    const bool u1 = (last || k + 1 != sp) && k + 1 != rprev;
+                    if constexpr (sizeof(T) == 4) {
+                        if (u0 && u1) {   // both columns: paired FP32 fmas, same operations per element
+                            const float2 x_r = make_float2(ar[e], ar[e + 1]), x_i = make_float2(ci[e], ci[e + 1]);
+#pragma unroll
+                            for (int j = 0; j < R; ++j) {
+                                const float2 fim = make_float2(f[j].im, f[j].im);
+                                const float2 nfr = make_float2(-f[j].re, -f[j].re);
+                                const float2 nfi = make_float2(-f[j].im, -f[j].im);
+                                float2 a2 = make_float2(vr[j][k], vr[j][k + 1]);
+                                float2 c2 = make_float2(vi[j][k], vi[j][k + 1]);
+                                a2 = __ffma2_rn(nfr, x_r, __ffma2_rn(fim, x_i, a2));
+                                c2 = __ffma2_rn(nfr, x_i, __ffma2_rn(nfi, x_r, c2));
+                                vr[j][k] = a2.x; vr[j][k + 1] = a2.y;
+                                vi[j][k] = c2.x; vi[j][k + 1] = c2.y;
+                            }
+                            continue;
+                        }
+                    }
+#pragma unroll
+                    for (int j = 0; j < R; ++j) {
+                        if (u0) upd(j, k, ar[e], ci[e]);
+                        if (u1) upd(j, k + 1, ar[e + 1], ci[e + 1]);
+                    }
+                }
+            }
+        }
+        if (cur) {
+            // 5. every warp's candidate; the winner of step s
+            if (!mbar_wait_spin(bar_a, (uint32_t)(s & 1), wait_ns) && !timed_out) {
+                timed_out = true;
+                dev_error(err, FDFD_DEVERR_TIMEOUT);
+            }
+            unsigned gkey = 0u;
+#pragma unroll
+            for (int q = 0; q < NWM / 4; ++q) {
+                const uint4 kv = reinterpret_cast<const uint4*>(cand_key[slot])[q];
+                gkey = max(gkey, max(max(kv.x, kv.y), max(kv.z, kv.w)));
+            }
+            const int ww = min(pivot_key_row(gkey) / (32 * R), NWM - 1);   // a warp holds 32*R consecutive rows
+            xp = cand_row[slot][ww];
+            pl_p = cand_lrow[slot][ww];
+            const cplx<T> p = cmk(xp[s], xp[NB + s]);
+            const bool bad = !(fabs(p.re) + fabs(p.im) > (T)0) || !isfinite(p.re) || !isfinite(p.im);
+            if (bad && t == 0) dev_error(err, FDFD_DEVERR_SINGULAR);
+            inv_p = bad ? cmk((T)0, (T)0) : cand_inv[slot][ww];
+#pragma unroll
+            for (int j = 0; j < R; ++j) {
+                isp[j] = lrow[j] == pl_p;
+                const cplx<T> fi = cmul(cmk(vr[j][sp], vi[j][sp]), inv_p);
+                f[j] = isp[j] ? cmk((T)0, (T)0) : fi;
+            }
+        }
+    };
+#pragma unroll 1
+    for (int g = 0; g < NG; ++g) {
+#pragma unroll
+        for (int sp = 0; sp < GS; ++sp) step(g, sp, false);
+        if constexpr (NG > 1) {
+            // rotate the register columns by GS: the next group's columns to 0 .. GS-1
+#pragma unroll
+            for (int j = 0; j < R; ++j)
+#pragma unroll
+                for (int c = 0; c < GS; ++c) {   // GS cycles of length NG: one value in flight
+                    const T tr = vr[j][c], ti = vi[j][c];
+#pragma unroll
+                    for (int q = 0; q + 1 < NG; ++q) {
+                        vr[j][c + q * GS] = vr[j][c + (q + 1) * GS];
+                        vi[j][c + q * GS] = vi[j][c + (q + 1) * GS];
+                    }
+                    vr[j][c + (NG - 1) * GS] = tr;
+                    vi[j][c + (NG - 1) * GS] = ti;
+                }
+        }
+    }
+    // the registers are back in column order; a full panel's last step is still to apply
+    if (w == NB) step(NG, 0, true);
+    // deferred pivot-row scales; the rows of G staged in logical order
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+        if (lrow[j] >= b) continue;
+        rsm[lrow[j]] = row0 + j;
+#pragma unroll
+        for (int v = 0; v < CPR; ++v) {
+            VT a, c;
+#pragma unroll
+            for (int e = 0; e < VW; ++e) {
+                const cplx<T> x = cmul(alpha[j], cmk(vr[j][v * VW + e], vi[j][v * VW + e]));
+                reinterpret_cast<T*>(&a)[e] = x.re;
+                reinterpret_cast<T*>(&c)[e] = x.im;
+            }
+            reinterpret_cast<VT*>(srow(0, lrow[j]))[v] = a;
+            reinterpret_cast<VT*>(srow(1, lrow[j]))[v] = c;
+        }
+    }
+    __syncthreads();
+    int* rs = rowsrc + (size_t)job * b;
+    int* pp = perm + (size_t)job * b;
+    int rsv[R], pv[R];
+#pragma unroll
+    for (int u = 0; u < R; ++u) {
+        const int i = t + u * NT;
+        rsv[u] = i < b ? rsm[i] : 0;
+        pv[u] = i < b ? pp[rsv[u]] : 0;
+    }
+    // G (b x NB; the update reads K = NB columns), coalesced
+    {
+        T* gp = GP.slot(job);
+        const long long pe = GP.plane_elems();
+        for (int idx = t; idx < b * CPR; idx += NT) {
+            const int r = idx / CPR, v = idx % CPR;
+            const VT a = reinterpret_cast<const VT*>(srow(0, r))[v];
+            const VT c = reinterpret_cast<const VT*>(srow(1, r))[v];
+            const long long o = (long long)r * GP.ld + v * VW;
+            *reinterpret_cast<VT*>(gp + o) = a;
+            *reinterpret_cast<VT*>(gp + pe + o) = c;
+            if (GP.planes == 4) {   // pre-split tensor-core operand: TF32 residual planes
+                VT al, cl;
+#pragma unroll
+                for (int e = 0; e < VW; ++e) {
+                    reinterpret_cast<T*>(&al)[e] = (T)tf32_lo((float)reinterpret_cast<const T*>(&a)[e]);
+                    reinterpret_cast<T*>(&cl)[e] = (T)tf32_lo((float)reinterpret_cast<const T*>(&c)[e]);
+                }
+                *reinterpret_cast<VT*>(gp + 2 * pe + o) = al;
+                *reinterpret_cast<VT*>(gp + 3 * pe + o) = cl;
+            }
+        }
+    }
+    __syncthreads();   // every old perm entry is read before any is overwritten
+#pragma unroll
+    for (int u = 0; u < R; ++u) {
+        const int i = t + u * NT;
+        if (i < b) {
+            pp[i] = pv[u];
+            rs[i] = rsv[u];
+        }
+    }
+}
+
+// Gauss-Jordan panel step, cluster form, for levels with few matrices: the b x NB
+// panel of one matrix is split by rows over the CL CTAs of a thread-block cluster
+// (CL = 2, 4 or 8), so a level with n matrices keeps n·CL SMs busy instead of n.
+// CTA rank cr holds the physical rows [cr·RPC, cr·RPC + RPC) (RPC = NT/4 · R);
+// inside a CTA the layout is that of gj_panel_quad_kernel (lane quads share R
+// rows, lane c of a quad holds columns [c·C, c·C + C)).  A column step: every warp
+// publishes its best candidate row in its own CTA's shared memory and its key in
+// the key table of every CTA of the cluster; one cluster barrier (release /
+// acquire, so the published rows are visible cluster-wide); every thread takes
+// the largest of the CL·NW keys and reads its C columns of the winning row, the
+// reciprocal of the pivot and the pivot's logical row from the owning CTA through
+// the cluster's shared-memory window.  Candidate slots alternate by step parity:
+// the slot written at step j was last read at step j-2, before the barrier of
+// step j-1.  Pivot keys, the reciprocal and the fma sequence are those of the quad
+// kernel, so both forms give identical results.  grid: njobs·CL, block NT;
+// requires b <= CL·RPC.
+template <int CL> __device__ __forceinline__ void cluster_barrier() {
+    if constexpr (CL > 1)
+        asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+    else
+        __syncthreads();
+}
+template <typename P> __device__ __forceinline__ P* cluster_peer(P* p, unsigned rank) {
+    return static_cast<P*>(__cluster_map_shared_rank((void*)p, rank));
+}
+
+template <typename T, int NB, int R, int NT, int CL>
+__global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT)
+    gj_panel_cl_kernel(Pool<T> M, const int* slots, Pool<T> GP, int* perm, int* rowsrc, int c0, unsigned* err) {
+    constexpr int NW = NT / 32, C = NB / 4, RPC = NT / 4 * R;
+    constexpr int VW = 16 / sizeof(T);
+    constexpr int NK = CL * NW;                       // keys per step, cluster-wide
+    static_assert(C % VW == 0 && (R & (R - 1)) == 0 && NK % 4 == 0 && NT % 32 == 0, "cluster panel tiling");
+    typedef typename Vec16<T>::type VT;
+    __shared__ __align__(16) T cand_row[2][NW][2 * NB];   // [parity][warp][re | im]
+    __shared__ __align__(16) unsigned cand_key[2][NK];    // [parity][rank * NW + warp]
+    __shared__ cplx<T> cand_inv[2][NW];
+    __shared__ int cand_lrow[2][NW];
+    __shared__ int rsm[CL * RPC];                          // composed row exchanges, every row of the matrix
+    const int b = M.rows;
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const int qc = lane & 3;                         // column block of this lane
+    const int qbase = lane & ~3;                     // first lane of the quad
+    unsigned cr;
+    asm("mov.u32 %0, %%cluster_ctarank;" : "=r"(cr));
+    const int rbase = (int)cr * RPC;                 // first physical row of this CTA
+    const int row0 = rbase + (warp * 8 + (lane >> 2)) * R;
+    const int job = blockIdx.x / CL;
+    const T* Mre = M.slot(slots[job]);
+    const T* Mim = Mre + M.plane_elems();
+    const int ld = M.ld;
+    const int w = min(NB, b - c0);
+    T vr[R][C], vi[R][C];
+    int lrow[R];
+    cplx<T> alpha[R];                                // deferred pivot-row scales
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+        const int i = row0 + j;
+        lrow[j] = i < b ? i : INT_MAX;
+        alpha[j] = cmk((T)1, (T)0);
+#pragma unroll
+        for (int v = 0; v < C / VW; ++v) {
+            const int col = qc * C + v * VW;
+            VT a = {}, c = {};
+            if (i < b && col < w) {   // c0 + NB <= ld: the vector stays in the row
+                a = *reinterpret_cast<const VT*>(Mre + (size_t)i * ld + c0 + col);
+                c = *reinterpret_cast<const VT*>(Mim + (size_t)i * ld + c0 + col);
+            }
+#pragma unroll
+            for (int e = 0; e < VW; ++e) {
+                const bool ok = i < b && col + e < w;
+                vr[j][v * VW + e] = ok ? reinterpret_cast<const T*>(&a)[e] : (T)0;
+                vi[j][v * VW + e] = ok ? reinterpret_cast<const T*>(&c)[e] : (T)0;
+            }
+        }
+    }
+    // every CTA of the cluster runs before its shared memory is written remotely
+    cluster_barrier<CL>();
+#pragma unroll 1
+    for (int g = 0; g * C < w; ++g) {
+#pragma unroll
+        for (int sp = 0; sp < C; ++sp) {
+            const int jj = g * C + sp;
+            if (jj < w) {   // uniform
+                const int r0 = c0 + jj;
+                const int par = jj & 1;
+                unsigned key = 0;
+                if (qc == g) {
+#pragma unroll
+                    for (int j = 0; j < R; ++j)
+                        if (lrow[j] >= r0 && lrow[j] < b)
+                            key = max(key, pivot_key((float)(fabs(vr[j][sp]) + fabs(vi[j][sp])), row0 + j));
+                }
+                const unsigned wkey = __reduce_max_sync(0xffffffffu, key);
+                if (wkey != 0u) {
+                    const int wphys = pivot_key_row(wkey) - rbase;
+                    const int wq = (wphys / R) & 7, jsel = wphys & (R - 1);
+                    if ((lane >> 2) == wq) {
+                        T* crow = cand_row[par][warp];
+#pragma unroll
+                        for (int j = 0; j < R; ++j) {
+                            if (j == jsel) {
+#pragma unroll
+                                for (int v = 0; v < C / VW; ++v) {
+                                    VT a, c;
+#pragma unroll
+                                    for (int e = 0; e < VW; ++e) {
+                                        reinterpret_cast<T*>(&a)[e] = vr[j][v * VW + e];
+                                        reinterpret_cast<T*>(&c)[e] = vi[j][v * VW + e];
+                                    }
+                                    reinterpret_cast<VT*>(crow + qc * C)[v] = a;
+                                    reinterpret_cast<VT*>(crow + NB + qc * C)[v] = c;
+                                }
+                                if (qc == g) {
+                                    cand_inv[par][warp] = cinv_pow2(cmk(vr[j][sp], vi[j][sp]));
+                                    cand_lrow[par][warp] = lrow[j];
+                                }
+                            }
+                        }
+                    }
+                }
+                // the warp's key into the key table of every CTA (lane d writes CTA d's)
+                if (lane < CL) *cluster_peer(&cand_key[par][cr * NW + warp], (unsigned)lane) = wkey;
+                cluster_barrier<CL>();
+                unsigned gkey = 0u;
+#pragma unroll
+                for (int q = 0; q < NK / 4; ++q) {
+                    const uint4 kv = reinterpret_cast<const uint4*>(cand_key[par])[q];
+                    gkey = max(gkey, max(max(kv.x, kv.y), max(kv.z, kv.w)));
+                }
+                const int wrow = pivot_key_row(gkey);
+                // CTA holding the pivot row and its warp (wrow < b whenever a key is set: the
+                // holder of logical row r0 always is a candidate; the clamps only bound the ranks)
+                const unsigned wc = (unsigned)min(wrow / RPC, CL - 1);
+                const int ww = min((wrow - (int)wc * RPC) / (8 * R), NW - 1);
+                const T* pr = cluster_peer(cand_row[par][ww], wc);
+                const int pl = *cluster_peer(&cand_lrow[par][ww], wc);
+                const cplx<T> p = cmk(pr[jj], pr[NB + jj]);
+                const bool bad = !(fabs(p.re) + fabs(p.im) > (T)0) || !isfinite(p.re) || !isfinite(p.im);
+                if (bad && t == 0 && cr == 0) dev_error(err, FDFD_DEVERR_SINGULAR);
+                const cplx<T> inv = bad ? cmk((T)0, (T)0) : *cluster_peer(&cand_inv[par][ww], wc);
+                cplx<T> f[R];
+                bool isp[R];
+#pragma unroll
+                for (int j = 0; j < R; ++j) {
+                    const T cr_ = __shfl_sync(0xffffffffu, vr[j][sp], qbase + g);
+                    const T ci_ = __shfl_sync(0xffffffffu, vi[j][sp], qbase + g);
+                    isp[j] = lrow[j] == pl;
+                    const cplx<T> fi = cmul(cmk(cr_, ci_), inv);
+                    f[j] = isp[j] ? cmk((T)0, (T)0) : fi;
+                }
+                T xr[C], xi[C];
+#pragma unroll
+                for (int v = 0; v < C / VW; ++v) {
+                    const VT a = reinterpret_cast<const VT*>(pr + qc * C)[v];
+                    const VT c = reinterpret_cast<const VT*>(pr + NB + qc * C)[v];
+#pragma unroll
+                    for (int e = 0; e < VW; ++e) {
+                        xr[v * VW + e] = reinterpret_cast<const T*>(&a)[e];
+                        xi[v * VW + e] = reinterpret_cast<const T*>(&c)[e];
+                    }
+                }
+                if constexpr (sizeof(T) == 4 && C % 2 == 0) {
+#pragma unroll
+                    for (int j = 0; j < R; ++j) {
+                        const float2 fim = make_float2(f[j].im, f[j].im), nfr = make_float2(-f[j].re, -f[j].re);
+                        const float2 nfi = make_float2(-f[j].im, -f[j].im);
+#pragma unroll
+                        for (int k = 0; k < C; k += 2) {
+                            const float2 x_r = make_float2(xr[k], xr[k + 1]), x_i = make_float2(xi[k], xi[k + 1]);
+                            float2 a = make_float2(vr[j][k], vr[j][k + 1]), c = make_float2(vi[j][k], vi[j][k + 1]);
+                            a = __ffma2_rn(nfr, x_r, __ffma2_rn(fim, x_i, a));
+                            c = __ffma2_rn(nfr, x_i, __ffma2_rn(nfi, x_r, c));
+                            vr[j][k] = a.x; vr[j][k + 1] = a.y;
+                            vi[j][k] = c.x; vi[j][k + 1] = c.y;
+                        }
+                    }
+                } else {
+#pragma unroll
+                    for (int j = 0; j < R; ++j)
+#pragma unroll
+                        for (int k = 0; k < C; ++k) {
+                            vr[j][k] = fma(-f[j].re, xr[k], fma(f[j].im, xi[k], vr[j][k]));
+                            vi[j][k] = fma(-f[j].re, xi[k], fma(-f[j].im, xr[k], vi[j][k]));
+                        }
+                }
+#pragma unroll
+                for (int j = 0; j < R; ++j) {
+                    if (qc == g) {
+                        vr[j][sp] = isp[j] ? (T)1 : -f[j].re;
+                        vi[j][sp] = isp[j] ? (T)0 : -f[j].im;
+                    }
+                    if (isp[j]) alpha[j] = inv;
+                    lrow[j] = (lrow[j] == r0) ? pl : (isp[j] ? r0 : lrow[j]);
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < R; ++j)
+#pragma unroll
+        for (int k = 0; k < C; ++k) {
+            const cplx<T> x = cmul(alpha[j], cmk(vr[j][k], vi[j][k]));
+            vr[j][k] = x.re;
+            vi[j][k] = x.im;
+        }
+    // the composed row exchanges into every CTA's table (row r of the exchanged
+    // matrix is row rsm[r] of M); the barrier also ends the last step's remote reads
+    for (int d = qc; d < CL; d += 4) {   // the quad's lanes share the stores to the CL tables
+#pragma unroll
+        for (int j = 0; j < R; ++j)
+            if (lrow[j] < b) *cluster_peer(&rsm[lrow[j]], (unsigned)d) = row0 + j;
+    }
+    cluster_barrier<CL>();
+    int* rs = rowsrc + (size_t)job * b;
+    int* pp = perm + (size_t)job * b;
+    constexpr int PPT = (RPC + NT - 1) / NT;         // bookkeeping rows per thread (this CTA's slice)
+    const int iend = min(b, rbase + RPC);
+    int rsv[PPT], pv[PPT];
+#pragma unroll
+    for (int u = 0; u < PPT; ++u) {
+        const int i = rbase + t + u * NT;
+        rsv[u] = i < iend ? rsm[i] : 0;
+        pv[u] = i < iend ? pp[rsv[u]] : 0;
+    }
+    {
+        T* gp = GP.slot(job);
+        const long long pe = GP.plane_elems();
+#pragma unroll
+        for (int j = 0; j < R; ++j) {
+            if (lrow[j] >= b) continue;
+            const long long o = (long long)lrow[j] * GP.ld;
+#pragma unroll
+            for (int v = 0; v < C / VW; ++v) {
+                VT a, c;
+#pragma unroll
+                for (int e = 0; e < VW; ++e) {
+                    reinterpret_cast<T*>(&a)[e] = vr[j][v * VW + e];
+                    reinterpret_cast<T*>(&c)[e] = vi[j][v * VW + e];
+                }
+                const int col = qc * C + v * VW;
+                *reinterpret_cast<VT*>(gp + o + col) = a;
+                *reinterpret_cast<VT*>(gp + pe + o + col) = c;
+                if (GP.planes == 4) {   // pre-split tensor-core operand: TF32 residual planes
+                    VT al, cl;
+#pragma unroll
+                    for (int e = 0; e < VW; ++e) {
+                        reinterpret_cast<T*>(&al)[e] = (T)tf32_lo((float)reinterpret_cast<const T*>(&a)[e]);
+                        reinterpret_cast<T*>(&cl)[e] = (T)tf32_lo((float)reinterpret_cast<const T*>(&c)[e]);
+                    }
+                    *reinterpret_cast<VT*>(gp + 2 * pe + o + col) = al;
+                    *reinterpret_cast<VT*>(gp + 3 * pe + o + col) = cl;
+                }
+            }
+        }
+    }
+    cluster_barrier<CL>();   // every old perm entry is read, cluster-wide, before any is overwritten
+#pragma unroll
+    for (int u = 0; u < PPT; ++u) {
+        const int i = rbase + t + u * NT;
+        if (i < iend) {
+            pp[i] = pv[u];
+            rs[i] = rsv[u];
+        }
+    }
+}
+
 // Dst[r][perm[j]] = Src[r][j] per row (through shared memory, so Src may be Dst).
 // grid: (ceil(b/8), njobs), block 256
 template <typename T>
@@ -1321,11 +1935,57 @@ static int gj_panel_launch(cudaStream_t s, int njobs, Pool<T> M, const int* slot
     return (int)cudaGetLastError();
 }
 
+// cluster form with CL CTAs per matrix, R = 4 rows per lane quad: NT = bmax / CL
+// threads for matrices of up to bmax rows
+template <typename T, int NB, int R>
+static int gj_panel_row_launch(cudaStream_t s, int njobs, Pool<T> M, const int* slots, Pool<T> GP, int* perm,
+                               int* rowsrc, int c0, unsigned* err, uint64_t wait_ns) {
+    const int nt = ceil_div(M.rows, 32 * R) * 32;
+    if (nt > 512) return (int)cudaErrorInvalidValue;
+    static const cudaError_t attr = cudaFuncSetAttribute(gj_panel_row_kernel<T, NB, R>,
+                                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                         (int)gj_panel_row_smem<T, NB>(512 * R));
+    if (attr != cudaSuccess) return (int)attr;
+    gj_panel_row_kernel<T, NB, R><<<njobs, nt, gj_panel_row_smem<T, NB>(nt * R), s>>>(M, slots, GP, perm, rowsrc,
+                                                                                     c0, err, wait_ns);
+    return (int)cudaGetLastError();
+}
+
+template <typename T, int NB, int CL, int BMAX>
+static int gj_panel_cl_launch(cudaStream_t s, int njobs, Pool<T> M, const int* slots, Pool<T> GP, int* perm,
+                              int* rowsrc, int c0, unsigned* err) {
+    constexpr int NT = BMAX / CL;
+    gj_panel_cl_kernel<T, NB, 4, NT, CL><<<njobs * CL, NT, 0, s>>>(M, slots, GP, perm, rowsrc, c0, err);
+    return (int)cudaGetLastError();
+}
+
 template <typename T>
 int launch_gj_panel(cudaStream_t s, int nb, int njobs, Pool<T> M, const int* slots, Pool<T> GP, int* perm,
-                    int* rowsrc, int c0, unsigned* err, GjFuse fz) {
+                    int* rowsrc, int c0, unsigned* err, GjFuse fz, int cl, int form, uint64_t wait_ns) {
     const bool two = M.rows > 512;
     if (M.rows > 1024) return (int)cudaErrorInvalidValue;
+    if (form == 1 && cl <= 1 && !fz.fused) {
+        // row form: panel widths as in the other forms, one row per thread up to 512 rows
+        constexpr int NBS = sizeof(T) == 4 ? 32 : 16, NBT = NBS / 2;
+        if (!two && nb == NBS) return gj_panel_row_launch<T, NBS, 1>(s, njobs, M, slots, GP, perm, rowsrc, c0, err, wait_ns);
+        if (two && nb == NBT) return gj_panel_row_launch<T, NBT, 2>(s, njobs, M, slots, GP, perm, rowsrc, c0, err, wait_ns);
+        return (int)cudaErrorInvalidValue;
+    }
+    if (cl > 1 && !fz.fused) {
+        // panel widths as in the single-CTA forms: 32 / 16 (FP32), 16 / 8 (FP64)
+        constexpr int NBS = sizeof(T) == 4 ? 32 : 16, NBT = NBS / 2;
+        if (!two && nb == NBS) {
+            if (cl == 2) return gj_panel_cl_launch<T, NBS, 2, 512>(s, njobs, M, slots, GP, perm, rowsrc, c0, err);
+            if (cl == 4) return gj_panel_cl_launch<T, NBS, 4, 512>(s, njobs, M, slots, GP, perm, rowsrc, c0, err);
+            if (cl == 8) return gj_panel_cl_launch<T, NBS, 8, 512>(s, njobs, M, slots, GP, perm, rowsrc, c0, err);
+        }
+        if (two && nb == NBT) {
+            if (cl == 2) return gj_panel_cl_launch<T, NBT, 2, 1024>(s, njobs, M, slots, GP, perm, rowsrc, c0, err);
+            if (cl == 4) return gj_panel_cl_launch<T, NBT, 4, 1024>(s, njobs, M, slots, GP, perm, rowsrc, c0, err);
+            if (cl == 8) return gj_panel_cl_launch<T, NBT, 8, 1024>(s, njobs, M, slots, GP, perm, rowsrc, c0, err);
+        }
+        return (int)cudaErrorInvalidValue;
+    }
     // lane-quad form: one barrier per column step; four rows per quad up to b = 512,
     // eight (with the half-width panel) up to 1024 in FP32
     constexpr int NB1 = sizeof(T) == 4 ? 32 : 16;
@@ -1519,7 +2179,7 @@ void launch_mcopy(cudaStream_t s, int njobs, Pool<T> S, Pool<T> Dp, const int3* 
     template void launch_level1_combine<T>(cudaStream_t, int, NodeMap, const cplx<double>*, double, Pool<T>,  \
                                            Pool<T>, const L1Job*);                                           \
     template int launch_gj_panel<T>(cudaStream_t, int, int, Pool<T>, const int*, Pool<T>, int*, int*, int,    \
-                                    unsigned*, GjFuse);                                                      \
+                                    unsigned*, GjFuse, int, int, uint64_t);                                  \
     template int launch_gj_rt<T>(cudaStream_t, int, int, Pool<T>, const int*, Pool<T>, const int*, int, int); \
     template void launch_gj_unpermute<T>(cudaStream_t, int, Pool<T>, const int*, Pool<T>, const int*,        \
                                          const int*);                                                       \

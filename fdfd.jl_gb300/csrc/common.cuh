@@ -95,5 +95,48 @@ __device__ __forceinline__ void dev_error(unsigned* err, unsigned bits) {
     if (err) atomicOr(err, bits);
 }
 
+// ---- mbarriers (shared memory) ---------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// bounded wait: false once limit_ns of %globaltimer have passed.  The tensor-core
+// GEMM's pipeline waits take the launch's limit (GemmArgs::wait_ns, settable per
+// handle); the waits that drain a CTA's own copies and MMAs in flight before it
+// frees TMEM and exits always take FDFD_WAIT_LIMIT_NS, so a short pipeline limit
+// never lets a CTA leave with asynchronous work outstanding.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, uint64_t limit_ns) {
+    if (mbar_try(bar, parity)) return true;
+    uint64_t t0 = globaltimer_ns();
+    while (true) {
+        if (mbar_try(bar, parity)) return true;
+        if (globaltimer_ns() - t0 > limit_ns) return false;
+        __nanosleep(64);
+    }
+}
+// the same bound without the back-off, for waits expected to end within a few
+// hundred cycles
+__device__ __forceinline__ bool mbar_wait_spin(uint32_t bar, uint32_t parity, uint64_t limit_ns) {
+    if (mbar_try(bar, parity)) return true;
+    const uint64_t t0 = globaltimer_ns();
+    while (!mbar_try(bar, parity))
+        if (globaltimer_ns() - t0 > limit_ns) return false;
+    return true;
+}
+
 // ---- misc ------------------------------------------------------------------
 static inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }

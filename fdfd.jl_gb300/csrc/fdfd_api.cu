@@ -207,6 +207,11 @@ struct fdfd_handle {
     bool use_tc = true;
     bool level1_gj = false;     // invert first-step blocks by Gauss-Jordan instead of the O(b²) kernel
     bool tri_sweep = true;      // first-step sweep products through the tridiagonal factors, not the dense inverses
+    int gj_form = 0;               // one-CTA Gauss-Jordan panel: 0 lane-quad form, 1 pipelined row form
+                                   // (FDFD_GJ_FORM)
+    int gj_cl = 1;                 // CTAs per matrix of the Gauss-Jordan panel (1: one CTA per matrix, the
+                                   // default; 2/4/8: always that cluster; -1: by the level's matrix count;
+                                   // FDFD_GJ_CL)
     int gj_fused_k = 0;            // FP32 tensor-core Gauss-Jordan: columns of the panels that share one
                                    // update (0: one update per panel, the default; FDFD_GJ_FUSED_K)
     int gj_fused_min = 1;          // ... for batches of at least this many matrices
@@ -912,6 +917,18 @@ int gemm(fdfd_handle* h, int pa, int pb, int pc, const int* a_slot, const int* b
 // ---------------------------------------------------------------------------
 int gj_invert_fused(fdfd_handle* h, const int* d_slots, const int* d_iota, int njobs);
 
+// block-wait limit of the kernels with bounded waits (the handle's, else 2 s)
+static uint64_t wait_limit(const fdfd_handle* h) { return h->wait_ns ? h->wait_ns : FDFD_WAIT_LIMIT_NS; }
+
+// CTAs per matrix of the Gauss-Jordan panel: a level with few matrices spreads each
+// panel over a cluster of CTAs, as many as keep every cluster resident at once
+static int gj_cluster(const fdfd_handle* h, int njobs) {
+    if (h->gj_cl == 1 || h->gj_cl == 2 || h->gj_cl == 4 || h->gj_cl == 8) return h->gj_cl > 1 ? h->gj_cl : 0;
+    for (int cl : {8, 4, 2})
+        if ((long long)njobs * cl <= h->num_sms) return cl;
+    return 0;
+}
+
 template <typename T> int gj_invert(fdfd_handle* h, const int* d_slots, const int* d_iota, int njobs) {
     if (njobs == 0) return FDFD_OK;
     FactorStore<T>& F = store<T>(h);
@@ -949,7 +966,7 @@ template <typename T> int gj_invert(fdfd_handle* h, const int* d_slots, const in
         const int* pslots = F.gj_slots + par * h->max_ne;   // GP/RP slots of this parity
         int ev = prof_begin(h);
         int e = launch_gj_panel<T>(h->stream, nb, njobs, pool_of(F, cur), cur_slots, GPp, F.perm, rs, c0, h->derr,
-                                   GjFuse{});
+                                   GjFuse{}, gj_cluster(h, njobs), h->gj_form, wait_limit(h));
         h->launches++;
         if (e) return set_err(h, FDFD_ECUDA, "gj_panel launch failed: %s", cudaGetErrorString((cudaError_t)e));
         // Rᵀ reads the pivot rows in full: the previous panel's wide update, which ran
@@ -1041,7 +1058,8 @@ int gj_invert_fused(fdfd_handle* h, const int* d_slots, const int* d_iota, int n
             // super-panel's input for the first, the narrow product's output after that
             int ev = prof_begin(h);
             int e = launch_gj_panel<float>(h->stream, nb, njobs, pool_of(F, si == 0 ? cur : alt),
-                                           si == 0 ? cur_slots : alt_slots, GPq, F.perm, tot, c0, h->derr, fz);
+                                           si == 0 ? cur_slots : alt_slots, GPq, F.perm, tot, c0, h->derr, fz, 0, 0,
+                                           wait_limit(h));
             h->launches++;
             if (e) return set_err(h, FDFD_ECUDA, "gj_panel launch failed: %s", cudaGetErrorString((cudaError_t)e));
             if (si == 0) {
@@ -1789,6 +1807,8 @@ int fdfd_create(fdfd_handle** out, int Nx, int Ny, int Npx, int Npy, double dx, 
     const char* env2 = getenv("FDFD_DENSE_L1_SWEEP");
     if (env2 && env2[0] == '1') h->tri_sweep = false;
     if (const char* e = getenv("FDFD_GJ_FUSED_K")) h->gj_fused_k = std::max(0, atoi(e));
+    if (const char* e = getenv("FDFD_GJ_CL")) h->gj_cl = atoi(e);
+    if (const char* e = getenv("FDFD_GJ_FORM")) h->gj_form = atoi(e) == 1 ? 1 : 0;
     if (const char* e = getenv("FDFD_GJ_FUSED_MIN")) h->gj_fused_min = std::max(1, atoi(e));
     NodeMap& m = h->map;
     m.Nx = Nx; m.Ny = Ny;

@@ -56,38 +56,8 @@ template <int BN, int TWO = 0> struct TcTile {
     static_assert(MIN_BLOCKS * (SMEM_BYTES + 1024) <= 227 * 1024, "shared memory per SM");
 };
 
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-    return (uint32_t)__cvta_generic_to_shared(p);
-}
-
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
-}
 __device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(ok)
-        : "r"(bar), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-// bounded wait: false once limit_ns of %globaltimer have passed.  The pipeline
-// waits take the launch's limit (GemmArgs::wait_ns, settable per handle); the
-// waits that drain a CTA's own copies and MMAs in flight before it frees TMEM
-// and exits always take FDFD_WAIT_LIMIT_NS, so a short pipeline limit never
-// lets a CTA leave with asynchronous work outstanding.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, uint64_t limit_ns) {
-    if (mbar_try(bar, parity)) return true;
-    uint64_t t0 = globaltimer_ns();
-    while (true) {
-        if (mbar_try(bar, parity)) return true;
-        if (globaltimer_ns() - t0 > limit_ns) return false;
-        __nanosleep(64);
-    }
 }
 
 __device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map, int c0, int c1, int c2,

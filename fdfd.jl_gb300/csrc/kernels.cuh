@@ -109,9 +109,13 @@ struct GjFuse {
 // (returns a cudaError_t value).  Writes the panel transformation to GP,
 // updates perm and writes rowsrc[job][r], the row of M that lands at row r
 // after this panel's interchanges (fused: of the super-panel's input matrix).
+// cl = 2, 4 or 8 splits each matrix's panel over a cluster of cl CTAs (not with
+// fused super-panels), 0 or 1 runs one CTA per matrix: in the lane-quad form
+// (form 0) or the pipelined row form (form 1, not with fused super-panels; its
+// block waits end after wait_ns with FDFD_DEVERR_TIMEOUT).
 template <typename T>
 int launch_gj_panel(cudaStream_t s, int nb, int njobs, Pool<T> M, const int* slots, Pool<T> GP, int* perm,
-                    int* rowsrc, int c0, unsigned* err, GjFuse fz);
+                    int* rowsrc, int c0, unsigned* err, GjFuse fz, int cl, int form, uint64_t wait_ns);
 // The panel's transposed pivot rows (identity on the panel columns) into RP
 // columns [0, rcw) (zero beyond the panel; rcw <= 0: all of RP.cols), read
 // from M through rowsrc; M must hold the rows after the previous update.
