@@ -55,19 +55,38 @@ __global__ void build_tridiag_kernel(NodeMap m, const cplx<double>* st, double s
 // Transposed stores are staged in shared memory and written as 16-element
 // transposed row segments, two per warp instruction.  The short tile keeps the
 // staging at 34 KB, so five CTAs share an SM (the kernel waits on memory:
-// resident warps are what keeps HBM busy).
+// resident warps are what keeps HBM busy).  Shared-memory layouts keep a warp's
+// accesses on distinct banks: the per-column factors are stored lane-major
+// (column 4·lane + e at e·32 + lane), and staged column c starts at c·17 + c/32
+// (the skew spreads the 4·lane column stride over all 32 banks).
 // grid: (ceil(b/128), ceil(b/L1_TR), njobs), dynamic smem level1_combine_smem<T>()
 // ---------------------------------------------------------------------------
 template <typename T> struct Vec16;
 template <> struct Vec16<float> { typedef float4 type; };
 template <> struct Vec16<double> { typedef double2 type; };
 
-constexpr int L1_TR = 16;   // tile rows
+constexpr int L1_TR = 16;                       // tile rows
+constexpr int L1_PS = 128 * (L1_TR + 1) + 4;    // staging plane stride (elements), skew included
 template <typename T>
-constexpr size_t level1_combine_smem() { return (size_t)2 * 2 * 128 * (L1_TR + 1) * sizeof(T) + 4 * 128 * 2 * sizeof(T); }
+constexpr size_t level1_combine_smem() { return (size_t)2 * 2 * L1_PS * sizeof(T) + 4 * 128 * 2 * sizeof(T); }
+
+// The five stencil planes of every node in the factor precision, scaled, contiguous
+// in the in-line index: tab[(node·5 + plane)·b + i] = (T)(st · scale), converted
+// once per factorization (FP64 issue is scarce, and a transposed node map strides
+// st by Nx).  grid: (ceil(b/256), n), block 256
+template <typename T>
+__global__ void stencil_table_kernel(NodeMap m, const cplx<double>* st, double scale, cplx<T>* tab) {
+    const int node = blockIdx.y, i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m.b) return;
+#pragma unroll
+    for (int p = 0; p < 5; ++p) {
+        const cplx<double> v = st_at<T>(st, m, p, node, i);
+        tab[((size_t)node * 5 + p) * m.b + i] = cmk((T)(v.re * scale), (T)(v.im * scale));
+    }
+}
 
 template <typename T>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 5 : 1) level1_combine_kernel(NodeMap m, const cplx<double>* st, double scale,
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 5 : 1) level1_combine_kernel(NodeMap m, const cplx<T>* tab,
                                                              Pool<T> D, Pool<T> C, const L1Job* jobs) {
     constexpr int CPL = 4;                    // columns per lane
     constexpr int VW = 16 / sizeof(T);
@@ -75,8 +94,9 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 5 : 1) level1_combine_ke
     typedef typename Vec16<T>::type VT;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     constexpr int SR = L1_TR + 1;            // staging row stride
-    T* tU = reinterpret_cast<T*>(smem_raw);  // [plane][tile column][tile row]
-    T* tL = tU + 2 * 128 * SR;
+    T* tU = reinterpret_cast<T*>(smem_raw);  // [plane][tile column][tile row], plane stride L1_PS
+    T* tL = tU + 2 * L1_PS;
+    auto sidx = [](int c, int r) { return c * SR + (c >> 5) + r; };   // staged element (tile column c, row r)
     const L1Job J = jobs[blockIdx.z];
     const int b = m.b;
     const int c0 = blockIdx.x * 128, r0 = blockIdx.y * L1_TR;
@@ -91,20 +111,21 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 5 : 1) level1_combine_ke
     T* __restrict__ Us = C.slot(J.u_slot);
     T* __restrict__ Ls = C.slot(J.l_slot);
     const long long cpe = C.plane_elems();
-    // stencil values are FP64; the arithmetic runs in the factor precision T
-    auto tv = [&](cplx<double> v) { return cmk((T)(v.re * scale), (T)(v.im * scale)); };
+    // scaled stencil values in the factor precision (stencil_table_kernel)
+    auto tv = [&](int plane, int node, int i) { return tab[((size_t)node * 5 + plane) * b + i]; };
     const cplx<T> z = cmk((T)0, (T)0);
     // per-column coupling factors of the neighbours, shared by the tile's rows:
-    // [0] l_next, [1] u_next, [2] u_prev, [3] l_prev for the 128 tile columns
-    cplx<T>* fac = reinterpret_cast<cplx<T>*>(tL + 2 * 128 * SR);
+    // [0] l_next, [1] u_next, [2] u_prev, [3] l_prev for the 128 tile columns,
+    // tile column 4·lane + e at e·32 + lane
+    cplx<T>* fac = reinterpret_cast<cplx<T>*>(tL + 2 * L1_PS);
     for (int t = threadIdx.x; t < 4 * 128; t += 256) {
-        const int k = t / 128, c = c0 + t % 128;
+        const int k = t / 128, cl = t % 128, c = c0 + cl;
         cplx<T> v = z;
         if (c < b) {
-            if (k < 2 && J.next_elim) v = tv(st_at<T>(st, m, k == 0 ? m.p_cprev() : m.p_cnext(), J.next, c));
-            if (k >= 2 && J.prev_elim) v = tv(st_at<T>(st, m, k == 2 ? m.p_cnext() : m.p_cprev(), J.prev, c));
+            if (k < 2 && J.next_elim) v = tv(k == 0 ? m.p_cprev() : m.p_cnext(), J.next, c);
+            if (k >= 2 && J.prev_elim) v = tv(k == 2 ? m.p_cnext() : m.p_cprev(), J.prev, c);
         }
-        fac[t] = v;
+        fac[k * 128 + (cl % CPL) * 32 + cl / CPL] = v;
     }
     __syncthreads();
     const bool full = cb0 + CPL <= b;        // all four columns inside the matrix
@@ -116,13 +137,13 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 5 : 1) level1_combine_ke
             // nothing to compute; the transposed staging of this element stays unused
             continue;
         }
-        const cplx<T> ls = tv(st_at<T>(st, m, m.p_cprev(), J.s, r));
-        const cplx<T> us = tv(st_at<T>(st, m, m.p_cnext(), J.s, r));
+        const cplx<T> ls = tv(m.p_cprev(), J.s, r);
+        const cplx<T> us = tv(m.p_cnext(), J.s, r);
         // the cyclic tridiagonal row of D_s: three entries, converted once per row
         // (b >= 3, so no two of them share a column)
-        const cplx<T> t_d = tv(st_at<T>(st, m, 0, J.s, r));
-        const cplx<T> t_l = tv(st_at<T>(st, m, m.p_inprev(), J.s, r));
-        const cplx<T> t_u = tv(st_at<T>(st, m, m.p_innext(), J.s, r));
+        const cplx<T> t_d = tv(0, J.s, r);
+        const cplx<T> t_l = tv(m.p_inprev(), J.s, r);
+        const cplx<T> t_u = tv(m.p_innext(), J.s, r);
         const int c_l = r == 0 ? b - 1 : r - 1, c_u = r == b - 1 ? 0 : r + 1;
         T gpr[CPL], gpi[CPL], gnr[CPL], gni[CPL];
         const long long o = (long long)r * D.ld + cb0;   // cb0 < b <= ld, cb0 % 4 == 0: vectors stay in the row
@@ -153,15 +174,15 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 5 : 1) level1_combine_ke
             cplx<T> uv = z, lv = z;
             if (J.prev_elim) {
                 const cplx<T> lg = cmul(ls, cmk(gpr[e], gpi[e]));
-                dv = csub(dv, cmul(lg, fac[2 * 128 + cl0 + e]));
-                lv = cneg(cmul(lg, fac[3 * 128 + cl0 + e]));
+                dv = csub(dv, cmul(lg, fac[2 * 128 + e * 32 + lane]));
+                lv = cneg(cmul(lg, fac[3 * 128 + e * 32 + lane]));
             } else if (c == r) {
                 lv = ls;
             }
             if (J.next_elim) {
                 const cplx<T> ug = cmul(us, cmk(gnr[e], gni[e]));
-                dv = csub(dv, cmul(ug, fac[cl0 + e]));
-                uv = cneg(cmul(ug, fac[128 + cl0 + e]));
+                dv = csub(dv, cmul(ug, fac[e * 32 + lane]));
+                uv = cneg(cmul(ug, fac[128 + e * 32 + lane]));
             } else if (c == r) {
                 uv = us;
             }
@@ -196,16 +217,16 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 5 : 1) level1_combine_ke
         else {
 #pragma unroll
             for (int e = 0; e < CPL; ++e) {
-                tU[(cl0 + e) * SR + rl] = ur[e];
-                tU[128 * SR + (cl0 + e) * SR + rl] = ui[e];
+                tU[sidx(cl0 + e, rl)] = ur[e];
+                tU[L1_PS + sidx(cl0 + e, rl)] = ui[e];
             }
         }
         if (!J.l_trans) put_row(Ls, cpe, lr, li);
         else {
 #pragma unroll
             for (int e = 0; e < CPL; ++e) {
-                tL[(cl0 + e) * SR + rl] = lr[e];
-                tL[128 * SR + (cl0 + e) * SR + rl] = li[e];
+                tL[sidx(cl0 + e, rl)] = lr[e];
+                tL[L1_PS + sidx(cl0 + e, rl)] = li[e];
             }
         }
     }
@@ -219,8 +240,8 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 5 : 1) level1_combine_ke
         for (int cl = 2 * warp + lane / L1_TR; cl < 128; cl += 16) {
             const int cc = c0 + cl;
             if (cc >= b || rr >= b) continue;
-            if (J.u_trans) store_elem<T>(C, Us, cc, rr, cmk(tU[cl * SR + tr], tU[128 * SR + cl * SR + tr]), 0);
-            if (J.l_trans) store_elem<T>(C, Ls, cc, rr, cmk(tL[cl * SR + tr], tL[128 * SR + cl * SR + tr]), 0);
+            if (J.u_trans) store_elem<T>(C, Us, cc, rr, cmk(tU[sidx(cl, tr)], tU[L1_PS + sidx(cl, tr)]), 0);
+            if (J.l_trans) store_elem<T>(C, Ls, cc, rr, cmk(tL[sidx(cl, tr)], tL[L1_PS + sidx(cl, tr)]), 0);
         }
     }
 }
@@ -1913,13 +1934,14 @@ void launch_build_tridiag(cudaStream_t s, int njobs, NodeMap m, const cplx<doubl
 }
 template <typename T>
 void launch_level1_combine(cudaStream_t s, int njobs, NodeMap m, const cplx<double>* st, double scale, Pool<T> D,
-                           Pool<T> C, const L1Job* jobs) {
+                           Pool<T> C, const L1Job* jobs, cplx<T>* tab) {
+    stencil_table_kernel<T><<<dim3(ceil_div(m.b, 256), m.n), 256, 0, s>>>(m, st, scale, tab);
     const size_t smem = level1_combine_smem<T>();
     static const cudaError_t attr =
         cudaFuncSetAttribute(level1_combine_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     (void)attr;
-    level1_combine_kernel<T><<<dim3(ceil_div(m.b, 128), ceil_div(m.b, L1_TR), njobs), 256, smem, s>>>(m, st, scale,
-                                                                                                     D, C, jobs);
+    level1_combine_kernel<T><<<dim3(ceil_div(m.b, 128), ceil_div(m.b, L1_TR), njobs), 256, smem, s>>>(m, tab, D, C,
+                                                                                                     jobs);
 }
 void launch_perm_init(cudaStream_t s, int njobs, int* perm, int b) {
     perm_init_kernel<int><<<dim3(ceil_div(b, 256), njobs), 256, 0, s>>>(perm, b);
@@ -2177,7 +2199,7 @@ void launch_mcopy(cudaStream_t s, int njobs, Pool<T> S, Pool<T> Dp, const int3* 
     template void launch_build_tridiag<T>(cudaStream_t, int, NodeMap, const cplx<double>*, double, Pool<T>,   \
                                           const int*);                                                       \
     template void launch_level1_combine<T>(cudaStream_t, int, NodeMap, const cplx<double>*, double, Pool<T>,  \
-                                           Pool<T>, const L1Job*);                                           \
+                                           Pool<T>, const L1Job*, cplx<T>*);                                 \
     template int launch_gj_panel<T>(cudaStream_t, int, int, Pool<T>, const int*, Pool<T>, int*, int*, int,    \
                                     unsigned*, GjFuse, int, int, uint64_t);                                  \
     template int launch_gj_rt<T>(cudaStream_t, int, int, Pool<T>, const int*, Pool<T>, const int*, int, int); \

@@ -93,6 +93,7 @@ template <typename T> struct FactorStore {
     int* gj_slots = nullptr;    // 0 .. 2*max_ne-1: GP/RP slot lists of both parities
     cplx<T>* trifac = nullptr;  // first-step tridiagonal factors (8*b per node)
     int* tripiv = nullptr;      // and their interchanges (b per node)
+    cplx<T>* sttab = nullptr;   // scaled stencil planes of every node in the factor precision (5*b per node)
     bool tc_ok = false;
     TcMaps tc;       // TMA descriptors (FP32 only)
     bool complete = false;   // every pool above allocated
@@ -207,6 +208,8 @@ struct fdfd_handle {
     bool use_tc = true;
     bool level1_gj = false;     // invert first-step blocks by Gauss-Jordan instead of the O(b²) kernel
     bool tri_sweep = true;      // first-step sweep products through the tridiagonal factors, not the dense inverses
+    bool gj_presplit = true;       // FP32 panel buffers G, Rᵀ stored with their TF32 residual planes
+                                   // (FDFD_GJ_PRESPLIT=0: two planes, split inside the GEMM)
     int gj_form = 0;               // one-CTA Gauss-Jordan panel: 0 lane-quad form, 1 pipelined row form
                                    // (FDFD_GJ_FORM)
     int gj_cl = 1;                 // CTAs per matrix of the Gauss-Jordan panel (1: one CTA per matrix, the
@@ -619,7 +622,7 @@ template <typename T> int alloc_pool(fdfd_handle* h, Pool<T>& P, int rows, int c
 
 template <typename T> void free_store(fdfd_handle* h, FactorStore<T>& F) {
     void* bufs[] = {F.D.base, F.C.base, F.X.base, F.GP.base, F.RP.base, F.Tg.base, F.rv, F.xv, F.wv,
-                    F.perm, F.rowsrc, F.inv, F.gsub, F.gj_slots, F.trifac, F.tripiv};
+                    F.perm, F.rowsrc, F.inv, F.gsub, F.gj_slots, F.trifac, F.tripiv, F.sttab};
     for (void* p : bufs) dev_free(h, p);
     if (F.hC || F.hX) {
         const long long se = F.C.slot_elems();
@@ -661,7 +664,7 @@ template <typename T> void factor_bytes(const fdfd_handle* h, double* resident, 
     const int nC = h->ckpt ? h->orig_nC : h->nCslots, nX = h->ckpt ? h->orig_nX : h->nXslots;
     const double N = (double)h->Nx * h->Ny;
     const double work = sb * gj_max + 2.0 * 2 * h->max_ne * b * 32 * 4 * sizeof(T) + 3.0 * h->max_ne * b * 4 +
-                        (double)n * 9 * b * sizeof(cplx<T>) + 3.0 * n * 2 * ld * sizeof(T) +
+                        (double)n * 14 * b * sizeof(cplx<T>) + 3.0 * n * 2 * ld * sizeof(T) +
                         (2.0 * restart_len(h, 1) + 4) * N * sizeof(cplx<double>);
     *resident = sb * (n + nC + nX) + work;
     *windowed = sb * (n + nA + nB + 2 + nXw + 1) + work;
@@ -782,8 +785,9 @@ template <typename T> int alloc_factor_pools(fdfd_handle* h) {
     RET(alloc_pool<T>(h, F.D, b, b, ld, planes, n));
     RET(alloc_pool<T>(h, F.C, b, b, ld, planes, h->nCslots));
     RET(alloc_pool<T>(h, F.X, b, b, ld, planes, h->nXslots));
-    // the panel buffers are short-K tensor-core operands: stored pre-split (re, im, re_lo, im_lo)
-    const int pplanes = sizeof(T) == 4 ? 4 : 2;
+    // the panel buffers are short-K tensor-core operands: stored pre-split (re, im, re_lo, im_lo),
+    // unless gj_presplit is off (the GEMM then forms the residual planes itself)
+    const int pplanes = (sizeof(T) == 4 && h->gj_presplit) ? 4 : 2;
     // two sets (panel parity) so that a panel can run while the previous panel's update reads the other set
     RET(alloc_pool<T>(h, F.GP, b, pc, pc, pplanes, 2 * h->max_ne));
     RET(alloc_pool<T>(h, F.RP, b, pc, pc, pplanes, 2 * h->max_ne));
@@ -810,6 +814,7 @@ template <typename T> int alloc_factor_pools(fdfd_handle* h) {
         RET(dev_alloc(h, (void**)&F.trifac, n1 * 8 * b * sizeof(cplx<T>)));
         RET(dev_alloc(h, (void**)&F.tripiv, n1 * b * sizeof(int)));
     }
+    if (h->sj.size() > 1) RET(dev_alloc(h, (void**)&F.sttab, (size_t)h->map.n * 5 * b * sizeof(cplx<T>)));
     if (h->ckpt) {
         const size_t se = (size_t)F.C.slot_elems() * sizeof(T);
         const size_t bc = se * (h->orig_nC - 2), bx = se * (h->orig_nX - 1);
@@ -1141,9 +1146,10 @@ template <typename T> int factor_impl(fdfd_handle* h) {
             }
             // bytes: two inverses read (re, im), D written (re, im), both couplings written (all planes)
             int ev1 = prof_begin(h);
-            launch_level1_combine<T>(h->stream, S.nl1, h->map, h->st, h->scale, F.D, F.C, J<L1Job>(h, S.l1));
+            launch_level1_combine<T>(h->stream, S.nl1, h->map, h->st, h->scale, F.D, F.C, J<L1Job>(h, S.l1),
+                                     F.sttab);
             prof_end(h, ev1, FDFD_PROF_LEVEL1, (6.0 + 2.0 * F.C.planes) * sizeof(T) * b * b * S.nl1);
-            h->launches++;
+            h->launches += 2;
             RET(check_launch(h, "level1_combine"));
         } else {
             RET(gj_invert<T>(h, J<int>(h, S.elim), J<int>(h, S.iota), ne));
@@ -1809,6 +1815,7 @@ int fdfd_create(fdfd_handle** out, int Nx, int Ny, int Npx, int Npy, double dx, 
     if (const char* e = getenv("FDFD_GJ_FUSED_K")) h->gj_fused_k = std::max(0, atoi(e));
     if (const char* e = getenv("FDFD_GJ_CL")) h->gj_cl = atoi(e);
     if (const char* e = getenv("FDFD_GJ_FORM")) h->gj_form = atoi(e) == 1 ? 1 : 0;
+    if (const char* e = getenv("FDFD_GJ_PRESPLIT")) h->gj_presplit = atoi(e) != 0;
     if (const char* e = getenv("FDFD_GJ_FUSED_MIN")) h->gj_fused_min = std::max(1, atoi(e));
     NodeMap& m = h->map;
     m.Nx = Nx; m.Ny = Ny;

@@ -83,9 +83,10 @@ struct L1Job {                 // survivor of the first reduction step
 template <typename T>
 void launch_build_tridiag(cudaStream_t s, int njobs, NodeMap m, const cplx<double>* st, double scale, Pool<T> D,
                           const int* nodes);
+// (tab: workspace of 5·b·n cplx<T>, the scaled stencil table of every node, written first)
 template <typename T>
 void launch_level1_combine(cudaStream_t s, int njobs, NodeMap m, const cplx<double>* st, double scale, Pool<T> D,
-                           Pool<T> C, const L1Job* jobs);
+                           Pool<T> C, const L1Job* jobs, cplx<T>* tab);
 void launch_perm_init(cudaStream_t s, int njobs, int* perm, int b);
 // D[node] = (cyclic tridiagonal block of node)⁻¹ in O(b²) (first reduction step);
 // fac: 8*b cplx<T> and piv: b ints of workspace per job
