@@ -33,10 +33,11 @@ __device__ void stage_vectors(const GemvArgs<T>& g, const int mslot[2], const in
     for (int t = 0; t < 2; ++t) {
         if (mslot[t] < 0) continue;
         const T* v = V[t] + ((size_t)vnode[t] * g.rtot + g.r0) * 2 * g.ld;
-        for (int idx = threadIdx.x; idx < R * 2 * bpad; idx += blockDim.x) {
-            const int r = idx / (2 * bpad), rem = idx % (2 * bpad), p = rem / bpad, i = rem % bpad;
-            sv[((size_t)t * R + r) * 2 * bpad + p * bpad + i] =
-                (i < g.b && r < g.nrhs) ? v[((size_t)r * 2 + p) * g.ld + i] : (T)0;
+        for (int rp = 0; rp < 2 * R; ++rp) {   // (right-hand side, plane) = (rp / 2, rp % 2)
+            const T* src = v + (size_t)rp * g.ld;
+            T* dst = sv + ((size_t)t * 2 * R + rp) * bpad;
+            const bool live = rp / 2 < g.nrhs;
+            for (int i = threadIdx.x; i < bpad; i += blockDim.x) dst[i] = (live && i < g.b) ? src[i] : (T)0;
         }
     }
 }
@@ -89,14 +90,30 @@ __global__ void __launch_bounds__(256) gemv_n_kernel(GemvArgs<T> g) {
                     const int c = (c0 + u) * CW + lane * VW;
                     const T* er = reinterpret_cast<const T*>(&mr[u]);
                     const T* ei = reinterpret_cast<const T*>(&mi[u]);
+                    // the 16-byte vector is inside the row, in its padding, or (b not a multiple
+                    // of VW) straddles b: its entries at b and beyond are zeroed, and the input
+                    // vector's padding is zero, so they add nothing
+                    if (c < b) {
+                        if (c + VW > b) {
 #pragma unroll
-                    for (int e = 0; e < VW; ++e) {
-                        if (c + e < b) {      // masks the row padding beyond b
+                            for (int e = 0; e < VW; ++e)
+                                if (c + e >= b) {
+                                    reinterpret_cast<T*>(&mr[u])[e] = 0;
+                                    reinterpret_cast<T*>(&mi[u])[e] = 0;
+                                }
+                        }
 #pragma unroll
-                            for (int r = 0; r < R; ++r) {
-                                const T vr = vt[(r * 2) * bpad + c + e], vi = vt[(r * 2 + 1) * bpad + c + e];
-                                ar[r] = fma(er[e], vr, ar[r]); ar[r] = fma(-ei[e], vi, ar[r]);
-                                ai[r] = fma(er[e], vi, ai[r]); ai[r] = fma(ei[e], vr, ai[r]);
+                        for (int r = 0; r < R; ++r) {
+                            const typename V16<T>::type v_r =
+                                *reinterpret_cast<const typename V16<T>::type*>(vt + (r * 2) * bpad + c);
+                            const typename V16<T>::type v_i =
+                                *reinterpret_cast<const typename V16<T>::type*>(vt + (r * 2 + 1) * bpad + c);
+                            const T* xr = reinterpret_cast<const T*>(&v_r);
+                            const T* xi = reinterpret_cast<const T*>(&v_i);
+#pragma unroll
+                            for (int e = 0; e < VW; ++e) {
+                                ar[r] = fma(er[e], xr[e], ar[r]); ar[r] = fma(-ei[e], xi[e], ar[r]);
+                                ai[r] = fma(er[e], xi[e], ai[r]); ai[r] = fma(ei[e], xr[e], ai[r]);
                             }
                         }
                     }
