@@ -208,6 +208,8 @@ struct fdfd_handle {
     bool use_tc = true;
     bool level1_gj = false;     // invert first-step blocks by Gauss-Jordan instead of the O(b²) kernel
     bool tri_sweep = true;      // first-step sweep products through the tridiagonal factors, not the dense inverses
+    bool gemv_bulk = false;        // untuned N-form sweep products through the bulk-copy pipeline where it
+                                   // fits (FDFD_GEMV_BULK=1), else register loads; the autotuner times both
     bool gj_presplit = true;       // FP32 panel buffers G, Rᵀ stored with their TF32 residual planes
                                    // (FDFD_GJ_PRESPLIT=0: two planes, split inside the GEMM)
     int gj_form = 0;               // one-CTA Gauss-Jordan panel: 0 lane-quad form, 1 pipelined row form
@@ -1207,11 +1209,14 @@ template <typename T> int gemv(fdfd_handle* h, int tr, int p1, int p2, const T* 
         g.b = b; g.ld = h->map.ld; g.nrhs = std::min(rmax, nrhs - r0); g.rtot = nrhs; g.r0 = r0;
         g.alpha = alpha;
         g.nsm = h->num_sms;
+        g.nmat = nblk > njobs ? 2 : 1;
+        g.err = h->derr;
         g.shape = h->force_shape;
         if (!g.shape) {
             auto it = h->tune_gemv.find(std::make_tuple(tr, njobs, g.nrhs));
             if (it != h->tune_gemv.end()) g.shape = it->second;
         }
+        if (!tr && g.shape == 0 && !h->gemv_bulk) g.shape = GEMV_SHAPE_REGISTER_RULE;
         int ev = prof_begin(h);
         int e = launch_gemv<T>(h->stream, tr, njobs, g);
         // algorithmic bytes: every referenced block (re + im planes) read once; per job and
@@ -1816,6 +1821,7 @@ int fdfd_create(fdfd_handle** out, int Nx, int Ny, int Npx, int Npy, double dx, 
     if (const char* e = getenv("FDFD_GJ_CL")) h->gj_cl = atoi(e);
     if (const char* e = getenv("FDFD_GJ_FORM")) h->gj_form = atoi(e) == 1 ? 1 : 0;
     if (const char* e = getenv("FDFD_GJ_PRESPLIT")) h->gj_presplit = atoi(e) != 0;
+    if (const char* e = getenv("FDFD_GEMV_BULK")) h->gemv_bulk = atoi(e) != 0;
     if (const char* e = getenv("FDFD_GJ_FUSED_MIN")) h->gj_fused_min = std::max(1, atoi(e));
     NodeMap& m = h->map;
     m.Nx = Nx; m.Ny = Ny;
@@ -2951,8 +2957,9 @@ template <typename T> int autotune_impl(fdfd_handle* h) {
         int best = 0;
         double tbest = 1e30;
         std::string cand;
-        const int cands[2][3] = {{1, 2, 4}, {8, 16, 32}};
+        const int cands[2][6] = {{1, 2, 4, -2, -4, -8}, {8, 16, 32, 0, 0, 0}};
         for (int c : cands[tr]) {
+            if (c == 0) continue;
             h->force_shape = c;
             double ms = 0;
             const int rc = time_launch(h, [&] { return gemv<T>(h, tr, p1, p2, V1, V2, Y0, Y, jobs, yjobs, njobs,

@@ -207,6 +207,7 @@ void launch_gemm_simt(cudaStream_t s, int njobs, const GemmArgs<T>& g);
 // ---- sweep.cu -------------------------------------------------------------------
 // y[job] = y0[job] + alpha·(op(M1)·v1 + op(M2)·v2) on node-planar vectors,
 // op = identity (N-form storage) or the stored transpose (T-form storage).
+#define GEMV_SHAPE_REGISTER_RULE 100
 template <typename T> struct GemvArgs {
     Pool<T> P1, P2;
     const T* V1; const T* V2;
@@ -219,8 +220,12 @@ template <typename T> struct GemvArgs {
     int rpw, og;        // launch shape, set by launch_gemv: rows per warp (N form),
                         // lanes per output group (T form)
     int nsm;            // streaming multiprocessors of the device (launch shape)
-    int shape;          // launch shape chosen by the caller (autotuner): rpw in {1, 2, 4} (N form)
-                        // or og in {8, 16, 32} (T form); 0: launch_gemv's rule
+    int shape;          // launch shape chosen by the caller (autotuner): rpw in {1, 2, 4} (N form, register
+                        // loads), -2, -4 or -8 (N form, bulk-copy pipeline with that many rows per warp),
+                        // og in {8, 16, 32} (T form); 0: launch_gemv's rule
+    int nmat;           // most factor blocks one job references (1 or 2)
+    // (a positive shape outside {1, 2, 4} selects the N form's register loads with launch_gemv's rule)
+    unsigned* err;      // device error word (a bulk-copy wait that runs out sets FDFD_DEVERR_TIMEOUT)
 };
 // TR = 1: matrices stored transposed.  Returns a cudaError_t value.
 template <typename T>

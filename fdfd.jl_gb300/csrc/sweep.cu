@@ -140,6 +140,162 @@ __global__ void __launch_bounds__(256) gemv_n_kernel(GemvArgs<T> g) {
     }
 }
 
+// N-form product fed by bulk copies: each warp owns rows row_base .. row_base+RW-1
+// and streams them (both planes of every block of the job) into a private ring of
+// shared-memory slots with cp.async.bulk, one mbarrier per slot, so the bytes in
+// flight are bounded by shared memory rather than by registers.  The warp then
+// works like gemv_n_kernel on a row (lanes over 16-byte column vectors, the same
+// per-lane order of the fmas and the same shuffle reduction), so both kernels give
+// identical results.  Slot s is refilled with row k + nslot once the warp has
+// finished row k (a __syncwarp, then a proxy fence orders the generic reads before
+// the asynchronous write).  Every slot wait is bounded (FDFD_WAIT_LIMIT_NS); a wait
+// that runs out sets FDFD_DEVERR_TIMEOUT and the warp waits (bounded) for the copies
+// it has issued before it leaves.
+// grid: (ceil(b/(8*RW)), njobs), block 256, dynamic shared memory
+// gemv_nb_smem<T, R>(b) + 8 * ring_bytes; ring_bytes a multiple of 16 holding at
+// least one slot of two blocks (4 row planes of ceil16(b·sizeof(T)) bytes).
+template <typename T, int R>
+__host__ __device__ constexpr size_t gemv_nb_smem(int b) {
+    return ((size_t)2 * R * 2 * ((b + 32 * (16 / sizeof(T)) - 1) / (32 * (16 / sizeof(T))) * 32 * (16 / sizeof(T))) *
+                sizeof(T) + 127) / 128 * 128;
+}
+
+template <typename T, int R>
+__global__ void __launch_bounds__(256) gemv_nb_kernel(GemvArgs<T> g, int RW, int ring_bytes) {
+    constexpr int VW = 16 / sizeof(T);
+    constexpr int CW = 32 * VW;
+    constexpr int MAXS = 8;
+    typedef typename V16<T>::type VT;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ __align__(8) uint64_t bars[8][MAXS];
+    T* sv = reinterpret_cast<T*>(smem_raw);
+    const int b = g.b;
+    const int nch = (b + CW - 1) / CW;
+    const int bpad = nch * CW;
+    const int4 J = g.jobs[blockIdx.y];
+    const int2 Y = g.yjobs[blockIdx.y];
+    const int mslot[2] = {J.x, J.z}, vnode[2] = {J.y, J.w};
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int rb = (b * (int)sizeof(T) + 15) & ~15;     // bytes copied per row and plane
+    const int nm = (mslot[0] >= 0 ? 1 : 0) + (mslot[1] >= 0 ? 1 : 0);
+    const int slot_bytes = (nm > 0 ? nm : 1) * 2 * rb;
+    const int nslot = min(MAXS, ring_bytes / slot_bytes);   // >= 1 by the launcher's sizing
+    unsigned char* ring = smem_raw + gemv_nb_smem<T, R>(b) + (size_t)warp * ring_bytes;
+    if (lane == 0)
+        for (int q = 0; q < nslot; ++q) mbar_init(smem_u32(&bars[warp][q]), 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    stage_vectors<T>(g, mslot, vnode, sv, R, bpad);
+    __syncthreads();
+    const int row_base = (blockIdx.x * 8 + warp) * RW;
+    const int nrows = max(0, min(RW, b - row_base));
+    // lane 0: the planes of row row_base + k of every block of the job into slot k % nslot
+    auto issue = [&](int k) {
+        const int q = k % nslot, row = row_base + k;
+        const uint32_t bar = smem_u32(&bars[warp][q]);
+        const uint32_t dst = smem_u32(ring + (size_t)q * slot_bytes);
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(nm * 2 * rb)
+                     : "memory");
+        int m = 0;
+        for (int t = 0; t < 2; ++t) {
+            if (mslot[t] < 0) continue;
+            const Pool<T>& P = t ? g.P2 : g.P1;
+            const T* src = P.slot(mslot[t]) + (size_t)row * P.ld;
+#pragma unroll
+            for (int pl = 0; pl < 2; ++pl)
+                asm volatile(
+                    "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                        dst + (uint32_t)((2 * m + pl) * rb)),
+                    "l"(src + pl * P.plane_elems()), "r"(rb), "r"(bar)
+                    : "memory");
+            ++m;
+        }
+    };
+    if (lane == 0 && nm > 0)
+        for (int k = 0; k < min(nslot, nrows); ++k) issue(k);
+    T* y = g.Y + ((size_t)Y.x * g.rtot + g.r0) * 2 * g.ld;
+    const T* y0 = Y.y >= 0 ? g.Y0 + ((size_t)Y.y * g.rtot + g.r0) * 2 * g.ld : nullptr;
+    int k = 0;
+    bool ok = true;
+    for (; k < nrows; ++k) {
+        const int q = k % nslot, row = row_base + k;
+        if (nm > 0) {   // a job without blocks only writes y0 (or zero)
+            const bool okl = mbar_wait(smem_u32(&bars[warp][q]), (uint32_t)((k / nslot) & 1), FDFD_WAIT_LIMIT_NS);
+            if (!__all_sync(0xffffffffu, okl)) {
+                ok = false;
+                break;
+            }
+        }
+        const unsigned char* slot = ring + (size_t)q * slot_bytes;
+        T ar[R], ai[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) { ar[r] = 0; ai[r] = 0; }
+        int m = 0;
+        for (int t = 0; t < 2; ++t) {
+            if (mslot[t] < 0) continue;
+            const T* Mr = reinterpret_cast<const T*>(slot + (size_t)(2 * m) * rb);
+            const T* Mi = reinterpret_cast<const T*>(slot + (size_t)(2 * m + 1) * rb);
+            const T* vt = sv + (size_t)t * R * 2 * bpad;
+            ++m;
+            for (int ch = 0; ch < nch; ++ch) {
+                const int c = ch * CW + lane * VW;
+                if (c >= b) continue;
+                VT mr = *reinterpret_cast<const VT*>(Mr + c), mi = *reinterpret_cast<const VT*>(Mi + c);
+                if (c + VW > b) {   // b not a multiple of VW: entries at b and beyond add nothing
+#pragma unroll
+                    for (int e = 0; e < VW; ++e)
+                        if (c + e >= b) {
+                            reinterpret_cast<T*>(&mr)[e] = 0;
+                            reinterpret_cast<T*>(&mi)[e] = 0;
+                        }
+                }
+                const T* er = reinterpret_cast<const T*>(&mr);
+                const T* ei = reinterpret_cast<const T*>(&mi);
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    const VT v_r = *reinterpret_cast<const VT*>(vt + (r * 2) * bpad + c);
+                    const VT v_i = *reinterpret_cast<const VT*>(vt + (r * 2 + 1) * bpad + c);
+                    const T* xr = reinterpret_cast<const T*>(&v_r);
+                    const T* xi = reinterpret_cast<const T*>(&v_i);
+#pragma unroll
+                    for (int e = 0; e < VW; ++e) {
+                        ar[r] = fma(er[e], xr[e], ar[r]); ar[r] = fma(-ei[e], xi[e], ar[r]);
+                        ai[r] = fma(er[e], xi[e], ai[r]); ai[r] = fma(ei[e], xr[e], ai[r]);
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < R; ++r)
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                ar[r] += __shfl_down_sync(0xffffffffu, ar[r], o);
+                ai[r] += __shfl_down_sync(0xffffffffu, ai[r], o);
+            }
+        if (lane == 0) {
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                if (r >= g.nrhs) break;
+                T br = 0, bi = 0;
+                if (y0) { br = y0[(r * 2) * g.ld + row]; bi = y0[(r * 2 + 1) * g.ld + row]; }
+                y[(r * 2) * g.ld + row] = br + g.alpha * ar[r];
+                y[(r * 2 + 1) * g.ld + row] = bi + g.alpha * ai[r];
+            }
+        }
+        __syncwarp();   // every lane is done with slot q
+        if (lane == 0 && nm > 0 && k + nslot < nrows) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            issue(k + nslot);
+        }
+    }
+    if (!ok) {
+        // row k's wait ran out: report it, then let this warp's issued copies land
+        if (lane == 0) dev_error(g.err, FDFD_DEVERR_TIMEOUT);
+        const int issued = min(nrows, k + nslot);
+        for (int kk = k; kk < issued; ++kk)
+            (void)mbar_wait(smem_u32(&bars[warp][kk % nslot]), (uint32_t)((kk / nslot) & 1), FDFD_WAIT_LIMIT_NS);
+    }
+}
+
 // Stored-transpose form (row-major Mᵀ): y[i] = Σ_j Mᵀ[j][i] v[j].  A lane owns
 // VW consecutive outputs (one 16-byte load per row j); a group of og lanes
 // covers og*VW outputs, the 8*(32/og) lane groups of the block split the j
@@ -489,6 +645,27 @@ int gemv_launch_r(cudaStream_t s, int tr, int njobs, const GemvArgs<T>& g) {
         while (a.og > 8 && (long long)ceil_div(g.b, a.og * VW) * njobs < want) a.og >>= 1;
         if (g.shape == 8 || g.shape == 16 || g.shape == 32) a.og = g.shape;
         gemv_t_kernel<T, R><<<dim3(ceil_div(g.b, a.og * VW), njobs), 256, smem, s>>>(a);
+    } else if (g.shape <= 0) {
+        // bulk-copy pipeline: per warp a ring of three slots of the launch's blocks per job
+        // (at least two slots, and one slot of two blocks), inside 200 KB of shared memory
+        static const cudaError_t attr_nb = cudaFuncSetAttribute(
+            gemv_nb_kernel<T, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        if (attr_nb != cudaSuccess) return (int)attr_nb;
+        const size_t rb = (size_t)(g.b * (int)sizeof(T) + 15) / 16 * 16;
+        const size_t svb = gemv_nb_smem<T, R>(g.b);
+        const size_t nmx = g.nmat > 1 ? 2 : 1;
+        size_t ring = 3 * nmx * 2 * rb;
+        if (svb + 8 * ring > 200 * 1024) ring = (200 * 1024 - std::min<size_t>(svb, 200 * 1024)) / 8 / 16 * 16;
+        if (ring >= 2 * nmx * 2 * rb && ring >= 4 * rb) {
+            int rw = 8;
+            while (rw > 1 && (long long)ceil_div(g.b, 8 * rw) * njobs < 2 * want / 4) rw >>= 1;
+            if (g.shape == -2 || g.shape == -4 || g.shape == -8) rw = -g.shape;
+            gemv_nb_kernel<T, R><<<dim3(ceil_div(g.b, 8 * rw), njobs), 256, svb + 8 * ring, s>>>(a, rw, (int)ring);
+            return (int)cudaGetLastError();
+        }
+        a.rpw = 4;
+        while (a.rpw > 1 && (long long)ceil_div(g.b, 8 * a.rpw) * njobs < want) a.rpw >>= 1;
+        gemv_n_kernel<T, R><<<dim3(ceil_div(g.b, 8 * a.rpw), njobs), 256, smem, s>>>(a);
     } else {
         a.rpw = 4;
         while (a.rpw > 1 && (long long)ceil_div(g.b, 8 * a.rpw) * njobs < want) a.rpw >>= 1;

@@ -1,4 +1,6 @@
-"""Gauss-Jordan panel forms against the one-CTA lane-quad form, through the C ABI.
+"""Alternative kernel forms against the default ones, through the C ABI: the
+Gauss-Jordan panel forms against the one-CTA lane-quad form, and the bulk-copy
+sweep products against the register-load kernel.
 
 * cluster form: one matrix's panel split over 2, 4 or 8 CTAs of a thread-block
   cluster (FDFD_GJ_CL, read when the handle is created; -1 picks the size per
@@ -58,3 +60,21 @@ def test_panel_forms_match_quad_form(lib, fdfd, oracle, monkeypatch, prec, size)
     ref = oracle.solve(g, p.eps, p.src, p.omega, oracle.TM, p.pml_m, p.pml_lnR)
     tol = 1e-8 if prec == "mixed" else 1e-10
     assert max(rel(auto[0], ref[0]), rel(auto[1], ref[1]), rel(auto[2], ref[2])) <= tol
+
+
+@pytest.mark.parametrize("prec", ["mixed", "fp64"])
+@pytest.mark.parametrize("size", [(260, 200), (301, 197)])
+def test_bulk_copy_sweep_matches_register_form(lib, fdfd, monkeypatch, prec, size):
+    """The N-form sweep products through the bulk-copy pipeline (the default where it fits)
+    give the fields of the register-load kernel bit for bit (b = 200: 16-byte rows; b = 197:
+    a row end inside a 16-byte vector)."""
+    from fdfd_gb300 import workloads as W
+    p = W.design_guide(size[0], size[1], design=(48, 48), seed=12, npml=12)
+    P = fdfd.FDFD_PREC_FP64 if prec == "fp64" else fdfd.FDFD_PREC_MIXED
+    monkeypatch.setenv("FDFD_GEMV_BULK", "0")
+    ref = run(fdfd, monkeypatch, p, P, [])
+    monkeypatch.setenv("FDFD_GEMV_BULK", "1")
+    got = run(fdfd, monkeypatch, p, P, [])
+    assert got[3].iterations == ref[3].iterations and got[3].rel_residual <= TOL_RES
+    for a, b in zip(got[:3], ref[:3]):
+        assert np.array_equal(a, b), rel(a, b)
