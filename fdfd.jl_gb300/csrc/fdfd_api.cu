@@ -223,7 +223,7 @@ struct fdfd_handle {
     // autotuner (fdfd_autotune): tile width per tensor-core GEMM shape (M, N, K, jobs, pre-split
     // operands) and launch shape per sweep product (form, jobs, right-hand sides per launch)
     std::map<std::tuple<int, int, int, int, int>, int> tune_gemm;
-    std::map<std::tuple<int, int, int>, int> tune_gemv;
+    std::map<std::tuple<int, int, int, int>, int> tune_gemv;   // (form, jobs, blocks per job, rhs) -> shape
     std::string tune_log;
     int force_bn = 0, force_shape = 0;   // set while the autotuner times a candidate
     // profiling (CUDA events around launches on the handle's stream)
@@ -1213,7 +1213,7 @@ template <typename T> int gemv(fdfd_handle* h, int tr, int p1, int p2, const T* 
         g.err = h->derr;
         g.shape = h->force_shape;
         if (!g.shape) {
-            auto it = h->tune_gemv.find(std::make_tuple(tr, njobs, g.nrhs));
+            auto it = h->tune_gemv.find(std::make_tuple(tr, njobs, g.nmat, g.nrhs));
             if (it != h->tune_gemv.end()) g.shape = it->second;
         }
         if (!tr && g.shape == 0 && !h->gemv_bulk) g.shape = GEMV_SHAPE_REGISTER_RULE;
@@ -2951,8 +2951,8 @@ template <typename T> int autotune_impl(fdfd_handle* h) {
     }
     // ---- sweep product launch shapes
     auto tune_v = [&](int tr, int p1, int p2, const T* V1, const T* V2, const T* Y0, T* Y, const int4* jobs,
-                      const int2* yjobs, int njobs, int nrhs, const char* role) -> int {
-        const auto key = std::make_tuple(tr, njobs, nrhs);
+                      const int2* yjobs, int njobs, int nblk, int nrhs, const char* role) -> int {
+        const auto key = std::make_tuple(tr, njobs, nblk > njobs ? 2 : 1, nrhs);
         if (njobs == 0 || h->tune_gemv.count(key)) return FDFD_OK;
         int best = 0;
         double tbest = 1e30;
@@ -2963,7 +2963,7 @@ template <typename T> int autotune_impl(fdfd_handle* h) {
             h->force_shape = c;
             double ms = 0;
             const int rc = time_launch(h, [&] { return gemv<T>(h, tr, p1, p2, V1, V2, Y0, Y, jobs, yjobs, njobs,
-                                                               njobs, nrhs, (T)1); }, &ms);
+                                                               nblk, nrhs, (T)1); }, &ms);
             h->force_shape = 0;
             RET(rc);
             snprintf(line, sizeof line, " %d:%.4f", c, ms);
@@ -2983,20 +2983,20 @@ template <typename T> int autotune_impl(fdfd_handle* h) {
         for (int e = 1; e <= E; ++e) {
             const StepJobs& S = h->sj[e];
             if (e == 1 && !(F.trifac && h->tri_sweep && !h->level1_gj))
-                RET(tune_v(0, P_D, P_D, F.rv, F.rv, nullptr, F.xv, J<int4>(h, S.fwd1), J<int2>(h, S.fwd1y), S.ne, nr,
-                           "inverse"));
+                RET(tune_v(0, P_D, P_D, F.rv, F.rv, nullptr, F.xv, J<int4>(h, S.fwd1), J<int2>(h, S.fwd1y), S.ne, S.ne,
+                           nr, "inverse"));
             if (e >= 2) {
-                RET(tune_v(0, P_D, P_D, F.rv, F.rv, nullptr, F.xv, J<int4>(h, S.fwd1), J<int2>(h, S.fwd1y), S.ne, nr,
-                           "inverse"));
-                RET(tune_v(0, P_C, P_C, F.xv, F.xv, F.rv, F.rv, J<int4>(h, S.f2), J<int2>(h, S.f2y), S.nf2, nr,
-                           "coupling"));
-                RET(tune_v(1, P_X, P_X, F.xv, F.xv, F.xv, F.xv, J<int4>(h, S.bw), J<int2>(h, S.bwy), S.ne, nr,
-                           "back"));
+                RET(tune_v(0, P_D, P_D, F.rv, F.rv, nullptr, F.xv, J<int4>(h, S.fwd1), J<int2>(h, S.fwd1y), S.ne, S.ne,
+                           nr, "inverse"));
+                RET(tune_v(0, P_C, P_C, F.xv, F.xv, F.rv, F.rv, J<int4>(h, S.f2), J<int2>(h, S.f2y), S.nf2, S.nf2b,
+                           nr, "coupling"));
+                RET(tune_v(1, P_X, P_X, F.xv, F.xv, F.xv, F.xv, J<int4>(h, S.bw), J<int2>(h, S.bwy), S.ne, 2 * S.ne,
+                           nr, "back"));
             }
         }
-        RET(tune_v(0, P_D, P_D, F.rv, F.rv, nullptr, F.xv, J<int4>(h, h->fin_g1), J<int2>(h, h->fin_g1y), 1, nr,
+        RET(tune_v(0, P_D, P_D, F.rv, F.rv, nullptr, F.xv, J<int4>(h, h->fin_g1), J<int2>(h, h->fin_g1y), 1, 1, nr,
                    "inverse"));
-        RET(tune_v(1, P_X, P_X, F.xv, F.xv, F.xv, F.xv, J<int4>(h, h->fin_bx), J<int2>(h, h->fin_bxy), 1, nr,
+        RET(tune_v(1, P_X, P_X, F.xv, F.xv, F.xv, F.xv, J<int4>(h, h->fin_bx), J<int2>(h, h->fin_bxy), 1, 1, nr,
                    "back"));
     }
     h->prof_on = prof;
