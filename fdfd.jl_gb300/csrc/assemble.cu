@@ -5,6 +5,8 @@
 // column-major `A[:]` ordering of src/solver/driven.jl:21).  All neighbours are
 // periodic, exactly as the reference's difference matrices (src/grid.jl:138-151,
 // the ±(N-1) corner entries).
+#include <algorithm>
+
 #include "common.cuh"
 #include "kernels.cuh"
 
@@ -648,4 +650,27 @@ __global__ void vdotu_kernel(long long N, const cplx<double>* __restrict__ m, co
         part[blockIdx.x * 2] = a;
         part[blockIdx.x * 2 + 1] = b;
     }
+}
+
+// First invalid entries of a staged host input of n complex values (interleaved):
+// first[0] = lowest double index of a NaN or ±inf, first[1] (when zeros) = lowest
+// complex index whose real and imaginary parts are both zero.  first[] starts at
+// ~0ull; a thread only writes when it finds something, so valid input costs one
+// read of the data.  grid-stride, any grid.
+__global__ void validate_kernel(const double2* __restrict__ x, long long n, int zeros, unsigned long long* first) {
+    unsigned long long bad = ~0ull, zero = ~0ull;
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
+        const double2 v = x[c];
+        if (!isfinite(v.x) && (unsigned long long)(2 * c) < bad) bad = 2 * c;
+        else if (!isfinite(v.y) && (unsigned long long)(2 * c + 1) < bad) bad = 2 * c + 1;
+        if (zeros && v.x == 0.0 && v.y == 0.0 && (unsigned long long)c < zero) zero = c;
+    }
+    if (bad != ~0ull) atomicMin(&first[0], bad);
+    if (zero != ~0ull) atomicMin(&first[1], zero);
+}
+void launch_validate(cudaStream_t s, int nsm, const double* x, long long n, int zeros, unsigned long long* first) {
+    cudaMemsetAsync(first, 0xFF, 2 * sizeof(unsigned long long), s);
+    const long long want = (n + 255) / 256;
+    const int grid = (int)std::max(1LL, std::min(want, 4LL * std::max(1, nsm)));
+    validate_kernel<<<grid, 256, 0, s>>>(reinterpret_cast<const double2*>(x), n, zeros, first);
 }

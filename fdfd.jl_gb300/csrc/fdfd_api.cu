@@ -161,6 +161,9 @@ struct fdfd_handle {
     unsigned long long wait_ns = 0;      // pipeline wait limit of the tensor-core GEMM (0: default)
     // FP64 device buffers (natural layout)
     cplx<double>* eps = nullptr;     // Nx*Ny
+    cplx<double>* eps_stage = nullptr;   // fdfd_set_eps: the new ϵᵣ, validated before it replaces eps
+    unsigned long long* vflags = nullptr;     // validate_kernel's first invalid entries (device) ...
+    unsigned long long* vflags_h = nullptr;   // ... and their pinned host copy
     cplx<double>* sf = nullptr;      // 2*(2Nx+2Ny)
     cplx<double>* st = nullptr;      // 5*Nx*Ny
     unsigned* derr = nullptr;        // device error word
@@ -326,6 +329,25 @@ int dev_alloc(fdfd_handle* h, void** p, size_t bytes) {
     h->alloc_bytes[*p] = bytes;
     return FDFD_OK;
 }
+
+// first invalid entries of n complex values already on the device (on the handle's
+// stream, which it synchronises): *bad = lowest double index of a NaN/inf, *zero (may
+// be null) = lowest complex index of a zero; -1 where there is none
+int validate_device(fdfd_handle* h, const double* dx, long long n, bool zeros, long long* bad, long long* zero) {
+    if (!h->vflags) RET(dev_alloc(h, (void**)&h->vflags, 2 * sizeof(unsigned long long)));
+    if (!h->vflags_h && cudaMallocHost((void**)&h->vflags_h, 2 * sizeof(unsigned long long)) != cudaSuccess) {
+        h->vflags_h = nullptr;
+        return set_err(h, FDFD_ENOMEM, "pinned host allocation failed");
+    }
+    launch_validate(h->stream, h->num_sms, dx, n, zeros ? 1 : 0, h->vflags);
+    h->launches++;
+    CK(cudaMemcpyAsync(h->vflags_h, h->vflags, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    *bad = h->vflags_h[0] == ~0ull ? -1 : (long long)h->vflags_h[0];
+    if (zero) *zero = (zeros && h->vflags_h[1] != ~0ull) ? (long long)h->vflags_h[1] : -1;
+    return FDFD_OK;
+}
+
 
 // frees a dev_alloc'd buffer and returns its bytes to the handle's count
 void dev_free(fdfd_handle* h, void* p) {
@@ -1880,8 +1902,9 @@ void fdfd_destroy(fdfd_handle* h) {
         h->mf = nullptr;
     }
     void* bufs[] = {h->eps, h->sf, h->st, h->derr, h->dargs, h->part, h->red, h->kb, h->kx, h->kr, h->kV, h->kZ,
-                    h->kc, h->io, h->djobs, h->mode_buf, h->nl_d1};
+                    h->kc, h->io, h->djobs, h->mode_buf, h->nl_d1, h->eps_stage, h->vflags};
     for (void* p : bufs) dev_free(h, p);
+    if (h->vflags_h) cudaFreeHost(h->vflags_h);
     free_store(h, h->f32);
     free_store(h, h->f64);
     for (auto& e : h->ev) if (e) cudaEventDestroy(e);
@@ -1955,10 +1978,15 @@ int fdfd_set_device_budget(fdfd_handle* h, long long bytes) {
 int fdfd_set_eps(fdfd_handle* h, const double* eps_r) {
     if (!h || !eps_r) return h ? set_err(h, FDFD_EINVAL, "eps_r is NULL") : FDFD_EINVAL;
     long long N = (long long)h->Nx * h->Ny;
-    if (const long long k = first_nonfinite(eps_r, 2 * N); k >= 0)
-        return set_err(h, FDFD_EINVAL, "eps_r has a non-finite entry at %lld", k / 2);
-    if (const long long k = first_zero(eps_r, N); k >= 0) return set_err(h, FDFD_EINVAL, "eps_r is zero at %lld", k);
-    CK(cudaMemcpyAsync(h->eps, eps_r, N * sizeof(cplx<double>), cudaMemcpyHostToDevice, h->stream));
+    // staged and validated on the device (one read at HBM speed instead of two host scans);
+    // a rejected ϵᵣ leaves the handle's permittivity as it was
+    if (!h->eps_stage) RET(dev_alloc(h, (void**)&h->eps_stage, N * sizeof(cplx<double>)));
+    CK(cudaMemcpyAsync(h->eps_stage, eps_r, N * sizeof(cplx<double>), cudaMemcpyHostToDevice, h->stream));
+    long long kbad = -1, kzero = -1;
+    RET(validate_device(h, reinterpret_cast<const double*>(h->eps_stage), N, true, &kbad, &kzero));
+    if (kbad >= 0) return set_err(h, FDFD_EINVAL, "eps_r has a non-finite entry at %lld", kbad / 2);
+    if (kzero >= 0) return set_err(h, FDFD_EINVAL, "eps_r is zero at %lld", kzero);
+    CK(cudaMemcpyAsync(h->eps, h->eps_stage, N * sizeof(cplx<double>), cudaMemcpyDeviceToDevice, h->stream));
     if (h->mf)
         for (fdfd_handle* s : h->mf->sub) {
             CK(cudaMemcpyAsync(s->eps, h->eps, N * sizeof(cplx<double>), cudaMemcpyDeviceToDevice, h->stream));
@@ -2077,7 +2105,6 @@ int fdfd_solve(fdfd_handle* h, const double* src, int nrhs, double* f1, double* 
     if (!src || nrhs < 1) return set_err(h, FDFD_EINVAL, "invalid source arguments");
     auto t0 = std::chrono::steady_clock::now();
     long long N = (long long)h->Nx * h->Ny;
-    if (first_nonfinite(src, 2 * N * nrhs) >= 0) return set_err(h, FDFD_EINVAL, "src has a non-finite entry");
     size_t bytes = (size_t)N * nrhs * sizeof(cplx<double>);
     // staging: [src | f1 | f2 | f3], kept by the handle between calls
     if (h->io_cap < 4 * bytes) {
@@ -2095,6 +2122,11 @@ int fdfd_solve(fdfd_handle* h, const double* src, int nrhs, double* f1, double* 
     int rc = FDFD_OK;
     if (cudaMemcpyAsync(dsrc, src, bytes, cudaMemcpyHostToDevice, h->stream) != cudaSuccess)
         rc = set_err(h, FDFD_ECUDA, "copy of src failed");
+    if (rc == FDFD_OK) {   // validated on the device, before any solve work
+        long long kbad = -1;
+        rc = validate_device(h, reinterpret_cast<const double*>(dsrc), N * nrhs, false, &kbad, nullptr);
+        if (rc == FDFD_OK && kbad >= 0) rc = set_err(h, FDFD_EINVAL, "src has a non-finite entry");
+    }
     if (rc == FDFD_OK) rc = solve_core(h, dsrc, nrhs, d1, d2, d3, stats);
     if (rc == FDFD_OK || rc == FDFD_ENOCONV) {
         if (f1) cudaMemcpyAsync(f1, d1, bytes, cudaMemcpyDeviceToHost, h->stream);

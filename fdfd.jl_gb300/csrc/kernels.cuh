@@ -30,6 +30,9 @@ struct NodeMap {
 struct AssembleArgs { SFactorArgs sf; StencilArgs st; };
 __global__ void sfactor_kernel(const SFactorArgs* a, cplx<double>* out);
 __global__ void stencil_kernel(const StencilArgs* a, const cplx<double>* eps, const cplx<double>* sf, cplx<double>* st);
+// first[0]: lowest double index of a non-finite entry of x (n complex values), first[1]
+// (zeros != 0): lowest complex index with a zero value; ~0ull where there is none
+void launch_validate(cudaStream_t s, int nsm, const double* x, long long n, int zeros, unsigned long long* first);
 __global__ void residual_kernel(int Nx, int Ny, int nrhs, const cplx<double>* st, const cplx<double>* x,
                                 const cplx<double>* b, cplx<double>* r, double* part);
 // Coupled sideband system of a modulated device: K = 2s+1 stencils (one per

@@ -329,11 +329,42 @@ def test_errors(lib, fdfd):
     eps[3, 4] = np.nan
     with pytest.raises(fdfd.FDFDError) as e:
         h.set_eps(eps)
-    assert e.value.code == fdfd._lib.FDFD_EINVAL
+    assert e.value.code == fdfd._lib.FDFD_EINVAL and "non-finite entry at 83" in str(e.value)   # 3 + 20 * 4, x fastest
     h.set_eps(np.ones((20, 16)))
     with pytest.raises(fdfd.FDFDError):
         h.factor(-1.0)
     h.close()
+
+
+def test_rejected_inputs_leave_the_handle_unchanged(lib, fdfd):
+    """ϵᵣ and sources are validated on the device after the copy: a rejected ϵᵣ (NaN, inf or a
+    complex zero) leaves the previous permittivity in place, a rejected source leaves the factors,
+    and the handle then solves as before."""
+    h = handle_for(fdfd, 40, 30, (6, 6), 0.05, 0.05, 4.0, np.log(1e-8), fdfd.TM, fdfd.FDFD_PREC_MIXED)
+    eps = np.ones((40, 30), dtype=complex)
+    eps[15:25, 10:20] = 6.0
+    src = np.zeros((40, 30), dtype=complex)
+    src[10, 15] = 1.0
+    h.set_eps(eps)
+    h.factor(2 * np.pi * 299792458.0 / 1.55e-6)
+    ref = h.solve(src)[:3]
+    for bad, msg in ((np.inf, "non-finite entry at 501"), (0.0, "is zero at 501")):
+        e2 = eps.copy()
+        e2[21, 12] = bad                      # index 21 + 40 * 12 = 501 in the x-fastest order
+        with pytest.raises(fdfd.FDFDError) as e:
+            h.set_eps(e2)
+        assert e.value.code == fdfd._lib.FDFD_EINVAL and msg in str(e.value), str(e.value)
+    s2 = src.copy()
+    s2[3, 3] = np.nan
+    with pytest.raises(fdfd.FDFDError) as e:
+        h.solve(s2)
+    assert e.value.code == fdfd._lib.FDFD_EINVAL
+    got = h.solve(src)[:3]                    # same factors
+    h.factor(2 * np.pi * 299792458.0 / 1.55e-6)
+    again = h.solve(src)[:3]                  # refactored from the kept permittivity
+    h.close()
+    for a, b, c in zip(ref, got, again):
+        assert np.array_equal(a, b) and np.array_equal(a, c)
 
 
 @pytest.mark.parametrize("prec", ["fp64", "mixed"])
