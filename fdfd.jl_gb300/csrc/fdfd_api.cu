@@ -94,6 +94,8 @@ template <typename T> struct FactorStore {
     cplx<T>* trifac = nullptr;  // first-step tridiagonal factors (8*b per node)
     int* tripiv = nullptr;      // and their interchanges (b per node)
     cplx<T>* sttab = nullptr;   // scaled stencil planes of every node in the factor precision (5*b per node)
+    Pool<T> Wk;                 // split-K partial products (FP32 tensor-core path)
+    int* wk_iota = nullptr;     // 0 .. Wk.count-1
     bool tc_ok = false;
     TcMaps tc;       // TMA descriptors (FP32 only)
     bool complete = false;   // every pool above allocated
@@ -211,6 +213,8 @@ struct fdfd_handle {
     bool use_tc = true;
     bool level1_gj = false;     // invert first-step blocks by Gauss-Jordan instead of the O(b²) kernel
     bool tri_sweep = true;      // first-step sweep products through the tridiagonal factors, not the dense inverses
+    bool splitk = true;            // split-K for tensor-core products whose tiles fill less than half the
+                                   // SMs (FDFD_SPLITK=0: off)
     bool gemv_bulk = false;        // untuned N-form sweep products through the bulk-copy pipeline where it
                                    // fits (FDFD_GEMV_BULK=1), else register loads; the autotuner times both
     bool gj_presplit = true;       // FP32 panel buffers G, Rᵀ stored with their TF32 residual planes
@@ -646,7 +650,8 @@ template <typename T> int alloc_pool(fdfd_handle* h, Pool<T>& P, int rows, int c
 
 template <typename T> void free_store(fdfd_handle* h, FactorStore<T>& F) {
     void* bufs[] = {F.D.base, F.C.base, F.X.base, F.GP.base, F.RP.base, F.Tg.base, F.rv, F.xv, F.wv,
-                    F.perm, F.rowsrc, F.inv, F.gsub, F.gj_slots, F.trifac, F.tripiv, F.sttab};
+                    F.perm, F.rowsrc, F.inv, F.gsub, F.gj_slots, F.trifac, F.tripiv, F.sttab, F.Wk.base,
+                    F.wk_iota};
     for (void* p : bufs) dev_free(h, p);
     if (F.hC || F.hX) {
         const long long se = F.C.slot_elems();
@@ -672,6 +677,20 @@ template <typename T> void free_store(fdfd_handle* h, FactorStore<T>& F) {
 // ---------------------------------------------------------------------------
 int restart_len(const fdfd_handle* h, int nrhs);
 
+// K slices of a tensor-core product with bcols-wide tiles: a product whose tiles fill less
+// than half of the SMs is split along K (at most 8 slices of at least 64 columns, at most
+// SPLITK_SLOTS partial products per launch) so that its CTAs cover the GPU; 1 = no split
+constexpr int SPLITK_SLOTS = 64;
+static int splitk_of(const fdfd_handle* h, int M, int N, int K, int njobs, int bcols) {
+    if (!h->splitk || K < 256) return 1;
+    const long long tiles = (long long)ceil_div(M, 128) * ceil_div(N, bcols) * njobs;
+    if (2 * tiles > h->num_sms) return 1;
+    int ks = (int)std::min<long long>(8, h->num_sms / tiles);
+    ks = std::min(ks, K / 64);
+    while (ks > 1 && (long long)njobs * ks > SPLITK_SLOTS) --ks;
+    return ks < 2 ? 1 : ks;
+}
+
 // device bytes the factorization and a one-source solve will add, resident and in
 // checkpoint mode: D, C and X blocks, the Gauss-Jordan and first-step work space,
 // the sweep vectors and the FP64 Krylov basis (estimates of the later allocations)
@@ -687,7 +706,8 @@ template <typename T> void factor_bytes(const fdfd_handle* h, double* resident, 
     }
     const int nC = h->ckpt ? h->orig_nC : h->nCslots, nX = h->ckpt ? h->orig_nX : h->nXslots;
     const double N = (double)h->Nx * h->Ny;
-    const double work = sb * gj_max + 2.0 * 2 * h->max_ne * b * 32 * 4 * sizeof(T) + 3.0 * h->max_ne * b * 4 +
+    const double wk = (sizeof(T) == 4 && h->use_tc && h->splitk && b >= 256) ? sb * SPLITK_SLOTS : 0.0;   // split-K
+    const double work = wk + sb * gj_max + 2.0 * 2 * h->max_ne * b * 32 * 4 * sizeof(T) + 3.0 * h->max_ne * b * 4 +
                         (double)n * 14 * b * sizeof(cplx<T>) + 3.0 * n * 2 * ld * sizeof(T) +
                         (2.0 * restart_len(h, 1) + 4) * N * sizeof(cplx<double>);
     *resident = sb * (n + nC + nX) + work;
@@ -815,6 +835,29 @@ template <typename T> int alloc_factor_pools(fdfd_handle* h) {
     // two sets (panel parity) so that a panel can run while the previous panel's update reads the other set
     RET(alloc_pool<T>(h, F.GP, b, pc, pc, pplanes, 2 * h->max_ne));
     RET(alloc_pool<T>(h, F.RP, b, pc, pc, pplanes, 2 * h->max_ne));
+    // split-K work space: the most slices any Schur product of the plan can take
+    if (sizeof(T) == 4 && h->use_tc && h->splitk) {
+        long long wk = 0;
+        auto need = [&](int nj) {
+            for (int bc : {64, 128, 256}) {
+                const int ks = splitk_of(h, b, b, b, nj, bc);
+                if (ks > 1) wk = std::max(wk, (long long)nj * ks);
+            }
+        };
+        for (int e = 2; e < (int)h->sj.size(); ++e) {
+            need(2 * h->sj[e].ne);
+            need(h->sj[e].ne);
+            need(h->sj[e].ncp);
+        }
+        need(1);
+        if (wk > 1) {
+            RET(alloc_pool<T>(h, F.Wk, b, b, ld, 2, wk));
+            std::vector<int> io(wk);
+            for (long long i = 0; i < wk; ++i) io[i] = (int)i;
+            RET(dev_alloc(h, (void**)&F.wk_iota, io.size() * sizeof(int)));
+            CK(cudaMemcpy(F.wk_iota, io.data(), io.size() * sizeof(int), cudaMemcpyHostToDevice));
+        }
+    }
     {
         std::vector<int> sl(2 * h->max_ne);
         for (int i = 0; i < 2 * h->max_ne; ++i) sl[i] = i;
@@ -925,7 +968,38 @@ int gemm(fdfd_handle* h, int pa, int pb, int pc, const int* a_slot, const int* b
             auto it = h->tune_gemm.find(std::make_tuple(M, N, K, njobs, (int)(g.A.planes == 4)));
             if (it != h->tune_gemm.end()) bn = it->second;
         }
-        int rc = tc_gemm_launch(reinterpret_cast<GemmArgs<float>*>(&g), c_trans_arr, pa, pb, njobs, &F.tc,
+        // split-K (deterministic): partial products into the Wk slots, then their ordered sum
+        // with the α, β and storage form of the product
+        const int bne = (bn == 64 || bn == 128 || bn == 256 || bn == TC_BN128_TWO) ? bn
+                                                                                   : tc_pick_bn(M, N, K, njobs, h->num_sms);
+        int ks = (F.Wk.base && mask_w == 0 && n_off == 0 && skip_w == 0 && !row_dst && !row_src && pcin < 0 &&
+                  g.A.planes == 2)
+                     ? splitk_of(h, M, N, K, njobs, bne == TC_BN128_TWO ? 128 : bne)
+                     : 1;
+        int rc = 0;
+        if (ks > 1) {
+            GemmArgs<T> pg = g;
+            pg.kslice = ceil_div(K, ks * 8) * 8;
+            ks = ceil_div(K, pg.kslice);
+            pg.ksplit = ks;
+            pg.C = F.Wk;
+            pg.c_slot = F.wk_iota;
+            pg.alpha = (T)1;
+            pg.beta = 0;
+            pg.c_trans = 0;
+            if ((long long)njobs * ks > F.Wk.count || M > F.Wk.rows || N > F.Wk.cols) ks = 1;
+            else {
+                rc = tc_gemm_launch(reinterpret_cast<GemmArgs<float>*>(&pg), nullptr, pa, pb, njobs, &F.tc,
+                                    h->num_sms, stream, bn);
+                if (rc == 0)
+                    rc = tc_splitk_sum(*reinterpret_cast<const Pool<float>*>(&F.Wk), ks,
+                                       *reinterpret_cast<const Pool<float>*>(&g.C), c_slot, c_trans_arr, c_trans,
+                                       njobs, M, N, (float)alpha, beta, stream);
+                h->launches++;
+            }
+        }
+        if (ks <= 1)
+            rc = tc_gemm_launch(reinterpret_cast<GemmArgs<float>*>(&g), c_trans_arr, pa, pb, njobs, &F.tc,
                                 h->num_sms, stream, bn);
         if (rc != 0) return set_err(h, FDFD_ECUDA, "tcgen05 GEMM launch failed (%d)", rc);
         prof_end(h, ev, prof_cls >= 0 ? prof_cls : FDFD_PROF_GEMM_TC, prof_cls >= 0 ? prof_work : flops);
@@ -1844,6 +1918,7 @@ int fdfd_create(fdfd_handle** out, int Nx, int Ny, int Npx, int Npy, double dx, 
     if (const char* e = getenv("FDFD_GJ_FORM")) h->gj_form = atoi(e) == 1 ? 1 : 0;
     if (const char* e = getenv("FDFD_GJ_PRESPLIT")) h->gj_presplit = atoi(e) != 0;
     if (const char* e = getenv("FDFD_GEMV_BULK")) h->gemv_bulk = atoi(e) != 0;
+    if (const char* e = getenv("FDFD_SPLITK")) h->splitk = atoi(e) != 0;
     if (const char* e = getenv("FDFD_GJ_FUSED_MIN")) h->gj_fused_min = std::max(1, atoi(e));
     NodeMap& m = h->map;
     m.Nx = Nx; m.Ny = Ny;

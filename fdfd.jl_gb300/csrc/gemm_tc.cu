@@ -144,9 +144,14 @@ __global__ void __launch_bounds__(TcTile<BN, TWO>::THREADS, TcTile<BN, TWO>::MIN
     const GemmArgs<float>& g = P.g;
     const uint64_t wait_ns = g.wait_ns ? g.wait_ns : FDFD_WAIT_LIMIT_NS;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int job = blockIdx.z;
+    // split-K: CTA z works on job z / ksplit over one slice of K and writes its own C slot
+    const int ks = g.ksplit > 1 ? g.ksplit : 1;
+    const int job = blockIdx.z / ks;
+    const int cjob = ks > 1 ? (int)blockIdx.z : job;     // index into c_slot
+    const int kbeg = ks > 1 ? (int)(blockIdx.z % ks) * g.kslice : 0;
+    const int klen = ks > 1 ? min(g.kslice, g.K - kbeg) : g.K;
     const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
-    const int nk = (g.K + BK - 1) / BK;
+    const int nk = (klen + BK - 1) / BK;
     const bool presplit = g.A.planes == 4;             // operand form (A and B alike)
     const int np = presplit ? 4 : 2;                   // planes loaded by TMA
     unsigned char* smem = reinterpret_cast<unsigned char*>(
@@ -188,7 +193,7 @@ __global__ void __launch_bounds__(TcTile<BN, TWO>::THREADS, TcTile<BN, TWO>::MIN
                 const uint32_t bar = smem_u32(&bar_full[s]);
                 mbar_expect_tx(bar, np * (A_PLANE_BYTES + B_PLANE_BYTES));
                 const uint32_t st = sbase + s * STAGE_BYTES;
-                const int k0 = kt * BK;
+                const int k0 = kbeg + kt * BK;
                 for (int p = 0; p < np; ++p)
                     tma_load_3d(st + p * A_PLANE_BYTES, &mapA, k0, m0, aslot * np + p, bar);
                 for (int p = 0; p < np; ++p)
@@ -256,7 +261,7 @@ __global__ void __launch_bounds__(TcTile<BN, TWO>::THREADS, TcTile<BN, TWO>::MIN
         // ld-padded, so the range [n0, min(n0 + BN, ld)) is 16-byte aligned and sized.
         if (g.beta && nk <= STAGES && !(g.c_trans_arr ? g.c_trans_arr[job] : g.c_trans)) {
             const bool sep = g.Cin.base != nullptr;
-            const float* Ci = sep ? g.Cin.slot(g.cin_slot[job]) : g.C.slot(g.c_slot[job]);
+            const float* Ci = sep ? g.Cin.slot(g.cin_slot[job]) : g.C.slot(g.c_slot[cjob]);
             const long long cipe = sep ? g.Cin.plane_elems() : g.C.plane_elems();
             const int cild = sep ? g.Cin.ld : g.C.ld;
             const int* rsrc = (sep && g.row_src) ? g.row_src + (long long)job * g.M : nullptr;
@@ -311,7 +316,7 @@ __global__ void __launch_bounds__(TcTile<BN, TWO>::THREADS, TcTile<BN, TWO>::MIN
             const int row0 = m0 + q * 32;
             const int row = row0 + lane;
             const int ctr = g.c_trans_arr ? g.c_trans_arr[job] : g.c_trans;
-            float* C = g.C.slot(g.c_slot[job]);
+            float* C = g.C.slot(g.c_slot[cjob]);
             const long long pe = g.C.plane_elems();
             const long long ld = g.C.ld;
             // β term source: C itself, or row row_src[m] of Cin
@@ -506,11 +511,67 @@ int tc_launch_bn(const GemmArgs<float>* g, const int* c_trans_arr, const CUtenso
     TcParams P;
     P.g = *g;
     if (c_trans_arr) P.g.c_trans_arr = c_trans_arr;
-    dim3 grid((g->N + BN - 1) / BN, (g->M + BM - 1) / BM, njobs);
+    dim3 grid((g->N + BN - 1) / BN, (g->M + BM - 1) / BM, njobs * (g->ksplit > 1 ? g->ksplit : 1));
     gemm_tc_kernel<BN, TWO><<<grid, Tile::THREADS, Tile::SMEM_BYTES, stream>>>(*mapA, *mapB, P);
     return (int)cudaGetLastError();
 }
 }  // namespace
+
+// Split-K sum: C[c_slot[job]] = alpha·Σ_{s<ks} W[job·ks + s] (+ C itself when beta), the
+// slices added in order (deterministic); stored transposed (Cᵀ) when trans, through a
+// 32 x 32 shared tile so both the reads and the writes coalesce.
+// grid (ceil(N/32), ceil(M/32), njobs), block (32, 8)
+__global__ void splitk_sum_kernel(Pool<float> W, int ks, Pool<float> Cp, const int* c_slot, const int* c_trans_arr,
+                                  int c_trans, int M, int N, float alpha, int beta) {
+    __shared__ float t[2][32][33];
+    const int job = blockIdx.z;
+    const int c0 = blockIdx.x * 32, r0 = blockIdx.y * 32;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const long long wpe = W.plane_elems(), cpe = Cp.plane_elems();
+    float* C = Cp.slot(c_slot[job]);
+    const int tr = c_trans_arr ? c_trans_arr[job] : c_trans;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int r = r0 + ty + 8 * q, c = c0 + tx;
+        float sr = 0.f, si = 0.f;
+        if (r < M && c < N) {
+            for (int s = 0; s < ks; ++s) {
+                const float* w = W.slot((long long)job * ks + s) + (long long)r * W.ld + c;
+                sr += w[0];
+                si += w[wpe];
+            }
+            sr *= alpha;
+            si *= alpha;
+            if (!tr) {
+                const long long o = (long long)r * Cp.ld + c;
+                if (beta) { sr += C[o]; si += C[cpe + o]; }
+                C[o] = sr;
+                C[cpe + o] = si;
+            }
+        }
+        t[0][ty + 8 * q][tx] = sr;
+        t[1][ty + 8 * q][tx] = si;
+    }
+    if (!tr) return;   // uniform per block
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int cl = ty + 8 * q;
+        const int cc = c0 + cl, rr = r0 + tx;
+        if (cc < N && rr < M) {
+            const long long o = (long long)cc * Cp.ld + rr;
+            C[o] = t[0][tx][cl];
+            C[cpe + o] = t[1][tx][cl];
+        }
+    }
+}
+
+int tc_splitk_sum(const Pool<float>& W, int ks, const Pool<float>& C, const int* c_slot, const int* c_trans_arr,
+                  int c_trans, int njobs, int M, int N, float alpha, int beta, cudaStream_t stream) {
+    splitk_sum_kernel<<<dim3((N + 31) / 32, (M + 31) / 32, njobs), dim3(32, 8), 0, stream>>>(
+        W, ks, C, c_slot, c_trans_arr, c_trans, M, N, alpha, beta);
+    return (int)cudaGetLastError();
+}
 
 int tc_gemm_launch_maps(const GemmArgs<float>* g, const int* c_trans_arr, const CUtensorMap* mapA,
                         const CUtensorMap* mapB, int bn, int njobs, cudaStream_t stream) {

@@ -18,6 +18,11 @@ bool tc_make_map(const Pool<float>& P, CUtensorMap* box128, CUtensorMap* box256,
 bool tc_make_maps(const Pool<float>* D, const Pool<float>* C, const Pool<float>* X, const Pool<float>* GP,
                   const Pool<float>* RP, TcMaps* out);
 
+// C[c_slot[job]] = alpha·Σ_{s<ks} W[job·ks + s] (+ beta·C), N form or transposed per job:
+// the second phase of a split-K product (returns a cudaError_t value)
+int tc_splitk_sum(const Pool<float>& W, int ks, const Pool<float>& C, const int* c_slot, const int* c_trans_arr,
+                  int c_trans, int njobs, int M, int N, float alpha, int beta, cudaStream_t stream);
+
 // tile code of the 128-column tile sized for two CTAs per SM (three pipeline
 // stages, four epilogue warps): its B tiles use the 128-row box
 #define TC_BN128_TWO 129

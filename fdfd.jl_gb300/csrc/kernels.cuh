@@ -203,6 +203,10 @@ template <typename T> struct GemmArgs {
     // tensor-core kernel only: limit of each pipeline wait in ns of %globaltimer
     // (0: FDFD_WAIT_LIMIT_NS); the drain waits before exit always take the full limit
     unsigned long long wait_ns;
+    // tensor-core kernel only, split-K partial products: ksplit > 1 runs grid z = jobs x
+    // ksplit, CTA z taking job z / ksplit over K columns [(z % ksplit)·kslice, +kslice) and
+    // writing its raw product to C slot c_slot[z] (alpha 1, beta 0, N form, no windows)
+    int ksplit = 0, kslice = 0;
 };
 template <typename T>
 void launch_gemm_simt(cudaStream_t s, int njobs, const GemmArgs<T>& g);

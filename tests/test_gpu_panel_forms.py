@@ -1,6 +1,7 @@
 """Alternative kernel forms against the default ones, through the C ABI: the
-Gauss-Jordan panel forms against the one-CTA lane-quad form, and the bulk-copy
-sweep products against the register-load kernel.
+Gauss-Jordan panel forms against the one-CTA lane-quad form, the bulk-copy
+sweep products against the register-load kernel, and split-K Schur products
+against unsplit ones.
 
 * cluster form: one matrix's panel split over 2, 4 or 8 CTAs of a thread-block
   cluster (FDFD_GJ_CL, read when the handle is created; -1 picks the size per
@@ -78,3 +79,24 @@ def test_bulk_copy_sweep_matches_register_form(lib, fdfd, monkeypatch, prec, siz
     assert got[3].iterations == ref[3].iterations and got[3].rel_residual <= TOL_RES
     for a, b in zip(got[:3], ref[:3]):
         assert np.array_equal(a, b), rel(a, b)
+
+
+def test_splitk_schur_products_match(lib, fdfd, oracle, monkeypatch):
+    """Split-K Schur products (the default for products whose tiles fill less than half of the
+    SMs: partial products over K slices, then their sum in a fixed order) give the fields of
+    the unsplit products to within the mixed form's rounding, and the oracle's; the result is
+    the same on a second run (deterministic)."""
+    from fdfd_gb300 import workloads as W
+    p = W.design_guide(600, 300, design=(64, 64), seed=13, npml=12)   # b = 300: the deep levels split
+    P = fdfd.FDFD_PREC_MIXED
+    monkeypatch.setenv("FDFD_SPLITK", "0")
+    ref = run(fdfd, monkeypatch, p, P, [])
+    monkeypatch.setenv("FDFD_SPLITK", "1")
+    got = run(fdfd, monkeypatch, p, P, [])
+    got2 = run(fdfd, monkeypatch, p, P, [])
+    assert got[3].rel_residual <= TOL_RES and abs(got[3].iterations - ref[3].iterations) <= 1
+    for a, b, c in zip(got[:3], ref[:3], got2[:3]):
+        assert rel(a, b) <= 1e-9 and np.array_equal(a, c)
+    g = oracle.Grid((p.Nx, p.Ny), p.npml, ((0.0, 0.0), (p.Nx * p.dx, p.Ny * p.dy)))
+    o = oracle.solve(g, p.eps, p.src, p.omega, oracle.TM, p.pml_m, p.pml_lnR)
+    assert max(rel(got[0], o[0]), rel(got[1], o[1]), rel(got[2], o[2])) <= 1e-8
