@@ -221,9 +221,10 @@ struct fdfd_handle {
                                    // (FDFD_GJ_PRESPLIT=0: two planes, split inside the GEMM)
     int gj_form = 0;               // one-CTA Gauss-Jordan panel: 0 lane-quad form, 1 pipelined row form
                                    // (FDFD_GJ_FORM)
-    int gj_cl = 1;                 // CTAs per matrix of the Gauss-Jordan panel (1: one CTA per matrix, the
-                                   // default; 2/4/8: always that cluster; -1: by the level's matrix count;
-                                   // FDFD_GJ_CL)
+    int gj_cl = -2;                // CTAs per matrix of the Gauss-Jordan panel (-2, the default: clusters of 8
+                                   // for the deep levels, where eight CTAs per matrix fit in half of the SMs,
+                                   // else one; 1: always one; 2/4/8: always that cluster; -1: the largest
+                                   // cluster the level's matrix count fits; FDFD_GJ_CL)
     int gj_fused_k = 0;            // FP32 tensor-core Gauss-Jordan: columns of the panels that share one
                                    // update (0: one update per panel, the default; FDFD_GJ_FUSED_K)
     int gj_fused_min = 1;          // ... for batches of at least this many matrices
@@ -1027,6 +1028,8 @@ static uint64_t wait_limit(const fdfd_handle* h) { return h->wait_ns ? h->wait_n
 // panel over a cluster of CTAs, as many as keep every cluster resident at once
 static int gj_cluster(const fdfd_handle* h, int njobs) {
     if (h->gj_cl == 1 || h->gj_cl == 2 || h->gj_cl == 4 || h->gj_cl == 8) return h->gj_cl > 1 ? h->gj_cl : 0;
+    if (h->gj_cl == -2)   // deep levels only: eight CTAs per matrix within half of the SMs
+        return (long long)njobs * 8 * 2 <= h->num_sms ? 8 : 0;
     for (int cl : {8, 4, 2})
         if ((long long)njobs * cl <= h->num_sms) return cl;
     return 0;

@@ -5,7 +5,7 @@ against unsplit ones.
 
 * cluster form: one matrix's panel split over 2, 4 or 8 CTAs of a thread-block
   cluster (FDFD_GJ_CL, read when the handle is created; -1 picks the size per
-  level from its matrix count);
+  level from its matrix count, -2 (the default) clusters of 8 for the deep levels);
 * row form: one row per thread, software-pipelined column steps (FDFD_GJ_FORM=1).
 
 Each form takes the same pivots and performs the same arithmetic per element, so
@@ -20,7 +20,8 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 TOL_RES = 1e-10
-FORMS = [("FDFD_GJ_CL", "2"), ("FDFD_GJ_CL", "4"), ("FDFD_GJ_CL", "8"), ("FDFD_GJ_CL", "-1"), ("FDFD_GJ_FORM", "1")]
+FORMS = [("FDFD_GJ_CL", "2"), ("FDFD_GJ_CL", "4"), ("FDFD_GJ_CL", "8"), ("FDFD_GJ_CL", "-1"), ("FDFD_GJ_CL", "-2"),
+         ("FDFD_GJ_FORM", "1")]
 
 
 def rel(a, b):
