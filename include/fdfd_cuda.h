@@ -154,7 +154,10 @@ int  fdfd_checkpoint_info(const fdfd_handle* h, int* active, long long* host_byt
                           long long* copied_bytes);
 
 /* Relative permittivity ϵᵣ (Device.ϵᵣ, src/device.jl:19-25), Nx*Ny complex.
- * Rejects NaN/Inf.  Invalidates any existing factorization. */
+ * Rejects NaN/Inf and complex zeros (FDFD_EINVAL, with the first such index in
+ * fdfd_last_error); the check runs on the device after the copy, and a
+ * rejected ϵᵣ leaves the handle's permittivity and factorization unchanged.
+ * Otherwise invalidates any existing factorization. */
 int  fdfd_set_eps(fdfd_handle* h, const double* eps_r);
 
 /* Assemble the driven operator of solve() at angular frequency omega (SI
@@ -164,6 +167,8 @@ int  fdfd_factor(fdfd_handle* h, double omega);
 
 /* Driven solve with the current factorization for nrhs current sources
  * (Device.src, b = iω·src, driven.jl:36,46), each Nx*Ny complex, stacked.
+ * A source with a NaN/Inf entry is rejected (FDFD_EINVAL) before any solve work
+ * (checked on the device after the copy).
  * Outputs (each nrhs*Nx*Ny complex, any may be NULL):
  *   TM: f1 = Ez, f2 = Hx, f3 = Hy  (driven.jl:38-42)
  *   TE: f1 = Hz, f2 = Ex, f3 = Ey  (driven.jl:48-53)
