@@ -213,6 +213,16 @@ struct fdfd_handle {
     bool use_tc = true;
     bool level1_gj = false;     // invert first-step blocks by Gauss-Jordan instead of the O(b²) kernel
     bool tri_sweep = true;      // first-step sweep products through the tridiagonal factors, not the dense inverses
+    // fdfd_factor through a captured CUDA graph: a second consecutive factorization at the same ω
+    // captures the assembly and factorization; later ones at that ω replay it (ϵᵣ and the new
+    // assembly arguments are read from device memory).  cfg_gen counts the changes a captured
+    // graph depends on (storage, launch shapes, wait limit, checkpoint mode, budget).
+    bool graph_factor = true;      // FDFD_FACTOR_GRAPH=0: plain launches only
+    cudaGraph_t fgraph = nullptr;
+    cudaGraphExec_t fgexec = nullptr;
+    double fg_omega = 0, fg_scale = 0, last_plain_omega = -1;
+    long long fg_kernels = 0;
+    unsigned fg_gen = 0, cfg_gen = 1;
     bool splitk = true;            // split-K for tensor-core products whose tiles fill less than half the
                                    // SMs (FDFD_SPLITK=0: off)
     bool gemv_bulk = false;        // untuned N-form sweep products through the bulk-copy pipeline where it
@@ -650,6 +660,7 @@ template <typename T> int alloc_pool(fdfd_handle* h, Pool<T>& P, int rows, int c
 }
 
 template <typename T> void free_store(fdfd_handle* h, FactorStore<T>& F) {
+    h->cfg_gen++;   // a captured factorization addresses this storage
     void* bufs[] = {F.D.base, F.C.base, F.X.base, F.GP.base, F.RP.base, F.Tg.base, F.rv, F.xv, F.wv,
                     F.perm, F.rowsrc, F.inv, F.gsub, F.gj_slots, F.trifac, F.tripiv, F.sttab, F.Wk.base,
                     F.wk_iota};
@@ -717,6 +728,7 @@ template <typename T> void factor_bytes(const fdfd_handle* h, double* resident, 
 
 // remaps the coupling and X slot tables onto the device windows and rebuilds the job lists
 int ckpt_engage(fdfd_handle* h) {
+    h->cfg_gen++;
     const int E = (int)h->steps.size();
     int nA = 0, nB = 0, nXw = 0;
     for (int e = 1; e <= E; ++e) {
@@ -1922,6 +1934,7 @@ int fdfd_create(fdfd_handle** out, int Nx, int Ny, int Npx, int Npy, double dx, 
     if (const char* e = getenv("FDFD_GJ_PRESPLIT")) h->gj_presplit = atoi(e) != 0;
     if (const char* e = getenv("FDFD_GEMV_BULK")) h->gemv_bulk = atoi(e) != 0;
     if (const char* e = getenv("FDFD_SPLITK")) h->splitk = atoi(e) != 0;
+    if (const char* e = getenv("FDFD_FACTOR_GRAPH")) h->graph_factor = atoi(e) != 0;
     if (const char* e = getenv("FDFD_GJ_FUSED_MIN")) h->gj_fused_min = std::max(1, atoi(e));
     NodeMap& m = h->map;
     m.Nx = Nx; m.Ny = Ny;
@@ -1971,6 +1984,8 @@ int fdfd_create(fdfd_handle** out, int Nx, int Ny, int Npx, int Npy, double dx, 
 void fdfd_destroy(fdfd_handle* h) {
     if (!h) return;
     if (h->stream) cudaStreamSynchronize(h->stream);
+    if (h->fgexec) cudaGraphExecDestroy(h->fgexec);
+    if (h->fgraph) cudaGraphDestroy(h->fgraph);
     if (h->mf) {
         for (fdfd_handle* s : h->mf->sub) fdfd_destroy(s);
         dev_free(h, h->mf->deps);
@@ -2020,6 +2035,7 @@ int fdfd_set_wait_limit(fdfd_handle* h, long long ns) {
     if (h->mf)
         for (fdfd_handle* s : h->mf->sub) s->wait_ns = ns > 0 ? (unsigned long long)ns : 0ull;
     h->wait_ns = ns > 0 ? (unsigned long long)ns : 0ull;
+    h->cfg_gen++;
     return FDFD_OK;
 }
 
@@ -2034,6 +2050,7 @@ int fdfd_set_checkpoint(fdfd_handle* h, int mode) {
     if (!h->ckpt && mode == 1 && (h->f32.complete || h->f64.complete))
         return set_err(h, FDFD_EINVAL, "fdfd_set_checkpoint(1) must come before the first factorization");
     h->ckpt_mode = mode;
+    h->cfg_gen++;
     return FDFD_OK;
 }
 
@@ -2050,6 +2067,7 @@ int fdfd_set_device_budget(fdfd_handle* h, long long bytes) {
     if (h->mf)
         for (fdfd_handle* s : h->mf->sub) s->dev_budget = bytes;
     h->dev_budget = bytes;
+    h->cfg_gen++;
     return FDFD_OK;
 }
 
@@ -2077,11 +2095,14 @@ int fdfd_set_eps(fdfd_handle* h, const double* eps_r) {
     return FDFD_OK;
 }
 
-int fdfd_factor(fdfd_handle* h, double omega) {
-    if (!h) return FDFD_EINVAL;
-    if (h->mf) return set_err(h, FDFD_EINVAL, "modulated device: use fdfd_mf_factor");
-    if (!h->eps_set) return set_err(h, FDFD_EINVAL, "fdfd_set_eps must be called before fdfd_factor");
-    if (!(omega > 0) || !std::isfinite(omega)) return set_err(h, FDFD_EINVAL, "omega must be positive and finite");
+}  // extern "C"
+
+namespace {
+
+int factor_work(fdfd_handle* h);
+
+// the ordinary driven factorization: assembly (with its scale), then the factorization
+int factor_plain(fdfd_handle* h, double omega) {
     h->launches = 0;
     h->factored = false;
     cudaEventRecord(h->ev[0], h->stream);
@@ -2090,6 +2111,80 @@ int fdfd_factor(fdfd_handle* h, double omega) {
     RET(factor_op(h));
     cudaEventRecord(h->ev[2], h->stream);
     h->omega = omega;
+    return FDFD_OK;
+}
+
+// capture of the work factor_plain just did (assembly kernels reading their arguments from
+// device memory, then the factorization) as this handle's graph; nothing runs
+int factor_capture(fdfd_handle* h, double omega) {
+    if (h->fgexec) { cudaGraphExecDestroy(h->fgexec); h->fgexec = nullptr; }
+    if (h->fgraph) { cudaGraphDestroy(h->fgraph); h->fgraph = nullptr; }
+    const long long l0 = h->launches;
+    if (cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        cudaGetLastError();
+        return FDFD_OK;   // no graph: the plain path stays in use
+    }
+    int rc = factor_work(h);
+    cudaGraph_t g = nullptr;
+    const cudaError_t ee = cudaStreamEndCapture(h->stream, &g);
+    const long long kernels = h->launches - l0;
+    h->launches = l0;
+    if (rc == FDFD_OK && ee == cudaSuccess && g && cudaGraphInstantiate(&h->fgexec, g, 0) == cudaSuccess) {
+        h->fgraph = g;
+        h->fg_omega = omega;
+        h->fg_scale = h->scale;
+        h->fg_kernels = kernels;
+        h->fg_gen = h->cfg_gen;
+        return FDFD_OK;
+    }
+    cudaGetLastError();
+    if (g) cudaGraphDestroy(g);
+    h->fgexec = nullptr;
+    h->err.clear();
+    return FDFD_OK;   // capture is an optimisation: its failure leaves the plain path
+}
+
+// replay: the assembly arguments for ω (device memory, on the handle's stream), then the graph
+int factor_replay(fdfd_handle* h, double omega) {
+    const int op = h->pol == FDFD_TM ? OP_TM_DRIVEN : OP_TE_DRIVEN;
+    h->launches = 0;
+    h->factored = false;
+    cudaEventRecord(h->ev[0], h->stream);
+    RET(assemble_args(h, op, omega, zd(0, 0), omega, h->stream));
+    cudaEventRecord(h->ev[1], h->stream);
+    if (cudaGraphLaunch(h->fgexec, h->stream) != cudaSuccess) {
+        cudaGetLastError();
+        return set_err(h, FDFD_ECUDA, "cudaGraphLaunch of the factorization failed");
+    }
+    cudaEventRecord(h->ev[2], h->stream);
+    h->launches = h->fg_kernels;
+    h->scale = h->fg_scale;   // the scale the captured work was built with
+    h->op = op;
+    RET(check_device(h, "factor"));
+    h->fact_prec = h->precision;
+    h->fell_back = false;
+    h->factored = true;
+    h->omega = omega;
+    return FDFD_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fdfd_factor(fdfd_handle* h, double omega) {
+    if (!h) return FDFD_EINVAL;
+    if (h->mf) return set_err(h, FDFD_EINVAL, "modulated device: use fdfd_mf_factor");
+    if (!h->eps_set) return set_err(h, FDFD_EINVAL, "fdfd_set_eps must be called before fdfd_factor");
+    if (!(omega > 0) || !std::isfinite(omega)) return set_err(h, FDFD_EINVAL, "omega must be positive and finite");
+    // (not while profiling, whose per-launch events need plain launches, nor in checkpoint
+    // mode, whose host copies are left to the plain path)
+    const bool graphable = h->graph_factor && !h->prof_on && !h->ckpt && h->ckpt_mode != 1;
+    if (graphable && h->fgexec && h->fg_gen == h->cfg_gen && h->fg_omega == omega) return factor_replay(h, omega);
+    RET(factor_plain(h, omega));
+    // a second consecutive factorization at this ω: capture it for the next ones
+    if (graphable && h->fact_prec == h->precision && h->last_plain_omega == omega) RET(factor_capture(h, omega));
+    h->last_plain_omega = omega;
     return FDFD_OK;
 }
 
@@ -2363,7 +2458,7 @@ int fdfd_batch_factor(fdfd_batch* B, const double* omegas, int* status) {
     if (!B->exec) {
         // the ordinary factorizations: storage, scaling, and this call's results
         for (int i = 0; i < n; ++i) {
-            const int rc = fdfd_factor(B->hs[i], omegas[i]);
+            const int rc = B->hs[i]->eps_set ? factor_plain(B->hs[i], omegas[i]) : FDFD_EINVAL;
             if (status) status[i] = rc;
             if (rc != FDFD_OK && first == FDFD_OK) {
                 first = rc;
@@ -3124,6 +3219,7 @@ extern "C" {
 int fdfd_autotune(fdfd_handle* h) {
     if (!h) return FDFD_EINVAL;
     if (h->mf) return set_err(h, FDFD_EINVAL, "fdfd_autotune: tune the sideband handles of a modulated device");
+    h->cfg_gen++;   // new launch shapes
     return h->precision == FDFD_PREC_FP64 ? autotune_impl<double>(h) : autotune_impl<float>(h);
 }
 

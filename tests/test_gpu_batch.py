@@ -124,3 +124,38 @@ def test_mirror_solve_batches_frequencies(lib, fdfd):
         for c in ("Ez", "Hx", "Hy"):
             assert rel(a[c], b[c]) <= 1e-8
     assert max(s["rel_residual"] for s in st) <= TOL_RES
+
+
+def test_factor_graph_replay_matches_plain_factorization(lib, fdfd, monkeypatch):
+    """fdfd_factor captures its own work on the second consecutive factorization at one ω and
+    replays it afterwards (ϵᵣ read from device memory): the fields equal those of plain launches
+    bit for bit, also after a new permittivity, and a new ω falls back to plain launches.  New
+    launch shapes (autotune) drop the graph; the tuner's timing-based choices can differ between
+    the two runs, so that last step is compared to rounding."""
+    from fdfd_gb300 import workloads as W
+    p = W.design_guide(160, 96, design=(40, 40), seed=9, npml=12)
+    e2 = p.eps.copy()
+    e2[60:80, 40:60] = 3.0
+
+    def runs(graph):
+        monkeypatch.setenv("FDFD_FACTOR_GRAPH", "1" if graph else "0")
+        h = make(fdfd, p, 1, fdfd.FDFD_PREC_MIXED)
+        out = []
+        for eps, om in ((p.eps, p.omega), (p.eps, p.omega), (p.eps, p.omega), (e2, p.omega),
+                        (e2, p.omega * 1.02), (e2, p.omega)):
+            h.set_eps(eps)
+            h.factor(om)
+            out.append(h.solve(p.src)[:3])
+        h.autotune()
+        h.factor(p.omega)
+        out.append(h.solve(p.src)[:3])
+        h.close()
+        return out
+
+    plain, graph = runs(False), runs(True)
+    for k, (a, b) in enumerate(zip(plain, graph)):
+        for x, y in zip(a, b):
+            if k < 6:
+                assert np.array_equal(x, y), (k, rel(x, y))
+            else:   # after autotune: the two runs' timing-based choices may differ (split-K, tiles)
+                assert rel(x, y) <= 1e-9, (k, rel(x, y))
