@@ -223,6 +223,14 @@ struct fdfd_handle {
     double fg_omega = 0, fg_scale = 0, last_plain_omega = -1;
     long long fg_kernels = 0;
     unsigned fg_gen = 0, cfg_gen = 1;
+    // the preconditioner's sweep (node vectors rv -> xv) as a graph per factor precision, keyed by
+    // the right-hand-side count, the vector buffer and cfg_gen; replayed by every FGMRES iteration
+    cudaGraph_t sg_graph[2] = {nullptr, nullptr};
+    cudaGraphExec_t sg_exec[2] = {nullptr, nullptr};
+    int sg_nrhs[2] = {0, 0};
+    const void* sg_rv[2] = {nullptr, nullptr};
+    unsigned sg_gen[2] = {0, 0};
+    long long sg_kernels[2] = {0, 0};
     bool splitk = true;            // split-K for tensor-core products whose tiles fill less than half the
                                    // SMs (FDFD_SPLITK=0: off)
     bool gemv_bulk = false;        // untuned N-form sweep products through the bulk-copy pipeline where it
@@ -1414,6 +1422,48 @@ template <typename T> int sweep_impl(fdfd_handle* h, int nrhs) {
     return check_launch(h, "sweep");
 }
 
+// the sweep through this handle's graph for (T, nrhs, vector buffer, cfg_gen): captured on the first
+// use of that key (without running), then launched; plain launches while profiling, in checkpoint
+// mode (host copies), with graphs off, or when the capture fails
+template <typename T> int sweep_graph(fdfd_handle* h, int nrhs) {
+    const int ti = sizeof(T) == 4 ? 0 : 1;
+    FactorStore<T>& F = store<T>(h);
+    if (!h->graph_factor || h->prof_on || h->ckpt || h->ckpt_mode == 1) return sweep_impl<T>(h, nrhs);
+    if (!(h->sg_exec[ti] && h->sg_nrhs[ti] == nrhs && h->sg_rv[ti] == (const void*)F.rv &&
+          h->sg_gen[ti] == h->cfg_gen)) {
+        if (h->sg_exec[ti]) { cudaGraphExecDestroy(h->sg_exec[ti]); h->sg_exec[ti] = nullptr; }
+        if (h->sg_graph[ti]) { cudaGraphDestroy(h->sg_graph[ti]); h->sg_graph[ti] = nullptr; }
+        if (cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+            cudaGetLastError();
+            return sweep_impl<T>(h, nrhs);
+        }
+        const long long l0 = h->launches;
+        const int rc = sweep_impl<T>(h, nrhs);
+        cudaGraph_t g = nullptr;
+        const cudaError_t ee = cudaStreamEndCapture(h->stream, &g);
+        const long long kernels = h->launches - l0;
+        h->launches = l0;
+        if (rc != FDFD_OK || ee != cudaSuccess || !g || cudaGraphInstantiate(&h->sg_exec[ti], g, 0) != cudaSuccess) {
+            cudaGetLastError();
+            if (g) cudaGraphDestroy(g);
+            h->sg_exec[ti] = nullptr;
+            h->err.clear();
+            return sweep_impl<T>(h, nrhs);
+        }
+        h->sg_graph[ti] = g;
+        h->sg_nrhs[ti] = nrhs;
+        h->sg_rv[ti] = (const void*)F.rv;
+        h->sg_gen[ti] = h->cfg_gen;
+        h->sg_kernels[ti] = kernels;
+    }
+    if (cudaGraphLaunch(h->sg_exec[ti], h->stream) != cudaSuccess) {
+        cudaGetLastError();
+        return set_err(h, FDFD_ECUDA, "cudaGraphLaunch of the sweep failed");
+    }
+    h->launches += h->sg_kernels[ti];
+    return FDFD_OK;
+}
+
 // preconditioner: out = (scale·A)⁻¹ (scale·in) = A⁻¹ in  (FP64 natural layout, nrhs vectors)
 template <typename T> int precond_impl(fdfd_handle* h, const cplx<double>* in, cplx<double>* out, int nrhs) {
     RET(alloc_vectors<T>(h, nrhs));
@@ -1422,7 +1472,7 @@ template <typename T> int precond_impl(fdfd_handle* h, const cplx<double>* in, c
     dim3 grid(ceil_div(N, 256), nrhs);
     launch_to_nodes<T>(grid, h->stream, h->map, nrhs, in, h->scale, F.rv);
     h->launches++;
-    RET(sweep_impl<T>(h, nrhs));
+    RET(sweep_graph<T>(h, nrhs));
     launch_from_nodes<T>(grid, h->stream, h->map, nrhs, (const T*)F.xv, 1.0, 0, out);
     h->launches++;
     return check_launch(h, "precond");
@@ -1986,6 +2036,10 @@ void fdfd_destroy(fdfd_handle* h) {
     if (h->stream) cudaStreamSynchronize(h->stream);
     if (h->fgexec) cudaGraphExecDestroy(h->fgexec);
     if (h->fgraph) cudaGraphDestroy(h->fgraph);
+    for (int i = 0; i < 2; ++i) {
+        if (h->sg_exec[i]) cudaGraphExecDestroy(h->sg_exec[i]);
+        if (h->sg_graph[i]) cudaGraphDestroy(h->sg_graph[i]);
+    }
     if (h->mf) {
         for (fdfd_handle* s : h->mf->sub) fdfd_destroy(s);
         dev_free(h, h->mf->deps);
