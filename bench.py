@@ -742,7 +742,9 @@ def main():
     hbm_units = {"sweep": "dense factor blocks each product references (re, im planes) and the first step's "
                           "tridiagonal factors (8b complex + b pivots per node), read once per sweep, + node vectors",
                  "gj_update": "each matrix read and written once per Gauss-Jordan panel (re, im planes)",
-                 "level1": "first-step inverses written; two inverses read, three blocks written per survivor"}
+                 "level1": "first-step inverses written; two inverses read, three blocks written per survivor",
+                 "residual": "matrix-free 5-point stencil residual r = b - A x: 80 B of stencil planes + x, b, r "
+                             "(16 B each) per unknown; FP64-issue bound before HBM"}
     roof_hbm = {}
     for k, unit in hbm_units.items():
         c = prof[k]
