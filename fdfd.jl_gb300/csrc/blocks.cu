@@ -619,10 +619,10 @@ __global__ void __launch_bounds__(512, 1) gj_panel_kernel(Pool<T> M, const int* 
 // update, which the look-ahead runs concurrently with this panel's column steps.
 // One CTA per 128 columns and matrix; the tile is staged through shared memory so
 // reads and writes coalesce.  grid: (ceil(b/128), njobs), block 512
-template <typename T, int NB>
+template <typename T, int NB, int TW = 128>
 __global__ void __launch_bounds__(512) gj_rt_kernel(Pool<T> M, const int* slots, Pool<T> RP, const int* rowsrc,
                                                     int c0, int rcw) {
-    constexpr int NT = 512, TW = 128;
+    constexpr int NT = 512;
     constexpr int IT = NB * TW / NT;               // loads per thread
     static_assert((NB * TW) % NT == 0, "tile split");
     __shared__ T buf[2 * NB * (TW + 1)];
@@ -2033,6 +2033,16 @@ int launch_gj_rt(cudaStream_t s, int nb, int njobs, Pool<T> M, const int* slots,
                  int c0, int rcw) {
     const dim3 grid(ceil_div(M.rows, 128), njobs);
     if (rcw <= 0 || rcw > RP.cols) rcw = RP.cols;
+    // a few matrices: 32-column tiles, four times the CTAs for the latency-bound gather
+    static const int nsm = [] {
+        int d = 0, n = 0;
+        cudaGetDevice(&d);
+        return cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, d) == cudaSuccess && n > 0 ? n : 1;
+    }();
+    if (nb == 32 && (long long)ceil_div(M.rows, 32) * njobs <= 2LL * nsm) {
+        gj_rt_kernel<T, 32, 32><<<dim3(ceil_div(M.rows, 32), njobs), 512, 0, s>>>(M, slots, RP, rowsrc, c0, rcw);
+        return (int)cudaGetLastError();
+    }
     if (nb == 32) gj_rt_kernel<T, 32><<<grid, 512, 0, s>>>(M, slots, RP, rowsrc, c0, rcw);
     else if (nb == 16) gj_rt_kernel<T, 16><<<grid, 512, 0, s>>>(M, slots, RP, rowsrc, c0, rcw);
     else if (nb == 8) gj_rt_kernel<T, 8><<<grid, 512, 0, s>>>(M, slots, RP, rowsrc, c0, rcw);
