@@ -1381,7 +1381,7 @@ template <typename T> int sweep_impl(fdfd_handle* h, int nrhs) {
         }
         if (e == 1) {
             if (S.nf2) {
-                launch_diag_sweep<T>(h->stream, S.nf2, h->map, h->st, h->scale, nrhs, J<int4>(h, S.dswf), 0,
+                launch_diag_sweep<T>(h->stream, S.nf2, h->map, F.sttab, nrhs, J<int4>(h, S.dswf), 0,
                                      (const T*)F.xv, F.rv);
                 h->launches++;
             }
@@ -1404,7 +1404,7 @@ template <typename T> int sweep_impl(fdfd_handle* h, int nrhs) {
     for (int e = E; e >= 1; --e) {
         const StepJobs& S = h->sj[e];
         if (e == 1) {
-            launch_diag_sweep<T>(h->stream, S.ne, h->map, h->st, h->scale, nrhs, J<int4>(h, S.dswb), 1,
+            launch_diag_sweep<T>(h->stream, S.ne, h->map, F.sttab, nrhs, J<int4>(h, S.dswb), 1,
                                  (const T*)F.xv, F.wv);
             h->launches++;
             if (tri1) {

@@ -250,6 +250,7 @@ int launch_tri_apply(cudaStream_t s, int b, int ld, int njobs, int nrhs, const i
 // r[s] -= u_s ⊙ z[next] + l_s ⊙ z[prev]  (first reduction step, diagonal couplings)
 // mode 0: survivors update r from eliminated neighbours (jobs: L1Job-like int4 (s, prev, next, flags))
 // mode 1: eliminated k: w[k] = l_k ⊙ x[prev] + u_k ⊙ x[next]
+// (l, u: the scaled coupling planes of the factorization's stencil table)
 template <typename T>
-void launch_diag_sweep(cudaStream_t s, int njobs, NodeMap m, const cplx<double>* st, double scale, int nrhs,
-                       const int4* jobs, int mode, const T* src, T* dst);
+void launch_diag_sweep(cudaStream_t s, int njobs, NodeMap m, const cplx<T>* tab, int nrhs, const int4* jobs,
+                       int mode, const T* src, T* dst);

@@ -401,16 +401,14 @@ __global__ void __launch_bounds__(256) gemv_t_kernel(GemvArgs<T> g) {
 // mode 1: dst[node]  = l_node ⊙ src[prev] + u_node ⊙ src[next]   (backward, eliminated)
 // grid: (ceil(b/256), njobs), block 256
 template <typename T>
-__global__ void diag_sweep_kernel(NodeMap m, const cplx<double>* st, double scale, int nrhs, const int4* jobs,
-                                  int mode, const T* src, T* dst) {
+__global__ void diag_sweep_kernel(NodeMap m, const cplx<T>* tab, int nrhs, const int4* jobs, int mode, const T* src,
+                                  T* dst) {
     const int4 J = jobs[blockIdx.y];
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m.b) return;
-    long long N = (long long)m.Nx * m.Ny;
-    long long k = m.nat(J.x, i);
-    const cplx<double> ld_ = cscale(st[m.p_cprev() * N + k], scale);
-    const cplx<double> ud_ = cscale(st[m.p_cnext() * N + k], scale);
-    const cplx<T> l = cmk((T)ld_.re, (T)ld_.im), u = cmk((T)ud_.re, (T)ud_.im);
+    // the node's scaled couplings from the factorization's stencil table (contiguous in i)
+    const cplx<T> l = tab[((size_t)J.x * 5 + m.p_cprev()) * m.b + i];
+    const cplx<T> u = tab[((size_t)J.x * 5 + m.p_cnext()) * m.b + i];
     const int ld = m.ld;
     for (int r = 0; r < nrhs; ++r) {
         cplx<T> acc = cmk((T)0, (T)0);
@@ -695,9 +693,9 @@ int gemv_max_rhs(int b) {
 }
 
 template <typename T>
-void launch_diag_sweep(cudaStream_t s, int njobs, NodeMap m, const cplx<double>* st, double scale, int nrhs,
-                       const int4* jobs, int mode, const T* src, T* dst) {
-    diag_sweep_kernel<T><<<dim3(ceil_div(m.b, 256), njobs), 256, 0, s>>>(m, st, scale, nrhs, jobs, mode, src, dst);
+void launch_diag_sweep(cudaStream_t s, int njobs, NodeMap m, const cplx<T>* tab, int nrhs, const int4* jobs,
+                       int mode, const T* src, T* dst) {
+    diag_sweep_kernel<T><<<dim3(ceil_div(m.b, 256), njobs), 256, 0, s>>>(m, tab, nrhs, jobs, mode, src, dst);
 }
 template <typename T>
 int launch_tri_apply(cudaStream_t s, int b, int ld, int njobs, int nrhs, const int* jobs, const cplx<T>* fac,
@@ -719,7 +717,7 @@ template int launch_gemv<float>(cudaStream_t, int, int, const GemvArgs<float>&);
 template int launch_gemv<double>(cudaStream_t, int, int, const GemvArgs<double>&);
 template int gemv_max_rhs<float>(int);
 template int gemv_max_rhs<double>(int);
-template void launch_diag_sweep<float>(cudaStream_t, int, NodeMap, const cplx<double>*, double, int, const int4*,
+template void launch_diag_sweep<float>(cudaStream_t, int, NodeMap, const cplx<float>*, int, const int4*,
                                        int, const float*, float*);
-template void launch_diag_sweep<double>(cudaStream_t, int, NodeMap, const cplx<double>*, double, int, const int4*,
+template void launch_diag_sweep<double>(cudaStream_t, int, NodeMap, const cplx<double>*, int, const int4*,
                                         int, const double*, double*);
