@@ -286,19 +286,6 @@ long long first_nonfinite(const double* x, long long n) {
     return -1;
 }
 
-// index of the first complex zero among the n interleaved values z, or -1
-long long first_zero(const double* z, long long n) {
-    for (long long c = 0; c < n; c += 4096) {
-        const long long e = std::min(n, c + 4096);
-        int any = 0;
-        for (long long k = c; k < e; ++k) any |= (z[2 * k] == 0.0) & (z[2 * k + 1] == 0.0);
-        if (any)
-            for (long long k = c; k < e; ++k)
-                if (z[2 * k] == 0.0 && z[2 * k + 1] == 0.0) return k;
-    }
-    return -1;
-}
-
 int set_err(fdfd_handle* h, int code, const char* fmt, ...) {
     char buf[512];
     va_list ap;
@@ -998,7 +985,8 @@ int gemm(fdfd_handle* h, int pa, int pb, int pc, const int* a_slot, const int* b
                      ? splitk_of(h, M, N, K, njobs, bne == TC_BN128_TWO ? 128 : bne)
                      : 1;
         int rc = 0;
-        if (ks > 1) {
+        if constexpr (sizeof(T) != 4) ks = 1;   // (the tensor-core path is FP32 only)
+        else if (ks > 1) {
             GemmArgs<T> pg = g;
             pg.kslice = ceil_div(K, ks * 8) * 8;
             ks = ceil_div(K, pg.kslice);
@@ -1013,9 +1001,8 @@ int gemm(fdfd_handle* h, int pa, int pb, int pc, const int* a_slot, const int* b
                 rc = tc_gemm_launch(reinterpret_cast<GemmArgs<float>*>(&pg), nullptr, pa, pb, njobs, &F.tc,
                                     h->num_sms, stream, bn);
                 if (rc == 0)
-                    rc = tc_splitk_sum(*reinterpret_cast<const Pool<float>*>(&F.Wk), ks,
-                                       *reinterpret_cast<const Pool<float>*>(&g.C), c_slot, c_trans_arr, c_trans,
-                                       njobs, M, N, (float)alpha, beta, stream);
+                    rc = tc_splitk_sum(F.Wk, ks, g.C, c_slot, c_trans_arr, c_trans, njobs, M, N, (float)alpha, beta,
+                                       stream);
                 h->launches++;
             }
         }
